@@ -1,0 +1,442 @@
+/*
+ * nesf.h -- C ABI of the GB300-native interface-flux library (libnesf.so).
+ *
+ * The library is a drop-in for the interface-flux step of NumericalEarth.jl's
+ * EarthSystemModel: the similarity-theory (Monin-Obukhov) fixed-point solve at
+ * the atmosphere-ocean and atmosphere-sea-ice interfaces, the sea-ice-ocean
+ * fluxes, the PrescribedAtmosphere space/time interpolation onto the exchange
+ * grid, and the assembly of net ocean and sea-ice boundary fluxes.
+ *
+ * Conventions (mirroring Oceananigans `parent(field)` arrays):
+ *   - every 2-D array is column-major with i fastest; element (i, j), with
+ *     Oceananigans' 1-based interior index i in [1-hx, nx+hx], j in [1-hy, ny+hy],
+ *     lives at  ptr[(i - 1 + hx) + (j - 1 + hy) * stride_j];
+ *   - 3-D ocean fields are passed as the pointer of their k = Nz slice, which
+ *     has the same 2-D layout (all fields of one grid share halo sizes);
+ *   - array pointers are DEVICE pointers (CuArrays / torch CUDA tensors) unless
+ *     an entry point says otherwise; the library never frees caller memory;
+ *   - all work is enqueued on the caller's stream (`stream`, a cudaStream_t,
+ *     NULL = legacy default stream) and returns without synchronising, except
+ *     where a `nesf_stats*` is passed (the stats are read back at the end);
+ *   - every entry point returns an nesf_status; nesf_last_error() describes
+ *     the most recent failure on the calling thread.
+ *
+ * Reference interfaces replaced (paths inside NumericalEarth.jl v0.6.2):
+ *   src/EarthSystemModels/InterfaceComputations/atmosphere_ocean_fluxes.jl:17
+ *   src/EarthSystemModels/InterfaceComputations/atmosphere_sea_ice_fluxes.jl:18
+ *   src/EarthSystemModels/InterfaceComputations/sea_ice_ocean_fluxes.jl:20
+ *   src/Atmospheres/interpolate_atmospheric_state.jl:9
+ *   src/Atmospheres/prescribed_atmosphere_regridder.jl:41
+ *   src/Radiations/interpolate_radiation_state.jl:4
+ *   src/Oceans/assemble_net_ocean_fluxes.jl:16
+ *   src/SeaIces/assemble_net_sea_ice_fluxes.jl:11
+ *   src/Radiations/apply_air_sea_radiative_fluxes.jl:18
+ *   src/Radiations/apply_air_sea_ice_radiative_fluxes.jl:15
+ *   src/EarthSystemModels/time_step_earth_system_model.jl:38 (update_state!)
+ */
+#ifndef NESF_H
+#define NESF_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NESF_ABI_VERSION 1
+
+/* ------------------------------------------------------------------ status */
+typedef enum {
+    NESF_OK = 0,
+    NESF_ERR_ARG = 1,          /* bad argument (null pointer, size, kind)        */
+    NESF_ERR_NONFINITE = 2,    /* non-finite input detected by the input scan    */
+    NESF_ERR_TIMEOUT = 3,      /* a bounded device-side wait gave up             */
+    NESF_ERR_CUDA = 4,         /* CUDA runtime error                             */
+    NESF_ERR_UNSUPPORTED = 5,  /* option combination not implemented             */
+    NESF_ERR_CAPACITY = 6      /* size beyond a fixed capacity                   */
+} nesf_status;
+
+typedef enum { NESF_F64 = 0, NESF_F32 = 1 } nesf_dtype;
+
+/* ------------------------------------------------------------------ grid */
+typedef struct {
+    int32_t nx, ny;        /* interior cells                                   */
+    int32_t hx, hy;        /* halo widths of every 2-D array of the call       */
+    int64_t stride_j;      /* elements between (i, j) and (i, j+1); >= nx+2hx  */
+} nesf_grid;
+
+/* ------------------------------------------------- thermodynamic parameters
+ * AtmosphereThermodynamicsParameters, src/Atmospheres/thermodynamic_parameters.jl:61-69,106-116,149-165 */
+typedef struct {
+    double gas_constant;                     /* R   = 8.3144598  */
+    double dry_air_molar_mass;               /* Md  = 0.02897    */
+    double water_molar_mass;                 /* Mv  = 0.018015   */
+    double dry_air_adiabatic_exponent;       /* kd  = 2/7        */
+    double water_vapor_heat_capacity;        /* cpv = 1859       */
+    double liquid_water_heat_capacity;       /* cpl = 4181       */
+    double water_ice_heat_capacity;          /* cpi = 2100       */
+    double reference_vaporization_enthalpy;  /* Lv0 = 2500800    */
+    double reference_sublimation_enthalpy;   /* Ls0 = 2834400    */
+    double reference_temperature;            /* T0  = 273.16     */
+    double triple_point_temperature;         /* Ttr = 273.16     */
+    double triple_point_pressure;            /* ptr = 611.657    */
+} nesf_thermodynamics_parameters;
+
+/* ----------------------------------------------------- stability functions
+ * similarity_theory_turbulent_fluxes.jl:487-532 (Edson momentum), 571-618
+ * (Edson scalar), 637-677 (SHEBA), 683-710 (Paulson), 712-725 (Split),
+ * 742-752 (linear stable). Coefficients are stored in the field order of the
+ * reference struct(s). */
+typedef enum {
+    NESF_PSI_ZERO = 0,                    /* psi == 0 (neutral)                          */
+    NESF_PSI_EDSON_MOMENTUM = 1,          /* c = zmax A+ B+ C+ D+ A- B- C- D- E- F-     */
+    NESF_PSI_EDSON_SCALAR = 2,            /* c = zmax A+ B+ C+ D+ E+ A- B- C- D- E- F-  */
+    NESF_PSI_SHEBA_PAULSON_MOMENTUM = 3,  /* c = sheba a b, paulson a b                  */
+    NESF_PSI_SHEBA_PAULSON_SCALAR = 4,    /* c = sheba a b c, paulson a                  */
+    NESF_PSI_LINEAR_PAULSON_MOMENTUM = 5, /* c = linear coef zmax, paulson a b           */
+    NESF_PSI_LINEAR_PAULSON_SCALAR = 6    /* c = linear coef zmax, paulson a             */
+} nesf_psi_kind;
+
+typedef struct {
+    int32_t kind;
+    int32_t pad_;
+    double c[12];
+} nesf_stability_function;
+
+/* -------------------------------------------------------- roughness lengths
+ * roughness_lengths.jl:1-16 (structs), 74-75 (gravity wave parameter), 93-139
+ * (constructors), 182-189 (viscosity), 197-246 (roughness_length). */
+typedef enum {
+    NESF_ROUGHNESS_CONSTANT = 0,  /* a Number: ell = value                     */
+    NESF_ROUGHNESS_MOMENTUM = 1,  /* MomentumRoughnessLength                   */
+    NESF_ROUGHNESS_SCALAR = 2     /* ScalarRoughnessLength + ReynoldsScaling    */
+} nesf_roughness_kind;
+
+typedef struct {
+    int32_t kind;
+    int32_t wave_kind;            /* 0: constant Charnock; 1: WindDependentWaveFormulation */
+    int32_t viscosity_kind;       /* 0: constant nu; 1: TemperatureDependentAirViscosity   */
+    int32_t pad_;
+    double value;                 /* constant length                                       */
+    double gravitational_acceleration;
+    double air_kinematic_viscosity;       /* nu (constant)                                 */
+    double viscosity_coefficients[4];     /* C0..C3 of the temperature-dependent law       */
+    double charnock;                      /* constant wave_formulation (0.02)              */
+    double wave_umax, wave_c1, wave_c2;   /* WindDependentWaveFormulation(Umax, C1, C2)    */
+    double smooth_wall_parameter;         /* 0.11                                          */
+    double maximum_roughness_length;
+    double reynolds_A, reynolds_b;        /* ReynoldsScalingFunction(A, b)                 */
+} nesf_roughness_length;
+
+/* --------------------------------------------------- SimilarityTheoryFluxes
+ * similarity_theory_turbulent_fluxes.jl:9-18,174-214; compute_interface_state.jl:5-24 */
+typedef enum { NESF_SUBGRID_NONE = 0, NESF_SUBGRID_CONSTANT = 1, NESF_SUBGRID_CONVECTIVE = 2 } nesf_subgrid_kind;
+typedef enum { NESF_STOP_CONVERGENCE = 0, NESF_STOP_FIXED_ITERATIONS = 1 } nesf_stop_kind;
+typedef enum { NESF_PROFILE_LOGARITHMIC = 0, NESF_PROFILE_COARE = 1 } nesf_profile_kind;
+
+typedef struct {
+    double von_karman_constant;          /* 0.4  */
+    double turbulent_prandtl_number;     /* 1    */
+    int32_t subgrid_kind;                /* convective part of SubgridVelocityCorrection       */
+    int32_t similarity_form;             /* nesf_profile_kind                                  */
+    double gustiness_parameter;          /* beta = 1.2                                         */
+    double minimum_gustiness;            /* 0.01                                               */
+    double constant_subgrid_velocity;    /* for NESF_SUBGRID_CONSTANT                          */
+    double mesoscale_subgrid_velocity;   /* static mesoscale slot (0 = nothing)                */
+    nesf_stability_function stability[3];     /* momentum, temperature, water vapor            */
+    nesf_roughness_length roughness[3];       /* momentum, temperature, water vapor            */
+    double zero_plane_displacement;      /* d = 0                                              */
+    int32_t stop_kind;                   /* nesf_stop_kind                                     */
+    int32_t maxiter;                     /* ConvergenceStopCriteria.maxiter or FixedIterations */
+    double tolerance;                    /* absolute drift tolerance 1e-8                      */
+} nesf_similarity_theory_fluxes;
+
+/* ------------------------------------------- interface + component properties */
+typedef enum { NESF_PHASE_LIQUID = 0, NESF_PHASE_ICE = 1 } nesf_phase;
+typedef enum { NESF_RELATIVE_VELOCITY = 0, NESF_WIND_VELOCITY = 1 } nesf_velocity_formulation;
+typedef enum {
+    NESF_BULK_TEMPERATURE = 0,             /* interface_states.jl:330-333            */
+    NESF_SKIN_TEMPERATURE_CONDUCTIVE = 1,  /* ice/snow: interface_states.jl:468-524  */
+    NESF_SKIN_TEMPERATURE_DIFFUSIVE = 2    /* ocean DiffusiveFlux: interface_states.jl:434-457 */
+} nesf_temperature_formulation;
+
+typedef struct {
+    nesf_similarity_theory_fluxes fluxes;
+    nesf_thermodynamics_parameters thermo;
+    int32_t humidity_phase;               /* nesf_phase                                  */
+    int32_t has_water_mole_fraction;      /* 0: nothing (x = 1)                          */
+    double water_mole_fraction;           /* x_H2O = 0.98 for the ocean                  */
+    int32_t velocity_formulation;         /* nesf_velocity_formulation                   */
+    int32_t temperature_formulation;      /* nesf_temperature_formulation                */
+    double max_delta_T;                   /* SkinTemperature max_dT = 5                  */
+    double ice_conductivity;              /* 2    (ConductiveFlux)                       */
+    double snow_conductivity;             /* 0.31 (IceSnowConductiveFlux); 0 = no snow   */
+    double diffusive_kappa, diffusive_delta;  /* DiffusiveFlux(kappa, delta)            */
+    double gravitational_acceleration;    /* atmosphere_properties g = 9.80665           */
+    double surface_layer_height;          /* h    = 10                                   */
+    double boundary_layer_height;         /* h_bl = 512                                  */
+    double interior_temperature_offset;   /* 273.15: interior temperatures in Celsius    */
+    double interface_temperature_offset;  /* 273.15: interface temperature field in C    */
+    int32_t has_radiation;                /* radiation state present                     */
+    int32_t pad_;
+    double stefan_boltzmann_constant;     /* 5.670374419e-8                              */
+    double albedo, emissivity;            /* surface radiation properties                */
+    double liquidus_freshwater_melting_temperature;  /* LinearLiquidus: 0 (Celsius)     */
+    double liquidus_slope;                           /* 0.054                           */
+    double interior_reference_density;    /* rho_o (ocean skin temperature)             */
+    double interior_heat_capacity;        /* c_o                                         */
+} nesf_interface_params;
+
+/* ------------------------------------------------------ solver precision */
+typedef enum {
+    NESF_PLAIN_F64 = 0,   /* every iteration in FP64: the drop-in                         */
+    NESF_F32_POLISH = 1   /* FP32 iterations; FP64 polish where the FP32 residual stalls  */
+} nesf_precision;
+
+typedef struct {
+    int32_t precision;        /* nesf_precision                                        */
+    int32_t polish_maxiter;   /* FP64 polish iterations at most (default 3)            */
+    int32_t block_size;       /* threads per block; 0 = library default                */
+    int32_t schedule;         /* 0: one thread per cell; 1: persistent lane refill      */
+    int32_t ctas_per_sm;      /* persistent schedule: CTAs per SM (0 = occupancy)       */
+    int32_t warm_start;       /* 1: MLP initial guess (needs mlp weights)              */
+    const void* mlp;          /* device pointer to packed MLP weights (nesf_mlp_*)      */
+    double fallback_ratio;    /* cold-start fallback when r1 > ratio * r1(cold); 10    */
+} nesf_solver_options;
+
+/* -------------------------------------------------------------- statistics */
+#define NESF_ITER_HIST_BINS 128
+typedef struct {
+    int64_t cells;              /* cells visited                                   */
+    int64_t solved;             /* cells that ran the fixed point                  */
+    int64_t iterations;         /* sum of iterations over solved cells             */
+    int64_t max_iterations;
+    int64_t nonconverged;       /* cells that stopped at maxiter                   */
+    int64_t polished;           /* cells that needed an FP64 polish                */
+    int64_t polish_iterations;  /* FP64 polish iterations                          */
+    int64_t cold_fallbacks;     /* warm starts rejected by the residual test       */
+    int64_t histogram[NESF_ITER_HIST_BINS]; /* iterations (FP32+FP64) per solved cell */
+} nesf_stats;
+
+/* ------------------------------------------- atmosphere-ocean field bundle
+ * Arguments of _compute_atmosphere_ocean_interface_state!
+ * (atmosphere_ocean_fluxes.jl:80-197) */
+typedef struct {
+    nesf_grid grid;
+    int32_t dtype;                 /* nesf_dtype of every float array below               */
+    int32_t pad_;
+    const void* u_atm;  const void* v_atm;  const void* T_atm;  const void* p_atm;  const void* q_atm;
+    const void* u_oc;              /* ocean u at k = Nz (x-face)                          */
+    const void* v_oc;              /* ocean v at k = Nz (y-face)                          */
+    const void* T_oc;              /* ocean T at k = Nz (interior temperature units)     */
+    const void* S_oc;              /* ocean S at k = Nz                                   */
+    const uint8_t* inactive;       /* 1 = land/immersed (halo included); NULL = none      */
+    const void* sw_down;           /* downwelling shortwave (skin formulations only)      */
+    const void* lw_down;           /* downwelling longwave                                */
+    const void* kappa;             /* interior diffusivity (InteriorDiffusivity) or NULL  */
+    /* outputs: AtmosphereSurfaceFluxes (component_interfaces.jl:69-78) + T_s */
+    void* latent_heat; void* sensible_heat; void* water_vapor;
+    void* x_momentum;  void* y_momentum;
+    void* friction_velocity; void* temperature_scale; void* water_vapor_scale;
+    void* interface_temperature;
+    int32_t* iterations;           /* optional: iterations per cell (same layout)         */
+} nesf_ao_fields;
+
+/* --------------------------------------------- atmosphere-sea-ice bundle
+ * _compute_atmosphere_sea_ice_interface_state! (atmosphere_sea_ice_fluxes.jl:65-185) */
+typedef struct {
+    nesf_grid grid;
+    int32_t dtype;
+    int32_t pad_;
+    const void* u_atm; const void* v_atm; const void* T_atm; const void* p_atm; const void* q_atm;
+    const void* T_oc; const void* S_oc;          /* ocean surface under the ice         */
+    const void* ice_thickness;                   /* h_i                                 */
+    const void* snow_thickness;                  /* h_s (NULL = no snow)                */
+    const void* consolidation_thickness;         /* h_c                                 */
+    const void* ice_concentration;               /* aleph                               */
+    const uint8_t* inactive;
+    const void* sw_down; const void* lw_down;
+    /* in/out: interface (top surface) temperature; read as the initial T_s */
+    void* interface_temperature;
+    /* outputs: AtmosphereSeaIceFluxes (component_interfaces.jl:111-117) */
+    void* latent_heat; void* sensible_heat; void* water_vapor; void* x_momentum; void* y_momentum;
+    int32_t* iterations;
+} nesf_ai_fields;
+
+/* ----------------------------------------------------- sea-ice-ocean bundle
+ * sea_ice_ocean_fluxes.jl:106-226 + sea_ice_ocean_heat_flux_formulations.jl:118-313 */
+typedef struct {
+    int32_t formulation;            /* 0: ThreeEquationHeatFlux; 1: IceBathHeatFlux        */
+    int32_t conductive;             /* ThreeEquation with ConductiveFlux internal flux      */
+    double heat_transfer_coefficient;   /* alpha_h 0.0095 (IceBath 0.006)                 */
+    double salt_transfer_coefficient;   /* alpha_s = alpha_h / 35                         */
+    double friction_velocity;           /* constant u* 0.002                              */
+    double ice_conductivity;            /* k for ConductiveFlux                           */
+    double reference_latent_heat;       /* phase_transitions.reference_latent_heat        */
+    double liquidus_freshwater_melting_temperature, liquidus_slope;
+    double ocean_reference_density, ocean_heat_capacity;
+    double dt;                          /* sea-ice time step                               */
+    int32_t nz;                         /* ocean levels for the frazil column             */
+    int32_t pad_;
+    int64_t stride_k;                   /* elements between levels of the 3-D T/S arrays  */
+} nesf_io_params;
+
+typedef struct {
+    nesf_grid grid;
+    int32_t dtype;
+    int32_t pad_;
+    void* T_oc;                      /* 3-D ocean temperature, pointer of level k = 1 (mutated by frazil) */
+    const void* S_oc;                /* 3-D ocean salinity, pointer of level k = 1                         */
+    const double* dz;                /* host or device? device array of nz layer thicknesses              */
+    const void* ice_salinity; const void* ice_thickness; const void* consolidation_thickness;
+    const void* ice_concentration;
+    const void* internal_temperature;   /* ice top temperature (ConductiveFlux formulation)  */
+    const void* ice_mass_flux; const void* snow_mass_flux;
+    /* outputs: SeaIceOceanFluxes (component_interfaces.jl:143-150) + interface T, S */
+    void* interface_heat; void* frazil_heat; void* salt; void* freshwater;
+    void* interface_T; void* interface_S;
+} nesf_io_fields;
+
+/* ----------------------------------------------- prescribed atmosphere
+ * PrescribedAtmosphere on a regular longitude-latitude grid, two time levels */
+typedef struct {
+    int32_t nx, ny;                   /* atmosphere interior size                        */
+    int32_t hx, hy;
+    int64_t stride_j;
+    int64_t stride_t;                 /* elements between the two time snapshots          */
+    double lon0, dlon;                /* longitude of the first cell centre, spacing      */
+    double lat0, dlat;                /* latitude of the first cell centre, spacing       */
+} nesf_atmos_grid;
+
+typedef struct {
+    double lon0, dlon, lat0, dlat;    /* exchange grid: first cell centre and spacing     */
+} nesf_exchange_coords;
+
+typedef struct {
+    nesf_grid grid;                   /* exchange grid layout                              */
+    nesf_exchange_coords coords;
+    nesf_atmos_grid atmos;
+    int32_t dtype;                    /* dtype of atmosphere AND exchange arrays           */
+    int32_t pad_;
+    double time_weight;               /* n~ in [0, 1] between snapshot 1 and 2            */
+    const void* u; const void* v; const void* T; const void* q; const void* p;
+    const void* rain; const void* snow;           /* may be NULL (zero)                    */
+    const void* sw_down; const void* lw_down;     /* radiation; may be NULL                */
+    /* exchange-grid outputs (NULL skips the variable) */
+    void* u_out; void* v_out; void* T_out; void* q_out; void* p_out;
+    void* rain_out; void* snow_out; void* sw_out; void* lw_out;
+    /* optional fractional-index cache, FP64, exchange layout; NULL = recompute inline */
+    const double* frac_i; const double* frac_j;
+} nesf_interp_fields;
+
+/* ------------------------------------------------------- net-flux assembly */
+typedef struct {
+    double ocean_reference_density;   /* rho_o */
+    double ocean_heat_capacity;       /* c_o   */
+    double interface_temperature_offset;   /* 273.15 when T_s is stored in Celsius */
+    double stefan_boltzmann_constant;
+    double ocean_albedo, ocean_emissivity;
+    double ice_albedo, ice_emissivity;
+} nesf_assembly_params;
+
+typedef struct {
+    nesf_grid grid;
+    int32_t dtype;
+    int32_t pad_;
+    const uint8_t* inactive;
+    const void* ice_concentration;                   /* NULL = no sea ice               */
+    const void* ocean_surface_temperature;           /* T_oc at k = Nz (Celsius)        */
+    const void* rain; const void* snow; const void* intercepted_snow; const void* land_freshwater;
+    /* atmosphere-ocean fluxes */
+    const void* ao_sensible; const void* ao_latent; const void* ao_water_vapor;
+    const void* ao_x_momentum; const void* ao_y_momentum;
+    const void* ao_interface_temperature;
+    /* sea-ice-ocean fluxes (NULL = none) */
+    const void* io_interface_heat; const void* io_frazil_heat; const void* io_salt;
+    const void* io_freshwater; const void* io_x_momentum; const void* io_y_momentum;
+    /* atmosphere-sea-ice fluxes (NULL = none) */
+    const void* ai_sensible; const void* ai_latent; const void* ai_x_momentum; const void* ai_y_momentum;
+    const void* ai_interface_temperature;
+    /* radiation (NULL = no radiation) */
+    const void* sw_down; const void* lw_down;
+    /* outputs: net ocean fluxes (Oceans.jl:174-191) */
+    void* ocean_u; void* ocean_v; void* ocean_T; void* ocean_S; void* ocean_eta; void* ocean_heat_content;
+    /* outputs: net sea-ice fluxes (sea_ice_simulation.jl:223-237) */
+    void* ice_top_heat; void* ice_top_snowfall; void* ice_top_u; void* ice_top_v; void* ice_bottom_heat;
+    /* optional radiation diagnostics (InterfaceRadiationFlux) */
+    void* ocean_upwelling_longwave; void* ocean_downwelling_longwave; void* ocean_downwelling_shortwave;
+    void* ice_upwelling_longwave; void* ice_downwelling_longwave; void* ice_downwelling_shortwave;
+} nesf_assembly_fields;
+
+/* ------------------------------------------------------------------ API */
+typedef struct nesf_context nesf_context;   /* library-owned scratch per device */
+
+int32_t     nesf_abi_version(void);
+const char* nesf_version(void);
+const char* nesf_last_error(void);
+/* sizes of the public structs, for binding checks: fills n entries */
+int32_t     nesf_struct_sizes(int64_t* sizes, int32_t n);
+
+/* Fill parameter structs with the reference defaults (host memory). */
+void nesf_default_thermodynamics(nesf_thermodynamics_parameters* p);
+void nesf_default_ao_params(nesf_interface_params* p);      /* ComponentInterfaces AO defaults */
+void nesf_default_ai_params(nesf_interface_params* p);      /* AO defaults + ice/skin changes  */
+void nesf_default_io_params(nesf_io_params* p);
+void nesf_default_assembly_params(nesf_assembly_params* p);
+void nesf_default_solver_options(nesf_solver_options* o);
+
+int nesf_context_create(int32_t device, nesf_context** ctx);
+int nesf_context_destroy(nesf_context* ctx);
+
+/* compute_atmosphere_ocean_fluxes! (atmosphere_ocean_fluxes.jl:17-60):
+ * launches over the halo ring (0:nx+1, 0:ny+1) like interface_kernel_parameters
+ * (InterfaceComputations.jl:100-116). */
+int nesf_compute_atmosphere_ocean_fluxes(nesf_context* ctx, const nesf_interface_params* params,
+                                         const nesf_ao_fields* fields, const nesf_solver_options* opts,
+                                         nesf_stats* stats, void* stream);
+
+/* Ensemble variant: `members` independent copies of the AO problem laid out
+ * back to back (member stride `member_stride` elements in every array), each
+ * with its own parameters (`params[members]`, host memory). */
+int nesf_compute_atmosphere_ocean_fluxes_ensemble(nesf_context* ctx, const nesf_interface_params* params,
+                                                  int32_t members, int64_t member_stride,
+                                                  const nesf_ao_fields* fields, const nesf_solver_options* opts,
+                                                  nesf_stats* stats, void* stream);
+
+/* compute_atmosphere_sea_ice_fluxes! (atmosphere_sea_ice_fluxes.jl:18-62) */
+int nesf_compute_atmosphere_sea_ice_fluxes(nesf_context* ctx, const nesf_interface_params* params,
+                                           const nesf_ai_fields* fields, const nesf_solver_options* opts,
+                                           nesf_stats* stats, void* stream);
+
+/* compute_sea_ice_ocean_fluxes! (sea_ice_ocean_fluxes.jl:33-77): interior (:xy) launch */
+int nesf_compute_sea_ice_ocean_fluxes(nesf_context* ctx, const nesf_io_params* params,
+                                      const nesf_io_fields* fields, void* stream);
+
+/* initialize!(exchanger) -> _compute_fractional_indices! (prescribed_atmosphere_regridder.jl:41-71) */
+int nesf_compute_fractional_indices(const nesf_grid* grid, const nesf_exchange_coords* coords,
+                                    const nesf_atmos_grid* atmos, double* frac_i, double* frac_j,
+                                    void* stream);
+
+/* interpolate_state!(exchanger, grid, ::PrescribedAtmosphere, model)
+ * (interpolate_atmospheric_state.jl:9-137) and the radiation twin
+ * (interpolate_radiation_state.jl:4-69): halo-ring launch. */
+int nesf_interpolate_atmosphere_state(const nesf_interp_fields* fields, void* stream);
+
+/* update_net_fluxes!(model, ocean) (assemble_net_ocean_fluxes.jl:30-153) */
+int nesf_assemble_net_ocean_fluxes(const nesf_assembly_params* params, const nesf_assembly_fields* fields,
+                                   void* stream);
+/* update_net_fluxes!(model, sea_ice) (assemble_net_sea_ice_fluxes.jl:11-81) */
+int nesf_assemble_net_sea_ice_fluxes(const nesf_assembly_params* params, const nesf_assembly_fields* fields,
+                                     void* stream);
+/* apply_air_sea_radiative_fluxes! (apply_air_sea_radiative_fluxes.jl:18-111) */
+int nesf_apply_air_sea_radiative_fluxes(const nesf_assembly_params* params, const nesf_assembly_fields* fields,
+                                        void* stream);
+/* apply_air_sea_ice_radiative_fluxes! (apply_air_sea_ice_radiative_fluxes.jl:15-90) */
+int nesf_apply_air_sea_ice_radiative_fluxes(const nesf_assembly_params* params, const nesf_assembly_fields* fields,
+                                            void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NESF_H */

@@ -1,0 +1,677 @@
+// nesf_capi.cu -- the extern "C" entry points of libnesf.so (declared in include/nesf.h).
+//
+// Validation, parameter conversion and dispatch to the kernels. Each entry point
+// returns an nesf_status and records a message for nesf_last_error() on failure.
+#include <cstdio>
+#include <cstring>
+#include <cstdarg>
+#include <mutex>
+#include <new>
+
+#include "nesf_solve.cuh"
+#include "nesf_exchange.cuh"
+
+using namespace nesf;
+
+struct nesf_context {
+    int device;
+    DevStats* d_stats;          // device statistics accumulator
+    DevStats* h_stats;          // pinned host copy
+    DevIface<double>* d_p64;    // per-member parameters (ensemble)
+    DevIface<float>* d_p32;
+    int32_t capacity_members;
+    std::mutex lock;            // serialises use of the scratch above
+};
+
+static thread_local char g_err[512] = "";
+
+static int fail(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+static int cuda_fail(cudaError_t e, const char* what) {
+    return fail(NESF_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define NESF_CUDA(call)                                   \
+    do {                                                  \
+        cudaError_t e_ = (call);                          \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+// Switches to the context's device for the duration of a call.
+struct DeviceGuard {
+    int prev = -1;
+    bool ok = true;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) { ok = false; return; }
+        if (prev != dev && cudaSetDevice(dev) != cudaSuccess) ok = false;
+    }
+    ~DeviceGuard() {
+        int cur;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+extern "C" {
+
+int32_t nesf_abi_version(void) { return NESF_ABI_VERSION; }
+const char* nesf_version(void) { return "nesf 0.1.0 (sm_103a)"; }
+const char* nesf_last_error(void) { return g_err; }
+
+int32_t nesf_struct_sizes(int64_t* sizes, int32_t n) {
+    const int64_t s[] = {
+        (int64_t)sizeof(nesf_grid), (int64_t)sizeof(nesf_thermodynamics_parameters),
+        (int64_t)sizeof(nesf_stability_function), (int64_t)sizeof(nesf_roughness_length),
+        (int64_t)sizeof(nesf_similarity_theory_fluxes), (int64_t)sizeof(nesf_interface_params),
+        (int64_t)sizeof(nesf_solver_options), (int64_t)sizeof(nesf_stats), (int64_t)sizeof(nesf_ao_fields),
+        (int64_t)sizeof(nesf_ai_fields), (int64_t)sizeof(nesf_io_params), (int64_t)sizeof(nesf_io_fields),
+        (int64_t)sizeof(nesf_atmos_grid), (int64_t)sizeof(nesf_exchange_coords), (int64_t)sizeof(nesf_interp_fields),
+        (int64_t)sizeof(nesf_assembly_params), (int64_t)sizeof(nesf_assembly_fields)};
+    int32_t m = (int32_t)(sizeof s / sizeof s[0]);
+    for (int32_t k = 0; k < n && k < m; k++) sizes[k] = s[k];
+    return m;
+}
+
+// ---------------------------------------------------------------- defaults
+void nesf_default_thermodynamics(nesf_thermodynamics_parameters* t) {
+    // src/Atmospheres/thermodynamic_parameters.jl:61-69,106-116,149-165
+    t->gas_constant = 8.3144598;
+    t->dry_air_molar_mass = 0.02897;
+    t->water_molar_mass = 0.018015;
+    t->dry_air_adiabatic_exponent = 2.0 / 7.0;
+    t->water_vapor_heat_capacity = 1859;
+    t->liquid_water_heat_capacity = 4181;
+    t->water_ice_heat_capacity = 2100;
+    t->reference_vaporization_enthalpy = 2500800;
+    t->reference_sublimation_enthalpy = 2834400;
+    t->reference_temperature = 273.16;
+    t->triple_point_temperature = 273.16;
+    t->triple_point_pressure = 611.657;
+}
+
+static void default_fluxes(nesf_similarity_theory_fluxes* f, bool ice) {
+    memset(f, 0, sizeof *f);
+    // similarity_theory_turbulent_fluxes.jl:174-214
+    f->von_karman_constant = 0.4;
+    f->turbulent_prandtl_number = 1;
+    f->subgrid_kind = NESF_SUBGRID_CONVECTIVE;
+    f->gustiness_parameter = 1.2;
+    f->minimum_gustiness = 0.01;
+    f->similarity_form = NESF_PROFILE_LOGARITHMIC;
+    const double pi = 3.14159265358979323846;
+    if (!ice) {
+        // Edson et al. 2013 (:487-499, :571-584)
+        double m[11] = {50.0, 0.35, 0.7, 0.75, 5 / 0.35, 15.0, 2.0, pi / 2, 10.15, 3.0, pi / sqrt(3.0)};
+        double s[12] = {50.0, 0.35, 2.0 / 3.0, 3.0 / 2.0, 14.28, 8.525, 15.0, 2.0, 0.0, 34.15, 3.0, pi / sqrt(3.0)};
+        f->stability[0].kind = NESF_PSI_EDSON_MOMENTUM;
+        for (int k = 0; k < 11; k++) f->stability[0].c[k] = m[k];
+        for (int n = 1; n < 3; n++) {
+            f->stability[n].kind = NESF_PSI_EDSON_SCALAR;
+            for (int k = 0; k < 12; k++) f->stability[n].c[k] = s[k];
+        }
+    } else {
+        // Paulson unstable + SHEBA stable (:637-640, 659-663, 683-703, 779-789)
+        f->stability[0].kind = NESF_PSI_SHEBA_PAULSON_MOMENTUM;
+        f->stability[0].c[0] = 6.5; f->stability[0].c[1] = 1.3;
+        f->stability[0].c[2] = 16.0; f->stability[0].c[3] = pi / 2;
+        for (int n = 1; n < 3; n++) {
+            f->stability[n].kind = NESF_PSI_SHEBA_PAULSON_SCALAR;
+            f->stability[n].c[0] = 5.0; f->stability[n].c[1] = 5.0; f->stability[n].c[2] = 3.0;
+            f->stability[n].c[3] = 16.0;
+        }
+    }
+    // roughness_lengths.jl:93-139
+    nesf_roughness_length* r = &f->roughness[0];
+    r->kind = NESF_ROUGHNESS_MOMENTUM;
+    r->gravitational_acceleration = 9.80665;
+    r->air_kinematic_viscosity = 1.5e-5;
+    r->charnock = 0.02;
+    r->smooth_wall_parameter = 0.11;
+    r->maximum_roughness_length = 1.0;
+    for (int n = 1; n < 3; n++) {
+        nesf_roughness_length* q = &f->roughness[n];
+        q->kind = NESF_ROUGHNESS_SCALAR;
+        q->air_kinematic_viscosity = 1.5e-5;
+        q->reynolds_A = 5.85e-5;
+        q->reynolds_b = 0.72;
+        q->maximum_roughness_length = 1.6e-4;
+    }
+    f->stop_kind = NESF_STOP_CONVERGENCE;
+    f->maxiter = 100;
+    f->tolerance = 1e-8;
+}
+
+void nesf_default_ao_params(nesf_interface_params* p) {
+    memset(p, 0, sizeof *p);
+    default_fluxes(&p->fluxes, false);
+    nesf_default_thermodynamics(&p->thermo);
+    p->humidity_phase = NESF_PHASE_LIQUID;       // component_interfaces.jl:353-358
+    p->has_water_mole_fraction = 1;
+    p->water_mole_fraction = 0.98;
+    p->velocity_formulation = NESF_RELATIVE_VELOCITY;
+    p->temperature_formulation = NESF_BULK_TEMPERATURE;
+    p->max_delta_T = 5;
+    p->gravitational_acceleration = 9.80665;
+    p->surface_layer_height = 10;
+    p->boundary_layer_height = 512;
+    p->interior_temperature_offset = 273.15;
+    p->interface_temperature_offset = 273.15;
+    p->stefan_boltzmann_constant = 5.670374419e-8;
+    p->albedo = 0;          // radiation off by default (has_radiation = 0)
+    p->emissivity = 0;
+    p->liquidus_freshwater_melting_temperature = 0;
+    p->liquidus_slope = 0.054;
+    p->interior_reference_density = 1020;
+    p->interior_heat_capacity = 3991.86795711963;
+}
+
+void nesf_default_ai_params(nesf_interface_params* p) {
+    nesf_default_ao_params(p);
+    default_fluxes(&p->fluxes, true);
+    p->humidity_phase = NESF_PHASE_ICE;          // component_interfaces.jl:280-281
+    p->has_water_mole_fraction = 0;
+    p->water_mole_fraction = 1;
+    p->temperature_formulation = NESF_SKIN_TEMPERATURE_CONDUCTIVE;   // sea_ice_simulation.jl:240-249
+    p->ice_conductivity = 2;
+    p->snow_conductivity = 0.31;
+    p->has_radiation = 1;
+    p->albedo = 0.7;                             // prescribed_radiation.jl:53-54
+    p->emissivity = 1.0;
+}
+
+void nesf_default_io_params(nesf_io_params* p) {
+    memset(p, 0, sizeof *p);
+    p->formulation = 0;                          // ThreeEquationHeatFlux(sea_ice)
+    p->conductive = 1;
+    p->heat_transfer_coefficient = 0.0095;
+    p->salt_transfer_coefficient = 0.0095 / 35;
+    p->friction_velocity = 0.002;
+    p->ice_conductivity = 2;
+    p->reference_latent_heat = 334e3;
+    p->liquidus_freshwater_melting_temperature = 0;
+    p->liquidus_slope = 0.054;
+    p->ocean_reference_density = 1020;
+    p->ocean_heat_capacity = 3991.86795711963;
+    p->dt = 300;
+    p->nz = 1;
+    p->stride_k = 0;
+}
+
+void nesf_default_assembly_params(nesf_assembly_params* p) {
+    p->ocean_reference_density = 1020;
+    p->ocean_heat_capacity = 3991.86795711963;
+    p->interface_temperature_offset = 273.15;
+    p->stefan_boltzmann_constant = 5.670374419e-8;
+    p->ocean_albedo = 0.05;
+    p->ocean_emissivity = 0.97;
+    p->ice_albedo = 0.7;
+    p->ice_emissivity = 1.0;
+}
+
+void nesf_default_solver_options(nesf_solver_options* o) {
+    memset(o, 0, sizeof *o);
+    o->precision = NESF_PLAIN_F64;
+    o->polish_maxiter = 1;
+    o->block_size = 128;
+    o->schedule = 0;
+    o->ctas_per_sm = 0;
+    o->warm_start = 0;
+    o->mlp = nullptr;
+    o->fallback_ratio = 10.0;
+}
+
+// ---------------------------------------------------------------- context
+int nesf_context_create(int32_t device, nesf_context** out) {
+    if (!out) return fail(NESF_ERR_ARG, "nesf_context_create: null output pointer");
+    *out = nullptr;
+    int n = 0;
+    NESF_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return fail(NESF_ERR_ARG, "nesf_context_create: device %d of %d", device, n);
+    DeviceGuard g(device);
+    if (!g.ok) return fail(NESF_ERR_CUDA, "nesf_context_create: cannot select device %d", device);
+    nesf_context* c = new (std::nothrow) nesf_context();
+    if (!c) return fail(NESF_ERR_ARG, "nesf_context_create: out of host memory");
+    c->device = device;
+    c->capacity_members = 0;
+    c->d_p64 = nullptr;
+    c->d_p32 = nullptr;
+    cudaError_t e = cudaMalloc(&c->d_stats, sizeof(DevStats));
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_stats, sizeof(DevStats));
+    if (e != cudaSuccess) {
+        cudaFree(c->d_stats);
+        delete c;
+        return cuda_fail(e, "nesf_context_create");
+    }
+    *out = c;
+    return NESF_OK;
+}
+
+int nesf_context_destroy(nesf_context* c) {
+    if (!c) return NESF_OK;
+    {
+        DeviceGuard g(c->device);
+        cudaFree(c->d_stats);
+        cudaFreeHost(c->h_stats);
+        cudaFree(c->d_p64);
+        cudaFree(c->d_p32);
+    }
+    delete c;
+    return NESF_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ helpers
+static int check_grid(const nesf_grid& g, int hmin, const char* who) {
+    if (g.nx <= 0 || g.ny <= 0) return fail(NESF_ERR_ARG, "%s: grid size %d x %d", who, g.nx, g.ny);
+    if (g.hx < hmin || g.hy < hmin)
+        return fail(NESF_ERR_ARG, "%s: halo (%d, %d) smaller than %d", who, g.hx, g.hy, hmin);
+    if (g.stride_j < (int64_t)g.nx + 2 * g.hx)
+        return fail(NESF_ERR_ARG, "%s: stride_j %lld < nx + 2hx", who, (long long)g.stride_j);
+    return NESF_OK;
+}
+
+static Layout2 layout(const nesf_grid& g) { return Layout2{g.nx, g.ny, g.hx, g.hy, g.stride_j}; }
+
+static int check_params(const nesf_interface_params* p, const char* who) {
+    if (!p) return fail(NESF_ERR_ARG, "%s: null params", who);
+    const nesf_similarity_theory_fluxes& f = p->fluxes;
+    if (f.maxiter < 0) return fail(NESF_ERR_ARG, "%s: maxiter %d < 0", who, f.maxiter);
+    if (!(f.tolerance >= 0)) return fail(NESF_ERR_ARG, "%s: tolerance must be >= 0", who);
+    for (int n = 0; n < 3; n++) {
+        if (f.stability[n].kind < NESF_PSI_ZERO || f.stability[n].kind > NESF_PSI_LINEAR_PAULSON_SCALAR)
+            return fail(NESF_ERR_ARG, "%s: stability function kind %d", who, f.stability[n].kind);
+        if (f.roughness[n].kind < NESF_ROUGHNESS_CONSTANT || f.roughness[n].kind > NESF_ROUGHNESS_SCALAR)
+            return fail(NESF_ERR_ARG, "%s: roughness kind %d", who, f.roughness[n].kind);
+    }
+    if (f.roughness[0].kind == NESF_ROUGHNESS_SCALAR)
+        return fail(NESF_ERR_ARG, "%s: the momentum roughness cannot be a ScalarRoughnessLength", who);
+    if (p->temperature_formulation < NESF_BULK_TEMPERATURE ||
+        p->temperature_formulation > NESF_SKIN_TEMPERATURE_DIFFUSIVE)
+        return fail(NESF_ERR_ARG, "%s: temperature formulation %d", who, p->temperature_formulation);
+    if (p->surface_layer_height <= 0) return fail(NESF_ERR_ARG, "%s: surface_layer_height <= 0", who);
+    return NESF_OK;
+}
+
+static nesf_solver_options options_or_default(const nesf_solver_options* o) {
+    nesf_solver_options d;
+    nesf_default_solver_options(&d);
+    if (!o) return d;
+    nesf_solver_options r = *o;
+    if (r.polish_maxiter <= 0) r.polish_maxiter = d.polish_maxiter;
+    return r;
+}
+
+static int check_options(const nesf_solver_options& o, const char* who) {
+    if (o.precision != NESF_PLAIN_F64 && o.precision != NESF_F32_POLISH)
+        return fail(NESF_ERR_ARG, "%s: precision %d", who, o.precision);
+    if (o.warm_start) return fail(NESF_ERR_UNSUPPORTED, "%s: warm start needs nesf_coupling_step", who);
+    return NESF_OK;
+}
+
+static void stats_to_public(const DevStats& d, nesf_stats* s) {
+    s->cells = (int64_t)d.cells;
+    s->solved = (int64_t)d.solved;
+    s->iterations = (int64_t)d.iterations;
+    s->max_iterations = (int64_t)d.max_iterations;
+    s->nonconverged = (int64_t)d.nonconverged;
+    s->polished = (int64_t)d.polished;
+    s->polish_iterations = (int64_t)d.polish_iterations;
+    s->cold_fallbacks = (int64_t)d.cold_fallbacks;
+    for (int k = 0; k < NESF_ITER_HIST_BINS; k++) s->histogram[k] = (int64_t)d.hist[k];
+}
+
+// Runs `launch(d_stats or nullptr)` with optional statistics readback.
+template <class F>
+static int with_stats(nesf_context* ctx, nesf_stats* stats, cudaStream_t s, F launch) {
+    DevStats* ds = nullptr;
+    if (stats) {
+        if (!ctx) return fail(NESF_ERR_ARG, "statistics need a context");
+        ds = ctx->d_stats;
+        NESF_CUDA(cudaMemsetAsync(ds, 0, sizeof(DevStats), s));
+    }
+    cudaError_t e = launch(ds);
+    if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    if (stats) {
+        NESF_CUDA(cudaMemcpyAsync(ctx->h_stats, ds, sizeof(DevStats), cudaMemcpyDeviceToHost, s));
+        NESF_CUDA(cudaStreamSynchronize(s));
+        stats_to_public(*ctx->h_stats, stats);
+    }
+    return NESF_OK;
+}
+
+template <class S>
+static AOArgs<S> ao_args(const nesf_ao_fields* f, int64_t member_stride) {
+    AOArgs<S> a;
+    a.L = layout(f->grid);
+    a.member_stride = member_stride;
+    a.ua = (const S*)f->u_atm; a.va = (const S*)f->v_atm; a.Ta = (const S*)f->T_atm;
+    a.pa = (const S*)f->p_atm; a.qa = (const S*)f->q_atm;
+    a.uo = (const S*)f->u_oc; a.vo = (const S*)f->v_oc; a.To = (const S*)f->T_oc; a.So = (const S*)f->S_oc;
+    a.inactive = f->inactive;
+    a.sw = (const S*)f->sw_down; a.lw = (const S*)f->lw_down; a.kappa = (const S*)f->kappa;
+    a.Qv = (S*)f->latent_heat; a.QT = (S*)f->sensible_heat; a.Jv = (S*)f->water_vapor;
+    a.tx = (S*)f->x_momentum; a.ty = (S*)f->y_momentum;
+    a.us = (S*)f->friction_velocity; a.ts = (S*)f->temperature_scale; a.qs = (S*)f->water_vapor_scale;
+    a.Ts = (S*)f->interface_temperature;
+    a.iters = f->iterations;
+    return a;
+}
+
+static int check_ao_fields(const nesf_ao_fields* f, const nesf_interface_params* p, const char* who) {
+    if (!f) return fail(NESF_ERR_ARG, "%s: null fields", who);
+    int r = check_grid(f->grid, 2, who);
+    if (r) return r;
+    if (f->dtype != NESF_F64 && f->dtype != NESF_F32) return fail(NESF_ERR_ARG, "%s: dtype %d", who, f->dtype);
+    const void* req[] = {f->u_atm, f->v_atm, f->T_atm, f->p_atm, f->q_atm, f->u_oc, f->v_oc, f->T_oc, f->S_oc};
+    const char* names[] = {"u_atm", "v_atm", "T_atm", "p_atm", "q_atm", "u_oc", "v_oc", "T_oc", "S_oc"};
+    for (int k = 0; k < 9; k++)
+        if (!req[k]) return fail(NESF_ERR_ARG, "%s: required input %s is NULL", who, names[k]);
+    if (p->temperature_formulation == NESF_SKIN_TEMPERATURE_CONDUCTIVE)
+        return fail(NESF_ERR_UNSUPPORTED, "%s: conductive skin temperature over the ocean", who);
+    if (p->has_radiation && p->temperature_formulation != NESF_BULK_TEMPERATURE && (!f->sw_down || !f->lw_down))
+        return fail(NESF_ERR_ARG, "%s: skin temperature with radiation needs sw_down and lw_down", who);
+    return NESF_OK;
+}
+
+extern "C" int nesf_compute_atmosphere_ocean_fluxes(nesf_context* ctx, const nesf_interface_params* params,
+                                                    const nesf_ao_fields* f, const nesf_solver_options* opts,
+                                                    nesf_stats* stats, void* stream) {
+    const char* who = "nesf_compute_atmosphere_ocean_fluxes";
+    int r = check_params(params, who);
+    if (r) return r;
+    if ((r = check_ao_fields(f, params, who))) return r;
+    nesf_solver_options o = options_or_default(opts);
+    if ((r = check_options(o, who))) return r;
+    std::unique_lock<std::mutex> lk;
+    if (ctx) lk = std::unique_lock<std::mutex>(ctx->lock);
+    DeviceGuard g(ctx ? ctx->device : 0);
+    DevIface<double> P64 = make_dev_iface<double>(*params);
+    DevIface<float> P32 = make_dev_iface<float>(*params);
+    cudaStream_t s = (cudaStream_t)stream;
+    bool skin = params->temperature_formulation != NESF_BULK_TEMPERATURE;
+    return with_stats(ctx, stats, s, [&](DevStats* ds) {
+        if (f->dtype == NESF_F64)
+            return launch_ao(ao_args<double>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin,
+                             o.polish_maxiter, ds, o.block_size, s);
+        return launch_ao(ao_args<float>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, o.polish_maxiter,
+                         ds, o.block_size, s);
+    });
+}
+
+extern "C" int nesf_compute_atmosphere_ocean_fluxes_ensemble(nesf_context* ctx, const nesf_interface_params* params,
+                                                             int32_t members, int64_t member_stride,
+                                                             const nesf_ao_fields* f,
+                                                             const nesf_solver_options* opts, nesf_stats* stats,
+                                                             void* stream) {
+    const char* who = "nesf_compute_atmosphere_ocean_fluxes_ensemble";
+    if (!ctx) return fail(NESF_ERR_ARG, "%s: needs a context", who);
+    if (members <= 0 || members > 65535) return fail(NESF_ERR_ARG, "%s: members = %d", who, members);
+    int r;
+    for (int m = 0; m < members; m++)
+        if ((r = check_params(params + m, who))) return r;
+    if ((r = check_ao_fields(f, params, who))) return r;
+    for (int m = 1; m < members; m++)
+        if (params[m].temperature_formulation != params[0].temperature_formulation)
+            return fail(NESF_ERR_ARG, "%s: members must share the temperature formulation", who);
+    int64_t plane = f->grid.stride_j * ((int64_t)f->grid.ny + 2 * f->grid.hy);
+    if (member_stride < plane) return fail(NESF_ERR_ARG, "%s: member_stride smaller than one array", who);
+    nesf_solver_options o = options_or_default(opts);
+    if ((r = check_options(o, who))) return r;
+    std::lock_guard<std::mutex> lk(ctx->lock);
+    DeviceGuard g(ctx->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (members > ctx->capacity_members) {
+        cudaFree(ctx->d_p64);
+        cudaFree(ctx->d_p32);
+        ctx->d_p64 = nullptr;
+        ctx->d_p32 = nullptr;
+        ctx->capacity_members = 0;
+        NESF_CUDA(cudaMalloc(&ctx->d_p64, sizeof(DevIface<double>) * members));
+        NESF_CUDA(cudaMalloc(&ctx->d_p32, sizeof(DevIface<float>) * members));
+        ctx->capacity_members = members;
+    }
+    DevIface<double>* h64 = new DevIface<double>[members];
+    DevIface<float>* h32 = new DevIface<float>[members];
+    for (int m = 0; m < members; m++) {
+        h64[m] = make_dev_iface<double>(params[m]);
+        h32[m] = make_dev_iface<float>(params[m]);
+    }
+    cudaError_t e = cudaMemcpyAsync(ctx->d_p64, h64, sizeof(DevIface<double>) * members, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->d_p32, h32, sizeof(DevIface<float>) * members, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);   // host staging buffers are freed below
+    delete[] h64;
+    delete[] h32;
+    if (e != cudaSuccess) return cuda_fail(e, who);
+    DevIface<double> P64 = make_dev_iface<double>(params[0]);
+    DevIface<float> P32 = make_dev_iface<float>(params[0]);
+    bool skin = params->temperature_formulation != NESF_BULK_TEMPERATURE;
+    return with_stats(ctx, stats, s, [&](DevStats* ds) {
+        if (f->dtype == NESF_F64)
+            return launch_ao(ao_args<double>(f, member_stride), P64, P32, ctx->d_p64, ctx->d_p32, members,
+                             o.precision, skin, o.polish_maxiter, ds, o.block_size, s);
+        return launch_ao(ao_args<float>(f, member_stride), P64, P32, ctx->d_p64, ctx->d_p32, members, o.precision,
+                         skin, o.polish_maxiter, ds, o.block_size, s);
+    });
+}
+
+template <class S>
+static AIArgs<S> ai_args(const nesf_ai_fields* f) {
+    AIArgs<S> a;
+    a.L = layout(f->grid);
+    a.ua = (const S*)f->u_atm; a.va = (const S*)f->v_atm; a.Ta = (const S*)f->T_atm;
+    a.pa = (const S*)f->p_atm; a.qa = (const S*)f->q_atm;
+    a.To = (const S*)f->T_oc; a.So = (const S*)f->S_oc;
+    a.hi = (const S*)f->ice_thickness; a.hs = (const S*)f->snow_thickness;
+    a.hc = (const S*)f->consolidation_thickness; a.aleph = (const S*)f->ice_concentration;
+    a.inactive = f->inactive;
+    a.sw = (const S*)f->sw_down; a.lw = (const S*)f->lw_down;
+    a.Ts = (S*)f->interface_temperature;
+    a.Qv = (S*)f->latent_heat; a.QT = (S*)f->sensible_heat; a.Jv = (S*)f->water_vapor;
+    a.tx = (S*)f->x_momentum; a.ty = (S*)f->y_momentum;
+    a.iters = f->iterations;
+    return a;
+}
+
+extern "C" int nesf_compute_atmosphere_sea_ice_fluxes(nesf_context* ctx, const nesf_interface_params* params,
+                                                      const nesf_ai_fields* f, const nesf_solver_options* opts,
+                                                      nesf_stats* stats, void* stream) {
+    const char* who = "nesf_compute_atmosphere_sea_ice_fluxes";
+    int r = check_params(params, who);
+    if (r) return r;
+    if (!f) return fail(NESF_ERR_ARG, "%s: null fields", who);
+    if ((r = check_grid(f->grid, 1, who))) return r;
+    if (f->dtype != NESF_F64 && f->dtype != NESF_F32) return fail(NESF_ERR_ARG, "%s: dtype %d", who, f->dtype);
+    const void* req[] = {f->u_atm, f->v_atm, f->T_atm, f->p_atm, f->q_atm, f->T_oc, f->S_oc, f->ice_thickness,
+                         f->consolidation_thickness, f->ice_concentration, f->interface_temperature};
+    for (const void* q : req)
+        if (!q) return fail(NESF_ERR_ARG, "%s: a required array is NULL", who);
+    if (params->temperature_formulation == NESF_SKIN_TEMPERATURE_DIFFUSIVE)
+        return fail(NESF_ERR_UNSUPPORTED, "%s: diffusive skin temperature over sea ice", who);
+    if (params->temperature_formulation == NESF_SKIN_TEMPERATURE_CONDUCTIVE && params->snow_conductivity > 0 &&
+        !f->snow_thickness)
+        return fail(NESF_ERR_ARG, "%s: snow conductivity given but snow_thickness is NULL", who);
+    if (params->has_radiation && (!f->sw_down || !f->lw_down))
+        return fail(NESF_ERR_ARG, "%s: radiation enabled but sw_down/lw_down NULL", who);
+    nesf_solver_options o = options_or_default(opts);
+    if ((r = check_options(o, who))) return r;
+    std::unique_lock<std::mutex> lk;
+    if (ctx) lk = std::unique_lock<std::mutex>(ctx->lock);
+    DeviceGuard g(ctx ? ctx->device : 0);
+    DevIface<double> P64 = make_dev_iface<double>(*params);
+    DevIface<float> P32 = make_dev_iface<float>(*params);
+    cudaStream_t s = (cudaStream_t)stream;
+    return with_stats(ctx, stats, s, [&](DevStats* ds) {
+        if (f->dtype == NESF_F64) return launch_ai(ai_args<double>(f), P64, P32, o.precision, o.polish_maxiter, ds, s);
+        return launch_ai(ai_args<float>(f), P64, P32, o.precision, o.polish_maxiter, ds, s);
+    });
+}
+
+template <class S>
+static IOArgs<S> io_args(const nesf_io_fields* f) {
+    IOArgs<S> a;
+    a.L = layout(f->grid);
+    a.T3 = (S*)f->T_oc; a.S3 = (const S*)f->S_oc; a.dz = f->dz;
+    a.Si = (const S*)f->ice_salinity; a.hi = (const S*)f->ice_thickness; a.hc = (const S*)f->consolidation_thickness;
+    a.aleph = (const S*)f->ice_concentration; a.Tint = (const S*)f->internal_temperature;
+    a.Ei = (const S*)f->ice_mass_flux; a.Es = (const S*)f->snow_mass_flux;
+    a.Qio = (S*)f->interface_heat; a.frazil = (S*)f->frazil_heat; a.Js = (S*)f->salt; a.Jw = (S*)f->freshwater;
+    a.Tb = (S*)f->interface_T; a.Sb = (S*)f->interface_S;
+    return a;
+}
+
+extern "C" int nesf_compute_sea_ice_ocean_fluxes(nesf_context* ctx, const nesf_io_params* p, const nesf_io_fields* f,
+                                                 void* stream) {
+    const char* who = "nesf_compute_sea_ice_ocean_fluxes";
+    if (!p || !f) return fail(NESF_ERR_ARG, "%s: null argument", who);
+    int r = check_grid(f->grid, 0, who);
+    if (r) return r;
+    if (f->dtype != NESF_F64 && f->dtype != NESF_F32) return fail(NESF_ERR_ARG, "%s: dtype %d", who, f->dtype);
+    if (p->nz < 1) return fail(NESF_ERR_ARG, "%s: nz = %d", who, p->nz);
+    if (p->nz > 1 && p->stride_k <= 0) return fail(NESF_ERR_ARG, "%s: stride_k must be > 0 for nz > 1", who);
+    if (!(p->reference_latent_heat != 0) || !(p->dt > 0) || !(p->ocean_reference_density > 0))
+        return fail(NESF_ERR_ARG, "%s: latent heat, dt and density must be nonzero/positive", who);
+    const void* req[] = {f->T_oc, f->S_oc, f->dz, f->ice_salinity, f->ice_thickness, f->consolidation_thickness,
+                         f->ice_concentration};
+    for (const void* q : req)
+        if (!q) return fail(NESF_ERR_ARG, "%s: a required array is NULL", who);
+    if (p->conductive && p->formulation == 0 && !f->internal_temperature)
+        return fail(NESF_ERR_ARG, "%s: conductive three-equation flux needs internal_temperature", who);
+    DeviceGuard g(ctx ? ctx->device : 0);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = f->dtype == NESF_F64 ? launch_io(io_args<double>(f), *p, s) : launch_io(io_args<float>(f), *p, s);
+    if (e != cudaSuccess) return cuda_fail(e, who);
+    return NESF_OK;
+}
+
+extern "C" int nesf_compute_fractional_indices(const nesf_grid* g, const nesf_exchange_coords* c,
+                                               const nesf_atmos_grid* a, double* fi, double* fj, void* stream) {
+    const char* who = "nesf_compute_fractional_indices";
+    if (!g || !c || !a || !fi || !fj) return fail(NESF_ERR_ARG, "%s: null argument", who);
+    int r = check_grid(*g, 0, who);
+    if (r) return r;
+    if (!(a->dlon != 0) || !(a->dlat != 0)) return fail(NESF_ERR_ARG, "%s: zero atmosphere spacing", who);
+    cudaError_t e = launch_frac(layout(*g), *c, *a, fi, fj, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, who);
+    return NESF_OK;
+}
+
+extern "C" int nesf_interpolate_atmosphere_state(const nesf_interp_fields* f, void* stream) {
+    const char* who = "nesf_interpolate_atmosphere_state";
+    if (!f) return fail(NESF_ERR_ARG, "%s: null fields", who);
+    int r = check_grid(f->grid, 1, who);
+    if (r) return r;
+    const nesf_atmos_grid& ag = f->atmos;
+    if (ag.nx <= 0 || ag.ny <= 0 || ag.hx < 0 || ag.hy < 0 || ag.stride_j < (int64_t)ag.nx + 2 * ag.hx)
+        return fail(NESF_ERR_ARG, "%s: atmosphere grid", who);
+    if (!(ag.dlon != 0) || !(ag.dlat != 0)) return fail(NESF_ERR_ARG, "%s: zero atmosphere spacing", who);
+    if (f->dtype != NESF_F64 && f->dtype != NESF_F32) return fail(NESF_ERR_ARG, "%s: dtype %d", who, f->dtype);
+    if ((f->frac_i == nullptr) != (f->frac_j == nullptr))
+        return fail(NESF_ERR_ARG, "%s: give both fractional index caches or neither", who);
+    const void* src[9] = {f->u, f->v, f->T, f->q, f->p, f->rain, f->snow, f->sw_down, f->lw_down};
+    void* dst[9] = {f->u_out, f->v_out, f->T_out, f->q_out, f->p_out, f->rain_out, f->snow_out, f->sw_out, f->lw_out};
+    for (int k = 0; k < 5; k++)
+        if (dst[k] && !src[k]) return fail(NESF_ERR_ARG, "%s: output %d requested without its input", who, k);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e;
+    if (f->dtype == NESF_F64) {
+        InterpArgs<double> a;
+        a.L = layout(f->grid); a.coords = f->coords; a.atmos = ag; a.tn = f->time_weight;
+        for (int k = 0; k < 9; k++) { a.src[k] = (const double*)src[k]; a.dst[k] = (double*)dst[k]; }
+        a.frac_i = f->frac_i; a.frac_j = f->frac_j;
+        e = launch_interp(a, s);
+    } else {
+        InterpArgs<float> a;
+        a.L = layout(f->grid); a.coords = f->coords; a.atmos = ag; a.tn = f->time_weight;
+        for (int k = 0; k < 9; k++) { a.src[k] = (const float*)src[k]; a.dst[k] = (float*)dst[k]; }
+        a.frac_i = f->frac_i; a.frac_j = f->frac_j;
+        e = launch_interp(a, s);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, who);
+    return NESF_OK;
+}
+
+template <class S>
+static AsmArgs<S> asm_args(const nesf_assembly_fields* f, int with_rad) {
+    AsmArgs<S> a;
+    a.L = layout(f->grid);
+    a.with_radiation = with_rad;
+    AsmFields<S>& q = a.f;
+    q.inactive = f->inactive;
+    q.aleph = (const S*)f->ice_concentration; q.To = (const S*)f->ocean_surface_temperature;
+    q.rain = (const S*)f->rain; q.snow = (const S*)f->snow; q.isnow = (const S*)f->intercepted_snow;
+    q.land_fw = (const S*)f->land_freshwater;
+    q.ao_QT = (const S*)f->ao_sensible; q.ao_Qv = (const S*)f->ao_latent; q.ao_Jv = (const S*)f->ao_water_vapor;
+    q.ao_tx = (const S*)f->ao_x_momentum; q.ao_ty = (const S*)f->ao_y_momentum;
+    q.ao_Ts = (const S*)f->ao_interface_temperature;
+    q.io_Q = (const S*)f->io_interface_heat; q.io_Qf = (const S*)f->io_frazil_heat; q.io_Js = (const S*)f->io_salt;
+    q.io_Jw = (const S*)f->io_freshwater; q.io_tx = (const S*)f->io_x_momentum; q.io_ty = (const S*)f->io_y_momentum;
+    q.ai_QT = (const S*)f->ai_sensible; q.ai_Qv = (const S*)f->ai_latent; q.ai_tx = (const S*)f->ai_x_momentum;
+    q.ai_ty = (const S*)f->ai_y_momentum; q.ai_Ts = (const S*)f->ai_interface_temperature;
+    q.sw = (const S*)f->sw_down; q.lw = (const S*)f->lw_down;
+    q.o_u = (S*)f->ocean_u; q.o_v = (S*)f->ocean_v; q.o_T = (S*)f->ocean_T; q.o_S = (S*)f->ocean_S;
+    q.o_eta = (S*)f->ocean_eta; q.o_H = (S*)f->ocean_heat_content;
+    q.i_top = (S*)f->ice_top_heat; q.i_snow = (S*)f->ice_top_snowfall; q.i_u = (S*)f->ice_top_u;
+    q.i_v = (S*)f->ice_top_v; q.i_bottom = (S*)f->ice_bottom_heat;
+    q.o_up_lw = (S*)f->ocean_upwelling_longwave; q.o_dn_lw = (S*)f->ocean_downwelling_longwave;
+    q.o_dn_sw = (S*)f->ocean_downwelling_shortwave;
+    q.i_up_lw = (S*)f->ice_upwelling_longwave; q.i_dn_lw = (S*)f->ice_downwelling_longwave;
+    q.i_dn_sw = (S*)f->ice_downwelling_shortwave;
+    return a;
+}
+
+static int run_assembly(const nesf_assembly_params* p, const nesf_assembly_fields* f, int which, void* stream,
+                        const char* who) {
+    if (!p || !f) return fail(NESF_ERR_ARG, "%s: null argument", who);
+    int r = check_grid(f->grid, 1, who);
+    if (r) return r;
+    if (f->dtype != NESF_F64 && f->dtype != NESF_F32) return fail(NESF_ERR_ARG, "%s: dtype %d", who, f->dtype);
+    if (!(p->ocean_reference_density > 0) || !(p->ocean_heat_capacity > 0))
+        return fail(NESF_ERR_ARG, "%s: density and heat capacity must be positive", who);
+    switch (which) {
+    case 0:
+        if (!f->ocean_surface_temperature || !f->ao_sensible || !f->ao_latent || !f->ao_water_vapor ||
+            !f->ao_x_momentum || !f->ao_y_momentum)
+            return fail(NESF_ERR_ARG, "%s: atmosphere-ocean fluxes and ocean temperature are required", who);
+        break;
+    case 1:
+        if (!f->ice_concentration || !f->ai_sensible || !f->ai_latent || !f->ai_x_momentum || !f->ai_y_momentum)
+            return fail(NESF_ERR_ARG, "%s: sea-ice concentration and atmosphere-sea-ice fluxes are required", who);
+        break;
+    case 2:
+        if (!f->ao_interface_temperature || !f->sw_down || !f->lw_down || !f->ocean_T)
+            return fail(NESF_ERR_ARG, "%s: T_s, radiation and ocean_T are required", who);
+        break;
+    default:
+        if (!f->ai_interface_temperature || !f->sw_down || !f->lw_down || !f->ice_top_heat || !f->ice_concentration)
+            return fail(NESF_ERR_ARG, "%s: T_s, radiation, concentration and top heat are required", who);
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = f->dtype == NESF_F64 ? launch_assemble(asm_args<double>(f, 0), *p, which, s)
+                                         : launch_assemble(asm_args<float>(f, 0), *p, which, s);
+    if (e != cudaSuccess) return cuda_fail(e, who);
+    return NESF_OK;
+}
+
+extern "C" int nesf_assemble_net_ocean_fluxes(const nesf_assembly_params* p, const nesf_assembly_fields* f,
+                                              void* stream) {
+    return run_assembly(p, f, 0, stream, "nesf_assemble_net_ocean_fluxes");
+}
+extern "C" int nesf_assemble_net_sea_ice_fluxes(const nesf_assembly_params* p, const nesf_assembly_fields* f,
+                                                void* stream) {
+    return run_assembly(p, f, 1, stream, "nesf_assemble_net_sea_ice_fluxes");
+}
+extern "C" int nesf_apply_air_sea_radiative_fluxes(const nesf_assembly_params* p, const nesf_assembly_fields* f,
+                                                   void* stream) {
+    return run_assembly(p, f, 2, stream, "nesf_apply_air_sea_radiative_fluxes");
+}
+extern "C" int nesf_apply_air_sea_ice_radiative_fluxes(const nesf_assembly_params* p, const nesf_assembly_fields* f,
+                                                       void* stream) {
+    return run_assembly(p, f, 3, stream, "nesf_apply_air_sea_ice_radiative_fluxes");
+}

@@ -1,0 +1,441 @@
+// nesf_device.cuh -- per-cell similarity-theory physics for the interface-flux kernels.
+//
+// Everything here is templated on the compute type R (double for the drop-in
+// FP64 solver and the polish step, float for the FP32 sweep). The formulas
+// restate NumericalEarth.jl v0.6.2 (paths below are inside that project) and
+// keep its left-to-right operation order; hoisted quantities are the ones the
+// reference recomputes every iteration from unchanged inputs, so hoisting them
+// does not change a result.
+#pragma once
+
+#include <cstdint>
+#include <cmath>
+#include <cuda_runtime.h>
+
+#include "../../include/nesf.h"
+
+namespace nesf {
+
+// ------------------------------------------------------------------ math
+template <class R> struct M;
+template <> struct M<double> {
+    static __device__ __forceinline__ double log(double x) { return ::log(x); }
+    static __device__ __forceinline__ double exp(double x) { return ::exp(x); }
+    static __device__ __forceinline__ double pow(double x, double y) { return ::pow(x, y); }
+    static __device__ __forceinline__ double atan(double x) { return ::atan(x); }
+    static __device__ __forceinline__ double cbrt(double x) { return ::cbrt(x); }
+    static __device__ __forceinline__ double sqrt(double x) { return ::sqrt(x); }
+    static __device__ __forceinline__ double fmin(double a, double b) { return ::fmin(a, b); }
+    static __device__ __forceinline__ double fmax(double a, double b) { return ::fmax(a, b); }
+    static __device__ __forceinline__ double fabs(double a) { return ::fabs(a); }
+    static __device__ __forceinline__ double inf() { return __longlong_as_double(0x7ff0000000000000LL); }
+};
+template <> struct M<float> {
+    static __device__ __forceinline__ float log(float x) { return ::logf(x); }
+    static __device__ __forceinline__ float exp(float x) { return ::expf(x); }
+    static __device__ __forceinline__ float pow(float x, float y) { return ::powf(x, y); }
+    static __device__ __forceinline__ float atan(float x) { return ::atanf(x); }
+    static __device__ __forceinline__ float cbrt(float x) { return ::cbrtf(x); }
+    static __device__ __forceinline__ float sqrt(float x) { return ::sqrtf(x); }
+    static __device__ __forceinline__ float fmin(float a, float b) { return ::fminf(a, b); }
+    static __device__ __forceinline__ float fmax(float a, float b) { return ::fmaxf(a, b); }
+    static __device__ __forceinline__ float fabs(float a) { return ::fabsf(a); }
+    static __device__ __forceinline__ float inf() { return __int_as_float(0x7f800000); }
+};
+
+// --------------------------------------------------------- device parameters
+template <class R> struct DevStab {
+    int32_t kind;
+    R c[12];
+};
+
+template <class R> struct DevRough {
+    int32_t kind, wave_kind, visc_kind;
+    R value, g, nu, nuc[4], charnock, umax, c1, c2, smooth, lmax, A, b;
+};
+
+// Flattened nesf_interface_params with the derived thermodynamic constants
+// (thermodynamic_parameters.jl:73-78, 256) evaluated once on the host.
+template <class R> struct DevIface {
+    // thermodynamics
+    R Rd, Rv, eps, einv, cpd, cpv, cpl, cpi, Lv0, Ls0, T0, Ttr, ptr;
+    // similarity theory
+    R vk;
+    int32_t subgrid_kind, form;
+    R beta, min_gust, const_sg, meso_sg;
+    DevStab<R> psi[3];
+    DevRough<R> rough[3];
+    R d0;
+    int32_t stop_kind, maxiter;
+    R tol;
+    int32_t scalar_same;      // temperature and vapour share roughness and psi
+    // interface properties
+    int32_t phase, vel_form, temp_form, has_rad;
+    R x;                      // water mole fraction (1 when `nothing`)
+    R max_dT, k_ice, k_snow, kap_diff, del_diff;
+    R g, h, hbl, off_int, off_ifc;
+    R sigma, alb, emis, Tfw, slope, rho_i, c_i;
+};
+
+// ------------------------------------------------------------- thermodynamics
+// Thermodynamics.jl restatements (saturation_vapor_pressure, air_density, cp_m,
+// latent heats, virtual temperature) with the parameter set of
+// src/Atmospheres/thermodynamic_parameters.jl.
+template <class R>
+__device__ __forceinline__ R esat(const DevIface<R>& P, R T, int phase) {
+    R LH0 = phase == NESF_PHASE_ICE ? P.Ls0 : P.Lv0;
+    R cpc = phase == NESF_PHASE_ICE ? P.cpi : P.cpl;
+    R dcp = P.cpv - cpc;
+    return P.ptr * M<R>::pow(T / P.Ttr, dcp / P.Rv) *
+           M<R>::exp((LH0 - dcp * P.T0) / P.Rv * (R(1) / P.Ttr - R(1) / T));
+}
+
+template <class R> __device__ __forceinline__ R gas_constant_air(const DevIface<R>& P, R q) {
+    return P.Rd * (R(1) + (P.eps - R(1)) * q);
+}
+template <class R> __device__ __forceinline__ R air_density(const DevIface<R>& P, R T, R p, R q) {
+    return p / (gas_constant_air(P, q) * T);
+}
+template <class R> __device__ __forceinline__ R cp_m(const DevIface<R>& P, R q) {
+    return P.cpd + (P.cpv - P.cpd) * q;
+}
+template <class R> __device__ __forceinline__ R latent_heat_vapor(const DevIface<R>& P, R T) {
+    return P.Lv0 + (P.cpv - P.cpl) * (T - P.T0);
+}
+template <class R> __device__ __forceinline__ R latent_heat_sublim(const DevIface<R>& P, R T) {
+    return P.Ls0 + (P.cpv - P.cpi) * (T - P.T0);
+}
+template <class R> __device__ __forceinline__ R virtual_temperature(const DevIface<R>& P, R T, R q) {
+    return gas_constant_air(P, q) / P.Rd * T;
+}
+
+// surface_specific_humidity(::ImpureSaturationSpecificHumidity)
+// (InterfaceComputations/interface_states.jl:55-74)
+template <class R>
+__device__ __forceinline__ R surface_specific_humidity(const DevIface<R>& P, R pa, R Ts) {
+    R pv = P.x * esat(P, Ts, P.phase);
+    pv = M<R>::fmin(pv, R(0.999) * pa);
+    return P.einv * pv / (pa - (R(1) - P.einv) * pv);
+}
+
+// surface_atmosphere_temperature (interface_states.jl:308-317)
+template <class R>
+__device__ __forceinline__ R surface_atmosphere_temperature(const DevIface<R>& P, R Ta, R qa) {
+    R c = cp_m(P, qa);
+    return Ta + P.g * P.h / c;
+}
+
+// -------------------------------------------------------- stability functions
+// similarity_theory_turbulent_fluxes.jl. The reference evaluates both branches
+// and selects with ifelse(zeta < 0, ...); here only the selected branch is
+// evaluated, which gives the same value.
+template <class R>
+__device__ __noinline__ R psi_edson_momentum(const DevStab<R> s, R z) {   // :501-532
+    const R* c = s.c;
+    if (z < R(0)) {
+        R Am = c[5], Bm = c[6], Cm = c[7], Dm = c[8], Em = c[9], Fm = c[10];
+        R zm = z;
+        R f1 = M<R>::sqrt(M<R>::sqrt(R(1) - Am * zm));
+        R psi1 = Bm * M<R>::log((R(1) + f1) / Bm) + M<R>::log((R(1) + f1 * f1) / Bm) - Bm * M<R>::atan(f1) + Cm;
+        R f2 = M<R>::cbrt(R(1) - Dm * zm);
+        R sE = M<R>::sqrt(Em);
+        R psi2 = Em / R(2) * M<R>::log((R(1) + f2 + f2 * f2) / Em) - sE * M<R>::atan((R(1) + R(2) * f2) / sE) + Fm;
+        R f = zm * zm / (R(1) + zm * zm);
+        return (R(1) - f) * psi1 + f * psi2;
+    } else {
+        R zmax = c[0], Ap = c[1], Bp = c[2], Cp = c[3], Dp = c[4];
+        R zp = z;
+        R dz = M<R>::fmin(zmax, Ap * zp);
+        return -Bp * zp - Cp * (zp - Dp) * M<R>::exp(-dz) - Cp * Dp;
+    }
+}
+
+template <class R>
+__device__ __noinline__ R psi_edson_scalar(const DevStab<R> s, R z) {     // :586-618
+    const R* c = s.c;
+    if (z < R(0)) {
+        R Am = c[6], Bm = c[7], Cm = c[8], Dm = c[9], Em = c[10], Fm = c[11];
+        R zm = z;
+        R f1 = M<R>::sqrt(R(1) - Am * zm);
+        R psi1 = Bm * M<R>::log((R(1) + f1) / Bm) + Cm;
+        R f2 = M<R>::cbrt(R(1) - Dm * zm);
+        R sE = M<R>::sqrt(Em);
+        R psi2 = Em / R(2) * M<R>::log((R(1) + f2 + f2 * f2) / Em) - sE * M<R>::atan((R(1) + R(2) * f2) / sE) + Fm;
+        R f = zm * zm / (R(1) + zm * zm);
+        return (R(1) - f) * psi1 + f * psi2;
+    } else {
+        R zmax = c[0], Ap = c[1], Bp = c[2], Cp = c[3], Dp = c[4], Ep = c[5];
+        R zp = z;
+        R dz = M<R>::fmin(zmax, Ap * zp);
+        return -M<R>::pow(R(1) + Bp * zp, Cp) - Bp * (zp - Dp) * M<R>::exp(-dz) - Ep;
+    }
+}
+
+template <class R>
+__device__ __noinline__ R psi_sheba_momentum(R a, R b, R z) {     // :643-657
+    R zp = M<R>::fmax(R(0), z);
+    R x = M<R>::cbrt(R(1) + zp);
+    R B = M<R>::cbrt((R(1) - b) / b);
+    R rt3 = M<R>::sqrt(R(3));
+    R P1 = -R(3) * a * (x - R(1)) / b;
+    R P2 = a * B / (R(2) * b) *
+           (R(2) * M<R>::log((x + B) / (R(1) + B)) - M<R>::log((x * x - B * x + B * B) / (R(1) - B + B * B)) +
+            R(2) * rt3 * (M<R>::atan((R(2) * x - B) / (rt3 * B)) - M<R>::atan((R(2) - B) / (rt3 * B))));
+    return P1 + P2;
+}
+
+template <class R>
+__device__ __noinline__ R psi_sheba_scalar(R a, R b, R c, R z) {  // :665-677
+    R B = M<R>::sqrt(c * c - R(4));
+    R zp = M<R>::fmax(R(0), z);
+    R P1 = -b / R(2) * M<R>::log(R(1) + c * zp + zp * zp);
+    R P2 = (b * c / (R(2) * B) - a / B) *
+           (M<R>::log((R(2) * zp + c - B) / (R(2) * zp + c + B)) - M<R>::log((c - B) / (c + B)));
+    return P1 + P2;
+}
+
+template <class R>
+__device__ __noinline__ R psi_paulson_momentum(R a, R b, R z) {   // :688-699
+    R zm = M<R>::fmin(R(0), z);
+    R x = M<R>::sqrt(M<R>::sqrt(R(1) - a * zm));
+    R P1 = R(2) * M<R>::log((R(1) + x) / R(2));
+    R P2 = M<R>::log((R(1) + x * x) / R(2));
+    R P3 = -R(2) * M<R>::atan(x);
+    return P1 + P2 + P3 + b;
+}
+
+template <class R>
+__device__ __noinline__ R psi_paulson_scalar(R a, R z) {          // :705-710
+    R zm = M<R>::fmin(R(0), z);
+    R x = M<R>::sqrt(M<R>::sqrt(R(1) - a * zm));
+    return R(2) * M<R>::log((R(1) + x * x) / R(2));
+}
+
+template <class R>
+__device__ __forceinline__ R psi_linear(R coef, R zmax, R z) {       // :747-752
+    R zp = M<R>::fmax(R(0), z);
+    return -coef * M<R>::fmin(zp, zmax);
+}
+
+// stability_profile dispatch; SplitStabilityFunction (:720-725) takes the stable
+// branch for z > 0.
+template <class R>
+__device__ __forceinline__ R stability(const DevStab<R>& s, R z) {
+    const R* c = s.c;
+    switch (s.kind) {
+    case NESF_PSI_EDSON_MOMENTUM: return psi_edson_momentum(s, z);
+    case NESF_PSI_EDSON_SCALAR: return psi_edson_scalar(s, z);
+    case NESF_PSI_SHEBA_PAULSON_MOMENTUM:
+        return z > R(0) ? psi_sheba_momentum(c[0], c[1], z) : psi_paulson_momentum(c[2], c[3], z);
+    case NESF_PSI_SHEBA_PAULSON_SCALAR:
+        return z > R(0) ? psi_sheba_scalar(c[0], c[1], c[2], z) : psi_paulson_scalar(c[3], z);
+    case NESF_PSI_LINEAR_PAULSON_MOMENTUM:
+        return z > R(0) ? psi_linear(c[0], c[1], z) : psi_paulson_momentum(c[2], c[3], z);
+    case NESF_PSI_LINEAR_PAULSON_SCALAR:
+        return z > R(0) ? psi_linear(c[0], c[1], z) : psi_paulson_scalar(c[2], z);
+    default: return R(0);
+    }
+}
+
+// similarity_profile (:242-253)
+template <class R>
+__device__ __forceinline__ R similarity_profile(int form, const DevStab<R>& psi, R h, R l, R L) {
+    R zeta = h / L;
+    R ph = stability(psi, zeta);
+    if (form == NESF_PROFILE_COARE) return M<R>::log(h / l) - ph;
+    R pl = stability(psi, l / L);
+    return M<R>::log(h / l) - ph + pl;
+}
+
+// ---------------------------------------------------------- roughness lengths
+// roughness_lengths.jl:182-189 (viscosity), 197-210 (momentum), 231-246 (scalar)
+template <class R>
+__device__ __forceinline__ R air_viscosity(const DevRough<R>& r, R T) {
+    if (r.visc_kind == 0) return r.nu;
+    R Tc = T - R(273.15);
+    return r.nuc[0] + r.nuc[1] * Tc + r.nuc[2] * Tc * Tc + r.nuc[3] * (Tc * Tc * Tc);
+}
+
+template <class R>
+__device__ __forceinline__ R momentum_roughness(const DevRough<R>& r, R us, R U, R nu) {
+    if (r.kind == NESF_ROUGHNESS_CONSTANT) return r.value;
+    R Cg = r.charnock;
+    if (r.wave_kind == 1) Cg = M<R>::fmax(R(0), r.c1 * M<R>::fmin(U, r.umax) + r.c2);
+    R lW = Cg * (us * us) / r.g;
+    R lR = r.smooth == R(0) ? R(0) : r.smooth * nu / us;
+    return M<R>::fmin(lW + lR, r.lmax);
+}
+
+template <class R>
+__device__ __forceinline__ R scalar_roughness(const DevRough<R>& r, R lu, R us, R nu) {
+    if (r.kind == NESF_ROUGHNESS_CONSTANT) return r.value;
+    R Rs = lu * us / nu;
+    R ls = Rs == R(0) ? R(0) : r.A / M<R>::pow(Rs, r.b);
+    return M<R>::fmin(ls, r.lmax);
+}
+
+// vsgs2 (similarity_theory_turbulent_fluxes.jl:88-98)
+template <class R>
+__device__ __forceinline__ R vsgs2(const DevIface<R>& P, R us, R bs) {
+    R conv = R(0);
+    if (P.subgrid_kind == NESF_SUBGRID_CONSTANT) {
+        conv = P.const_sg * P.const_sg;
+    } else if (P.subgrid_kind == NESF_SUBGRID_CONVECTIVE) {
+        R Jb = -us * bs;
+        R UG = M<R>::fmax(P.min_gust, P.beta * M<R>::cbrt(M<R>::fmax(R(0), Jb) * P.hbl));
+        conv = UG * UG;
+    }
+    return conv + P.meso_sg * P.meso_sg;
+}
+
+// ------------------------------------------------------------ the fixed point
+// Per-cell state the iteration needs and that does not change between
+// iterations (for BulkTemperature everything that depends on T_s).
+template <class R> struct CellConst {
+    R ua, va, Ta, pa, qa;        // atmosphere
+    R ui, vi;                    // interface velocities
+    R Ti, Si;                    // interior temperature (K) and salinity
+    R hi, hs, hc;                // ice state (conductive skin)
+    R sw, lw, kappa;             // radiation, interior diffusivity (<0: none)
+    R du, dv, dU2;               // velocity difference and its square norm
+    R tha;                       // surface_atmosphere_temperature
+    R rho_a, cp_a, L_s;          // air density, cp_m, latent_heat_sublim (skin only)
+};
+
+// Quantities that depend on the interface temperature.
+template <class R> struct SurfaceConst {
+    R Ts, qs, dth, dq;
+    R gTv, A1, A2;   // b* = gTv * (theta* A1 + A2 q*)   (buoyancy_scale, :417-425)
+    R nu_u, nu_t, nu_q;
+};
+
+template <class R>
+__device__ __forceinline__ void surface_const(const DevIface<R>& P, const CellConst<R>& c, R Ts, R qs,
+                                              SurfaceConst<R>& s) {
+    s.Ts = Ts;
+    s.qs = qs;
+    s.dq = c.qa - qs;
+    s.dth = c.tha - Ts;
+    R Tv = virtual_temperature(P, Ts, qs);
+    R delta = P.eps - R(1);
+    s.gTv = P.g / Tv;
+    s.A1 = R(1) + delta * qs;
+    s.A2 = delta * Tv;
+    s.nu_u = air_viscosity(P.rough[0], Ts);
+    s.nu_t = air_viscosity(P.rough[1], Ts);
+    s.nu_q = air_viscosity(P.rough[2], Ts);
+}
+
+// iterate_interface_fluxes(::SimilarityTheoryFluxes) (:315-385)
+template <class R>
+__device__ __forceinline__ void iterate_fluxes(const DevIface<R>& P, const CellConst<R>& c, const SurfaceConst<R>& s,
+                                               R us, R ts, R qst, R& us_n, R& ts_n, R& qs_n) {
+    R bs = s.gTv * (ts * s.A1 + s.A2 * qst);
+    R Usg2 = vsgs2(P, us, bs);
+    R U = M<R>::sqrt(c.dU2 + Usg2);
+    R lu = momentum_roughness(P.rough[0], us, U, s.nu_u);
+    R lt = scalar_roughness(P.rough[1], lu, us, s.nu_t);
+    R h = M<R>::fmax(P.h - P.d0, R(2) * lu);
+    R L = bs == R(0) ? M<R>::inf() : us * us / (P.vk * bs);
+    R chiu = P.vk / similarity_profile(P.form, P.psi[0], h, lu, L);
+    R chit = P.vk / similarity_profile(P.form, P.psi[1], h, lt, L);
+    R chiq;
+    if (P.scalar_same) {
+        chiq = chit;
+    } else {
+        R lq = scalar_roughness(P.rough[2], lu, us, s.nu_q);
+        chiq = P.vk / similarity_profile(P.form, P.psi[2], h, lq, L);
+    }
+    us_n = chiu * U;
+    ts_n = chit * s.dth;
+    qs_n = chiq * s.dq;
+}
+
+template <class R> __device__ __forceinline__ R clampr(R x, R lo, R hi) {
+    return M<R>::fmin(M<R>::fmax(x, lo), hi);
+}
+
+// compute_interface_temperature(::SkinTemperature) (interface_states.jl:526-577) with
+// flux_balance_temperature (434-457 diffusive, 468-524 conductive ice/snow).
+template <class R>
+__device__ __forceinline__ R skin_temperature(const DevIface<R>& P, const CellConst<R>& c, R Tm1, R us, R ts, R qst) {
+    R sigma = P.has_rad ? P.sigma : R(0);
+    R eps = P.has_rad ? P.emis : R(0);
+    R alb = P.has_rad ? P.alb : R(0);
+    R SW = P.has_rad ? c.sw : R(0);
+    R LW = P.has_rad ? c.lw : R(0);
+    R T2 = Tm1 * Tm1;
+    R Iup = sigma * eps * (T2 * T2);
+    R Qd = -(R(1) - alb) * SW - eps * LW;
+    R QT = -c.rho_a * c.cp_a * us * ts;
+    R Qv = -c.rho_a * c.L_s * us * qst;
+    R Tat = c.tha;
+    if (P.temp_form == NESF_SKIN_TEMPERATURE_DIFFUSIVE) {
+        R kap = c.kappa >= R(0) ? M<R>::fmax(c.kappa, P.kap_diff) : P.kap_diff;
+        R del = P.del_diff;
+        R Qa = Qv + Iup + Qd;
+        R lam = R(1) / (P.rho_i * P.c_i);
+        R JT = Qa * lam;
+        R dT = Tat - Tm1;
+        R OmT = QT * lam;
+        R D = kap * dT - OmT * del;
+        R Tst = (c.Ti * kap * dT - (JT * dT + OmT * Tat) * del) / D;
+        Tst = D == R(0) ? Tm1 : Tst;
+        return c.Ti + clampr(Tst - c.Ti, -P.max_dT, P.max_dT);
+    }
+    R Rth = P.k_snow > R(0) ? c.hs / P.k_snow + c.hi / P.k_ice : c.hi / P.k_ice;
+    R Tb = P.Tfw - P.slope * c.Si;
+    Tb = Tb + P.off_ifc;
+    R dT = Tat - Tm1;
+    R Qa = Qv + Iup + Qd;
+    R Om = dT == R(0) ? R(0) : QT / dT;
+    R beta = R(4) * Iup / Tm1;
+    R D = R(1) + beta * Rth - Om * Rth;
+    R Tst = (Tb + beta * Rth * Tm1 - Om * Rth * Tat - Qa * Rth) / D;
+    Tst = D == R(0) ? Tm1 : Tst;
+    Tst = isnan(Tst) ? Tm1 : Tst;
+    R Tp = Tm1 + clampr(Tst - Tm1, -P.max_dT, P.max_dT);
+    R Tm = P.Tfw + P.off_ifc;
+    Tp = M<R>::fmin(Tp, Tm);
+    return c.hi >= c.hc ? Tp : Tb;
+}
+
+// One iterate_interface_state (compute_interface_state.jl:69-122). For the bulk
+// formulation `s` is fixed; for skin formulations it is rebuilt from the new T_s.
+template <class R, bool SKIN>
+__device__ __forceinline__ void iterate_state(const DevIface<R>& P, const CellConst<R>& c, SurfaceConst<R>& s,
+                                              R& us, R& ts, R& qst) {
+    if (SKIN) {
+        R Ts = skin_temperature(P, c, s.Ts, us, ts, qst);
+        R qs = surface_specific_humidity(P, c.pa, Ts);
+        surface_const(P, c, Ts, qs, s);
+    }
+    R a, b, d;
+    iterate_fluxes(P, c, s, us, ts, qst, a, b, d);
+    us = a;
+    ts = b;
+    qst = d;
+}
+
+// compute_interface_state with ConvergenceStopCriteria / FixedIterations
+// (compute_interface_state.jl:10-24, 31-58). Returns the iteration count; the
+// last drift is left in `drift`.
+template <class R, bool SKIN>
+__device__ __forceinline__ int fixed_point(const DevIface<R>& P, const CellConst<R>& c, SurfaceConst<R>& s,
+                                           R& us, R& ts, R& qst, int maxiter, R& drift) {
+    int it = 0;
+    drift = M<R>::inf();
+    if (P.stop_kind == NESF_STOP_FIXED_ITERATIONS) {
+        for (; it < maxiter; it++) iterate_state<R, SKIN>(P, c, s, us, ts, qst);
+        return it;
+    }
+    do {
+        R u0 = us, t0 = ts, q0 = qst;
+        iterate_state<R, SKIN>(P, c, s, us, ts, qst);
+        it++;
+        drift = M<R>::fabs(us - u0) + M<R>::fabs(ts - t0) + M<R>::fabs(qst - q0);
+    } while (!(drift < P.tol) && it < maxiter);
+    return it;
+}
+
+}  // namespace nesf

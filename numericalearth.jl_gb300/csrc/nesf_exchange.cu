@@ -1,0 +1,319 @@
+// nesf_exchange.cu -- the streaming kernels of the interface-flux step:
+//   sea-ice-ocean fluxes  (InterfaceComputations/sea_ice_ocean_fluxes.jl:106-226,
+//                          sea_ice_ocean_heat_flux_formulations.jl:176-313)
+//   fractional indices    (Atmospheres/prescribed_atmosphere_regridder.jl:51-71)
+//   atmosphere + radiation interpolation (Atmospheres/interpolate_atmospheric_state.jl:91-137,
+//                          Radiations/interpolate_radiation_state.jl:43-69)
+//   net ocean / sea-ice flux assembly (Oceans/assemble_net_ocean_fluxes.jl:74-153,
+//                          SeaIces/assemble_net_sea_ice_fluxes.jl:42-81)
+//   radiative add-ons     (Radiations/apply_air_sea_radiative_fluxes.jl:62-111,
+//                          Radiations/apply_air_sea_ice_radiative_fluxes.jl:55-90)
+// All are HBM-bound: one thread per cell, i fastest, read-once/write-once.
+#include "nesf_exchange.cuh"
+
+namespace nesf {
+
+// ------------------------------------------------------------- sea ice - ocean
+template <class S>
+__global__ void __launch_bounds__(256) io_kernel(IOArgs<S> a, nesf_io_params p) {
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = (int64_t)a.L.nx * a.L.ny;
+    if (r >= n) return;
+    int i = 1 + (int)(r % a.L.nx), j = 1 + (int)(r / a.L.nx);
+    int64_t k2 = a.L.at(i, j);
+    double rho = p.ocean_reference_density, cpo = p.ocean_heat_capacity;
+    // Part 1: frazil over the column, top level first (sea_ice_ocean_fluxes.jl:153-181)
+    double dQ = 0.0;
+    for (int kk = p.nz; kk >= 1; kk--) {
+        int64_t k3 = k2 + (int64_t)(kk - 1) * p.stride_k;
+        double dz = a.dz[kk - 1];
+        double Tk = (double)a.T3[k3], Sk = (double)a.S3[k3];
+        double Tm = p.liquidus_freshwater_melting_temperature - p.liquidus_slope * Sk;
+        bool freezing = Tk < Tm;
+        double dE = (freezing ? 1.0 : 0.0) * rho * cpo * (Tm - Tk);
+        if (freezing) a.T3[k3] = (S)Tm;
+        dQ -= dE * dz / p.dt;
+    }
+    st(a.frazil, k2, dQ);
+    int64_t kN = k2 + (int64_t)(p.nz - 1) * p.stride_k;
+    double TN = (double)a.T3[kN], SN = (double)a.S3[kN];
+    double Si = ld(a.Si, k2), h = ld(a.hi, k2), aleph = ld(a.aleph, k2), hc = ld(a.hc, k2);
+    double Tsi = (p.conductive && a.Tint) ? ld(a.Tint, k2) : 0.0;
+    double Qio, Tb, Sb;
+    if (p.formulation == 1) {
+        double Tm = p.liquidus_freshwater_melting_temperature - p.liquidus_slope * SN;
+        Qio = rho * cpo * p.heat_transfer_coefficient * p.friction_velocity * (TN - Tm) * aleph;
+        Tb = Tm;
+        Sb = SN;
+    } else {
+        // solve_interface_conditions (sea_ice_ocean_heat_flux_formulations.jl:280-313)
+        double E = p.reference_latent_heat;
+        double kap = 0.0, Ti = 0.0;
+        if (p.conductive) {
+            kap = h >= hc ? p.ice_conductivity / (h * E) : 0.0;
+            Ti = Tsi;
+        }
+        double l1 = -p.liquidus_slope, l2 = p.liquidus_freshwater_melting_temperature;
+        double us = p.friction_velocity;
+        double eta = rho * cpo * p.heat_transfer_coefficient * us / E;
+        double gam = rho * p.salt_transfer_coefficient * us;
+        double th = eta + kap;
+        double qa = th * l1;
+        double qb = -gam - eta * TN - kap * Ti + th * (l2 - l1 * Si);
+        double qc = gam * SN + (eta * TN + kap * Ti - th * l2) * Si;
+        double xi = qa == 0 ? 0.0 : 1 / (2 * qa);
+        double D = fmax(qb * qb - 4 * qa * qc, 0.0);
+        double Ss = (-qb - sqrt(D)) * xi;
+        Ss = Ss < 0 ? (-qb + sqrt(D)) * xi : Ss;
+        double Ts = l2 - p.liquidus_slope * Ss;
+        double q = eta * (TN - Ts) + kap * (Ti - Ts);
+        Qio = E * q * aleph;
+        Tb = Ts;
+        Sb = Ss;
+        st(a.Tb, k2, Tb);
+        st(a.Sb, k2, Sb);
+    }
+    st(a.Qio, k2, Qio);
+    double Ei = ldz(a.Ei, k2), Es = ldz(a.Es, k2);
+    st(a.Jw, k2, -(Ei + Es) / rho);
+    st(a.Js, k2, Ei * Si / rho);
+}
+
+// ---------------------------------------------------------- fractional indices
+__global__ void frac_kernel(Layout2 L, nesf_exchange_coords c, nesf_atmos_grid ag, double* fi, double* fj) {
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int wx = L.nx + 2 * L.hx, wy = L.ny + 2 * L.hy;
+    if (r >= (int64_t)wx * wy) return;
+    int i = 1 - L.hx + (int)(r % wx), j = 1 - L.hy + (int)(r / wx);
+    int64_t k = L.at(i, j);
+    double lon = c.lon0 + (i - 1) * c.dlon;
+    double lat = c.lat0 + (j - 1) * c.dlat;
+    fi[k] = (lon - ag.lon0) / ag.dlon + 1;
+    fj[k] = (lat - ag.lat0) / ag.dlat + 1;
+}
+
+// ------------------------------------------------------------- interpolation
+template <class S>
+__device__ __forceinline__ double interp_one(const nesf_atmos_grid& ag, const S* __restrict__ d, int i0, int i1,
+                                             int j0, int j1, double xi, double eta, double tn) {
+    double v[2];
+#pragma unroll
+    for (int n = 0; n < 2; n++) {
+        const S* b = d + (int64_t)n * ag.stride_t;
+        auto at = [&](int ii, int jj) {
+            return (double)__ldg(b + (int64_t)(ii - 1 + ag.hx) + (int64_t)(jj - 1 + ag.hy) * ag.stride_j);
+        };
+        v[n] = (1 - xi) * (1 - eta) * at(i0, j0) + (1 - xi) * eta * at(i0, j1) + xi * (1 - eta) * at(i1, j0) +
+               xi * eta * at(i1, j1);
+    }
+    return v[1] * tn + v[0] * (1 - tn);
+}
+
+__device__ __forceinline__ int wrap_i(int i, int n) {
+    int m = (i - 1) % n;
+    if (m < 0) m += n;
+    return m + 1;
+}
+__device__ __forceinline__ int clamp_j(int j, int n) { return j < 1 ? 1 : (j > n ? n : j); }
+
+template <class S>
+__global__ void __launch_bounds__(256) interp_kernel(InterpArgs<S> a) {
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int nxr = a.L.nx + 2;
+    if (r >= (int64_t)nxr * (a.L.ny + 2)) return;
+    int i = (int)(r % nxr), j = (int)(r / nxr);
+    int64_t k = a.L.at(i, j);
+    double fi, fj;
+    if (a.frac_i) {
+        fi = a.frac_i[k];
+        fj = a.frac_j[k];
+    } else {
+        double lon = a.coords.lon0 + (i - 1) * a.coords.dlon;
+        double lat = a.coords.lat0 + (j - 1) * a.coords.dlat;
+        fi = (lon - a.atmos.lon0) / a.atmos.dlon + 1;
+        fj = (lat - a.atmos.lat0) / a.atmos.dlat + 1;
+    }
+    double fli = floor(fi), flj = floor(fj);
+    int im = (int)fli, jm = (int)flj;
+    double xi = fi - fli, eta = fj - flj;
+    int i0 = wrap_i(im, a.atmos.nx), i1 = wrap_i(im + 1, a.atmos.nx);
+    int j0 = clamp_j(jm, a.atmos.ny), j1 = clamp_j(jm + 1, a.atmos.ny);
+#pragma unroll
+    for (int n = 0; n < 9; n++) {
+        if (!a.dst[n]) continue;
+        double v = a.src[n] ? interp_one(a.atmos, a.src[n], i0, i1, j0, j1, xi, eta, a.tn) : 0.0;
+        a.dst[n][k] = (S)v;
+    }
+}
+
+// ------------------------------------------------------------------ assembly
+template <class S>
+__global__ void __launch_bounds__(256) assemble_ocean_kernel(AsmArgs<S> a, nesf_assembly_params p) {
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= (int64_t)a.L.nx * a.L.ny) return;
+    int i = 1 + (int)(r % a.L.nx), j = 1 + (int)(r / a.L.nx);
+    int64_t k = a.L.at(i, j), kw = k - 1, ks = k - a.L.sj;
+    double rinv = 1 / p.ocean_reference_density;
+    double cinv = 1 / p.ocean_heat_capacity;
+    double al = ldz(a.f.aleph, k);
+    double To = ld(a.f.To, k);
+    double Jr = ldz(a.f.rain, k), Js = ldz(a.f.snow, k), Ps = ldz(a.f.isnow, k), Jl = ldz(a.f.land_fw, k);
+    double QT = ld(a.f.ao_QT, k), Qv = ld(a.f.ao_Qv, k), Jv = ld(a.f.ao_Jv, k);
+    double SQao = (QT + Qv) * (1 - al);
+    double SFao = -(Jr + Jl + Js - Ps) * rinv + (1 - al) * Jv * rinv;
+    double Jwao = -SFao;
+    bool inactive = a.f.inactive ? a.f.inactive[k] != 0 : false;
+    double Qin = ldz(a.f.io_Q, k), Jsio = ldz(a.f.io_Js, k), Jwio = ldz(a.f.io_Jw, k);
+    double JTao = SQao * rinv * cinv;
+    double JTio = Qin * rinv * cinv;
+    double aw = ldz(a.f.aleph, kw), as = ldz(a.f.aleph, ks);
+    double tcx = rinv * (1 - al) * ld(a.f.ao_tx, k);
+    double tcxw = rinv * (1 - aw) * ld(a.f.ao_tx, kw);
+    double tcy = rinv * (1 - al) * ld(a.f.ao_ty, k);
+    double tcys = rinv * (1 - as) * ld(a.f.ao_ty, ks);
+    double txao = (tcxw + tcx) / 2;
+    double tyao = (tcys + tcy) / 2;
+    double txio = ldz(a.f.io_tx, k) * rinv * ((aw + al) / 2);
+    double tyio = ldz(a.f.io_ty, k) * rinv * ((as + al) / 2);
+    st(a.f.o_u, k, inactive ? 0.0 : txao + txio);
+    st(a.f.o_v, k, inactive ? 0.0 : tyao + tyio);
+    double JT = inactive ? 0.0 : JTao + JTio;
+    if (a.with_radiation) {
+        // apply_air_sea_radiative_fluxes fused: J_T += radiative part
+        double Ts = ld(a.f.ao_Ts, k) + p.interface_temperature_offset;
+        double T2 = Ts * Ts;
+        double Iup = p.stefan_boltzmann_constant * p.ocean_emissivity * (T2 * T2);
+        double Ia = -p.ocean_emissivity * ld(a.f.lw, k);
+        double It = -(1 - p.ocean_albedo) * ld(a.f.sw, k);
+        Ia *= (1 - al);
+        It *= (1 - al);
+        double Iup_o = Iup * (1 - al);
+        double SQ = Iup_o + Ia + It;
+        double JTr = SQ * rinv * cinv;
+        JT += inactive ? 0.0 : JTr;
+        st(a.f.o_up_lw, k, Iup);
+        st(a.f.o_dn_lw, k, -Ia);
+        st(a.f.o_dn_sw, k, -It);
+    }
+    st(a.f.o_T, k, JT);
+    st(a.f.o_S, k, inactive ? 0.0 : Jsio);
+    st(a.f.o_eta, k, inactive ? 0.0 : Jwao + Jwio);
+    st(a.f.o_H, k, inactive ? 0.0 : To * Jwao);
+}
+
+template <class S>
+__global__ void __launch_bounds__(256) assemble_ice_kernel(AsmArgs<S> a, nesf_assembly_params p) {
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= (int64_t)a.L.nx * a.L.ny) return;
+    int i = 1 + (int)(r % a.L.nx), j = 1 + (int)(r / a.L.nx);
+    int64_t k = a.L.at(i, j), kw = k - 1, ks = k - a.L.sj;
+    double al = ld(a.f.aleph, k);
+    double QT = ld(a.f.ai_QT, k), Qv = ld(a.f.ai_Qv, k);
+    double Qf = ldz(a.f.io_Qf, k), Qi = ldz(a.f.io_Q, k);
+    double Js = ldz(a.f.snow, k);
+    double SQt = (QT + Qv) * al;
+    double SQb = Qf + Qi;
+    bool inactive = a.f.inactive ? a.f.inactive[k] != 0 : false;
+    double top = inactive ? 0.0 : SQt;
+    if (a.with_radiation) {
+        double Ts = ld(a.f.ai_Ts, k) + p.interface_temperature_offset;
+        double T2 = Ts * Ts;
+        double Iup = p.stefan_boltzmann_constant * p.ice_emissivity * (T2 * T2);
+        double Ia = -p.ice_emissivity * ld(a.f.lw, k);
+        double It = -(1 - p.ice_albedo) * ld(a.f.sw, k);
+        double SQ = (Iup + Ia + It) * al;
+        top += inactive ? 0.0 : SQ;
+        st(a.f.i_up_lw, k, Iup);
+        st(a.f.i_dn_lw, k, -Ia);
+        st(a.f.i_dn_sw, k, -It);
+    }
+    st(a.f.i_top, k, top);
+    st(a.f.i_snow, k, inactive ? 0.0 : Js);
+    st(a.f.i_u, k, inactive ? 0.0 : (ld(a.f.ai_tx, kw) + ld(a.f.ai_tx, k)) / 2);
+    st(a.f.i_v, k, inactive ? 0.0 : (ld(a.f.ai_ty, ks) + ld(a.f.ai_ty, k)) / 2);
+    st(a.f.i_bottom, k, inactive ? 0.0 : SQb);
+}
+
+// Radiation alone, added in place to an already assembled J_T / top heat flux.
+template <class S, bool ICE>
+__global__ void __launch_bounds__(256) radiation_kernel(AsmArgs<S> a, nesf_assembly_params p) {
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= (int64_t)a.L.nx * a.L.ny) return;
+    int i = 1 + (int)(r % a.L.nx), j = 1 + (int)(r / a.L.nx);
+    int64_t k = a.L.at(i, j);
+    bool inactive = a.f.inactive ? a.f.inactive[k] != 0 : false;
+    if (!ICE) {
+        double rinv = 1 / p.ocean_reference_density, cinv = 1 / p.ocean_heat_capacity;
+        double al = ldz(a.f.aleph, k);
+        double Ts = ld(a.f.ao_Ts, k) + p.interface_temperature_offset;
+        double T2 = Ts * Ts;
+        double Iup = p.stefan_boltzmann_constant * p.ocean_emissivity * (T2 * T2);
+        double Ia = -p.ocean_emissivity * ld(a.f.lw, k);
+        double It = -(1 - p.ocean_albedo) * ld(a.f.sw, k);
+        Ia *= (1 - al);
+        It *= (1 - al);
+        double Iup_o = Iup * (1 - al);
+        double SQ = Iup_o + Ia + It;
+        double JT = SQ * rinv * cinv;
+        a.f.o_T[k] = (S)((double)a.f.o_T[k] + (inactive ? 0.0 : JT));
+        st(a.f.o_up_lw, k, Iup);
+        st(a.f.o_dn_lw, k, -Ia);
+        st(a.f.o_dn_sw, k, -It);
+    } else {
+        double al = ld(a.f.aleph, k);
+        double Ts = ld(a.f.ai_Ts, k) + p.interface_temperature_offset;
+        double T2 = Ts * Ts;
+        double Iup = p.stefan_boltzmann_constant * p.ice_emissivity * (T2 * T2);
+        double Ia = -p.ice_emissivity * ld(a.f.lw, k);
+        double It = -(1 - p.ice_albedo) * ld(a.f.sw, k);
+        double SQ = (Iup + Ia + It) * al;
+        a.f.i_top[k] = (S)((double)a.f.i_top[k] + (inactive ? 0.0 : SQ));
+        st(a.f.i_up_lw, k, Iup);
+        st(a.f.i_dn_lw, k, -Ia);
+        st(a.f.i_dn_sw, k, -It);
+    }
+}
+
+// ------------------------------------------------------------------ launchers
+static inline unsigned blocks_for(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
+
+template <class S>
+cudaError_t launch_io(const IOArgs<S>& a, const nesf_io_params& p, cudaStream_t s) {
+    int64_t n = (int64_t)a.L.nx * a.L.ny;
+    io_kernel<S><<<blocks_for(n, 256), 256, 0, s>>>(a, p);
+    return cudaGetLastError();
+}
+template cudaError_t launch_io<double>(const IOArgs<double>&, const nesf_io_params&, cudaStream_t);
+template cudaError_t launch_io<float>(const IOArgs<float>&, const nesf_io_params&, cudaStream_t);
+
+cudaError_t launch_frac(const Layout2& L, const nesf_exchange_coords& c, const nesf_atmos_grid& ag, double* fi,
+                        double* fj, cudaStream_t s) {
+    int64_t n = (int64_t)(L.nx + 2 * L.hx) * (L.ny + 2 * L.hy);
+    frac_kernel<<<blocks_for(n, 256), 256, 0, s>>>(L, c, ag, fi, fj);
+    return cudaGetLastError();
+}
+
+template <class S>
+cudaError_t launch_interp(const InterpArgs<S>& a, cudaStream_t s) {
+    int64_t n = (int64_t)(a.L.nx + 2) * (a.L.ny + 2);
+    interp_kernel<S><<<blocks_for(n, 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+template cudaError_t launch_interp<double>(const InterpArgs<double>&, cudaStream_t);
+template cudaError_t launch_interp<float>(const InterpArgs<float>&, cudaStream_t);
+
+template <class S>
+cudaError_t launch_assemble(const AsmArgs<S>& a, const nesf_assembly_params& p, int which, cudaStream_t s) {
+    int64_t n = (int64_t)a.L.nx * a.L.ny;
+    switch (which) {
+    case 0: assemble_ocean_kernel<S><<<blocks_for(n, 256), 256, 0, s>>>(a, p); break;
+    case 1: assemble_ice_kernel<S><<<blocks_for(n, 256), 256, 0, s>>>(a, p); break;
+    case 2: radiation_kernel<S, false><<<blocks_for(n, 256), 256, 0, s>>>(a, p); break;
+    default: radiation_kernel<S, true><<<blocks_for(n, 256), 256, 0, s>>>(a, p); break;
+    }
+    return cudaGetLastError();
+}
+template cudaError_t launch_assemble<double>(const AsmArgs<double>&, const nesf_assembly_params&, int, cudaStream_t);
+template cudaError_t launch_assemble<float>(const AsmArgs<float>&, const nesf_assembly_params&, int, cudaStream_t);
+
+}  // namespace nesf

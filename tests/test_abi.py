@@ -1,0 +1,80 @@
+"""libnesf.so loads without a GPU, exports every entry point of include/nesf.h,
+and its struct layouts agree with the Python bindings."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from nesf import _abi as A
+from nesf import _lib
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "nesf.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(nesf_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_entry_point():
+    lib = C.CDLL(_lib.LIB_PATH if os.path.exists(_lib.LIB_PATH) else _lib.load()._name)
+    names = declared_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    # and the Python binding covers them all
+    assert set(names) <= set(_lib.SIGNATURES), set(names) - set(_lib.SIGNATURES)
+
+
+def test_struct_sizes_match_bindings():
+    lib = _lib.load()
+    n = len(A.STRUCTS_IN_SIZE_ORDER)
+    sizes = (C.c_int64 * n)()
+    m = lib.nesf_struct_sizes(sizes, n)
+    assert m == n
+    for k, cls in enumerate(A.STRUCTS_IN_SIZE_ORDER):
+        assert sizes[k] == C.sizeof(cls), cls.__name__
+
+
+def test_defaults_match_reference_constructors():
+    """The library's defaults equal the Python mirror of the reference constructors."""
+    from nesf import params as P
+    lib = _lib.load()
+    ao = A.InterfaceParams()
+    lib.nesf_default_ao_params(C.byref(ao))
+    mine = P.atmosphere_ocean_interface_spec().to_c()
+    assert bytes(ao) == bytes(mine)
+    ai = A.InterfaceParams()
+    lib.nesf_default_ai_params(C.byref(ai))
+    mine = P.atmosphere_sea_ice_interface_spec().to_c()
+    assert bytes(ai) == bytes(mine)
+    io = A.IOParams()
+    lib.nesf_default_io_params(C.byref(io))
+    assert bytes(io) == bytes(P.SeaIceOceanSpec().to_c())
+    ap = A.AssemblyParams()
+    lib.nesf_default_assembly_params(C.byref(ap))
+    assert bytes(ap) == bytes(P.AssemblySpec().to_c())
+
+
+def test_argument_errors_without_gpu():
+    """Bad arguments are rejected on the host before any device work."""
+    lib = _lib.load()
+    p = A.InterfaceParams()
+    lib.nesf_default_ao_params(C.byref(p))
+    f = A.AOFields()
+    f.grid = A.Grid(10, 10, 1, 1, 12)     # halo 1 is too small for the face averages
+    f.dtype = A.NESF_F64
+    code = lib.nesf_compute_atmosphere_ocean_fluxes(None, C.byref(p), C.byref(f), None, None, None)
+    assert code == A.NESF_ERR_ARG
+    assert b"halo" in lib.nesf_last_error()
+    f.grid = A.Grid(10, 10, 2, 2, 14)
+    code = lib.nesf_compute_atmosphere_ocean_fluxes(None, C.byref(p), C.byref(f), None, None, None)
+    assert code == A.NESF_ERR_ARG and b"u_atm" in lib.nesf_last_error()
+    p.fluxes.maxiter = -1
+    code = lib.nesf_compute_atmosphere_ocean_fluxes(None, C.byref(p), C.byref(f), None, None, None)
+    assert code == A.NESF_ERR_ARG and b"maxiter" in lib.nesf_last_error()
+    assert lib.nesf_abi_version() == 1
+    with pytest.raises(_lib.NesfError):
+        _lib.check(A.NESF_ERR_ARG)

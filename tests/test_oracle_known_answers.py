@@ -1,0 +1,200 @@
+"""The CPU oracle against the known answers the reference's own tests hold.
+
+test_surface_fluxes.jl:81-110      zero fluxes when dU = dtheta = dq = 0
+test_surface_fluxes.jl:148-211     neutral log-law closed form
+test_subgrid_velocity_corrections.jl:17-42  ConvectiveGustiness bit identity
+test_coefficient_based_fluxes.jl:39-57      linear / Large-Yeager stability values
+test_sea_ice_ocean_heat_fluxes.jl:48-178    three-equation interface properties
+plus e_sat(T_triple) = p_triple (docs/src/interface_fluxes.md:86-97).
+"""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+
+from nesf import _abi as A
+from nesf import params as P
+from nesf import synthetic as syn
+
+
+def one_cell(**values):
+    """A 1x1 exchange grid (halo 2) filled with constant values."""
+    L = syn.Layout(1, 1, 2, 2)
+    arrs = {k: np.full(L.shape, float(v)) for k, v in values.items()}
+    return L, arrs
+
+
+def test_esat_triple_point(oracle):
+    th = P.AtmosphereThermodynamicsParameters().to_c()
+    lib = oracle.load()
+    for phase in (A.PHASE_LIQUID, A.PHASE_ICE):
+        assert lib.oracle_saturation_vapor_pressure(C.byref(th), 273.16, phase) == 611.657
+
+
+@pytest.mark.parametrize("u,v", [(3.0, -4.0), (0.0, 7.5)])
+def test_zero_fluxes(oracle, u, v):
+    """dU = 0, dtheta = 0 (lapse-corrected) and q_s = q_a give fluxes below eps(Float32)."""
+    spec = P.atmosphere_ocean_interface_spec()
+    th = spec.thermodynamics_parameters
+    Ta, qa, pa = 15 + 273.15, 0.003, 101325.0
+    cp = th.cp_d + (th.water_vapor_heat_capacity - th.cp_d) * qa
+    To = Ta - 273.15 + spec.surface_layer_height / cp * spec.gravitational_acceleration
+    # the reference mocks q_s = q_a (FixedSpecificHumidity); here the water mole fraction
+    # is chosen so that the impure saturation humidity at T_o equals q_a
+    einv = 1 / th.Rv_over_Rd
+    pv = qa * pa / (einv + (1 - einv) * qa)
+    es = syn.esat_liquid(np.float64(To + 273.15), th)
+    spec.specific_humidity = P.ImpureSaturationSpecificHumidity("liquid", float(pv / es))
+    L, arrs = one_cell(u_atm=u, v_atm=v, T_atm=Ta, p_atm=pa, q_atm=qa, u_oc=u, v_oc=v, T_oc=To, S_oc=35.0)
+    out = oracle.ao_fluxes(spec.to_c(), L, arrs)
+    eps32 = np.finfo(np.float32).eps
+    for k in ("x_momentum", "y_momentum", "sensible_heat", "latent_heat", "water_vapor"):
+        assert abs(L.interior(out[k])[0, 0]) < eps32, k
+
+
+def test_neutral_log_law(oracle):
+    """psi = 0, constant roughness 1e-4, no gustiness: u* = k dU / log(h/l) etc."""
+    ell = 1e-4
+    flux = P.SimilarityTheoryFluxes(momentum_roughness_length=ell, temperature_roughness_length=ell,
+                                    water_vapor_roughness_length=ell, subgrid_velocities=None,
+                                    stability_functions=None)
+    spec = P.atmosphere_ocean_interface_spec(flux_formulation=flux)
+    th = spec.thermodynamics_parameters
+    ua, va, Ta, qa, pa = 5.5, -2.0, 288.15, 0.003, 100500.0
+    L, arrs = one_cell(u_atm=ua, v_atm=va, T_atm=Ta, p_atm=pa, q_atm=qa, u_oc=0, v_oc=0, T_oc=15.0, S_oc=30.0)
+    c = spec.to_c()
+    out = oracle.ao_fluxes(c, L, arrs)
+    lib = oracle.load()
+    To = 15.0 + 273.15
+    qo = lib.oracle_surface_specific_humidity(C.byref(c), pa, To)
+    cp = th.cp_d + (th.water_vapor_heat_capacity - th.cp_d) * qa
+    rho = pa / (th.R_d * (1 + (th.Rv_over_Rd - 1) * qa) * Ta)
+    Lv = th.reference_vaporization_enthalpy + (th.water_vapor_heat_capacity - th.liquid_water_heat_capacity) * (
+        Ta - th.reference_temperature)
+    h, g, k = spec.surface_layer_height, spec.gravitational_acceleration, 0.4
+    dU = math.hypot(ua, va)
+    dth = Ta - To + h / cp * g
+    dq = qa - qo
+    us = k / math.log(h / ell) * dU
+    ts = k / math.log(h / ell) * dth
+    qs = k / math.log(h / ell) * dq
+    expect = {"x_momentum": -rho * us ** 2 * ua / dU, "y_momentum": -rho * us ** 2 * va / dU,
+              "sensible_heat": -rho * cp * us * ts, "water_vapor": -rho * us * qs,
+              "latent_heat": -rho * us * qs * Lv}
+    for key, val in expect.items():
+        assert L.interior(out[key])[0, 0] == pytest.approx(val, rel=1.5e-8), key
+    assert L.interior(out["iterations"])[0, 0] == 2     # exact after one step; the second confirms
+
+
+def test_gustiness_bit_identity(oracle):
+    f = P.SimilarityTheoryFluxes().to_c()
+    lib = oracle.load()
+    for us, bs, hbl in ((0.3, -0.005, 600.0), (0.3, 0.005, 600.0), (1e-4, 0.0, 512.0)):
+        Jb = -us * bs
+        UG = max(0.01, 1.2 * float(np.cbrt(max(0.0, Jb) * hbl)))
+        assert lib.oracle_vsgs2(C.byref(f), us, bs, hbl) == UG ** 2
+    assert lib.oracle_vsgs2(C.byref(f), 0.3, -0.005, 600.0) > 0.01 ** 2
+    assert lib.oracle_vsgs2(C.byref(f), 0.3, 0.005, 600.0) == 0.01 ** 2
+    f0 = P.SimilarityTheoryFluxes(subgrid_velocities=P.ConvectiveGustiness(0, 0)).to_c()
+    assert lib.oracle_vsgs2(C.byref(f0), 0.3, -0.005, 600.0) == 0.0
+    # SubgridVelocityCorrection composition: convective + mesoscale^2
+    vsg = P.mahrt_sun_subgrid_velocity(25e3)
+    assert vsg == pytest.approx(0.32 * 4 ** 0.33)
+    fs = P.SimilarityTheoryFluxes(subgrid_velocities=P.SubgridVelocityCorrection(P.ConvectiveGustiness(), vsg)).to_c()
+    assert lib.oracle_vsgs2(C.byref(fs), 0.3, -0.005, 600.0) == lib.oracle_vsgs2(C.byref(f), 0.3, -0.005, 600.0) + vsg ** 2
+
+
+def test_stability_values(oracle):
+    lib = oracle.load()
+    ly = P.large_yeager_stability_functions()
+    m, s = ly.momentum.to_c(), ly.temperature.to_c()
+    lin = P.SplitStabilityFunction(P.LinearStableStabilityFunction(), P.PaulsonScalarStabilityFunction()).to_c()
+    psi = lambda f, z: lib.oracle_stability(C.byref(f), z)
+    assert psi(lin, 0.0) == pytest.approx(0.0, abs=1e-12)
+    assert psi(lin, 1.0) == pytest.approx(-5.0)
+    assert psi(lin, 20.0) == pytest.approx(-50.0)
+    assert psi(m, -1.0) > 0
+    assert psi(m, 1.0) == pytest.approx(-5.0)
+    assert psi(m, 0.0) == pytest.approx(0.0, abs=1e-10)
+    assert psi(s, -1.0) > 0
+    assert psi(s, 1.0) == pytest.approx(-5.0)
+
+
+def _edson_momentum_py(z, c):
+    zmax, Ap, Bp, Cp, Dp, Am, Bm, Cm, Dm, Em, Fm = c
+    zm, zp = min(0.0, z), max(0.0, z)
+    dz = min(zmax, Ap * zp)
+    psip = -Bp * zp - Cp * (zp - Dp) * math.exp(-dz) - Cp * Dp
+    f1 = math.sqrt(math.sqrt(1 - Am * zm))
+    psi1 = Bm * math.log((1 + f1) / Bm) + math.log((1 + f1 ** 2) / Bm) - Bm * math.atan(f1) + Cm
+    f2 = np.cbrt(1 - Dm * zm)
+    psi2 = Em / 2 * math.log((1 + f2 + f2 ** 2) / Em) - math.sqrt(Em) * math.atan((1 + 2 * f2) / math.sqrt(Em)) + Fm
+    f = zm ** 2 / (1 + zm ** 2)
+    return psip if not z < 0 else (1 - f) * psi1 + f * psi2
+
+
+def _edson_scalar_py(z, c):
+    zmax, Ap, Bp, Cp, Dp, Ep, Am, Bm, Cm, Dm, Em, Fm = c
+    zm, zp = min(0.0, z), max(0.0, z)
+    dz = min(zmax, Ap * zp)
+    psip = -(1 + Bp * zp) ** Cp - Bp * (zp - Dp) * math.exp(-dz) - Ep
+    f1 = math.sqrt(1 - Am * zm)
+    psi1 = Bm * math.log((1 + f1) / Bm) + Cm
+    f2 = np.cbrt(1 - Dm * zm)
+    psi2 = Em / 2 * math.log((1 + f2 + f2 ** 2) / Em) - math.sqrt(Em) * math.atan((1 + 2 * f2) / math.sqrt(Em)) + Fm
+    f = zm ** 2 / (1 + zm ** 2)
+    return psip if not z < 0 else (1 - f) * psi1 + f * psi2
+
+
+def test_edson_functions_match_independent_restatement(oracle):
+    """A second restatement (Python, straight from similarity_theory_turbulent_fluxes.jl:501-618)."""
+    lib = oracle.load()
+    em, es = P.EdsonMomentumStabilityFunction(), P.EdsonScalarStabilityFunction()
+    cm, cs = em.to_c(), es.to_c()
+    for z in (-50.0, -3.2, -1.0, -0.1, -1e-6, 0.0, 1e-6, 0.1, 1.0, 7.5, 80.0):
+        assert lib.oracle_stability(C.byref(cm), z) == pytest.approx(_edson_momentum_py(z, em.coefficients()), rel=1e-13, abs=1e-15)
+        assert lib.oracle_stability(C.byref(cs), z) == pytest.approx(_edson_scalar_py(z, es.coefficients()), rel=1e-13, abs=1e-15)
+    # continuity at zero and the neutral limit psi(0) = 0
+    assert abs(lib.oracle_stability(C.byref(cm), 0.0)) < 1e-12
+    assert abs(lib.oracle_stability(C.byref(cs), -1e-12)) < 1e-9
+
+
+def _tef(oracle, To, So, Si, us=0.002):
+    spec = P.SeaIceOceanSpec(heat_flux=P.ThreeEquationHeatFlux(conductive=False, friction_velocity=us),
+                             reference_latent_heat=334e3, ocean_reference_density=1025.0, ocean_heat_capacity=3991.0)
+    p = spec.to_c()
+    Tb, Sb, q = C.c_double(), C.c_double(), C.c_double()
+    oracle.load().oracle_solve_interface_conditions(C.byref(p), To, So, Si, 1.0, 0.1, 0.0,
+                                                    C.byref(Tb), C.byref(Sb), C.byref(q))
+    return Tb.value, Sb.value, q.value
+
+
+def test_three_equation_properties(oracle):
+    liq = P.LinearLiquidus()
+    Tb, Sb, q = _tef(oracle, 2.0, 35.0, 5.0)
+    assert 5.0 <= Sb <= 35.0 and Tb == pytest.approx(liq.melting_temperature(Sb)) and q > 0
+    Tb, Sb, q = _tef(oracle, liq.melting_temperature(35.0) + 0.5, 35.0, 5.0)
+    assert 5.0 <= Sb <= 35.0 and Tb == pytest.approx(liq.melting_temperature(Sb)) and q > 0
+    To = liq.melting_temperature(35.0)
+    Tb, Sb, q = _tef(oracle, To, 35.0, 5.0)
+    assert Sb == pytest.approx(35.0) and Tb == pytest.approx(To) and abs(q) < np.finfo(float).eps
+    for So in (30.0, 33.0, 35.0, 37.0, 40.0):
+        Tb, Sb, q = _tef(oracle, 1.0, So, 5.0)
+        assert 5.0 <= Sb <= So and Tb == pytest.approx(liq.melting_temperature(Sb))
+    Tb, Sb, q = _tef(oracle, 1.0, 35.0, 0.0)
+    assert 0.0 <= Sb <= 35.0 and Tb == pytest.approx(liq.melting_temperature(Sb))
+    for us in (0.1, 0.0001):
+        Tb, Sb, q = _tef(oracle, 1.0, 35.0, 5.0, us)
+        assert 5.0 <= Sb <= 35.0 and Tb == pytest.approx(liq.melting_temperature(Sb))
+
+
+def test_ao_solver_converges_on_1deg_sample(oracle):
+    """Every cell of a 1-degree sample converges well before maxiter, with physical fluxes."""
+    st = syn.ao_1deg(nx=60, ny=30)
+    out = oracle.ao_fluxes(P.atmosphere_ocean_interface_spec().to_c(), st.layout, st.fields)
+    it = st.layout.ring(out["iterations"])
+    assert it.min() >= 2 and it.max() < 100
+    us = st.layout.interior(out["friction_velocity"])
+    assert np.all(us > 0) and np.all(us < 3)
+    assert np.all(np.isfinite(st.layout.interior(out["latent_heat"])))
