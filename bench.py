@@ -1,0 +1,402 @@
+"""Benchmark of the interface-flux coupling step on one GB300 (or N independent replicas).
+
+Workload: the 1/8 degree coupled ocean + sea-ice exchange grid (2880 x 1280,
+latitude -80..80, 30 % land, sea ice poleward of 55 degrees), forced by a
+640 x 320 prescribed atmosphere at two 3-hourly snapshots interpolated onto the
+exchange grid; FP32 fields in HBM. One step = update_state: interpolation,
+atmosphere-ocean + atmosphere-sea-ice + sea-ice-ocean fluxes, net ocean and
+sea-ice flux assembly with radiation. The step's working set (~0.8 GB) exceeds
+L2, so no flush is needed between timed steps.
+
+Metric: flux cells/s (water cells solved at the atmosphere-ocean interface +
+ice-covered cells at the atmosphere-sea-ice interface, per second), for the
+FP32 + FP64-polish solver; the plain FP64 solver is timed on the same step and
+reported beside it, with the max relative flux error of the fast solver.
+
+--impl reference times the CPU restatement of the reference's path (the
+reference is Julia; no Julia toolchain is available) on all host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "numericalearth.jl_gb300")
+for _p in (REPO, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "flux cells/s at <=1e-5 rel err: FP32+batch+warm-start vs plain FP64, 1 GB300"
+WORKLOAD = "coupled_eighth: 2880x1280 ocean+sea-ice exchange grid, 30% land, 640x320x2 prescribed atmosphere"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="nesf", choices=["nesf", "reference"])
+    ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--small", action="store_true", help="small grid (profiling captures)")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.file is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as fh:
+            for line in fh:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            return json.load(fh), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def make_state(small):
+    from nesf import synthetic as syn
+    if small:
+        return syn.coupled(seed=1004, nx=720, ny=320, lat_s=-80, lat_n=80, land=0.3, interpolate=True)
+    return syn.coupled_eighth()
+
+
+# algorithmic bytes per cell of each phase for FP32 fields (element size 4 B):
+#  atmosphere-ocean solve: 9 inputs (u, v, T, p, q atmosphere; u, v, T, S ocean) + mask (1 B)
+#                          read, 9 outputs written                       -> 18*4 + 1 = 73 B
+#  atmosphere-sea-ice:     12 inputs + mask read, 6 outputs (incl. T_s)   -> 18*4 + 1 = 73 B
+#  sea-ice-ocean:          T, S, Si, h, hc, aleph, T_int, E_i, E_s read; T (frazil), 6 outputs -> 16*4 = 64 B
+#  interpolation:          9 exchange-grid outputs (+ 2 FP64 fractional indices read) -> 9*4 + 16 = 52 B
+#  assembly + radiation:   ocean 17 reads + 6 writes, ice 11 reads + 5 writes, radiation 6 diag writes
+BYTES_PER_CELL = {"interp": 52, "ao": 73, "ai": 73, "io": 64, "asm": 4 * (17 + 6 + 11 + 5 + 6 + 4) + 2}
+
+
+def phase_times(model, precision, reps=3):
+    """Per-phase device time (ms) with CUDA events on the launching stream."""
+    import torch
+    s = torch.cuda.current_stream()
+    names = ["interp", "ao", "ai", "io", "asm"]
+    acc = {n: 0.0 for n in names}
+    from nesf import api
+    from nesf import fields as F
+    for _ in range(reps):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+        ev[0].record(s)
+        model.interpolate_state()
+        ev[1].record(s)
+        api.compute_atmosphere_ocean_fluxes(model.ao_spec, model.layout, model.x, model.ao, precision=precision)
+        ev[2].record(s)
+        api.compute_atmosphere_sea_ice_fluxes(model.ai_spec, model.layout, {k: model.x.get(k) for k in F.AI_INPUTS},
+                                              model.ai, precision=precision)
+        ev[3].record(s)
+        x = model.x
+        api.compute_sea_ice_ocean_fluxes(model.io_spec, model.layout,
+                                         {"ice_salinity": x["ice_salinity"], "ice_thickness": x["ice_thickness"],
+                                          "consolidation_thickness": x["consolidation_thickness"],
+                                          "ice_concentration": x["ice_concentration"],
+                                          "internal_temperature": x["ice_temperature"],
+                                          "ice_mass_flux": x["ice_mass_flux"], "snow_mass_flux": x["snow_mass_flux"]},
+                                         model.io, model.T3, model.S3, model.dz)
+        ev[4].record(s)
+        model.update_net_fluxes()
+        ev[5].record(s)
+        torch.cuda.synchronize()
+        for k, n in enumerate(names):
+            acc[n] += ev[k].elapsed_time(ev[k + 1]) / reps
+    return acc
+
+
+def time_steps(model, precision, steps, warmup, world):
+    import torch
+    for _ in range(warmup):
+        model.update_state(precision)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches = 0
+    e0.record(s)
+    for _ in range(steps):
+        launches += model.update_state(precision)
+    e1.record(s)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, launches
+
+
+def error_stats(model):
+    """Max / p99 relative error of the fast solver against the plain FP64 solver on the full step
+    outputs (normalised by max(|ref|, 1e-6 max|ref|))."""
+    import torch
+    from nesf import fields as F
+    L = model.layout
+    res = {}
+    model.reset()
+    model.update_state("f64")
+    torch.cuda.synchronize()
+    ref = {("ao", k): L.ring(model.ao[k].double().cpu().numpy()) for k in F.AO_OUTPUTS}
+    ref.update({("ai", k): L.ring(model.ai[k].double().cpu().numpy()) for k in F.AI_OUTPUTS})
+    model.reset()
+    model.update_state("f32")
+    torch.cuda.synchronize()
+    got = {("ao", k): L.ring(model.ao[k].double().cpu().numpy()) for k in F.AO_OUTPUTS}
+    got.update({("ai", k): L.ring(model.ai[k].double().cpu().numpy()) for k in F.AI_OUTPUTS})
+    for key, r in ref.items():
+        g = got[key]
+        den = np.maximum(np.abs(r), 1e-6 * np.abs(r).max())
+        e = np.abs(g - r) / np.where(den > 0, den, 1.0)
+        res[f"{key[0]}.{key[1]}"] = {"max": float(e.max()), "p99": float(np.percentile(e, 99))}
+    model.reset()
+    return res
+
+
+def e2e_step_time(model, precision, steps, warmup):
+    """Same step through the public API with host buffers: pinned H2D of the step's inputs
+    (ocean and sea-ice surface state + the two atmosphere snapshots), the step, and a D2H
+    read of the net boundary fluxes, all inside the timed region."""
+    import torch
+    from nesf.coupled import ICE_NET, OCEAN_NET, STEP_INPUTS
+    names = [k for k in STEP_INPUTS if k in model.x]
+    host_in = {k: model.x[k].cpu().pin_memory() for k in names}
+    atm_in = {k: v.cpu().pin_memory() for k, v in model.atmos_src.items()} if model.atmos is not None else {}
+    host_out = {k: torch.empty_like(model.net[k], device="cpu").pin_memory() for k in OCEAN_NET + ICE_NET}
+    h2d = sum(t.numel() * t.element_size() for t in host_in.values()) + \
+        sum(t.numel() * t.element_size() for t in atm_in.values())
+    d2h = sum(t.numel() * t.element_size() for t in host_out.values())
+    s = torch.cuda.current_stream()
+
+    def one():
+        for k, t in host_in.items():
+            model.x[k].copy_(t, non_blocking=True)
+        for k, t in atm_in.items():
+            model.atmos_src[k].copy_(t, non_blocking=True)
+        model.update_state(precision)
+        for k, t in host_out.items():
+            t.copy_(model.net[k], non_blocking=True)
+
+    for _ in range(warmup):
+        one()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(steps):
+        one()
+    e1.record(s)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps, h2d, d2h
+
+
+def cpu_baseline(state, target_s=12.0):
+    """The oracle (C restatement, OpenMP over all host threads) on bands of rows of the same
+    workload: interpolation of the prescribed atmosphere onto the band, then the
+    atmosphere-ocean and atmosphere-sea-ice solves; returns solved cells/s and the sample."""
+    from nesf import api
+    from nesf import params as P
+    from nesf import synthetic as syn
+    from oracle import oracle
+    L = state.layout
+    f = state.fields
+    rows = 8
+    threads = oracle.get_threads()
+    done_cells = 0
+    elapsed = 0.0
+    ao = P.atmosphere_ocean_interface_spec().to_c()
+    ai = P.atmosphere_sea_ice_interface_spec().to_c()
+    sub = syn.Layout(L.nx, rows, L.hx, L.hy)
+    height = rows + 2 * L.hy
+    positions = np.linspace(0, L.shape[0] - height, 97).astype(int)
+    atmos = state.atmos
+    bands = 0
+    while elapsed < target_s and bands < 10 * len(positions):
+        lo = int(positions[bands % len(positions)])
+        band = {k: np.ascontiguousarray(v[lo:lo + height].astype(np.float64) if v.dtype != np.uint8
+                                        else v[lo:lo + height]) for k, v in f.items() if v.ndim == 2}
+        t0 = time.perf_counter()
+        if "u_atm" not in band:
+            c = state.coords
+            bc = api.exchange_coords(syn.LonLat(c.lon0, c.dlon, c.lat0 + lo * c.dlat, c.dlat))
+            out = oracle.interpolate(sub, bc, api.atmos_grid_struct(atmos), atmos["arrays"], atmos["time_weight"])
+            for n, k in (("u", "u_atm"), ("v", "v_atm"), ("T", "T_atm"), ("q", "q_atm"), ("p", "p_atm"),
+                         ("sw", "sw_down"), ("lw", "lw_down")):
+                band[k] = out[n]
+        oracle.ao_fluxes(ao, sub, band, with_iterations=False)
+        oracle.ai_fluxes(ai, sub, band, band["ice_temperature"], with_iterations=False)
+        elapsed += time.perf_counter() - t0
+        water = sub.interior(band["inactive"]) == 0
+        ice = sub.interior(band["ice_concentration"]) > 0
+        done_cells += int(water.sum() + (water & ice).sum())
+        bands += 1
+    return {"value": done_cells / elapsed, "unit": "flux cells/s", "cores": threads, "kind": "port",
+            "sample": f"{bands} bands of {rows} rows x {L.nx} cells spread over the domain ({done_cells} "
+                      f"solved cells): interpolation + AO + AI solves, {elapsed:.1f} s of CPU work"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle
+    state = make_state(args.small)
+    for _ in range(args.warmup):
+        cpu_baseline(state, target_s=0.5)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(state, target_s=max(1.0, 60.0 / max(1, args.steps))))
+    wall = time.perf_counter() - t0
+    v = float(np.mean([x["value"] for x in vals]))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "flux cells/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * wall / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample": "row bands of the workload", "parallelism": "openmp"},
+            "cpu_baseline": {"value": v, "unit": "flux cells/s", "cores": oracle.get_threads(), "kind": "port",
+                             "sample": vals[-1]["sample"] + " (the reference is Julia; no Julia toolchain here)"},
+            "e2e": {"value": v, "unit": "flux cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    import __graft_entry__
+    __graft_entry__.build()
+    from nesf.coupled import CoupledModel
+    state = make_state(args.small)
+    model = CoupledModel(state)
+    n_ao, n_ai = model.active_cells()
+    cells = n_ao + n_ai
+    prec = args.precision
+
+    # warm-up both solvers, then the timed region (fast path) with clock sampling
+    with ClockSampler(local) as clocks:
+        ms, launches = time_steps(model, prec, args.steps, args.warmup, world)
+    clk = clocks.summary()
+    ms_plain, _ = time_steps(model, "f64", max(3, args.steps // 4), 1, world)
+    phases = phase_times(model, prec)
+    phases_plain = phase_times(model, "f64", reps=1)
+    value = cells * world / (ms / 1000.0)
+    line = {"metric": METRIC, "value": value, "unit": "flux cells/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64polish" if prec == "f32" else "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "cells_ao": n_ao, "cells_ai": n_ai, "fields": "fp32",
+                       "warm_start": False, "schedule": "one thread per cell, per-phase kernels",
+                       "l2": "working set > L2 (no flush needed)", "parallelism": f"replicas x{world}"},
+            "gpu_launches": launches,
+            "clocks": clk,
+            "plain_f64": {"value": cells * world / (ms_plain / 1000.0), "ms_per_step": ms_plain,
+                          "phases_ms": phases_plain},
+            "phases_ms": phases}
+    if rank == 0:
+        line["speedup_vs_plain_f64"] = ms_plain / ms
+        model.reset()
+        s_ao, s_ai = model.compute_fluxes(prec, stats=True)
+        model.reset()
+        p_ao, p_ai = model.compute_fluxes("f64", stats=True)
+        model.reset()
+        strip = lambda d: {k: (v if not hasattr(v, "tolist") else v.tolist()) for k, v in d.items() if k != "histogram"}
+        line["solver_stats"] = {"ao": strip(s_ao), "ai": strip(s_ai), "ao_plain": strip(p_ao), "ai_plain": strip(p_ai)}
+        line["errors_vs_plain_f64"] = error_stats(model)
+        # roofline of the dominant kernel (HBM: algorithmic bytes / event-timed duration)
+        peaks, kind = measured_peaks()
+        top = max(phases, key=phases.get)
+        n_cells = {"interp": (model.layout.nx + 2) * (model.layout.ny + 2),
+                   "ao": (model.layout.nx + 2) * (model.layout.ny + 2),
+                   "ai": (model.layout.nx + 2) * (model.layout.ny + 2),
+                   "io": model.layout.nx * model.layout.ny, "asm": model.layout.nx * model.layout.ny}[top]
+        alg = BYTES_PER_CELL[top] * n_cells
+        achieved = alg / (phases[top] / 1000.0) / 1e9
+        line["roofline"] = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peaks["hbm_gbs"],
+                            "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                            "algorithmic_bytes": alg, "peak_source": kind}
+        if not args.no_e2e:
+            ms_e2e, h2d, d2h = e2e_step_time(model, prec, max(3, args.steps // 2), 1)
+            line["e2e"] = {"value": cells / (ms_e2e / 1000.0), "unit": "flux cells/s", "h2d_bytes_per_step": h2d,
+                           "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e}
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(state)
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

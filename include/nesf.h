@@ -195,13 +195,16 @@ typedef enum {
 
 typedef struct {
     int32_t precision;        /* nesf_precision                                        */
-    int32_t polish_maxiter;   /* FP64 polish iterations at most (default 3)            */
+    int32_t polish_maxiter;   /* FP64 Newton polish steps at most (default 3; 1-3 are
+                                 used by contraction rate)                            */
     int32_t block_size;       /* threads per block; 0 = library default                */
     int32_t schedule;         /* 0: one thread per cell; 1: persistent lane refill      */
     int32_t ctas_per_sm;      /* persistent schedule: CTAs per SM (0 = occupancy)       */
     int32_t warm_start;       /* 1: MLP initial guess (needs mlp weights)              */
     const void* mlp;          /* device pointer to packed MLP weights (nesf_mlp_*)      */
     double fallback_ratio;    /* cold-start fallback when r1 > ratio * r1(cold); 10    */
+    double path_tolerance;    /* replay cells whose reference stopping error may exceed
+                                 this relative bound (FP32 polish); default 2e-6         */
 } nesf_solver_options;
 
 /* -------------------------------------------------------------- statistics */
@@ -215,6 +218,9 @@ typedef struct {
     int64_t polished;           /* cells that needed an FP64 polish                */
     int64_t polish_iterations;  /* FP64 polish iterations                          */
     int64_t cold_fallbacks;     /* warm starts rejected by the residual test       */
+    int64_t fp64_redo;          /* cells replayed in FP64 (sum of replay_reasons)  */
+    int64_t replay_reasons[5];  /* calm u*, no FP32 convergence, slow contraction,
+                                   stopping-error bound, singular Newton matrix   */
     int64_t histogram[NESF_ITER_HIST_BINS]; /* iterations (FP32+FP64) per solved cell */
 } nesf_stats;
 

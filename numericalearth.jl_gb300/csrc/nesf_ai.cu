@@ -1,44 +1,31 @@
 // nesf_ai.cu -- atmosphere-sea-ice similarity-theory solve.
 //
-// _compute_atmosphere_ocean_interface_state!  (InterfaceComputations/atmosphere_ocean_fluxes.jl:80-197)
 // _compute_atmosphere_sea_ice_interface_state! (InterfaceComputations/atmosphere_sea_ice_fluxes.jl:65-185)
 //
-// One thread per surface cell over the halo ring (0:nx+1, 0:ny+1), SoA loads of
-// the Oceananigans parent arrays (i fastest, so a warp reads 32 consecutive
-// cells of a row). Two precisions:
-//   PLAIN   every iteration in FP64 (the drop-in, parity with the CPU solver);
-//   POLISH  FP64 prologue for the loop invariants, the fixed point in FP32 until
-//           it converges (drift < tol) or stalls at FP32 resolution, then FP64
-//           fixed-point polish steps from the FP32 state for the stalled cells.
+// Same structure as the atmosphere-ocean kernel: one thread per cell over the
+// halo ring, PLAIN or POLISH solve in pass 1, packed FP64 replays in pass 2. The
+// interface temperature is a SkinTemperature over ice and snow, so the solver
+// state carries T_s as a fourth component.
 #include "nesf_solve.cuh"
 
 namespace nesf {
 
-// ------------------------------------------------------------------ AI kernel
-template <class S, int PREC>
-__global__ void __launch_bounds__(128) ai_kernel(AIArgs<S> a, DevIface<double> P64, DevIface<float> P32,
-                                                 int polish_maxiter, DevStats* stats) {
-    const int nxr = a.L.nx + 2;
-    const int64_t ring = (int64_t)nxr * (a.L.ny + 2);
-    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= ring) return;
-    int i = (int)(r % nxr), j = (int)(r / nxr);
-    int64_t k = a.L.at(i, j);
-    const DevIface<double>& P = P64;
-    CellConst<double> c;
+template <class S>
+__device__ __forceinline__ void ai_load(const DevIface<double>& P, const AIArgs<S>& a, int64_t k,
+                                        CellConst<double>& c, double& aleph, double& Ts0, bool& land) {
     c.ua = ld(a.ua, k); c.va = ld(a.va, k); c.Ta = ld(a.Ta, k); c.pa = ld(a.pa, k); c.qa = ld(a.qa, k);
-    c.Ti = ld(a.To, k) + P.off_int;
+    c.Ti = ld(a.To, k) + P.off_int;      // ocean below the ice (atmosphere_sea_ice_fluxes.jl:92-94)
     c.Si = ld(a.So, k);
-    c.ui = 0; c.vi = 0;
+    c.ui = 0; c.vi = 0;                  // sea-ice velocities are not used (:97-98)
     c.hi = ld(a.hi, k);
     c.hs = ldz(a.hs, k);
     c.hc = ld(a.hc, k);
-    double aleph = ld(a.aleph, k);
-    double Ts0 = ld(a.Ts, k) + P.off_ifc;
+    aleph = ld(a.aleph, k);
+    Ts0 = ld(a.Ts, k) + P.off_ifc;
     c.sw = ldz(a.sw, k);
     c.lw = ldz(a.lw, k);
     c.kappa = -1.0;
-    bool land = a.inactive ? a.inactive[k] != 0 : false;
+    land = a.inactive ? a.inactive[k] != 0 : false;
     if (P.vel_form == NESF_WIND_VELOCITY) { c.du = c.ua; c.dv = c.va; }
     else { c.du = c.ua - 0.0; c.dv = c.va - 0.0; }
     c.dU2 = c.du * c.du + c.dv * c.dv;
@@ -46,27 +33,13 @@ __global__ void __launch_bounds__(128) ai_kernel(AIArgs<S> a, DevIface<double> P
     c.rho_a = air_density(P, c.Ta, c.pa, c.qa);
     c.cp_a = cp_m(P, c.qa);
     c.L_s = latent_heat_sublim(P, c.Ta);
+}
 
-    double us = 1e-4, ts = 1e-4, qst = 1e-4;
-    double qs0 = surface_specific_humidity(P, c.pa, Ts0);
-    SurfaceConst<double> s;
-    surface_const(P, c, Ts0, qs0, s);
-    bool ice_free = aleph == 0;
-    bool needs = P.stop_kind == NESF_STOP_CONVERGENCE;
-    int iters = 0, piters = 0;
-    bool nonconv = false;
-    bool solved = !((needs && land) || ice_free);
-    double Ts;
-    if (solved) {
-        if (P.temp_form == NESF_BULK_TEMPERATURE)
-            iters = solve_cell<PREC, false>(P64, P32, c, s, us, ts, qst, polish_maxiter, nonconv, piters);
-        else
-            iters = solve_cell<PREC, true>(P64, P32, c, s, us, ts, qst, polish_maxiter, nonconv, piters);
-        Ts = s.Ts;
-    } else {
-        us = ts = qst = 0;
-        Ts = c.Ti;
-    }
+// The flux epilogue (atmosphere_sea_ice_fluxes.jl:154-184).
+template <class S>
+__device__ __forceinline__ void ai_store(const DevIface<double>& P, const AIArgs<S>& a, int64_t k,
+                                         const CellConst<double>& c, double us, double ts, double qst, double Ts,
+                                         int iters) {
     double du = c.du, dv = c.dv;
     double dU = sqrt(du * du + dv * dv);
     double tx = dU == 0 ? 0.0 : -(us * us) * du / dU;
@@ -79,27 +52,152 @@ __global__ void __launch_bounds__(128) ai_kernel(AIArgs<S> a, DevIface<double> P
     st(a.ty, k, rho * ty);
     a.Ts[k] = (S)(Ts - P.off_ifc);
     if (a.iters) a.iters[k] = iters;
-    if (stats) stats_add(stats, true, solved, iters, nonconv, piters > 0, piters, false, 0);
+}
+
+template <bool SKIN>
+__device__ __forceinline__ int ai_plain(const DevIface<double>& P, const CellConst<double>& c, double Ts0,
+                                        double& us, double& ts, double& qst, double& Ts, bool& nonconv) {
+    double qs0 = surface_specific_humidity(P, c.pa, Ts0);
+    SurfaceConst<double> s;
+    surface_const(P, c, Ts0, qs0, s);
+    us = ts = qst = 1e-4;   // initial guess (atmosphere_sea_ice_fluxes.jl:127)
+    int it = solve_plain<SKIN>(P, c, s, us, ts, qst, nonconv);
+    Ts = s.Ts;
+    return it;
+}
+
+// Pass 0: ice-free and land cells get the zero state with the ocean temperature
+// (atmosphere_sea_ice_fluxes.jl:141-142); the others go to the work list.
+template <class S>
+__global__ void __launch_bounds__(128) ai_classify_kernel(AIArgs<S> a, DevIface<double> P, DevIface<float> Pf,
+                                                          WorkList wl, DevStats* stats) {
+    const int nxr = a.L.nx + 2;
+    const int64_t ring = (int64_t)nxr * (a.L.ny + 2);
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool in = r < ring;
+    int i = in ? (int)(r % nxr) : 0, j = in ? (int)(r / nxr) : 0;
+    int64_t k = a.L.at(i, j);
+    bool skip = false, active = false, stable = false;
+    CellConst<double> c;
+    double aleph = 0, Ts0 = 0;
+    if (in) {
+        bool land;
+        ai_load(P, a, k, c, aleph, Ts0, land);
+        bool needs = P.stop_kind == NESF_STOP_CONVERGENCE;
+        skip = (needs && land) || aleph == 0;
+        active = !skip;
+        if (active) stable = stable_class(Pf, (float)c.Ta, (float)c.pa, (float)c.qa, (float)Ts0);
+    }
+    worklist_push(wl, 0, active, stable, (uint32_t)r);
+    if (skip) {
+        ai_store(P, a, k, c, 0.0, 0.0, 0.0, c.Ti, 0);
+        if (stats) stats_add(stats, true, false, 0, false, false, 0, false, false);
+    }
+}
+
+// Pass 1: the compacted ice cells, one thread each.
+template <class S, int PREC>
+__global__ void __launch_bounds__(128) ai_kernel(AIArgs<S> a, DevIface<double> P64, DevIface<float> P32,
+                                                 SolveOpts so, WorkList wl, ReplayQueue rq, DevStats* stats) {
+    const int nxr = a.L.nx + 2;
+    int64_t r = worklist_get(wl, 0, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+    if (r < 0) return;
+    int i = (int)(r % nxr), j = (int)(r / nxr);
+    int64_t k = a.L.at(i, j);
+    const DevIface<double>& P = P64;
+    CellConst<double> c;
+    double aleph, Ts0;
+    bool land;
+    ai_load(P, a, k, c, aleph, Ts0, land);
+    bool skin = P.temp_form != NESF_BULK_TEMPERATURE;
+    bool needs = P.stop_kind == NESF_STOP_CONVERGENCE;
+    double us = 0, ts = 0, qst = 0, Ts = c.Ti;
+    int iters = 0, f64it = 0;
+    bool nonconv = false, polished = false, replay = false;
+    int reason = -1;
+    if (PREC == NESF_PLAIN_F64 || !needs) {
+        iters = skin ? ai_plain<true>(P, c, Ts0, us, ts, qst, Ts, nonconv)
+                     : ai_plain<false>(P, c, Ts0, us, ts, qst, Ts, nonconv);
+    } else {
+        double qs0 = surface_specific_humidity(P, c.pa, Ts0);
+        SurfaceConst<double> s;
+        surface_const(P, c, Ts0, qs0, s);
+        us = ts = qst = 1e-4;
+        int f32it;
+        polished = skin ? solve_fast<true>(P, P32, c, s, us, ts, qst, so, f32it, f64it, reason)
+                        : solve_fast<false>(P, P32, c, s, us, ts, qst, so, f32it, f64it, reason);
+        iters = f32it + f64it;
+        Ts = s.Ts;
+        replay = !polished;
+    }
+    if (PREC != NESF_PLAIN_F64) replay_push(rq, replay, (uint32_t)r);
+    if (replay) {
+        if (stats) {
+            stats_add(stats, true, false, 0, false, false, 0, true, false);
+            stats_replay_reason(stats, reason);
+        }
+        return;
+    }
+    ai_store(P, a, k, c, us, ts, qst, Ts, iters);
+    if (stats) stats_add(stats, true, true, iters, nonconv, polished, f64it, false, false);
+}
+
+// Pass 2: the queued cells, packed, through the reference's FP64 iteration. The
+// initial interface temperature is still in a.Ts: pass 1 did not write these cells.
+template <class S>
+__global__ void __launch_bounds__(128) ai_replay_kernel(AIArgs<S> a, DevIface<double> P, ReplayQueue rq,
+                                                        DevStats* stats) {
+    const int nxr = a.L.nx + 2;
+    const unsigned n = *rq.count;
+    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n && (int64_t)q < rq.capacity;
+         q += gridDim.x * blockDim.x) {
+        int64_t r = rq.idx[q];
+        int i = (int)(r % nxr), j = (int)(r / nxr);
+        int64_t k = a.L.at(i, j);
+        CellConst<double> c;
+        double aleph, Ts0;
+        bool land;
+        ai_load(P, a, k, c, aleph, Ts0, land);
+        double us, ts, qst, Ts;
+        bool nonconv;
+        int it = P.temp_form != NESF_BULK_TEMPERATURE ? ai_plain<true>(P, c, Ts0, us, ts, qst, Ts, nonconv)
+                                                      : ai_plain<false>(P, c, Ts0, us, ts, qst, Ts, nonconv);
+        ai_store(P, a, k, c, us, ts, qst, Ts, it);
+        if (stats) stats_add(stats, false, true, it, nonconv, false, it, false, false);
+    }
 }
 
 template <class S>
 static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
-                               int polish_maxiter, DevStats* stats, cudaStream_t stream) {
+                               SolveOpts so, const WorkList& wl, const ReplayQueue& rq, DevStats* stats,
+                               cudaStream_t stream) {
     const int64_t ring = (int64_t)(a.L.nx + 2) * (a.L.ny + 2);
     const int block = 128;
     dim3 grid((unsigned)((ring + block - 1) / block));
-    if (prec == NESF_PLAIN_F64) ai_kernel<S, NESF_PLAIN_F64><<<grid, block, 0, stream>>>(a, P64, P32, polish_maxiter, stats);
-    else ai_kernel<S, NESF_F32_POLISH><<<grid, block, 0, stream>>>(a, P64, P32, polish_maxiter, stats);
+    cudaError_t e = cudaMemsetAsync(wl.count, 0, sizeof(unsigned) * 2, stream);
+    if (e == cudaSuccess && prec != NESF_PLAIN_F64) e = cudaMemsetAsync(rq.count, 0, sizeof(unsigned), stream);
+    if (e != cudaSuccess) return e;
+    ai_classify_kernel<S><<<grid, block, 0, stream>>>(a, P64, P32, wl, stats);
+    if (prec == NESF_PLAIN_F64)
+        ai_kernel<S, NESF_PLAIN_F64><<<grid, block, 0, stream>>>(a, P64, P32, so, wl, rq, stats);
+    else
+        ai_kernel<S, NESF_F32_POLISH><<<grid, block, 0, stream>>>(a, P64, P32, so, wl, rq, stats);
+    e = cudaGetLastError();
+    if (e != cudaSuccess || prec == NESF_PLAIN_F64) return e;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    ai_replay_kernel<S><<<(unsigned)sms * 4, block, 0, stream>>>(a, P64, rq, stats);
     return cudaGetLastError();
 }
 
 cudaError_t launch_ai(const AIArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
-                      int polish_maxiter, DevStats* stats, cudaStream_t stream) {
-    return launch_ai_t(a, P64, P32, prec, polish_maxiter, stats, stream);
+                      SolveOpts so, const WorkList& wl, const ReplayQueue& rq, DevStats* stats, cudaStream_t stream) {
+    return launch_ai_t(a, P64, P32, prec, so, wl, rq, stats, stream);
 }
 cudaError_t launch_ai(const AIArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
-                      int polish_maxiter, DevStats* stats, cudaStream_t stream) {
-    return launch_ai_t(a, P64, P32, prec, polish_maxiter, stats, stream);
+                      SolveOpts so, const WorkList& wl, const ReplayQueue& rq, DevStats* stats, cudaStream_t stream) {
+    return launch_ai_t(a, P64, P32, prec, so, wl, rq, stats, stream);
 }
 
 }  // namespace nesf

@@ -1,126 +1,211 @@
 // nesf_ao.cu -- atmosphere-ocean similarity-theory solve.
 //
-// _compute_atmosphere_ocean_interface_state!  (InterfaceComputations/atmosphere_ocean_fluxes.jl:80-197)
-// _compute_atmosphere_sea_ice_interface_state! (InterfaceComputations/atmosphere_sea_ice_fluxes.jl:65-185)
+// _compute_atmosphere_ocean_interface_state! (InterfaceComputations/atmosphere_ocean_fluxes.jl:80-197)
 //
 // One thread per surface cell over the halo ring (0:nx+1, 0:ny+1), SoA loads of
 // the Oceananigans parent arrays (i fastest, so a warp reads 32 consecutive
-// cells of a row). Two precisions:
-//   PLAIN   every iteration in FP64 (the drop-in, parity with the CPU solver);
-//   POLISH  FP64 prologue for the loop invariants, the fixed point in FP32 until
-//           it converges (drift < tol) or stalls at FP32 resolution, then FP64
-//           fixed-point polish steps from the FP32 state for the stalled cells.
+// cells of a row). Pass 0 writes the land cells and compacts the others into a
+// work list split by stability class; pass 1 solves the listed cells (PLAIN:
+// FP64; POLISH: FP32 sweep + FP64 Newton); pass 2 replays, packed into full
+// warps, the POLISH cells that must follow the reference's FP64 iteration.
 #include "nesf_solve.cuh"
 
 namespace nesf {
 
-// ------------------------------------------------------------------ AO kernel
-template <class S, int PREC, bool SKIN>
-__device__ __forceinline__ void ao_cell(const DevIface<double>& P64, const DevIface<float>& P32, const AOArgs<S>& a,
-                                        int i, int j, int64_t moff, int polish_maxiter, DevStats* stats) {
-    const Layout2& L = a.L;
-    int64_t k = L.at(i, j) + moff;
-    CellConst<double> c;
+// assemble_interior_state + the atmosphere reads (atmosphere_ocean_fluxes.jl:62-71, 97-128)
+template <class S>
+__device__ __forceinline__ void ao_load(const DevIface<double>& P, const AOArgs<S>& a, int64_t k, bool skin,
+                                        CellConst<double>& c, bool& land) {
     c.ua = ld(a.ua, k); c.va = ld(a.va, k); c.Ta = ld(a.Ta, k); c.pa = ld(a.pa, k); c.qa = ld(a.qa, k);
-    // assemble_interior_state: centre averages of the face velocities (atmosphere_ocean_fluxes.jl:62-71)
-    c.ui = (ld(a.uo, k) + ld(a.uo, k + 1)) / 2;
-    c.vi = (ld(a.vo, k) + ld(a.vo, k + L.sj)) / 2;
-    c.Ti = ld(a.To, k) + P64.off_int;
+    c.ui = (ld(a.uo, k) + ld(a.uo, k + 1)) / 2;          // centre average of the x-face velocity
+    c.vi = (ld(a.vo, k) + ld(a.vo, k + a.L.sj)) / 2;     // centre average of the y-face velocity
+    c.Ti = ld(a.To, k) + P.off_int;
     c.Si = ld(a.So, k);
     c.hi = c.hs = c.hc = 0;
     c.sw = ldz(a.sw, k);
     c.lw = ldz(a.lw, k);
     c.kappa = a.kappa ? ld(a.kappa, k) : -1.0;
-    bool land = a.inactive ? a.inactive[k] != 0 : false;
-    if (P64.vel_form == NESF_WIND_VELOCITY) { c.du = c.ua; c.dv = c.va; }
+    land = a.inactive ? a.inactive[k] != 0 : false;
+    if (P.vel_form == NESF_WIND_VELOCITY) { c.du = c.ua; c.dv = c.va; }
     else { c.du = c.ua - c.ui; c.dv = c.va - c.vi; }
     c.dU2 = c.du * c.du + c.dv * c.dv;
-    c.tha = surface_atmosphere_temperature(P64, c.Ta, c.qa);
-    if (SKIN) {
-        c.rho_a = air_density(P64, c.Ta, c.pa, c.qa);
-        c.cp_a = cp_m(P64, c.qa);
-        c.L_s = latent_heat_sublim(P64, c.Ta);
+    c.tha = surface_atmosphere_temperature(P, c.Ta, c.qa);
+    if (skin) {
+        c.rho_a = air_density(P, c.Ta, c.pa, c.qa);
+        c.cp_a = cp_m(P, c.qa);
+        c.L_s = latent_heat_sublim(P, c.Ta);
     } else {
         c.rho_a = c.cp_a = c.L_s = 0;
     }
+}
 
-    double us = 1e-4, ts = 1e-4, qst = 1e-4;
-    double qs0 = surface_specific_humidity(P64, c.pa, c.Ti);
-    SurfaceConst<double> s;
-    surface_const(P64, c, c.Ti, qs0, s);
-    bool needs = P64.stop_kind == NESF_STOP_CONVERGENCE;
-    int iters = 0, piters = 0;
-    bool nonconv = false;
-    bool solved = !(needs && land);
-    if (solved) iters = solve_cell<PREC, SKIN>(P64, P32, c, s, us, ts, qst, polish_maxiter, nonconv, piters);
-    double Ts = s.Ts, ui = c.ui, vi = c.vi;
+// The flux epilogue (atmosphere_ocean_fluxes.jl:157-196).
+template <class S>
+__device__ __forceinline__ void ao_store(const DevIface<double>& P, const AOArgs<S>& a, int64_t k,
+                                         const CellConst<double>& c, bool land, double us, double ts, double qst,
+                                         double Ts, int iters) {
+    double ui = c.ui, vi = c.vi;
     if (land) {   // zero_interface_state (interface_states.jl:800-803)
         us = ts = qst = 0;
         Ts = 273.15;
         ui = vi = 0;
     }
     double du, dv;
-    if (P64.vel_form == NESF_WIND_VELOCITY) { du = c.ua; dv = c.va; }
+    if (P.vel_form == NESF_WIND_VELOCITY) { du = c.ua; dv = c.va; }
     else { du = c.ua - ui; dv = c.va - vi; }
     double dU = sqrt(du * du + dv * dv);
     double tx = dU == 0 ? 0.0 : -(us * us) * du / dU;
     double ty = dU == 0 ? 0.0 : -(us * us) * dv / dU;
-    double rho = air_density(P64, c.Ta, c.pa, c.qa);
-    double cp = cp_m(P64, c.qa);
-    double Lv = latent_heat_vapor(P64, c.Ta);
+    double rho = air_density(P, c.Ta, c.pa, c.qa);
+    double cp = cp_m(P, c.qa);
+    double Lv = latent_heat_vapor(P, c.Ta);
     st(a.Qv, k, -rho * Lv * us * qst);
     st(a.QT, k, -rho * cp * us * ts);
     st(a.Jv, k, -rho * us * qst);
     st(a.tx, k, rho * tx);
     st(a.ty, k, rho * ty);
-    st(a.Ts, k, Ts - P64.off_ifc);
+    st(a.Ts, k, Ts - P.off_ifc);
     st(a.us, k, us);
     st(a.ts, k, ts);
     st(a.qs, k, qst);
     if (a.iters) a.iters[k] = iters;
-    if (stats) stats_add(stats, true, solved, iters, nonconv, piters > 0, piters, false, 0);
 }
 
-template <class S, int PREC, bool SKIN, bool ENS>
-__global__ void __launch_bounds__(128, ENS ? 4 : 1) ao_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
-                                                 const DevIface<double>* __restrict__ P64s,
-                                                 const DevIface<float>* __restrict__ P32s, int polish_maxiter,
-                                                 DevStats* stats) {
+// Pass 0: land cells get the zero interface state; the others are compacted into
+// the member's work list by the sign class of their buoyancy flux.
+template <class S, bool ENS>
+__global__ void __launch_bounds__(128) ao_classify_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
+                                                          const DevIface<double>* __restrict__ P64s,
+                                                          const DevIface<float>* __restrict__ P32s, WorkList wl,
+                                                          DevStats* stats) {
     const int nxr = a.L.nx + 2;
     const int64_t ring = (int64_t)nxr * (a.L.ny + 2);
+    const int m = blockIdx.y;
+    const DevIface<double>& P = ENS ? P64s[m] : P64;
+    const DevIface<float>& Pf = ENS ? P32s[m] : P32;
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool in = r < ring;
+    int i = in ? (int)(r % nxr) : 0, j = in ? (int)(r / nxr) : 0;
+    int64_t k = a.L.at(i, j) + (int64_t)m * a.member_stride;
+    bool land = in && a.inactive ? a.inactive[k] != 0 : false;
+    bool needs = P.stop_kind == NESF_STOP_CONVERGENCE;
+    bool active = in && !land;
+    bool stable = false;
+    if (active) {
+        float Ts = (float)(ld(a.To, k) + P.off_int);
+        stable = stable_class(Pf, ldf(a.Ta, k), ldf(a.pa, k), ldf(a.qa, k), Ts);
+    }
+    worklist_push(wl, m, active, stable, (uint32_t)r);
+    if (in && land) {
+        CellConst<double> c;
+        bool l;
+        ao_load(P, a, k, false, c, l);
+        ao_store(P, a, k, c, true, 0.0, 0.0, 0.0, 273.15, needs ? 0 : P.maxiter);
+    }
+    if (stats && in && land) stats_add(stats, true, false, 0, false, false, 0, false, false);
+}
+
+// Pass 1: the compacted cells (unstable first, then stable), one thread each.
+template <class S, int PREC, bool SKIN, bool ENS>
+__global__ void __launch_bounds__(128, ENS ? 4 : 1) ao_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
+                                                              const DevIface<double>* __restrict__ P64s,
+                                                              const DevIface<float>* __restrict__ P32s, SolveOpts so,
+                                                              WorkList wl, ReplayQueue rq, DevStats* stats) {
+    const int nxr = a.L.nx + 2;
+    const int64_t ring = (int64_t)nxr * (a.L.ny + 2);
+    const int m = blockIdx.y;
+    __shared__ DevIface<double> sP64;
+    __shared__ DevIface<float> sP32;
     if (ENS) {
-        __shared__ DevIface<double> sP64;
-        __shared__ DevIface<float> sP32;
-        int m = blockIdx.y;
         if (threadIdx.x == 0) {
             sP64 = P64s[m];
             sP32 = P32s[m];
         }
         __syncthreads();
-        if (r < ring) {
-            int i = (int)(r % nxr), j = (int)(r / nxr);
-            ao_cell<S, PREC, SKIN>(sP64, sP32, a, i, j, (int64_t)m * a.member_stride, polish_maxiter, stats);
-        }
+    }
+    const DevIface<double>& Pd = ENS ? sP64 : P64;
+    const DevIface<float>& Pf = ENS ? sP32 : P32;
+    int64_t r = worklist_get(wl, m, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+    if (r < 0) return;
+    int i = (int)(r % nxr), j = (int)(r / nxr);
+    int64_t k = a.L.at(i, j) + (int64_t)m * a.member_stride;
+    CellConst<double> c;
+    bool land;
+    ao_load(Pd, a, k, SKIN, c, land);
+    double us = 1e-4, ts = 1e-4, qst = 1e-4;   // initial guess (atmosphere_ocean_fluxes.jl:132)
+    double qs0 = surface_specific_humidity(Pd, c.pa, c.Ti);
+    SurfaceConst<double> s;
+    surface_const(Pd, c, c.Ti, qs0, s);
+    bool needs = Pd.stop_kind == NESF_STOP_CONVERGENCE;
+    int iters = 0, f64it = 0;
+    bool nonconv = false, polished = false, replay = false;
+    int reason = -1;
+    if (PREC == NESF_PLAIN_F64 || !needs) {
+        iters = solve_plain<SKIN>(Pd, c, s, us, ts, qst, nonconv);
     } else {
-        if (r < ring) {
-            int i = (int)(r % nxr), j = (int)(r / nxr);
-            ao_cell<S, PREC, SKIN>(P64, P32, a, i, j, 0, polish_maxiter, stats);
+        int f32it;
+        polished = solve_fast<SKIN>(Pd, Pf, c, s, us, ts, qst, so, f32it, f64it, reason);
+        iters = f32it + f64it;
+        replay = !polished;
+    }
+    if (PREC != NESF_PLAIN_F64) replay_push(rq, replay, (uint32_t)(m * ring + r));
+    if (replay) {
+        if (stats) {
+            stats_add(stats, true, false, 0, false, false, 0, true, false);
+            stats_replay_reason(stats, reason);
         }
+        return;
+    }
+    ao_store(Pd, a, k, c, false, us, ts, qst, s.Ts, iters);
+    if (stats) stats_add(stats, true, true, iters, nonconv, polished, f64it, false, false);
+}
+
+// Pass 2: the queued cells, packed, through the reference's FP64 iteration.
+template <class S, bool SKIN>
+__global__ void __launch_bounds__(128) ao_replay_kernel(AOArgs<S> a, DevIface<double> P64,
+                                                        const DevIface<double>* __restrict__ P64s, ReplayQueue rq,
+                                                        DevStats* stats) {
+    const int nxr = a.L.nx + 2;
+    const int64_t ring = (int64_t)nxr * (a.L.ny + 2);
+    const unsigned n = *rq.count;
+    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n && (int64_t)q < rq.capacity;
+         q += gridDim.x * blockDim.x) {
+        uint32_t id = rq.idx[q];
+        int64_t m = (int64_t)id / ring, r = (int64_t)id % ring;
+        const DevIface<double>& P = P64s ? P64s[m] : P64;
+        int i = (int)(r % nxr), j = (int)(r / nxr);
+        int64_t k = a.L.at(i, j) + m * a.member_stride;
+        CellConst<double> c;
+        bool land;
+        ao_load(P, a, k, SKIN, c, land);
+        double us = 1e-4, ts = 1e-4, qst = 1e-4;
+        double qs0 = surface_specific_humidity(P, c.pa, c.Ti);
+        SurfaceConst<double> s;
+        surface_const(P, c, c.Ti, qs0, s);
+        bool nonconv;
+        int it = solve_plain<SKIN>(P, c, s, us, ts, qst, nonconv);
+        ao_store(P, a, k, c, false, us, ts, qst, s.Ts, it);
+        if (stats) stats_add(stats, false, true, it, nonconv, false, it, false, false);
     }
 }
 
 template <class S>
 static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                                const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec,
-                               bool skin, int polish_maxiter, DevStats* stats, int block, cudaStream_t stream) {
+                               bool skin, SolveOpts so, const WorkList& wl, const ReplayQueue& rq, DevStats* stats,
+                               cudaStream_t stream) {
     const int64_t ring = (int64_t)(a.L.nx + 2) * (a.L.ny + 2);
-    if (block <= 0) block = 128;
-    block = 128;   // kernels are compiled with __launch_bounds__(128)
-    dim3 grid((unsigned)((ring + block - 1) / block), members > 1 ? members : 1);
+    const int threads = 128;   // kernels are compiled with __launch_bounds__(128)
+    const int nm = members > 1 ? members : 1;
+    dim3 grid((unsigned)((ring + threads - 1) / threads), nm);
     bool ens = members > 1 || P64s != nullptr;
+    cudaError_t e = cudaMemsetAsync(wl.count, 0, sizeof(unsigned) * 2 * nm, stream);
+    if (e == cudaSuccess && prec != NESF_PLAIN_F64) e = cudaMemsetAsync(rq.count, 0, sizeof(unsigned), stream);
+    if (e != cudaSuccess) return e;
+    if (ens) ao_classify_kernel<S, true><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, stats);
+    else ao_classify_kernel<S, false><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, stats);
 #define NESF_AO_LAUNCH(PR, SK, EN) \
-    ao_kernel<S, PR, SK, EN><<<grid, block, 0, stream>>>(a, P64, P32, P64s, P32s, polish_maxiter, stats)
+    ao_kernel<S, PR, SK, EN><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, so, wl, rq, stats)
 #define NESF_AO_ENS(PR, SK) \
     do { if (ens) NESF_AO_LAUNCH(PR, SK, true); else NESF_AO_LAUNCH(PR, SK, false); } while (0)
 #define NESF_AO_SKIN(PR) \
@@ -130,18 +215,28 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
 #undef NESF_AO_SKIN
 #undef NESF_AO_ENS
 #undef NESF_AO_LAUNCH
+    e = cudaGetLastError();
+    if (e != cudaSuccess || prec == NESF_PLAIN_F64) return e;
+    // pass 2: enough resident blocks to sweep the queue (grid-stride)
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    unsigned g2 = (unsigned)sms * 4;
+    const DevIface<double>* pm = ens ? P64s : nullptr;
+    if (skin) ao_replay_kernel<S, true><<<g2, threads, 0, stream>>>(a, P64, pm, rq, stats);
+    else ao_replay_kernel<S, false><<<g2, threads, 0, stream>>>(a, P64, pm, rq, stats);
     return cudaGetLastError();
 }
 
 cudaError_t launch_ao(const AOArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
-                      int polish_maxiter, DevStats* stats, int block, cudaStream_t stream) {
-    return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, polish_maxiter, stats, block, stream);
+                      SolveOpts so, const WorkList& wl, const ReplayQueue& rq, DevStats* stats, cudaStream_t stream) {
+    return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, stats, stream);
 }
 cudaError_t launch_ao(const AOArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
-                      int polish_maxiter, DevStats* stats, int block, cudaStream_t stream) {
-    return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, polish_maxiter, stats, block, stream);
+                      SolveOpts so, const WorkList& wl, const ReplayQueue& rq, DevStats* stats, cudaStream_t stream) {
+    return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, stats, stream);
 }
 
 }  // namespace nesf

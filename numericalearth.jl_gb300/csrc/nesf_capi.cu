@@ -20,6 +20,13 @@ struct nesf_context {
     DevIface<double>* d_p64;    // per-member parameters (ensemble)
     DevIface<float>* d_p32;
     int32_t capacity_members;
+    uint32_t* d_replay;         // replay queue of the FP32 + polish solver
+    unsigned int* d_replay_count;
+    int64_t replay_capacity;
+    uint32_t* d_work;           // compacted work lists of the solves
+    unsigned int* d_work_count; // two counters per ensemble member
+    int64_t work_capacity;
+    int32_t work_members;
     std::mutex lock;            // serialises use of the scratch above
 };
 
@@ -216,13 +223,14 @@ void nesf_default_assembly_params(nesf_assembly_params* p) {
 void nesf_default_solver_options(nesf_solver_options* o) {
     memset(o, 0, sizeof *o);
     o->precision = NESF_PLAIN_F64;
-    o->polish_maxiter = 1;
+    o->polish_maxiter = 3;
     o->block_size = 128;
     o->schedule = 0;
     o->ctas_per_sm = 0;
     o->warm_start = 0;
     o->mlp = nullptr;
     o->fallback_ratio = 10.0;
+    o->path_tolerance = 2e-6;
 }
 
 // ---------------------------------------------------------------- context
@@ -240,7 +248,14 @@ int nesf_context_create(int32_t device, nesf_context** out) {
     c->capacity_members = 0;
     c->d_p64 = nullptr;
     c->d_p32 = nullptr;
+    c->d_replay = nullptr;
+    c->replay_capacity = 0;
+    c->d_work = nullptr;
+    c->d_work_count = nullptr;
+    c->work_capacity = 0;
+    c->work_members = 0;
     cudaError_t e = cudaMalloc(&c->d_stats, sizeof(DevStats));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_replay_count, sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_stats, sizeof(DevStats));
     if (e != cudaSuccess) {
         cudaFree(c->d_stats);
@@ -259,6 +274,10 @@ int nesf_context_destroy(nesf_context* c) {
         cudaFreeHost(c->h_stats);
         cudaFree(c->d_p64);
         cudaFree(c->d_p32);
+        cudaFree(c->d_replay);
+        cudaFree(c->d_replay_count);
+        cudaFree(c->d_work);
+        cudaFree(c->d_work_count);
     }
     delete c;
     return NESF_OK;
@@ -304,6 +323,7 @@ static nesf_solver_options options_or_default(const nesf_solver_options* o) {
     if (!o) return d;
     nesf_solver_options r = *o;
     if (r.polish_maxiter <= 0) r.polish_maxiter = d.polish_maxiter;
+    if (!(r.path_tolerance > 0)) r.path_tolerance = d.path_tolerance;
     return r;
 }
 
@@ -311,6 +331,67 @@ static int check_options(const nesf_solver_options& o, const char* who) {
     if (o.precision != NESF_PLAIN_F64 && o.precision != NESF_F32_POLISH)
         return fail(NESF_ERR_ARG, "%s: precision %d", who, o.precision);
     if (o.warm_start) return fail(NESF_ERR_UNSUPPORTED, "%s: warm start needs nesf_coupling_step", who);
+    return NESF_OK;
+}
+
+// The context's replay queue, grown to `cells` entries (caller holds ctx->lock).
+// Growing synchronises the device: size the first call for the largest grid.
+static int replay_queue(nesf_context* ctx, int64_t cells, ReplayQueue* q) {
+    if (cells > ctx->replay_capacity) {
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) return cuda_fail(e, "replay queue");
+        cudaFree(ctx->d_replay);
+        ctx->d_replay = nullptr;
+        ctx->replay_capacity = 0;
+        NESF_CUDA(cudaMalloc(&ctx->d_replay, sizeof(uint32_t) * (size_t)cells));
+        ctx->replay_capacity = cells;
+    }
+    q->idx = ctx->d_replay;
+    q->count = ctx->d_replay_count;
+    q->capacity = ctx->replay_capacity;
+    return NESF_OK;
+}
+
+// The context's work lists: `members` segments of `per_member` entries.
+static int work_list(nesf_context* ctx, int64_t per_member, int32_t members, WorkList* w) {
+    int64_t need = per_member * members;
+    if (need > ctx->work_capacity || members > ctx->work_members) {
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) return cuda_fail(e, "work list");
+        cudaFree(ctx->d_work);
+        cudaFree(ctx->d_work_count);
+        ctx->d_work = nullptr;
+        ctx->d_work_count = nullptr;
+        ctx->work_capacity = 0;
+        ctx->work_members = 0;
+        int64_t cap = need > ctx->work_capacity ? need : ctx->work_capacity;
+        int32_t mem = members > ctx->work_members ? members : ctx->work_members;
+        NESF_CUDA(cudaMalloc(&ctx->d_work, sizeof(uint32_t) * (size_t)cap));
+        NESF_CUDA(cudaMalloc(&ctx->d_work_count, sizeof(unsigned int) * 2 * (size_t)mem));
+        ctx->work_capacity = cap;
+        ctx->work_members = mem;
+    }
+    w->idx = ctx->d_work;
+    w->count = ctx->d_work_count;
+    w->per_member = per_member;
+    return NESF_OK;
+}
+
+// Library-owned context of the current device, for calls that pass none.
+static nesf_context* g_default_ctx[64];
+static std::mutex g_default_lock;
+
+static int context_or_default(nesf_context** ctx) {
+    if (*ctx) return NESF_OK;
+    int dev = 0;
+    NESF_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(NESF_ERR_ARG, "device %d", dev);
+    std::lock_guard<std::mutex> lk(g_default_lock);
+    if (!g_default_ctx[dev]) {
+        int r = nesf_context_create(dev, &g_default_ctx[dev]);
+        if (r) return r;
+    }
+    *ctx = g_default_ctx[dev];
     return NESF_OK;
 }
 
@@ -323,6 +404,8 @@ static void stats_to_public(const DevStats& d, nesf_stats* s) {
     s->polished = (int64_t)d.polished;
     s->polish_iterations = (int64_t)d.polish_iterations;
     s->cold_fallbacks = (int64_t)d.cold_fallbacks;
+    s->fp64_redo = (int64_t)d.fp64_redo;
+    for (int k = 0; k < 5; k++) s->replay_reasons[k] = (int64_t)d.replay_reasons[k];
     for (int k = 0; k < NESF_ITER_HIST_BINS; k++) s->histogram[k] = (int64_t)d.hist[k];
 }
 
@@ -331,7 +414,6 @@ template <class F>
 static int with_stats(nesf_context* ctx, nesf_stats* stats, cudaStream_t s, F launch) {
     DevStats* ds = nullptr;
     if (stats) {
-        if (!ctx) return fail(NESF_ERR_ARG, "statistics need a context");
         ds = ctx->d_stats;
         NESF_CUDA(cudaMemsetAsync(ds, 0, sizeof(DevStats), s));
     }
@@ -388,19 +470,24 @@ extern "C" int nesf_compute_atmosphere_ocean_fluxes(nesf_context* ctx, const nes
     if ((r = check_ao_fields(f, params, who))) return r;
     nesf_solver_options o = options_or_default(opts);
     if ((r = check_options(o, who))) return r;
-    std::unique_lock<std::mutex> lk;
-    if (ctx) lk = std::unique_lock<std::mutex>(ctx->lock);
-    DeviceGuard g(ctx ? ctx->device : 0);
+    if ((r = context_or_default(&ctx))) return r;
+    std::lock_guard<std::mutex> lk(ctx->lock);
+    DeviceGuard g(ctx->device);
     DevIface<double> P64 = make_dev_iface<double>(*params);
     DevIface<float> P32 = make_dev_iface<float>(*params);
     cudaStream_t s = (cudaStream_t)stream;
     bool skin = params->temperature_formulation != NESF_BULK_TEMPERATURE;
+    int64_t ring = (int64_t)(f->grid.nx + 2) * (f->grid.ny + 2);
+    ReplayQueue rq;
+    WorkList wl;
+    if ((r = replay_queue(ctx, ring, &rq))) return r;
+    if ((r = work_list(ctx, ring, 1, &wl))) return r;
+    SolveOpts so{o.polish_maxiter, (float)o.path_tolerance};
     return with_stats(ctx, stats, s, [&](DevStats* ds) {
         if (f->dtype == NESF_F64)
-            return launch_ao(ao_args<double>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin,
-                             o.polish_maxiter, ds, o.block_size, s);
-        return launch_ao(ao_args<float>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, o.polish_maxiter,
-                         ds, o.block_size, s);
+            return launch_ao(ao_args<double>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl, rq, ds,
+                             s);
+        return launch_ao(ao_args<float>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl, rq, ds, s);
     });
 }
 
@@ -452,12 +539,19 @@ extern "C" int nesf_compute_atmosphere_ocean_fluxes_ensemble(nesf_context* ctx, 
     DevIface<double> P64 = make_dev_iface<double>(params[0]);
     DevIface<float> P32 = make_dev_iface<float>(params[0]);
     bool skin = params->temperature_formulation != NESF_BULK_TEMPERATURE;
+    int64_t ring = (int64_t)(f->grid.nx + 2) * (f->grid.ny + 2);
+    if (ring * members > 0xffffffffLL) return fail(NESF_ERR_CAPACITY, "%s: too many cells for the queue", who);
+    ReplayQueue rq;
+    WorkList wl;
+    if ((r = replay_queue(ctx, ring * members, &rq))) return r;
+    if ((r = work_list(ctx, ring, members, &wl))) return r;
+    SolveOpts so{o.polish_maxiter, (float)o.path_tolerance};
     return with_stats(ctx, stats, s, [&](DevStats* ds) {
         if (f->dtype == NESF_F64)
             return launch_ao(ao_args<double>(f, member_stride), P64, P32, ctx->d_p64, ctx->d_p32, members,
-                             o.precision, skin, o.polish_maxiter, ds, o.block_size, s);
+                             o.precision, skin, so, wl, rq, ds, s);
         return launch_ao(ao_args<float>(f, member_stride), P64, P32, ctx->d_p64, ctx->d_p32, members, o.precision,
-                         skin, o.polish_maxiter, ds, o.block_size, s);
+                         skin, so, wl, rq, ds, s);
     });
 }
 
@@ -501,15 +595,21 @@ extern "C" int nesf_compute_atmosphere_sea_ice_fluxes(nesf_context* ctx, const n
         return fail(NESF_ERR_ARG, "%s: radiation enabled but sw_down/lw_down NULL", who);
     nesf_solver_options o = options_or_default(opts);
     if ((r = check_options(o, who))) return r;
-    std::unique_lock<std::mutex> lk;
-    if (ctx) lk = std::unique_lock<std::mutex>(ctx->lock);
-    DeviceGuard g(ctx ? ctx->device : 0);
+    if ((r = context_or_default(&ctx))) return r;
+    std::lock_guard<std::mutex> lk(ctx->lock);
+    DeviceGuard g(ctx->device);
     DevIface<double> P64 = make_dev_iface<double>(*params);
     DevIface<float> P32 = make_dev_iface<float>(*params);
     cudaStream_t s = (cudaStream_t)stream;
+    int64_t ring = (int64_t)(f->grid.nx + 2) * (f->grid.ny + 2);
+    ReplayQueue rq;
+    WorkList wl;
+    if ((r = replay_queue(ctx, ring, &rq))) return r;
+    if ((r = work_list(ctx, ring, 1, &wl))) return r;
+    SolveOpts so{o.polish_maxiter, (float)o.path_tolerance};
     return with_stats(ctx, stats, s, [&](DevStats* ds) {
-        if (f->dtype == NESF_F64) return launch_ai(ai_args<double>(f), P64, P32, o.precision, o.polish_maxiter, ds, s);
-        return launch_ai(ai_args<float>(f), P64, P32, o.precision, o.polish_maxiter, ds, s);
+        if (f->dtype == NESF_F64) return launch_ai(ai_args<double>(f), P64, P32, o.precision, so, wl, rq, ds, s);
+        return launch_ai(ai_args<float>(f), P64, P32, o.precision, so, wl, rq, ds, s);
     });
 }
 

@@ -25,8 +25,13 @@ template <> struct M<double> {
     static __device__ __forceinline__ double atan(double x) { return ::atan(x); }
     static __device__ __forceinline__ double cbrt(double x) { return ::cbrt(x); }
     static __device__ __forceinline__ double sqrt(double x) { return ::sqrt(x); }
-    static __device__ __forceinline__ double fmin(double a, double b) { return ::fmin(a, b); }
-    static __device__ __forceinline__ double fmax(double a, double b) { return ::fmax(a, b); }
+    // Julia's min / max: NaN-propagating, -0.0 < 0.0
+    static __device__ __forceinline__ double fmin(double x, double y) {
+        return (isnan(x) || isnan(y)) ? x + y : (x == y ? (signbit(x) ? x : y) : (x < y ? x : y));
+    }
+    static __device__ __forceinline__ double fmax(double x, double y) {
+        return (isnan(x) || isnan(y)) ? x + y : (x == y ? (signbit(x) ? y : x) : (x > y ? x : y));
+    }
     static __device__ __forceinline__ double fabs(double a) { return ::fabs(a); }
     static __device__ __forceinline__ double inf() { return __longlong_as_double(0x7ff0000000000000LL); }
 };
@@ -37,8 +42,12 @@ template <> struct M<float> {
     static __device__ __forceinline__ float atan(float x) { return ::atanf(x); }
     static __device__ __forceinline__ float cbrt(float x) { return ::cbrtf(x); }
     static __device__ __forceinline__ float sqrt(float x) { return ::sqrtf(x); }
-    static __device__ __forceinline__ float fmin(float a, float b) { return ::fminf(a, b); }
-    static __device__ __forceinline__ float fmax(float a, float b) { return ::fmaxf(a, b); }
+    static __device__ __forceinline__ float fmin(float x, float y) {
+        return (isnan(x) || isnan(y)) ? x + y : (x == y ? (signbit(x) ? x : y) : (x < y ? x : y));
+    }
+    static __device__ __forceinline__ float fmax(float x, float y) {
+        return (isnan(x) || isnan(y)) ? x + y : (x == y ? (signbit(x) ? y : x) : (x > y ? x : y));
+    }
     static __device__ __forceinline__ float fabs(float a) { return ::fabsf(a); }
     static __device__ __forceinline__ float inf() { return __int_as_float(0x7f800000); }
 };
@@ -134,7 +143,7 @@ __device__ __noinline__ R psi_edson_momentum(const DevStab<R> s, R z) {   // :50
     const R* c = s.c;
     if (z < R(0)) {
         R Am = c[5], Bm = c[6], Cm = c[7], Dm = c[8], Em = c[9], Fm = c[10];
-        R zm = z;
+        R zm = M<R>::fmin(R(0), z);
         R f1 = M<R>::sqrt(M<R>::sqrt(R(1) - Am * zm));
         R psi1 = Bm * M<R>::log((R(1) + f1) / Bm) + M<R>::log((R(1) + f1 * f1) / Bm) - Bm * M<R>::atan(f1) + Cm;
         R f2 = M<R>::cbrt(R(1) - Dm * zm);
@@ -144,7 +153,7 @@ __device__ __noinline__ R psi_edson_momentum(const DevStab<R> s, R z) {   // :50
         return (R(1) - f) * psi1 + f * psi2;
     } else {
         R zmax = c[0], Ap = c[1], Bp = c[2], Cp = c[3], Dp = c[4];
-        R zp = z;
+        R zp = M<R>::fmax(R(0), z);
         R dz = M<R>::fmin(zmax, Ap * zp);
         return -Bp * zp - Cp * (zp - Dp) * M<R>::exp(-dz) - Cp * Dp;
     }
@@ -155,7 +164,7 @@ __device__ __noinline__ R psi_edson_scalar(const DevStab<R> s, R z) {     // :58
     const R* c = s.c;
     if (z < R(0)) {
         R Am = c[6], Bm = c[7], Cm = c[8], Dm = c[9], Em = c[10], Fm = c[11];
-        R zm = z;
+        R zm = M<R>::fmin(R(0), z);
         R f1 = M<R>::sqrt(R(1) - Am * zm);
         R psi1 = Bm * M<R>::log((R(1) + f1) / Bm) + Cm;
         R f2 = M<R>::cbrt(R(1) - Dm * zm);
@@ -165,7 +174,7 @@ __device__ __noinline__ R psi_edson_scalar(const DevStab<R> s, R z) {     // :58
         return (R(1) - f) * psi1 + f * psi2;
     } else {
         R zmax = c[0], Ap = c[1], Bp = c[2], Cp = c[3], Dp = c[4], Ep = c[5];
-        R zp = z;
+        R zp = M<R>::fmax(R(0), z);
         R dz = M<R>::fmin(zmax, Ap * zp);
         return -M<R>::pow(R(1) + Bp * zp, Cp) - Bp * (zp - Dp) * M<R>::exp(-dz) - Ep;
     }
@@ -351,14 +360,18 @@ __device__ __forceinline__ void iterate_fluxes(const DevIface<R>& P, const CellC
     qs_n = chiq * s.dq;
 }
 
+// Julia clamp: ifelse(x > hi, hi, ifelse(x < lo, lo, x))
 template <class R> __device__ __forceinline__ R clampr(R x, R lo, R hi) {
-    return M<R>::fmin(M<R>::fmax(x, lo), hi);
+    return x > hi ? hi : (x < lo ? lo : x);
 }
 
 // compute_interface_temperature(::SkinTemperature) (interface_states.jl:526-577) with
 // flux_balance_temperature (434-457 diffusive, 468-524 conductive ice/snow).
+// `pinned` is set when the result is fixed by the melting-point cap or the
+// unconsolidated-ice branch (T_s does not depend on the fluxes there).
 template <class R>
-__device__ __forceinline__ R skin_temperature(const DevIface<R>& P, const CellConst<R>& c, R Tm1, R us, R ts, R qst) {
+__device__ __forceinline__ R skin_temperature(const DevIface<R>& P, const CellConst<R>& c, R Tm1, R us, R ts, R qst,
+                                              bool* pinned = nullptr) {
     R sigma = P.has_rad ? P.sigma : R(0);
     R eps = P.has_rad ? P.emis : R(0);
     R alb = P.has_rad ? P.alb : R(0);
@@ -396,6 +409,7 @@ __device__ __forceinline__ R skin_temperature(const DevIface<R>& P, const CellCo
     Tst = isnan(Tst) ? Tm1 : Tst;
     R Tp = Tm1 + clampr(Tst - Tm1, -P.max_dT, P.max_dT);
     R Tm = P.Tfw + P.off_ifc;
+    if (pinned) *pinned = !(Tp < Tm) || !(c.hi >= c.hc);
     Tp = M<R>::fmin(Tp, Tm);
     return c.hi >= c.hc ? Tp : Tb;
 }
@@ -404,9 +418,9 @@ __device__ __forceinline__ R skin_temperature(const DevIface<R>& P, const CellCo
 // formulation `s` is fixed; for skin formulations it is rebuilt from the new T_s.
 template <class R, bool SKIN>
 __device__ __forceinline__ void iterate_state(const DevIface<R>& P, const CellConst<R>& c, SurfaceConst<R>& s,
-                                              R& us, R& ts, R& qst) {
+                                              R& us, R& ts, R& qst, bool* pinned = nullptr) {
     if (SKIN) {
-        R Ts = skin_temperature(P, c, s.Ts, us, ts, qst);
+        R Ts = skin_temperature(P, c, s.Ts, us, ts, qst, pinned);
         R qs = surface_specific_humidity(P, c.pa, Ts);
         surface_const(P, c, Ts, qs, s);
     }

@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(256) io_kernel(IOArgs<S> a, nesf_io_params p) 
         double qb = -gam - eta * TN - kap * Ti + th * (l2 - l1 * Si);
         double qc = gam * SN + (eta * TN + kap * Ti - th * l2) * Si;
         double xi = qa == 0 ? 0.0 : 1 / (2 * qa);
-        double D = fmax(qb * qb - 4 * qa * qc, 0.0);
+        double D = M<double>::fmax(qb * qb - 4 * qa * qc, 0.0);   // Julia max
         double Ss = (-qb - sqrt(D)) * xi;
         Ss = Ss < 0 ? (-qb + sqrt(D)) * xi : Ss;
         double Ts = l2 - p.liquidus_slope * Ss;

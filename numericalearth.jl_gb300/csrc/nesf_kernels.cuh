@@ -85,14 +85,14 @@ template <class S, class R> __device__ __forceinline__ void st(S* p, int64_t k, 
 // --------------------------------------------------------------- statistics
 struct DevStats {
     unsigned long long cells, solved, iterations, max_iterations, nonconverged, polished, polish_iterations,
-        cold_fallbacks;
+        cold_fallbacks, fp64_redo;
+    unsigned long long replay_reasons[5];
     unsigned long long hist[NESF_ITER_HIST_BINS];
 };
 
 // Accumulate one cell's statistics through warp-aggregated atomics.
 __device__ __forceinline__ void stats_add(DevStats* S, bool active, bool solved, int iters, bool nonconv,
-                                          bool polished, int piters, bool fallback, int maxiter_limit) {
-    (void)maxiter_limit;
+                                          bool polished, int piters, bool redo, bool fallback) {
     unsigned mask = __activemask();
     unsigned a = __reduce_add_sync(mask, active ? 1u : 0u);
     unsigned s = __reduce_add_sync(mask, solved ? 1u : 0u);
@@ -102,6 +102,7 @@ __device__ __forceinline__ void stats_add(DevStats* S, bool active, bool solved,
     unsigned po = __reduce_add_sync(mask, polished ? 1u : 0u);
     unsigned pi = __reduce_add_sync(mask, (unsigned)piters);
     unsigned fb = __reduce_add_sync(mask, fallback ? 1u : 0u);
+    unsigned rd = __reduce_add_sync(mask, redo ? 1u : 0u);
     int lane = threadIdx.x & 31;
     int leader = __ffs(mask) - 1;
     if (lane == leader) {
@@ -113,11 +114,17 @@ __device__ __forceinline__ void stats_add(DevStats* S, bool active, bool solved,
         if (po) atomicAdd(&S->polished, (unsigned long long)po);
         if (pi) atomicAdd(&S->polish_iterations, (unsigned long long)pi);
         if (fb) atomicAdd(&S->cold_fallbacks, (unsigned long long)fb);
+        if (rd) atomicAdd(&S->fp64_redo, (unsigned long long)rd);
     }
     // histogram: lanes with the same bin add once through their group leader
     int bin = solved ? (iters < NESF_ITER_HIST_BINS ? iters : NESF_ITER_HIST_BINS - 1) : -1;
     unsigned grp = __match_any_sync(mask, bin);
     if (solved && lane == __ffs(grp) - 1) atomicAdd(&S->hist[bin], (unsigned long long)__popc(grp));
+}
+
+// Count a deferred replay by its reason (0..4).
+__device__ __forceinline__ void stats_replay_reason(DevStats* S, int reason) {
+    if (reason >= 0 && reason < 5) atomicAdd(&S->replay_reasons[reason], 1ull);
 }
 
 }  // namespace nesf

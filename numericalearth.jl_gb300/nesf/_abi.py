@@ -108,13 +108,13 @@ class InterfaceParams(C.Structure):
 
 class SolverOptions(C.Structure):
     _fields_ = [("precision", i32), ("polish_maxiter", i32), ("block_size", i32), ("schedule", i32),
-                ("ctas_per_sm", i32), ("warm_start", i32), ("mlp", vp), ("fallback_ratio", d)]
+                ("ctas_per_sm", i32), ("warm_start", i32), ("mlp", vp), ("fallback_ratio", d), ("path_tolerance", d)]
 
 
 class Stats(C.Structure):
     _fields_ = [("cells", i64), ("solved", i64), ("iterations", i64), ("max_iterations", i64),
                 ("nonconverged", i64), ("polished", i64), ("polish_iterations", i64),
-                ("cold_fallbacks", i64), ("histogram", i64 * ITER_HIST_BINS)]
+                ("cold_fallbacks", i64), ("fp64_redo", i64), ("replay_reasons", i64 * 5), ("histogram", i64 * ITER_HIST_BINS)]
 
 
 class AOFields(C.Structure):

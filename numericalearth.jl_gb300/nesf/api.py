@@ -1,0 +1,242 @@
+"""Host API: the reference's interface-flux entry points over libnesf.so.
+
+Names follow NumericalEarth.jl (`compute_atmosphere_ocean_fluxes!` becomes
+`compute_atmosphere_ocean_fluxes`, `update_state!` becomes `update_state`).
+Arrays are torch CUDA tensors in the Oceananigans parent layout; torch only
+provides device memory and streams, all arithmetic runs in libnesf.so.
+"""
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Dict, Optional
+
+import numpy as np
+
+from . import _abi as A
+from . import fields as F
+from . import params as P
+from ._lib import check, load
+
+PRECISIONS = {"f64": A.PLAIN_F64, "plain": A.PLAIN_F64, "f32": A.F32_POLISH, "f32_polish": A.F32_POLISH}
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("nesf needs a CUDA device: there is no CPU path")
+    return torch
+
+
+def _stream_handle(stream):
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+class Context:
+    """Library-owned scratch (statistics, ensemble parameters) for one device."""
+
+    def __init__(self, device=0):
+        self.lib = load()
+        h = C.c_void_p()
+        check(self.lib.nesf_context_create(int(device), C.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if self.handle:
+            self.lib.nesf_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_DEFAULT_CTX = {}
+
+
+def default_context(device=None):
+    torch = _torch()
+    dev = torch.cuda.current_device() if device is None else device
+    if dev not in _DEFAULT_CTX:
+        _DEFAULT_CTX[dev] = Context(dev)
+    return _DEFAULT_CTX[dev]
+
+
+def solver_options(precision="f64", polish_maxiter=0, block_size=128, schedule=0):
+    o = A.SolverOptions()
+    load().nesf_default_solver_options(C.byref(o))
+    o.precision = PRECISIONS[precision]
+    o.polish_maxiter = polish_maxiter
+    o.block_size = block_size
+    o.schedule = schedule
+    return o
+
+
+def stats_dict(s):
+    return {"cells": s.cells, "solved": s.solved, "iterations": s.iterations, "max_iterations": s.max_iterations,
+            "nonconverged": s.nonconverged, "polished": s.polished, "polish_iterations": s.polish_iterations,
+            "cold_fallbacks": s.cold_fallbacks, "fp64_redo": s.fp64_redo, "replay_reasons": list(s.replay_reasons), "histogram": np.array(s.histogram[:], dtype=np.int64)}
+
+
+def _grid_of(layout):
+    return F.make_grid(layout)
+
+
+def compute_atmosphere_ocean_fluxes(spec, layout, state, out, precision="f64", polish_maxiter=0, stats=False,
+                                    iterations=None, ctx=None, stream=None):
+    """atmosphere_ocean_fluxes.jl:17-60 on device tensors. `state` holds AO inputs
+    (fields.AO_INPUTS), `out` the AtmosphereSurfaceFluxes + interface temperature."""
+    lib = load()
+    arrays = {k: state.get(k) for k in F.AO_INPUTS}
+    arrays.update({k: out.get(k) for k in F.AO_OUTPUTS})
+    arrays["iterations"] = iterations
+    f = F.pack(A.AOFields, _grid_of(layout), arrays)
+    p = spec.to_c() if hasattr(spec, "to_c") else spec
+    o = solver_options(precision, polish_maxiter)
+    st = A.Stats() if stats else None
+    ctx = ctx or default_context()
+    check(lib.nesf_compute_atmosphere_ocean_fluxes(ctx.handle, C.byref(p), C.byref(f), C.byref(o),
+                                                   C.byref(st) if st is not None else None, _stream_handle(stream)))
+    return stats_dict(st) if st is not None else None
+
+
+def compute_atmosphere_ocean_fluxes_ensemble(specs, layout, state, out, precision="f32", polish_maxiter=0,
+                                             stats=False, iterations=None, ctx=None, stream=None):
+    """Members stacked along the first tensor dimension, each with its own parameters."""
+    lib = load()
+    members = len(specs)
+    arrays = {k: state.get(k) for k in F.AO_INPUTS}
+    arrays.update({k: out.get(k) for k in F.AO_OUTPUTS})
+    arrays["iterations"] = iterations
+    f = F.pack(A.AOFields, _grid_of(layout), arrays)
+    ps = (A.InterfaceParams * members)(*[s.to_c() if hasattr(s, "to_c") else s for s in specs])
+    stride = layout.shape[0] * layout.shape[1]
+    o = solver_options(precision, polish_maxiter)
+    st = A.Stats() if stats else None
+    ctx = ctx or default_context()
+    check(lib.nesf_compute_atmosphere_ocean_fluxes_ensemble(ctx.handle, ps, members, stride, C.byref(f), C.byref(o),
+                                                            C.byref(st) if st is not None else None,
+                                                            _stream_handle(stream)))
+    return stats_dict(st) if st is not None else None
+
+
+def compute_atmosphere_sea_ice_fluxes(spec, layout, state, out, precision="f64", polish_maxiter=0, stats=False,
+                                      iterations=None, ctx=None, stream=None):
+    """atmosphere_sea_ice_fluxes.jl:18-62; `out['interface_temperature']` is read as the
+    initial skin temperature and overwritten with the solved one."""
+    lib = load()
+    arrays = {k: state.get(k) for k in F.AI_INPUTS}
+    arrays.update({k: out.get(k) for k in F.AI_OUTPUTS})
+    arrays["interface_temperature"] = out["interface_temperature"]
+    arrays["iterations"] = iterations
+    f = F.pack(A.AIFields, _grid_of(layout), arrays)
+    p = spec.to_c() if hasattr(spec, "to_c") else spec
+    o = solver_options(precision, polish_maxiter)
+    st = A.Stats() if stats else None
+    ctx = ctx or default_context()
+    check(lib.nesf_compute_atmosphere_sea_ice_fluxes(ctx.handle, C.byref(p), C.byref(f), C.byref(o),
+                                                     C.byref(st) if st is not None else None, _stream_handle(stream)))
+    return stats_dict(st) if st is not None else None
+
+
+def compute_sea_ice_ocean_fluxes(spec, layout, state, out, T3, S3, dz, stream=None, ctx=None):
+    """sea_ice_ocean_fluxes.jl:33-77. T3/S3: (nz, ny+2hy, nx+2hx) tensors; T3 is mutated
+    by frazil formation; dz: float64 tensor of nz layer thicknesses."""
+    lib = load()
+    nz = T3.shape[0] if T3.dim() == 3 else 1
+    stride_k = T3.shape[-1] * T3.shape[-2]
+    p = spec.to_c(nz=nz, stride_k=stride_k) if hasattr(spec, "to_c") else spec
+    arrays = {k: state.get(k) for k in ("ice_salinity", "ice_thickness", "consolidation_thickness",
+                                        "ice_concentration", "internal_temperature", "ice_mass_flux",
+                                        "snow_mass_flux")}
+    arrays.update({k: out.get(k) for k in F.IO_OUTPUTS})
+    arrays.update(T_oc=T3, S_oc=S3, dz=dz)
+    f = F.pack(A.IOFields, _grid_of(layout), arrays)
+    check(lib.nesf_compute_sea_ice_ocean_fluxes(ctx.handle if ctx else None, C.byref(p), C.byref(f),
+                                                _stream_handle(stream)))
+
+
+def atmos_grid_struct(atmos):
+    La, ca = atmos["layout"], atmos["coords"]
+    return A.AtmosGrid(La.nx, La.ny, La.hx, La.hy, La.stride_j, atmos["stride_t"], ca.lon0, ca.dlon, ca.lat0, ca.dlat)
+
+
+def exchange_coords(c):
+    return A.ExchangeCoords(c.lon0, c.dlon, c.lat0, c.dlat)
+
+
+INTERP_SRC = {"u": "u", "v": "v", "T": "T", "q": "q", "p": "p", "rain": "rain", "snow": "snow", "sw": "sw_down",
+              "lw": "lw_down"}
+INTERP_DST = {"u": "u_out", "v": "v_out", "T": "T_out", "q": "q_out", "p": "p_out", "rain": "rain_out",
+              "snow": "snow_out", "sw": "sw_out", "lw": "lw_out"}
+
+
+def interpolate_atmosphere_state(layout, coords, atmos, atmos_arrays, out, time_weight, frac=None, stream=None):
+    """interpolate_atmospheric_state.jl:9-137 + interpolate_radiation_state.jl:4-69.
+    `atmos_arrays` maps u v T q p rain snow sw lw to (2, ...) device tensors; `out` maps
+    the same names to exchange-grid tensors."""
+    lib = load()
+    arrays = {}
+    for n, t in atmos_arrays.items():
+        arrays[INTERP_SRC[n]] = t
+    for n, t in out.items():
+        arrays[INTERP_DST[n]] = t
+    if frac is not None:
+        arrays["frac_i"], arrays["frac_j"] = frac
+    f = F.pack(A.InterpFields, _grid_of(layout), arrays, coords=exchange_coords(coords),
+               atmos=atmos_grid_struct(atmos), time_weight=float(time_weight))
+    check(lib.nesf_interpolate_atmosphere_state(C.byref(f), _stream_handle(stream)))
+
+
+def compute_fractional_indices(layout, coords, atmos, fi, fj, stream=None):
+    """prescribed_atmosphere_regridder.jl:41-71 (fi, fj: float64 device tensors)."""
+    lib = load()
+    g = _grid_of(layout)
+    check(lib.nesf_compute_fractional_indices(C.byref(g), C.byref(exchange_coords(coords)),
+                                              C.byref(atmos_grid_struct(atmos)), C.c_void_p(fi.data_ptr()),
+                                              C.c_void_p(fj.data_ptr()), _stream_handle(stream)))
+
+
+def _assembly(fn, spec, layout, arrays, stream):
+    lib = load()
+    f = F.pack(A.AssemblyFields, _grid_of(layout), arrays)
+    p = spec.to_c() if hasattr(spec, "to_c") else spec
+    check(getattr(lib, fn)(C.byref(p), C.byref(f), _stream_handle(stream)))
+
+
+def assemble_net_ocean_fluxes(spec, layout, arrays, stream=None):
+    """update_net_fluxes!(model, ocean) (assemble_net_ocean_fluxes.jl:30-153)."""
+    _assembly("nesf_assemble_net_ocean_fluxes", spec, layout, arrays, stream)
+
+
+def assemble_net_sea_ice_fluxes(spec, layout, arrays, stream=None):
+    """update_net_fluxes!(model, sea_ice) (assemble_net_sea_ice_fluxes.jl:11-81)."""
+    _assembly("nesf_assemble_net_sea_ice_fluxes", spec, layout, arrays, stream)
+
+
+def apply_air_sea_radiative_fluxes(spec, layout, arrays, stream=None):
+    """apply_air_sea_radiative_fluxes.jl:18-111."""
+    _assembly("nesf_apply_air_sea_radiative_fluxes", spec, layout, arrays, stream)
+
+
+def apply_air_sea_ice_radiative_fluxes(spec, layout, arrays, stream=None):
+    """apply_air_sea_ice_radiative_fluxes.jl:15-90."""
+    _assembly("nesf_apply_air_sea_ice_radiative_fluxes", spec, layout, arrays, stream)
+
+
+def to_device(arrays, device="cuda", dtype=None):
+    """numpy dict -> torch tensors on the device (uint8/int arrays keep their dtype)."""
+    torch = _torch()
+    out = {}
+    for k, v in arrays.items():
+        if v is None:
+            out[k] = None
+            continue
+        t = torch.from_numpy(np.ascontiguousarray(v))
+        if dtype is not None and t.is_floating_point():
+            t = t.to(dtype)
+        out[k] = t.to(device)
+    return out

@@ -20,6 +20,9 @@ LIB = os.path.join(HERE, "libnesf.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+# The streaming kernels (interpolation, sea-ice-ocean fluxes, assembly) are HBM-bound:
+# without contracted multiply-adds they round exactly like the CPU restatement.
+PER_FILE_FLAGS = {"nesf_exchange.cu": ["-fmad=false"]}
 
 
 def nvcc():
@@ -57,7 +60,7 @@ def build(force=False, verbose=False, jobs=None):
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
-        cmd = [exe, *ARCH, *NVCC_FLAGS, "-I", INCLUDE, "-c", src, "-o", obj]
+        cmd = [exe, *ARCH, *NVCC_FLAGS, *PER_FILE_FLAGS.get(os.path.basename(src), []), "-I", INCLUDE, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")

@@ -1,0 +1,140 @@
+"""The coupling-step state and `update_state` (time_step_earth_system_model.jl:38-83).
+
+`CoupledModel` holds, on one device, what `update_state!(::EarthSystemModel)`
+touches for an ocean + sea-ice model forced by a PrescribedAtmosphere and
+PrescribedRadiation: the coarse atmosphere snapshots, the exchange-grid state,
+the interface fluxes and the net boundary fluxes. `update_state` runs the four
+phases through libnesf.so:
+  1. interpolate_state!        atmosphere + radiation onto the exchange grid
+  2. compute_*_fluxes!         atmosphere-ocean, atmosphere-sea-ice, sea-ice-ocean
+  3. update_net_fluxes!        ocean and sea ice
+  4. apply_*_radiative_fluxes! ocean and sea ice
+"""
+import numpy as np
+
+from . import api
+from . import fields as F
+from . import params as P
+
+OCEAN_NET = ("ocean_u", "ocean_v", "ocean_T", "ocean_S", "ocean_eta", "ocean_heat_content")
+ICE_NET = ("ice_top_heat", "ice_top_snowfall", "ice_top_u", "ice_top_v", "ice_bottom_heat")
+RAD_DIAG = ("ocean_upwelling_longwave", "ocean_downwelling_longwave", "ocean_downwelling_shortwave",
+            "ice_upwelling_longwave", "ice_downwelling_longwave", "ice_downwelling_shortwave")
+ATMOS_NAMES = ("u", "v", "T", "q", "p", "rain", "snow", "sw", "lw")
+EXCHANGE_ATMOS = {"u": "u_atm", "v": "v_atm", "T": "T_atm", "q": "q_atm", "p": "p_atm", "rain": "rain",
+                  "snow": "snow", "sw": "sw_down", "lw": "lw_down"}
+# per-step host inputs of the end-to-end path (everything a coupling step consumes)
+STEP_INPUTS = ("u_oc", "v_oc", "T_oc", "S_oc", "ice_concentration", "ice_thickness", "snow_thickness",
+               "consolidation_thickness", "ice_salinity", "ice_temperature", "ice_mass_flux", "snow_mass_flux")
+
+
+class CoupledModel:
+    def __init__(self, state, device="cuda", ao_spec=None, ai_spec=None, io_spec=None, assembly_spec=None,
+                 dz_top=10.0):
+        import torch
+        self.torch = torch
+        self.state = state
+        self.layout = state.layout
+        self.coords = state.coords
+        self.device = device
+        L = self.layout
+        f = state.fields
+        self.dtype = torch.float32 if state.dtype == np.float32 else torch.float64
+        dt = self.dtype
+        self.ao_spec = ao_spec or P.atmosphere_ocean_interface_spec()
+        self.ai_spec = ai_spec or P.atmosphere_sea_ice_interface_spec()
+        self.io_spec = io_spec or P.SeaIceOceanSpec()
+        self.asm_spec = assembly_spec or P.AssemblySpec()
+        z = lambda: torch.zeros(L.shape, dtype=dt, device=device)
+        # exchange-grid surface state
+        self.x = {k: torch.from_numpy(np.ascontiguousarray(v)).to(device) for k, v in f.items()}
+        self.T3 = self.x["T_oc"].view((1,) + L.shape)
+        self.S3 = self.x["S_oc"].view((1,) + L.shape)
+        self.dz = torch.tensor([dz_top], dtype=torch.float64, device=device)
+        self.atmos = state.atmos
+        if state.atmos is not None:
+            self.atmos_src = {n: torch.from_numpy(state.atmos["arrays"][n]).to(device) for n in ATMOS_NAMES}
+            for n in ATMOS_NAMES:
+                self.x[EXCHANGE_ATMOS[n]] = z()
+            self.fi = torch.zeros(L.shape, dtype=torch.float64, device=device)
+            self.fj = torch.zeros_like(self.fi)
+            # initialize!(exchanger): fractional indices once (prescribed_atmosphere_regridder.jl:41-49)
+            api.compute_fractional_indices(L, self.coords, self.atmos, self.fi, self.fj)
+        self.ai_T = self.x["ice_temperature"].clone()     # AI interface (top surface) temperature, in/out
+        self.ao = {k: z() for k in F.AO_OUTPUTS}
+        self.ai = {k: z() for k in F.AI_OUTPUTS}
+        self.ai["interface_temperature"] = self.ai_T
+        self.io = {k: z() for k in F.IO_OUTPUTS}
+        self.net = {k: z() for k in OCEAN_NET + ICE_NET + RAD_DIAG}
+        self.zero_io_stress = z()
+        self.intercepted = z()
+
+    # -------------------------------------------------------------- phases
+    def interpolate_state(self, stream=None):
+        if self.atmos is None:
+            return 0
+        out = {n: self.x[EXCHANGE_ATMOS[n]] for n in ATMOS_NAMES}
+        api.interpolate_atmosphere_state(self.layout, self.coords, self.atmos, self.atmos_src, out,
+                                         self.atmos["time_weight"], frac=(self.fi, self.fj), stream=stream)
+        return 1
+
+    def compute_fluxes(self, precision="f64", polish_maxiter=0, stats=False, stream=None):
+        x = self.x
+        s_ao = api.compute_atmosphere_ocean_fluxes(self.ao_spec, self.layout, x, self.ao, precision=precision,
+                                                   polish_maxiter=polish_maxiter, stats=stats, stream=stream)
+        ai_state = {k: x.get(k) for k in F.AI_INPUTS}
+        s_ai = api.compute_atmosphere_sea_ice_fluxes(self.ai_spec, self.layout, ai_state, self.ai,
+                                                     precision=precision, polish_maxiter=polish_maxiter,
+                                                     stats=stats, stream=stream)
+        io_state = {"ice_salinity": x["ice_salinity"], "ice_thickness": x["ice_thickness"],
+                    "consolidation_thickness": x["consolidation_thickness"],
+                    "ice_concentration": x["ice_concentration"], "internal_temperature": x["ice_temperature"],
+                    "ice_mass_flux": x["ice_mass_flux"], "snow_mass_flux": x["snow_mass_flux"]}
+        api.compute_sea_ice_ocean_fluxes(self.io_spec, self.layout, io_state, self.io, self.T3, self.S3, self.dz,
+                                         stream=stream)
+        return (s_ao, s_ai) if stats else 3
+
+    def assembly_arrays(self):
+        x, ao, ai, io, n = self.x, self.ao, self.ai, self.io, self.net
+        arr = dict(inactive=x["inactive"], ice_concentration=x["ice_concentration"],
+                   ocean_surface_temperature=x["T_oc"], rain=x["rain"], snow=x["snow"],
+                   intercepted_snow=self.intercepted, ao_sensible=ao["sensible_heat"], ao_latent=ao["latent_heat"],
+                   ao_water_vapor=ao["water_vapor"], ao_x_momentum=ao["x_momentum"], ao_y_momentum=ao["y_momentum"],
+                   ao_interface_temperature=ao["interface_temperature"], io_interface_heat=io["interface_heat"],
+                   io_frazil_heat=io["frazil_heat"], io_salt=io["salt"], io_freshwater=io["freshwater"],
+                   io_x_momentum=self.zero_io_stress, io_y_momentum=self.zero_io_stress,
+                   ai_sensible=ai["sensible_heat"], ai_latent=ai["latent_heat"], ai_x_momentum=ai["x_momentum"],
+                   ai_y_momentum=ai["y_momentum"], ai_interface_temperature=ai["interface_temperature"],
+                   sw_down=x["sw_down"], lw_down=x["lw_down"])
+        arr.update(n)
+        return arr
+
+    def update_net_fluxes(self, stream=None):
+        arr = self.assembly_arrays()
+        api.assemble_net_ocean_fluxes(self.asm_spec, self.layout, arr, stream=stream)
+        api.assemble_net_sea_ice_fluxes(self.asm_spec, self.layout, arr, stream=stream)
+        api.apply_air_sea_radiative_fluxes(self.asm_spec, self.layout, arr, stream=stream)
+        api.apply_air_sea_ice_radiative_fluxes(self.asm_spec, self.layout, arr, stream=stream)
+        return 4
+
+    def update_state(self, precision="f64", polish_maxiter=0, stream=None):
+        """One coupling step; returns the number of kernel launches."""
+        n = self.interpolate_state(stream)
+        n += self.compute_fluxes(precision, polish_maxiter, stream=stream)
+        n += self.update_net_fluxes(stream)
+        return n
+
+    # ---------------------------------------------------------- bookkeeping
+    def active_cells(self):
+        """Cells solved per step: water cells (atmosphere-ocean) + ice-covered water cells
+        (atmosphere-sea-ice), interior only."""
+        L = self.layout
+        water = L.interior(self.state.fields["inactive"]) == 0
+        ice = L.interior(self.state.fields["ice_concentration"]) > 0
+        return int(water.sum()), int((water & ice).sum())
+
+    def reset(self):
+        """Restore the state a step mutates (AI interface temperature, frazil-adjusted T)."""
+        f = self.state.fields
+        self.x["T_oc"].copy_(self.torch.from_numpy(f["T_oc"]).to(self.device))
+        self.ai_T.copy_(self.x["ice_temperature"])

@@ -44,6 +44,19 @@ static inline int64_t idx2(const nesf_grid* g, int i, int j) {
     return (int64_t)(i - 1 + g->hx) + (int64_t)(j - 1 + g->hy) * g->stride_j;
 }
 static inline double rd(const void* a, int64_t k) { return ((const double*)a)[k]; }
+
+/* Julia's min / max / clamp on floats: a NaN argument gives NaN (C's fmin/fmax
+ * would drop it), and min(-0.0, 0.0) = -0.0, max(-0.0, 0.0) = 0.0. */
+static inline double jmin(double x, double y) {
+    if (isnan(x) || isnan(y)) return x + y;
+    if (x == y) return signbit(x) ? x : y;
+    return x < y ? x : y;
+}
+static inline double jmax(double x, double y) {
+    if (isnan(x) || isnan(y)) return x + y;
+    if (x == y) return signbit(x) ? y : x;
+    return x > y ? x : y;
+}
 static inline double rdz(const void* a, int64_t k) { return a ? ((const double*)a)[k] : 0.0; }
 static inline void wr(void* a, int64_t k, double v) { if (a) ((double*)a)[k] = v; }
 
@@ -101,7 +114,7 @@ double oracle_surface_specific_humidity(const nesf_interface_params* p, double p
     double x = p->has_water_mole_fraction ? p->water_mole_fraction : 1.0;
     double pv = x * oracle_saturation_vapor_pressure(t, Ts, p->humidity_phase);
     double einv = 1 / Rv_over_Rd(t);
-    pv = fmin(pv, 0.999 * pa);
+    pv = jmin(pv, 0.999 * pa);
     return einv * pv / (pa - (1 - einv) * pv);
 }
 
@@ -112,15 +125,15 @@ static inline double surface_atmosphere_temperature(const nesf_interface_params*
 }
 
 /* ------------------------------------------------- stability functions */
-static inline double zmin0(double z) { return fmin(0.0, z); }
-static inline double zmax0(double z) { return fmax(0.0, z); }
+static inline double zmin0(double z) { return jmin(0.0, z); }
+static inline double zmax0(double z) { return jmax(0.0, z); }
 
 /* EdsonMomentumStabilityFunction (similarity_theory_turbulent_fluxes.jl:501-532) */
 static double psi_edson_momentum(const double* c, double z) {
     double zmax = c[0], Ap = c[1], Bp = c[2], Cp = c[3], Dp = c[4];
     double Am = c[5], Bm = c[6], Cm = c[7], Dm = c[8], Em = c[9], Fm = c[10];
     double zm = zmin0(z), zp = zmax0(z);
-    double dz = fmin(zmax, Ap * zp);
+    double dz = jmin(zmax, Ap * zp);
     double psip = -Bp * zp - Cp * (zp - Dp) * exp(-dz) - Cp * Dp;
     double f1 = sqrt(sqrt(1 - Am * zm));
     double psi1 = Bm * log((1 + f1) / Bm) + log((1 + f1 * f1) / Bm) - Bm * atan(f1) + Cm;
@@ -136,7 +149,7 @@ static double psi_edson_scalar(const double* c, double z) {
     double zmax = c[0], Ap = c[1], Bp = c[2], Cp = c[3], Dp = c[4], Ep = c[5];
     double Am = c[6], Bm = c[7], Cm = c[8], Dm = c[9], Em = c[10], Fm = c[11];
     double zm = zmin0(z), zp = zmax0(z);
-    double dz = fmin(zmax, Ap * zp);
+    double dz = jmin(zmax, Ap * zp);
     double psip = -pow(1 + Bp * zp, Cp) - Bp * (zp - Dp) * exp(-dz) - Ep;
     double f1 = sqrt(1 - Am * zm);
     double psi1 = Bm * log((1 + f1) / Bm) + Cm;
@@ -188,7 +201,7 @@ static double psi_paulson_scalar(double a, double z) {
 /* LinearStableStabilityFunction (similarity_theory_turbulent_fluxes.jl:747-752) */
 static double psi_linear(double coef, double zmax, double z) {
     double zp = zmax0(z);
-    return -coef * fmin(zp, zmax);
+    return -coef * jmin(zp, zmax);
 }
 
 /* stability_profile dispatch; SplitStabilityFunction (:720-725) selects stable for z > 0 */
@@ -238,7 +251,7 @@ double oracle_vsgs2(const nesf_similarity_theory_fluxes* f, double ustar, double
         conv = f->constant_subgrid_velocity * f->constant_subgrid_velocity;
     } else if (f->subgrid_kind == NESF_SUBGRID_CONVECTIVE) {
         double Jb = -ustar * bstar;
-        double UG = fmax(f->minimum_gustiness, f->gustiness_parameter * cbrt(fmax(0.0, Jb) * hbl));
+        double UG = jmax(f->minimum_gustiness, f->gustiness_parameter * cbrt(jmax(0.0, Jb) * hbl));
         conv = UG * UG;
     }
     double meso = f->mesoscale_subgrid_velocity * f->mesoscale_subgrid_velocity;
@@ -259,12 +272,12 @@ double oracle_momentum_roughness(const nesf_roughness_length* r, double ustar, d
     double nu = air_viscosity(r, Ts);
     double g = r->gravitational_acceleration;
     double Cg = r->charnock;
-    if (r->wave_kind == 1) Cg = fmax(0.0, r->wave_c1 * fmin(U, r->wave_umax) + r->wave_c2);
+    if (r->wave_kind == 1) Cg = jmax(0.0, r->wave_c1 * jmin(U, r->wave_umax) + r->wave_c2);
     double Cnu = r->smooth_wall_parameter;
     double lW = Cg * (ustar * ustar) / g;
     double lR = Cnu == 0 ? 0.0 : Cnu * nu / ustar;
     double ls = lW + lR;
-    return fmin(ls, r->maximum_roughness_length);
+    return jmin(ls, r->maximum_roughness_length);
 }
 
 /* roughness_length(::ScalarRoughnessLength) + ReynoldsScalingFunction (roughness_lengths.jl:231-246) */
@@ -274,7 +287,7 @@ double oracle_scalar_roughness(const nesf_roughness_length* r, double lu, double
     double nu = air_viscosity(r, Ts);
     double Rs = lu * ustar / nu;
     double ls = Rs == 0 ? 0.0 : r->reynolds_A / pow(Rs, r->reynolds_b);
-    return fmin(ls, r->maximum_roughness_length);
+    return jmin(ls, r->maximum_roughness_length);
 }
 
 /* buoyancy_scale (similarity_theory_turbulent_fluxes.jl:417-425) */
@@ -311,7 +324,7 @@ static void iterate_fluxes(const nesf_interface_params* p, const cell_in* c, dou
     double lu = oracle_momentum_roughness(&F->roughness[0], ustar, U, Ts);
     double lq = oracle_scalar_roughness(&F->roughness[2], lu, ustar, U, Ts);
     double lt = oracle_scalar_roughness(&F->roughness[1], lu, ustar, U, Ts);
-    double h = fmax(dh - F->zero_plane_displacement, 2 * lu);   /* displaced_profile_height (:313) */
+    double h = jmax(dh - F->zero_plane_displacement, 2 * lu);   /* displaced_profile_height (:313) */
     double k = F->von_karman_constant;
     double L = bstar == 0 ? INFINITY : ustar * ustar / (k * bstar);
     double chiu = k / similarity_profile(F->similarity_form, &F->stability[0], h, lu, L);
@@ -322,7 +335,8 @@ static void iterate_fluxes(const nesf_interface_params* p, const cell_in* c, dou
     *qst = chiq * dq;
 }
 
-static inline double clampd(double x, double lo, double hi) { return fmin(fmax(x, lo), hi); }
+/* Julia clamp: ifelse(x > hi, hi, ifelse(x < lo, lo, x)) (a NaN x stays NaN) */
+static inline double clampd(double x, double lo, double hi) { return x > hi ? hi : (x < lo ? lo : x); }
 
 /* compute_interface_temperature (interface_states.jl:333 bulk; 526-577 skin) with
  * flux_balance_temperature (434-457 diffusive; 468-524 conductive ice/snow) */
@@ -346,7 +360,7 @@ static double interface_temperature(const nesf_interface_params* p, const cell_i
     double Tat = surface_atmosphere_temperature(p, c->Ta, c->qa);
     if (p->temperature_formulation == NESF_SKIN_TEMPERATURE_DIFFUSIVE) {
         /* internal_diffusivity: a constant, or max(interior kappa, minimum) (interface_states.jl:390-391) */
-        double kap = c->kappa >= 0 ? fmax(c->kappa, p->diffusive_kappa) : p->diffusive_kappa;
+        double kap = c->kappa >= 0 ? jmax(c->kappa, p->diffusive_kappa) : p->diffusive_kappa;
         double del = p->diffusive_delta;
         double rho_i = p->interior_reference_density, c_i = p->interior_heat_capacity;
         double Qa = Qv + Iup + Qd;
@@ -376,7 +390,7 @@ static double interface_temperature(const nesf_interface_params* p, const cell_i
     double dTs = Tst - Tm1;
     double Tp = Tm1 + clampd(dTs, -p->max_delta_T, p->max_delta_T);
     double Tm = p->liquidus_freshwater_melting_temperature + off;
-    Tp = fmin(Tp, Tm);
+    Tp = jmin(Tp, Tm);
     Tp = c->hi >= c->hc ? Tp : Tb;
     return Tp;
 }
@@ -574,7 +588,7 @@ void oracle_solve_interface_conditions(const nesf_io_params* p, double To, doubl
     double b = -gam - eta * To - kap * Ti + th * (l2 - l1 * Si);
     double c = gam * So + (eta * To + kap * Ti - th * l2) * Si;
     double xi = a == 0 ? 0.0 : 1 / (2 * a);
-    double D = fmax(b * b - 4 * a * c, 0.0);
+    double D = jmax(b * b - 4 * a * c, 0.0);
     double S = (-b - sqrt(D)) * xi;
     S = S < 0 ? (-b + sqrt(D)) * xi : S;
     double T = l2 - p->liquidus_slope * S;
