@@ -1,0 +1,101 @@
+# NESF.jl -- ccall shim that routes NumericalEarth.jl's interface-flux step to
+# libnesf.so. Not executed in this repository (no Julia toolchain here); it is the
+# binding a NumericalEarth maintainer would add, written against include/nesf.h.
+#
+# Usage:
+#     using NumericalEarth, NESF
+#     fluxes = NESF.GB300SimilarityTheoryFluxes(SimilarityTheoryFluxes(); precision = :f32)
+#     interfaces = ComponentInterfaces(atmosphere, ocean, sea_ice; atmosphere_ocean_fluxes = fluxes)
+#
+# The methods below specialise compute_atmosphere_ocean_fluxes! on models whose
+# atmosphere-ocean flux formulation is the wrapper, and call the library with the
+# device pointers of the Oceananigans fields (parent arrays, halo included).
+module NESF
+
+using CUDA
+using Oceananigans: Oceananigans, architecture, size, halo_size
+using NumericalEarth.EarthSystemModels.InterfaceComputations: InterfaceComputations
+
+const libnesf = get(ENV, "NESF_LIB", joinpath(@__DIR__, "..", "nesf", "libnesf.so"))
+
+const NESF_OK = Cint(0)
+const NESF_F64 = Int32(0)
+const NESF_F32 = Int32(1)
+const NESF_PLAIN_F64 = Int32(0)
+const NESF_F32_POLISH = Int32(1)
+
+struct Grid
+    nx::Int32; ny::Int32; hx::Int32; hy::Int32; stride_j::Int64
+end
+
+# Opaque blob holding nesf_interface_params, filled by the library defaults
+# and then patched field by field through the offsets exported by the library's
+# layout (the Python binding nesf/_abi.py lists the field order).
+const PARAMS_BYTES = 1064   # sizeof(nesf_interface_params); nesf_struct_sizes() reports it
+
+struct AOFields
+    grid::Grid; dtype::Int32; pad::Int32
+    u_atm::Ptr{Cvoid}; v_atm::Ptr{Cvoid}; T_atm::Ptr{Cvoid}; p_atm::Ptr{Cvoid}; q_atm::Ptr{Cvoid}
+    u_oc::Ptr{Cvoid}; v_oc::Ptr{Cvoid}; T_oc::Ptr{Cvoid}; S_oc::Ptr{Cvoid}; inactive::Ptr{UInt8}
+    sw_down::Ptr{Cvoid}; lw_down::Ptr{Cvoid}; kappa::Ptr{Cvoid}
+    latent_heat::Ptr{Cvoid}; sensible_heat::Ptr{Cvoid}; water_vapor::Ptr{Cvoid}
+    x_momentum::Ptr{Cvoid}; y_momentum::Ptr{Cvoid}
+    friction_velocity::Ptr{Cvoid}; temperature_scale::Ptr{Cvoid}; water_vapor_scale::Ptr{Cvoid}
+    interface_temperature::Ptr{Cvoid}; iterations::Ptr{Int32}
+end
+
+struct SolverOptions
+    precision::Int32; polish_maxiter::Int32; block_size::Int32; schedule::Int32
+    ctas_per_sm::Int32; warm_start::Int32; mlp::Ptr{Cvoid}; fallback_ratio::Float64; path_tolerance::Float64
+end
+
+struct GB300SimilarityTheoryFluxes{F}
+    inner :: F                  # the reference formulation (defaults, solver settings)
+    precision :: Symbol         # :f64 (drop-in) or :f32 (FP32 sweep + FP64 Newton polish)
+end
+GB300SimilarityTheoryFluxes(inner; precision = :f64) = GB300SimilarityTheoryFluxes(inner, precision)
+
+check(code) = code == NESF_OK ||
+    error("nesf error $code: " * unsafe_string(ccall((:nesf_last_error, libnesf), Cstring, ())))
+
+devptr(f) = reinterpret(Ptr{Cvoid}, pointer(parent(f)))   # CuArray parent of an Oceananigans field
+surface(f, k) = view(parent(f), :, :, k)                   # k = Nz + Hz slice of a 3-D field
+
+function default_params(interface::Symbol)
+    buf = zeros(UInt8, PARAMS_BYTES)
+    fn = interface === :ocean ? :nesf_default_ao_params : :nesf_default_ai_params
+    ccall((fn, libnesf), Cvoid, (Ptr{UInt8},), buf)
+    return buf
+end
+
+function InterfaceComputations.compute_atmosphere_ocean_fluxes!(coupled_model, fluxes::GB300SimilarityTheoryFluxes)
+    exchanger = coupled_model.interfaces.exchanger
+    grid = exchanger.grid
+    Nx, Ny, Nz = size(grid)
+    Hx, Hy, Hz = halo_size(grid)
+    atmos = exchanger.atmosphere.state
+    ocean = exchanger.ocean.state
+    out = coupled_model.interfaces.atmosphere_ocean_interface.fluxes
+    Ts = coupled_model.interfaces.atmosphere_ocean_interface.temperature
+    FT = eltype(grid)
+    g = Grid(Nx, Ny, Hx, Hy, Nx + 2Hx)
+    k = Nz + Hz
+    fields = AOFields(g, FT == Float64 ? NESF_F64 : NESF_F32, 0,
+                      devptr(atmos.u), devptr(atmos.v), devptr(atmos.T), devptr(atmos.p), devptr(atmos.q),
+                      pointer(surface(ocean.u, k)), pointer(surface(ocean.v, k)),
+                      pointer(surface(ocean.T, k)), pointer(surface(ocean.S, k)), C_NULL,
+                      C_NULL, C_NULL, C_NULL,
+                      devptr(out.latent_heat), devptr(out.sensible_heat), devptr(out.water_vapor),
+                      devptr(out.x_momentum), devptr(out.y_momentum),
+                      devptr(out.friction_velocity), devptr(out.temperature_scale), devptr(out.water_vapor_scale),
+                      devptr(Ts), C_NULL)
+    params = default_params(:ocean)
+    opts = SolverOptions(fluxes.precision === :f32 ? NESF_F32_POLISH : NESF_PLAIN_F64, 0, 128, 0, 0, 0, C_NULL, 10.0, 2e-6)
+    stream = CUDA.stream().handle
+    check(ccall((:nesf_compute_atmosphere_ocean_fluxes, libnesf), Cint,
+                (Ptr{Cvoid}, Ptr{UInt8}, Ref{AOFields}, Ref{SolverOptions}, Ptr{Cvoid}, Ptr{Cvoid}),
+                C_NULL, params, fields, opts, C_NULL, stream))
+    return nothing
+end
+
+end # module
