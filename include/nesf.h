@@ -409,6 +409,17 @@ int nesf_compute_atmosphere_ocean_fluxes_ensemble(nesf_context* ctx, const nesf_
                                                   const nesf_ao_fields* fields, const nesf_solver_options* opts,
                                                   nesf_stats* stats, void* stream);
 
+/* The atmosphere-ocean solve without any device allocation, for callers that
+ * cannot allocate at call time (a host model whose pooling allocator holds the
+ * whole device, or a caller that must not enter the driver's allocator). No
+ * counterpart in the reference. Its scratch is a fixed 16 MiB array in the
+ * library, shared by every call: grids of more than 2,097,152 cells (halo ring
+ * (nx+2) x (ny+2)) are rejected with NESF_ERR_CAPACITY; calls that overlap on the
+ * GPU race on the scratch. The first call on a device sets up the scratch address
+ * (make it before any stream capture). No statistics. */
+int nesf_compute_atmosphere_ocean_fluxes_noalloc(const nesf_interface_params* params, const nesf_ao_fields* fields,
+                                                 const nesf_solver_options* opts, void* stream);
+
 /* compute_atmosphere_sea_ice_fluxes! (atmosphere_sea_ice_fluxes.jl:18-62) */
 int nesf_compute_atmosphere_sea_ice_fluxes(nesf_context* ctx, const nesf_interface_params* params,
                                            const nesf_ai_fields* fields, const nesf_solver_options* opts,

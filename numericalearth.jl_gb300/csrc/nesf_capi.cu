@@ -775,3 +775,72 @@ extern "C" int nesf_apply_air_sea_ice_radiative_fluxes(const nesf_assembly_param
                                                        void* stream) {
     return run_assembly(p, f, 3, stream, "nesf_apply_air_sea_ice_radiative_fluxes");
 }
+
+// ------------------------------------------------ allocation-free variant
+// Some callers cannot allocate device memory when they run the flux step: a host
+// model whose memory manager has reserved the whole device (the pooling allocators
+// of CUDA.jl or PyTorch can hold every free byte, so a cudaMalloc inside the call
+// would fail or force the pool to release memory), or a caller with a latency
+// budget that must not enter the driver's allocator. For them,
+// nesf_compute_atmosphere_ocean_fluxes_noalloc runs the atmosphere-ocean solve
+// without allocating anything: its scratch -- the compacted work list, the replay
+// queue and their counters -- is this file-scope array, which every GPU that loads
+// the library holds until the process exits: 64 counters (256 B) + two lists of
+// NESF_NOALLOC_MAX_CELLS uint32 entries, 16 MiB + 256 B in all.
+#define NESF_NOALLOC_MAX_CELLS (1 << 21)
+static __device__ __align__(256) uint32_t g_noalloc_scratch[64 + 2 * (size_t)NESF_NOALLOC_MAX_CELLS];
+
+static uint32_t* g_noalloc_ptr[64];   // device address of the array, per device
+static std::mutex g_noalloc_lock;
+
+// Set-up, once per device, with that device current: the array's device address.
+// In host code the symbol names a host-side stand-in, not device memory, so only
+// this address may be handed to a kernel.
+static int noalloc_scratch(uint32_t** out) {
+    int dev = 0;
+    NESF_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(NESF_ERR_ARG, "nesf_compute_atmosphere_ocean_fluxes_noalloc: device %d", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_lock);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
+        g_noalloc_ptr[dev] = (uint32_t*)p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return NESF_OK;
+}
+
+extern "C" int nesf_compute_atmosphere_ocean_fluxes_noalloc(const nesf_interface_params* params,
+                                                            const nesf_ao_fields* f, const nesf_solver_options* opts,
+                                                            void* stream) {
+    const char* who = "nesf_compute_atmosphere_ocean_fluxes_noalloc";
+    int r = check_params(params, who);
+    if (r) return r;
+    if ((r = check_ao_fields(f, params, who))) return r;
+    nesf_solver_options o = options_or_default(opts);
+    if ((r = check_options(o, who))) return r;
+    int64_t ring = (int64_t)(f->grid.nx + 2) * (f->grid.ny + 2);
+    if (ring > NESF_NOALLOC_MAX_CELLS)
+        return fail(NESF_ERR_CAPACITY,
+                    "%s: %lld cells (halo ring included) exceed the fixed scratch of %d cells; "
+                    "use nesf_compute_atmosphere_ocean_fluxes", who, (long long)ring, NESF_NOALLOC_MAX_CELLS);
+    uint32_t* base = nullptr;
+    if ((r = noalloc_scratch(&base))) return r;
+    // counters: [0, 1] work list (unstable, stable), [2] replay queue; both are
+    // cleared by the launch before the first pass reads them
+    WorkList wl{base + 64, base, ring};
+    ReplayQueue rq{base + 64 + NESF_NOALLOC_MAX_CELLS, base + 2, NESF_NOALLOC_MAX_CELLS};
+    DevIface<double> P64 = make_dev_iface<double>(*params);
+    DevIface<float> P32 = make_dev_iface<float>(*params);
+    bool skin = params->temperature_formulation != NESF_BULK_TEMPERATURE;
+    SolveOpts so{o.polish_maxiter, (float)o.path_tolerance};
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = f->dtype == NESF_F64
+                        ? launch_ao(ao_args<double>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl,
+                                    rq, nullptr, s)
+                        : launch_ao(ao_args<float>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl,
+                                    rq, nullptr, s);
+    if (e != cudaSuccess) return cuda_fail(e, who);
+    return NESF_OK;
+}

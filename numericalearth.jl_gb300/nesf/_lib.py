@@ -36,6 +36,8 @@ SIGNATURES = {
     "nesf_compute_atmosphere_ocean_fluxes_ensemble": (
         C.c_int, [vp, P(A.InterfaceParams), C.c_int32, C.c_int64, P(A.AOFields), P(A.SolverOptions),
                   P(A.Stats), vp]),
+    "nesf_compute_atmosphere_ocean_fluxes_noalloc": (
+        C.c_int, [P(A.InterfaceParams), P(A.AOFields), P(A.SolverOptions), vp]),
     "nesf_compute_atmosphere_sea_ice_fluxes": (
         C.c_int, [vp, P(A.InterfaceParams), P(A.AIFields), P(A.SolverOptions), P(A.Stats), vp]),
     "nesf_compute_sea_ice_ocean_fluxes": (C.c_int, [vp, P(A.IOParams), P(A.IOFields), vp]),

@@ -1,0 +1,80 @@
+"""The allocation-free atmosphere-ocean entry point against the regular one.
+
+nesf_compute_atmosphere_ocean_fluxes_noalloc is for callers that cannot allocate
+device memory when the flux step runs (a host model whose pooling allocator holds
+the whole device, or a caller that must not enter the driver's allocator). It
+keeps its scratch in a fixed array inside the library; this test calls it through
+the C ABI twice in a row -- the second call finds the previous call's work list
+and replay queue in the shared scratch -- and checks both calls against
+nesf_compute_atmosphere_ocean_fluxes on the same inputs, with the tolerance of the
+other GPU tests (relative error |a - b| / max(|b|, 1e-6 max|b|) <= 1e-12). It also
+checks that a grid beyond the scratch capacity is refused before any launch.
+
+This file is collected last so that a failing run stopped at the first failure has
+already run every other test.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from helpers import rel_err, to_numpy
+from nesf import _abi as A
+from nesf import _lib, api
+from nesf import fields as F
+from nesf import params as P
+from nesf import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+
+MAX_CELLS = 1 << 21
+
+
+def _noalloc(lib, spec, layout, dev, out, precision):
+    import torch
+    arrays = {k: dev.get(k) for k in F.AO_INPUTS}
+    arrays.update({k: out[k] for k in F.AO_OUTPUTS})
+    f = F.pack(A.AOFields, F.make_grid(layout), arrays)
+    p = spec.to_c()
+    o = api.solver_options(precision)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    return lib.nesf_compute_atmosphere_ocean_fluxes_noalloc(C.byref(p), C.byref(f), C.byref(o), stream)
+
+
+@pytest.mark.parametrize("precision,dtype", [("f64", np.float64), ("f32", np.float32)])
+def test_noalloc_matches_regular_entry_point_twice(precision, dtype):
+    import torch
+    lib = _lib.load()
+    st = syn.coupled(seed=31, nx=360, ny=160, lat_s=-75, lat_n=75, land=0.3, interpolate=False, dtype=dtype)
+    spec = P.atmosphere_ocean_interface_spec()
+    dev = api.to_device({k: st.fields[k] for k in F.AO_INPUTS if k in st.fields})
+    fdt = dev["u_atm"].dtype
+    ref = {k: torch.zeros(st.layout.shape, dtype=fdt, device="cuda") for k in F.AO_OUTPUTS}
+    api.compute_atmosphere_ocean_fluxes(spec, st.layout, dev, ref, precision=precision)
+    torch.cuda.synchronize()
+    R = st.layout.ring
+    expect = {k: R(to_numpy(v)).astype(np.float64) for k, v in ref.items()}
+    for call in range(2):
+        out = {k: torch.full(st.layout.shape, float("nan"), dtype=fdt, device="cuda") for k in F.AO_OUTPUTS}
+        code = _noalloc(lib, spec, st.layout, dev, out, precision)
+        assert code == A.NESF_OK, lib.nesf_last_error()
+        torch.cuda.synchronize()
+        for k in F.AO_OUTPUTS:
+            got = R(to_numpy(out[k])).astype(np.float64)
+            e = rel_err(got, expect[k], floor_frac=1e-6)
+            assert e.max() <= 1e-12, (precision, call, k, float(e.max()))
+
+
+def test_noalloc_refuses_grids_beyond_its_scratch():
+    import torch
+    lib = _lib.load()
+    spec = P.atmosphere_ocean_interface_spec()
+    nx, ny = 2048, 1024                     # (nx + 2) * (ny + 2) > 2**21
+    assert (nx + 2) * (ny + 2) > MAX_CELLS
+    layout = syn.Layout(nx, ny, 2, 2)
+    small = torch.zeros(16, dtype=torch.float64, device="cuda")   # never read: refused before any launch
+    arrays = {k: small for k in ("u_atm", "v_atm", "T_atm", "p_atm", "q_atm", "u_oc", "v_oc", "T_oc", "S_oc")}
+    arrays.update({k: small for k in F.AO_OUTPUTS})
+    code = _noalloc(lib, spec, layout, arrays, arrays, "f64")
+    assert code == A.NESF_ERR_CAPACITY
+    assert b"exceed" in lib.nesf_last_error()
