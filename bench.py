@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="small grid (profiling captures)")
+    ap.add_argument("--no-plain", action="store_true", help="time only --precision (profiling captures)")
     return ap.parse_args()
 
 
@@ -350,6 +351,11 @@ def main():
     with ClockSampler(local) as clocks:
         ms, launches = time_steps(model, prec, args.steps, args.warmup, world)
     clk = clocks.summary()
+    if args.no_plain:
+        print(json.dumps({"metric": METRIC, "value": cells * world / (ms / 1000.0), "unit": "flux cells/s",
+                          "ms_per_step": ms, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                          "note": "profiling run: --precision only"}))
+        return
     ms_plain, _ = time_steps(model, "f64", max(3, args.steps // 4), 1, world)
     phases = phase_times(model, prec)
     phases_plain = phase_times(model, "f64", reps=1)
