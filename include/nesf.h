@@ -189,8 +189,14 @@ typedef struct {
 
 /* ------------------------------------------------------ solver precision */
 typedef enum {
-    NESF_PLAIN_F64 = 0,   /* every iteration in FP64: the drop-in                         */
-    NESF_F32_POLISH = 1   /* FP32 iterations; FP64 polish where the FP32 residual stalls  */
+    NESF_PLAIN_F64 = 0,    /* every iteration in FP64: the drop-in                         */
+    NESF_F32_POLISH = 1,   /* FP32 iterations, then an FP64 Newton polish of every cell    */
+    NESF_F32_ADAPTIVE = 2  /* as NESF_F32_POLISH, but a cell keeps its FP32 result when
+                              each state component converged at FP32 resolution, the
+                              fixed-point map contracts by at most fp32_rho and the FP32
+                              rounding of its cancelling differences, amplified by
+                              1 / (1 - rho), stays within path_tolerance; the others are
+                              polished in FP64                                            */
 } nesf_precision;
 
 typedef struct {
@@ -205,6 +211,8 @@ typedef struct {
     double fallback_ratio;    /* cold-start fallback when r1 > ratio * r1(cold); 10    */
     double path_tolerance;    /* replay cells whose reference stopping error may exceed
                                  this relative bound (FP32 polish); default 2e-6         */
+    double fp32_rho;          /* NESF_F32_ADAPTIVE: largest contraction rate at which the
+                                 FP32 result is kept; default 0.8 (0 or less: default)  */
 } nesf_solver_options;
 
 /* -------------------------------------------------------------- statistics */
@@ -412,7 +420,7 @@ int nesf_compute_atmosphere_ocean_fluxes_ensemble(nesf_context* ctx, const nesf_
 /* The atmosphere-ocean solve without any device allocation, for callers that
  * cannot allocate at call time (a host model whose pooling allocator holds the
  * whole device, or a caller that must not enter the driver's allocator). No
- * counterpart in the reference. Its scratch is a fixed 16 MiB array in the
+ * counterpart in the reference. Its scratch is a fixed 24 MiB array in the
  * library, shared by every call: grids of more than 2,097,152 cells (halo ring
  * (nx+2) x (ny+2)) are rejected with NESF_ERR_CAPACITY; calls that overlap on the
  * GPU race on the scratch. The first call on a device sets up the scratch address

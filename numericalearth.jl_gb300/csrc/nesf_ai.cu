@@ -113,33 +113,73 @@ __global__ void __launch_bounds__(128) ai_kernel(AIArgs<S> a, DevIface<double> P
     bool needs = P.stop_kind == NESF_STOP_CONVERGENCE;
     double us = 0, ts = 0, qst = 0, Ts = c.Ti;
     int iters = 0, f64it = 0;
-    bool nonconv = false, polished = false, replay = false;
-    int reason = -1;
+    bool nonconv = false;
+    int outcome = FAST_SOLVED, reason = -1;
     if (PREC == NESF_PLAIN_F64 || !needs) {
         iters = skin ? ai_plain<true>(P, c, Ts0, us, ts, qst, Ts, nonconv)
                      : ai_plain<false>(P, c, Ts0, us, ts, qst, Ts, nonconv);
     } else {
-        double qs0 = surface_specific_humidity(P, c.pa, Ts0);
-        SurfaceConst<double> s;
-        surface_const(P, c, Ts0, qs0, s);
+        SurfaceConst<double> s{};
+        if (skin) s.Ts = Ts0;   // solve_fast reads only T_s of a skin state
+        else surface_const(P, c, Ts0, surface_specific_humidity(P, c.pa, Ts0), s);
         us = ts = qst = 1e-4;
         int f32it;
-        polished = skin ? solve_fast<true>(P, P32, c, s, us, ts, qst, so, f32it, f64it, reason)
-                        : solve_fast<false>(P, P32, c, s, us, ts, qst, so, f32it, f64it, reason);
+        const bool accept32 = so.fp32_rho > 0.0f;
+        outcome = skin ? solve_fast<true>(P, P32, c, s, us, ts, qst, so, accept32, f32it, f64it, reason)
+                       : solve_fast<false>(P, P32, c, s, us, ts, qst, so, accept32, f32it, f64it, reason);
         iters = f32it + f64it;
         Ts = s.Ts;
-        replay = !polished;
     }
-    if (PREC != NESF_PLAIN_F64) replay_push(rq, replay, (uint32_t)r);
-    if (replay) {
+    if (PREC != NESF_PLAIN_F64) {
+        replay_push(rq, outcome == FAST_REPLAY, (uint32_t)r);
+        polish_push(rq, outcome == FAST_POLISH, (uint32_t)r);
+    }
+    if (outcome != FAST_SOLVED) {
         if (stats) {
-            stats_add(stats, true, false, 0, false, false, 0, true, false);
-            stats_replay_reason(stats, reason);
+            stats_add(stats, true, false, 0, false, false, 0, outcome == FAST_REPLAY, false);
+            if (outcome == FAST_REPLAY) stats_replay_reason(stats, reason);
         }
         return;
     }
     ai_store(P, a, k, c, us, ts, qst, Ts, iters);
-    if (stats) stats_add(stats, true, true, iters, nonconv, polished, f64it, false, false);
+    if (stats) stats_add(stats, true, true, iters, nonconv, f64it > 0, f64it, false, false);
+}
+
+// Pass 1b (ADAPTIVE): the cells whose FP32 result was not kept, packed, through the
+// FP32 sweep + FP64 Newton polish; those that need it go on to the replay. The
+// initial interface temperature is still in a.Ts: pass 1 did not write these cells.
+template <class S, bool SKIN>
+__global__ void __launch_bounds__(128) ai_polish_kernel(AIArgs<S> a, DevIface<double> P, DevIface<float> P32,
+                                                        SolveOpts so, ReplayQueue rq, DevStats* stats) {
+    const int nxr = a.L.nx + 2;
+    const unsigned n = rq.count[1];
+    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n && (int64_t)q < rq.capacity;
+         q += gridDim.x * blockDim.x) {
+        uint32_t id = rq.idx[rq.capacity + q];
+        int64_t r = id;
+        int i = (int)(r % nxr), j = (int)(r / nxr);
+        int64_t k = a.L.at(i, j);
+        CellConst<double> c;
+        double aleph, Ts0;
+        bool land;
+        ai_load(P, a, k, c, aleph, Ts0, land);
+        SurfaceConst<double> s{};
+        if (SKIN) s.Ts = Ts0;
+        else surface_const(P, c, Ts0, surface_specific_humidity(P, c.pa, Ts0), s);
+        double us = 1e-4, ts = 1e-4, qst = 1e-4;
+        int f32it, f64it, reason = -1;
+        int outcome = solve_fast<SKIN>(P, P32, c, s, us, ts, qst, so, false, f32it, f64it, reason);
+        replay_push(rq, outcome == FAST_REPLAY, id);
+        if (outcome == FAST_REPLAY) {
+            if (stats) {
+                stats_add(stats, false, false, 0, false, false, 0, true, false);
+                stats_replay_reason(stats, reason);
+            }
+            continue;
+        }
+        ai_store(P, a, k, c, us, ts, qst, s.Ts, f32it + f64it);
+        if (stats) stats_add(stats, false, true, f32it + f64it, false, true, f64it, false, false);
+    }
 }
 
 // Pass 2: the queued cells, packed, through the reference's FP64 iteration. The
@@ -148,7 +188,7 @@ template <class S>
 __global__ void __launch_bounds__(128) ai_replay_kernel(AIArgs<S> a, DevIface<double> P, ReplayQueue rq,
                                                         DevStats* stats) {
     const int nxr = a.L.nx + 2;
-    const unsigned n = *rq.count;
+    const unsigned n = rq.count[0];
     for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n && (int64_t)q < rq.capacity;
          q += gridDim.x * blockDim.x) {
         int64_t r = rq.idx[q];
@@ -175,7 +215,7 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     const int block = 128;
     dim3 grid((unsigned)((ring + block - 1) / block));
     cudaError_t e = cudaMemsetAsync(wl.count, 0, sizeof(unsigned) * 2, stream);
-    if (e == cudaSuccess && prec != NESF_PLAIN_F64) e = cudaMemsetAsync(rq.count, 0, sizeof(unsigned), stream);
+    if (e == cudaSuccess && prec != NESF_PLAIN_F64) e = cudaMemsetAsync(rq.count, 0, 2 * sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
     ai_classify_kernel<S><<<grid, block, 0, stream>>>(a, P64, P32, wl, stats);
     if (prec == NESF_PLAIN_F64)
@@ -187,6 +227,14 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (so.fp32_rho > 0.0f) {
+        if (P64.temp_form != NESF_BULK_TEMPERATURE)
+            ai_polish_kernel<S, true><<<(unsigned)sms * 4, block, 0, stream>>>(a, P64, P32, so, rq, stats);
+        else
+            ai_polish_kernel<S, false><<<(unsigned)sms * 4, block, 0, stream>>>(a, P64, P32, so, rq, stats);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
     ai_replay_kernel<S><<<(unsigned)sms * 4, block, 0, stream>>>(a, P64, rq, stats);
     return cudaGetLastError();
 }

@@ -133,31 +133,74 @@ __global__ void __launch_bounds__(128, ENS ? 4 : 1) ao_kernel(AOArgs<S> a, DevIf
     bool land;
     ao_load(Pd, a, k, SKIN, c, land);
     double us = 1e-4, ts = 1e-4, qst = 1e-4;   // initial guess (atmosphere_ocean_fluxes.jl:132)
-    double qs0 = surface_specific_humidity(Pd, c.pa, c.Ti);
-    SurfaceConst<double> s;
-    surface_const(Pd, c, c.Ti, qs0, s);
     bool needs = Pd.stop_kind == NESF_STOP_CONVERGENCE;
+    SurfaceConst<double> s{};
+    if (SKIN && PREC != NESF_PLAIN_F64 && needs) s.Ts = c.Ti;   // solve_fast reads only T_s of a skin state
+    else surface_const(Pd, c, c.Ti, surface_specific_humidity(Pd, c.pa, c.Ti), s);
     int iters = 0, f64it = 0;
-    bool nonconv = false, polished = false, replay = false;
-    int reason = -1;
+    bool nonconv = false;
+    int outcome = FAST_SOLVED, reason = -1;
     if (PREC == NESF_PLAIN_F64 || !needs) {
         iters = solve_plain<SKIN>(Pd, c, s, us, ts, qst, nonconv);
     } else {
         int f32it;
-        polished = solve_fast<SKIN>(Pd, Pf, c, s, us, ts, qst, so, f32it, f64it, reason);
+        outcome = solve_fast<SKIN>(Pd, Pf, c, s, us, ts, qst, so, so.fp32_rho > 0.0f, f32it, f64it, reason);
         iters = f32it + f64it;
-        replay = !polished;
     }
-    if (PREC != NESF_PLAIN_F64) replay_push(rq, replay, (uint32_t)(m * ring + r));
-    if (replay) {
+    const uint32_t id = (uint32_t)(m * ring + r);
+    if (PREC != NESF_PLAIN_F64) {
+        replay_push(rq, outcome == FAST_REPLAY, id);
+        polish_push(rq, outcome == FAST_POLISH, id);
+    }
+    if (outcome != FAST_SOLVED) {
         if (stats) {
-            stats_add(stats, true, false, 0, false, false, 0, true, false);
-            stats_replay_reason(stats, reason);
+            stats_add(stats, true, false, 0, false, false, 0, outcome == FAST_REPLAY, false);
+            if (outcome == FAST_REPLAY) stats_replay_reason(stats, reason);
         }
         return;
     }
     ao_store(Pd, a, k, c, false, us, ts, qst, s.Ts, iters);
-    if (stats) stats_add(stats, true, true, iters, nonconv, polished, f64it, false, false);
+    if (stats) stats_add(stats, true, true, iters, nonconv, f64it > 0, f64it, false, false);
+}
+
+// Pass 1b (ADAPTIVE): the cells whose FP32 result was not kept, packed, through
+// the FP32 sweep + FP64 Newton polish; those that need it go on to the replay.
+template <class S, bool SKIN>
+__global__ void __launch_bounds__(128) ao_polish_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
+                                                        const DevIface<double>* __restrict__ P64s,
+                                                        const DevIface<float>* __restrict__ P32s, SolveOpts so,
+                                                        ReplayQueue rq, DevStats* stats) {
+    const int nxr = a.L.nx + 2;
+    const int64_t ring = (int64_t)nxr * (a.L.ny + 2);
+    const unsigned n = rq.count[1];
+    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n && (int64_t)q < rq.capacity;
+         q += gridDim.x * blockDim.x) {
+        uint32_t id = rq.idx[rq.capacity + q];
+        int64_t m = (int64_t)id / ring, r = (int64_t)id % ring;
+        const DevIface<double>& P = P64s ? P64s[m] : P64;
+        const DevIface<float>& Pf = P32s ? P32s[m] : P32;
+        int i = (int)(r % nxr), j = (int)(r / nxr);
+        int64_t k = a.L.at(i, j) + m * a.member_stride;
+        CellConst<double> c;
+        bool land;
+        ao_load(P, a, k, SKIN, c, land);
+        double us = 1e-4, ts = 1e-4, qst = 1e-4;
+        SurfaceConst<double> s{};
+        if (SKIN) s.Ts = c.Ti;
+        else surface_const(P, c, c.Ti, surface_specific_humidity(P, c.pa, c.Ti), s);
+        int f32it, f64it, reason = -1;
+        int outcome = solve_fast<SKIN>(P, Pf, c, s, us, ts, qst, so, false, f32it, f64it, reason);
+        replay_push(rq, outcome == FAST_REPLAY, id);
+        if (outcome == FAST_REPLAY) {
+            if (stats) {
+                stats_add(stats, false, false, 0, false, false, 0, true, false);
+                stats_replay_reason(stats, reason);
+            }
+            continue;
+        }
+        ao_store(P, a, k, c, false, us, ts, qst, s.Ts, f32it + f64it);
+        if (stats) stats_add(stats, false, true, f32it + f64it, false, true, f64it, false, false);
+    }
 }
 
 // Pass 2: the queued cells, packed, through the reference's FP64 iteration.
@@ -167,7 +210,7 @@ __global__ void __launch_bounds__(128) ao_replay_kernel(AOArgs<S> a, DevIface<do
                                                         DevStats* stats) {
     const int nxr = a.L.nx + 2;
     const int64_t ring = (int64_t)nxr * (a.L.ny + 2);
-    const unsigned n = *rq.count;
+    const unsigned n = rq.count[0];
     for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n && (int64_t)q < rq.capacity;
          q += gridDim.x * blockDim.x) {
         uint32_t id = rq.idx[q];
@@ -200,7 +243,7 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
     dim3 grid((unsigned)((ring + threads - 1) / threads), nm);
     bool ens = members > 1 || P64s != nullptr;
     cudaError_t e = cudaMemsetAsync(wl.count, 0, sizeof(unsigned) * 2 * nm, stream);
-    if (e == cudaSuccess && prec != NESF_PLAIN_F64) e = cudaMemsetAsync(rq.count, 0, sizeof(unsigned), stream);
+    if (e == cudaSuccess && prec != NESF_PLAIN_F64) e = cudaMemsetAsync(rq.count, 0, 2 * sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
     if (ens) ao_classify_kernel<S, true><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, stats);
     else ao_classify_kernel<S, false><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, stats);
@@ -217,12 +260,18 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
 #undef NESF_AO_LAUNCH
     e = cudaGetLastError();
     if (e != cudaSuccess || prec == NESF_PLAIN_F64) return e;
-    // pass 2: enough resident blocks to sweep the queue (grid-stride)
+    // passes 1b and 2: enough resident blocks to sweep the queues (grid-stride)
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     unsigned g2 = (unsigned)sms * 4;
     const DevIface<double>* pm = ens ? P64s : nullptr;
+    if (so.fp32_rho > 0.0f) {
+        if (skin) ao_polish_kernel<S, true><<<g2, threads, 0, stream>>>(a, P64, P32, pm, ens ? P32s : nullptr, so, rq, stats);
+        else ao_polish_kernel<S, false><<<g2, threads, 0, stream>>>(a, P64, P32, pm, ens ? P32s : nullptr, so, rq, stats);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
     if (skin) ao_replay_kernel<S, true><<<g2, threads, 0, stream>>>(a, P64, pm, rq, stats);
     else ao_replay_kernel<S, false><<<g2, threads, 0, stream>>>(a, P64, pm, rq, stats);
     return cudaGetLastError();

@@ -20,8 +20,8 @@ struct nesf_context {
     DevIface<double>* d_p64;    // per-member parameters (ensemble)
     DevIface<float>* d_p32;
     int32_t capacity_members;
-    uint32_t* d_replay;         // replay queue of the FP32 + polish solver
-    unsigned int* d_replay_count;
+    uint32_t* d_replay;         // replay + polish queues of the FP32 solvers (2 x capacity)
+    unsigned int* d_replay_count;   // [2]
     int64_t replay_capacity;
     uint32_t* d_work;           // compacted work lists of the solves
     unsigned int* d_work_count; // two counters per ensemble member
@@ -231,6 +231,7 @@ void nesf_default_solver_options(nesf_solver_options* o) {
     o->mlp = nullptr;
     o->fallback_ratio = 10.0;
     o->path_tolerance = 2e-6;
+    o->fp32_rho = 0.8;
 }
 
 // ---------------------------------------------------------------- context
@@ -255,7 +256,7 @@ int nesf_context_create(int32_t device, nesf_context** out) {
     c->work_capacity = 0;
     c->work_members = 0;
     cudaError_t e = cudaMalloc(&c->d_stats, sizeof(DevStats));
-    if (e == cudaSuccess) e = cudaMalloc(&c->d_replay_count, sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_replay_count, 2 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_stats, sizeof(DevStats));
     if (e != cudaSuccess) {
         cudaFree(c->d_stats);
@@ -324,18 +325,26 @@ static nesf_solver_options options_or_default(const nesf_solver_options* o) {
     nesf_solver_options r = *o;
     if (r.polish_maxiter <= 0) r.polish_maxiter = d.polish_maxiter;
     if (!(r.path_tolerance > 0)) r.path_tolerance = d.path_tolerance;
+    if (!(r.fp32_rho > 0)) r.fp32_rho = d.fp32_rho;
     return r;
 }
 
+// The kernels' knobs; fp32_rho = 0 keeps no FP32 result (NESF_F32_POLISH).
+static SolveOpts solve_opts(const nesf_solver_options& o) {
+    float rho = o.precision == NESF_F32_ADAPTIVE ? (float)(o.fp32_rho < 0.99 ? o.fp32_rho : 0.99) : 0.0f;
+    return SolveOpts{o.polish_maxiter, (float)o.path_tolerance, rho};
+}
+
 static int check_options(const nesf_solver_options& o, const char* who) {
-    if (o.precision != NESF_PLAIN_F64 && o.precision != NESF_F32_POLISH)
+    if (o.precision != NESF_PLAIN_F64 && o.precision != NESF_F32_POLISH && o.precision != NESF_F32_ADAPTIVE)
         return fail(NESF_ERR_ARG, "%s: precision %d", who, o.precision);
     if (o.warm_start) return fail(NESF_ERR_UNSUPPORTED, "%s: warm start needs nesf_coupling_step", who);
     return NESF_OK;
 }
 
-// The context's replay queue, grown to `cells` entries (caller holds ctx->lock).
-// Growing synchronises the device: size the first call for the largest grid.
+// The context's queues of deferred cells (replay and polish), grown to `cells`
+// entries each (caller holds ctx->lock). Growing synchronises the device: size
+// the first call for the largest grid.
 static int replay_queue(nesf_context* ctx, int64_t cells, ReplayQueue* q) {
     if (cells > ctx->replay_capacity) {
         cudaError_t e = cudaDeviceSynchronize();
@@ -343,7 +352,7 @@ static int replay_queue(nesf_context* ctx, int64_t cells, ReplayQueue* q) {
         cudaFree(ctx->d_replay);
         ctx->d_replay = nullptr;
         ctx->replay_capacity = 0;
-        NESF_CUDA(cudaMalloc(&ctx->d_replay, sizeof(uint32_t) * (size_t)cells));
+        NESF_CUDA(cudaMalloc(&ctx->d_replay, 2 * sizeof(uint32_t) * (size_t)cells));
         ctx->replay_capacity = cells;
     }
     q->idx = ctx->d_replay;
@@ -482,7 +491,7 @@ extern "C" int nesf_compute_atmosphere_ocean_fluxes(nesf_context* ctx, const nes
     WorkList wl;
     if ((r = replay_queue(ctx, ring, &rq))) return r;
     if ((r = work_list(ctx, ring, 1, &wl))) return r;
-    SolveOpts so{o.polish_maxiter, (float)o.path_tolerance};
+    SolveOpts so = solve_opts(o);
     return with_stats(ctx, stats, s, [&](DevStats* ds) {
         if (f->dtype == NESF_F64)
             return launch_ao(ao_args<double>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl, rq, ds,
@@ -545,7 +554,7 @@ extern "C" int nesf_compute_atmosphere_ocean_fluxes_ensemble(nesf_context* ctx, 
     WorkList wl;
     if ((r = replay_queue(ctx, ring * members, &rq))) return r;
     if ((r = work_list(ctx, ring, members, &wl))) return r;
-    SolveOpts so{o.polish_maxiter, (float)o.path_tolerance};
+    SolveOpts so = solve_opts(o);
     return with_stats(ctx, stats, s, [&](DevStats* ds) {
         if (f->dtype == NESF_F64)
             return launch_ao(ao_args<double>(f, member_stride), P64, P32, ctx->d_p64, ctx->d_p32, members,
@@ -606,7 +615,7 @@ extern "C" int nesf_compute_atmosphere_sea_ice_fluxes(nesf_context* ctx, const n
     WorkList wl;
     if ((r = replay_queue(ctx, ring, &rq))) return r;
     if ((r = work_list(ctx, ring, 1, &wl))) return r;
-    SolveOpts so{o.polish_maxiter, (float)o.path_tolerance};
+    SolveOpts so = solve_opts(o);
     return with_stats(ctx, stats, s, [&](DevStats* ds) {
         if (f->dtype == NESF_F64) return launch_ai(ai_args<double>(f), P64, P32, o.precision, so, wl, rq, ds, s);
         return launch_ai(ai_args<float>(f), P64, P32, o.precision, so, wl, rq, ds, s);
@@ -783,12 +792,13 @@ extern "C" int nesf_apply_air_sea_ice_radiative_fluxes(const nesf_assembly_param
 // would fail or force the pool to release memory), or a caller with a latency
 // budget that must not enter the driver's allocator. For them,
 // nesf_compute_atmosphere_ocean_fluxes_noalloc runs the atmosphere-ocean solve
-// without allocating anything: its scratch -- the compacted work list, the replay
-// queue and their counters -- is this file-scope array, which every GPU that loads
-// the library holds until the process exits: 64 counters (256 B) + two lists of
-// NESF_NOALLOC_MAX_CELLS uint32 entries, 16 MiB + 256 B in all.
+// without allocating anything: its scratch -- the compacted work list, the queues
+// of cells to replay and to polish, and their counters -- is this file-scope array,
+// which every GPU that loads the library holds until the process exits: 64
+// counters (256 B) + three lists of NESF_NOALLOC_MAX_CELLS uint32 entries, 24 MiB
+// + 256 B in all.
 #define NESF_NOALLOC_MAX_CELLS (1 << 21)
-static __device__ __align__(256) uint32_t g_noalloc_scratch[64 + 2 * (size_t)NESF_NOALLOC_MAX_CELLS];
+static __device__ __align__(256) uint32_t g_noalloc_scratch[64 + 3 * (size_t)NESF_NOALLOC_MAX_CELLS];
 
 static uint32_t* g_noalloc_ptr[64];   // device address of the array, per device
 static std::mutex g_noalloc_lock;
@@ -827,14 +837,14 @@ extern "C" int nesf_compute_atmosphere_ocean_fluxes_noalloc(const nesf_interface
                     "use nesf_compute_atmosphere_ocean_fluxes", who, (long long)ring, NESF_NOALLOC_MAX_CELLS);
     uint32_t* base = nullptr;
     if ((r = noalloc_scratch(&base))) return r;
-    // counters: [0, 1] work list (unstable, stable), [2] replay queue; both are
-    // cleared by the launch before the first pass reads them
+    // counters: [0, 1] work list (unstable, stable), [2, 3] replay and polish
+    // queues; the launch clears them before the first pass reads them
     WorkList wl{base + 64, base, ring};
     ReplayQueue rq{base + 64 + NESF_NOALLOC_MAX_CELLS, base + 2, NESF_NOALLOC_MAX_CELLS};
     DevIface<double> P64 = make_dev_iface<double>(*params);
     DevIface<float> P32 = make_dev_iface<float>(*params);
     bool skin = params->temperature_formulation != NESF_BULK_TEMPERATURE;
-    SolveOpts so{o.polish_maxiter, (float)o.path_tolerance};
+    SolveOpts so = solve_opts(o);
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = f->dtype == NESF_F64
                         ? launch_ao(ao_args<double>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl,

@@ -93,15 +93,18 @@ __global__ void frac_kernel(Layout2 L, nesf_exchange_coords c, nesf_atmos_grid a
 }
 
 // ------------------------------------------------------------- interpolation
+// Arithmetic in the storage type S: FP64 fields interpolate exactly as the
+// reference's Float64 kernels, FP32 fields as its Float32 ones (the weights from
+// the FP64 fractional indices, rounded once).
 template <class S>
-__device__ __forceinline__ double interp_one(const nesf_atmos_grid& ag, const S* __restrict__ d, int i0, int i1,
-                                             int j0, int j1, double xi, double eta, double tn) {
-    double v[2];
+__device__ __forceinline__ S interp_one(const nesf_atmos_grid& ag, const S* __restrict__ d, int i0, int i1, int j0,
+                                        int j1, S xi, S eta, S tn) {
+    S v[2];
 #pragma unroll
     for (int n = 0; n < 2; n++) {
         const S* b = d + (int64_t)n * ag.stride_t;
         auto at = [&](int ii, int jj) {
-            return (double)__ldg(b + (int64_t)(ii - 1 + ag.hx) + (int64_t)(jj - 1 + ag.hy) * ag.stride_j);
+            return __ldg(b + (int64_t)(ii - 1 + ag.hx) + (int64_t)(jj - 1 + ag.hy) * ag.stride_j);
         };
         v[n] = (1 - xi) * (1 - eta) * at(i0, j0) + (1 - xi) * eta * at(i0, j1) + xi * (1 - eta) * at(i1, j0) +
                xi * eta * at(i1, j1);
@@ -135,139 +138,143 @@ __global__ void __launch_bounds__(256) interp_kernel(InterpArgs<S> a) {
     }
     double fli = floor(fi), flj = floor(fj);
     int im = (int)fli, jm = (int)flj;
-    double xi = fi - fli, eta = fj - flj;
+    S xi = (S)(fi - fli), eta = (S)(fj - flj);
     int i0 = wrap_i(im, a.atmos.nx), i1 = wrap_i(im + 1, a.atmos.nx);
     int j0 = clamp_j(jm, a.atmos.ny), j1 = clamp_j(jm + 1, a.atmos.ny);
+    const S tn = (S)a.tn;
 #pragma unroll
     for (int n = 0; n < 9; n++) {
         if (!a.dst[n]) continue;
-        double v = a.src[n] ? interp_one(a.atmos, a.src[n], i0, i1, j0, j1, xi, eta, a.tn) : 0.0;
-        a.dst[n][k] = (S)v;
+        a.dst[n][k] = a.src[n] ? interp_one<S>(a.atmos, a.src[n], i0, i1, j0, j1, xi, eta, tn) : S(0);
     }
 }
 
 // ------------------------------------------------------------------ assembly
+// Arithmetic in the storage type S, as the interpolation.
 template <class S>
 __global__ void __launch_bounds__(256) assemble_ocean_kernel(AsmArgs<S> a, nesf_assembly_params p) {
+    using R = S;
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= (int64_t)a.L.nx * a.L.ny) return;
     int i = 1 + (int)(r % a.L.nx), j = 1 + (int)(r / a.L.nx);
     int64_t k = a.L.at(i, j), kw = k - 1, ks = k - a.L.sj;
-    double rinv = 1 / p.ocean_reference_density;
-    double cinv = 1 / p.ocean_heat_capacity;
-    double al = ldz(a.f.aleph, k);
-    double To = ld(a.f.To, k);
-    double Jr = ldz(a.f.rain, k), Js = ldz(a.f.snow, k), Ps = ldz(a.f.isnow, k), Jl = ldz(a.f.land_fw, k);
-    double QT = ld(a.f.ao_QT, k), Qv = ld(a.f.ao_Qv, k), Jv = ld(a.f.ao_Jv, k);
-    double SQao = (QT + Qv) * (1 - al);
-    double SFao = -(Jr + Jl + Js - Ps) * rinv + (1 - al) * Jv * rinv;
-    double Jwao = -SFao;
+    const R rinv = R(1) / R(p.ocean_reference_density);
+    const R cinv = R(1) / R(p.ocean_heat_capacity);
+    R al = ldzr<R>(a.f.aleph, k);
+    R To = ldr<R>(a.f.To, k);
+    R Jr = ldzr<R>(a.f.rain, k), Js = ldzr<R>(a.f.snow, k), Ps = ldzr<R>(a.f.isnow, k), Jl = ldzr<R>(a.f.land_fw, k);
+    R QT = ldr<R>(a.f.ao_QT, k), Qv = ldr<R>(a.f.ao_Qv, k), Jv = ldr<R>(a.f.ao_Jv, k);
+    R SQao = (QT + Qv) * (1 - al);
+    R SFao = -(Jr + Jl + Js - Ps) * rinv + (1 - al) * Jv * rinv;
+    R Jwao = -SFao;
     bool inactive = a.f.inactive ? a.f.inactive[k] != 0 : false;
-    double Qin = ldz(a.f.io_Q, k), Jsio = ldz(a.f.io_Js, k), Jwio = ldz(a.f.io_Jw, k);
-    double JTao = SQao * rinv * cinv;
-    double JTio = Qin * rinv * cinv;
-    double aw = ldz(a.f.aleph, kw), as = ldz(a.f.aleph, ks);
-    double tcx = rinv * (1 - al) * ld(a.f.ao_tx, k);
-    double tcxw = rinv * (1 - aw) * ld(a.f.ao_tx, kw);
-    double tcy = rinv * (1 - al) * ld(a.f.ao_ty, k);
-    double tcys = rinv * (1 - as) * ld(a.f.ao_ty, ks);
-    double txao = (tcxw + tcx) / 2;
-    double tyao = (tcys + tcy) / 2;
-    double txio = ldz(a.f.io_tx, k) * rinv * ((aw + al) / 2);
-    double tyio = ldz(a.f.io_ty, k) * rinv * ((as + al) / 2);
-    st(a.f.o_u, k, inactive ? 0.0 : txao + txio);
-    st(a.f.o_v, k, inactive ? 0.0 : tyao + tyio);
-    double JT = inactive ? 0.0 : JTao + JTio;
+    R Qin = ldzr<R>(a.f.io_Q, k), Jsio = ldzr<R>(a.f.io_Js, k), Jwio = ldzr<R>(a.f.io_Jw, k);
+    R JTao = SQao * rinv * cinv;
+    R JTio = Qin * rinv * cinv;
+    R aw = ldzr<R>(a.f.aleph, kw), as = ldzr<R>(a.f.aleph, ks);
+    R tcx = rinv * (1 - al) * ldr<R>(a.f.ao_tx, k);
+    R tcxw = rinv * (1 - aw) * ldr<R>(a.f.ao_tx, kw);
+    R tcy = rinv * (1 - al) * ldr<R>(a.f.ao_ty, k);
+    R tcys = rinv * (1 - as) * ldr<R>(a.f.ao_ty, ks);
+    R txao = (tcxw + tcx) / 2;
+    R tyao = (tcys + tcy) / 2;
+    R txio = ldzr<R>(a.f.io_tx, k) * rinv * ((aw + al) / 2);
+    R tyio = ldzr<R>(a.f.io_ty, k) * rinv * ((as + al) / 2);
+    st(a.f.o_u, k, inactive ? R(0) : txao + txio);
+    st(a.f.o_v, k, inactive ? R(0) : tyao + tyio);
+    R JT = inactive ? R(0) : JTao + JTio;
     if (a.with_radiation) {
         // apply_air_sea_radiative_fluxes fused: J_T += radiative part
-        double Ts = ld(a.f.ao_Ts, k) + p.interface_temperature_offset;
-        double T2 = Ts * Ts;
-        double Iup = p.stefan_boltzmann_constant * p.ocean_emissivity * (T2 * T2);
-        double Ia = -p.ocean_emissivity * ld(a.f.lw, k);
-        double It = -(1 - p.ocean_albedo) * ld(a.f.sw, k);
+        R Ts = ldr<R>(a.f.ao_Ts, k) + R(p.interface_temperature_offset);
+        R T2 = Ts * Ts;
+        R Iup = R(p.stefan_boltzmann_constant) * R(p.ocean_emissivity) * (T2 * T2);
+        R Ia = -R(p.ocean_emissivity) * ldr<R>(a.f.lw, k);
+        R It = -(1 - R(p.ocean_albedo)) * ldr<R>(a.f.sw, k);
         Ia *= (1 - al);
         It *= (1 - al);
-        double Iup_o = Iup * (1 - al);
-        double SQ = Iup_o + Ia + It;
-        double JTr = SQ * rinv * cinv;
-        JT += inactive ? 0.0 : JTr;
+        R Iup_o = Iup * (1 - al);
+        R SQ = Iup_o + Ia + It;
+        R JTr = SQ * rinv * cinv;
+        JT += inactive ? R(0) : JTr;
         st(a.f.o_up_lw, k, Iup);
         st(a.f.o_dn_lw, k, -Ia);
         st(a.f.o_dn_sw, k, -It);
     }
     st(a.f.o_T, k, JT);
-    st(a.f.o_S, k, inactive ? 0.0 : Jsio);
-    st(a.f.o_eta, k, inactive ? 0.0 : Jwao + Jwio);
-    st(a.f.o_H, k, inactive ? 0.0 : To * Jwao);
+    st(a.f.o_S, k, inactive ? R(0) : Jsio);
+    st(a.f.o_eta, k, inactive ? R(0) : Jwao + Jwio);
+    st(a.f.o_H, k, inactive ? R(0) : To * Jwao);
 }
 
 template <class S>
 __global__ void __launch_bounds__(256) assemble_ice_kernel(AsmArgs<S> a, nesf_assembly_params p) {
+    using R = S;
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= (int64_t)a.L.nx * a.L.ny) return;
     int i = 1 + (int)(r % a.L.nx), j = 1 + (int)(r / a.L.nx);
     int64_t k = a.L.at(i, j), kw = k - 1, ks = k - a.L.sj;
-    double al = ld(a.f.aleph, k);
-    double QT = ld(a.f.ai_QT, k), Qv = ld(a.f.ai_Qv, k);
-    double Qf = ldz(a.f.io_Qf, k), Qi = ldz(a.f.io_Q, k);
-    double Js = ldz(a.f.snow, k);
-    double SQt = (QT + Qv) * al;
-    double SQb = Qf + Qi;
+    R al = ldr<R>(a.f.aleph, k);
+    R QT = ldr<R>(a.f.ai_QT, k), Qv = ldr<R>(a.f.ai_Qv, k);
+    R Qf = ldzr<R>(a.f.io_Qf, k), Qi = ldzr<R>(a.f.io_Q, k);
+    R Js = ldzr<R>(a.f.snow, k);
+    R SQt = (QT + Qv) * al;
+    R SQb = Qf + Qi;
     bool inactive = a.f.inactive ? a.f.inactive[k] != 0 : false;
-    double top = inactive ? 0.0 : SQt;
+    R top = inactive ? R(0) : SQt;
     if (a.with_radiation) {
-        double Ts = ld(a.f.ai_Ts, k) + p.interface_temperature_offset;
-        double T2 = Ts * Ts;
-        double Iup = p.stefan_boltzmann_constant * p.ice_emissivity * (T2 * T2);
-        double Ia = -p.ice_emissivity * ld(a.f.lw, k);
-        double It = -(1 - p.ice_albedo) * ld(a.f.sw, k);
-        double SQ = (Iup + Ia + It) * al;
-        top += inactive ? 0.0 : SQ;
+        R Ts = ldr<R>(a.f.ai_Ts, k) + R(p.interface_temperature_offset);
+        R T2 = Ts * Ts;
+        R Iup = R(p.stefan_boltzmann_constant) * R(p.ice_emissivity) * (T2 * T2);
+        R Ia = -R(p.ice_emissivity) * ldr<R>(a.f.lw, k);
+        R It = -(1 - R(p.ice_albedo)) * ldr<R>(a.f.sw, k);
+        R SQ = (Iup + Ia + It) * al;
+        top += inactive ? R(0) : SQ;
         st(a.f.i_up_lw, k, Iup);
         st(a.f.i_dn_lw, k, -Ia);
         st(a.f.i_dn_sw, k, -It);
     }
     st(a.f.i_top, k, top);
-    st(a.f.i_snow, k, inactive ? 0.0 : Js);
-    st(a.f.i_u, k, inactive ? 0.0 : (ld(a.f.ai_tx, kw) + ld(a.f.ai_tx, k)) / 2);
-    st(a.f.i_v, k, inactive ? 0.0 : (ld(a.f.ai_ty, ks) + ld(a.f.ai_ty, k)) / 2);
-    st(a.f.i_bottom, k, inactive ? 0.0 : SQb);
+    st(a.f.i_snow, k, inactive ? R(0) : Js);
+    st(a.f.i_u, k, inactive ? R(0) : (ldr<R>(a.f.ai_tx, kw) + ldr<R>(a.f.ai_tx, k)) / 2);
+    st(a.f.i_v, k, inactive ? R(0) : (ldr<R>(a.f.ai_ty, ks) + ldr<R>(a.f.ai_ty, k)) / 2);
+    st(a.f.i_bottom, k, inactive ? R(0) : SQb);
 }
 
 // Radiation alone, added in place to an already assembled J_T / top heat flux.
 template <class S, bool ICE>
 __global__ void __launch_bounds__(256) radiation_kernel(AsmArgs<S> a, nesf_assembly_params p) {
+    using R = S;
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= (int64_t)a.L.nx * a.L.ny) return;
     int i = 1 + (int)(r % a.L.nx), j = 1 + (int)(r / a.L.nx);
     int64_t k = a.L.at(i, j);
     bool inactive = a.f.inactive ? a.f.inactive[k] != 0 : false;
     if (!ICE) {
-        double rinv = 1 / p.ocean_reference_density, cinv = 1 / p.ocean_heat_capacity;
-        double al = ldz(a.f.aleph, k);
-        double Ts = ld(a.f.ao_Ts, k) + p.interface_temperature_offset;
-        double T2 = Ts * Ts;
-        double Iup = p.stefan_boltzmann_constant * p.ocean_emissivity * (T2 * T2);
-        double Ia = -p.ocean_emissivity * ld(a.f.lw, k);
-        double It = -(1 - p.ocean_albedo) * ld(a.f.sw, k);
+        const R rinv = R(1) / R(p.ocean_reference_density), cinv = R(1) / R(p.ocean_heat_capacity);
+        R al = ldzr<R>(a.f.aleph, k);
+        R Ts = ldr<R>(a.f.ao_Ts, k) + R(p.interface_temperature_offset);
+        R T2 = Ts * Ts;
+        R Iup = R(p.stefan_boltzmann_constant) * R(p.ocean_emissivity) * (T2 * T2);
+        R Ia = -R(p.ocean_emissivity) * ldr<R>(a.f.lw, k);
+        R It = -(1 - R(p.ocean_albedo)) * ldr<R>(a.f.sw, k);
         Ia *= (1 - al);
         It *= (1 - al);
-        double Iup_o = Iup * (1 - al);
-        double SQ = Iup_o + Ia + It;
-        double JT = SQ * rinv * cinv;
-        a.f.o_T[k] = (S)((double)a.f.o_T[k] + (inactive ? 0.0 : JT));
+        R Iup_o = Iup * (1 - al);
+        R SQ = Iup_o + Ia + It;
+        R JT = SQ * rinv * cinv;
+        a.f.o_T[k] = a.f.o_T[k] + (inactive ? R(0) : JT);
         st(a.f.o_up_lw, k, Iup);
         st(a.f.o_dn_lw, k, -Ia);
         st(a.f.o_dn_sw, k, -It);
     } else {
-        double al = ld(a.f.aleph, k);
-        double Ts = ld(a.f.ai_Ts, k) + p.interface_temperature_offset;
-        double T2 = Ts * Ts;
-        double Iup = p.stefan_boltzmann_constant * p.ice_emissivity * (T2 * T2);
-        double Ia = -p.ice_emissivity * ld(a.f.lw, k);
-        double It = -(1 - p.ice_albedo) * ld(a.f.sw, k);
-        double SQ = (Iup + Ia + It) * al;
-        a.f.i_top[k] = (S)((double)a.f.i_top[k] + (inactive ? 0.0 : SQ));
+        R al = ldr<R>(a.f.aleph, k);
+        R Ts = ldr<R>(a.f.ai_Ts, k) + R(p.interface_temperature_offset);
+        R T2 = Ts * Ts;
+        R Iup = R(p.stefan_boltzmann_constant) * R(p.ice_emissivity) * (T2 * T2);
+        R Ia = -R(p.ice_emissivity) * ldr<R>(a.f.lw, k);
+        R It = -(1 - R(p.ice_albedo)) * ldr<R>(a.f.sw, k);
+        R SQ = (Iup + Ia + It) * al;
+        a.f.i_top[k] = a.f.i_top[k] + (inactive ? R(0) : SQ);
         st(a.f.i_up_lw, k, Iup);
         st(a.f.i_dn_lw, k, -Ia);
         st(a.f.i_dn_sw, k, -It);

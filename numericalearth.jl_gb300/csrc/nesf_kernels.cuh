@@ -81,6 +81,10 @@ template <class S> __device__ __forceinline__ double ld(const S* p, int64_t k) {
 template <class S> __device__ __forceinline__ float ldf(const S* p, int64_t k) { return (float)__ldg(p + k); }
 template <class S> __device__ __forceinline__ double ldz(const S* p, int64_t k) { return p ? (double)__ldg(p + k) : 0.0; }
 template <class S, class R> __device__ __forceinline__ void st(S* p, int64_t k, R v) { if (p) p[k] = (S)v; }
+// loads converted to the arithmetic type R of a kernel (the storage type of the
+// streaming kernels: FP32 fields are computed in FP32, FP64 fields in FP64)
+template <class R, class S> __device__ __forceinline__ R ldr(const S* p, int64_t k) { return (R)__ldg(p + k); }
+template <class R, class S> __device__ __forceinline__ R ldzr(const S* p, int64_t k) { return p ? (R)__ldg(p + k) : R(0); }
 
 // --------------------------------------------------------------- statistics
 struct DevStats {

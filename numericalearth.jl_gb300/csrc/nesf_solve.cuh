@@ -11,6 +11,12 @@
 //         leaves that much room there -- are queued for a replay of the
 //         reference's FP64 iteration from the start, which a second, packed
 //         kernel runs. Replaying them in place would idle the other 31 lanes.
+// ADAPTIVE POLISH, except that a cell keeps its FP32 result when every state
+//         component converged at FP32 resolution and F contracts by at most
+//         `fp32_rho`: the scales then carry the FP32 evaluation error (a few ulps,
+//         the differences that cancel being anchored in FP64, see the delta form
+//         below) amplified by 1 / (1 - rho). The other cells are queued for a
+//         packed pass that polishes them in FP64.
 #pragma once
 
 #include "nesf_kernels.cuh"
@@ -21,6 +27,7 @@ namespace nesf {
 struct SolveOpts {
     int polish_steps;   // FP64 Newton steps
     float path_tol;     // replay threshold on the reference's stopping-error bound
+    float fp32_rho;     // ADAPTIVE: keep the FP32 result below this contraction (0: never)
 };
 
 // Active cells of one solve, compacted and split by the sign of the surface
@@ -33,10 +40,13 @@ struct WorkList {
     int64_t per_member;
 };
 
-// Cells whose FP64 replay is deferred to the second pass.
+// Cells deferred to the packed passes. idx holds 2 * capacity entries: cells to
+// replay in FP64 at [0, capacity), cells to polish (ADAPTIVE) at [capacity, 2 *
+// capacity); count[0] and count[1] are their numbers (zeroed before the solve).
+// A cell that the polish pass sends on to the replay holds one entry in each.
 struct ReplayQueue {
     uint32_t* idx;          // linear cell ids (member * ring + ring index)
-    unsigned int* count;    // number of queued cells (zeroed before the first pass)
+    unsigned int* count;
     int64_t capacity;
 };
 
@@ -69,42 +79,6 @@ struct SweepTrace {
     float lam;      // |d_k|_1 / |d_(k-1)|_1
 };
 
-// Runs the FP32 fixed point from the reference's start. Returns the number of
-// FP32 iterations and sets `state`: 0 converged (drift < tol), 1 stalled at FP32
-// resolution, 2 reached maxiter.
-template <bool SKIN>
-__device__ __forceinline__ int f32_sweep(const DevIface<float>& P, const CellConst<float>& c, SurfaceConst<float>& s,
-                                         float& us, float& ts, float& qst, int maxiter, int& state, SweepTrace& tr) {
-    int it = 0;
-    float prev = M<float>::inf();
-    int rising = 0;
-    state = 2;
-    tr.d[0] = tr.d[1] = tr.d[2] = 0.0f;
-    tr.lam = 1.0f;
-    while (it < maxiter) {
-        float u0 = us, t0 = ts, q0 = qst;
-        iterate_state<float, SKIN>(P, c, s, us, ts, qst);
-        it++;
-        float du = fabsf(us - u0), dt = fabsf(ts - t0), dq = fabsf(qst - q0);
-        float drift = du + dt + dq;
-        // FP32 resolution of the drift sum: the ulps of the scales themselves
-        float res = 1.1920929e-7f * (fabsf(us) + fabsf(ts) + fabsf(qst));
-        if (drift > 64.0f * res || it <= 2) {
-            tr.d[0] = du; tr.d[1] = dt; tr.d[2] = dq;
-            tr.lam = it > 1 ? drift / prev : 1.0f;
-        }
-        if (drift < P.tol) { state = 0; break; }
-        if (drift <= 8.0f * res) { state = 1; break; }
-        if (drift <= 1024.0f * res && drift >= prev) {
-            if (++rising >= 2) { state = 1; break; }
-        } else {
-            rising = 0;
-        }
-        prev = drift;
-    }
-    return it;
-}
-
 template <class R, class Q>
 __device__ __forceinline__ void convert_const(const CellConst<R>& a, CellConst<Q>& b) {
     b.ua = Q(a.ua); b.va = Q(a.va); b.Ta = Q(a.Ta); b.pa = Q(a.pa); b.qa = Q(a.qa);
@@ -119,6 +93,144 @@ __device__ __forceinline__ void convert_surface(const SurfaceConst<R>& a, Surfac
     b.Ts = Q(a.Ts); b.qs = Q(a.qs); b.dth = Q(a.dth); b.dq = Q(a.dq);
     b.gTv = Q(a.gTv); b.A1 = Q(a.A1); b.A2 = Q(a.A2);
     b.nu_u = Q(a.nu_u); b.nu_t = Q(a.nu_t); b.nu_q = Q(a.nu_q);
+}
+
+// ------------------------------------------------ FP32 skin map in delta form
+// The FP32 sweep of a skin temperature carries tau = T_s - theta_a instead of
+// T_s. theta_a - T_s nearly cancels where the surface is close to the air
+// temperature, and an FP32 T_s resolves only ~1.5e-5 K at 270 K: carried as tau,
+// dtheta = -tau keeps FP32's relative precision. The other differences that
+// cancel are anchored the same way, in FP64 once per cell: q_a - q_s(T_s) as
+// (q_a - q_s(theta_a)) - (q_s(T_s) - q_s(theta_a)), the second term from the
+// Clausius-Clapeyron ratio e_sat(T_s) / e_sat(theta_a) (log1p / expm1 of a small
+// argument); and the net surface flux Q_v + I_up + Q_d as (I_up(theta_a) + Q_d)
+// + (I_up(T_s) - I_up(theta_a)) + Q_v, I_up(T_s) - I_up(theta_a) from
+// (1 + tau / theta_a)^4 - 1. The map is the reference's map; only its rounding
+// differs. The FP64 polish and replay evaluate the reference's form.
+template <class R> struct SkinAnchor {
+    R dTi, dTb, dTm;   // interior, conductive-base and melting temperatures minus theta_a
+    R pva, qsa, dqa;   // x e_sat(theta_a), q_s(theta_a) (no saturation cap), q_a - q_s(theta_a)
+    R Qa0, Iupa;       // I_up(theta_a) + Q_d, I_up(theta_a) = sigma eps theta_a^4
+    R gA, gK;          // ln e_sat(T) = gA ln T - gK / T + const
+};
+
+__device__ __forceinline__ SkinAnchor<float> skin_anchor(const DevIface<double>& P, const CellConst<double>& c) {
+    const double tha = c.tha;
+    SkinAnchor<float> a;
+    a.dTi = (float)(c.Ti - tha);
+    double Tb = P.Tfw - P.slope * c.Si;
+    Tb = Tb + P.off_ifc;
+    a.dTb = (float)(Tb - tha);
+    a.dTm = (float)(P.Tfw + P.off_ifc - tha);
+    double pv = P.x * esat(P, tha, P.phase);
+    double qsa = P.einv * pv / (c.pa - (1.0 - P.einv) * pv);
+    a.pva = (float)pv;
+    a.qsa = (float)qsa;
+    a.dqa = (float)(c.qa - qsa);
+    double sigma = P.has_rad ? P.sigma : 0.0, eps = P.has_rad ? P.emis : 0.0;
+    double alb = P.has_rad ? P.alb : 0.0, SW = P.has_rad ? c.sw : 0.0, LW = P.has_rad ? c.lw : 0.0;
+    double T2 = tha * tha;
+    double Iup = sigma * eps * (T2 * T2);
+    double Qd = -(1.0 - alb) * SW - eps * LW;
+    a.Iupa = (float)Iup;
+    a.Qa0 = (float)(Iup + Qd);
+    double LH0 = P.phase == NESF_PHASE_ICE ? P.Ls0 : P.Lv0;
+    double cpc = P.phase == NESF_PHASE_ICE ? P.cpi : P.cpl;
+    double dcp = P.cpv - cpc;
+    a.gA = (float)(dcp / P.Rv);
+    a.gK = (float)((LH0 - dcp * P.T0) / P.Rv);
+    return a;
+}
+
+// flux_balance_temperature (interface_states.jl:434-457 diffusive, 468-524
+// conductive) + the clamps of compute_interface_temperature, as tau -> tau'.
+// `cond` (optional) receives the condition number of the update: the sum of the
+// magnitudes of the terms that make up T_st - theta_a over the magnitude of their
+// sum (1 where T_s is pinned), by which FP32 rounding of the terms is amplified.
+template <class R>
+__device__ __forceinline__ R skin_tau(const DevIface<R>& P, const CellConst<R>& c, const SkinAnchor<R>& A, R tau,
+                                      R us, R ts, R qst, R* cond = nullptr) {
+    R r = tau / c.tha;
+    R dI = A.Iupa * (r * (R(4) + r * (R(6) + r * (R(4) + r))));   // I_up(T_s) - I_up(theta_a)
+    R QT = -c.rho_a * c.cp_a * us * ts;
+    R Qv = -c.rho_a * c.L_s * us * qst;
+    R Qa = A.Qa0 + dI + Qv;
+    R dT = -tau;                                                    // theta_a - T_s
+    if (P.temp_form == NESF_SKIN_TEMPERATURE_DIFFUSIVE) {
+        R kap = c.kappa >= R(0) ? M<R>::fmax(c.kappa, P.kap_diff) : P.kap_diff;
+        R del = P.del_diff;
+        R lam = R(1) / (P.rho_i * P.c_i);
+        R JT = Qa * lam;
+        R OmT = QT * lam;
+        R D = kap * dT - OmT * del;
+        R n1 = A.dTi * kap * dT, n2 = JT * dT * del;
+        R tst = (n1 - n2) / D;                                       // T_st - theta_a
+        tst = D == R(0) ? tau : tst;
+        R dev = tst - A.dTi;
+        if (cond) {
+            R qa_mag = (fabs(A.Qa0) + fabs(dI) + fabs(Qv)) / fmax(fabs(Qa), R(1e-30));
+            *cond = fabs(dev) > P.max_dT ? R(1) : (fabs(n1) + fabs(n2) * qa_mag) / fmax(fabs(n1 - n2), R(1e-30));
+        }
+        return A.dTi + clampr(dev, -P.max_dT, P.max_dT);
+    }
+    R Rth = P.k_snow > R(0) ? c.hs / P.k_snow + c.hi / P.k_ice : c.hi / P.k_ice;
+    R Om = dT == R(0) ? R(0) : QT / dT;
+    R beta = R(4) * (A.Iupa + dI) / (c.tha + tau);
+    R D = R(1) + beta * Rth - Om * Rth;
+    R n2 = beta * Rth * tau;
+    R tst = (A.dTb + n2 - Qa * Rth) / D;
+    tst = D == R(0) ? tau : tst;
+    tst = isnan(tst) ? tau : tst;
+    R tp = tau + clampr(tst - tau, -P.max_dT, P.max_dT);
+    bool free = tp < A.dTm && c.hi >= c.hc;
+    if (cond) {
+        R mag = fabs(A.dTb) + fabs(n2) + Rth * (fabs(A.Qa0) + fabs(dI) + fabs(Qv));
+        *cond = free ? mag / fmax(fabs(A.dTb + n2 - Qa * Rth), R(1e-30)) : R(1);
+    }
+    tp = M<R>::fmin(tp, A.dTm);
+    return c.hi >= c.hc ? tp : A.dTb;
+}
+
+// One FP32 application of F to (u*, theta*, q*, tau) (iterate_interface_state).
+// `cond` (optional) receives the larger condition number of the two anchored
+// differences, q_a - q_s and the temperature update.
+template <class R>
+__device__ __forceinline__ void iterate_skin_delta(const DevIface<R>& P, const CellConst<R>& c,
+                                                   const SkinAnchor<R>& A, R& us, R& ts, R& qst, R& tau,
+                                                   R* cond = nullptr) {
+    R t1 = skin_tau(P, c, A, tau, us, ts, qst, cond);
+    R T = c.tha + t1;
+    R g = A.gA * log1pf(t1 / c.tha) + A.gK * t1 / (c.tha * T);    // ln e_sat(T) - ln e_sat(theta_a)
+    R dpv = A.pva * expm1f(g);
+    R pv = A.pva + dpv;
+    R c2 = R(1) - P.einv;
+    SurfaceConst<R> s;
+    if (!(pv > R(0.999) * c.pa)) {
+        R dqs = P.einv * c.pa * dpv / ((c.pa - c2 * pv) * (c.pa - c2 * A.pva));   // q_s(T) - q_s(theta_a)
+        s.qs = A.qsa + dqs;
+        s.dq = A.dqa - dqs;
+        if (cond) *cond = fmax(*cond, (fabs(A.dqa) + fabs(dqs)) / fmax(fabs(s.dq), R(1e-30)));
+    } else {
+        R pvc = R(0.999) * c.pa;   // the saturation cap of surface_specific_humidity
+        s.qs = P.einv * pvc / (c.pa - c2 * pvc);
+        s.dq = c.qa - s.qs;
+    }
+    s.Ts = T;
+    s.dth = -t1;
+    R Tv = virtual_temperature(P, T, s.qs);
+    R delta = P.eps - R(1);
+    s.gTv = P.g / Tv;
+    s.A1 = R(1) + delta * s.qs;
+    s.A2 = delta * Tv;
+    s.nu_u = air_viscosity(P.rough[0], T);
+    s.nu_t = air_viscosity(P.rough[1], T);
+    s.nu_q = air_viscosity(P.rough[2], T);
+    R a, b, d;
+    iterate_fluxes(P, c, s, us, ts, qst, a, b, d);
+    us = a;
+    ts = b;
+    qst = d;
+    tau = t1;
 }
 
 // One application of the fixed-point map F (iterate_interface_state) to the
@@ -188,15 +300,6 @@ __device__ __forceinline__ float state_floor(int i) {
     return i == 0 ? 1e-4f : (i == 1 ? 1e-5f : (i == 2 ? 1e-8f : 1e-3f));
 }
 
-// FP32 sweep + FP64 Newton polish. Returns false when the cell must replay the
-// reference's FP64 iteration (us, ts, qst, s64 are then untouched). On success
-// the solution is in us, ts, qst and s64 (interface temperature); `fp32_it`
-// counts FP32 map evaluations and `fp64_it` FP64 ones.
-//
-// The FP32 sweep and the N + 1 evaluations of the finite-difference Jacobian run
-// through one loop around a single inlined copy of the map, so a warp executes
-// the same instructions for both: the kernel's hot code stays small enough for
-// the instruction cache.
 // Central-difference step of the Jacobian column of state component k: large
 // enough that FP32 rounding of F (T_s carries only ~1.5e-5 K at 270 K) stays far
 // below the difference, small enough that the O(h^2) curvature error is negligible.
@@ -206,19 +309,96 @@ __device__ __forceinline__ float jac_step(int k, float xk) {
 
 enum ReplayReason { REPLAY_CALM = 0, REPLAY_NO_FP32 = 1, REPLAY_SLOW = 2, REPLAY_BOUND = 3, REPLAY_SINGULAR = 4 };
 
+// What solve_fast decided for a cell.
+enum FastOutcome { FAST_SOLVED = 0, FAST_POLISH = 1, FAST_REPLAY = 2 };
+
+// Infinity norm (max row sum) of an N x N matrix.
+template <int N>
+__device__ __forceinline__ float inf_norm(const float (&a)[N][N]) {
+    float n = 0.0f;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        float r = 0.0f;
+#pragma unroll
+        for (int j = 0; j < N; j++) r += fabsf(a[i][j]);
+        n = fmaxf(n, r);   // fmaxf drops a NaN row: the caller checks the sum below
+    }
+    return n;
+}
+
+// Upper bound of the spectral radius of J from Gelfand's formula on the 32nd
+// power, ||J^32||^(1/32) >= rho(J) in any induced norm; J^32 comes from five
+// squarings with the norm taken out at each. Unlike a power-iteration ratio it
+// is not fooled by a complex pair of dominant eigenvalues (a damped rotation of
+// the state, common with a skin temperature). +inf when J holds a NaN.
+template <int N>
+__device__ __forceinline__ float spectral_bound(const float (&J)[N][N]) {
+    float A[N][N];
+    float chk = 0.0f;
+#pragma unroll
+    for (int i = 0; i < N; i++)
+#pragma unroll
+        for (int j = 0; j < N; j++) { A[i][j] = J[i][j]; chk += J[i][j]; }
+    if (chk != chk) return M<float>::inf();
+    float e = 0.0f;   // J^(2^s) = A * exp(e)
+#pragma unroll 1
+    for (int s = 0; s < 5; s++) {
+        float n = inf_norm<N>(A);
+        if (!(n > 0.0f)) return 0.0f;   // nilpotent at FP32 resolution
+        e = 2.0f * (e + logf(n));
+        float inv = 1.0f / n;
+        float B[N][N];
+#pragma unroll
+        for (int i = 0; i < N; i++)
+#pragma unroll
+            for (int j = 0; j < N; j++) B[i][j] = A[i][j] * inv;
+#pragma unroll
+        for (int i = 0; i < N; i++)
+#pragma unroll
+            for (int j = 0; j < N; j++) {
+                float t = 0.0f;
+#pragma unroll
+                for (int k = 0; k < N; k++) t += B[i][k] * B[k][j];
+                A[i][j] = t;
+            }
+    }
+    float n = inf_norm<N>(A);
+    if (!(n > 0.0f)) return 0.0f;
+    return expf((logf(n) + e) * (1.0f / 32.0f));
+}
+
+// FP32 sweep + FP64 Newton polish. On FAST_SOLVED the solution is in us, ts, qst
+// and s64 (interface temperature); on FAST_POLISH (only with accept32: the FP32
+// result is not good enough and the cell goes to the packed polish pass) and
+// FAST_REPLAY (the cell must follow the reference's FP64 iteration; `reason`
+// says why) us, ts, qst and s64 are untouched. `fp32_it` counts FP32 map
+// evaluations and `fp64_it` FP64 ones.
+//
+// accept32 (ADAPTIVE): the sweep runs until every component, not just the drift
+// sum, is converged at FP32 resolution, and the FP32 result is kept when F
+// contracts by at most so.fp32_rho. On FAST_SOLVED s64.Ts is the interface
+// temperature; the rest of s64 is not updated.
+//
+// The FP32 sweep and the 2N evaluations of the central-difference Jacobian run
+// through one loop around a single inlined copy of the map, so a warp executes
+// the same instructions for both: the kernel's hot code stays small enough for
+// the instruction cache.
 template <bool SKIN>
-__device__ __forceinline__ bool solve_fast(const DevIface<double>& P64, const DevIface<float>& P32,
-                                           const CellConst<double>& c64, SurfaceConst<double>& s64, double& us,
-                                           double& ts, double& qst, const SolveOpts& so, int& fp32_it,
-                                           int& fp64_it, int& reason) {
+__device__ __forceinline__ int solve_fast(const DevIface<double>& P64, const DevIface<float>& P32,
+                                          const CellConst<double>& c64, SurfaceConst<double>& s64, double& us,
+                                          double& ts, double& qst, const SolveOpts& so, bool accept32, int& fp32_it,
+                                          int& fp64_it, int& reason) {
     constexpr int N = SKIN ? 4 : 3;
     fp64_it = 0;
     CellConst<float> c32;
     SurfaceConst<float> s32;
     convert_const(c64, c32);
     convert_surface(s64, s32);
+    SkinAnchor<float> anc{};
+    if (SKIN) anc = skin_anchor(P64, c64);
     const float tol = (float)P64.tol;
-    float x[4] = {(float)us, (float)ts, (float)qst, SKIN ? s32.Ts : 0.0f};   // sweep state
+    // sweep state; a skin temperature as tau = T_s - theta_a (the delta form)
+    float x[4] = {(float)us, (float)ts, (float)qst, SKIN ? (float)(s64.Ts - c64.tha) : 0.0f};
     float yp[4] = {0, 0, 0, 0};   // F(x + h e_j) of the column in progress
     float J[N][N];
     SweepTrace tr;
@@ -226,9 +406,11 @@ __device__ __forceinline__ bool solve_fast(const DevIface<double>& P64, const De
     tr.lam = 1.0f;
     float prev = M<float>::inf();
     int rising = 0;
+    bool stalled = false;  // the sweep ended on the rising-drift rule
     int it = 0;            // sweep iterations
     int phase = 0;         // 0 sweep; 2 + 2j / 3 + 2j: F(x + h e_j) / F(x - h e_j)
     float h = 0.0f;
+    float cond = 1.0f;     // condition of the anchored differences at the last sweep iterate
     const int limit = P32.maxiter;
 #pragma unroll 1
     for (;;) {
@@ -240,14 +422,20 @@ __device__ __forceinline__ bool solve_fast(const DevIface<double>& P64, const De
             for (int k = 0; k < 4; k++)
                 if (k == jj) { h = jac_step(k, x[k]); xin[k] += sgn * h; }
         }
-        SurfaceConst<float> sv = s32;
-        if (SKIN) sv.Ts = xin[3];
-        float yu = xin[0], yt = xin[1], yq = xin[2];
-        iterate_state<float, SKIN>(P32, c32, sv, yu, yt, yq);
-        float y[4] = {yu, yt, yq, SKIN ? sv.Ts : 0.0f};
+        float yu = xin[0], yt = xin[1], yq = xin[2], yT = xin[3];
+        if (SKIN) {
+            float cd = 1.0f;
+            iterate_skin_delta<float>(P32, c32, anc, yu, yt, yq, yT, &cd);
+            if (phase == 0) cond = cd;
+        } else {
+            SurfaceConst<float> sv = s32;
+            iterate_state<float, false>(P32, c32, sv, yu, yt, yq);
+        }
+        float y[4] = {yu, yt, yq, yT};
         if (phase == 0) {
             it++;
             float du = fabsf(y[0] - x[0]), dt = fabsf(y[1] - x[1]), dq = fabsf(y[2] - x[2]);
+            float dT = SKIN ? fabsf(y[3] - x[3]) : 0.0f;
             float drift = du + dt + dq;
 #pragma unroll
             for (int k = 0; k < 4; k++) x[k] = y[k];
@@ -257,18 +445,24 @@ __device__ __forceinline__ bool solve_fast(const DevIface<double>& P64, const De
                 tr.d[0] = du; tr.d[1] = dt; tr.d[2] = dq;
                 tr.lam = it > 1 ? drift / prev : 1.0f;
             }
-            bool done = drift < tol || drift <= 8.0f * res;
-            if (!done && drift <= 1024.0f * res && drift >= prev) done = ++rising >= 2;
+            // each component within 4 of its own ulps (ADAPTIVE), or the sum within 8
+            const float u4 = 4.0f * 1.1920929e-7f;
+            // (tau to 1e-7 K besides: dtheta = -tau)
+            bool quiet = accept32 ? (du <= u4 * fabsf(x[0]) && dt <= u4 * fabsf(x[1]) && dq <= u4 * fabsf(x[2]) &&
+                                     dT <= u4 * fabsf(x[3]) + 1e-7f)
+                                  : drift <= 8.0f * res;
+            bool done = drift < tol || quiet;
+            if (!done && drift <= 1024.0f * res && drift >= prev) { done = ++rising >= 2; stalled = done; }
             else if (!done) rising = 0;
             prev = drift;
             if (done) {
                 // calm cells: the reference's absolute drift rule leaves tol / u* of relative room
-                if (fabsf(x[0]) * so.path_tol < tol) { fp32_it = it; reason = REPLAY_CALM; return false; }
+                if (fabsf(x[0]) * so.path_tol < tol) { fp32_it = it; reason = REPLAY_CALM; return FAST_REPLAY; }
                 phase = 2;
             } else if (it >= limit) {
                 fp32_it = it;
                 reason = REPLAY_NO_FP32;
-                return false;                             // no FP32 convergence
+                return FAST_REPLAY;                       // no FP32 convergence
             }
         } else if (!(phase & 1)) {
 #pragma unroll
@@ -287,12 +481,16 @@ __device__ __forceinline__ bool solve_fast(const DevIface<double>& P64, const De
         }
     }
     fp32_it = it + 2 * N;
-    // ---- spectral radius and dominant mode of J (power iteration from the last drift)
+    // ---- contraction rate of F at the solution
+    const float rho_est = spectral_bound<N>(J);
+    if (!(rho_est < 0.995f)) { reason = REPLAY_SLOW; return FAST_REPLAY; }
+    // ---- the reference's stopping error along its slowest mode: e = rho / (1 - rho) d, |d|_1 < tol.
+    // Mode shape: power iteration from the last drift (each component's largest share over the
+    // last two iterates, which a rotating complex mode alternates between), or the last drift.
     float v[4] = {tr.d[0], tr.d[1], tr.d[2], 0.0f};
     float vn = v[0] + v[1] + v[2];
-    float rho_est = 0.0f;
     if (vn > 0.0f) {
-        float rho = tr.lam, r2 = 0.0f;
+        float frac[3] = {v[0] / vn, v[1] / vn, v[2] / vn};
 #pragma unroll
         for (int k = 0; k < 8; k++) {
             float w[4] = {0.0f, 0.0f, 0.0f, 0.0f};
@@ -300,27 +498,37 @@ __device__ __forceinline__ bool solve_fast(const DevIface<double>& P64, const De
             for (int ii = 0; ii < N; ii++)
 #pragma unroll
                 for (int jj = 0; jj < N; jj++) w[ii] += J[ii][jj] * v[jj];
-            float wn = 0.0f, vs = 0.0f;
+            float wn = 0.0f;
 #pragma unroll
-            for (int ii = 0; ii < N; ii++) { wn += fabsf(w[ii]); vs += fabsf(v[ii]); }
-            float g = vs > 0.0f ? wn / vs : 0.0f;
-            if (k >= 6) r2 = k == 6 ? g : sqrtf(r2 * g);   // geometric mean of the last two ratios
-            float inv = wn > 0.0f ? 1.0f / wn : 0.0f;
+            for (int ii = 0; ii < N; ii++) wn += fabsf(w[ii]);
+            if (!(wn > 0.0f)) break;          // J nilpotent on the drift: keep the drift's shape
+            float inv = 1.0f / wn;
 #pragma unroll
-            for (int ii = 0; ii < N; ii++) v[ii] = w[ii] * inv;   // signed: the spectral radius of J, not of |J|
+            for (int ii = 0; ii < N; ii++) v[ii] = w[ii] * inv;   // signed: J's modes, not |J|'s
+            float mn = fabsf(v[0]) + fabsf(v[1]) + fabsf(v[2]);
+            if (k >= 6 && mn > 0.0f) {
+#pragma unroll
+                for (int ii = 0; ii < 3; ii++) frac[ii] = k == 6 ? fabsf(v[ii]) / mn : fmaxf(frac[ii], fabsf(v[ii]) / mn);
+            }
         }
-        rho = r2 > 0.0f ? r2 : rho;
-        rho_est = rho;
-        // ---- the reference's stopping error along the mode: e = rho / (1 - rho) d, |d|_1 < tol
-        if (!(rho < 0.995f)) { reason = REPLAY_SLOW; return false; }
-        // mode shape: the power iteration's vector, or the last drift when J is nilpotent
-        float mn = fabsf(v[0]) + fabsf(v[1]) + fabsf(v[2]);
-        float k = rho / (1.0f - rho) * tol;
+        float kb = rho_est / (1.0f - rho_est) * tol;
 #pragma unroll
-        for (int ii = 0; ii < 3; ii++) {
-            float frac = r2 > 0.0f && mn > 0.0f ? fabsf(v[ii]) / mn : tr.d[ii] / vn;
-            if (!(k * frac <= so.path_tol * fmaxf(fabsf(x[ii]), state_floor(ii)))) { reason = REPLAY_BOUND; return false; }
+        for (int ii = 0; ii < 3; ii++)
+            if (!(kb * frac[ii] <= so.path_tol * fmaxf(fabsf(x[ii]), state_floor(ii)))) {
+                reason = REPLAY_BOUND;
+                return FAST_REPLAY;
+            }
+    }
+    // ---- ADAPTIVE: keep the FP32 result of a quiet, well-contracting cell
+    if (accept32) {
+        // FP32 rounding of the anchored terms (~1e-7 of each), amplified by their
+        // cancellation and by 1 / (1 - rho), must stay within path_tol
+        if (!stalled && rho_est <= so.fp32_rho && cond * 1.2e-7f <= so.path_tol * (1.0f - rho_est)) {
+            us = x[0]; ts = x[1]; qst = x[2];
+            if (SKIN) s64.Ts = c64.tha + (double)x[3];
+            return FAST_SOLVED;
         }
+        return FAST_POLISH;
     }
     // ---- FP64 Newton steps on x = F(x)
     float A[N][N], Ainv[N][N];
@@ -328,7 +536,7 @@ __device__ __forceinline__ bool solve_fast(const DevIface<double>& P64, const De
     for (int ii = 0; ii < N; ii++)
 #pragma unroll
         for (int jj = 0; jj < N; jj++) A[ii][jj] = (ii == jj ? 1.0f : 0.0f) - J[ii][jj];
-    if (!invert<N>(A, Ainv)) { reason = REPLAY_SINGULAR; return false; }
+    if (!invert<N>(A, Ainv)) { reason = REPLAY_SINGULAR; return FAST_REPLAY; }
     float A3i[3][3];
     if (SKIN) {
         float A3[3][3];
@@ -336,9 +544,9 @@ __device__ __forceinline__ bool solve_fast(const DevIface<double>& P64, const De
         for (int ii = 0; ii < 3; ii++)
 #pragma unroll
             for (int jj = 0; jj < 3; jj++) A3[ii][jj] = (ii == jj ? 1.0f : 0.0f) - J[ii][jj];
-        if (!invert<3>(A3, A3i)) { reason = REPLAY_SINGULAR; return false; }
+        if (!invert<3>(A3, A3i)) { reason = REPLAY_SINGULAR; return FAST_REPLAY; }
     }
-    double xd[4] = {(double)x[0], (double)x[1], (double)x[2], SKIN ? (double)x[3] : 0.0};
+    double xd[4] = {(double)x[0], (double)x[1], (double)x[2], SKIN ? c64.tha + (double)x[3] : 0.0};
     // a Newton step with an approximate J shrinks the error by about |dJ| / (1 - rho):
     // slowly contracting cells take more steps, up to polish_steps
     const int want = 1 + (rho_est > 0.5f ? 1 : 0) + (rho_est > 0.8f ? 1 : 0);
@@ -372,13 +580,8 @@ __device__ __forceinline__ bool solve_fast(const DevIface<double>& P64, const De
         if (SKIN) xd[3] = pinned ? y[3] : xd[3] + (double)dl[3];
     }
     us = xd[0]; ts = xd[1]; qst = xd[2];
-    if (SKIN) {
-        // the interface state that goes with the polished temperature
-        s64.Ts = xd[3];
-        double qs = surface_specific_humidity(P64, c64.pa, s64.Ts);
-        surface_const(P64, c64, s64.Ts, qs, s64);
-    }
-    return true;
+    if (SKIN) s64.Ts = xd[3];   // the callers read the interface temperature alone
+    return FAST_SOLVED;
 }
 
 // Warp-aggregated append of `id` to one side of a member's work list.
@@ -425,19 +628,23 @@ __device__ __forceinline__ bool stable_class(const DevIface<float>& P, float Ta,
     return dth * (1.0f + delta * qs) + delta * Tv * dq > 0.0f;
 }
 
-// Warp-aggregated append of `id` to the replay queue (lanes with want = true).
-__device__ __forceinline__ void replay_push(const ReplayQueue& q, bool want, uint32_t id) {
+// Warp-aggregated append of `id` to one part of the deferred-cell queue (lanes
+// with want = true): part 0 the FP64 replays, part 1 the FP64 polishes.
+__device__ __forceinline__ void queue_push(const ReplayQueue& q, int part, bool want, uint32_t id) {
     unsigned mask = __activemask();
     unsigned ballot = __ballot_sync(mask, want);
     if (!want) return;
     int lane = threadIdx.x & 31;
     int leader = __ffs(ballot) - 1;
     unsigned base = 0;
-    if (lane == leader) base = atomicAdd(q.count, (unsigned)__popc(ballot));
+    if (lane == leader) base = atomicAdd(&q.count[part], (unsigned)__popc(ballot));
     base = __shfl_sync(ballot, base, leader);
     unsigned pos = base + __popc(ballot & ((1u << lane) - 1u));
-    if ((int64_t)pos < q.capacity) q.idx[pos] = id;
+    if ((int64_t)pos < q.capacity) q.idx[(int64_t)part * q.capacity + pos] = id;
 }
+
+__device__ __forceinline__ void replay_push(const ReplayQueue& q, bool want, uint32_t id) { queue_push(q, 0, want, id); }
+__device__ __forceinline__ void polish_push(const ReplayQueue& q, bool want, uint32_t id) { queue_push(q, 1, want, id); }
 
 cudaError_t launch_ao(const AOArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,

@@ -23,6 +23,7 @@ const NESF_F64 = Int32(0)
 const NESF_F32 = Int32(1)
 const NESF_PLAIN_F64 = Int32(0)
 const NESF_F32_POLISH = Int32(1)
+const NESF_F32_ADAPTIVE = Int32(2)
 
 struct Grid
     nx::Int32; ny::Int32; hx::Int32; hy::Int32; stride_j::Int64
@@ -47,11 +48,13 @@ end
 struct SolverOptions
     precision::Int32; polish_maxiter::Int32; block_size::Int32; schedule::Int32
     ctas_per_sm::Int32; warm_start::Int32; mlp::Ptr{Cvoid}; fallback_ratio::Float64; path_tolerance::Float64
+    fp32_rho::Float64
 end
 
 struct GB300SimilarityTheoryFluxes{F}
     inner :: F                  # the reference formulation (defaults, solver settings)
-    precision :: Symbol         # :f64 (drop-in) or :f32 (FP32 sweep + FP64 Newton polish)
+    precision :: Symbol         # :f64 (drop-in), :f32 (FP32 sweep + FP64 Newton polish) or
+                                # :f32_adaptive (FP32 result kept where well conditioned)
 end
 GB300SimilarityTheoryFluxes(inner; precision = :f64) = GB300SimilarityTheoryFluxes(inner, precision)
 
@@ -90,7 +93,9 @@ function InterfaceComputations.compute_atmosphere_ocean_fluxes!(coupled_model, f
                       devptr(out.friction_velocity), devptr(out.temperature_scale), devptr(out.water_vapor_scale),
                       devptr(Ts), C_NULL)
     params = default_params(:ocean)
-    opts = SolverOptions(fluxes.precision === :f32 ? NESF_F32_POLISH : NESF_PLAIN_F64, 0, 128, 0, 0, 0, C_NULL, 10.0, 2e-6)
+    prec = fluxes.precision === :f32 ? NESF_F32_POLISH :
+           fluxes.precision === :f32_adaptive ? NESF_F32_ADAPTIVE : NESF_PLAIN_F64
+    opts = SolverOptions(prec, 0, 128, 0, 0, 0, C_NULL, 10.0, 2e-6, 0.8)
     stream = CUDA.stream().handle
     check(ccall((:nesf_compute_atmosphere_ocean_fluxes, libnesf), Cint,
                 (Ptr{Cvoid}, Ptr{UInt8}, Ref{AOFields}, Ref{SolverOptions}, Ptr{Cvoid}, Ptr{Cvoid}),

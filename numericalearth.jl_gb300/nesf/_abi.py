@@ -50,6 +50,7 @@ SKIN_TEMPERATURE_DIFFUSIVE = 2
 
 PLAIN_F64 = 0
 F32_POLISH = 1
+F32_ADAPTIVE = 2
 
 ITER_HIST_BINS = 128
 
@@ -108,7 +109,8 @@ class InterfaceParams(C.Structure):
 
 class SolverOptions(C.Structure):
     _fields_ = [("precision", i32), ("polish_maxiter", i32), ("block_size", i32), ("schedule", i32),
-                ("ctas_per_sm", i32), ("warm_start", i32), ("mlp", vp), ("fallback_ratio", d), ("path_tolerance", d)]
+                ("ctas_per_sm", i32), ("warm_start", i32), ("mlp", vp), ("fallback_ratio", d), ("path_tolerance", d),
+                ("fp32_rho", d)]
 
 
 class Stats(C.Structure):

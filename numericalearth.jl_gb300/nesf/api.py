@@ -16,7 +16,8 @@ from . import fields as F
 from . import params as P
 from ._lib import check, load
 
-PRECISIONS = {"f64": A.PLAIN_F64, "plain": A.PLAIN_F64, "f32": A.F32_POLISH, "f32_polish": A.F32_POLISH}
+PRECISIONS = {"f64": A.PLAIN_F64, "plain": A.PLAIN_F64, "f32": A.F32_POLISH, "f32_polish": A.F32_POLISH,
+              "f32_adaptive": A.F32_ADAPTIVE}
 
 
 def _torch():

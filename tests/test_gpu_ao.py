@@ -82,6 +82,62 @@ def test_f32_polish_within_1e5_1deg(ao1):
     assert stats["nonconverged"] == 0
 
 
+def test_f32_adaptive_within_1e5_1deg(ao1):
+    """ADAPTIVE keeps the FP32 result of most bulk-temperature cells and stays within 1e-5."""
+    st, spec, ref = ao1
+    gpu, stats = run_gpu_ao(spec, st, "f32_adaptive", stats=True)
+    for k in ALL_OUT:
+        e = rel_err(ring(st, gpu[k]), ring(st, ref[k]), floor_frac=1e-6)
+        assert e.max() <= 1e-5, (k, e.max())
+    n = (st.layout.nx + 2) * (st.layout.ny + 2)
+    assert stats["cells"] == n and stats["solved"] == n
+    kept = stats["solved"] - stats["polished"] - stats["fp64_redo"]
+    assert kept > 0.5 * n, stats          # FP32 results kept without any FP64 iteration
+    assert stats["fp64_redo"] < 0.05 * n
+    assert stats["nonconverged"] == 0
+
+
+def test_f32_adaptive_fp32_fields_with_land(oracle):
+    """FP32 storage and 30 % land through the adaptive solver and its packed polish pass."""
+    st = syn.coupled(seed=17, nx=160, ny=80, lat_s=-75, lat_n=75, land=0.3, interpolate=False)
+    spec = P.atmosphere_ocean_interface_spec()
+    ref = oracle.ao_fluxes(spec.to_c(), st.layout, widen(st.fields))
+    gpu, stats = run_gpu_ao(spec, st, "f32_adaptive", stats=True)
+    for k in ALL_OUT:
+        e = rel_err(ring(st, gpu[k]).astype(np.float64), ring(st, ref[k]), floor_frac=1e-6)
+        assert e.max() <= 1e-5, (k, e.max())
+    land = ring(st, st.fields["inactive"]) != 0
+    assert np.all(ring(st, gpu["friction_velocity"])[land] == 0)
+    assert stats["solved"] == int((~land).sum()) and stats["polished"] > 0
+
+
+@pytest.mark.parametrize("precision", ["f32", "f32_adaptive"])
+def test_fp32_solvers_with_diffusive_skin(oracle, precision):
+    """A diffusive skin temperature (T_s in the state): the FP32 sweep carries tau = T_s - theta_a,
+    so theta_a - T_s does not cancel in FP32; the polished and the kept FP32 results stay within
+    1e-5 where an FP32 T_s would be ~1e-4 off in sensible heat."""
+    st = syn.ao_1deg(seed=5, nx=64, ny=32)
+    spec = P.atmosphere_ocean_interface_spec(temperature=P.SkinTemperature(P.DiffusiveFlux(1e-2, 1.0)),
+                                             radiation=P.SurfaceRadiationProperties(0.05, 0.97))
+    ref = oracle.ao_fluxes(spec.to_c(), st.layout, st.fields)
+    gpu, stats = run_gpu_ao(spec, st, precision, stats=True)
+    n = (st.layout.nx + 2) * (st.layout.ny + 2)
+    assert stats["solved"] == n
+    kept = stats["solved"] - stats["polished"] - stats["fp64_redo"]
+    if precision == "f32":
+        assert kept == 0
+    else:
+        assert kept > 0.5 * n, stats
+    # cells where the reference stops at maxiter without converging are not compared
+    conv = ring(st, ref["iterations"]) < spec.flux_formulation.solver_stop_criteria.__dict__.get("maxiter", 10 ** 9)
+    assert conv.mean() > 0.9
+    for k in FLUXES:
+        e = rel_err(ring(st, gpu[k])[conv], ring(st, ref[k])[conv], floor_frac=1e-6)
+        assert e.max() <= 1e-5, (k, e.max())
+    T = lambda a: ring(st, a["interface_temperature"])[conv] + 273.15
+    assert rel_err(T(gpu), T(ref)).max() <= 1e-8
+
+
 def test_land_mask_and_fp32_fields(oracle):
     """30 % land, FP32 storage: land cells take the zero interface state, water cells match."""
     st = syn.coupled(seed=7, nx=96, ny=48, lat_s=-70, lat_n=70, land=0.3, interpolate=False)

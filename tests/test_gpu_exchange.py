@@ -54,11 +54,14 @@ def test_atmosphere_sea_ice_plain_matches_oracle(oracle, coupled64):
     assert np.allclose(R(gpu["interface_temperature"])[free], R(st.fields["T_oc"])[free], rtol=0, atol=1e-12)
 
 
-def test_atmosphere_sea_ice_f32_polish(oracle):
+@pytest.mark.parametrize("precision", ["f32", "f32_adaptive"])
+def test_atmosphere_sea_ice_f32_polish(oracle, precision):
+    """FP32 sweep (skin temperature in delta form) + FP64 polish, and the adaptive mode that
+    keeps the FP32 result of well-conditioned cells; both within 1e-5."""
     st = syn.coupled(seed=22, nx=120, ny=64, lat_s=-80, lat_n=80, land=0.0, interpolate=False)
     spec = P.atmosphere_sea_ice_interface_spec()
     ref = oracle.ai_fluxes(spec.to_c(), st.layout, widen(st.fields), st.fields["ice_temperature"])
-    gpu = run_ai(spec, st, "f32")
+    gpu = run_ai(spec, st, precision)
     R = st.layout.ring
     for k in F.AI_OUTPUTS:
         e = rel_err(R(gpu[k]), R(ref[k]), floor_frac=1e-6)
@@ -115,6 +118,73 @@ def test_interpolation_matches_oracle(oracle):
     for n in src:
         assert rel_err(R(to_numpy(out[n])), R(ref[n]), floor_frac=1e-6).max() <= 1e-13, n
         assert np.array_equal(to_numpy(out[n]), to_numpy(out2[n])), n
+
+
+def test_interpolation_fp32_fields(oracle):
+    """FP32 fields interpolate in FP32 arithmetic, like the reference's Float32 kernels: against
+    the FP64 oracle on the same (FP32) atmosphere, positive fields (T, p, q, radiation) are within
+    1e-6 relative and every field within 1e-6 of its largest magnitude (u and v change sign, so
+    their bilinear sums can cancel)."""
+    import torch
+    st = syn.ao_quarter_land(nx=200, ny=80, dtype=np.float32)
+    at = st.atmos
+    ag = api.atmos_grid_struct(at)
+    coords = api.exchange_coords(st.coords)
+    ref = oracle.interpolate(st.layout, coords, ag, widen(at["arrays"]), at["time_weight"])
+    src = api.to_device(at["arrays"])
+    assert src["T"].dtype == torch.float32
+    out = {n: torch.zeros(st.layout.shape, dtype=torch.float32, device="cuda") for n in src}
+    api.interpolate_atmosphere_state(st.layout, st.coords, at, src, out, at["time_weight"])
+    torch.cuda.synchronize()
+    R = st.layout.ring
+    for n in src:
+        g, r = R(to_numpy(out[n])).astype(np.float64), R(ref[n])
+        assert np.abs(g - r).max() <= 1e-6 * np.abs(r).max(), n
+        if n in ("T", "p", "q", "sw", "lw"):
+            assert rel_err(g, r, floor_frac=1e-6).max() <= 1e-6, n
+
+
+def test_assembly_fp32_fields(oracle, coupled64):
+    """FP32 fields assemble in FP32 arithmetic: within 1e-6 of each output's largest magnitude,
+    and 1e-5 relative on 99 % of the cells. The net heat flux sums terms of opposite sign
+    (emitted longwave ~400 W/m2 against absorbed longwave and the turbulent fluxes), so the
+    FP32 rounding of the terms is a larger fraction of the sum."""
+    import torch
+    st = coupled64
+    L = st.layout
+    rng = np.random.default_rng(5)
+    f32 = lambda a: np.asarray(a, dtype=np.float32)
+    names_in = ["ao_sensible", "ao_latent", "ao_water_vapor", "ao_x_momentum", "ao_y_momentum",
+                "io_interface_heat", "io_frazil_heat", "io_salt", "io_freshwater", "io_x_momentum",
+                "io_y_momentum", "ai_sensible", "ai_latent", "ai_x_momentum", "ai_y_momentum", "intercepted_snow"]
+    arrays = {n: f32(rng.normal(0, 50, L.shape)) for n in names_in}
+    arrays["ao_interface_temperature"] = f32(st.fields["T_oc"])
+    arrays["ai_interface_temperature"] = f32(st.fields["ice_temperature"])
+    arrays.update(ice_concentration=f32(st.fields["ice_concentration"]), ocean_surface_temperature=f32(st.fields["T_oc"]),
+                  rain=f32(st.fields["rain"]), snow=f32(st.fields["snow"]), sw_down=f32(st.fields["sw_down"]),
+                  lw_down=f32(st.fields["lw_down"]), inactive=st.fields["inactive"])
+    outs = ["ocean_u", "ocean_v", "ocean_T", "ocean_S", "ocean_eta", "ocean_heat_content", "ice_top_heat",
+            "ice_top_snowfall", "ice_top_u", "ice_top_v", "ice_bottom_heat", "ocean_upwelling_longwave",
+            "ocean_downwelling_longwave", "ocean_downwelling_shortwave", "ice_upwelling_longwave",
+            "ice_downwelling_longwave", "ice_downwelling_shortwave"]
+    host = widen(arrays)
+    host.update({n: np.zeros(L.shape) for n in outs})
+    spec = P.AssemblySpec()
+    pc = spec.to_c()
+    for which in ("ocean", "sea_ice", "ocean_radiation", "sea_ice_radiation"):
+        oracle.assemble(pc, L, host, which)
+    dev = api.to_device(arrays)
+    dev.update({n: torch.zeros(L.shape, dtype=torch.float32, device="cuda") for n in outs})
+    api.assemble_net_ocean_fluxes(spec, L, dev)
+    api.assemble_net_sea_ice_fluxes(spec, L, dev)
+    api.apply_air_sea_radiative_fluxes(spec, L, dev)
+    api.apply_air_sea_ice_radiative_fluxes(spec, L, dev)
+    torch.cuda.synchronize()
+    I = L.interior
+    for n in outs:
+        g, r = I(to_numpy(dev[n])).astype(np.float64), I(host[n])
+        assert np.abs(g - r).max() <= 1e-6 * np.abs(r).max(), n
+        assert np.percentile(rel_err(g, r, floor_frac=1e-6), 99) <= 1e-5, n
 
 
 def test_assembly_and_radiation_match_oracle(oracle, coupled64):

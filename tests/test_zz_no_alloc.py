@@ -41,7 +41,7 @@ def _noalloc(lib, spec, layout, dev, out, precision):
     return lib.nesf_compute_atmosphere_ocean_fluxes_noalloc(C.byref(p), C.byref(f), C.byref(o), stream)
 
 
-@pytest.mark.parametrize("precision,dtype", [("f64", np.float64), ("f32", np.float32)])
+@pytest.mark.parametrize("precision,dtype", [("f64", np.float64), ("f32", np.float32), ("f32_adaptive", np.float32)])
 def test_noalloc_matches_regular_entry_point_twice(precision, dtype):
     import torch
     lib = _lib.load()
