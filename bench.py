@@ -169,9 +169,11 @@ def phase_times(model, precision, reps=3):
 
 
 def time_steps(model, precision, steps, warmup, world):
+    """Device time per coupling step, replaying the step captured as a CUDA graph."""
     import torch
+    model.capture(precision)
     for _ in range(warmup):
-        model.update_state(precision)
+        model.graph_step()
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -181,7 +183,7 @@ def time_steps(model, precision, steps, warmup, world):
     launches = 0
     e0.record(s)
     for _ in range(steps):
-        launches += model.update_state(precision)
+        launches += model.graph_step()
     e1.record(s)
     torch.cuda.synchronize()
     if world > 1:
@@ -223,8 +225,9 @@ def error_stats(model, precision):
 
 def e2e_step_time(model, precision, steps, warmup):
     """Same step through the public API with host buffers: pinned H2D of the step's inputs
-    (ocean and sea-ice surface state + the two atmosphere snapshots), the step, and a D2H
-    read of the net boundary fluxes, all inside the timed region."""
+    (ocean and sea-ice surface state + the two atmosphere snapshots) into the model's
+    fields, the captured step (nesf_graph_launch), and a D2H read of the net boundary
+    fluxes, all inside the timed region."""
     import torch
     from nesf.coupled import ICE_NET, OCEAN_NET, STEP_INPUTS
     names = [k for k in STEP_INPUTS if k in model.x]
@@ -236,12 +239,14 @@ def e2e_step_time(model, precision, steps, warmup):
     d2h = sum(t.numel() * t.element_size() for t in host_out.values())
     s = torch.cuda.current_stream()
 
+    model.capture(precision)
+
     def one():
         for k, t in host_in.items():
             model.x[k].copy_(t, non_blocking=True)
         for k, t in atm_in.items():
             model.atmos_src[k].copy_(t, non_blocking=True)
-        model.update_state(precision)
+        model.graph_step()
         for k, t in host_out.items():
             t.copy_(model.net[k], non_blocking=True)
 
@@ -365,7 +370,9 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": {"f32": "f32+f64polish", "f32_adaptive": "f32 (f64 polish where ill-conditioned)"}.get(prec, "f64"), "data": "synthetic",
             "config": {"workload": WORKLOAD, "cells_ao": n_ao, "cells_ai": n_ai, "fields": "fp32",
-                       "warm_start": False, "schedule": "one thread per cell, per-phase kernels",
+                       "warm_start": False,
+                       "schedule": "one thread per cell, compacted work lists, packed polish/replay passes; "
+                                   "the step replayed as one CUDA graph",
                        "l2": "working set > L2 (no flush needed)", "parallelism": f"replicas x{world}"},
             "gpu_launches": launches,
             "clocks": clk,

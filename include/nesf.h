@@ -460,6 +460,52 @@ int nesf_apply_air_sea_radiative_fluxes(const nesf_assembly_params* params, cons
 int nesf_apply_air_sea_ice_radiative_fluxes(const nesf_assembly_params* params, const nesf_assembly_fields* fields,
                                             void* stream);
 
+/* ------------------------------------------------------- the coupling step
+ * The interface-flux part of update_state!(::EarthSystemModel)
+ * (EarthSystemModels/time_step_earth_system_model.jl:38-83) in one call, in the
+ * reference's order: interpolate_state! (when `interp` is given),
+ * compute_atmosphere_ocean_fluxes!, compute_atmosphere_sea_ice_fluxes! and
+ * compute_sea_ice_ocean_fluxes! (when their parameters are given),
+ * update_net_fluxes! for the ocean and the sea ice (when `assembly_params` is
+ * given; the sea-ice half only with sea ice), then the radiative add-ons (when
+ * `radiation` is 1). The pointers of one phase's fields must agree with the
+ * arrays the next phase reads (a model's fields); nothing is checked across
+ * phases. No statistics. */
+typedef struct {
+    const nesf_interface_params* ao_params;         /* required                          */
+    const nesf_ao_fields* ao;                       /* required                          */
+    const nesf_interface_params* ai_params;         /* NULL: no sea ice                  */
+    const nesf_ai_fields* ai;
+    const nesf_io_params* io_params;                /* NULL: no sea-ice-ocean fluxes     */
+    const nesf_io_fields* io;
+    const nesf_interp_fields* interp;               /* NULL: exchange-grid state given   */
+    const nesf_assembly_params* assembly_params;    /* NULL: no net-flux assembly        */
+    const nesf_assembly_fields* assembly;
+    int32_t radiation;                              /* 1: radiative add-ons after assembly */
+    int32_t pad_;
+} nesf_coupling_step_args;
+
+int nesf_coupling_step(nesf_context* ctx, const nesf_coupling_step_args* args, const nesf_solver_options* opts,
+                       void* stream);
+
+/* A CUDA graph of one coupling step, captured once and replayed each step: the
+ * launch sequence (16 kernels and 4 counter resets for a coupled step) becomes one
+ * graph launch. Everything the step reads is baked in at capture -- the field
+ * pointers, parameters and options -- so the caller keeps its buffers between
+ * launches (a model's fields are fixed; new atmosphere snapshots are copied into
+ * the captured snapshot arrays). The interpolation's time weight changes every
+ * step and is set with nesf_graph_set_time_weight. The graph uses the context's
+ * scratch: do not run other solves on the same context concurrently with it.
+ * Capture sizes the scratch first (it may synchronise the device then); launches
+ * never allocate or synchronise. */
+typedef struct nesf_graph nesf_graph;
+
+int nesf_graph_capture(nesf_context* ctx, const nesf_coupling_step_args* args, const nesf_solver_options* opts,
+                       nesf_graph** out);
+int nesf_graph_set_time_weight(nesf_graph* graph, double time_weight);
+int nesf_graph_launch(nesf_graph* graph, void* stream);
+int nesf_graph_destroy(nesf_graph* graph);
+
 #ifdef __cplusplus
 }
 #endif

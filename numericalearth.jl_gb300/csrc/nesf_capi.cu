@@ -78,7 +78,8 @@ int32_t nesf_struct_sizes(int64_t* sizes, int32_t n) {
         (int64_t)sizeof(nesf_solver_options), (int64_t)sizeof(nesf_stats), (int64_t)sizeof(nesf_ao_fields),
         (int64_t)sizeof(nesf_ai_fields), (int64_t)sizeof(nesf_io_params), (int64_t)sizeof(nesf_io_fields),
         (int64_t)sizeof(nesf_atmos_grid), (int64_t)sizeof(nesf_exchange_coords), (int64_t)sizeof(nesf_interp_fields),
-        (int64_t)sizeof(nesf_assembly_params), (int64_t)sizeof(nesf_assembly_fields)};
+        (int64_t)sizeof(nesf_assembly_params), (int64_t)sizeof(nesf_assembly_fields),
+        (int64_t)sizeof(nesf_coupling_step_args)};
     int32_t m = (int32_t)(sizeof s / sizeof s[0]);
     for (int32_t k = 0; k < n && k < m; k++) sizes[k] = s[k];
     return m;
@@ -852,5 +853,158 @@ extern "C" int nesf_compute_atmosphere_ocean_fluxes_noalloc(const nesf_interface
                         : launch_ao(ao_args<float>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl,
                                     rq, nullptr, s);
     if (e != cudaSuccess) return cuda_fail(e, who);
+    return NESF_OK;
+}
+
+// ------------------------------------------------------------ coupling step
+// Scratch for the solves of a step, sized before any capture (growing it
+// synchronises the device, which a stream capture forbids).
+static int coupling_scratch(nesf_context* ctx, const nesf_coupling_step_args* a) {
+    int64_t cells = (int64_t)(a->ao->grid.nx + 2) * (a->ao->grid.ny + 2);
+    if (a->ai_params && a->ai) {
+        int64_t c2 = (int64_t)(a->ai->grid.nx + 2) * (a->ai->grid.ny + 2);
+        cells = c2 > cells ? c2 : cells;
+    }
+    std::lock_guard<std::mutex> lk(ctx->lock);
+    DeviceGuard g(ctx->device);
+    ReplayQueue rq;
+    WorkList wl;
+    int r = replay_queue(ctx, cells, &rq);
+    if (r == NESF_OK) r = work_list(ctx, cells, 1, &wl);
+    return r;
+}
+
+extern "C" int nesf_coupling_step(nesf_context* ctx, const nesf_coupling_step_args* a,
+                                  const nesf_solver_options* opts, void* stream) {
+    const char* who = "nesf_coupling_step";
+    if (!a || !a->ao_params || !a->ao) return fail(NESF_ERR_ARG, "%s: the atmosphere-ocean interface is required", who);
+    if (a->radiation && !a->assembly_params) return fail(NESF_ERR_ARG, "%s: radiation needs the assembly", who);
+    if (a->assembly_params && !a->assembly) return fail(NESF_ERR_ARG, "%s: assembly parameters without fields", who);
+    if ((a->ai_params == nullptr) != (a->ai == nullptr) || (a->io_params == nullptr) != (a->io == nullptr))
+        return fail(NESF_ERR_ARG, "%s: give the parameters and the fields of an interface together", who);
+    int r = context_or_default(&ctx);
+    if (r) return r;
+    const bool ice = a->ai_params != nullptr;
+    // update_state! order (time_step_earth_system_model.jl:50-80)
+    if (a->interp && (r = nesf_interpolate_atmosphere_state(a->interp, stream))) return r;
+    if ((r = nesf_compute_atmosphere_ocean_fluxes(ctx, a->ao_params, a->ao, opts, nullptr, stream))) return r;
+    if (ice && (r = nesf_compute_atmosphere_sea_ice_fluxes(ctx, a->ai_params, a->ai, opts, nullptr, stream))) return r;
+    if (a->io_params && (r = nesf_compute_sea_ice_ocean_fluxes(ctx, a->io_params, a->io, stream))) return r;
+    if (a->assembly_params) {
+        if ((r = nesf_assemble_net_ocean_fluxes(a->assembly_params, a->assembly, stream))) return r;
+        if (ice && (r = nesf_assemble_net_sea_ice_fluxes(a->assembly_params, a->assembly, stream))) return r;
+        if (a->radiation) {
+            if ((r = nesf_apply_air_sea_radiative_fluxes(a->assembly_params, a->assembly, stream))) return r;
+            if (ice && (r = nesf_apply_air_sea_ice_radiative_fluxes(a->assembly_params, a->assembly, stream)))
+                return r;
+        }
+    }
+    return NESF_OK;
+}
+
+struct nesf_graph {
+    int device;
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+    cudaGraphNode_t interp_node;           // null when the step has no interpolation
+    cudaKernelNodeParams interp_params;    // its launch configuration
+    alignas(16) unsigned char interp_args[sizeof(InterpArgs<double>)];   // its argument, time weight updated
+    bool interp_fp64;
+};
+
+extern "C" int nesf_graph_capture(nesf_context* ctx, const nesf_coupling_step_args* a,
+                                  const nesf_solver_options* opts, nesf_graph** out) {
+    const char* who = "nesf_graph_capture";
+    if (!out) return fail(NESF_ERR_ARG, "%s: null output pointer", who);
+    *out = nullptr;
+    if (!a || !a->ao_params || !a->ao) return fail(NESF_ERR_ARG, "%s: the atmosphere-ocean interface is required", who);
+    int r = context_or_default(&ctx);
+    if (r) return r;
+    if ((r = coupling_scratch(ctx, a))) return r;
+    DeviceGuard g(ctx->device);
+    nesf_graph* G = new (std::nothrow) nesf_graph();
+    if (!G) return fail(NESF_ERR_ARG, "%s: out of host memory", who);
+    G->device = ctx->device;
+    cudaStream_t cs = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        if (cs) cudaStreamDestroy(cs);
+        delete G;
+        return cuda_fail(e, "nesf_graph_capture: begin");
+    }
+    r = nesf_coupling_step(ctx, a, opts, cs);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(cs, &graph);
+    cudaStreamDestroy(cs);
+    if (r != NESF_OK || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        delete G;
+        return r != NESF_OK ? r : cuda_fail(e, "nesf_graph_capture: end");
+    }
+    G->graph = graph;
+    // the interpolation node, whose time weight changes every step
+    if (a->interp) {
+        G->interp_fp64 = a->interp->dtype == NESF_F64;
+        const void* fn = interp_kernel_address(G->interp_fp64);
+        size_t n = 0;
+        e = cudaGraphGetNodes(graph, nullptr, &n);
+        cudaGraphNode_t nodes[256];
+        if (e == cudaSuccess && n <= 256) e = cudaGraphGetNodes(graph, nodes, &n);
+        for (size_t k = 0; e == cudaSuccess && k < n && k < 256; k++) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(nodes[k], &t) != cudaSuccess || t != cudaGraphNodeTypeKernel) continue;
+            cudaKernelNodeParams kp;
+            if (cudaGraphKernelNodeGetParams(nodes[k], &kp) != cudaSuccess || kp.func != fn) continue;
+            G->interp_node = nodes[k];
+            G->interp_params = kp;
+            memcpy(G->interp_args, kp.kernelParams[0],
+                   G->interp_fp64 ? sizeof(InterpArgs<double>) : sizeof(InterpArgs<float>));
+        }
+        if (e == cudaSuccess && !G->interp_node) e = cudaErrorInvalidValue;
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            delete G;
+            return cuda_fail(e, "nesf_graph_capture: interpolation node");
+        }
+    }
+    e = cudaGraphInstantiate(&G->exec, graph, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        delete G;
+        return cuda_fail(e, "nesf_graph_capture: instantiate");
+    }
+    *out = G;
+    return NESF_OK;
+}
+
+extern "C" int nesf_graph_set_time_weight(nesf_graph* G, double tn) {
+    if (!G) return fail(NESF_ERR_ARG, "nesf_graph_set_time_weight: null graph");
+    if (!G->interp_node) return fail(NESF_ERR_ARG, "nesf_graph_set_time_weight: the graph has no interpolation");
+    if (!(tn >= 0.0 && tn <= 1.0)) return fail(NESF_ERR_ARG, "nesf_graph_set_time_weight: weight %g", tn);
+    DeviceGuard g(G->device);
+    if (G->interp_fp64) ((InterpArgs<double>*)G->interp_args)->tn = tn;
+    else ((InterpArgs<float>*)G->interp_args)->tn = tn;
+    void* args[1] = {G->interp_args};
+    cudaKernelNodeParams kp = G->interp_params;
+    kp.kernelParams = args;
+    kp.extra = nullptr;
+    NESF_CUDA(cudaGraphExecKernelNodeSetParams(G->exec, G->interp_node, &kp));
+    return NESF_OK;
+}
+
+extern "C" int nesf_graph_launch(nesf_graph* G, void* stream) {
+    if (!G) return fail(NESF_ERR_ARG, "nesf_graph_launch: null graph");
+    DeviceGuard g(G->device);
+    NESF_CUDA(cudaGraphLaunch(G->exec, (cudaStream_t)stream));
+    return NESF_OK;
+}
+
+extern "C" int nesf_graph_destroy(nesf_graph* G) {
+    if (!G) return NESF_OK;
+    DeviceGuard g(G->device);
+    if (G->exec) cudaGraphExecDestroy(G->exec);
+    if (G->graph) cudaGraphDestroy(G->graph);
+    delete G;
     return NESF_OK;
 }

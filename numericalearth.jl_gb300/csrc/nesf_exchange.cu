@@ -309,6 +309,10 @@ cudaError_t launch_interp(const InterpArgs<S>& a, cudaStream_t s) {
 template cudaError_t launch_interp<double>(const InterpArgs<double>&, cudaStream_t);
 template cudaError_t launch_interp<float>(const InterpArgs<float>&, cudaStream_t);
 
+const void* interp_kernel_address(bool fp64) {
+    return fp64 ? (const void*)interp_kernel<double> : (const void*)interp_kernel<float>;
+}
+
 template <class S>
 cudaError_t launch_assemble(const AsmArgs<S>& a, const nesf_assembly_params& p, int which, cudaStream_t s) {
     int64_t n = (int64_t)a.L.nx * a.L.ny;

@@ -47,6 +47,8 @@ template <class S> cudaError_t launch_io(const IOArgs<S>& a, const nesf_io_param
 cudaError_t launch_frac(const Layout2& L, const nesf_exchange_coords& c, const nesf_atmos_grid& ag, double* fi,
                         double* fj, cudaStream_t s);
 template <class S> cudaError_t launch_interp(const InterpArgs<S>& a, cudaStream_t s);
+// The interpolation kernel's address, to find its node in a captured graph.
+const void* interp_kernel_address(bool fp64);
 // which: 0 net ocean, 1 net sea ice, 2 ocean radiation, 3 sea-ice radiation
 template <class S>
 cudaError_t launch_assemble(const AsmArgs<S>& a, const nesf_assembly_params& p, int which, cudaStream_t s);

@@ -191,8 +191,17 @@ class AssemblyFields(C.Structure):
     _fields_ = [("grid", Grid), ("dtype", i32), ("pad_", i32)] + [(n, vp) for n in ASSEMBLY_FIELD_NAMES]
 
 
+class CouplingStepArgs(C.Structure):
+    _fields_ = [("ao_params", C.POINTER(InterfaceParams)), ("ao", C.POINTER(AOFields)),
+                ("ai_params", C.POINTER(InterfaceParams)), ("ai", C.POINTER(AIFields)),
+                ("io_params", C.POINTER(IOParams)), ("io", C.POINTER(IOFields)),
+                ("interp", C.POINTER(InterpFields)),
+                ("assembly_params", C.POINTER(AssemblyParams)), ("assembly", C.POINTER(AssemblyFields)),
+                ("radiation", i32), ("pad_", i32)]
+
+
 # Order of nesf_struct_sizes(): must match the library.
 STRUCTS_IN_SIZE_ORDER = (Grid, ThermodynamicsParameters, StabilityFunction, RoughnessLength,
                          SimilarityTheoryFluxesC, InterfaceParams, SolverOptions, Stats, AOFields,
                          AIFields, IOParams, IOFields, AtmosGrid, ExchangeCoords, InterpFields,
-                         AssemblyParams, AssemblyFields)
+                         AssemblyParams, AssemblyFields, CouplingStepArgs)

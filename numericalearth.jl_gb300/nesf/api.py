@@ -228,6 +228,90 @@ def apply_air_sea_ice_radiative_fluxes(spec, layout, arrays, stream=None):
     _assembly("nesf_apply_air_sea_ice_radiative_fluxes", spec, layout, arrays, stream)
 
 
+# ------------------------------------------------------------- coupling step
+class CouplingStep:
+    """The packed arguments of nesf_coupling_step for one model's fields: the ctypes
+    structs are built once and kept alive here, so the device pointers they hold
+    stay those of the model's tensors (which must not be reallocated)."""
+
+    def __init__(self, ao_spec, layout, ao_arrays, ai_spec=None, ai_arrays=None, io_spec=None, io_arrays=None,
+                 io_levels=(1, 0), interp=None, assembly_spec=None, assembly_arrays=None, radiation=True):
+        g = _grid_of(layout)
+        self.ao_p = ao_spec.to_c() if hasattr(ao_spec, "to_c") else ao_spec
+        self.ao_f = F.pack(A.AOFields, g, ao_arrays)
+        self.args = A.CouplingStepArgs()
+        self.args.ao_params = C.pointer(self.ao_p)
+        self.args.ao = C.pointer(self.ao_f)
+        if ai_spec is not None:
+            self.ai_p = ai_spec.to_c() if hasattr(ai_spec, "to_c") else ai_spec
+            self.ai_f = F.pack(A.AIFields, g, ai_arrays)
+            self.args.ai_params = C.pointer(self.ai_p)
+            self.args.ai = C.pointer(self.ai_f)
+        if io_spec is not None:
+            nz, stride_k = io_levels
+            self.io_p = io_spec.to_c(nz=nz, stride_k=stride_k) if hasattr(io_spec, "to_c") else io_spec
+            self.io_f = F.pack(A.IOFields, g, io_arrays)
+            self.args.io_params = C.pointer(self.io_p)
+            self.args.io = C.pointer(self.io_f)
+        if interp is not None:
+            coords, atmos, atmos_arrays, out, frac, tn = interp
+            arrays = {INTERP_SRC[n]: t for n, t in atmos_arrays.items()}
+            arrays.update({INTERP_DST[n]: t for n, t in out.items()})
+            if frac is not None:
+                arrays["frac_i"], arrays["frac_j"] = frac
+            self.interp_f = F.pack(A.InterpFields, g, arrays, coords=exchange_coords(coords),
+                                   atmos=atmos_grid_struct(atmos), time_weight=float(tn))
+            self.args.interp = C.pointer(self.interp_f)
+        if assembly_spec is not None:
+            self.asm_p = assembly_spec.to_c() if hasattr(assembly_spec, "to_c") else assembly_spec
+            self.asm_f = F.pack(A.AssemblyFields, g, assembly_arrays)
+            self.args.assembly_params = C.pointer(self.asm_p)
+            self.args.assembly = C.pointer(self.asm_f)
+            self.args.radiation = 1 if radiation else 0
+
+    def set_time_weight(self, tn):
+        """Time weight of the interpolation for direct (non-graph) steps."""
+        self.interp_f.time_weight = float(tn)
+
+
+def coupling_step(step, precision="f32_adaptive", ctx=None, stream=None):
+    """update_state!'s interface-flux phases in one native call (nesf_coupling_step)."""
+    lib = load()
+    o = solver_options(precision)
+    ctx = ctx or default_context()
+    check(lib.nesf_coupling_step(ctx.handle, C.byref(step.args), C.byref(o), _stream_handle(stream)))
+
+
+class Graph:
+    """A captured CUDA graph of one coupling step (nesf_graph_capture)."""
+
+    def __init__(self, step, precision="f32_adaptive", ctx=None):
+        self.lib = load()
+        self.step = step                     # keeps the captured pointers' owners alive
+        self.ctx = ctx or default_context()
+        o = solver_options(precision)
+        h = C.c_void_p()
+        check(self.lib.nesf_graph_capture(self.ctx.handle, C.byref(step.args), C.byref(o), C.byref(h)))
+        self.handle = h
+
+    def set_time_weight(self, tn):
+        check(self.lib.nesf_graph_set_time_weight(self.handle, float(tn)))
+
+    def launch(self, stream=None):
+        check(self.lib.nesf_graph_launch(self.handle, _stream_handle(stream)))
+
+    def close(self):
+        if self.handle:
+            self.lib.nesf_graph_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def to_device(arrays, device="cuda", dtype=None):
     """numpy dict -> torch tensors on the device (uint8/int arrays keep their dtype)."""
     torch = _torch()

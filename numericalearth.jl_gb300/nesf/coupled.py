@@ -118,11 +118,64 @@ class CoupledModel:
         return 4
 
     def update_state(self, precision="f64", polish_maxiter=0, stream=None):
-        """One coupling step; returns the number of kernel launches."""
-        n = self.interpolate_state(stream)
-        n += self.compute_fluxes(precision, polish_maxiter, stream=stream)
-        n += self.update_net_fluxes(stream)
-        return n
+        """One coupling step through the per-phase entry points; returns the number of
+        kernels it launches."""
+        self.interpolate_state(stream)
+        self.compute_fluxes(precision, polish_maxiter, stream=stream)
+        self.update_net_fluxes(stream)
+        return self.kernels_per_step(precision)
+
+    def kernels_per_step(self, precision):
+        """Kernels one step launches: interpolation; per solve classify + solve (+ the packed
+        polish pass of the adaptive mode, + the replay pass of the FP32 modes); sea-ice-ocean;
+        ocean and sea-ice assembly and their radiative add-ons."""
+        per_solve = 2 + (precision == "f32_adaptive") + (precision != "f64" and precision != "plain")
+        return (1 if self.atmos is not None else 0) + 2 * per_solve + 1 + 4
+
+    # ------------------------------------------------- native step and graph
+    def step_args(self):
+        """nesf_coupling_step arguments over this model's tensors (built once)."""
+        if getattr(self, "_step", None) is None:
+            x = self.x
+            ao_arrays = {k: x.get(k) for k in F.AO_INPUTS}
+            ao_arrays.update({k: self.ao.get(k) for k in F.AO_OUTPUTS})
+            ai_arrays = {k: x.get(k) for k in F.AI_INPUTS}
+            ai_arrays.update({k: self.ai.get(k) for k in F.AI_OUTPUTS})
+            ai_arrays["interface_temperature"] = self.ai["interface_temperature"]
+            io_arrays = {"ice_salinity": x["ice_salinity"], "ice_thickness": x["ice_thickness"],
+                         "consolidation_thickness": x["consolidation_thickness"],
+                         "ice_concentration": x["ice_concentration"], "internal_temperature": x["ice_temperature"],
+                         "ice_mass_flux": x["ice_mass_flux"], "snow_mass_flux": x["snow_mass_flux"]}
+            io_arrays.update({k: self.io.get(k) for k in F.IO_OUTPUTS})
+            io_arrays.update(T_oc=self.T3, S_oc=self.S3, dz=self.dz)
+            interp = None
+            if self.atmos is not None:
+                out = {n: self.x[EXCHANGE_ATMOS[n]] for n in ATMOS_NAMES}
+                interp = (self.coords, self.atmos, self.atmos_src, out, (self.fi, self.fj),
+                          self.atmos["time_weight"])
+            L = self.layout
+            self._step = api.CouplingStep(self.ao_spec, L, ao_arrays, self.ai_spec, ai_arrays, self.io_spec,
+                                          io_arrays, (self.T3.shape[0], L.shape[0] * L.shape[1]), interp,
+                                          self.asm_spec, self.assembly_arrays(), radiation=True)
+        return self._step
+
+    def native_step(self, precision="f32_adaptive", stream=None):
+        """One coupling step through nesf_coupling_step; returns the kernels launched."""
+        api.coupling_step(self.step_args(), precision, stream=stream)
+        return self.kernels_per_step(precision)
+
+    def capture(self, precision="f32_adaptive"):
+        """Capture one coupling step as a CUDA graph (nesf_graph_capture)."""
+        self.graph = api.Graph(self.step_args(), precision)
+        self.graph_precision = precision
+        return self.graph
+
+    def graph_step(self, stream=None, time_weight=None):
+        """Replay the captured step; returns the kernels it runs."""
+        if time_weight is not None:
+            self.graph.set_time_weight(time_weight)
+        self.graph.launch(stream)
+        return self.kernels_per_step(self.graph_precision)
 
     # ---------------------------------------------------------- bookkeeping
     def active_cells(self):
