@@ -382,6 +382,30 @@ typedef struct {
     void* ice_upwelling_longwave; void* ice_downwelling_longwave; void* ice_downwelling_shortwave;
 } nesf_assembly_fields;
 
+/* ------------------------------------------------ area integrals (FP64)
+ * The global flux integrals behind the reference's conservation checks,
+ * int dA(a) = sum(a) * A_z and int dA(a, b) = sum(a .* b) * A_z
+ * (test/test_conservation.jl:100-101), over the interior cells, as compensated
+ * FP64 sums: each integral is returned as a pair (sum, residual) whose sum is the
+ * exact sum of the cell terms to ~1e-30 relative. Cell term: a (times b when
+ * `factor` is given) times the cell area (`area`, 2-D FP64 in the parent layout, or
+ * `row_area`, ny FP64 entries for j = 1..ny), products rounded in FP64; with
+ * neither, the sum is multiplied by `uniform_area` at the end, as the reference
+ * does. Cells with inactive != 0 are skipped when `inactive` is given. The
+ * reduction order is fixed: the result is the same on every run. */
+#define NESF_MAX_INTEGRALS 16
+typedef struct {
+    nesf_grid grid;
+    int32_t dtype;                                /* nesf_dtype of field[] and factor[] */
+    int32_t n;                                    /* integrals, 1..NESF_MAX_INTEGRALS  */
+    const void* field[NESF_MAX_INTEGRALS];
+    const void* factor[NESF_MAX_INTEGRALS];       /* NULL: no second factor            */
+    const uint8_t* inactive;
+    const double* area;
+    const double* row_area;
+    double uniform_area;
+} nesf_integral_fields;
+
 /* ------------------------------------------------------------------ API */
 typedef struct nesf_context nesf_context;   /* library-owned scratch per device */
 
@@ -459,6 +483,10 @@ int nesf_apply_air_sea_radiative_fluxes(const nesf_assembly_params* params, cons
 /* apply_air_sea_ice_radiative_fluxes! (apply_air_sea_ice_radiative_fluxes.jl:15-90) */
 int nesf_apply_air_sea_ice_radiative_fluxes(const nesf_assembly_params* params, const nesf_assembly_fields* fields,
                                             void* stream);
+
+/* int dA of up to 16 fields; result: device memory, 2 n doubles (sum, residual) per
+ * integral, written on `stream`. */
+int nesf_area_integrals(nesf_context* ctx, const nesf_integral_fields* fields, double* result, void* stream);
 
 /* ------------------------------------------------------- the coupling step
  * The interface-flux part of update_state!(::EarthSystemModel)

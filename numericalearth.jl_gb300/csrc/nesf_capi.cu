@@ -27,8 +27,16 @@ struct nesf_context {
     unsigned int* d_work_count; // two counters per ensemble member
     int64_t work_capacity;
     int32_t work_members;
+    void* d_partials;           // per-block partial sums of the area integrals
     std::mutex lock;            // serialises use of the scratch above
 };
+
+namespace nesf {
+cudaError_t launch_integrals(const nesf_integral_fields& f, void* partials, int max_blocks, double* result,
+                             cudaStream_t s);
+}
+// blocks of the area-integral pass (x 16 integrals x 16 B of partial sums: 256 KiB)
+static const int kIntegralBlocks = 1024;
 
 static thread_local char g_err[512] = "";
 
@@ -79,7 +87,7 @@ int32_t nesf_struct_sizes(int64_t* sizes, int32_t n) {
         (int64_t)sizeof(nesf_ai_fields), (int64_t)sizeof(nesf_io_params), (int64_t)sizeof(nesf_io_fields),
         (int64_t)sizeof(nesf_atmos_grid), (int64_t)sizeof(nesf_exchange_coords), (int64_t)sizeof(nesf_interp_fields),
         (int64_t)sizeof(nesf_assembly_params), (int64_t)sizeof(nesf_assembly_fields),
-        (int64_t)sizeof(nesf_coupling_step_args)};
+        (int64_t)sizeof(nesf_coupling_step_args), (int64_t)sizeof(nesf_integral_fields)};
     int32_t m = (int32_t)(sizeof s / sizeof s[0]);
     for (int32_t k = 0; k < n && k < m; k++) sizes[k] = s[k];
     return m;
@@ -256,11 +264,15 @@ int nesf_context_create(int32_t device, nesf_context** out) {
     c->d_work_count = nullptr;
     c->work_capacity = 0;
     c->work_members = 0;
+    c->d_partials = nullptr;
     cudaError_t e = cudaMalloc(&c->d_stats, sizeof(DevStats));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_partials, (size_t)kIntegralBlocks * NESF_MAX_INTEGRALS * 16);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_replay_count, 2 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_stats, sizeof(DevStats));
     if (e != cudaSuccess) {
         cudaFree(c->d_stats);
+        cudaFree(c->d_partials);
+        cudaFree(c->d_replay_count);
         delete c;
         return cuda_fail(e, "nesf_context_create");
     }
@@ -280,6 +292,7 @@ int nesf_context_destroy(nesf_context* c) {
         cudaFree(c->d_replay_count);
         cudaFree(c->d_work);
         cudaFree(c->d_work_count);
+        cudaFree(c->d_partials);
     }
     delete c;
     return NESF_OK;
@@ -852,6 +865,25 @@ extern "C" int nesf_compute_atmosphere_ocean_fluxes_noalloc(const nesf_interface
                                     rq, nullptr, s)
                         : launch_ao(ao_args<float>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl,
                                     rq, nullptr, s);
+    if (e != cudaSuccess) return cuda_fail(e, who);
+    return NESF_OK;
+}
+
+// ------------------------------------------------------------ area integrals
+extern "C" int nesf_area_integrals(nesf_context* ctx, const nesf_integral_fields* f, double* result, void* stream) {
+    const char* who = "nesf_area_integrals";
+    if (!f || !result) return fail(NESF_ERR_ARG, "%s: null argument", who);
+    int r = check_grid(f->grid, 0, who);
+    if (r) return r;
+    if (f->dtype != NESF_F64 && f->dtype != NESF_F32) return fail(NESF_ERR_ARG, "%s: dtype %d", who, f->dtype);
+    if (f->n < 1 || f->n > NESF_MAX_INTEGRALS) return fail(NESF_ERR_ARG, "%s: n = %d", who, f->n);
+    for (int k = 0; k < f->n; k++)
+        if (!f->field[k]) return fail(NESF_ERR_ARG, "%s: field %d is NULL", who, k);
+    if (f->area && f->row_area) return fail(NESF_ERR_ARG, "%s: give area or row_area, not both", who);
+    if ((r = context_or_default(&ctx))) return r;
+    std::lock_guard<std::mutex> lk(ctx->lock);
+    DeviceGuard g(ctx->device);
+    cudaError_t e = launch_integrals(*f, ctx->d_partials, kIntegralBlocks, result, (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(e, who);
     return NESF_OK;
 }

@@ -200,8 +200,17 @@ class CouplingStepArgs(C.Structure):
                 ("radiation", i32), ("pad_", i32)]
 
 
+MAX_INTEGRALS = 16
+
+
+class IntegralFields(C.Structure):
+    _fields_ = [("grid", Grid), ("dtype", i32), ("n", i32), ("field", vp * MAX_INTEGRALS),
+                ("factor", vp * MAX_INTEGRALS), ("inactive", vp), ("area", vp), ("row_area", vp),
+                ("uniform_area", d)]
+
+
 # Order of nesf_struct_sizes(): must match the library.
 STRUCTS_IN_SIZE_ORDER = (Grid, ThermodynamicsParameters, StabilityFunction, RoughnessLength,
                          SimilarityTheoryFluxesC, InterfaceParams, SolverOptions, Stats, AOFields,
                          AIFields, IOParams, IOFields, AtmosGrid, ExchangeCoords, InterpFields,
-                         AssemblyParams, AssemblyFields, CouplingStepArgs)
+                         AssemblyParams, AssemblyFields, CouplingStepArgs, IntegralFields)

@@ -48,6 +48,7 @@ SIGNATURES = {
     "nesf_assemble_net_sea_ice_fluxes": (C.c_int, [P(A.AssemblyParams), P(A.AssemblyFields), vp]),
     "nesf_apply_air_sea_radiative_fluxes": (C.c_int, [P(A.AssemblyParams), P(A.AssemblyFields), vp]),
     "nesf_apply_air_sea_ice_radiative_fluxes": (C.c_int, [P(A.AssemblyParams), P(A.AssemblyFields), vp]),
+    "nesf_area_integrals": (C.c_int, [vp, P(A.IntegralFields), vp, vp]),
     "nesf_coupling_step": (C.c_int, [vp, P(A.CouplingStepArgs), P(A.SolverOptions), vp]),
     "nesf_graph_capture": (C.c_int, [vp, P(A.CouplingStepArgs), P(A.SolverOptions), P(vp)]),
     "nesf_graph_set_time_weight": (C.c_int, [vp, C.c_double]),

@@ -228,6 +228,31 @@ def apply_air_sea_ice_radiative_fluxes(spec, layout, arrays, stream=None):
     _assembly("nesf_apply_air_sea_ice_radiative_fluxes", spec, layout, arrays, stream)
 
 
+def area_integrals(layout, fields, factors=None, inactive=None, area=None, row_area=None, uniform_area=1.0,
+                   ctx=None, stream=None):
+    """Compensated FP64 area integrals (int dA(a) / int dA(a, b) of the reference's conservation
+    checks) of up to 16 device fields; returns a float64 device tensor (n, 2) of (sum, residual)."""
+    torch = _torch()
+    lib = load()
+    n = len(fields)
+    factors = factors or [None] * n
+    f = A.IntegralFields()
+    f.grid = _grid_of(layout)
+    f.dtype = A.NESF_F64 if fields[0].dtype == torch.float64 else A.NESF_F32
+    f.n = n
+    for k in range(n):
+        f.field[k] = fields[k].data_ptr()
+        f.factor[k] = factors[k].data_ptr() if factors[k] is not None else None
+    f.inactive = inactive.data_ptr() if inactive is not None else None
+    f.area = area.data_ptr() if area is not None else None
+    f.row_area = row_area.data_ptr() if row_area is not None else None
+    f.uniform_area = float(uniform_area)
+    out = torch.zeros((n, 2), dtype=torch.float64, device=fields[0].device)
+    ctx = ctx or default_context()
+    check(lib.nesf_area_integrals(ctx.handle, C.byref(f), C.c_void_p(out.data_ptr()), _stream_handle(stream)))
+    return out
+
+
 # ------------------------------------------------------------- coupling step
 class CouplingStep:
     """The packed arguments of nesf_coupling_step for one model's fields: the ctypes

@@ -177,6 +177,37 @@ class CoupledModel:
         self.graph.launch(stream)
         return self.kernels_per_step(self.graph_precision)
 
+    # ------------------------------------------------------ conservation
+    def row_areas(self, radius=6.371e6):
+        """Cell areas of the regular longitude-latitude exchange grid by row j = 1..ny
+        (R^2 dlambda (sin phi_north - sin phi_south)), FP64 on the device."""
+        c, L = self.coords, self.layout
+        lat = c.lat0 + np.arange(L.ny) * c.dlat
+        s = np.sin(np.radians(lat + c.dlat / 2)) - np.sin(np.radians(lat - c.dlat / 2))
+        a = radius ** 2 * np.radians(abs(c.dlon)) * np.abs(s)
+        return self.torch.from_numpy(a).to(self.device)
+
+    def heat_budget(self):
+        """The ocean heat budget of the last assembled step as compensated FP64 area integrals:
+        rho_o c_o int dA(J_T) against its sources, int dA(1 - aleph, Q_T + Q_v) + int dA(Q_io)
+        + int dA(1 - aleph, I_up) - int dA(I_lw) - int dA(I_sw) (the absorbed radiation is
+        assembled with its (1 - aleph) factor). Returns (rho_o c_o int J_T, sum of sources,
+        relative residual)."""
+        n, ao, io = self.net, self.ao, self.io
+        open_water = 1 - self.x["ice_concentration"]
+        rows = self.row_areas()
+        fields = [n["ocean_T"], ao["sensible_heat"], ao["latent_heat"], io["interface_heat"],
+                  n["ocean_upwelling_longwave"], n["ocean_downwelling_longwave"], n["ocean_downwelling_shortwave"]]
+        factors = [None, open_water, open_water, None, open_water, None, None]
+        r = api.area_integrals(self.layout, fields, factors, inactive=self.x["inactive"], row_area=rows)
+        v = r.cpu().numpy()
+        tot = v[:, 0] + v[:, 1]
+        rc = self.asm_spec.ocean_reference_density * self.asm_spec.ocean_heat_capacity
+        lhs = rc * tot[0]
+        terms = np.array([tot[1], tot[2], tot[3], tot[4], -tot[5], -tot[6]])
+        rhs = float(np.sum(terms))
+        return lhs, rhs, abs(lhs - rhs) / max(abs(lhs), float(np.abs(terms).sum()))
+
     # ---------------------------------------------------------- bookkeeping
     def active_cells(self):
         """Cells solved per step: water cells (atmosphere-ocean) + ice-covered water cells

@@ -172,3 +172,29 @@ def set_threads(n):
 
 def get_threads():
     return int(load().oracle_get_threads())
+
+
+def area_integrals(layout, fields, factors=None, inactive=None, area=None, row_area=None, uniform_area=1.0):
+    """Exact area integrals (fractions.Fraction) of the interior cells, the checker of
+    nesf_area_integrals: int dA(a) = sum(a) * A_z and int dA(a, b) = sum(a .* b) * A_z
+    (test/test_conservation.jl:100-101). Cell terms are the FP64 products a * b * area
+    rounded as the device rounds them; their sum is exact."""
+    from fractions import Fraction
+    I = layout.interior
+    mask = np.ones((layout.ny, layout.nx), bool) if inactive is None else I(inactive) == 0
+    factors = factors or [None] * len(fields)
+    out = []
+    for a, b in zip(fields, factors):
+        x = I(np.asarray(a)).astype(np.float64)
+        if b is not None:
+            x = x * I(np.asarray(b)).astype(np.float64)
+        if area is not None:
+            x = x * I(np.asarray(area, dtype=np.float64))
+        elif row_area is not None:
+            x = x * np.asarray(row_area, dtype=np.float64)[:, None]
+        terms = x[mask]
+        total = sum((Fraction(float(t)) for t in terms), Fraction(0))
+        if area is None and row_area is None:
+            total *= Fraction(float(uniform_area))
+        out.append(total)
+    return out

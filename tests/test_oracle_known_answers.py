@@ -198,3 +198,19 @@ def test_ao_solver_converges_on_1deg_sample(oracle):
     us = st.layout.interior(out["friction_velocity"])
     assert np.all(us > 0) and np.all(us < 3)
     assert np.all(np.isfinite(st.layout.interior(out["latent_heat"])))
+
+
+def test_exact_area_integrals_round_like_fsum():
+    """The integral checker's exact sums round to math.fsum of the same FP64 cell terms."""
+    import math
+    from nesf import synthetic as syn
+    from oracle import oracle as O
+    rng = np.random.default_rng(8)
+    L = syn.Layout(40, 20, 2, 2)
+    a = rng.normal(0, 1, L.shape) * 10.0 ** rng.integers(-6, 7, L.shape)
+    b = rng.uniform(0, 2, L.shape)
+    inactive = (rng.uniform(size=L.shape) < 0.2).astype(np.uint8)
+    ex = O.area_integrals(L, [a], [b], inactive=inactive, uniform_area=1.0)[0]
+    I = L.interior
+    terms = (I(a) * I(b))[I(inactive) == 0]
+    assert float(ex) == math.fsum(terms)
