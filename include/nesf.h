@@ -488,6 +488,53 @@ int nesf_apply_air_sea_ice_radiative_fluxes(const nesf_assembly_params* params, 
  * integral, written on `stream`. */
 int nesf_area_integrals(nesf_context* ctx, const nesf_integral_fields* fields, double* result, void* stream);
 
+/* ------------------------------------------------------ tensor-core check
+ * Self-check of the tcgen05 GEMM building blocks of the warm-start network in the
+ * three operand arrangements it uses (BF16 in, FP32 out; a, b, d device memory,
+ * row-major): which = 0: d[128x64] = a[128x64] b[64x64]^T; which = 1:
+ * d[128x64] = a[128x64] b[64x64]; which = 2: d[128x16] = a[128x128]^T b[128x16].
+ * Synchronises the stream; NESF_ERR_TIMEOUT if the MMA did not complete. */
+int nesf_mlp_selftest(const void* a, const void* b, float* d, int32_t which, void* stream);
+
+/* ------------------------------------------------- learned warm start
+ * A 6 -> 64 -> 64 -> 3 GELU network that predicts the transfer coefficients
+ * c_u = u* / dU, c_theta = theta* / dtheta_0, c_q = q* / dq_0 of a cell's fixed
+ * point from six features of its state before the iteration (bulk Richardson
+ * number, dU, dtheta_0, dq_0, ln h, ln of a neutral roughness). Its parameters live
+ * in one device blob of nesf_mlp_bytes() bytes (FP32 masters, BF16 copies, the
+ * gradient and the Adam moments); inference and training run on the tensor cores
+ * (tcgen05, BF16 operands, FP32 accumulation). Features are 8 floats per sample
+ * (6 used), targets 4 (c_u, c_theta, c_q, and a bit mask of the valid ones as a
+ * float), outputs 4 (c_u, c_theta, c_q, 1). The solvers take a trained blob through
+ * nesf_solver_options.mlp with warm_start = 1 (FP32 modes). No counterpart in the
+ * reference. */
+typedef struct {
+    int32_t epochs;
+    int32_t batch;              /* samples per Adam step (a multiple of 128) */
+    float learning_rate, beta1, beta2, eps;
+} nesf_mlp_train_options;
+
+int64_t nesf_mlp_bytes(void);
+int nesf_mlp_init(void* mlp, uint64_t seed, void* stream);
+/* Feature and target means and deviations from a sample set (stored in the blob). */
+int nesf_mlp_fit_normalization(void* mlp, const float* features, const float* targets, int64_t n, void* stream);
+/* Adds the gradient of the mean squared error of the n samples (normalised
+ * targets) to the blob's gradient and the error sum to its loss slots. */
+int nesf_mlp_gradient(void* mlp, const float* features, const float* targets, int64_t n, void* stream);
+/* Mini-batch Adam over the samples; `loss` (host, epochs entries, may be NULL)
+ * receives the mean loss of each epoch (synchronises the stream once per epoch). */
+int nesf_mlp_train(void* mlp, const float* features, const float* targets, int64_t n,
+                   const nesf_mlp_train_options* opts, float* loss, void* stream);
+int nesf_mlp_infer(void* mlp, const float* features, int64_t n, float* out, void* stream);
+/* Training samples from an atmosphere-ocean state: the features of every
+ * halo-ring cell (ring order, 8 floats: the 6 network inputs, then dU again and 0)
+ * and, when `targets` is given, the targets of the solved state in the fields'
+ * friction_velocity, temperature_scale and water_vapor_scale outputs. Land cells,
+ * and coefficients whose scale is near zero (|dtheta_0| < 0.05 K, |dq_0| < 1e-5),
+ * are masked out. */
+int nesf_mlp_ao_samples(const nesf_interface_params* params, const nesf_ao_fields* fields, float* features,
+                        float* targets, void* stream);
+
 /* ------------------------------------------------------- the coupling step
  * The interface-flux part of update_state!(::EarthSystemModel)
  * (EarthSystemModels/time_step_earth_system_model.jl:38-83) in one call, in the

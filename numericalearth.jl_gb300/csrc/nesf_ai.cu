@@ -70,7 +70,7 @@ __device__ __forceinline__ int ai_plain(const DevIface<double>& P, const CellCon
 // (atmosphere_sea_ice_fluxes.jl:141-142); the others go to the work list.
 template <class S>
 __global__ void __launch_bounds__(128) ai_classify_kernel(AIArgs<S> a, DevIface<double> P, DevIface<float> Pf,
-                                                          WorkList wl, DevStats* stats) {
+                                                          WorkList wl, float* feat, DevStats* stats) {
     const int nxr = a.L.nx + 2;
     const int64_t ring = (int64_t)nxr * (a.L.ny + 2);
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -88,7 +88,13 @@ __global__ void __launch_bounds__(128) ai_classify_kernel(AIArgs<S> a, DevIface<
         active = !skip;
         if (active) stable = stable_class(Pf, (float)c.Ta, (float)c.pa, (float)c.qa, (float)Ts0);
     }
-    worklist_push(wl, 0, active, stable, (uint32_t)r);
+    int64_t slot = worklist_push(wl, 0, active, stable, (uint32_t)r);
+    if (feat && slot >= 0) {
+        // warm-start features (FP32) from the state before the iteration
+        float tha = (float)c.tha;
+        mlp::store_features(feat, slot, mlp::warm_features(Pf, (float)c.dU2, tha, (float)Ts0, (float)c.qa,
+                                                           (float)c.pa));
+    }
     if (skip) {
         ai_store(P, a, k, c, 0.0, 0.0, 0.0, c.Ti, 0);
         if (stats) stats_add(stats, true, false, 0, false, false, 0, false, false);
@@ -98,10 +104,14 @@ __global__ void __launch_bounds__(128) ai_classify_kernel(AIArgs<S> a, DevIface<
 // Pass 1: the compacted ice cells, one thread each.
 template <class S, int PREC>
 __global__ void __launch_bounds__(128) ai_kernel(AIArgs<S> a, DevIface<double> P64, DevIface<float> P32,
-                                                 SolveOpts so, WorkList wl, ReplayQueue rq, DevStats* stats) {
+                                                 SolveOpts so, WorkList wl, ReplayQueue rq, const float* guess,
+                                                 DevStats* stats) {
     const int nxr = a.L.nx + 2;
-    int64_t r = worklist_get(wl, 0, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+    const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t r = worklist_get(wl, 0, w);
     if (r < 0) return;
+    float xw[3];
+    const float* warm = mlp::guess_at(guess, worklist_slot(wl, 0, w), xw);
     int i = (int)(r % nxr), j = (int)(r / nxr);
     int64_t k = a.L.at(i, j);
     const DevIface<double>& P = P64;
@@ -113,7 +123,7 @@ __global__ void __launch_bounds__(128) ai_kernel(AIArgs<S> a, DevIface<double> P
     bool needs = P.stop_kind == NESF_STOP_CONVERGENCE;
     double us = 0, ts = 0, qst = 0, Ts = c.Ti;
     int iters = 0, f64it = 0;
-    bool nonconv = false;
+    bool nonconv = false, fallback = false;
     int outcome = FAST_SOLVED, reason = -1;
     if (PREC == NESF_PLAIN_F64 || !needs) {
         iters = skin ? ai_plain<true>(P, c, Ts0, us, ts, qst, Ts, nonconv)
@@ -125,8 +135,9 @@ __global__ void __launch_bounds__(128) ai_kernel(AIArgs<S> a, DevIface<double> P
         us = ts = qst = 1e-4;
         int f32it;
         const bool accept32 = so.fp32_rho > 0.0f;
-        outcome = skin ? solve_fast<true>(P, P32, c, s, us, ts, qst, so, accept32, f32it, f64it, reason)
-                       : solve_fast<false>(P, P32, c, s, us, ts, qst, so, accept32, f32it, f64it, reason);
+        outcome = skin ? solve_fast<true>(P, P32, c, s, us, ts, qst, so, accept32, f32it, f64it, reason, warm, &fallback)
+                       : solve_fast<false>(P, P32, c, s, us, ts, qst, so, accept32, f32it, f64it, reason, warm,
+                                           &fallback);
         iters = f32it + f64it;
         Ts = s.Ts;
     }
@@ -136,13 +147,13 @@ __global__ void __launch_bounds__(128) ai_kernel(AIArgs<S> a, DevIface<double> P
     }
     if (outcome != FAST_SOLVED) {
         if (stats) {
-            stats_add(stats, true, false, 0, false, false, 0, outcome == FAST_REPLAY, false);
+            stats_add(stats, true, false, 0, false, false, 0, outcome == FAST_REPLAY, fallback);
             if (outcome == FAST_REPLAY) stats_replay_reason(stats, reason);
         }
         return;
     }
     ai_store(P, a, k, c, us, ts, qst, Ts, iters);
-    if (stats) stats_add(stats, true, true, iters, nonconv, f64it > 0, f64it, false, false);
+    if (stats) stats_add(stats, true, true, iters, nonconv, f64it > 0, f64it, false, fallback);
 }
 
 // Pass 1b (ADAPTIVE): the cells whose FP32 result was not kept, packed, through the
@@ -209,24 +220,30 @@ __global__ void __launch_bounds__(128) ai_replay_kernel(AIArgs<S> a, DevIface<do
 
 template <class S>
 static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
-                               SolveOpts so, const WorkList& wl, const ReplayQueue& rq, DevStats* stats,
-                               cudaStream_t stream) {
+                               SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws,
+                               DevStats* stats, cudaStream_t stream) {
     const int64_t ring = (int64_t)(a.L.nx + 2) * (a.L.ny + 2);
     const int block = 128;
     dim3 grid((unsigned)((ring + block - 1) / block));
-    cudaError_t e = cudaMemsetAsync(wl.count, 0, sizeof(unsigned) * 2, stream);
-    if (e == cudaSuccess && prec != NESF_PLAIN_F64) e = cudaMemsetAsync(rq.count, 0, 2 * sizeof(unsigned), stream);
-    if (e != cudaSuccess) return e;
-    ai_classify_kernel<S><<<grid, block, 0, stream>>>(a, P64, P32, wl, stats);
-    if (prec == NESF_PLAIN_F64)
-        ai_kernel<S, NESF_PLAIN_F64><<<grid, block, 0, stream>>>(a, P64, P32, so, wl, rq, stats);
-    else
-        ai_kernel<S, NESF_F32_POLISH><<<grid, block, 0, stream>>>(a, P64, P32, so, wl, rq, stats);
-    e = cudaGetLastError();
-    if (e != cudaSuccess || prec == NESF_PLAIN_F64) return e;
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const bool warm = ws.mlp != nullptr && prec != NESF_PLAIN_F64;
+    cudaError_t e = cudaMemsetAsync(wl.count, 0, sizeof(unsigned) * 2, stream);
+    if (e == cudaSuccess && prec != NESF_PLAIN_F64) e = cudaMemsetAsync(rq.count, 0, 2 * sizeof(unsigned), stream);
+    if (e != cudaSuccess) return e;
+    ai_classify_kernel<S><<<grid, block, 0, stream>>>(a, P64, P32, wl, warm ? ws.feat : nullptr, stats);
+    if (warm) {
+        e = mlp_pass((void*)ws.mlp, ws.feat, nullptr, ws.guess, 0, wl.count, wl.per_member, sms, true, stream);
+        if (e != cudaSuccess) return e;
+    }
+    const float* guess = warm ? ws.guess : nullptr;
+    if (prec == NESF_PLAIN_F64)
+        ai_kernel<S, NESF_PLAIN_F64><<<grid, block, 0, stream>>>(a, P64, P32, so, wl, rq, nullptr, stats);
+    else
+        ai_kernel<S, NESF_F32_POLISH><<<grid, block, 0, stream>>>(a, P64, P32, so, wl, rq, guess, stats);
+    e = cudaGetLastError();
+    if (e != cudaSuccess || prec == NESF_PLAIN_F64) return e;
     if (so.fp32_rho > 0.0f) {
         if (P64.temp_form != NESF_BULK_TEMPERATURE)
             ai_polish_kernel<S, true><<<(unsigned)sms * 4, block, 0, stream>>>(a, P64, P32, so, rq, stats);
@@ -240,12 +257,14 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
 }
 
 cudaError_t launch_ai(const AIArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
-                      SolveOpts so, const WorkList& wl, const ReplayQueue& rq, DevStats* stats, cudaStream_t stream) {
-    return launch_ai_t(a, P64, P32, prec, so, wl, rq, stats, stream);
+                      SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
+                      cudaStream_t stream) {
+    return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream);
 }
 cudaError_t launch_ai(const AIArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
-                      SolveOpts so, const WorkList& wl, const ReplayQueue& rq, DevStats* stats, cudaStream_t stream) {
-    return launch_ai_t(a, P64, P32, prec, so, wl, rq, stats, stream);
+                      SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
+                      cudaStream_t stream) {
+    return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream);
 }
 
 }  // namespace nesf

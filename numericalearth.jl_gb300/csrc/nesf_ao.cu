@@ -71,13 +71,27 @@ __device__ __forceinline__ void ao_store(const DevIface<double>& P, const AOArgs
     if (a.iters) a.iters[k] = iters;
 }
 
+// Warm-start features of a cell in FP32 (the training samples use the same).
+template <class S>
+__device__ __forceinline__ mlp::Features ao_features(const DevIface<float>& P, const AOArgs<S>& a, int64_t k) {
+    float ua = ldf(a.ua, k), va = ldf(a.va, k), Ta = ldf(a.Ta, k), pa = ldf(a.pa, k), qa = ldf(a.qa, k);
+    float du = ua, dv = va;
+    if (P.vel_form != NESF_WIND_VELOCITY) {
+        du = ua - 0.5f * (ldf(a.uo, k) + ldf(a.uo, k + 1));
+        dv = va - 0.5f * (ldf(a.vo, k) + ldf(a.vo, k + a.L.sj));
+    }
+    float tha = surface_atmosphere_temperature(P, Ta, qa);
+    return mlp::warm_features(P, du * du + dv * dv, tha, ldf(a.To, k) + P.off_int, qa, pa);
+}
+
 // Pass 0: land cells get the zero interface state; the others are compacted into
-// the member's work list by the sign class of their buoyancy flux.
+// the member's work list by the sign class of their buoyancy flux (and, with a
+// warm start, leave their network features at their work-list slot).
 template <class S, bool ENS>
 __global__ void __launch_bounds__(128) ao_classify_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
                                                           const DevIface<double>* __restrict__ P64s,
                                                           const DevIface<float>* __restrict__ P32s, WorkList wl,
-                                                          DevStats* stats) {
+                                                          float* feat, DevStats* stats) {
     const int nxr = a.L.nx + 2;
     const int64_t ring = (int64_t)nxr * (a.L.ny + 2);
     const int m = blockIdx.y;
@@ -95,7 +109,8 @@ __global__ void __launch_bounds__(128) ao_classify_kernel(AOArgs<S> a, DevIface<
         float Ts = (float)(ld(a.To, k) + P.off_int);
         stable = stable_class(Pf, ldf(a.Ta, k), ldf(a.pa, k), ldf(a.qa, k), Ts);
     }
-    worklist_push(wl, m, active, stable, (uint32_t)r);
+    int64_t slot = worklist_push(wl, m, active, stable, (uint32_t)r);
+    if (feat && slot >= 0) mlp::store_features(feat, slot, ao_features(Pf, a, k));
     if (in && land) {
         CellConst<double> c;
         bool l;
@@ -110,7 +125,8 @@ template <class S, int PREC, bool SKIN, bool ENS>
 __global__ void __launch_bounds__(128, ENS ? 4 : 1) ao_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
                                                               const DevIface<double>* __restrict__ P64s,
                                                               const DevIface<float>* __restrict__ P32s, SolveOpts so,
-                                                              WorkList wl, ReplayQueue rq, DevStats* stats) {
+                                                              WorkList wl, ReplayQueue rq, const float* guess,
+                                                              DevStats* stats) {
     const int nxr = a.L.nx + 2;
     const int64_t ring = (int64_t)nxr * (a.L.ny + 2);
     const int m = blockIdx.y;
@@ -125,26 +141,30 @@ __global__ void __launch_bounds__(128, ENS ? 4 : 1) ao_kernel(AOArgs<S> a, DevIf
     }
     const DevIface<double>& Pd = ENS ? sP64 : P64;
     const DevIface<float>& Pf = ENS ? sP32 : P32;
-    int64_t r = worklist_get(wl, m, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+    const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t r = worklist_get(wl, m, w);
     if (r < 0) return;
     int i = (int)(r % nxr), j = (int)(r / nxr);
     int64_t k = a.L.at(i, j) + (int64_t)m * a.member_stride;
     CellConst<double> c;
     bool land;
     ao_load(Pd, a, k, SKIN, c, land);
+    float xw[3];
+    const float* warm = mlp::guess_at(guess, worklist_slot(wl, m, w), xw);
     double us = 1e-4, ts = 1e-4, qst = 1e-4;   // initial guess (atmosphere_ocean_fluxes.jl:132)
     bool needs = Pd.stop_kind == NESF_STOP_CONVERGENCE;
     SurfaceConst<double> s{};
     if (SKIN && PREC != NESF_PLAIN_F64 && needs) s.Ts = c.Ti;   // solve_fast reads only T_s of a skin state
     else surface_const(Pd, c, c.Ti, surface_specific_humidity(Pd, c.pa, c.Ti), s);
     int iters = 0, f64it = 0;
-    bool nonconv = false;
+    bool nonconv = false, fallback = false;
     int outcome = FAST_SOLVED, reason = -1;
     if (PREC == NESF_PLAIN_F64 || !needs) {
         iters = solve_plain<SKIN>(Pd, c, s, us, ts, qst, nonconv);
     } else {
         int f32it;
-        outcome = solve_fast<SKIN>(Pd, Pf, c, s, us, ts, qst, so, so.fp32_rho > 0.0f, f32it, f64it, reason);
+        outcome = solve_fast<SKIN>(Pd, Pf, c, s, us, ts, qst, so, so.fp32_rho > 0.0f, f32it, f64it, reason, warm,
+                                   &fallback);
         iters = f32it + f64it;
     }
     const uint32_t id = (uint32_t)(m * ring + r);
@@ -154,13 +174,13 @@ __global__ void __launch_bounds__(128, ENS ? 4 : 1) ao_kernel(AOArgs<S> a, DevIf
     }
     if (outcome != FAST_SOLVED) {
         if (stats) {
-            stats_add(stats, true, false, 0, false, false, 0, outcome == FAST_REPLAY, false);
+            stats_add(stats, true, false, 0, false, false, 0, outcome == FAST_REPLAY, fallback);
             if (outcome == FAST_REPLAY) stats_replay_reason(stats, reason);
         }
         return;
     }
     ao_store(Pd, a, k, c, false, us, ts, qst, s.Ts, iters);
-    if (stats) stats_add(stats, true, true, iters, nonconv, f64it > 0, f64it, false, false);
+    if (stats) stats_add(stats, true, true, iters, nonconv, f64it > 0, f64it, false, fallback);
 }
 
 // Pass 1b (ADAPTIVE): the cells whose FP32 result was not kept, packed, through
@@ -235,20 +255,31 @@ __global__ void __launch_bounds__(128) ao_replay_kernel(AOArgs<S> a, DevIface<do
 template <class S>
 static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                                const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec,
-                               bool skin, SolveOpts so, const WorkList& wl, const ReplayQueue& rq, DevStats* stats,
-                               cudaStream_t stream) {
+                               bool skin, SolveOpts so, const WorkList& wl, const ReplayQueue& rq,
+                               const WarmStart& ws, DevStats* stats, cudaStream_t stream) {
     const int64_t ring = (int64_t)(a.L.nx + 2) * (a.L.ny + 2);
     const int threads = 128;   // kernels are compiled with __launch_bounds__(128)
     const int nm = members > 1 ? members : 1;
     dim3 grid((unsigned)((ring + threads - 1) / threads), nm);
     bool ens = members > 1 || P64s != nullptr;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // warm start (FP32 modes, one member): features in pass 0, the network's guesses before pass 1
+    const bool warm = ws.mlp != nullptr && prec != NESF_PLAIN_F64 && !ens;
+    float* feat = warm ? ws.feat : nullptr;
+    const float* guess = warm ? ws.guess : nullptr;
     cudaError_t e = cudaMemsetAsync(wl.count, 0, sizeof(unsigned) * 2 * nm, stream);
     if (e == cudaSuccess && prec != NESF_PLAIN_F64) e = cudaMemsetAsync(rq.count, 0, 2 * sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
-    if (ens) ao_classify_kernel<S, true><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, stats);
-    else ao_classify_kernel<S, false><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, stats);
+    if (ens) ao_classify_kernel<S, true><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, nullptr, stats);
+    else ao_classify_kernel<S, false><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, feat, stats);
+    if (warm) {
+        e = mlp_pass((void*)ws.mlp, ws.feat, nullptr, ws.guess, 0, wl.count, wl.per_member, sms, true, stream);
+        if (e != cudaSuccess) return e;
+    }
 #define NESF_AO_LAUNCH(PR, SK, EN) \
-    ao_kernel<S, PR, SK, EN><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, so, wl, rq, stats)
+    ao_kernel<S, PR, SK, EN><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, so, wl, rq, guess, stats)
 #define NESF_AO_ENS(PR, SK) \
     do { if (ens) NESF_AO_LAUNCH(PR, SK, true); else NESF_AO_LAUNCH(PR, SK, false); } while (0)
 #define NESF_AO_SKIN(PR) \
@@ -261,9 +292,6 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
     e = cudaGetLastError();
     if (e != cudaSuccess || prec == NESF_PLAIN_F64) return e;
     // passes 1b and 2: enough resident blocks to sweep the queues (grid-stride)
-    int dev = 0, sms = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     unsigned g2 = (unsigned)sms * 4;
     const DevIface<double>* pm = ens ? P64s : nullptr;
     if (so.fp32_rho > 0.0f) {
@@ -279,13 +307,55 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
 
 cudaError_t launch_ao(const AOArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
-                      SolveOpts so, const WorkList& wl, const ReplayQueue& rq, DevStats* stats, cudaStream_t stream) {
-    return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, stats, stream);
+                      SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
+                      cudaStream_t stream) {
+    return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, ws, stats, stream);
 }
 cudaError_t launch_ao(const AOArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
-                      SolveOpts so, const WorkList& wl, const ReplayQueue& rq, DevStats* stats, cudaStream_t stream) {
-    return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, stats, stream);
+                      SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
+                      cudaStream_t stream) {
+    return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, ws, stats, stream);
 }
+
+}  // namespace nesf
+
+namespace nesf {
+
+// Training samples of the warm-start network: the features of every ring cell
+// (ring order) and the transfer coefficients of the solved state in the fields.
+template <class S>
+__global__ void __launch_bounds__(256) ao_samples_kernel(AOArgs<S> a, DevIface<float> P, float* feat, float* targ) {
+    const int nxr = a.L.nx + 2;
+    const int64_t ring = (int64_t)nxr * (a.L.ny + 2);
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= ring) return;
+    int i = (int)(r % nxr), j = (int)(r / nxr);
+    int64_t k = a.L.at(i, j);
+    mlp::Features F = ao_features(P, a, k);
+    mlp::store_features(feat, r, F);
+    if (!targ) return;
+    bool land = a.inactive ? a.inactive[k] != 0 : false;
+    float us = ldf(a.us, k), ts = ldf(a.ts, k), qs = ldf(a.qs, k);
+    float cu = us / F.U, ct = ts / F.dth, cq = qs / F.dq;
+    int mask = 0;
+    if (!land && isfinite(cu) && us > 0.0f) mask |= 1;
+    if (!land && fabsf(F.dth) >= 0.05f && isfinite(ct)) mask |= 2;
+    if (!land && fabsf(F.dq) >= 1e-5f && isfinite(cq)) mask |= 4;
+    *(float4*)(targ + r * 4) = make_float4(mask & 1 ? cu : 0.0f, mask & 2 ? ct : 0.0f, mask & 4 ? cq : 0.0f,
+                                           (float)mask);
+}
+
+template <class S>
+cudaError_t launch_ao_samples(const AOArgs<S>& a, const DevIface<float>& P32, float* feat, float* targ,
+                              cudaStream_t s) {
+    const int64_t ring = (int64_t)(a.L.nx + 2) * (a.L.ny + 2);
+    ao_samples_kernel<S><<<(unsigned)((ring + 255) / 256), 256, 0, s>>>(a, P32, feat, targ);
+    return cudaGetLastError();
+}
+template cudaError_t launch_ao_samples<double>(const AOArgs<double>&, const DevIface<float>&, float*, float*,
+                                               cudaStream_t);
+template cudaError_t launch_ao_samples<float>(const AOArgs<float>&, const DevIface<float>&, float*, float*,
+                                              cudaStream_t);
 
 }  // namespace nesf

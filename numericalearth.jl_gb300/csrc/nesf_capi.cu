@@ -28,6 +28,9 @@ struct nesf_context {
     int64_t work_capacity;
     int32_t work_members;
     void* d_partials;           // per-block partial sums of the area integrals
+    float* d_feat;              // warm start: features (8 floats) and guesses (4) per work-list slot
+    float* d_guess;
+    int64_t warm_capacity;
     std::mutex lock;            // serialises use of the scratch above
 };
 
@@ -265,6 +268,9 @@ int nesf_context_create(int32_t device, nesf_context** out) {
     c->work_capacity = 0;
     c->work_members = 0;
     c->d_partials = nullptr;
+    c->d_feat = nullptr;
+    c->d_guess = nullptr;
+    c->warm_capacity = 0;
     cudaError_t e = cudaMalloc(&c->d_stats, sizeof(DevStats));
     if (e == cudaSuccess) e = cudaMalloc(&c->d_partials, (size_t)kIntegralBlocks * NESF_MAX_INTEGRALS * 16);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_replay_count, 2 * sizeof(unsigned int));
@@ -293,6 +299,8 @@ int nesf_context_destroy(nesf_context* c) {
         cudaFree(c->d_work);
         cudaFree(c->d_work_count);
         cudaFree(c->d_partials);
+        cudaFree(c->d_feat);
+        cudaFree(c->d_guess);
     }
     delete c;
     return NESF_OK;
@@ -340,19 +348,21 @@ static nesf_solver_options options_or_default(const nesf_solver_options* o) {
     if (r.polish_maxiter <= 0) r.polish_maxiter = d.polish_maxiter;
     if (!(r.path_tolerance > 0)) r.path_tolerance = d.path_tolerance;
     if (!(r.fp32_rho > 0)) r.fp32_rho = d.fp32_rho;
+    if (!(r.fallback_ratio > 0)) r.fallback_ratio = d.fallback_ratio;
     return r;
 }
 
 // The kernels' knobs; fp32_rho = 0 keeps no FP32 result (NESF_F32_POLISH).
 static SolveOpts solve_opts(const nesf_solver_options& o) {
     float rho = o.precision == NESF_F32_ADAPTIVE ? (float)(o.fp32_rho < 0.99 ? o.fp32_rho : 0.99) : 0.0f;
-    return SolveOpts{o.polish_maxiter, (float)o.path_tolerance, rho};
+    return SolveOpts{o.polish_maxiter, (float)o.path_tolerance, rho, (float)o.fallback_ratio};
 }
 
 static int check_options(const nesf_solver_options& o, const char* who) {
     if (o.precision != NESF_PLAIN_F64 && o.precision != NESF_F32_POLISH && o.precision != NESF_F32_ADAPTIVE)
         return fail(NESF_ERR_ARG, "%s: precision %d", who, o.precision);
-    if (o.warm_start) return fail(NESF_ERR_UNSUPPORTED, "%s: warm start needs nesf_coupling_step", who);
+    if (o.warm_start && !o.mlp) return fail(NESF_ERR_ARG, "%s: warm_start without a network (mlp)", who);
+    if (o.warm_start && !(o.fallback_ratio > 0)) return fail(NESF_ERR_ARG, "%s: fallback_ratio must be > 0", who);
     return NESF_OK;
 }
 
@@ -403,6 +413,25 @@ static int work_list(nesf_context* ctx, int64_t per_member, int32_t members, Wor
 // Library-owned context of the current device, for calls that pass none.
 static nesf_context* g_default_ctx[64];
 static std::mutex g_default_lock;
+
+// The context's warm-start buffers for `cells` work-list slots (caller holds the lock).
+static int warm_buffers(nesf_context* ctx, const nesf_solver_options& o, int64_t cells, WarmStart* ws) {
+    *ws = WarmStart{nullptr, nullptr, nullptr};
+    if (!o.warm_start || o.precision == NESF_PLAIN_F64) return NESF_OK;
+    if (cells > ctx->warm_capacity) {
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) return cuda_fail(e, "warm-start buffers");
+        cudaFree(ctx->d_feat);
+        cudaFree(ctx->d_guess);
+        ctx->d_feat = ctx->d_guess = nullptr;
+        ctx->warm_capacity = 0;
+        NESF_CUDA(cudaMalloc(&ctx->d_feat, sizeof(float) * 8 * (size_t)cells));
+        NESF_CUDA(cudaMalloc(&ctx->d_guess, sizeof(float) * 4 * (size_t)cells));
+        ctx->warm_capacity = cells;
+    }
+    *ws = WarmStart{ctx->d_feat, ctx->d_guess, o.mlp};
+    return NESF_OK;
+}
 
 static int context_or_default(nesf_context** ctx) {
     if (*ctx) return NESF_OK;
@@ -503,14 +532,17 @@ extern "C" int nesf_compute_atmosphere_ocean_fluxes(nesf_context* ctx, const nes
     int64_t ring = (int64_t)(f->grid.nx + 2) * (f->grid.ny + 2);
     ReplayQueue rq;
     WorkList wl;
+    WarmStart ws;
     if ((r = replay_queue(ctx, ring, &rq))) return r;
     if ((r = work_list(ctx, ring, 1, &wl))) return r;
+    if ((r = warm_buffers(ctx, o, ring, &ws))) return r;
     SolveOpts so = solve_opts(o);
     return with_stats(ctx, stats, s, [&](DevStats* ds) {
         if (f->dtype == NESF_F64)
-            return launch_ao(ao_args<double>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl, rq, ds,
-                             s);
-        return launch_ao(ao_args<float>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl, rq, ds, s);
+            return launch_ao(ao_args<double>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl, rq, ws,
+                             ds, s);
+        return launch_ao(ao_args<float>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl, rq, ws, ds,
+                         s);
     });
 }
 
@@ -572,9 +604,9 @@ extern "C" int nesf_compute_atmosphere_ocean_fluxes_ensemble(nesf_context* ctx, 
     return with_stats(ctx, stats, s, [&](DevStats* ds) {
         if (f->dtype == NESF_F64)
             return launch_ao(ao_args<double>(f, member_stride), P64, P32, ctx->d_p64, ctx->d_p32, members,
-                             o.precision, skin, so, wl, rq, ds, s);
+                             o.precision, skin, so, wl, rq, WarmStart{}, ds, s);
         return launch_ao(ao_args<float>(f, member_stride), P64, P32, ctx->d_p64, ctx->d_p32, members, o.precision,
-                         skin, so, wl, rq, ds, s);
+                         skin, so, wl, rq, WarmStart{}, ds, s);
     });
 }
 
@@ -627,12 +659,14 @@ extern "C" int nesf_compute_atmosphere_sea_ice_fluxes(nesf_context* ctx, const n
     int64_t ring = (int64_t)(f->grid.nx + 2) * (f->grid.ny + 2);
     ReplayQueue rq;
     WorkList wl;
+    WarmStart ws;
     if ((r = replay_queue(ctx, ring, &rq))) return r;
     if ((r = work_list(ctx, ring, 1, &wl))) return r;
+    if ((r = warm_buffers(ctx, o, ring, &ws))) return r;
     SolveOpts so = solve_opts(o);
     return with_stats(ctx, stats, s, [&](DevStats* ds) {
-        if (f->dtype == NESF_F64) return launch_ai(ai_args<double>(f), P64, P32, o.precision, so, wl, rq, ds, s);
-        return launch_ai(ai_args<float>(f), P64, P32, o.precision, so, wl, rq, ds, s);
+        if (f->dtype == NESF_F64) return launch_ai(ai_args<double>(f), P64, P32, o.precision, so, wl, rq, ws, ds, s);
+        return launch_ai(ai_args<float>(f), P64, P32, o.precision, so, wl, rq, ws, ds, s);
     });
 }
 
@@ -862,9 +896,129 @@ extern "C" int nesf_compute_atmosphere_ocean_fluxes_noalloc(const nesf_interface
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = f->dtype == NESF_F64
                         ? launch_ao(ao_args<double>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl,
-                                    rq, nullptr, s)
+                                    rq, WarmStart{}, nullptr, s)
                         : launch_ao(ao_args<float>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl,
-                                    rq, nullptr, s);
+                                    rq, WarmStart{}, nullptr, s);
+    if (e != cudaSuccess) return cuda_fail(e, who);
+    return NESF_OK;
+}
+
+// ---------------------------------------------------- tensor-core check
+namespace nesf {
+cudaError_t launch_tc_selftest(const void* A, const void* B, float* D, int which, unsigned int* status,
+                               cudaStream_t s);
+}
+
+extern "C" int nesf_mlp_selftest(const void* a, const void* b, float* d, int32_t which, void* stream) {
+    const char* who = "nesf_mlp_selftest";
+    if (!a || !b || !d) return fail(NESF_ERR_ARG, "%s: null argument", who);
+    if (which < 0 || which > 2) return fail(NESF_ERR_ARG, "%s: which = %d", who, which);
+    unsigned int* st = nullptr;
+    NESF_CUDA(cudaMalloc(&st, sizeof(unsigned int)));
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaMemsetAsync(st, 0, sizeof(unsigned int), s);
+    if (e == cudaSuccess) e = launch_tc_selftest(a, b, d, which, st, s);
+    unsigned int h = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, st, sizeof h, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(st);
+    if (e != cudaSuccess) return cuda_fail(e, who);
+    if (h) return fail(NESF_ERR_TIMEOUT, "%s: the MMA did not complete", who);
+    return NESF_OK;
+}
+
+// ------------------------------------------------------ warm-start network
+namespace nesf {
+cudaError_t mlp_init(void* blob, uint64_t seed, cudaStream_t s);
+cudaError_t mlp_fit_normalization(void* blob, const float* x, const float* t, int64_t n, cudaStream_t s);
+cudaError_t mlp_adam(void* blob, float lr, float beta1, float beta2, float eps, cudaStream_t s);
+size_t mlp_blob_bytes();
+size_t mlp_loss_offset();
+}
+
+static int sm_count() {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms;
+}
+
+extern "C" int64_t nesf_mlp_bytes(void) { return (int64_t)mlp_blob_bytes(); }
+
+extern "C" int nesf_mlp_init(void* mlp, uint64_t seed, void* stream) {
+    if (!mlp) return fail(NESF_ERR_ARG, "nesf_mlp_init: null blob");
+    cudaError_t e = mlp_init(mlp, seed, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "nesf_mlp_init");
+    return NESF_OK;
+}
+
+extern "C" int nesf_mlp_fit_normalization(void* mlp, const float* x, const float* t, int64_t n, void* stream) {
+    if (!mlp || !x || !t || n <= 0) return fail(NESF_ERR_ARG, "nesf_mlp_fit_normalization: bad argument");
+    cudaError_t e = mlp_fit_normalization(mlp, x, t, n, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "nesf_mlp_fit_normalization");
+    return NESF_OK;
+}
+
+extern "C" int nesf_mlp_gradient(void* mlp, const float* x, const float* t, int64_t n, void* stream) {
+    if (!mlp || !x || !t || n <= 0) return fail(NESF_ERR_ARG, "nesf_mlp_gradient: bad argument");
+    int64_t tiles = (n + 127) / 128;
+    int grid = (int)(tiles < sm_count() ? tiles : sm_count());
+    cudaError_t e = mlp_pass(mlp, x, t, nullptr, n, nullptr, 0, grid, false, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "nesf_mlp_gradient");
+    return NESF_OK;
+}
+
+extern "C" int nesf_mlp_train(void* mlp, const float* x, const float* t, int64_t n, const nesf_mlp_train_options* o,
+                              float* loss, void* stream) {
+    const char* who = "nesf_mlp_train";
+    if (!mlp || !x || !t || !o || n <= 0) return fail(NESF_ERR_ARG, "%s: bad argument", who);
+    if (o->batch <= 0 || o->batch % 128 != 0) return fail(NESF_ERR_ARG, "%s: batch %d not a multiple of 128", who, o->batch);
+    if (o->epochs <= 0 || !(o->learning_rate > 0)) return fail(NESF_ERR_ARG, "%s: epochs / learning rate", who);
+    cudaStream_t s = (cudaStream_t)stream;
+    const int sms = sm_count();
+    float* loss_dev = (float*)((char*)mlp + mlp_loss_offset());
+    for (int ep = 0; ep < o->epochs; ep++) {
+        cudaError_t e = cudaMemsetAsync(loss_dev, 0, 2 * sizeof(float), s);
+        for (int64_t b0 = 0; e == cudaSuccess && b0 < n; b0 += o->batch) {
+            int64_t nb = n - b0 < o->batch ? n - b0 : o->batch;
+            int64_t tiles = (nb + 127) / 128;
+            int grid = (int)(tiles < sms ? tiles : sms);
+            e = mlp_pass(mlp, x + b0 * 8, t + b0 * 4, nullptr, nb, nullptr, 0, grid, false, s);
+            if (e == cudaSuccess) e = mlp_adam(mlp, o->learning_rate, o->beta1, o->beta2, o->eps, s);
+        }
+        if (e == cudaSuccess && loss) {
+            float h[2] = {0.0f, 0.0f};
+            e = cudaMemcpyAsync(h, loss_dev, sizeof h, cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            loss[ep] = h[1] > 0 ? h[0] / h[1] : 0.0f;
+        }
+        if (e != cudaSuccess) return cuda_fail(e, who);
+    }
+    return NESF_OK;
+}
+
+extern "C" int nesf_mlp_infer(void* mlp, const float* x, int64_t n, float* out, void* stream) {
+    if (!mlp || !x || !out || n <= 0) return fail(NESF_ERR_ARG, "nesf_mlp_infer: bad argument");
+    int64_t tiles = (n + 127) / 128;
+    int grid = (int)(tiles < sm_count() ? tiles : sm_count());
+    cudaError_t e = mlp_pass(mlp, x, nullptr, out, n, nullptr, 0, grid, false, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "nesf_mlp_infer");
+    return NESF_OK;
+}
+
+extern "C" int nesf_mlp_ao_samples(const nesf_interface_params* params, const nesf_ao_fields* f, float* feat,
+                                   float* targ, void* stream) {
+    const char* who = "nesf_mlp_ao_samples";
+    int r = check_params(params, who);
+    if (r) return r;
+    if ((r = check_ao_fields(f, params, who))) return r;
+    if (!feat) return fail(NESF_ERR_ARG, "%s: null features", who);
+    if (targ && (!f->friction_velocity || !f->temperature_scale || !f->water_vapor_scale))
+        return fail(NESF_ERR_ARG, "%s: targets need the solved u*, theta*, q* fields", who);
+    DevIface<float> P32 = make_dev_iface<float>(*params);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = f->dtype == NESF_F64 ? launch_ao_samples(ao_args<double>(f, 0), P32, feat, targ, s)
+                                         : launch_ao_samples(ao_args<float>(f, 0), P32, feat, targ, s);
     if (e != cudaSuccess) return cuda_fail(e, who);
     return NESF_OK;
 }

@@ -20,14 +20,24 @@
 #pragma once
 
 #include "nesf_kernels.cuh"
+#include "nesf_mlp.cuh"
 
 namespace nesf {
 
 // Knobs of the FP32 + FP64-polish solver.
 struct SolveOpts {
-    int polish_steps;   // FP64 Newton steps
-    float path_tol;     // replay threshold on the reference's stopping-error bound
-    float fp32_rho;     // ADAPTIVE: keep the FP32 result below this contraction (0: never)
+    int polish_steps;      // FP64 Newton steps
+    float path_tol;        // replay threshold on the reference's stopping-error bound
+    float fp32_rho;        // ADAPTIVE: keep the FP32 result below this contraction (0: never)
+    float fallback_ratio;  // warm start: cold start when the first residual exceeds this times the cold one
+};
+
+// Warm start of a solve: features written by the classify pass at the work-list
+// slots, the network's guesses (u*, theta*, q*, valid) at the same slots.
+struct WarmStart {
+    float* feat;           // 8 floats per slot
+    float* guess;          // 4 floats per slot
+    const void* mlp;       // trained network (null: cold start)
 };
 
 // Active cells of one solve, compacted and split by the sign of the surface
@@ -387,7 +397,8 @@ template <bool SKIN>
 __device__ __forceinline__ int solve_fast(const DevIface<double>& P64, const DevIface<float>& P32,
                                           const CellConst<double>& c64, SurfaceConst<double>& s64, double& us,
                                           double& ts, double& qst, const SolveOpts& so, bool accept32, int& fp32_it,
-                                          int& fp64_it, int& reason) {
+                                          int& fp64_it, int& reason, const float* xw = nullptr,
+                                          bool* fell_back = nullptr) {
     constexpr int N = SKIN ? 4 : 3;
     fp64_it = 0;
     CellConst<float> c32;
@@ -398,7 +409,14 @@ __device__ __forceinline__ int solve_fast(const DevIface<double>& P64, const Dev
     if (SKIN) anc = skin_anchor(P64, c64);
     const float tol = (float)P64.tol;
     // sweep state; a skin temperature as tau = T_s - theta_a (the delta form)
-    float x[4] = {(float)us, (float)ts, (float)qst, SKIN ? (float)(s64.Ts - c64.tha) : 0.0f};
+    const float x0[4] = {(float)us, (float)ts, (float)qst, SKIN ? (float)(s64.Ts - c64.tha) : 0.0f};
+    float x[4] = {x0[0], x0[1], x0[2], x0[3]};
+    // warm start: the network's (u*, theta*, q*) replaces the reference's start; T_s keeps its own
+    const bool warm = xw != nullptr && isfinite(xw[0]) && isfinite(xw[1]) && isfinite(xw[2]) && xw[0] > 0.0f;
+    if (warm) { x[0] = xw[0]; x[1] = xw[1]; x[2] = xw[2]; }
+    float yw[4] = {0, 0, 0, 0};   // first iterate from the warm start while the cold start is probed
+    float rw = 0.0f;
+    int probes = 0;
     float yp[4] = {0, 0, 0, 0};   // F(x + h e_j) of the column in progress
     float J[N][N];
     SweepTrace tr;
@@ -408,13 +426,17 @@ __device__ __forceinline__ int solve_fast(const DevIface<double>& P64, const Dev
     int rising = 0;
     bool stalled = false;  // the sweep ended on the rising-drift rule
     int it = 0;            // sweep iterations
-    int phase = 0;         // 0 sweep; 2 + 2j / 3 + 2j: F(x + h e_j) / F(x - h e_j)
+    int phase = 0;         // 0 sweep; 1 cold-start probe; 2 + 2j / 3 + 2j: F(x + h e_j) / F(x - h e_j)
     float h = 0.0f;
     float cond = 1.0f;     // condition of the anchored differences at the last sweep iterate
     const int limit = P32.maxiter;
 #pragma unroll 1
     for (;;) {
         float xin[4] = {x[0], x[1], x[2], x[3]};
+        if (phase == 1) {
+#pragma unroll
+            for (int k = 0; k < 4; k++) xin[k] = x0[k];
+        }
         if (phase >= 2) {
             const int jj = (phase - 2) >> 1;
             const float sgn = (phase & 1) ? -1.0f : 1.0f;
@@ -432,11 +454,36 @@ __device__ __forceinline__ int solve_fast(const DevIface<double>& P64, const Dev
             iterate_state<float, false>(P32, c32, sv, yu, yt, yq);
         }
         float y[4] = {yu, yt, yq, yT};
+        if (phase == 1) {
+            // cold-start fallback: keep the warm start unless its first residual exceeds
+            // fallback_ratio times the cold start's
+            probes = 1;
+            float rc = fabsf(y[0] - x0[0]) + fabsf(y[1] - x0[1]) + fabsf(y[2] - x0[2]);
+            const bool cold = !(rw <= so.fallback_ratio * rc);
+            if (cold && fell_back) *fell_back = true;
+            const float* from = cold ? x0 : x;
+            const float* to = cold ? y : yw;
+            tr.d[0] = fabsf(to[0] - from[0]); tr.d[1] = fabsf(to[1] - from[1]); tr.d[2] = fabsf(to[2] - from[2]);
+            tr.lam = 1.0f;
+            prev = cold ? rc : rw;
+#pragma unroll
+            for (int k = 0; k < 4; k++) x[k] = to[k];
+            phase = 0;
+            continue;
+        }
         if (phase == 0) {
             it++;
             float du = fabsf(y[0] - x[0]), dt = fabsf(y[1] - x[1]), dq = fabsf(y[2] - x[2]);
             float dT = SKIN ? fabsf(y[3] - x[3]) : 0.0f;
             float drift = du + dt + dq;
+            if (warm && it == 1 && drift > 0.01f * (fabsf(x[0]) + fabsf(x[1]) + fabsf(x[2]))) {
+                // a large first residual from the guess: probe the cold start before going on
+#pragma unroll
+                for (int k = 0; k < 4; k++) yw[k] = y[k];
+                rw = drift;
+                phase = 1;
+                continue;
+            }
 #pragma unroll
             for (int k = 0; k < 4; k++) x[k] = y[k];
             // FP32 resolution of the drift sum: the ulps of the scales themselves
@@ -480,7 +527,7 @@ __device__ __forceinline__ int solve_fast(const DevIface<double>& P64, const Dev
             if (++phase == 2 * N + 2) break;
         }
     }
-    fp32_it = it + 2 * N;
+    fp32_it = it + probes + 2 * N;
     // ---- contraction rate of F at the solution
     const float rho_est = spectral_bound<N>(J);
     if (!(rho_est < 0.995f)) { reason = REPLAY_SLOW; return FAST_REPLAY; }
@@ -584,10 +631,13 @@ __device__ __forceinline__ int solve_fast(const DevIface<double>& P64, const Dev
     return FAST_SOLVED;
 }
 
-// Warp-aggregated append of `id` to one side of a member's work list.
-__device__ __forceinline__ void worklist_push(const WorkList& w, int member, bool active, bool stable, uint32_t id) {
+// Warp-aggregated append of `id` to one side of a member's work list; returns the
+// slot it took (member * per_member + position), or -1.
+__device__ __forceinline__ int64_t worklist_push(const WorkList& w, int member, bool active, bool stable,
+                                                 uint32_t id) {
     unsigned mask = __activemask();
     int lane = threadIdx.x & 31;
+    int64_t slot = -1;
 #pragma unroll
     for (int side = 0; side < 2; side++) {
         bool want = active && (stable == (side == 1));
@@ -599,11 +649,18 @@ __device__ __forceinline__ void worklist_push(const WorkList& w, int member, boo
         base = __shfl_sync(mask, base, leader);
         if (want) {
             unsigned pos = base + __popc(ballot & ((1u << lane) - 1u));
-            uint32_t* seg = w.idx + (int64_t)member * w.per_member;
-            if (side == 0) seg[pos] = id;
-            else seg[w.per_member - 1 - pos] = id;
+            int64_t p = side == 0 ? (int64_t)pos : w.per_member - 1 - (int64_t)pos;
+            w.idx[(int64_t)member * w.per_member + p] = id;
+            slot = (int64_t)member * w.per_member + p;
         }
     }
+    return slot;
+}
+
+// The slot of the w-th entry of a member's work list (unstable cells first).
+__device__ __forceinline__ int64_t worklist_slot(const WorkList& wl, int member, int64_t w) {
+    const unsigned nu = wl.count[2 * member];
+    return (int64_t)member * wl.per_member + (w < nu ? w : wl.per_member - 1 - (w - nu));
 }
 
 // The w-th entry of a member's work list (unstable cells first), or -1.
@@ -648,13 +705,23 @@ __device__ __forceinline__ void polish_push(const ReplayQueue& q, bool want, uin
 
 cudaError_t launch_ao(const AOArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
-                      SolveOpts so, const WorkList& wl, const ReplayQueue& rq, DevStats* stats, cudaStream_t stream);
+                      SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
+                      cudaStream_t stream);
 cudaError_t launch_ao(const AOArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
-                      SolveOpts so, const WorkList& wl, const ReplayQueue& rq, DevStats* stats, cudaStream_t stream);
+                      SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
+                      cudaStream_t stream);
 cudaError_t launch_ai(const AIArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
-                      SolveOpts so, const WorkList& wl, const ReplayQueue& rq, DevStats* stats, cudaStream_t stream);
+                      SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
+                      cudaStream_t stream);
 cudaError_t launch_ai(const AIArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
-                      SolveOpts so, const WorkList& wl, const ReplayQueue& rq, DevStats* stats, cudaStream_t stream);
+                      SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
+                      cudaStream_t stream);
+template <class S>
+cudaError_t launch_ao_samples(const AOArgs<S>& a, const DevIface<float>& P32, float* feat, float* targ,
+                              cudaStream_t s);
+// The warm-start network's inference pass over a work list (nesf_mlp.cu).
+cudaError_t mlp_pass(void* blob, const float* x, const float* t, float* y, int64_t n, const unsigned int* count,
+                     int64_t per_member, int grid, bool state, cudaStream_t s);
 
 }  // namespace nesf

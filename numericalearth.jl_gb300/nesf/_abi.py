@@ -200,6 +200,31 @@ class CouplingStepArgs(C.Structure):
                 ("radiation", i32), ("pad_", i32)]
 
 
+class MlpTrainOptions(C.Structure):
+    _fields_ = [("epochs", i32), ("batch", i32), ("learning_rate", C.c_float), ("beta1", C.c_float),
+                ("beta2", C.c_float), ("eps", C.c_float)]
+
+
+# the warm-start network's device blob (nesf_mlp.cuh, struct Blob)
+MLP_IN, MLP_IN_PAD, MLP_HID, MLP_OUT, MLP_OUT_PAD = 6, 16, 64, 3, 16
+MLP_W1 = 0
+MLP_B1 = MLP_W1 + MLP_HID * MLP_IN_PAD
+MLP_W2 = MLP_B1 + MLP_HID
+MLP_B2 = MLP_W2 + MLP_HID * MLP_HID
+MLP_W3 = MLP_B2 + MLP_HID
+MLP_B3 = MLP_W3 + MLP_OUT_PAD * MLP_HID
+MLP_PARAMS = MLP_B3 + MLP_OUT_PAD
+
+
+class MlpBlob(C.Structure):
+    _fields_ = [("p", C.c_float * MLP_PARAMS), ("g", C.c_float * MLP_PARAMS), ("m", C.c_float * MLP_PARAMS),
+                ("v", C.c_float * MLP_PARAMS), ("in_mu", C.c_float * 8), ("in_sig", C.c_float * 8),
+                ("out_mu", C.c_float * 4), ("out_sig", C.c_float * 4), ("loss", C.c_float * 4), ("steps", i32),
+                ("error", i32), ("pad_", i32 * 2), ("stats", C.c_double * 32),
+                ("w1h", C.c_uint16 * (MLP_HID * MLP_IN_PAD)), ("w2h", C.c_uint16 * (MLP_HID * MLP_HID)),
+                ("w3h", C.c_uint16 * (MLP_OUT_PAD * MLP_HID))]
+
+
 MAX_INTEGRALS = 16
 
 

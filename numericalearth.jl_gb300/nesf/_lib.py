@@ -49,6 +49,14 @@ SIGNATURES = {
     "nesf_apply_air_sea_radiative_fluxes": (C.c_int, [P(A.AssemblyParams), P(A.AssemblyFields), vp]),
     "nesf_apply_air_sea_ice_radiative_fluxes": (C.c_int, [P(A.AssemblyParams), P(A.AssemblyFields), vp]),
     "nesf_area_integrals": (C.c_int, [vp, P(A.IntegralFields), vp, vp]),
+    "nesf_mlp_selftest": (C.c_int, [vp, vp, vp, C.c_int32, vp]),
+    "nesf_mlp_bytes": (C.c_int64, []),
+    "nesf_mlp_init": (C.c_int, [vp, C.c_uint64, vp]),
+    "nesf_mlp_fit_normalization": (C.c_int, [vp, vp, vp, C.c_int64, vp]),
+    "nesf_mlp_gradient": (C.c_int, [vp, vp, vp, C.c_int64, vp]),
+    "nesf_mlp_train": (C.c_int, [vp, vp, vp, C.c_int64, P(A.MlpTrainOptions), P(C.c_float), vp]),
+    "nesf_mlp_infer": (C.c_int, [vp, vp, C.c_int64, vp, vp]),
+    "nesf_mlp_ao_samples": (C.c_int, [P(A.InterfaceParams), P(A.AOFields), vp, vp, vp]),
     "nesf_coupling_step": (C.c_int, [vp, P(A.CouplingStepArgs), P(A.SolverOptions), vp]),
     "nesf_graph_capture": (C.c_int, [vp, P(A.CouplingStepArgs), P(A.SolverOptions), P(vp)]),
     "nesf_graph_set_time_weight": (C.c_int, [vp, C.c_double]),

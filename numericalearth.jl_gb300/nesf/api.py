@@ -66,13 +66,17 @@ def default_context(device=None):
     return _DEFAULT_CTX[dev]
 
 
-def solver_options(precision="f64", polish_maxiter=0, block_size=128, schedule=0):
+def solver_options(precision="f64", polish_maxiter=0, block_size=128, schedule=0, mlp=None):
+    """nesf_solver_options; `mlp` (a warm.WarmStartNetwork) turns on the learned warm start."""
     o = A.SolverOptions()
     load().nesf_default_solver_options(C.byref(o))
     o.precision = PRECISIONS[precision]
     o.polish_maxiter = polish_maxiter
     o.block_size = block_size
     o.schedule = schedule
+    if mlp is not None:
+        o.warm_start = 1
+        o.mlp = mlp.ptr
     return o
 
 
@@ -87,7 +91,7 @@ def _grid_of(layout):
 
 
 def compute_atmosphere_ocean_fluxes(spec, layout, state, out, precision="f64", polish_maxiter=0, stats=False,
-                                    iterations=None, ctx=None, stream=None):
+                                    iterations=None, ctx=None, stream=None, mlp=None):
     """atmosphere_ocean_fluxes.jl:17-60 on device tensors. `state` holds AO inputs
     (fields.AO_INPUTS), `out` the AtmosphereSurfaceFluxes + interface temperature."""
     lib = load()
@@ -96,7 +100,7 @@ def compute_atmosphere_ocean_fluxes(spec, layout, state, out, precision="f64", p
     arrays["iterations"] = iterations
     f = F.pack(A.AOFields, _grid_of(layout), arrays)
     p = spec.to_c() if hasattr(spec, "to_c") else spec
-    o = solver_options(precision, polish_maxiter)
+    o = solver_options(precision, polish_maxiter, mlp=mlp)
     st = A.Stats() if stats else None
     ctx = ctx or default_context()
     check(lib.nesf_compute_atmosphere_ocean_fluxes(ctx.handle, C.byref(p), C.byref(f), C.byref(o),
@@ -125,7 +129,7 @@ def compute_atmosphere_ocean_fluxes_ensemble(specs, layout, state, out, precisio
 
 
 def compute_atmosphere_sea_ice_fluxes(spec, layout, state, out, precision="f64", polish_maxiter=0, stats=False,
-                                      iterations=None, ctx=None, stream=None):
+                                      iterations=None, ctx=None, stream=None, mlp=None):
     """atmosphere_sea_ice_fluxes.jl:18-62; `out['interface_temperature']` is read as the
     initial skin temperature and overwritten with the solved one."""
     lib = load()
@@ -135,7 +139,7 @@ def compute_atmosphere_sea_ice_fluxes(spec, layout, state, out, precision="f64",
     arrays["iterations"] = iterations
     f = F.pack(A.AIFields, _grid_of(layout), arrays)
     p = spec.to_c() if hasattr(spec, "to_c") else spec
-    o = solver_options(precision, polish_maxiter)
+    o = solver_options(precision, polish_maxiter, mlp=mlp)
     st = A.Stats() if stats else None
     ctx = ctx or default_context()
     check(lib.nesf_compute_atmosphere_sea_ice_fluxes(ctx.handle, C.byref(p), C.byref(f), C.byref(o),
@@ -299,10 +303,10 @@ class CouplingStep:
         self.interp_f.time_weight = float(tn)
 
 
-def coupling_step(step, precision="f32_adaptive", ctx=None, stream=None):
+def coupling_step(step, precision="f32_adaptive", ctx=None, stream=None, mlp=None):
     """update_state!'s interface-flux phases in one native call (nesf_coupling_step)."""
     lib = load()
-    o = solver_options(precision)
+    o = solver_options(precision, mlp=mlp)
     ctx = ctx or default_context()
     check(lib.nesf_coupling_step(ctx.handle, C.byref(step.args), C.byref(o), _stream_handle(stream)))
 
@@ -310,11 +314,12 @@ def coupling_step(step, precision="f32_adaptive", ctx=None, stream=None):
 class Graph:
     """A captured CUDA graph of one coupling step (nesf_graph_capture)."""
 
-    def __init__(self, step, precision="f32_adaptive", ctx=None):
+    def __init__(self, step, precision="f32_adaptive", ctx=None, mlp=None):
         self.lib = load()
         self.step = step                     # keeps the captured pointers' owners alive
+        self.mlp = mlp                       # and the network the graph reads
         self.ctx = ctx or default_context()
-        o = solver_options(precision)
+        o = solver_options(precision, mlp=mlp)
         h = C.c_void_p()
         check(self.lib.nesf_graph_capture(self.ctx.handle, C.byref(step.args), C.byref(o), C.byref(h)))
         self.handle = h

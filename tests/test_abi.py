@@ -78,3 +78,8 @@ def test_argument_errors_without_gpu():
     assert lib.nesf_abi_version() == 1
     with pytest.raises(_lib.NesfError):
         _lib.check(A.NESF_ERR_ARG)
+
+
+def test_network_blob_layout_matches_binding():
+    lib = _lib.load()
+    assert lib.nesf_mlp_bytes() == C.sizeof(A.MlpBlob)
