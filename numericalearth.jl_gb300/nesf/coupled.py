@@ -68,6 +68,7 @@ class CoupledModel:
         self.net = {k: z() for k in OCEAN_NET + ICE_NET + RAD_DIAG}
         self.zero_io_stress = z()
         self.intercepted = z()
+        self.mlp = None       # a trained warm.WarmStartNetwork: warm start of the FP32 solvers
 
     # -------------------------------------------------------------- phases
     def interpolate_state(self, stream=None):
@@ -81,11 +82,12 @@ class CoupledModel:
     def compute_fluxes(self, precision="f64", polish_maxiter=0, stats=False, stream=None):
         x = self.x
         s_ao = api.compute_atmosphere_ocean_fluxes(self.ao_spec, self.layout, x, self.ao, precision=precision,
-                                                   polish_maxiter=polish_maxiter, stats=stats, stream=stream)
+                                                   polish_maxiter=polish_maxiter, stats=stats, stream=stream,
+                                                   mlp=self.mlp)
         ai_state = {k: x.get(k) for k in F.AI_INPUTS}
         s_ai = api.compute_atmosphere_sea_ice_fluxes(self.ai_spec, self.layout, ai_state, self.ai,
                                                      precision=precision, polish_maxiter=polish_maxiter,
-                                                     stats=stats, stream=stream)
+                                                     stats=stats, stream=stream, mlp=self.mlp)
         io_state = {"ice_salinity": x["ice_salinity"], "ice_thickness": x["ice_thickness"],
                     "consolidation_thickness": x["consolidation_thickness"],
                     "ice_concentration": x["ice_concentration"], "internal_temperature": x["ice_temperature"],
@@ -129,7 +131,8 @@ class CoupledModel:
         """Kernels one step launches: interpolation; per solve classify + solve (+ the packed
         polish pass of the adaptive mode, + the replay pass of the FP32 modes); sea-ice-ocean;
         ocean and sea-ice assembly and their radiative add-ons."""
-        per_solve = 2 + (precision == "f32_adaptive") + (precision != "f64" and precision != "plain")
+        fast = precision != "f64" and precision != "plain"
+        per_solve = 2 + (precision == "f32_adaptive") + fast + (fast and self.mlp is not None)
         return (1 if self.atmos is not None else 0) + 2 * per_solve + 1 + 4
 
     # ------------------------------------------------- native step and graph
@@ -161,12 +164,12 @@ class CoupledModel:
 
     def native_step(self, precision="f32_adaptive", stream=None):
         """One coupling step through nesf_coupling_step; returns the kernels launched."""
-        api.coupling_step(self.step_args(), precision, stream=stream)
+        api.coupling_step(self.step_args(), precision, stream=stream, mlp=self.mlp)
         return self.kernels_per_step(precision)
 
     def capture(self, precision="f32_adaptive"):
         """Capture one coupling step as a CUDA graph (nesf_graph_capture)."""
-        self.graph = api.Graph(self.step_args(), precision)
+        self.graph = api.Graph(self.step_args(), precision, mlp=self.mlp)
         self.graph_precision = precision
         return self.graph
 

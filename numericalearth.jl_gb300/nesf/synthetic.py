@@ -233,6 +233,33 @@ def coupled(seed=1004, nx=2880, ny=1280, lat_s=-80.0, lat_n=80.0, land=0.3, inte
     return st
 
 
+def warm_training_state(seed, nx=720, ny=360, dtype=np.float32, halo=HALO):
+    """Training states of the warm-start network: open ocean (no land, no ice) from 80 S to
+    80 N with the atmosphere on the exchange grid, the 1-degree distributions widened to
+    10 m wind speeds U(0, 40) m/s in a uniform direction and air - sea temperature
+    differences U(-15, +10) K."""
+    rng = np.random.default_rng(seed)
+    L = Layout(nx, ny, halo, halo)
+    c = lonlat(nx, ny, -80.0, 80.0)
+    _, lat = centres(L, c)
+    lat_int = L.interior(lat)
+    sst, S, uo, vo = _ocean_interior(rng, lat_int, nx, ny)
+    at = _atmos_interior(rng, sst, nx, ny)
+    speed = rng.uniform(0.0, 40.0, (ny, nx))
+    angle = rng.uniform(0.0, 2 * np.pi, (ny, nx))
+    at["u"], at["v"] = speed * np.cos(angle), speed * np.sin(angle)
+    at["T"] = sst + rng.uniform(-15.0, 10.0, (ny, nx))
+    RH = rng.uniform(0.6, 0.95, (ny, nx))
+    at["q"] = specific_humidity_from_rh(RH, at["T"], at["p"])
+    f = {"u_atm": at["u"], "v_atm": at["v"], "T_atm": at["T"], "p_atm": at["p"], "q_atm": at["q"],
+         "sw_down": at["sw"], "lw_down": at["lw"], "u_oc": uo, "v_oc": vo, "T_oc": sst - celsius_to_kelvin,
+         "S_oc": S}
+    st = SurfaceState(L, c, dtype)
+    st.fields = {k: pad(v, halo, halo).astype(dtype) for k, v in f.items()}
+    st.fields["inactive"] = np.zeros(L.shape, np.uint8)
+    return st
+
+
 def ao_quarter_land(seed=1001, **kw):
     kw.setdefault("nx", 1440)
     kw.setdefault("ny", 560)
