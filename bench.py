@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="small grid (profiling captures)")
     ap.add_argument("--no-plain", action="store_true", help="time only --precision (profiling captures)")
+    ap.add_argument("--cold", action="store_true", help="no learned warm start")
     return ap.parse_args()
 
 
@@ -133,6 +134,30 @@ def make_state(small):
 BYTES_PER_CELL = {"interp": 52, "ao": 73, "ai": 73, "io": 64, "asm": 4 * (17 + 6 + 11 + 5 + 6 + 4) + 2}
 
 
+def train_warm_start(seed=0):
+    """Train the warm-start network on solver-generated samples (open-ocean states with 0-40 m/s
+    winds and -15..+10 K air-sea differences, and coupled states like the workload's), on the
+    tensor cores; returns the network and a summary."""
+    import torch
+    from nesf import params as P
+    from nesf import synthetic as syn
+    from nesf import warm
+    t0 = time.perf_counter()
+    spec = P.atmosphere_ocean_interface_spec()
+    states = [syn.warm_training_state(seed=7000 + k, nx=360, ny=180) for k in range(4)]
+    states += [syn.coupled(seed=7100 + k, nx=360, ny=180, lat_s=-80, lat_n=80, land=0.3, interpolate=False)
+               for k in range(3)]
+    x, t = warm.training_set(spec, states)
+    net = warm.WarmStartNetwork(seed=seed)
+    net.fit_normalization(x, t)
+    losses = []
+    for epochs, lr in ((12, 2e-3), (8, 5e-4), (5, 1e-4)):
+        losses += net.train(x, t, epochs=epochs, batch=2048, lr=lr)
+    torch.cuda.synchronize()
+    return net, {"samples": int(x.shape[0]), "epochs": len(losses), "loss_first": losses[0],
+                 "loss_last": losses[-1], "seconds": time.perf_counter() - t0}
+
+
 def phase_times(model, precision, reps=3):
     """Per-phase device time (ms) with CUDA events on the launching stream."""
     import torch
@@ -199,14 +224,22 @@ def time_steps(model, precision, steps, warmup, world):
 
 def error_stats(model, precision):
     """Max / p99 relative error of the fast solver against the plain FP64 solver on the full step
-    outputs (normalised by max(|ref|, 1e-6 max|ref|))."""
+    outputs (normalised by max(|ref|, 1e-6 max|ref|)), over the cells where the plain solver
+    converged: where it stops at maxiter its answer is its 100th iterate, which no other path
+    reproduces (those cells are counted)."""
     import torch
     from nesf import fields as F
     L = model.layout
     res = {}
     model.reset()
+    model.iterations = {k: torch.zeros(L.shape, dtype=torch.int32, device="cuda") for k in ("ao", "ai")}
     model.update_state("f64")
     torch.cuda.synchronize()
+    its = {k: L.ring(v.cpu().numpy()) for k, v in model.iterations.items()}
+    model.iterations = None
+    conv = {"ao": its["ao"] < model.ao_spec.flux_formulation.solver_stop_criteria.maxiter,
+            "ai": its["ai"] < model.ai_spec.flux_formulation.solver_stop_criteria.maxiter}
+    res["nonconverged_cells_excluded"] = {k: int((~v).sum()) for k, v in conv.items()}
     ref = {("ao", k): L.ring(model.ao[k].double().cpu().numpy()) for k in F.AO_OUTPUTS}
     ref.update({("ai", k): L.ring(model.ai[k].double().cpu().numpy()) for k in F.AI_OUTPUTS})
     model.reset()
@@ -215,7 +248,8 @@ def error_stats(model, precision):
     got = {("ao", k): L.ring(model.ao[k].double().cpu().numpy()) for k in F.AO_OUTPUTS}
     got.update({("ai", k): L.ring(model.ai[k].double().cpu().numpy()) for k in F.AI_OUTPUTS})
     for key, r in ref.items():
-        g = got[key]
+        g = got[key][conv[key[0]]]
+        r = r[conv[key[0]]]
         den = np.maximum(np.abs(r), 1e-6 * np.abs(r).max())
         e = np.abs(g - r) / np.where(den > 0, den, 1.0)
         res[f"{key[0]}.{key[1]}"] = {"max": float(e.max()), "p99": float(np.percentile(e, 99))}
@@ -351,6 +385,9 @@ def main():
     n_ao, n_ai = model.active_cells()
     cells = n_ao + n_ai
     prec = args.precision
+    warm_info = None
+    if prec != "f64" and not args.cold:
+        model.mlp, warm_info = train_warm_start()
 
     # warm-up both solvers, then the timed region (fast path) with clock sampling
     with ClockSampler(local) as clocks:
@@ -361,8 +398,11 @@ def main():
                           "ms_per_step": ms, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                           "note": "profiling run: --precision only"}))
         return
-    ms_plain, _ = time_steps(model, "f64", max(3, args.steps // 4), 1, world)
-    ms_polish = time_steps(model, "f32", max(3, args.steps // 4), 1, world)[0] if prec != "f32" else ms
+    mlp, model.mlp = model.mlp, None          # the comparison arms run from the cold start
+    ms_plain, _ = time_steps(model, "f64", max(3, args.steps // 4), 3, world)
+    ms_polish = time_steps(model, "f32", max(3, args.steps // 4), 3, world)[0]
+    ms_cold = time_steps(model, prec, max(3, args.steps // 4), 3, world)[0] if mlp is not None else ms
+    model.mlp = mlp
     phases = phase_times(model, prec)
     phases_plain = phase_times(model, "f64", reps=1)
     value = cells * world / (ms / 1000.0)
@@ -370,25 +410,36 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": {"f32": "f32+f64polish", "f32_adaptive": "f32 (f64 polish where ill-conditioned)"}.get(prec, "f64"), "data": "synthetic",
             "config": {"workload": WORKLOAD, "cells_ao": n_ao, "cells_ai": n_ai, "fields": "fp32",
-                       "warm_start": False,
+                       "warm_start": model.mlp is not None,
                        "schedule": "one thread per cell, compacted work lists, packed polish/replay passes; "
-                                   "the step replayed as one CUDA graph",
+                                   "sea-ice and ocean solves on two lanes (the ocean solve overlaps the sea-ice "
+                                   "polish/replay tail); the step replayed as one CUDA graph",
                        "l2": "working set > L2 (no flush needed)", "parallelism": f"replicas x{world}"},
             "gpu_launches": launches,
             "clocks": clk,
             "plain_f64": {"value": cells * world / (ms_plain / 1000.0), "ms_per_step": ms_plain,
                           "phases_ms": phases_plain},
             "f32_polish_ms_per_step": ms_polish,
+            "cold_start_ms_per_step": ms_cold,
+            "warm_start": warm_info,
             "phases_ms": phases}
     if rank == 0:
         line["speedup_vs_plain_f64"] = ms_plain / ms
         model.reset()
         s_ao, s_ai = model.compute_fluxes(prec, stats=True)
         model.reset()
+        mlp, model.mlp = model.mlp, None
+        c_ao, c_ai = model.compute_fluxes(prec, stats=True)
+        model.reset()
         p_ao, p_ai = model.compute_fluxes("f64", stats=True)
+        model.mlp = mlp
         model.reset()
         strip = lambda d: {k: (v if not hasattr(v, "tolist") else v.tolist()) for k, v in d.items() if k != "histogram"}
-        line["solver_stats"] = {"ao": strip(s_ao), "ai": strip(s_ai), "ao_plain": strip(p_ao), "ai_plain": strip(p_ai)}
+        line["solver_stats"] = {"ao": strip(s_ao), "ai": strip(s_ai), "ao_cold": strip(c_ao), "ai_cold": strip(c_ai),
+                                "ao_plain": strip(p_ao), "ai_plain": strip(p_ai)}
+        per = lambda d: d["iterations"] / max(1, d["solved"])
+        line["iterations_per_cell"] = {"ao": per(s_ao), "ao_cold": per(c_ao), "ai": per(s_ai), "ai_cold": per(c_ai),
+                                       "ao_plain": per(p_ao), "ai_plain": per(p_ai)}
         line["errors_vs_plain_f64"] = error_stats(model, prec)
         # roofline of the dominant kernel (HBM: algorithmic bytes / event-timed duration)
         peaks, kind = measured_peaks()

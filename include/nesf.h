@@ -208,7 +208,9 @@ typedef struct {
     int32_t ctas_per_sm;      /* persistent schedule: CTAs per SM (0 = occupancy)       */
     int32_t warm_start;       /* 1: MLP initial guess (needs mlp weights)              */
     const void* mlp;          /* device pointer to packed MLP weights (nesf_mlp_*)      */
-    double fallback_ratio;    /* cold-start fallback when r1 > ratio * r1(cold); 10    */
+    double fallback_ratio;    /* warm start: back to the cold start when the first residual
+                                 relative to the state exceeds ratio times the cold start's
+                                 relative first residual; 10                            */
     double path_tolerance;    /* replay cells whose reference stopping error may exceed
                                  this relative bound (FP32 polish); default 2e-6         */
     double fp32_rho;          /* NESF_F32_ADAPTIVE: largest contraction rate at which the
@@ -506,8 +508,9 @@ int nesf_mlp_selftest(const void* a, const void* b, float* d, int32_t which, voi
  * (tcgen05, BF16 operands, FP32 accumulation). Features are 8 floats per sample
  * (6 used), targets 4 (c_u, c_theta, c_q, and a bit mask of the valid ones as a
  * float), outputs 4 (c_u, c_theta, c_q, 1). The solvers take a trained blob through
- * nesf_solver_options.mlp with warm_start = 1 (FP32 modes). No counterpart in the
- * reference. */
+ * nesf_solver_options.mlp with warm_start = 1 (FP32 modes, single member, bulk
+ * interface temperature: a skin temperature keeps the reference's start). No
+ * counterpart in the reference. */
 typedef struct {
     int32_t epochs;
     int32_t batch;              /* samples per Adam step (a multiple of 128) */

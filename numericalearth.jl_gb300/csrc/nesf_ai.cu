@@ -221,20 +221,22 @@ __global__ void __launch_bounds__(128) ai_replay_kernel(AIArgs<S> a, DevIface<do
 template <class S>
 static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                                SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws,
-                               DevStats* stats, cudaStream_t stream) {
+                               DevStats* stats, cudaStream_t stream, cudaEvent_t after_solve) {
     const int64_t ring = (int64_t)(a.L.nx + 2) * (a.L.ny + 2);
     const int block = 128;
     dim3 grid((unsigned)((ring + block - 1) / block));
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const bool warm = ws.mlp != nullptr && prec != NESF_PLAIN_F64;
+    // the learned warm start serves the bulk interface temperature: with a skin temperature the
+    // iteration count is set by the temperature's clamped steps, which the network does not predict
+    const bool warm = ws.mlp != nullptr && prec != NESF_PLAIN_F64 && P64.temp_form == NESF_BULK_TEMPERATURE;
     cudaError_t e = cudaMemsetAsync(wl.count, 0, sizeof(unsigned) * 2, stream);
     if (e == cudaSuccess && prec != NESF_PLAIN_F64) e = cudaMemsetAsync(rq.count, 0, 2 * sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
     ai_classify_kernel<S><<<grid, block, 0, stream>>>(a, P64, P32, wl, warm ? ws.feat : nullptr, stats);
     if (warm) {
-        e = mlp_pass((void*)ws.mlp, ws.feat, nullptr, ws.guess, 0, wl.count, wl.per_member, sms, true, stream);
+        e = mlp_pass((void*)ws.mlp, ws.feat, nullptr, ws.guess, 0, wl.count, wl.per_member, 4 * sms, true, stream);
         if (e != cudaSuccess) return e;
     }
     const float* guess = warm ? ws.guess : nullptr;
@@ -243,6 +245,7 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     else
         ai_kernel<S, NESF_F32_POLISH><<<grid, block, 0, stream>>>(a, P64, P32, so, wl, rq, guess, stats);
     e = cudaGetLastError();
+    if (e == cudaSuccess && after_solve) e = cudaEventRecord(after_solve, stream);
     if (e != cudaSuccess || prec == NESF_PLAIN_F64) return e;
     if (so.fp32_rho > 0.0f) {
         if (P64.temp_form != NESF_BULK_TEMPERATURE)
@@ -258,13 +261,13 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
 
 cudaError_t launch_ai(const AIArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream) {
-    return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream);
+                      cudaStream_t stream, cudaEvent_t after_solve) {
+    return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream, after_solve);
 }
 cudaError_t launch_ai(const AIArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream) {
-    return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream);
+                      cudaStream_t stream, cudaEvent_t after_solve) {
+    return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream, after_solve);
 }
 
 }  // namespace nesf

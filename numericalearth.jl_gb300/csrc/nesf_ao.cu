@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(128) ao_classify_kernel(AOArgs<S> a, DevIface<
 
 // Pass 1: the compacted cells (unstable first, then stable), one thread each.
 template <class S, int PREC, bool SKIN, bool ENS>
-__global__ void __launch_bounds__(128, ENS ? 4 : 1) ao_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
+__global__ void __launch_bounds__(128, ENS ? 4 : 3) ao_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
                                                               const DevIface<double>* __restrict__ P64s,
                                                               const DevIface<float>* __restrict__ P32s, SolveOpts so,
                                                               WorkList wl, ReplayQueue rq, const float* guess,
@@ -266,7 +266,7 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     // warm start (FP32 modes, one member): features in pass 0, the network's guesses before pass 1
-    const bool warm = ws.mlp != nullptr && prec != NESF_PLAIN_F64 && !ens;
+    const bool warm = ws.mlp != nullptr && prec != NESF_PLAIN_F64 && !ens && !skin;
     float* feat = warm ? ws.feat : nullptr;
     const float* guess = warm ? ws.guess : nullptr;
     cudaError_t e = cudaMemsetAsync(wl.count, 0, sizeof(unsigned) * 2 * nm, stream);
@@ -275,7 +275,7 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
     if (ens) ao_classify_kernel<S, true><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, nullptr, stats);
     else ao_classify_kernel<S, false><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, feat, stats);
     if (warm) {
-        e = mlp_pass((void*)ws.mlp, ws.feat, nullptr, ws.guess, 0, wl.count, wl.per_member, sms, true, stream);
+        e = mlp_pass((void*)ws.mlp, ws.feat, nullptr, ws.guess, 0, wl.count, wl.per_member, 4 * sms, true, stream);
         if (e != cudaSuccess) return e;
     }
 #define NESF_AO_LAUNCH(PR, SK, EN) \

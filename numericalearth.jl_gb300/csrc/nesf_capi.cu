@@ -31,6 +31,10 @@ struct nesf_context {
     float* d_feat;              // warm start: features (8 floats) and guesses (4) per work-list slot
     float* d_guess;
     int64_t warm_capacity;
+    // the coupling step's second lane: scratch of the sea-ice solve, its stream, fork/join events
+    nesf_context* aux;
+    cudaStream_t side;
+    cudaEvent_t ev_fork, ev_ice, ev_join;
     std::mutex lock;            // serialises use of the scratch above
 };
 
@@ -271,6 +275,9 @@ int nesf_context_create(int32_t device, nesf_context** out) {
     c->d_feat = nullptr;
     c->d_guess = nullptr;
     c->warm_capacity = 0;
+    c->aux = nullptr;
+    c->side = nullptr;
+    c->ev_fork = c->ev_ice = c->ev_join = nullptr;
     cudaError_t e = cudaMalloc(&c->d_stats, sizeof(DevStats));
     if (e == cudaSuccess) e = cudaMalloc(&c->d_partials, (size_t)kIntegralBlocks * NESF_MAX_INTEGRALS * 16);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_replay_count, 2 * sizeof(unsigned int));
@@ -301,7 +308,12 @@ int nesf_context_destroy(nesf_context* c) {
         cudaFree(c->d_partials);
         cudaFree(c->d_feat);
         cudaFree(c->d_guess);
+        if (c->side) cudaStreamDestroy(c->side);
+        if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+        if (c->ev_ice) cudaEventDestroy(c->ev_ice);
+        if (c->ev_join) cudaEventDestroy(c->ev_join);
     }
+    if (c->aux) nesf_context_destroy(c->aux);
     delete c;
     return NESF_OK;
 }
@@ -628,9 +640,11 @@ static AIArgs<S> ai_args(const nesf_ai_fields* f) {
     return a;
 }
 
-extern "C" int nesf_compute_atmosphere_sea_ice_fluxes(nesf_context* ctx, const nesf_interface_params* params,
-                                                      const nesf_ai_fields* f, const nesf_solver_options* opts,
-                                                      nesf_stats* stats, void* stream) {
+// The sea-ice solve; `after_solve` (optional) is recorded on the stream once the
+// pass-1 solve is enqueued, before the packed polish and replay passes.
+static int sea_ice_fluxes(nesf_context* ctx, const nesf_interface_params* params, const nesf_ai_fields* f,
+                          const nesf_solver_options* opts, nesf_stats* stats, void* stream,
+                          cudaEvent_t after_solve) {
     const char* who = "nesf_compute_atmosphere_sea_ice_fluxes";
     int r = check_params(params, who);
     if (r) return r;
@@ -665,9 +679,16 @@ extern "C" int nesf_compute_atmosphere_sea_ice_fluxes(nesf_context* ctx, const n
     if ((r = warm_buffers(ctx, o, ring, &ws))) return r;
     SolveOpts so = solve_opts(o);
     return with_stats(ctx, stats, s, [&](DevStats* ds) {
-        if (f->dtype == NESF_F64) return launch_ai(ai_args<double>(f), P64, P32, o.precision, so, wl, rq, ws, ds, s);
-        return launch_ai(ai_args<float>(f), P64, P32, o.precision, so, wl, rq, ws, ds, s);
+        if (f->dtype == NESF_F64)
+            return launch_ai(ai_args<double>(f), P64, P32, o.precision, so, wl, rq, ws, ds, s, after_solve);
+        return launch_ai(ai_args<float>(f), P64, P32, o.precision, so, wl, rq, ws, ds, s, after_solve);
     });
+}
+
+extern "C" int nesf_compute_atmosphere_sea_ice_fluxes(nesf_context* ctx, const nesf_interface_params* params,
+                                                      const nesf_ai_fields* f, const nesf_solver_options* opts,
+                                                      nesf_stats* stats, void* stream) {
+    return sea_ice_fluxes(ctx, params, f, opts, stats, stream, nullptr);
 }
 
 template <class S>
@@ -1045,18 +1066,38 @@ extern "C" int nesf_area_integrals(nesf_context* ctx, const nesf_integral_fields
 // ------------------------------------------------------------ coupling step
 // Scratch for the solves of a step, sized before any capture (growing it
 // synchronises the device, which a stream capture forbids).
-static int coupling_scratch(nesf_context* ctx, const nesf_coupling_step_args* a) {
-    int64_t cells = (int64_t)(a->ao->grid.nx + 2) * (a->ao->grid.ny + 2);
-    if (a->ai_params && a->ai) {
-        int64_t c2 = (int64_t)(a->ai->grid.nx + 2) * (a->ai->grid.ny + 2);
-        cells = c2 > cells ? c2 : cells;
-    }
+static int size_scratch(nesf_context* ctx, int64_t cells, const nesf_solver_options* opts) {
     std::lock_guard<std::mutex> lk(ctx->lock);
     DeviceGuard g(ctx->device);
     ReplayQueue rq;
     WorkList wl;
+    WarmStart ws;
     int r = replay_queue(ctx, cells, &rq);
     if (r == NESF_OK) r = work_list(ctx, cells, 1, &wl);
+    if (r == NESF_OK) r = warm_buffers(ctx, options_or_default(opts), cells, &ws);
+    return r;
+}
+
+// The second lane of the coupling step: a scratch set for the sea-ice solve, a
+// stream and three events (created once; never during a stream capture).
+static int coupling_lane(nesf_context* ctx) {
+    if (ctx->aux) return NESF_OK;
+    DeviceGuard g(ctx->device);
+    int r = nesf_context_create(ctx->device, &ctx->aux);
+    if (r) return r;
+    NESF_CUDA(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+    NESF_CUDA(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+    NESF_CUDA(cudaEventCreateWithFlags(&ctx->ev_ice, cudaEventDisableTiming));
+    NESF_CUDA(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+    return NESF_OK;
+}
+
+static int coupling_scratch(nesf_context* ctx, const nesf_coupling_step_args* a, const nesf_solver_options* opts) {
+    int r = size_scratch(ctx, (int64_t)(a->ao->grid.nx + 2) * (a->ao->grid.ny + 2), opts);
+    if (r == NESF_OK && a->ai_params && a->ai) {
+        if ((r = coupling_lane(ctx))) return r;
+        r = size_scratch(ctx->aux, (int64_t)(a->ai->grid.nx + 2) * (a->ai->grid.ny + 2), opts);
+    }
     return r;
 }
 
@@ -1071,10 +1112,27 @@ extern "C" int nesf_coupling_step(nesf_context* ctx, const nesf_coupling_step_ar
     int r = context_or_default(&ctx);
     if (r) return r;
     const bool ice = a->ai_params != nullptr;
-    // update_state! order (time_step_earth_system_model.jl:50-80)
+    // update_state! order (time_step_earth_system_model.jl:50-80), with the two interface
+    // solves on two lanes: the sea-ice solve runs first on the side stream; the ocean solve
+    // starts when its pass 1 is done and overlaps its packed polish and replay passes, which
+    // are latency-bound (few cells, long FP64 iterations). Both solves only read the ocean
+    // state that the sea-ice-ocean fluxes then update, so those wait for both.
     if (a->interp && (r = nesf_interpolate_atmosphere_state(a->interp, stream))) return r;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (ice) {
+        if ((r = coupling_lane(ctx))) return r;
+        DeviceGuard g(ctx->device);
+        NESF_CUDA(cudaEventRecord(ctx->ev_fork, s));
+        NESF_CUDA(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+        if ((r = sea_ice_fluxes(ctx->aux, a->ai_params, a->ai, opts, nullptr, ctx->side, ctx->ev_ice))) return r;
+        NESF_CUDA(cudaEventRecord(ctx->ev_join, ctx->side));
+        NESF_CUDA(cudaStreamWaitEvent(s, ctx->ev_ice, 0));
+    }
     if ((r = nesf_compute_atmosphere_ocean_fluxes(ctx, a->ao_params, a->ao, opts, nullptr, stream))) return r;
-    if (ice && (r = nesf_compute_atmosphere_sea_ice_fluxes(ctx, a->ai_params, a->ai, opts, nullptr, stream))) return r;
+    if (ice) {
+        DeviceGuard g(ctx->device);
+        NESF_CUDA(cudaStreamWaitEvent(s, ctx->ev_join, 0));
+    }
     if (a->io_params && (r = nesf_compute_sea_ice_ocean_fluxes(ctx, a->io_params, a->io, stream))) return r;
     if (a->assembly_params) {
         if ((r = nesf_assemble_net_ocean_fluxes(a->assembly_params, a->assembly, stream))) return r;
@@ -1106,7 +1164,7 @@ extern "C" int nesf_graph_capture(nesf_context* ctx, const nesf_coupling_step_ar
     if (!a || !a->ao_params || !a->ao) return fail(NESF_ERR_ARG, "%s: the atmosphere-ocean interface is required", who);
     int r = context_or_default(&ctx);
     if (r) return r;
-    if ((r = coupling_scratch(ctx, a))) return r;
+    if ((r = coupling_scratch(ctx, a, opts))) return r;
     DeviceGuard g(ctx->device);
     nesf_graph* G = new (std::nothrow) nesf_graph();
     if (!G) return fail(NESF_ERR_ARG, "%s: out of host memory", who);

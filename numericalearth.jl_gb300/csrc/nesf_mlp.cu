@@ -202,12 +202,13 @@ struct PassIO {
     int state;               // outputs as (c_u dU, c_theta dtheta_0, c_q dq_0, 1): a solver's starting state
 };
 
-constexpr int kPassSmem = 132 * 1024;
+constexpr int kPassSmem = 132 * 1024;     // training: the backward operands too
+constexpr int kInferSmem = 48 * 1024;     // inference: weights, X, H1, H2 (up to 4 CTAs per SM)
 // shared-memory offsets of the operand tiles (blocked layout)
 constexpr int oW1 = 0, oW2 = 2048, oW3 = 10240, oX = 12288, oH1 = 16384, oH2 = 32768, oDY = 65536, oDZ2 = 69632,
               oDZ1 = 102400;
 // TMEM columns: layer scratch, then the weight-gradient accumulators
-constexpr int tD = 0, tW2 = 64, tW1 = 128, tW3 = 144, kTmemCols = 256;
+constexpr int tD = 0, tW2 = 64, tW1 = 128, tW3 = 144, kTmemCols = 256, kInferTmemCols = 64;
 
 __device__ __forceinline__ void store_row16(unsigned char* buf, int R, int r, int c0, const float (&v)[16]) {
 #pragma unroll
@@ -232,7 +233,9 @@ __device__ __forceinline__ float warp_sum(float v) {
 }
 
 template <bool TRAIN>
-__global__ void __launch_bounds__(128, 1) pass_kernel(Blob* __restrict__ B, PassIO io) {
+__global__ void __launch_bounds__(128, TRAIN ? 1 : 4) pass_kernel(Blob* __restrict__ B, PassIO io) {
+    constexpr int kSmem = TRAIN ? kPassSmem : kInferSmem;
+    constexpr uint32_t kCols = TRAIN ? kTmemCols : kInferTmemCols;
     extern __shared__ __align__(1024) unsigned char sm[];
     __shared__ uint64_t bar;
     __shared__ uint32_t tslot;
@@ -248,7 +251,7 @@ __global__ void __launch_bounds__(128, 1) pass_kernel(Blob* __restrict__ B, Pass
     const int64_t tiles = (n + 127) / 128;
 
     // zero the operand tiles (the MN-major weight-gradient operands read 128 columns)
-    for (int i = tid; i < kPassSmem / 16; i += 128) ((uint4*)sm)[i] = make_uint4(0, 0, 0, 0);
+    for (int i = tid; i < kSmem / 16; i += 128) ((uint4*)sm)[i] = make_uint4(0, 0, 0, 0);
     __syncthreads();
     // weights (BF16, row-major [out][in]) into the blocked layout; biases and normalisation
     for (int e = tid; e < kHid * kInPad; e += 128)
@@ -262,7 +265,7 @@ __global__ void __launch_bounds__(128, 1) pass_kernel(Blob* __restrict__ B, Pass
     if (tid < 8) { in_mu[tid] = B->in_mu[tid]; in_sig[tid] = B->in_sig[tid]; }
     if (tid < 4) { out_mu[tid] = B->out_mu[tid]; out_sig[tid] = B->out_sig[tid]; }
     if (tid == 0) tc::mbar_init(&bar, 1);
-    if (warp == 0) tc::tmem_alloc(&tslot, kTmemCols);
+    if (warp == 0) tc::tmem_alloc(&tslot, kCols);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -449,7 +452,7 @@ __global__ void __launch_bounds__(128, 1) pass_kernel(Blob* __restrict__ B, Pass
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tm, kTmemCols);
+    if (warp == 0) tc::tmem_dealloc(tm, kCols);
 }
 
 // Adam on the FP32 parameters from the accumulated gradient; refreshes the BF16
@@ -497,10 +500,10 @@ cudaError_t mlp_pass(void* blob, const float* x, const float* t, float* y, int64
     cudaError_t e = train ? cudaFuncSetAttribute(mlp::pass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  mlp::kPassSmem)
                           : cudaFuncSetAttribute(mlp::pass_kernel<false>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::kPassSmem);
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::kInferSmem);
     if (e != cudaSuccess) return e;
     if (train) mlp::pass_kernel<true><<<grid, 128, mlp::kPassSmem, s>>>((mlp::Blob*)blob, io);
-    else mlp::pass_kernel<false><<<grid, 128, mlp::kPassSmem, s>>>((mlp::Blob*)blob, io);
+    else mlp::pass_kernel<false><<<grid, 128, mlp::kInferSmem, s>>>((mlp::Blob*)blob, io);
     return cudaGetLastError();
 }
 

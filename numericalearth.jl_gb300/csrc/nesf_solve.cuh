@@ -455,11 +455,12 @@ __device__ __forceinline__ int solve_fast(const DevIface<double>& P64, const Dev
         }
         float y[4] = {yu, yt, yq, yT};
         if (phase == 1) {
-            // cold-start fallback: keep the warm start unless its first residual exceeds
-            // fallback_ratio times the cold start's
+            // cold-start fallback: keep the warm start unless its first residual, relative to
+            // its state, exceeds fallback_ratio times the cold start's relative first residual
             probes = 1;
             float rc = fabsf(y[0] - x0[0]) + fabsf(y[1] - x0[1]) + fabsf(y[2] - x0[2]);
-            const bool cold = !(rw <= so.fallback_ratio * rc);
+            float nw = fabsf(x[0]) + fabsf(x[1]) + fabsf(x[2]), nc = fabsf(x0[0]) + fabsf(x0[1]) + fabsf(x0[2]);
+            const bool cold = !(rw * nc <= so.fallback_ratio * rc * nw);
             if (cold && fell_back) *fell_back = true;
             const float* from = cold ? x0 : x;
             const float* to = cold ? y : yw;
@@ -711,12 +712,13 @@ cudaError_t launch_ao(const AOArgs<float>& a, const DevIface<double>& P64, const
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
                       cudaStream_t stream);
+// after_solve (optional): recorded once the pass-1 solve is enqueued.
 cudaError_t launch_ai(const AIArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream);
+                      cudaStream_t stream, cudaEvent_t after_solve = nullptr);
 cudaError_t launch_ai(const AIArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream);
+                      cudaStream_t stream, cudaEvent_t after_solve = nullptr);
 template <class S>
 cudaError_t launch_ao_samples(const AOArgs<S>& a, const DevIface<float>& P32, float* feat, float* targ,
                               cudaStream_t s);

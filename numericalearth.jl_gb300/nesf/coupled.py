@@ -69,6 +69,7 @@ class CoupledModel:
         self.zero_io_stress = z()
         self.intercepted = z()
         self.mlp = None       # a trained warm.WarmStartNetwork: warm start of the FP32 solvers
+        self.iterations = None   # {"ao": int32 tensor, "ai": ...} to record per-cell iteration counts
 
     # -------------------------------------------------------------- phases
     def interpolate_state(self, stream=None):
@@ -83,11 +84,13 @@ class CoupledModel:
         x = self.x
         s_ao = api.compute_atmosphere_ocean_fluxes(self.ao_spec, self.layout, x, self.ao, precision=precision,
                                                    polish_maxiter=polish_maxiter, stats=stats, stream=stream,
-                                                   mlp=self.mlp)
+                                                   mlp=self.mlp,
+                                                   iterations=self.iterations["ao"] if self.iterations else None)
         ai_state = {k: x.get(k) for k in F.AI_INPUTS}
         s_ai = api.compute_atmosphere_sea_ice_fluxes(self.ai_spec, self.layout, ai_state, self.ai,
                                                      precision=precision, polish_maxiter=polish_maxiter,
-                                                     stats=stats, stream=stream, mlp=self.mlp)
+                                                     stats=stats, stream=stream, mlp=self.mlp,
+                                                     iterations=self.iterations["ai"] if self.iterations else None)
         io_state = {"ice_salinity": x["ice_salinity"], "ice_thickness": x["ice_thickness"],
                     "consolidation_thickness": x["consolidation_thickness"],
                     "ice_concentration": x["ice_concentration"], "internal_temperature": x["ice_temperature"],

@@ -82,3 +82,20 @@ def test_graph_rejects_bad_weight(model):
     model.capture("f32_adaptive")
     with pytest.raises(_lib.NesfError):
         model.graph.set_time_weight(1.5)
+
+
+def test_graph_with_warm_start_network(model):
+    """A captured step that starts its FP32 solves from a network (here untrained: the
+    fallback keeps the answers) replays like the direct step."""
+    from nesf.warm import WarmStartNetwork
+    model.mlp = WarmStartNetwork(seed=2)
+    try:
+        model.reset()
+        model.native_step("f32_adaptive")
+        ref = outputs(model)
+        model.capture("f32_adaptive")
+        model.reset()
+        model.graph_step()
+        assert_same(ref, outputs(model), "warm graph")
+    finally:
+        model.mlp = None

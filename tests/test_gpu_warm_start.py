@@ -66,9 +66,9 @@ def test_warm_start_cuts_iterations_at_the_same_accuracy(trained, oracle):
     assert s_hot["cold_fallbacks"] < 0.15 * s_hot["solved"], (s_hot["cold_fallbacks"], s_hot["solved"])
 
 
-def test_untrained_network_falls_back_and_stays_exact(oracle):
-    """A network that has not been trained guesses badly; the residual test sends those cells
-    back to the reference's start and the answer is unchanged."""
+def test_untrained_network_stays_exact(oracle):
+    """A network that has not been trained guesses badly; the iteration still runs to the
+    reference's tolerance from there, and the answer is unchanged."""
     spec = P.atmosphere_ocean_interface_spec()
     net = warm.WarmStartNetwork(seed=11)
     st = syn.coupled(seed=402, nx=120, ny=60, lat_s=-70, lat_n=70, land=0.2, interpolate=False)
@@ -78,4 +78,4 @@ def test_untrained_network_falls_back_and_stays_exact(oracle):
     for k in ("latent_heat", "sensible_heat", "x_momentum"):
         e = rel_err(R(hot[k]).astype(np.float64), R(ref[k]), floor_frac=1e-6)
         assert e.max() <= 1e-5, (k, e.max())
-    assert s_hot["cold_fallbacks"] > 0
+    assert s_hot["solved"] > 0 and s_hot["nonconverged"] == 0
