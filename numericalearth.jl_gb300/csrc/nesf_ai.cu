@@ -66,6 +66,35 @@ __device__ __forceinline__ int ai_plain(const DevIface<double>& P, const CellCon
     return it;
 }
 
+// The zero interface state of an ice-free or land cell through the flux epilogue
+// (atmosphere_sea_ice_fluxes.jl:141-142, 154-184) without its FP64 arithmetic: with
+// u* = theta* = q* = 0 every flux is a signed zero, -0 for the heat and vapour fluxes
+// (-rho u* ...) and the sign of -du for tau_x (likewise tau_y), +0 when dU = 0, given
+// a positive finite air density; other cells take the full epilogue.
+template <class S>
+__device__ __forceinline__ void ai_store_zero(const DevIface<double>& P, const DevIface<float>& Pf,
+                                              const AIArgs<S>& a, int64_t k) {
+    double ua = ld(a.ua, k), va = ld(a.va, k);
+    double Ti = ld(a.To, k) + P.off_int;
+    float rho = air_density(Pf, ldf(a.Ta, k), ldf(a.pa, k), ldf(a.qa, k));
+    if (!(rho > 0.0f && rho < 3.0e38f) || ua != ua || va != va) {
+        CellConst<double> c;
+        double aleph, Ts0;
+        bool land;
+        ai_load(P, a, k, c, aleph, Ts0, land);
+        ai_store(P, a, k, c, 0.0, 0.0, 0.0, c.Ti, 0);
+        return;
+    }
+    const bool calm = ua == 0.0 && va == 0.0;
+    st(a.Qv, k, -0.0);
+    st(a.QT, k, -0.0);
+    st(a.Jv, k, -0.0);
+    st(a.tx, k, calm ? 0.0 : copysign(0.0, -ua));
+    st(a.ty, k, calm ? 0.0 : copysign(0.0, -va));
+    a.Ts[k] = (S)(Ti - P.off_ifc);
+    if (a.iters) a.iters[k] = 0;
+}
+
 // Pass 0: ice-free and land cells get the zero state with the ocean temperature
 // (atmosphere_sea_ice_fluxes.jl:141-142); the others go to the work list.
 template <class S>
@@ -78,25 +107,27 @@ __global__ void __launch_bounds__(128) ai_classify_kernel(AIArgs<S> a, DevIface<
     int i = in ? (int)(r % nxr) : 0, j = in ? (int)(r / nxr) : 0;
     int64_t k = a.L.at(i, j);
     bool skip = false, active = false, stable = false;
-    CellConst<double> c;
-    double aleph = 0, Ts0 = 0;
+    float Ta = 0.0f, pa = 0.0f, qa = 0.0f, Ts0 = 0.0f;
     if (in) {
-        bool land;
-        ai_load(P, a, k, c, aleph, Ts0, land);
+        bool land = a.inactive ? a.inactive[k] != 0 : false;
         bool needs = P.stop_kind == NESF_STOP_CONVERGENCE;
-        skip = (needs && land) || aleph == 0;
+        skip = (needs && land) || ld(a.aleph, k) == 0.0;
         active = !skip;
-        if (active) stable = stable_class(Pf, (float)c.Ta, (float)c.pa, (float)c.qa, (float)Ts0);
+        if (active) {
+            Ta = ldf(a.Ta, k); pa = ldf(a.pa, k); qa = ldf(a.qa, k);
+            Ts0 = (float)(ld(a.Ts, k) + P.off_ifc);
+            stable = stable_class(Pf, Ta, pa, qa, Ts0);
+        }
     }
     int64_t slot = worklist_push(wl, 0, active, stable, (uint32_t)r);
     if (feat && slot >= 0) {
         // warm-start features (FP32) from the state before the iteration
-        float tha = (float)c.tha;
-        mlp::store_features(feat, slot, mlp::warm_features(Pf, (float)c.dU2, tha, (float)Ts0, (float)c.qa,
-                                                           (float)c.pa));
+        float ua = ldf(a.ua, k), va = ldf(a.va, k);
+        float tha = surface_atmosphere_temperature(Pf, Ta, qa);
+        mlp::store_features(feat, slot, mlp::warm_features(Pf, ua * ua + va * va, tha, Ts0, qa, pa));
     }
     if (skip) {
-        ai_store(P, a, k, c, 0.0, 0.0, 0.0, c.Ti, 0);
+        ai_store_zero(P, Pf, a, k);
         if (stats) stats_add(stats, true, false, 0, false, false, 0, false, false);
     }
 }
