@@ -54,6 +54,51 @@ __device__ __forceinline__ void ai_store(const DevIface<double>& P, const AIArgs
     if (a.iters) a.iters[k] = iters;
 }
 
+// The adaptive pass-1 prologue: ai_load's quantities in FP32, FP64 only where
+// differences cancel (the anchors, or theta_a - T_s and q_a - q_s).
+template <class S, bool SKIN>
+__device__ __forceinline__ void ai_load_fast(const DevIface<double>& P, const DevIface<float>& Pf, const AIArgs<S>& a,
+                                             int64_t k, Fast32& f) {
+    CellConst<float>& c = f.c;
+    c.ua = ldf(a.ua, k); c.va = ldf(a.va, k); c.Ta = ldf(a.Ta, k); c.pa = ldf(a.pa, k); c.qa = ldf(a.qa, k);
+    c.du = c.ua; c.dv = c.va;            // sea-ice velocities are not used (:97-98)
+    c.dU2 = c.du * c.du + c.dv * c.dv;
+    const double Ta = ld(a.Ta, k), qa = ld(a.qa, k), lift = lift_temperature(P, qa);
+    f.tha = Ta + lift;
+    c.tha = (float)f.tha;
+    c.rho_a = air_density(Pf, c.Ta, c.pa, c.qa);
+    c.cp_a = cp_m(Pf, c.qa);
+    c.L_s = latent_heat_sublim(Pf, c.Ta);
+    f.Ts0 = ld(a.Ts, k) + P.off_ifc;
+    if (SKIN) {
+        c.hi = ldf(a.hi, k);
+        c.hs = a.hs ? ldf(a.hs, k) : 0.0f;
+        c.hc = ldf(a.hc, k);
+        c.kappa = -1.0f;
+        f.anc = skin_anchor(P, f.tha, ld(a.To, k) + P.off_int, ld(a.So, k), qa, ld(a.pa, k), ldz(a.sw, k),
+                            ldz(a.lw, k));
+    } else {
+        fast_surface(P, Pf, Ta, qa, ld(a.pa, k), lift, f.Ts0, f.s);
+    }
+}
+
+// The adaptive pass-1 epilogue (ai_store's fluxes in FP32; the interface
+// temperature in FP64).
+template <class S>
+__device__ __forceinline__ void ai_store_fast(const DevIface<double>& P, const AIArgs<S>& a, int64_t k,
+                                              const Fast32& f, float us, float ts, float qst, double Ts, int iters) {
+    float tx, ty;
+    stress_fast(us, f.c.du, f.c.dv, tx, ty);
+    const float rho = f.c.rho_a;
+    st(a.Qv, k, -rho * us * qst * f.c.L_s);
+    st(a.QT, k, -rho * f.c.cp_a * us * ts);
+    st(a.Jv, k, -rho * us * qst);
+    st(a.tx, k, rho * tx);
+    st(a.ty, k, rho * ty);
+    a.Ts[k] = (S)(Ts - P.off_ifc);
+    if (a.iters) a.iters[k] = iters;
+}
+
 template <bool SKIN>
 __device__ __forceinline__ int ai_plain(const DevIface<double>& P, const CellConst<double>& c, double Ts0,
                                         double& us, double& ts, double& qst, double& Ts, bool& nonconv) {
@@ -133,7 +178,7 @@ __global__ void __launch_bounds__(128) ai_classify_kernel(AIArgs<S> a, DevIface<
 }
 
 // Pass 1: the compacted ice cells, one thread each.
-template <class S, int PREC>
+template <class S, int PREC, bool SKIN>
 __global__ void __launch_bounds__(128) ai_kernel(AIArgs<S> a, DevIface<double> P64, DevIface<float> P32,
                                                  SolveOpts so, WorkList wl, ReplayQueue rq, const float* guess,
                                                  DevStats* stats) {
@@ -146,36 +191,58 @@ __global__ void __launch_bounds__(128) ai_kernel(AIArgs<S> a, DevIface<double> P
     int i = (int)(r % nxr), j = (int)(r / nxr);
     int64_t k = a.L.at(i, j);
     const DevIface<double>& P = P64;
+    bool needs = P.stop_kind == NESF_STOP_CONVERGENCE;
+    if constexpr (PREC == NESF_F32_ADAPTIVE) {
+        // FP32 sweep kept when quiet and well contracting; the other cells go to the
+        // packed polish pass or, with fixed iteration counts, to the FP64 replay
+        if (!needs) {
+            replay_push(rq, true, (uint32_t)r);
+            polish_push(rq, false, (uint32_t)r);
+            if (stats) stats_add(stats, true, false, 0, false, false, 0, true, false);
+            return;
+        }
+        Fast32 f;
+        ai_load_fast<S, SKIN>(P, P32, a, k, f);
+        float x[4] = {1e-4f, 1e-4f, 1e-4f, SKIN ? (float)(f.Ts0 - f.tha) : 0.0f};   // :127
+        float J[SKIN ? 4 : 3][SKIN ? 4 : 3];
+        float rho;
+        int f32it = 0, reason = -1;
+        bool fallback = false;
+        int outcome = sweep_fp32<SKIN, true>(P32, f.c, f.s, f.anc, x, so, f32it, reason, J, rho, warm, &fallback);
+        replay_push(rq, outcome == FAST_REPLAY, (uint32_t)r);
+        polish_push(rq, outcome == FAST_POLISH, (uint32_t)r);
+        if (outcome != FAST_SOLVED) {
+            if (stats) {
+                stats_add(stats, true, false, 0, false, false, 0, outcome == FAST_REPLAY, fallback);
+                if (outcome == FAST_REPLAY) stats_replay_reason(stats, reason);
+            }
+            return;
+        }
+        ai_store_fast(P, a, k, f, x[0], x[1], x[2], SKIN ? f.tha + (double)x[3] : f.Ts0, f32it);
+        if (stats) stats_add(stats, true, true, f32it, false, false, 0, false, fallback);
+        return;
+    }
     CellConst<double> c;
     double aleph, Ts0;
     bool land;
     ai_load(P, a, k, c, aleph, Ts0, land);
-    bool skin = P.temp_form != NESF_BULK_TEMPERATURE;
-    bool needs = P.stop_kind == NESF_STOP_CONVERGENCE;
     double us = 0, ts = 0, qst = 0, Ts = c.Ti;
     int iters = 0, f64it = 0;
     bool nonconv = false, fallback = false;
     int outcome = FAST_SOLVED, reason = -1;
     if (PREC == NESF_PLAIN_F64 || !needs) {
-        iters = skin ? ai_plain<true>(P, c, Ts0, us, ts, qst, Ts, nonconv)
-                     : ai_plain<false>(P, c, Ts0, us, ts, qst, Ts, nonconv);
+        iters = ai_plain<SKIN>(P, c, Ts0, us, ts, qst, Ts, nonconv);
     } else {
         SurfaceConst<double> s{};
-        if (skin) s.Ts = Ts0;   // solve_fast reads only T_s of a skin state
+        if (SKIN) s.Ts = Ts0;   // solve_fast reads only T_s of a skin state
         else surface_const(P, c, Ts0, surface_specific_humidity(P, c.pa, Ts0), s);
         us = ts = qst = 1e-4;
         int f32it;
-        const bool accept32 = so.fp32_rho > 0.0f;
-        outcome = skin ? solve_fast<true>(P, P32, c, s, us, ts, qst, so, accept32, f32it, f64it, reason, warm, &fallback)
-                       : solve_fast<false>(P, P32, c, s, us, ts, qst, so, accept32, f32it, f64it, reason, warm,
-                                           &fallback);
+        outcome = solve_fast<SKIN>(P, P32, c, s, us, ts, qst, so, f32it, f64it, reason, warm, &fallback);
         iters = f32it + f64it;
         Ts = s.Ts;
     }
-    if (PREC != NESF_PLAIN_F64) {
-        replay_push(rq, outcome == FAST_REPLAY, (uint32_t)r);
-        polish_push(rq, outcome == FAST_POLISH, (uint32_t)r);
-    }
+    if (PREC != NESF_PLAIN_F64) replay_push(rq, outcome == FAST_REPLAY, (uint32_t)r);
     if (outcome != FAST_SOLVED) {
         if (stats) {
             stats_add(stats, true, false, 0, false, false, 0, outcome == FAST_REPLAY, fallback);
@@ -210,7 +277,7 @@ __global__ void __launch_bounds__(128) ai_polish_kernel(AIArgs<S> a, DevIface<do
         else surface_const(P, c, Ts0, surface_specific_humidity(P, c.pa, Ts0), s);
         double us = 1e-4, ts = 1e-4, qst = 1e-4;
         int f32it, f64it, reason = -1;
-        int outcome = solve_fast<SKIN>(P, P32, c, s, us, ts, qst, so, false, f32it, f64it, reason);
+        int outcome = solve_fast<SKIN>(P, P32, c, s, us, ts, qst, so, f32it, f64it, reason);
         replay_push(rq, outcome == FAST_REPLAY, id);
         if (outcome == FAST_REPLAY) {
             if (stats) {
@@ -271,15 +338,22 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
         if (e != cudaSuccess) return e;
     }
     const float* guess = warm ? ws.guess : nullptr;
-    if (prec == NESF_PLAIN_F64)
-        ai_kernel<S, NESF_PLAIN_F64><<<grid, block, 0, stream>>>(a, P64, P32, so, wl, rq, nullptr, stats);
-    else
-        ai_kernel<S, NESF_F32_POLISH><<<grid, block, 0, stream>>>(a, P64, P32, so, wl, rq, guess, stats);
+    // the adaptive pass 1 keeps FP32 results up to fp32_rho; fp32_rho = 0 keeps none: the
+    // POLISH pass 1, which polishes every cell in place
+    const bool adaptive = prec == NESF_F32_ADAPTIVE && so.fp32_rho > 0.0f;
+    const bool skin = P64.temp_form != NESF_BULK_TEMPERATURE;
+#define NESF_AI_LAUNCH(PR, SK, G) ai_kernel<S, PR, SK><<<grid, block, 0, stream>>>(a, P64, P32, so, wl, rq, G, stats)
+#define NESF_AI_SKIN(PR, G) do { if (skin) NESF_AI_LAUNCH(PR, true, G); else NESF_AI_LAUNCH(PR, false, G); } while (0)
+    if (prec == NESF_PLAIN_F64) NESF_AI_SKIN(NESF_PLAIN_F64, nullptr);
+    else if (adaptive) NESF_AI_SKIN(NESF_F32_ADAPTIVE, guess);
+    else NESF_AI_SKIN(NESF_F32_POLISH, guess);
+#undef NESF_AI_SKIN
+#undef NESF_AI_LAUNCH
     e = cudaGetLastError();
     if (e == cudaSuccess && after_solve) e = cudaEventRecord(after_solve, stream);
     if (e != cudaSuccess || prec == NESF_PLAIN_F64) return e;
-    if (so.fp32_rho > 0.0f) {
-        if (P64.temp_form != NESF_BULK_TEMPERATURE)
+    if (adaptive) {
+        if (skin)
             ai_polish_kernel<S, true><<<(unsigned)sms * 4, block, 0, stream>>>(a, P64, P32, so, rq, stats);
         else
             ai_polish_kernel<S, false><<<(unsigned)sms * 4, block, 0, stream>>>(a, P64, P32, so, rq, stats);

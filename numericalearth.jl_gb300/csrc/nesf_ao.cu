@@ -71,6 +71,58 @@ __device__ __forceinline__ void ao_store(const DevIface<double>& P, const AOArgs
     if (a.iters) a.iters[k] = iters;
 }
 
+// The adaptive pass-1 prologue: the cell's FP32 inputs with FP64 only where
+// differences cancel (ao_load's quantities, rounded to FP32).
+template <class S, bool SKIN>
+__device__ __forceinline__ void ao_load_fast(const DevIface<double>& P, const DevIface<float>& Pf, const AOArgs<S>& a,
+                                             int64_t k, Fast32& f) {
+    CellConst<float>& c = f.c;
+    c.ua = ldf(a.ua, k); c.va = ldf(a.va, k); c.Ta = ldf(a.Ta, k); c.pa = ldf(a.pa, k); c.qa = ldf(a.qa, k);
+    if (Pf.vel_form == NESF_WIND_VELOCITY) { c.du = c.ua; c.dv = c.va; }
+    else {   // in FP64: u_a - u_i cancels where the air moves with the water
+        c.du = (float)(ld(a.ua, k) - (ld(a.uo, k) + ld(a.uo, k + 1)) / 2);
+        c.dv = (float)(ld(a.va, k) - (ld(a.vo, k) + ld(a.vo, k + a.L.sj)) / 2);
+    }
+    c.dU2 = c.du * c.du + c.dv * c.dv;
+    const double Ta = ld(a.Ta, k), qa = ld(a.qa, k), lift = lift_temperature(P, qa);
+    f.tha = Ta + lift;
+    c.tha = (float)f.tha;
+    f.Ts0 = ld(a.To, k) + P.off_int;
+    if (SKIN) {
+        c.rho_a = air_density(Pf, c.Ta, c.pa, c.qa);
+        c.cp_a = cp_m(Pf, c.qa);
+        c.L_s = latent_heat_sublim(Pf, c.Ta);
+        c.kappa = a.kappa ? ldf(a.kappa, k) : -1.0f;
+        c.hi = c.hs = c.hc = 0.0f;
+        f.anc = skin_anchor(P, f.tha, f.Ts0, ld(a.So, k), qa, ld(a.pa, k), ldz(a.sw, k), ldz(a.lw, k));
+    } else {
+        fast_surface(P, Pf, Ta, qa, ld(a.pa, k), lift, f.Ts0, f.s);
+    }
+}
+
+// The adaptive pass-1 epilogue (ao_store's fluxes in FP32; the interface
+// temperature in FP64).
+template <class S>
+__device__ __forceinline__ void ao_store_fast(const DevIface<double>& P, const DevIface<float>& Pf,
+                                              const AOArgs<S>& a, int64_t k, const Fast32& f, float us, float ts,
+                                              float qst, double Ts, int iters) {
+    float tx, ty;
+    stress_fast(us, f.c.du, f.c.dv, tx, ty);
+    float rho = air_density(Pf, f.c.Ta, f.c.pa, f.c.qa);
+    float cp = cp_m(Pf, f.c.qa);
+    float Lv = latent_heat_vapor(Pf, f.c.Ta);
+    st(a.Qv, k, -rho * Lv * us * qst);
+    st(a.QT, k, -rho * cp * us * ts);
+    st(a.Jv, k, -rho * us * qst);
+    st(a.tx, k, rho * tx);
+    st(a.ty, k, rho * ty);
+    st(a.Ts, k, Ts - P.off_ifc);
+    st(a.us, k, us);
+    st(a.ts, k, ts);
+    st(a.qs, k, qst);
+    if (a.iters) a.iters[k] = iters;
+}
+
 // Warm-start features of a cell in FP32 (the training samples use the same).
 template <class S>
 __device__ __forceinline__ mlp::Features ao_features(const DevIface<float>& P, const AOArgs<S>& a, int64_t k) {
@@ -146,13 +198,44 @@ __global__ void __launch_bounds__(128, ENS ? 4 : 3) ao_kernel(AOArgs<S> a, DevIf
     if (r < 0) return;
     int i = (int)(r % nxr), j = (int)(r / nxr);
     int64_t k = a.L.at(i, j) + (int64_t)m * a.member_stride;
+    const uint32_t id = (uint32_t)(m * ring + r);
+    float xw[3];
+    const float* warm = mlp::guess_at(guess, worklist_slot(wl, m, w), xw);
+    bool needs = Pd.stop_kind == NESF_STOP_CONVERGENCE;
+    if constexpr (PREC == NESF_F32_ADAPTIVE) {
+        // FP32 sweep kept when quiet and well contracting; the other cells go to the
+        // packed polish pass or, with fixed iteration counts, to the FP64 replay
+        if (!needs) {
+            replay_push(rq, true, id);
+            polish_push(rq, false, id);
+            if (stats) stats_add(stats, true, false, 0, false, false, 0, true, false);
+            return;
+        }
+        Fast32 f;
+        ao_load_fast<S, SKIN>(Pd, Pf, a, k, f);
+        float x[4] = {1e-4f, 1e-4f, 1e-4f, SKIN ? f.anc.dTi : 0.0f};   // atmosphere_ocean_fluxes.jl:132
+        float J[SKIN ? 4 : 3][SKIN ? 4 : 3];
+        float rho;
+        int f32it = 0, reason = -1;
+        bool fallback = false;
+        int outcome = sweep_fp32<SKIN, true>(Pf, f.c, f.s, f.anc, x, so, f32it, reason, J, rho, warm, &fallback);
+        replay_push(rq, outcome == FAST_REPLAY, id);
+        polish_push(rq, outcome == FAST_POLISH, id);
+        if (outcome != FAST_SOLVED) {
+            if (stats) {
+                stats_add(stats, true, false, 0, false, false, 0, outcome == FAST_REPLAY, fallback);
+                if (outcome == FAST_REPLAY) stats_replay_reason(stats, reason);
+            }
+            return;
+        }
+        ao_store_fast(Pd, Pf, a, k, f, x[0], x[1], x[2], SKIN ? f.tha + (double)x[3] : f.Ts0, f32it);
+        if (stats) stats_add(stats, true, true, f32it, false, false, 0, false, fallback);
+        return;
+    }
     CellConst<double> c;
     bool land;
     ao_load(Pd, a, k, SKIN, c, land);
-    float xw[3];
-    const float* warm = mlp::guess_at(guess, worklist_slot(wl, m, w), xw);
     double us = 1e-4, ts = 1e-4, qst = 1e-4;   // initial guess (atmosphere_ocean_fluxes.jl:132)
-    bool needs = Pd.stop_kind == NESF_STOP_CONVERGENCE;
     SurfaceConst<double> s{};
     if (SKIN && PREC != NESF_PLAIN_F64 && needs) s.Ts = c.Ti;   // solve_fast reads only T_s of a skin state
     else surface_const(Pd, c, c.Ti, surface_specific_humidity(Pd, c.pa, c.Ti), s);
@@ -163,15 +246,10 @@ __global__ void __launch_bounds__(128, ENS ? 4 : 3) ao_kernel(AOArgs<S> a, DevIf
         iters = solve_plain<SKIN>(Pd, c, s, us, ts, qst, nonconv);
     } else {
         int f32it;
-        outcome = solve_fast<SKIN>(Pd, Pf, c, s, us, ts, qst, so, so.fp32_rho > 0.0f, f32it, f64it, reason, warm,
-                                   &fallback);
+        outcome = solve_fast<SKIN>(Pd, Pf, c, s, us, ts, qst, so, f32it, f64it, reason, warm, &fallback);
         iters = f32it + f64it;
     }
-    const uint32_t id = (uint32_t)(m * ring + r);
-    if (PREC != NESF_PLAIN_F64) {
-        replay_push(rq, outcome == FAST_REPLAY, id);
-        polish_push(rq, outcome == FAST_POLISH, id);
-    }
+    if (PREC != NESF_PLAIN_F64) replay_push(rq, outcome == FAST_REPLAY, id);
     if (outcome != FAST_SOLVED) {
         if (stats) {
             stats_add(stats, true, false, 0, false, false, 0, outcome == FAST_REPLAY, fallback);
@@ -209,7 +287,7 @@ __global__ void __launch_bounds__(128) ao_polish_kernel(AOArgs<S> a, DevIface<do
         if (SKIN) s.Ts = c.Ti;
         else surface_const(P, c, c.Ti, surface_specific_humidity(P, c.pa, c.Ti), s);
         int f32it, f64it, reason = -1;
-        int outcome = solve_fast<SKIN>(P, Pf, c, s, us, ts, qst, so, false, f32it, f64it, reason);
+        int outcome = solve_fast<SKIN>(P, Pf, c, s, us, ts, qst, so, f32it, f64it, reason);
         replay_push(rq, outcome == FAST_REPLAY, id);
         if (outcome == FAST_REPLAY) {
             if (stats) {
@@ -284,7 +362,11 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
     do { if (ens) NESF_AO_LAUNCH(PR, SK, true); else NESF_AO_LAUNCH(PR, SK, false); } while (0)
 #define NESF_AO_SKIN(PR) \
     do { if (skin) NESF_AO_ENS(PR, true); else NESF_AO_ENS(PR, false); } while (0)
+    // the adaptive pass 1 keeps FP32 results up to fp32_rho; fp32_rho = 0 keeps none: the
+    // POLISH pass 1, which polishes every cell in place
+    const bool adaptive = prec == NESF_F32_ADAPTIVE && so.fp32_rho > 0.0f;
     if (prec == NESF_PLAIN_F64) NESF_AO_SKIN(NESF_PLAIN_F64);
+    else if (adaptive) NESF_AO_SKIN(NESF_F32_ADAPTIVE);
     else NESF_AO_SKIN(NESF_F32_POLISH);
 #undef NESF_AO_SKIN
 #undef NESF_AO_ENS
@@ -294,7 +376,7 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
     // passes 1b and 2: enough resident blocks to sweep the queues (grid-stride)
     unsigned g2 = (unsigned)sms * 4;
     const DevIface<double>* pm = ens ? P64s : nullptr;
-    if (so.fp32_rho > 0.0f) {
+    if (adaptive) {
         if (skin) ao_polish_kernel<S, true><<<g2, threads, 0, stream>>>(a, P64, P32, pm, ens ? P32s : nullptr, so, rq, stats);
         else ao_polish_kernel<S, false><<<g2, threads, 0, stream>>>(a, P64, P32, pm, ens ? P32s : nullptr, so, rq, stats);
         e = cudaGetLastError();

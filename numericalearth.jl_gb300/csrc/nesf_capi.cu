@@ -704,8 +704,10 @@ static IOArgs<S> io_args(const nesf_io_fields* f) {
     return a;
 }
 
-extern "C" int nesf_compute_sea_ice_ocean_fluxes(nesf_context* ctx, const nesf_io_params* p, const nesf_io_fields* f,
-                                                 void* stream) {
+// part: 0 fluxes + frazil adjustment of the ocean temperature, 1 the fluxes alone
+// (the ocean state read only), 2 the adjustment alone (launch_io).
+static int sea_ice_ocean(nesf_context* ctx, const nesf_io_params* p, const nesf_io_fields* f, void* stream,
+                         int part) {
     const char* who = "nesf_compute_sea_ice_ocean_fluxes";
     if (!p || !f) return fail(NESF_ERR_ARG, "%s: null argument", who);
     int r = check_grid(f->grid, 0, who);
@@ -723,9 +725,15 @@ extern "C" int nesf_compute_sea_ice_ocean_fluxes(nesf_context* ctx, const nesf_i
         return fail(NESF_ERR_ARG, "%s: conductive three-equation flux needs internal_temperature", who);
     DeviceGuard g(ctx ? ctx->device : 0);
     cudaStream_t s = (cudaStream_t)stream;
-    cudaError_t e = f->dtype == NESF_F64 ? launch_io(io_args<double>(f), *p, s) : launch_io(io_args<float>(f), *p, s);
+    cudaError_t e = f->dtype == NESF_F64 ? launch_io(io_args<double>(f), *p, s, part)
+                                         : launch_io(io_args<float>(f), *p, s, part);
     if (e != cudaSuccess) return cuda_fail(e, who);
     return NESF_OK;
+}
+
+extern "C" int nesf_compute_sea_ice_ocean_fluxes(nesf_context* ctx, const nesf_io_params* p, const nesf_io_fields* f,
+                                                 void* stream) {
+    return sea_ice_ocean(ctx, p, f, stream, 0);
 }
 
 extern "C" int nesf_compute_fractional_indices(const nesf_grid* g, const nesf_exchange_coords* c,
@@ -1115,10 +1123,13 @@ extern "C" int nesf_coupling_step(nesf_context* ctx, const nesf_coupling_step_ar
     // update_state! order (time_step_earth_system_model.jl:50-80), with the two interface
     // solves on two lanes: the sea-ice solve runs first on the side stream; the ocean solve
     // starts when its pass 1 is done and overlaps its packed polish and replay passes, which
-    // are latency-bound (few cells, long FP64 iterations). Both solves only read the ocean
-    // state that the sea-ice-ocean fluxes then update, so those wait for both.
+    // are latency-bound (few cells, long FP64 iterations). The sea-ice-ocean fluxes read
+    // only the ocean and ice state, so they run on the main lane beside the sea-ice pass 1;
+    // their frazil adjustment of the ocean temperature, which both solves read, waits for
+    // both (the same state as update_state!'s order).
     if (a->interp && (r = nesf_interpolate_atmosphere_state(a->interp, stream))) return r;
     cudaStream_t s = (cudaStream_t)stream;
+    const bool io_split = ice && a->io_params;
     if (ice) {
         if ((r = coupling_lane(ctx))) return r;
         DeviceGuard g(ctx->device);
@@ -1126,6 +1137,7 @@ extern "C" int nesf_coupling_step(nesf_context* ctx, const nesf_coupling_step_ar
         NESF_CUDA(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
         if ((r = sea_ice_fluxes(ctx->aux, a->ai_params, a->ai, opts, nullptr, ctx->side, ctx->ev_ice))) return r;
         NESF_CUDA(cudaEventRecord(ctx->ev_join, ctx->side));
+        if (io_split && (r = sea_ice_ocean(ctx, a->io_params, a->io, stream, 1))) return r;
         NESF_CUDA(cudaStreamWaitEvent(s, ctx->ev_ice, 0));
     }
     if ((r = nesf_compute_atmosphere_ocean_fluxes(ctx, a->ao_params, a->ao, opts, nullptr, stream))) return r;
@@ -1133,7 +1145,7 @@ extern "C" int nesf_coupling_step(nesf_context* ctx, const nesf_coupling_step_ar
         DeviceGuard g(ctx->device);
         NESF_CUDA(cudaStreamWaitEvent(s, ctx->ev_join, 0));
     }
-    if (a->io_params && (r = nesf_compute_sea_ice_ocean_fluxes(ctx, a->io_params, a->io, stream))) return r;
+    if (a->io_params && (r = sea_ice_ocean(ctx, a->io_params, a->io, stream, io_split ? 2 : 0))) return r;
     if (a->assembly_params) {
         if ((r = nesf_assemble_net_ocean_fluxes(a->assembly_params, a->assembly, stream))) return r;
         if (ice && (r = nesf_assemble_net_sea_ice_fluxes(a->assembly_params, a->assembly, stream))) return r;

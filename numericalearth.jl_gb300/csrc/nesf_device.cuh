@@ -84,6 +84,9 @@ template <class R> struct DevIface {
     R max_dT, k_ice, k_snow, kap_diff, del_diff;
     R g, h, hbl, off_int, off_ifc;
     R sigma, alb, emis, Tfw, slope, rho_i, c_i;
+    // ln e_sat(T) = ln p_tr + esA ln(T / T_tr) + esK (1 / T_tr - 1 / T) for the interface's
+    // phase: esA = (cp_v - cp_c) / R_v, esK = (L_0 - (cp_v - cp_c) T_0) / R_v; inv_Ttr = 1 / T_tr
+    R esA, esK, inv_Ttr;
 };
 
 // ------------------------------------------------------------- thermodynamics
@@ -97,6 +100,15 @@ __device__ __forceinline__ R esat(const DevIface<R>& P, R T, int phase) {
     R dcp = P.cpv - cpc;
     return P.ptr * M<R>::pow(T / P.Ttr, dcp / P.Rv) *
            M<R>::exp((LH0 - dcp * P.T0) / P.Rv * (R(1) / P.Ttr - R(1) / T));
+}
+
+// The same saturation vapour pressure as one exponential, p_tr exp(esA ln(T / T_tr) +
+// esK (T - T_tr) / (T_tr T)): an exp and a log in place of pow and exp, equal to esat
+// within a few ulps. The FP32 solvers' FP64 anchors use it; the FP64 iterations that
+// follow the reference's operation order use esat.
+template <class R>
+__device__ __forceinline__ R esat_exp(const DevIface<R>& P, R T) {
+    return P.ptr * M<R>::exp(P.esA * M<R>::log(T * P.inv_Ttr) + P.esK * ((T - P.Ttr) * P.inv_Ttr) / T);
 }
 
 template <class R> __device__ __forceinline__ R gas_constant_air(const DevIface<R>& P, R q) {
@@ -123,6 +135,14 @@ template <class R> __device__ __forceinline__ R virtual_temperature(const DevIfa
 template <class R>
 __device__ __forceinline__ R surface_specific_humidity(const DevIface<R>& P, R pa, R Ts) {
     R pv = P.x * esat(P, Ts, P.phase);
+    pv = M<R>::fmin(pv, R(0.999) * pa);
+    return P.einv * pv / (pa - (R(1) - P.einv) * pv);
+}
+
+// surface_specific_humidity with esat_exp (the FP32 solvers' anchors).
+template <class R>
+__device__ __forceinline__ R surface_specific_humidity_exp(const DevIface<R>& P, R pa, R Ts) {
+    R pv = P.x * esat_exp(P, Ts);
     pv = M<R>::fmin(pv, R(0.999) * pa);
     return P.einv * pv / (pa - (R(1) - P.einv) * pv);
 }

@@ -14,7 +14,11 @@
 namespace nesf {
 
 // ------------------------------------------------------------- sea ice - ocean
-template <class S>
+// PART 0: the whole computation. PART 1: the fluxes alone, from the frazil-adjusted
+// column temperatures held in registers, leaving T3 unchanged; PART 2: the frazil
+// adjustment of T3 alone. PART 1 then PART 2 leave the same state as PART 0, and
+// PART 1 only reads the ocean state, so it may run beside kernels that read it.
+template <class S, int PART>
 __global__ void __launch_bounds__(256) io_kernel(IOArgs<S> a, nesf_io_params p) {
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t n = (int64_t)a.L.nx * a.L.ny;
@@ -23,20 +27,23 @@ __global__ void __launch_bounds__(256) io_kernel(IOArgs<S> a, nesf_io_params p) 
     int64_t k2 = a.L.at(i, j);
     double rho = p.ocean_reference_density, cpo = p.ocean_heat_capacity;
     // Part 1: frazil over the column, top level first (sea_ice_ocean_fluxes.jl:153-181)
-    double dQ = 0.0;
+    double dQ = 0.0, TN = 0.0;
     for (int kk = p.nz; kk >= 1; kk--) {
         int64_t k3 = k2 + (int64_t)(kk - 1) * p.stride_k;
-        double dz = a.dz[kk - 1];
         double Tk = (double)a.T3[k3], Sk = (double)a.S3[k3];
         double Tm = p.liquidus_freshwater_melting_temperature - p.liquidus_slope * Sk;
         bool freezing = Tk < Tm;
+        if (PART != 1 && freezing) a.T3[k3] = (S)Tm;
+        if (PART == 2) continue;
+        double dz = a.dz[kk - 1];
         double dE = (freezing ? 1.0 : 0.0) * rho * cpo * (Tm - Tk);
-        if (freezing) a.T3[k3] = (S)Tm;
         dQ -= dE * dz / p.dt;
+        if (kk == p.nz) TN = freezing ? (double)(S)Tm : Tk;   // the top level after the adjustment
     }
+    if (PART == 2) return;
     st(a.frazil, k2, dQ);
     int64_t kN = k2 + (int64_t)(p.nz - 1) * p.stride_k;
-    double TN = (double)a.T3[kN], SN = (double)a.S3[kN];
+    double SN = (double)a.S3[kN];
     double Si = ld(a.Si, k2), h = ld(a.hi, k2), aleph = ld(a.aleph, k2), hc = ld(a.hc, k2);
     double Tsi = (p.conductive && a.Tint) ? ld(a.Tint, k2) : 0.0;
     double Qio, Tb, Sb;
@@ -285,13 +292,15 @@ __global__ void __launch_bounds__(256) radiation_kernel(AsmArgs<S> a, nesf_assem
 static inline unsigned blocks_for(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
 
 template <class S>
-cudaError_t launch_io(const IOArgs<S>& a, const nesf_io_params& p, cudaStream_t s) {
+cudaError_t launch_io(const IOArgs<S>& a, const nesf_io_params& p, cudaStream_t s, int part) {
     int64_t n = (int64_t)a.L.nx * a.L.ny;
-    io_kernel<S><<<blocks_for(n, 256), 256, 0, s>>>(a, p);
+    if (part == 1) io_kernel<S, 1><<<blocks_for(n, 256), 256, 0, s>>>(a, p);
+    else if (part == 2) io_kernel<S, 2><<<blocks_for(n, 256), 256, 0, s>>>(a, p);
+    else io_kernel<S, 0><<<blocks_for(n, 256), 256, 0, s>>>(a, p);
     return cudaGetLastError();
 }
-template cudaError_t launch_io<double>(const IOArgs<double>&, const nesf_io_params&, cudaStream_t);
-template cudaError_t launch_io<float>(const IOArgs<float>&, const nesf_io_params&, cudaStream_t);
+template cudaError_t launch_io<double>(const IOArgs<double>&, const nesf_io_params&, cudaStream_t, int);
+template cudaError_t launch_io<float>(const IOArgs<float>&, const nesf_io_params&, cudaStream_t, int);
 
 cudaError_t launch_frac(const Layout2& L, const nesf_exchange_coords& c, const nesf_atmos_grid& ag, double* fi,
                         double* fj, cudaStream_t s) {

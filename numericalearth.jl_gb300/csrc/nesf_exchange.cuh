@@ -43,7 +43,8 @@ template <class S> struct AsmArgs {
     AsmFields<S> f;
 };
 
-template <class S> cudaError_t launch_io(const IOArgs<S>& a, const nesf_io_params& p, cudaStream_t s);
+// part 0: fluxes + frazil adjustment of T3; 1: the fluxes alone (T3 read only); 2: the adjustment alone.
+template <class S> cudaError_t launch_io(const IOArgs<S>& a, const nesf_io_params& p, cudaStream_t s, int part = 0);
 cudaError_t launch_frac(const Layout2& L, const nesf_exchange_coords& c, const nesf_atmos_grid& ag, double* fi,
                         double* fj, cudaStream_t s);
 template <class S> cudaError_t launch_interp(const InterpArgs<S>& a, cudaStream_t s);

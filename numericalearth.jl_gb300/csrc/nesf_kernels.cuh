@@ -65,6 +65,12 @@ inline DevIface<R> make_dev_iface(const nesf_interface_params& p) {
     d.sigma = R(p.stefan_boltzmann_constant); d.alb = R(p.albedo); d.emis = R(p.emissivity);
     d.Tfw = R(p.liquidus_freshwater_melting_temperature); d.slope = R(p.liquidus_slope);
     d.rho_i = R(p.interior_reference_density); d.c_i = R(p.interior_heat_capacity);
+    const bool ice = p.humidity_phase == NESF_PHASE_ICE;
+    double dcp = t.water_vapor_heat_capacity - (ice ? t.water_ice_heat_capacity : t.liquid_water_heat_capacity);
+    double L0 = ice ? t.reference_sublimation_enthalpy : t.reference_vaporization_enthalpy;
+    d.esA = R(dcp / Rv);
+    d.esK = R((L0 - dcp * t.reference_temperature) / Rv);
+    d.inv_Ttr = R(1.0 / t.triple_point_temperature);
     return d;
 }
 

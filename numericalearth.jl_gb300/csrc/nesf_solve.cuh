@@ -124,31 +124,30 @@ template <class R> struct SkinAnchor {
     R gA, gK;          // ln e_sat(T) = gA ln T - gK / T + const
 };
 
-__device__ __forceinline__ SkinAnchor<float> skin_anchor(const DevIface<double>& P, const CellConst<double>& c) {
-    const double tha = c.tha;
+// The anchors of a cell from theta_a and the interior temperature in FP64 (the
+// other inputs need no more than FP32's relative precision).
+__device__ __forceinline__ SkinAnchor<float> skin_anchor(const DevIface<double>& P, double tha, double Ti, double Si,
+                                                         double qa, double pa, double sw, double lw) {
     SkinAnchor<float> a;
-    a.dTi = (float)(c.Ti - tha);
-    double Tb = P.Tfw - P.slope * c.Si;
+    a.dTi = (float)(Ti - tha);
+    double Tb = P.Tfw - P.slope * Si;
     Tb = Tb + P.off_ifc;
     a.dTb = (float)(Tb - tha);
     a.dTm = (float)(P.Tfw + P.off_ifc - tha);
-    double pv = P.x * esat(P, tha, P.phase);
-    double qsa = P.einv * pv / (c.pa - (1.0 - P.einv) * pv);
+    double pv = P.x * esat_exp(P, tha);
+    double qsa = P.einv * pv / (pa - (1.0 - P.einv) * pv);
     a.pva = (float)pv;
     a.qsa = (float)qsa;
-    a.dqa = (float)(c.qa - qsa);
+    a.dqa = (float)(qa - qsa);
     double sigma = P.has_rad ? P.sigma : 0.0, eps = P.has_rad ? P.emis : 0.0;
-    double alb = P.has_rad ? P.alb : 0.0, SW = P.has_rad ? c.sw : 0.0, LW = P.has_rad ? c.lw : 0.0;
+    double alb = P.has_rad ? P.alb : 0.0, SW = P.has_rad ? sw : 0.0, LW = P.has_rad ? lw : 0.0;
     double T2 = tha * tha;
     double Iup = sigma * eps * (T2 * T2);
     double Qd = -(1.0 - alb) * SW - eps * LW;
     a.Iupa = (float)Iup;
     a.Qa0 = (float)(Iup + Qd);
-    double LH0 = P.phase == NESF_PHASE_ICE ? P.Ls0 : P.Lv0;
-    double cpc = P.phase == NESF_PHASE_ICE ? P.cpi : P.cpl;
-    double dcp = P.cpv - cpc;
-    a.gA = (float)(dcp / P.Rv);
-    a.gK = (float)((LH0 - dcp * P.T0) / P.Rv);
+    a.gA = (float)P.esA;
+    a.gK = (float)P.esK;
     return a;
 }
 
@@ -377,40 +376,31 @@ __device__ __forceinline__ float spectral_bound(const float (&J)[N][N]) {
     return expf((logf(n) + e) * (1.0f / 32.0f));
 }
 
-// FP32 sweep + FP64 Newton polish. On FAST_SOLVED the solution is in us, ts, qst
-// and s64 (interface temperature); on FAST_POLISH (only with accept32: the FP32
-// result is not good enough and the cell goes to the packed polish pass) and
-// FAST_REPLAY (the cell must follow the reference's FP64 iteration; `reason`
-// says why) us, ts, qst and s64 are untouched. `fp32_it` counts FP32 map
-// evaluations and `fp64_it` FP64 ones.
+// The FP32 sweep of a cell over the FP32 inputs of the map (c32, s32; with a skin
+// temperature the anchors `anc` and the state's fourth component tau = T_s -
+// theta_a, the delta form). x holds the start (u*, theta*, q*, tau) on entry and
+// the FP32 fixed point on return. Returns FAST_REPLAY (the cell must follow the
+// reference's FP64 iteration; `reason` says why), FAST_SOLVED (ACCEPT32 only: the
+// FP32 result is kept) or FAST_POLISH (the FP32 result needs FP64 Newton steps:
+// J and rho_est are set for them). `fp32_it` counts FP32 map evaluations.
 //
-// accept32 (ADAPTIVE): the sweep runs until every component, not just the drift
+// ACCEPT32 (ADAPTIVE): the sweep runs until every component, not just the drift
 // sum, is converged at FP32 resolution, and the FP32 result is kept when F
-// contracts by at most so.fp32_rho. On FAST_SOLVED s64.Ts is the interface
-// temperature; the rest of s64 is not updated.
+// contracts by at most so.fp32_rho.
 //
 // The FP32 sweep and the 2N evaluations of the central-difference Jacobian run
 // through one loop around a single inlined copy of the map, so a warp executes
 // the same instructions for both: the kernel's hot code stays small enough for
 // the instruction cache.
-template <bool SKIN>
-__device__ __forceinline__ int solve_fast(const DevIface<double>& P64, const DevIface<float>& P32,
-                                          const CellConst<double>& c64, SurfaceConst<double>& s64, double& us,
-                                          double& ts, double& qst, const SolveOpts& so, bool accept32, int& fp32_it,
-                                          int& fp64_it, int& reason, const float* xw = nullptr,
-                                          bool* fell_back = nullptr) {
+template <bool SKIN, bool ACCEPT32>
+__device__ __forceinline__ int sweep_fp32(const DevIface<float>& P32, const CellConst<float>& c32,
+                                          const SurfaceConst<float>& s32, const SkinAnchor<float>& anc,
+                                          float (&x)[4], const SolveOpts& so, int& fp32_it, int& reason,
+                                          float (&J)[SKIN ? 4 : 3][SKIN ? 4 : 3], float& rho_est,
+                                          const float* xw, bool* fell_back) {
     constexpr int N = SKIN ? 4 : 3;
-    fp64_it = 0;
-    CellConst<float> c32;
-    SurfaceConst<float> s32;
-    convert_const(c64, c32);
-    convert_surface(s64, s32);
-    SkinAnchor<float> anc{};
-    if (SKIN) anc = skin_anchor(P64, c64);
-    const float tol = (float)P64.tol;
-    // sweep state; a skin temperature as tau = T_s - theta_a (the delta form)
-    const float x0[4] = {(float)us, (float)ts, (float)qst, SKIN ? (float)(s64.Ts - c64.tha) : 0.0f};
-    float x[4] = {x0[0], x0[1], x0[2], x0[3]};
+    const float tol = P32.tol;
+    const float x0[4] = {x[0], x[1], x[2], x[3]};
     // warm start: the network's (u*, theta*, q*) replaces the reference's start; T_s keeps its own
     const bool warm = xw != nullptr && isfinite(xw[0]) && isfinite(xw[1]) && isfinite(xw[2]) && xw[0] > 0.0f;
     if (warm) { x[0] = xw[0]; x[1] = xw[1]; x[2] = xw[2]; }
@@ -418,7 +408,6 @@ __device__ __forceinline__ int solve_fast(const DevIface<double>& P64, const Dev
     float rw = 0.0f;
     int probes = 0;
     float yp[4] = {0, 0, 0, 0};   // F(x + h e_j) of the column in progress
-    float J[N][N];
     SweepTrace tr;
     tr.d[0] = tr.d[1] = tr.d[2] = 0.0f;
     tr.lam = 1.0f;
@@ -496,7 +485,7 @@ __device__ __forceinline__ int solve_fast(const DevIface<double>& P64, const Dev
             // each component within 4 of its own ulps (ADAPTIVE), or the sum within 8
             const float u4 = 4.0f * 1.1920929e-7f;
             // (tau to 1e-7 K besides: dtheta = -tau)
-            bool quiet = accept32 ? (du <= u4 * fabsf(x[0]) && dt <= u4 * fabsf(x[1]) && dq <= u4 * fabsf(x[2]) &&
+            bool quiet = ACCEPT32 ? (du <= u4 * fabsf(x[0]) && dt <= u4 * fabsf(x[1]) && dq <= u4 * fabsf(x[2]) &&
                                      dT <= u4 * fabsf(x[3]) + 1e-7f)
                                   : drift <= 8.0f * res;
             bool done = drift < tol || quiet;
@@ -530,7 +519,7 @@ __device__ __forceinline__ int solve_fast(const DevIface<double>& P64, const Dev
     }
     fp32_it = it + probes + 2 * N;
     // ---- contraction rate of F at the solution
-    const float rho_est = spectral_bound<N>(J);
+    rho_est = spectral_bound<N>(J);
     if (!(rho_est < 0.995f)) { reason = REPLAY_SLOW; return FAST_REPLAY; }
     // ---- the reference's stopping error along its slowest mode: e = rho / (1 - rho) d, |d|_1 < tol.
     // Mode shape: power iteration from the last drift (each component's largest share over the
@@ -568,16 +557,36 @@ __device__ __forceinline__ int solve_fast(const DevIface<double>& P64, const Dev
             }
     }
     // ---- ADAPTIVE: keep the FP32 result of a quiet, well-contracting cell
-    if (accept32) {
-        // FP32 rounding of the anchored terms (~1e-7 of each), amplified by their
-        // cancellation and by 1 / (1 - rho), must stay within path_tol
-        if (!stalled && rho_est <= so.fp32_rho && cond * 1.2e-7f <= so.path_tol * (1.0f - rho_est)) {
-            us = x[0]; ts = x[1]; qst = x[2];
-            if (SKIN) s64.Ts = c64.tha + (double)x[3];
-            return FAST_SOLVED;
-        }
-        return FAST_POLISH;
-    }
+    // FP32 rounding of the anchored terms (~1e-7 of each), amplified by their
+    // cancellation and by 1 / (1 - rho), must stay within path_tol
+    if (ACCEPT32 && !stalled && rho_est <= so.fp32_rho && cond * 1.2e-7f <= so.path_tol * (1.0f - rho_est))
+        return FAST_SOLVED;
+    return FAST_POLISH;
+}
+
+// FP32 sweep + FP64 Newton polish from the reference's FP64 cell constants (c64,
+// s64). On FAST_SOLVED the solution is in us, ts, qst and, with a skin
+// temperature, s64.Ts (the interface temperature; the rest of s64 is not
+// updated); on FAST_REPLAY they are untouched. `fp32_it` counts FP32 map
+// evaluations and `fp64_it` FP64 ones.
+template <bool SKIN>
+__device__ __forceinline__ int solve_fast(const DevIface<double>& P64, const DevIface<float>& P32,
+                                          const CellConst<double>& c64, SurfaceConst<double>& s64, double& us,
+                                          double& ts, double& qst, const SolveOpts& so, int& fp32_it, int& fp64_it,
+                                          int& reason, const float* xw = nullptr, bool* fell_back = nullptr) {
+    constexpr int N = SKIN ? 4 : 3;
+    fp64_it = 0;
+    CellConst<float> c32;
+    SurfaceConst<float> s32;
+    convert_const(c64, c32);
+    convert_surface(s64, s32);
+    SkinAnchor<float> anc{};
+    if (SKIN) anc = skin_anchor(P64, c64.tha, c64.Ti, c64.Si, c64.qa, c64.pa, c64.sw, c64.lw);
+    float x[4] = {(float)us, (float)ts, (float)qst, SKIN ? (float)(s64.Ts - c64.tha) : 0.0f};
+    float J[N][N];
+    float rho_est;
+    if (sweep_fp32<SKIN, false>(P32, c32, s32, anc, x, so, fp32_it, reason, J, rho_est, xw, fell_back) == FAST_REPLAY)
+        return FAST_REPLAY;
     // ---- FP64 Newton steps on x = F(x)
     float A[N][N], Ainv[N][N];
 #pragma unroll
@@ -630,6 +639,62 @@ __device__ __forceinline__ int solve_fast(const DevIface<double>& P64, const Dev
     us = xd[0]; ts = xd[1]; qst = xd[2];
     if (SKIN) s64.Ts = xd[3];   // the callers read the interface temperature alone
     return FAST_SOLVED;
+}
+
+// ------------------------------------------ adaptive pass 1: FP32 in and out
+// The inputs of an adaptive pass-1 cell: the map's constants in FP32, built from
+// the FP32 loads, with FP64 only where differences cancel -- theta_a - T_s and
+// q_a - q_s(T_s) for a bulk interface temperature (the surface constants s), the
+// anchors of the delta form for a skin temperature (anc) -- and the flux epilogue
+// in FP32. A kept FP32 result carries FP32 rounding anyway; the few FP64
+// operations left per cell replace the reference epilogue's FP64 divisions, square
+// roots and pow, which at 1/64 of the FP32 rate cost as much as the sweep.
+struct Fast32 {
+    CellConst<float> c;
+    SurfaceConst<float> s;    // bulk interface temperature
+    SkinAnchor<float> anc;    // skin temperature
+    double tha;               // theta_a (a skin state's T_s = theta_a + tau)
+    double Ts0;               // the interface temperature before the iteration
+};
+
+// theta_a - T_a = g h / cp_m(q_a) (surface_atmosphere_temperature), ~0.1 K. In FP64:
+// its FP32 rounding (~1e-8 K) would be a large part of a near-neutral theta_a - T_s.
+__device__ __forceinline__ double lift_temperature(const DevIface<double>& P, double qa) {
+    return P.g * P.h / cp_m(P, qa);
+}
+
+// Surface constants of a bulk interface temperature Ts: q_s and the differences
+// in FP64 (from the fields' own T_a and q_a: FP64 fields are not rounded first),
+// the rest in FP32 from the rounded T_s and q_s.
+__device__ __forceinline__ void fast_surface(const DevIface<double>& P, const DevIface<float>& Pf, double Ta,
+                                             double qa, double pa, double lift, double Ts, SurfaceConst<float>& s) {
+    double qs = surface_specific_humidity_exp(P, pa, Ts);
+    s.Ts = (float)Ts;
+    s.qs = (float)qs;
+    s.dth = (float)((Ta - Ts) + lift);
+    s.dq = (float)(qa - qs);
+    float Tv = virtual_temperature(Pf, s.Ts, s.qs);
+    float delta = Pf.eps - 1.0f;
+    s.gTv = Pf.g / Tv;
+    s.A1 = 1.0f + delta * s.qs;
+    s.A2 = delta * Tv;
+    s.nu_u = air_viscosity(Pf.rough[0], s.Ts);
+    s.nu_t = air_viscosity(Pf.rough[1], s.Ts);
+    s.nu_q = air_viscosity(Pf.rough[2], s.Ts);
+}
+
+// Momentum flux direction: (-u*^2 du / |dU|, -u*^2 dv / |dU|) in FP32, in FP64 where
+// |dU|^2 would underflow.
+__device__ __forceinline__ void stress_fast(float us, float du, float dv, float& tx, float& ty) {
+    float dU = sqrtf(du * du + dv * dv);
+    if (dU < 1e-18f && (du != 0.0f || dv != 0.0f)) {
+        double d = sqrt((double)du * du + (double)dv * dv);
+        tx = (float)(-((double)us * us) * du / d);
+        ty = (float)(-((double)us * us) * dv / d);
+        return;
+    }
+    tx = dU == 0.0f ? 0.0f : -(us * us) * du / dU;
+    ty = dU == 0.0f ? 0.0f : -(us * us) * dv / dU;
 }
 
 // Warp-aggregated append of `id` to one side of a member's work list; returns the

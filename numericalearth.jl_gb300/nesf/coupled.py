@@ -130,13 +130,14 @@ class CoupledModel:
         self.update_net_fluxes(stream)
         return self.kernels_per_step(precision)
 
-    def kernels_per_step(self, precision):
+    def kernels_per_step(self, precision, native=False):
         """Kernels one step launches: interpolation; per solve classify + solve (+ the packed
-        polish pass of the adaptive mode, + the replay pass of the FP32 modes); sea-ice-ocean;
-        ocean and sea-ice assembly and their radiative add-ons."""
+        polish pass of the adaptive mode, + the replay pass of the FP32 modes); sea-ice-ocean
+        (in the native step its fluxes and its frazil adjustment apart); ocean and sea-ice
+        assembly and their radiative add-ons."""
         fast = precision != "f64" and precision != "plain"
         per_solve = 2 + (precision == "f32_adaptive") + fast + (fast and self.mlp is not None)
-        return (1 if self.atmos is not None else 0) + 2 * per_solve + 1 + 4
+        return (1 if self.atmos is not None else 0) + 2 * per_solve + (2 if native else 1) + 4
 
     # ------------------------------------------------- native step and graph
     def step_args(self):
@@ -168,7 +169,7 @@ class CoupledModel:
     def native_step(self, precision="f32_adaptive", stream=None):
         """One coupling step through nesf_coupling_step; returns the kernels launched."""
         api.coupling_step(self.step_args(), precision, stream=stream, mlp=self.mlp)
-        return self.kernels_per_step(precision)
+        return self.kernels_per_step(precision, native=True)
 
     def capture(self, precision="f32_adaptive"):
         """Capture one coupling step as a CUDA graph (nesf_graph_capture)."""
@@ -181,7 +182,7 @@ class CoupledModel:
         if time_weight is not None:
             self.graph.set_time_weight(time_weight)
         self.graph.launch(stream)
-        return self.kernels_per_step(self.graph_precision)
+        return self.kernels_per_step(self.graph_precision, native=True)
 
     # ------------------------------------------------------ conservation
     def row_areas(self, radius=6.371e6):
