@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--small", action="store_true", help="small grid (profiling captures)")
     ap.add_argument("--no-plain", action="store_true", help="time only --precision (profiling captures)")
     ap.add_argument("--cold", action="store_true", help="no learned warm start")
+    ap.add_argument("--no-autotune", action="store_true", help="default launch shapes (no nesf_autotune)")
     return ap.parse_args()
 
 
@@ -388,6 +389,8 @@ def main():
     warm_info = None
     if prec != "f64" and not args.cold:
         model.mlp, warm_info = train_warm_start()
+    # launch shapes and schedule from the autotuner (nesf_autotune), on this workload
+    tuning = model.autotune(prec, reps=3) if not args.no_autotune else None
 
     # warm-up both solvers, then the timed region (fast path) with clock sampling
     with ClockSampler(local) as clocks:
@@ -414,7 +417,8 @@ def main():
                        "schedule": "one thread per cell, compacted work lists, packed polish/replay passes; "
                                    "sea-ice and ocean solves on two lanes (the ocean solve overlaps the sea-ice "
                                    "polish/replay tail); the step replayed as one CUDA graph",
-                       "l2": "working set > L2 (no flush needed)", "parallelism": f"replicas x{world}"},
+                       "l2": "working set > L2 (no flush needed)", "parallelism": f"replicas x{world}",
+                       "tuning": tuning},
             "gpu_launches": launches,
             "clocks": clk,
             "plain_f64": {"value": cells * world / (ms_plain / 1000.0), "ms_per_step": ms_plain,

@@ -584,6 +584,38 @@ int nesf_graph_set_time_weight(nesf_graph* graph, double time_weight);
 int nesf_graph_launch(nesf_graph* graph, void* stream);
 int nesf_graph_destroy(nesf_graph* graph);
 
+/* ------------------------------------------------------------ the autotuner
+ * Launch shapes and schedule of a context's solves and coupling steps. None of
+ * them changes a result: every cell's arithmetic is the same under each, so the
+ * outputs are bit-identical (the tests check it); only the time differs. 0 in a
+ * field means its default. Replaces nothing in the reference (Julia launches its
+ * kernels with KernelAbstractions' default workgroup); it is the `nesf_autotune`
+ * entry of the GB300 design. */
+typedef struct {
+    int32_t solve_block;      /* threads per block of the solves' pass 1: 32, 64, 96 or 128 (128)       */
+    int32_t deferred_per_sm;  /* blocks per SM of the packed polish and replay passes, 1..16 (4)      */
+    int32_t infer_per_sm;     /* blocks per SM of the warm-start inference pass, 1..8 (4)             */
+    int32_t two_lanes;        /* coupling step: sea-ice solve on a second stream beside the ocean's (1) */
+    int32_t io_overlap;       /* coupling step: sea-ice-ocean fluxes beside the sea-ice pass 1 (1)      */
+    int32_t pad_;
+    double step_ms;           /* nesf_autotune: the chosen configuration's mean step time            */
+} nesf_tuning;
+
+/* The context's tuning (a NULL context: the default context's). Fields out of
+ * range are an argument error; 0 selects the default. A graph keeps the tuning
+ * it was captured with. */
+int nesf_set_tuning(nesf_context* ctx, const nesf_tuning* tuning);
+int nesf_get_tuning(nesf_context* ctx, nesf_tuning* tuning);
+/* Coordinate search over the tuning on the caller's workload: for each field in
+ * turn, each candidate value is timed (CUDA events on `stream`, one untimed step,
+ * then `reps` steps) with the others at their best so far; the fastest setting is
+ * kept. The chosen tuning is set on the context and written to `out` with its
+ * step time. The steps run for real: the outputs and the in/out state (sea-ice
+ * surface temperature, frazil-adjusted ocean temperature) are left as that many
+ * coupling steps leave them. Synchronises `stream`. */
+int nesf_autotune(nesf_context* ctx, const nesf_coupling_step_args* args, const nesf_solver_options* opts,
+                  int32_t reps, nesf_tuning* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -321,7 +321,7 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
                                SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws,
                                DevStats* stats, cudaStream_t stream, cudaEvent_t after_solve) {
     const int64_t ring = (int64_t)(a.L.nx + 2) * (a.L.ny + 2);
-    const int block = 128;
+    const int block = so.block;   // <= 128: the kernels are compiled with __launch_bounds__(128)
     dim3 grid((unsigned)((ring + block - 1) / block));
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
@@ -334,7 +334,8 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     if (e != cudaSuccess) return e;
     ai_classify_kernel<S><<<grid, block, 0, stream>>>(a, P64, P32, wl, warm ? ws.feat : nullptr, stats);
     if (warm) {
-        e = mlp_pass((void*)ws.mlp, ws.feat, nullptr, ws.guess, 0, wl.count, wl.per_member, 4 * sms, true, stream);
+        e = mlp_pass((void*)ws.mlp, ws.feat, nullptr, ws.guess, 0, wl.count, wl.per_member, so.infer_per_sm * sms,
+                     true, stream);
         if (e != cudaSuccess) return e;
     }
     const float* guess = warm ? ws.guess : nullptr;
@@ -354,13 +355,13 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     if (e != cudaSuccess || prec == NESF_PLAIN_F64) return e;
     if (adaptive) {
         if (skin)
-            ai_polish_kernel<S, true><<<(unsigned)sms * 4, block, 0, stream>>>(a, P64, P32, so, rq, stats);
+            ai_polish_kernel<S, true><<<(unsigned)(sms * so.deferred_per_sm), 128, 0, stream>>>(a, P64, P32, so, rq, stats);
         else
-            ai_polish_kernel<S, false><<<(unsigned)sms * 4, block, 0, stream>>>(a, P64, P32, so, rq, stats);
+            ai_polish_kernel<S, false><<<(unsigned)(sms * so.deferred_per_sm), 128, 0, stream>>>(a, P64, P32, so, rq, stats);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    ai_replay_kernel<S><<<(unsigned)sms * 4, block, 0, stream>>>(a, P64, rq, stats);
+    ai_replay_kernel<S><<<(unsigned)(sms * so.deferred_per_sm), 128, 0, stream>>>(a, P64, rq, stats);
     return cudaGetLastError();
 }
 

@@ -336,7 +336,7 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
                                bool skin, SolveOpts so, const WorkList& wl, const ReplayQueue& rq,
                                const WarmStart& ws, DevStats* stats, cudaStream_t stream) {
     const int64_t ring = (int64_t)(a.L.nx + 2) * (a.L.ny + 2);
-    const int threads = 128;   // kernels are compiled with __launch_bounds__(128)
+    const int threads = so.block;   // <= 128: the kernels are compiled with __launch_bounds__(128)
     const int nm = members > 1 ? members : 1;
     dim3 grid((unsigned)((ring + threads - 1) / threads), nm);
     bool ens = members > 1 || P64s != nullptr;
@@ -353,7 +353,8 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
     if (ens) ao_classify_kernel<S, true><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, nullptr, stats);
     else ao_classify_kernel<S, false><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, feat, stats);
     if (warm) {
-        e = mlp_pass((void*)ws.mlp, ws.feat, nullptr, ws.guess, 0, wl.count, wl.per_member, 4 * sms, true, stream);
+        e = mlp_pass((void*)ws.mlp, ws.feat, nullptr, ws.guess, 0, wl.count, wl.per_member, so.infer_per_sm * sms,
+                     true, stream);
         if (e != cudaSuccess) return e;
     }
 #define NESF_AO_LAUNCH(PR, SK, EN) \
@@ -374,16 +375,16 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
     e = cudaGetLastError();
     if (e != cudaSuccess || prec == NESF_PLAIN_F64) return e;
     // passes 1b and 2: enough resident blocks to sweep the queues (grid-stride)
-    unsigned g2 = (unsigned)sms * 4;
+    unsigned g2 = (unsigned)(sms * so.deferred_per_sm);
     const DevIface<double>* pm = ens ? P64s : nullptr;
     if (adaptive) {
-        if (skin) ao_polish_kernel<S, true><<<g2, threads, 0, stream>>>(a, P64, P32, pm, ens ? P32s : nullptr, so, rq, stats);
-        else ao_polish_kernel<S, false><<<g2, threads, 0, stream>>>(a, P64, P32, pm, ens ? P32s : nullptr, so, rq, stats);
+        if (skin) ao_polish_kernel<S, true><<<g2, 128, 0, stream>>>(a, P64, P32, pm, ens ? P32s : nullptr, so, rq, stats);
+        else ao_polish_kernel<S, false><<<g2, 128, 0, stream>>>(a, P64, P32, pm, ens ? P32s : nullptr, so, rq, stats);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    if (skin) ao_replay_kernel<S, true><<<g2, threads, 0, stream>>>(a, P64, pm, rq, stats);
-    else ao_replay_kernel<S, false><<<g2, threads, 0, stream>>>(a, P64, pm, rq, stats);
+    if (skin) ao_replay_kernel<S, true><<<g2, 128, 0, stream>>>(a, P64, pm, rq, stats);
+    else ao_replay_kernel<S, false><<<g2, 128, 0, stream>>>(a, P64, pm, rq, stats);
     return cudaGetLastError();
 }
 

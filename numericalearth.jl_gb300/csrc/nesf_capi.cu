@@ -6,6 +6,7 @@
 #include <cstring>
 #include <cstdarg>
 #include <mutex>
+#include <vector>
 #include <new>
 
 #include "nesf_solve.cuh"
@@ -35,8 +36,20 @@ struct nesf_context {
     nesf_context* aux;
     cudaStream_t side;
     cudaEvent_t ev_fork, ev_ice, ev_join;
+    nesf_tuning tuning;         // launch shapes and schedule (nesf_set_tuning, nesf_autotune)
     std::mutex lock;            // serialises use of the scratch above
 };
+
+// The defaults of nesf_tuning's fields.
+static nesf_tuning default_tuning() {
+    nesf_tuning t{};
+    t.solve_block = 128;
+    t.deferred_per_sm = 4;
+    t.infer_per_sm = 4;
+    t.two_lanes = 1;
+    t.io_overlap = 1;
+    return t;
+}
 
 namespace nesf {
 cudaError_t launch_integrals(const nesf_integral_fields& f, void* partials, int max_blocks, double* result,
@@ -94,7 +107,8 @@ int32_t nesf_struct_sizes(int64_t* sizes, int32_t n) {
         (int64_t)sizeof(nesf_ai_fields), (int64_t)sizeof(nesf_io_params), (int64_t)sizeof(nesf_io_fields),
         (int64_t)sizeof(nesf_atmos_grid), (int64_t)sizeof(nesf_exchange_coords), (int64_t)sizeof(nesf_interp_fields),
         (int64_t)sizeof(nesf_assembly_params), (int64_t)sizeof(nesf_assembly_fields),
-        (int64_t)sizeof(nesf_coupling_step_args), (int64_t)sizeof(nesf_integral_fields)};
+        (int64_t)sizeof(nesf_coupling_step_args), (int64_t)sizeof(nesf_integral_fields),
+        (int64_t)sizeof(nesf_tuning)};
     int32_t m = (int32_t)(sizeof s / sizeof s[0]);
     for (int32_t k = 0; k < n && k < m; k++) sizes[k] = s[k];
     return m;
@@ -278,6 +292,7 @@ int nesf_context_create(int32_t device, nesf_context** out) {
     c->aux = nullptr;
     c->side = nullptr;
     c->ev_fork = c->ev_ice = c->ev_join = nullptr;
+    c->tuning = default_tuning();
     cudaError_t e = cudaMalloc(&c->d_stats, sizeof(DevStats));
     if (e == cudaSuccess) e = cudaMalloc(&c->d_partials, (size_t)kIntegralBlocks * NESF_MAX_INTEGRALS * 16);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_replay_count, 2 * sizeof(unsigned int));
@@ -364,10 +379,13 @@ static nesf_solver_options options_or_default(const nesf_solver_options* o) {
     return r;
 }
 
-// The kernels' knobs; fp32_rho = 0 keeps no FP32 result (NESF_F32_POLISH).
-static SolveOpts solve_opts(const nesf_solver_options& o) {
+// The kernels' knobs; fp32_rho = 0 keeps no FP32 result (NESF_F32_POLISH). Launch
+// shapes from the context's tuning (the defaults without a context).
+static SolveOpts solve_opts(const nesf_solver_options& o, const nesf_context* ctx = nullptr) {
     float rho = o.precision == NESF_F32_ADAPTIVE ? (float)(o.fp32_rho < 0.99 ? o.fp32_rho : 0.99) : 0.0f;
-    return SolveOpts{o.polish_maxiter, (float)o.path_tolerance, rho, (float)o.fallback_ratio};
+    const nesf_tuning t = ctx ? ctx->tuning : default_tuning();
+    return SolveOpts{o.polish_maxiter, (float)o.path_tolerance, rho, (float)o.fallback_ratio,
+                     t.solve_block, t.deferred_per_sm, t.infer_per_sm};
 }
 
 static int check_options(const nesf_solver_options& o, const char* who) {
@@ -548,7 +566,7 @@ extern "C" int nesf_compute_atmosphere_ocean_fluxes(nesf_context* ctx, const nes
     if ((r = replay_queue(ctx, ring, &rq))) return r;
     if ((r = work_list(ctx, ring, 1, &wl))) return r;
     if ((r = warm_buffers(ctx, o, ring, &ws))) return r;
-    SolveOpts so = solve_opts(o);
+    SolveOpts so = solve_opts(o, ctx);
     return with_stats(ctx, stats, s, [&](DevStats* ds) {
         if (f->dtype == NESF_F64)
             return launch_ao(ao_args<double>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl, rq, ws,
@@ -612,7 +630,7 @@ extern "C" int nesf_compute_atmosphere_ocean_fluxes_ensemble(nesf_context* ctx, 
     WorkList wl;
     if ((r = replay_queue(ctx, ring * members, &rq))) return r;
     if ((r = work_list(ctx, ring, members, &wl))) return r;
-    SolveOpts so = solve_opts(o);
+    SolveOpts so = solve_opts(o, ctx);
     return with_stats(ctx, stats, s, [&](DevStats* ds) {
         if (f->dtype == NESF_F64)
             return launch_ao(ao_args<double>(f, member_stride), P64, P32, ctx->d_p64, ctx->d_p32, members,
@@ -677,7 +695,7 @@ static int sea_ice_fluxes(nesf_context* ctx, const nesf_interface_params* params
     if ((r = replay_queue(ctx, ring, &rq))) return r;
     if ((r = work_list(ctx, ring, 1, &wl))) return r;
     if ((r = warm_buffers(ctx, o, ring, &ws))) return r;
-    SolveOpts so = solve_opts(o);
+    SolveOpts so = solve_opts(o, ctx);
     return with_stats(ctx, stats, s, [&](DevStats* ds) {
         if (f->dtype == NESF_F64)
             return launch_ai(ai_args<double>(f), P64, P32, o.precision, so, wl, rq, ws, ds, s, after_solve);
@@ -1127,21 +1145,28 @@ extern "C" int nesf_coupling_step(nesf_context* ctx, const nesf_coupling_step_ar
     // only the ocean and ice state, so they run on the main lane beside the sea-ice pass 1;
     // their frazil adjustment of the ocean temperature, which both solves read, waits for
     // both (the same state as update_state!'s order).
+    // The context's tuning may put the sea-ice solve in line (one lane) and the
+    // sea-ice-ocean fluxes after the solves; the outputs are the same.
     if (a->interp && (r = nesf_interpolate_atmosphere_state(a->interp, stream))) return r;
     cudaStream_t s = (cudaStream_t)stream;
-    const bool io_split = ice && a->io_params;
+    const bool io_split = ice && a->io_params && ctx->tuning.io_overlap;
+    const bool lanes = ice && ctx->tuning.two_lanes;
     if (ice) {
         if ((r = coupling_lane(ctx))) return r;
+        ctx->aux->tuning = ctx->tuning;
         DeviceGuard g(ctx->device);
-        NESF_CUDA(cudaEventRecord(ctx->ev_fork, s));
-        NESF_CUDA(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
-        if ((r = sea_ice_fluxes(ctx->aux, a->ai_params, a->ai, opts, nullptr, ctx->side, ctx->ev_ice))) return r;
-        NESF_CUDA(cudaEventRecord(ctx->ev_join, ctx->side));
+        if (lanes) {
+            NESF_CUDA(cudaEventRecord(ctx->ev_fork, s));
+            NESF_CUDA(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+            if ((r = sea_ice_fluxes(ctx->aux, a->ai_params, a->ai, opts, nullptr, ctx->side, ctx->ev_ice))) return r;
+            NESF_CUDA(cudaEventRecord(ctx->ev_join, ctx->side));
+        }
         if (io_split && (r = sea_ice_ocean(ctx, a->io_params, a->io, stream, 1))) return r;
-        NESF_CUDA(cudaStreamWaitEvent(s, ctx->ev_ice, 0));
+        if (lanes) NESF_CUDA(cudaStreamWaitEvent(s, ctx->ev_ice, 0));
+        else if ((r = sea_ice_fluxes(ctx->aux, a->ai_params, a->ai, opts, nullptr, s, nullptr))) return r;
     }
     if ((r = nesf_compute_atmosphere_ocean_fluxes(ctx, a->ao_params, a->ao, opts, nullptr, stream))) return r;
-    if (ice) {
+    if (lanes) {
         DeviceGuard g(ctx->device);
         NESF_CUDA(cudaStreamWaitEvent(s, ctx->ev_join, 0));
     }
@@ -1262,5 +1287,126 @@ extern "C" int nesf_graph_destroy(nesf_graph* G) {
     if (G->exec) cudaGraphExecDestroy(G->exec);
     if (G->graph) cudaGraphDestroy(G->graph);
     delete G;
+    return NESF_OK;
+}
+
+// ------------------------------------------------------------- the autotuner
+static int check_tuning(const nesf_tuning& t, const char* who) {
+    if (t.solve_block < 0 || t.solve_block > 128 || t.solve_block % 32)
+        return fail(NESF_ERR_ARG, "%s: solve_block %d (32, 64, 96 or 128)", who, t.solve_block);
+    if (t.deferred_per_sm < 0 || t.deferred_per_sm > 16)
+        return fail(NESF_ERR_ARG, "%s: deferred_per_sm %d (1..16)", who, t.deferred_per_sm);
+    if (t.infer_per_sm < 0 || t.infer_per_sm > 8)
+        return fail(NESF_ERR_ARG, "%s: infer_per_sm %d (1..8)", who, t.infer_per_sm);
+    if (t.two_lanes < 0 || t.two_lanes > 1 || t.io_overlap < 0 || t.io_overlap > 1)
+        return fail(NESF_ERR_ARG, "%s: two_lanes and io_overlap are 0 or 1", who);
+    return NESF_OK;
+}
+
+// 0 fields take the defaults; the flags are taken as given.
+static nesf_tuning complete_tuning(const nesf_tuning& t) {
+    nesf_tuning d = default_tuning(), r = t;
+    if (!r.solve_block) r.solve_block = d.solve_block;
+    if (!r.deferred_per_sm) r.deferred_per_sm = d.deferred_per_sm;
+    if (!r.infer_per_sm) r.infer_per_sm = d.infer_per_sm;
+    r.pad_ = 0;
+    return r;
+}
+
+extern "C" int nesf_set_tuning(nesf_context* ctx, const nesf_tuning* t) {
+    if (!t) return fail(NESF_ERR_ARG, "nesf_set_tuning: null tuning");
+    int r = check_tuning(*t, "nesf_set_tuning");
+    if (r || (r = context_or_default(&ctx))) return r;
+    std::lock_guard<std::mutex> lk(ctx->lock);
+    ctx->tuning = complete_tuning(*t);
+    ctx->tuning.step_ms = t->step_ms;
+    return NESF_OK;
+}
+
+extern "C" int nesf_get_tuning(nesf_context* ctx, nesf_tuning* t) {
+    if (!t) return fail(NESF_ERR_ARG, "nesf_get_tuning: null output");
+    int r = context_or_default(&ctx);
+    if (r) return r;
+    std::lock_guard<std::mutex> lk(ctx->lock);
+    *t = ctx->tuning;
+    return NESF_OK;
+}
+
+extern "C" int nesf_autotune(nesf_context* ctx, const nesf_coupling_step_args* a, const nesf_solver_options* opts,
+                             int32_t reps, nesf_tuning* out, void* stream) {
+    const char* who = "nesf_autotune";
+    if (!a) return fail(NESF_ERR_ARG, "%s: null arguments", who);
+    if (reps < 1 || reps > 1000) return fail(NESF_ERR_ARG, "%s: reps = %d (1..1000)", who, reps);
+    int r = context_or_default(&ctx);
+    if (r) return r;
+    cudaStream_t s = (cudaStream_t)stream;
+    const nesf_tuning start = ctx->tuning;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    {
+        DeviceGuard g(ctx->device);
+        NESF_CUDA(cudaEventCreate(&e0));
+        cudaError_t e = cudaEventCreate(&e1);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(e0);
+            return cuda_fail(e, who);
+        }
+    }
+    // mean step time of a tuning: one untimed step (it also sizes the scratch), then `reps`
+    auto timed = [&](const nesf_tuning& t, double* ms) -> int {
+        ctx->tuning = t;
+        int q = nesf_coupling_step(ctx, a, opts, stream);
+        if (q) return q;
+        DeviceGuard g(ctx->device);
+        NESF_CUDA(cudaEventRecord(e0, s));
+        for (int i = 0; i < reps; i++)
+            if ((q = nesf_coupling_step(ctx, a, opts, stream))) return q;
+        NESF_CUDA(cudaEventRecord(e1, s));
+        NESF_CUDA(cudaEventSynchronize(e1));
+        float f = 0.0f;
+        NESF_CUDA(cudaEventElapsedTime(&f, e0, e1));
+        *ms = (double)f / reps;
+        return NESF_OK;
+    };
+    const nesf_solver_options o = options_or_default(opts);
+    const bool ice = a->ai_params != nullptr;
+    const bool warm = o.warm_start && o.mlp && o.precision != NESF_PLAIN_F64;
+    const bool fast = o.precision != NESF_PLAIN_F64;
+    nesf_tuning best = complete_tuning(start);
+    double best_ms = 0.0;
+    r = timed(best, &best_ms);
+    // coordinate search: each field's candidates with the others at their best so far; a
+    // candidate must beat the best by 1 % (event timings of ~10 ms steps repeat to ~0.5 %)
+    struct Axis { int32_t nesf_tuning::*field; std::vector<int32_t> values; bool used; };
+    const Axis axes[] = {
+        {&nesf_tuning::solve_block, {128, 96, 64, 32}, true},
+        {&nesf_tuning::deferred_per_sm, {2, 4, 8, 16}, fast},
+        {&nesf_tuning::infer_per_sm, {2, 4, 8}, warm},
+        {&nesf_tuning::two_lanes, {1, 0}, ice},
+        {&nesf_tuning::io_overlap, {1, 0}, ice && a->io_params != nullptr},
+    };
+    for (const Axis& ax : axes) {
+        if (r || !ax.used) continue;
+        const int32_t current = best.*(ax.field);
+        for (int32_t v : ax.values) {
+            if (v == current || r) continue;
+            nesf_tuning t = best;
+            t.*(ax.field) = v;
+            double ms = 0.0;
+            if ((r = timed(t, &ms))) break;
+            if (ms < 0.99 * best_ms) { best = t; best_ms = ms; }
+        }
+    }
+    {
+        DeviceGuard g(ctx->device);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    if (r) {
+        ctx->tuning = start;
+        return r;
+    }
+    best.step_ms = best_ms;
+    ctx->tuning = best;
+    if (out) *out = best;
     return NESF_OK;
 }

@@ -30,6 +30,9 @@ struct SolveOpts {
     float path_tol;        // replay threshold on the reference's stopping-error bound
     float fp32_rho;        // ADAPTIVE: keep the FP32 result below this contraction (0: never)
     float fallback_ratio;  // warm start: cold start when the first residual exceeds this times the cold one
+    // launch shapes (host side; the autotuner's choice): threads per block of pass 1,
+    // blocks per SM of the packed polish/replay passes and of the warm-start inference
+    int block, deferred_per_sm, infer_per_sm;
 };
 
 // Warm start of a solve: features written by the classify pass at the work-list

@@ -234,8 +234,16 @@ class IntegralFields(C.Structure):
                 ("uniform_area", d)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("solve_block", i32), ("deferred_per_sm", i32), ("infer_per_sm", i32), ("two_lanes", i32),
+                ("io_overlap", i32), ("pad_", i32), ("step_ms", d)]
+
+
+TUNING_FIELDS = ("solve_block", "deferred_per_sm", "infer_per_sm", "two_lanes", "io_overlap")
+
+
 # Order of nesf_struct_sizes(): must match the library.
 STRUCTS_IN_SIZE_ORDER = (Grid, ThermodynamicsParameters, StabilityFunction, RoughnessLength,
                          SimilarityTheoryFluxesC, InterfaceParams, SolverOptions, Stats, AOFields,
                          AIFields, IOParams, IOFields, AtmosGrid, ExchangeCoords, InterpFields,
-                         AssemblyParams, AssemblyFields, CouplingStepArgs, IntegralFields)
+                         AssemblyParams, AssemblyFields, CouplingStepArgs, IntegralFields, Tuning)

@@ -62,6 +62,9 @@ SIGNATURES = {
     "nesf_graph_set_time_weight": (C.c_int, [vp, C.c_double]),
     "nesf_graph_launch": (C.c_int, [vp, vp]),
     "nesf_graph_destroy": (C.c_int, [vp]),
+    "nesf_set_tuning": (C.c_int, [vp, P(A.Tuning)]),
+    "nesf_get_tuning": (C.c_int, [vp, P(A.Tuning)]),
+    "nesf_autotune": (C.c_int, [vp, P(A.CouplingStepArgs), P(A.SolverOptions), C.c_int32, P(A.Tuning), vp]),
 }
 
 

@@ -311,6 +311,45 @@ def coupling_step(step, precision="f32_adaptive", ctx=None, stream=None, mlp=Non
     check(lib.nesf_coupling_step(ctx.handle, C.byref(step.args), C.byref(o), _stream_handle(stream)))
 
 
+def get_tuning(ctx=None):
+    """The context's launch shapes and schedule (nesf_get_tuning) as a dict."""
+    lib = load()
+    ctx = ctx or default_context()
+    t = A.Tuning()
+    check(lib.nesf_get_tuning(ctx.handle, C.byref(t)))
+    out = {k: int(getattr(t, k)) for k in A.TUNING_FIELDS}
+    out["step_ms"] = float(t.step_ms)
+    return out
+
+
+def set_tuning(ctx=None, **fields):
+    """Set fields of the context's tuning (nesf_set_tuning); the others keep their values."""
+    lib = load()
+    ctx = ctx or default_context()
+    cur = get_tuning(ctx)
+    unknown = set(fields) - set(A.TUNING_FIELDS)
+    if unknown:
+        raise ValueError(f"unknown tuning fields {sorted(unknown)}")
+    cur.update(fields)
+    t = A.Tuning(**{k: int(cur[k]) for k in A.TUNING_FIELDS})
+    check(lib.nesf_set_tuning(ctx.handle, C.byref(t)))
+    return get_tuning(ctx)
+
+
+def autotune(step, precision="f32_adaptive", reps=5, ctx=None, stream=None, mlp=None):
+    """Coordinate search of the context's tuning on one coupling step (nesf_autotune); returns
+    the chosen tuning (a dict with its mean step time, step_ms). The steps run for real."""
+    lib = load()
+    o = solver_options(precision, mlp=mlp)
+    ctx = ctx or default_context()
+    t = A.Tuning()
+    check(lib.nesf_autotune(ctx.handle, C.byref(step.args), C.byref(o), int(reps), C.byref(t),
+                            _stream_handle(stream)))
+    out = {k: int(getattr(t, k)) for k in A.TUNING_FIELDS}
+    out["step_ms"] = float(t.step_ms)
+    return out
+
+
 class Graph:
     """A captured CUDA graph of one coupling step (nesf_graph_capture)."""
 

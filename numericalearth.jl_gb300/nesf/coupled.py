@@ -171,6 +171,13 @@ class CoupledModel:
         api.coupling_step(self.step_args(), precision, stream=stream, mlp=self.mlp)
         return self.kernels_per_step(precision, native=True)
 
+    def autotune(self, precision="f32_adaptive", reps=5):
+        """Tune the default context's launch shapes and schedule on this model's step
+        (nesf_autotune). The steps run for real; the state is reset afterwards."""
+        t = api.autotune(self.step_args(), precision, reps=reps, mlp=self.mlp)
+        self.reset()
+        return t
+
     def capture(self, precision="f32_adaptive"):
         """Capture one coupling step as a CUDA graph (nesf_graph_capture)."""
         self.graph = api.Graph(self.step_args(), precision, mlp=self.mlp)

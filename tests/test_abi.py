@@ -83,3 +83,13 @@ def test_argument_errors_without_gpu():
 def test_network_blob_layout_matches_binding():
     lib = _lib.load()
     assert lib.nesf_mlp_bytes() == C.sizeof(A.MlpBlob)
+
+
+@pytest.mark.parametrize("field,value", [("solve_block", 48), ("solve_block", 160), ("deferred_per_sm", 17),
+                                         ("infer_per_sm", -1), ("two_lanes", 2), ("io_overlap", -1)])
+def test_tuning_out_of_range_is_an_argument_error(field, value):
+    """nesf_set_tuning checks its fields before it touches a device."""
+    lib = _lib.load()
+    t = A.Tuning(**{field: value})
+    assert lib.nesf_set_tuning(None, C.byref(t)) == A.NESF_ERR_ARG
+    assert field in lib.nesf_last_error().decode()

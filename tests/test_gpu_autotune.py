@@ -1,0 +1,95 @@
+"""The autotuner (nesf_autotune) and the tunings it chooses between: every launch
+shape and schedule gives bit-identical outputs (the cells' arithmetic does not
+depend on them), and the search sets a valid, timed tuning on the context."""
+import numpy as np
+import pytest
+
+from helpers import to_numpy
+from nesf import api
+from nesf import fields as F
+from nesf import synthetic as syn
+from nesf.coupled import CoupledModel, ICE_NET, OCEAN_NET, RAD_DIAG
+
+pytestmark = pytest.mark.gpu
+
+DEFAULT = dict(solve_block=128, deferred_per_sm=4, infer_per_sm=4, two_lanes=1, io_overlap=1)
+
+
+@pytest.fixture(scope="module")
+def model():
+    st = syn.coupled(seed=43, nx=240, ny=120, lat_s=-80, lat_n=80, land=0.3, interpolate=True)
+    m = CoupledModel(st)
+    yield m
+    api.set_tuning(**DEFAULT)
+
+
+def outputs(m):
+    import torch
+    torch.cuda.synchronize()
+    out = {("ao", k): to_numpy(m.ao[k]).copy() for k in F.AO_OUTPUTS}
+    out.update({("ai", k): to_numpy(m.ai[k]).copy() for k in F.AI_OUTPUTS})
+    out[("ai", "interface_temperature")] = to_numpy(m.ai["interface_temperature"]).copy()
+    out.update({("io", k): to_numpy(m.io[k]).copy() for k in F.IO_OUTPUTS})
+    out.update({("net", k): to_numpy(m.net[k]).copy() for k in OCEAN_NET + ICE_NET + RAD_DIAG})
+    out[("x", "T_oc")] = to_numpy(m.x["T_oc"]).copy()
+    return out
+
+
+def step(m, precision, **tuning):
+    api.set_tuning(**{**DEFAULT, **tuning})
+    m.reset()
+    m.native_step(precision)
+    return outputs(m)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32", "f32_adaptive"])
+def test_every_tuning_gives_the_same_outputs(model, precision):
+    ref = step(model, precision)
+    for tuning in (dict(solve_block=32), dict(solve_block=64, deferred_per_sm=16), dict(deferred_per_sm=1),
+                   dict(two_lanes=0), dict(io_overlap=0), dict(two_lanes=0, io_overlap=0, solve_block=96)):
+        got = step(model, precision, **tuning)
+        for k in ref:
+            assert np.array_equal(ref[k], got[k], equal_nan=True), (precision, tuning, k)
+
+
+def test_warm_start_inference_grid(model):
+    from nesf.warm import WarmStartNetwork
+    model.mlp = WarmStartNetwork(seed=3)
+    try:
+        ref = step(model, "f32_adaptive")
+        for n in (1, 2, 8):
+            got = step(model, "f32_adaptive", infer_per_sm=n)
+            for k in ref:
+                assert np.array_equal(ref[k], got[k], equal_nan=True), (n, k)
+    finally:
+        model.mlp = None
+
+
+def test_autotune_sets_a_valid_tuning(model):
+    api.set_tuning(**DEFAULT)
+    model.reset()
+    model.native_step("f32_adaptive")
+    ref = outputs(model)
+    t = model.autotune("f32_adaptive", reps=2)
+    assert t["step_ms"] > 0
+    assert t["solve_block"] in (32, 64, 96, 128) and 1 <= t["deferred_per_sm"] <= 16
+    assert t["two_lanes"] in (0, 1) and t["io_overlap"] in (0, 1)
+    cur = api.get_tuning()
+    assert {k: cur[k] for k in DEFAULT} == {k: t[k] for k in DEFAULT}
+    model.reset()
+    model.native_step("f32_adaptive")
+    got = outputs(model)
+    for k in ref:
+        assert np.array_equal(ref[k], got[k], equal_nan=True), k
+
+
+def test_graph_keeps_its_tuning(model):
+    """A graph captured under one tuning replays it after the context's tuning changes."""
+    ref = step(model, "f32_adaptive", two_lanes=0)
+    model.capture("f32_adaptive")
+    api.set_tuning(**DEFAULT)
+    model.reset()
+    model.graph_step()
+    got = outputs(model)
+    for k in ref:
+        assert np.array_equal(ref[k], got[k], equal_nan=True), k
