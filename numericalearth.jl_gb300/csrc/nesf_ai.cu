@@ -20,6 +20,7 @@ __device__ __forceinline__ void ai_load(const DevIface<double>& P, const AIArgs<
     c.hi = ld(a.hi, k);
     c.hs = ldz(a.hs, k);
     c.hc = ld(a.hc, k);
+    c.Rth = conductive_resistance(P, c.hs, c.hi);
     aleph = ld(a.aleph, k);
     Ts0 = ld(a.Ts, k) + P.off_ifc;
     c.sw = ldz(a.sw, k);
@@ -74,6 +75,7 @@ __device__ __forceinline__ void ai_load_fast(const DevIface<double>& P, const De
         c.hi = ldf(a.hi, k);
         c.hs = a.hs ? ldf(a.hs, k) : 0.0f;
         c.hc = ldf(a.hc, k);
+        c.Rth = conductive_resistance(Pf, c.hs, c.hi);
         c.kappa = -1.0f;
         f.anc = skin_anchor(P, f.tha, ld(a.To, k) + P.off_int, ld(a.So, k), qa, ld(a.pa, k), ldz(a.sw, k),
                             ldz(a.lw, k));

@@ -22,6 +22,7 @@ __device__ __forceinline__ void ao_load(const DevIface<double>& P, const AOArgs<
     c.Ti = ld(a.To, k) + P.off_int;
     c.Si = ld(a.So, k);
     c.hi = c.hs = c.hc = 0;
+    c.Rth = 0;
     c.sw = ldz(a.sw, k);
     c.lw = ldz(a.lw, k);
     c.kappa = a.kappa ? ld(a.kappa, k) : -1.0;
@@ -93,7 +94,7 @@ __device__ __forceinline__ void ao_load_fast(const DevIface<double>& P, const De
         c.cp_a = cp_m(Pf, c.qa);
         c.L_s = latent_heat_sublim(Pf, c.Ta);
         c.kappa = a.kappa ? ldf(a.kappa, k) : -1.0f;
-        c.hi = c.hs = c.hc = 0.0f;
+        c.hi = c.hs = c.hc = c.Rth = 0.0f;
         f.anc = skin_anchor(P, f.tha, f.Ts0, ld(a.So, k), qa, ld(a.pa, k), ldz(a.sw, k), ldz(a.lw, k));
     } else {
         fast_surface(P, Pf, Ta, qa, ld(a.pa, k), lift, f.Ts0, f.s);

@@ -3,9 +3,13 @@
 // Everything here is templated on the compute type R (double for the drop-in
 // FP64 solver and the polish step, float for the FP32 sweep). The formulas
 // restate NumericalEarth.jl v0.6.2 (paths below are inside that project) and
-// keep its left-to-right operation order; hoisted quantities are the ones the
-// reference recomputes every iteration from unchanged inputs, so hoisting them
-// does not change a result.
+// keep its operation order, with three kinds of exception, each moving a value
+// by about an ulp (the FP64 path stays within 1e-12 of the reference): quantities
+// the reference recomputes from unchanged inputs (every iteration, or every call
+// of a stability function) are computed once; a division by such a quantity is a
+// multiplication by its reciprocal; pow(x, y) is exp(y log x) and sums of logs
+// are the log of a product. On GB300 a dependent FP64 division costs ~640
+// cycles, log ~2.1k, atan ~1.9k and pow ~5.8k (an FMA 66).
 #pragma once
 
 #include <cstdint>
@@ -53,9 +57,16 @@ template <> struct M<float> {
 };
 
 // --------------------------------------------------------- device parameters
+// c: the coefficients (nesf_stability_function); k: constants derived from them on
+// the host, which the reference recomputes at every call (make_dev_iface):
+//   Edson (both):  1/B-, E-/2, 1/E-, sqrt(E-), 1/sqrt(E-)
+//   SHEBA momentum: B = cbrt((1-b)/b), -3a/b, aB/(2b), 1/(1+B), 1/(1-B+B^2),
+//                   1/(sqrt3 B), 2 sqrt3, atan((2-B)/(sqrt3 B))
+//   SHEBA scalar:  -b/2, bc/(2B) - a/B, c-B, c+B, log((c-B)/(c+B)) with B = sqrt(c^2-4)
 template <class R> struct DevStab {
     int32_t kind;
     R c[12];
+    R k[8];
 };
 
 template <class R> struct DevRough {
@@ -93,19 +104,21 @@ template <class R> struct DevIface {
 // Thermodynamics.jl restatements (saturation_vapor_pressure, air_density, cp_m,
 // latent heats, virtual temperature) with the parameter set of
 // src/Atmospheres/thermodynamic_parameters.jl.
+
+// saturation_vapor_pressure, e_sat = p_tr (T / T_tr)^A exp(K (1 / T_tr - 1 / T))
+// (docs/src/interface_fluxes.md:86-97, A = (cp_v - cp_c) / R_v, K = (L_0 - (cp_v -
+// cp_c) T_0) / R_v for the interface's phase). The FP64 iterations keep this
+// two-factor form: q_a - q_s(T_s) can cancel, and the difference multiplies the
+// rounding of e_sat by q_s / (q_a - q_s).
 template <class R>
-__device__ __forceinline__ R esat(const DevIface<R>& P, R T, int phase) {
-    R LH0 = phase == NESF_PHASE_ICE ? P.Ls0 : P.Lv0;
-    R cpc = phase == NESF_PHASE_ICE ? P.cpi : P.cpl;
-    R dcp = P.cpv - cpc;
-    return P.ptr * M<R>::pow(T / P.Ttr, dcp / P.Rv) *
-           M<R>::exp((LH0 - dcp * P.T0) / P.Rv * (R(1) / P.Ttr - R(1) / T));
+__device__ __forceinline__ R esat(const DevIface<R>& P, R T) {
+    return P.ptr * M<R>::pow(T / P.Ttr, P.esA) * M<R>::exp(P.esK * (R(1) / P.Ttr - R(1) / T));
 }
 
-// The same saturation vapour pressure as one exponential, p_tr exp(esA ln(T / T_tr) +
-// esK (T - T_tr) / (T_tr T)): an exp and a log in place of pow and exp, equal to esat
-// within a few ulps. The FP32 solvers' FP64 anchors use it; the FP64 iterations that
-// follow the reference's operation order use esat.
+// The same as one exponential, p_tr exp(A ln(T / T_tr) + K (T - T_tr) / (T_tr T)):
+// a log and an exp in place of pow and exp (FP64 pow costs ~5.8k cycles per
+// dependent call on this GPU, log + exp ~3k), within a few ulps of esat. The FP32
+// solvers' FP64 anchors use it (their own rounding is ~1e-7).
 template <class R>
 __device__ __forceinline__ R esat_exp(const DevIface<R>& P, R T) {
     return P.ptr * M<R>::exp(P.esA * M<R>::log(T * P.inv_Ttr) + P.esK * ((T - P.Ttr) * P.inv_Ttr) / T);
@@ -131,18 +144,10 @@ template <class R> __device__ __forceinline__ R virtual_temperature(const DevIfa
 }
 
 // surface_specific_humidity(::ImpureSaturationSpecificHumidity)
-// (InterfaceComputations/interface_states.jl:55-74)
-template <class R>
+// (InterfaceComputations/interface_states.jl:55-74); EXP: e_sat from esat_exp.
+template <class R, bool EXP = false>
 __device__ __forceinline__ R surface_specific_humidity(const DevIface<R>& P, R pa, R Ts) {
-    R pv = P.x * esat(P, Ts, P.phase);
-    pv = M<R>::fmin(pv, R(0.999) * pa);
-    return P.einv * pv / (pa - (R(1) - P.einv) * pv);
-}
-
-// surface_specific_humidity with esat_exp (the FP32 solvers' anchors).
-template <class R>
-__device__ __forceinline__ R surface_specific_humidity_exp(const DevIface<R>& P, R pa, R Ts) {
-    R pv = P.x * esat_exp(P, Ts);
+    R pv = P.x * (EXP ? esat_exp(P, Ts) : esat(P, Ts));
     pv = M<R>::fmin(pv, R(0.999) * pa);
     return P.einv * pv / (pa - (R(1) - P.einv) * pv);
 }
@@ -158,68 +163,71 @@ __device__ __forceinline__ R surface_atmosphere_temperature(const DevIface<R>& P
 // similarity_theory_turbulent_fluxes.jl. The reference evaluates both branches
 // and selects with ifelse(zeta < 0, ...); here only the selected branch is
 // evaluated, which gives the same value.
-template <class R>
-__device__ __noinline__ R psi_edson_momentum(const DevStab<R> s, R z) {   // :501-532
-    const R* c = s.c;
-    if (z < R(0)) {
-        R Am = c[5], Bm = c[6], Cm = c[7], Dm = c[8], Em = c[9], Fm = c[10];
-        R zm = M<R>::fmin(R(0), z);
+// Division by a coefficient is multiplication by its host-derived reciprocal, sums
+// of logarithms are the logarithm of a product, and pow is exp(y log x): each
+// moves a result by about an ulp, and the FP64 division, log, atan and pow they
+// save cost 0.6k-5.8k cycles per dependent call.
+
+// Convective branch (zeta < 0) of Edson's momentum (MOM) and scalar functions:
+// (1 - f) psi1 + f psi2, f = zeta^2 / (1 + zeta^2).
+template <class R, bool MOM>
+__device__ __noinline__ R psi_edson_unstable(R Am, R Bm, R iBm, R Cm, R Dm, R hEm, R iEm, R sE, R isE, R Fm,
+                                             R z) {
+    R zm = M<R>::fmin(R(0), z);
+    R psi1;
+    if (MOM) {
         R f1 = M<R>::sqrt(M<R>::sqrt(R(1) - Am * zm));
-        R psi1 = Bm * M<R>::log((R(1) + f1) / Bm) + M<R>::log((R(1) + f1 * f1) / Bm) - Bm * M<R>::atan(f1) + Cm;
-        R f2 = M<R>::cbrt(R(1) - Dm * zm);
-        R sE = M<R>::sqrt(Em);
-        R psi2 = Em / R(2) * M<R>::log((R(1) + f2 + f2 * f2) / Em) - sE * M<R>::atan((R(1) + R(2) * f2) / sE) + Fm;
-        R f = zm * zm / (R(1) + zm * zm);
-        return (R(1) - f) * psi1 + f * psi2;
+        psi1 = Bm * M<R>::log((R(1) + f1) * iBm) + M<R>::log((R(1) + f1 * f1) * iBm) - Bm * M<R>::atan(f1) + Cm;
     } else {
-        R zmax = c[0], Ap = c[1], Bp = c[2], Cp = c[3], Dp = c[4];
-        R zp = M<R>::fmax(R(0), z);
-        R dz = M<R>::fmin(zmax, Ap * zp);
-        return -Bp * zp - Cp * (zp - Dp) * M<R>::exp(-dz) - Cp * Dp;
-    }
-}
-
-template <class R>
-__device__ __noinline__ R psi_edson_scalar(const DevStab<R> s, R z) {     // :586-618
-    const R* c = s.c;
-    if (z < R(0)) {
-        R Am = c[6], Bm = c[7], Cm = c[8], Dm = c[9], Em = c[10], Fm = c[11];
-        R zm = M<R>::fmin(R(0), z);
         R f1 = M<R>::sqrt(R(1) - Am * zm);
-        R psi1 = Bm * M<R>::log((R(1) + f1) / Bm) + Cm;
-        R f2 = M<R>::cbrt(R(1) - Dm * zm);
-        R sE = M<R>::sqrt(Em);
-        R psi2 = Em / R(2) * M<R>::log((R(1) + f2 + f2 * f2) / Em) - sE * M<R>::atan((R(1) + R(2) * f2) / sE) + Fm;
-        R f = zm * zm / (R(1) + zm * zm);
-        return (R(1) - f) * psi1 + f * psi2;
-    } else {
-        R zmax = c[0], Ap = c[1], Bp = c[2], Cp = c[3], Dp = c[4], Ep = c[5];
-        R zp = M<R>::fmax(R(0), z);
-        R dz = M<R>::fmin(zmax, Ap * zp);
-        return -M<R>::pow(R(1) + Bp * zp, Cp) - Bp * (zp - Dp) * M<R>::exp(-dz) - Ep;
+        psi1 = Bm * M<R>::log((R(1) + f1) * iBm) + Cm;
     }
+    R f2 = M<R>::cbrt(R(1) - Dm * zm);
+    R psi2 = hEm * M<R>::log((R(1) + f2 + f2 * f2) * iEm) - sE * M<R>::atan((R(1) + R(2) * f2) * isE) + Fm;
+    R f = zm * zm / (R(1) + zm * zm);
+    return (R(1) - f) * psi1 + f * psi2;
 }
 
 template <class R>
-__device__ __noinline__ R psi_sheba_momentum(R a, R b, R z) {     // :643-657
+__device__ __forceinline__ R psi_edson_momentum(const DevStab<R>& s, R z) {   // :501-532
+    const R* c = s.c;
+    const R* k = s.k;
+    if (z < R(0)) return psi_edson_unstable<R, true>(c[5], c[6], k[0], c[7], c[8], k[1], k[2], k[3], k[4], c[10], z);
+    R zmax = c[0], Ap = c[1], Bp = c[2], Cp = c[3], Dp = c[4];
+    R zp = M<R>::fmax(R(0), z);
+    R dz = M<R>::fmin(zmax, Ap * zp);
+    return -Bp * zp - Cp * (zp - Dp) * M<R>::exp(-dz) - Cp * Dp;
+}
+
+template <class R>
+__device__ __forceinline__ R psi_edson_scalar(const DevStab<R>& s, R z) {     // :586-618
+    const R* c = s.c;
+    const R* k = s.k;
+    if (z < R(0)) return psi_edson_unstable<R, false>(c[6], c[7], k[0], c[8], c[9], k[1], k[2], k[3], k[4], c[11], z);
+    R zmax = c[0], Ap = c[1], Bp = c[2], Cp = c[3], Dp = c[4], Ep = c[5];
+    R zp = M<R>::fmax(R(0), z);
+    R dz = M<R>::fmin(zmax, Ap * zp);
+    R x = R(1) + Bp * zp;
+    R xC = Cp == R(1.5) ? x * M<R>::sqrt(x) : M<R>::exp(Cp * M<R>::log(x));   // x^Cp
+    return -xC - Bp * (zp - Dp) * M<R>::exp(-dz) - Ep;
+}
+
+template <class R>
+__device__ __noinline__ R psi_sheba_momentum(const R* k, R z) {     // :643-657
     R zp = M<R>::fmax(R(0), z);
     R x = M<R>::cbrt(R(1) + zp);
-    R B = M<R>::cbrt((R(1) - b) / b);
-    R rt3 = M<R>::sqrt(R(3));
-    R P1 = -R(3) * a * (x - R(1)) / b;
-    R P2 = a * B / (R(2) * b) *
-           (R(2) * M<R>::log((x + B) / (R(1) + B)) - M<R>::log((x * x - B * x + B * B) / (R(1) - B + B * B)) +
-            R(2) * rt3 * (M<R>::atan((R(2) * x - B) / (rt3 * B)) - M<R>::atan((R(2) - B) / (rt3 * B))));
+    R B = k[0];
+    R P1 = k[1] * (x - R(1));
+    R u = (x + B) * k[3], v = (x * x - B * x + B * B) * k[4];
+    R P2 = k[2] * (M<R>::log(u * u / v) + k[6] * (M<R>::atan((R(2) * x - B) * k[5]) - k[7]));
     return P1 + P2;
 }
 
 template <class R>
-__device__ __noinline__ R psi_sheba_scalar(R a, R b, R c, R z) {  // :665-677
-    R B = M<R>::sqrt(c * c - R(4));
+__device__ __noinline__ R psi_sheba_scalar(R c, const R* k, R z) {  // :665-677
     R zp = M<R>::fmax(R(0), z);
-    R P1 = -b / R(2) * M<R>::log(R(1) + c * zp + zp * zp);
-    R P2 = (b * c / (R(2) * B) - a / B) *
-           (M<R>::log((R(2) * zp + c - B) / (R(2) * zp + c + B)) - M<R>::log((c - B) / (c + B)));
+    R P1 = k[0] * M<R>::log(R(1) + c * zp + zp * zp);
+    R P2 = k[1] * (M<R>::log((R(2) * zp + k[2]) / (R(2) * zp + k[3])) - k[4]);
     return P1 + P2;
 }
 
@@ -227,17 +235,17 @@ template <class R>
 __device__ __noinline__ R psi_paulson_momentum(R a, R b, R z) {   // :688-699
     R zm = M<R>::fmin(R(0), z);
     R x = M<R>::sqrt(M<R>::sqrt(R(1) - a * zm));
-    R P1 = R(2) * M<R>::log((R(1) + x) / R(2));
-    R P2 = M<R>::log((R(1) + x * x) / R(2));
+    R u = (R(1) + x) * R(0.5);
+    R P12 = M<R>::log(u * u * ((R(1) + x * x) * R(0.5)));   // 2 log(u) + log((1 + x^2) / 2)
     R P3 = -R(2) * M<R>::atan(x);
-    return P1 + P2 + P3 + b;
+    return P12 + P3 + b;
 }
 
 template <class R>
 __device__ __noinline__ R psi_paulson_scalar(R a, R z) {          // :705-710
     R zm = M<R>::fmin(R(0), z);
     R x = M<R>::sqrt(M<R>::sqrt(R(1) - a * zm));
-    return R(2) * M<R>::log((R(1) + x * x) / R(2));
+    return R(2) * M<R>::log((R(1) + x * x) * R(0.5));
 }
 
 template <class R>
@@ -255,9 +263,9 @@ __device__ __forceinline__ R stability(const DevStab<R>& s, R z) {
     case NESF_PSI_EDSON_MOMENTUM: return psi_edson_momentum(s, z);
     case NESF_PSI_EDSON_SCALAR: return psi_edson_scalar(s, z);
     case NESF_PSI_SHEBA_PAULSON_MOMENTUM:
-        return z > R(0) ? psi_sheba_momentum(c[0], c[1], z) : psi_paulson_momentum(c[2], c[3], z);
+        return z > R(0) ? psi_sheba_momentum(s.k, z) : psi_paulson_momentum(c[2], c[3], z);
     case NESF_PSI_SHEBA_PAULSON_SCALAR:
-        return z > R(0) ? psi_sheba_scalar(c[0], c[1], c[2], z) : psi_paulson_scalar(c[3], z);
+        return z > R(0) ? psi_sheba_scalar(c[2], s.k, z) : psi_paulson_scalar(c[3], z);
     case NESF_PSI_LINEAR_PAULSON_MOMENTUM:
         return z > R(0) ? psi_linear(c[0], c[1], z) : psi_paulson_momentum(c[2], c[3], z);
     case NESF_PSI_LINEAR_PAULSON_SCALAR:
@@ -266,13 +274,13 @@ __device__ __forceinline__ R stability(const DevStab<R>& s, R z) {
     }
 }
 
-// similarity_profile (:242-253)
+// similarity_profile (:242-253), with 1 / L in place of L (h / L = h * (1 / L))
 template <class R>
-__device__ __forceinline__ R similarity_profile(int form, const DevStab<R>& psi, R h, R l, R L) {
-    R zeta = h / L;
+__device__ __forceinline__ R similarity_profile(int form, const DevStab<R>& psi, R h, R l, R invL) {
+    R zeta = h * invL;
     R ph = stability(psi, zeta);
     if (form == NESF_PROFILE_COARE) return M<R>::log(h / l) - ph;
-    R pl = stability(psi, l / L);
+    R pl = stability(psi, l * invL);
     return M<R>::log(h / l) - ph + pl;
 }
 
@@ -299,7 +307,7 @@ template <class R>
 __device__ __forceinline__ R scalar_roughness(const DevRough<R>& r, R lu, R us, R nu) {
     if (r.kind == NESF_ROUGHNESS_CONSTANT) return r.value;
     R Rs = lu * us / nu;
-    R ls = Rs == R(0) ? R(0) : r.A / M<R>::pow(Rs, r.b);
+    R ls = Rs == R(0) ? R(0) : r.A * M<R>::exp(-r.b * M<R>::log(Rs));   // A / Rs^b
     return M<R>::fmin(ls, r.lmax);
 }
 
@@ -329,7 +337,15 @@ template <class R> struct CellConst {
     R du, dv, dU2;               // velocity difference and its square norm
     R tha;                       // surface_atmosphere_temperature
     R rho_a, cp_a, L_s;          // air density, cp_m, latent_heat_sublim (skin only)
+    R Rth;                       // conductive resistance h_s / k_s + h_i / k_i (ice skin only)
 };
+
+// The ice and snow layers' thermal resistance (interface_states.jl:468-524), fixed
+// over the iteration.
+template <class R>
+__device__ __forceinline__ R conductive_resistance(const DevIface<R>& P, R hs, R hi) {
+    return P.k_snow > R(0) ? hs / P.k_snow + hi / P.k_ice : hi / P.k_ice;
+}
 
 // Quantities that depend on the interface temperature.
 template <class R> struct SurfaceConst {
@@ -365,15 +381,16 @@ __device__ __forceinline__ void iterate_fluxes(const DevIface<R>& P, const CellC
     R lu = momentum_roughness(P.rough[0], us, U, s.nu_u);
     R lt = scalar_roughness(P.rough[1], lu, us, s.nu_t);
     R h = M<R>::fmax(P.h - P.d0, R(2) * lu);
-    R L = bs == R(0) ? M<R>::inf() : us * us / (P.vk * bs);
-    R chiu = P.vk / similarity_profile(P.form, P.psi[0], h, lu, L);
-    R chit = P.vk / similarity_profile(P.form, P.psi[1], h, lt, L);
+    // 1 / L, L = u*^2 / (kappa b*) (Inf when b* = 0)
+    R invL = bs == R(0) ? R(0) : (P.vk * bs) / (us * us);
+    R chiu = P.vk / similarity_profile(P.form, P.psi[0], h, lu, invL);
+    R chit = P.vk / similarity_profile(P.form, P.psi[1], h, lt, invL);
     R chiq;
     if (P.scalar_same) {
         chiq = chit;
     } else {
         R lq = scalar_roughness(P.rough[2], lu, us, s.nu_q);
-        chiq = P.vk / similarity_profile(P.form, P.psi[2], h, lq, L);
+        chiq = P.vk / similarity_profile(P.form, P.psi[2], h, lq, invL);
     }
     us_n = chiu * U;
     ts_n = chit * s.dth;
@@ -416,7 +433,7 @@ __device__ __forceinline__ R skin_temperature(const DevIface<R>& P, const CellCo
         Tst = D == R(0) ? Tm1 : Tst;
         return c.Ti + clampr(Tst - c.Ti, -P.max_dT, P.max_dT);
     }
-    R Rth = P.k_snow > R(0) ? c.hs / P.k_snow + c.hi / P.k_ice : c.hi / P.k_ice;
+    R Rth = c.Rth;
     R Tb = P.Tfw - P.slope * c.Si;
     Tb = Tb + P.off_ifc;
     R dT = Tat - Tm1;

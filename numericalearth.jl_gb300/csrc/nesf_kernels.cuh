@@ -2,11 +2,48 @@
 // conversion, array access in the Oceananigans parent layout, statistics.
 #pragma once
 
+#include <cmath>
+
 #include "nesf_device.cuh"
 
 namespace nesf {
 
 // ------------------------------------------------------------ host conversion
+// The stability functions' constants that the reference recomputes at every call
+// (DevStab::k), in FP64.
+inline void derived_stability(const nesf_stability_function& f, double* k) {
+    for (int i = 0; i < 8; i++) k[i] = 0.0;
+    const double* c = f.c;
+    if (f.kind == NESF_PSI_EDSON_MOMENTUM || f.kind == NESF_PSI_EDSON_SCALAR) {
+        const int o = f.kind == NESF_PSI_EDSON_MOMENTUM ? 5 : 6;   // A- B- C- D- E- F- from c[o]
+        double Bm = c[o + 1], Em = c[o + 4];
+        k[0] = 1.0 / Bm;
+        k[1] = Em / 2;
+        k[2] = 1.0 / Em;
+        k[3] = std::sqrt(Em);
+        k[4] = 1.0 / std::sqrt(Em);
+    } else if (f.kind == NESF_PSI_SHEBA_PAULSON_MOMENTUM) {
+        double a = c[0], b = c[1];
+        double B = std::cbrt((1 - b) / b), rt3 = std::sqrt(3.0);
+        k[0] = B;
+        k[1] = -3 * a / b;
+        k[2] = a * B / (2 * b);
+        k[3] = 1.0 / (1 + B);
+        k[4] = 1.0 / (1 - B + B * B);
+        k[5] = 1.0 / (rt3 * B);
+        k[6] = 2 * rt3;
+        k[7] = std::atan((2 - B) / (rt3 * B));
+    } else if (f.kind == NESF_PSI_SHEBA_PAULSON_SCALAR) {
+        double a = c[0], b = c[1], cc = c[2];
+        double B = std::sqrt(cc * cc - 4);
+        k[0] = -b / 2;
+        k[1] = b * cc / (2 * B) - a / B;
+        k[2] = cc - B;
+        k[3] = cc + B;
+        k[4] = std::log((cc - B) / (cc + B));
+    }
+}
+
 template <class R>
 inline DevIface<R> make_dev_iface(const nesf_interface_params& p) {
     DevIface<R> d{};
@@ -30,6 +67,9 @@ inline DevIface<R> make_dev_iface(const nesf_interface_params& p) {
     for (int n = 0; n < 3; n++) {
         d.psi[n].kind = f.stability[n].kind;
         for (int k = 0; k < 12; k++) d.psi[n].c[k] = R(f.stability[n].c[k]);
+        double kd[8];
+        derived_stability(f.stability[n], kd);
+        for (int k = 0; k < 8; k++) d.psi[n].k[k] = R(kd[k]);
         const nesf_roughness_length& r = f.roughness[n];
         DevRough<R>& q = d.rough[n];
         q.kind = r.kind; q.wave_kind = r.wave_kind; q.visc_kind = r.viscosity_kind;

@@ -98,7 +98,7 @@ __device__ __forceinline__ void convert_const(const CellConst<R>& a, CellConst<Q
     b.ui = Q(a.ui); b.vi = Q(a.vi); b.Ti = Q(a.Ti); b.Si = Q(a.Si);
     b.hi = Q(a.hi); b.hs = Q(a.hs); b.hc = Q(a.hc); b.sw = Q(a.sw); b.lw = Q(a.lw); b.kappa = Q(a.kappa);
     b.du = Q(a.du); b.dv = Q(a.dv); b.dU2 = Q(a.dU2); b.tha = Q(a.tha);
-    b.rho_a = Q(a.rho_a); b.cp_a = Q(a.cp_a); b.L_s = Q(a.L_s);
+    b.rho_a = Q(a.rho_a); b.cp_a = Q(a.cp_a); b.L_s = Q(a.L_s); b.Rth = Q(a.Rth);
 }
 
 template <class R, class Q>
@@ -185,7 +185,7 @@ __device__ __forceinline__ R skin_tau(const DevIface<R>& P, const CellConst<R>& 
         }
         return A.dTi + clampr(dev, -P.max_dT, P.max_dT);
     }
-    R Rth = P.k_snow > R(0) ? c.hs / P.k_snow + c.hi / P.k_ice : c.hi / P.k_ice;
+    R Rth = c.Rth;
     R Om = dT == R(0) ? R(0) : QT / dT;
     R beta = R(4) * (A.Iupa + dI) / (c.tha + tau);
     R D = R(1) + beta * Rth - Om * Rth;
@@ -671,7 +671,7 @@ __device__ __forceinline__ double lift_temperature(const DevIface<double>& P, do
 // the rest in FP32 from the rounded T_s and q_s.
 __device__ __forceinline__ void fast_surface(const DevIface<double>& P, const DevIface<float>& Pf, double Ta,
                                              double qa, double pa, double lift, double Ts, SurfaceConst<float>& s) {
-    double qs = surface_specific_humidity_exp(P, pa, Ts);
+    double qs = surface_specific_humidity<double, true>(P, pa, Ts);
     s.Ts = (float)Ts;
     s.qs = (float)qs;
     s.dth = (float)((Ta - Ts) + lift);
