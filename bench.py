@@ -223,6 +223,25 @@ def time_steps(model, precision, steps, warmup, world):
     return ms, launches
 
 
+def step_timeline(model, precision):
+    """Kernel-boundary timeline of one replay of the step's graph (nesf_trace_*): per kernel
+    its stream and its end (and, after the first kernel of its stream, start) in ms."""
+    import torch
+    from nesf import api
+    api.trace_enable(True)
+    try:
+        model.capture(precision)
+        model.reset()
+        model.graph_step()
+        torch.cuda.synchronize()
+        marks = api.trace_read()
+    finally:
+        api.trace_enable(False)
+        model.capture(precision)
+    r = lambda x: None if x is None else round(x, 3)
+    return [{"kernel": n, "stream": s, "start_ms": r(b), "end_ms": r(e)} for n, s, b, e in api.timeline(marks)]
+
+
 def error_stats(model, precision):
     """Max / p99 relative error of the fast solver against the plain FP64 solver on the full step
     outputs (normalised by max(|ref|, 1e-6 max|ref|)), over the cells where the plain solver
@@ -429,6 +448,7 @@ def main():
             "phases_ms": phases}
     if rank == 0:
         line["speedup_vs_plain_f64"] = ms_plain / ms
+        line["timeline"] = step_timeline(model, prec)
         model.reset()
         s_ao, s_ai = model.compute_fluxes(prec, stats=True)
         model.reset()

@@ -616,6 +616,25 @@ int nesf_get_tuning(nesf_context* ctx, nesf_tuning* tuning);
 int nesf_autotune(nesf_context* ctx, const nesf_coupling_step_args* args, const nesf_solver_options* opts,
                   int32_t reps, nesf_tuning* out, void* stream);
 
+/* ---------------------------------------------------------------- tracing
+ * Kernel-boundary timeline of the coupling step: with tracing on, each
+ * nesf_coupling_step (or a graph captured from one) records a CUDA event at its
+ * start and after each kernel on the stream that ran it. nesf_trace_read returns,
+ * for the last step (or replay) the device has finished, each mark's name, its
+ * stream (0 the caller's, then the others in order of first use) and its time in
+ * ms since the start mark; up to NESF_TRACE_MAX marks. Tracing adds no host
+ * synchronisation to the step; reading waits for the marks. */
+#define NESF_TRACE_MAX 64
+typedef struct {
+    char name[32];
+    int32_t stream;
+    int32_t pad_;
+    double t_ms;
+} nesf_trace_entry;
+
+int nesf_trace_enable(nesf_context* ctx, int32_t on);
+int nesf_trace_read(nesf_context* ctx, nesf_trace_entry* entries, int32_t max, int32_t* count);
+
 #ifdef __cplusplus
 }
 #endif

@@ -256,12 +256,12 @@ __global__ void __launch_bounds__(128) ai_kernel(AIArgs<S> a, DevIface<double> P
     if (stats) stats_add(stats, true, true, iters, nonconv, f64it > 0, f64it, false, fallback);
 }
 
-// Pass 1b (ADAPTIVE): the cells whose FP32 result was not kept, packed, through the
-// FP32 sweep + FP64 Newton polish; those that need it go on to the replay. The
+// Pass 1b (ADAPTIVE): the cells whose FP32 result was not kept, packed, through pass
+// 1's FP32 sweep + FP64 Newton polish; those that need it go on to the replay. The
 // initial interface temperature is still in a.Ts: pass 1 did not write these cells.
 template <class S, bool SKIN>
 __global__ void __launch_bounds__(128) ai_polish_kernel(AIArgs<S> a, DevIface<double> P, DevIface<float> P32,
-                                                        SolveOpts so, ReplayQueue rq, DevStats* stats) {
+                                                        SolveOpts so, ReplayQueue rq, int rpart, DevStats* stats) {
     const int nxr = a.L.nx + 2;
     const unsigned n = rq.count[1];
     for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n && (int64_t)q < rq.capacity;
@@ -270,17 +270,28 @@ __global__ void __launch_bounds__(128) ai_polish_kernel(AIArgs<S> a, DevIface<do
         int64_t r = id;
         int i = (int)(r % nxr), j = (int)(r / nxr);
         int64_t k = a.L.at(i, j);
+        // pass 1's sweep (the same inputs, start and strict stopping rule: the same
+        // decisions), then the FP64 Newton steps with the reference's FP64 cell constants
+        Fast32 f;
+        ai_load_fast<S, SKIN>(P, P32, a, k, f);
+        float x[4] = {1e-4f, 1e-4f, 1e-4f, SKIN ? (float)(f.Ts0 - f.tha) : 0.0f};
+        float J[SKIN ? 4 : 3][SKIN ? 4 : 3];
+        float rho;
+        int f32it = 0, f64it = 0, reason = -1;
+        int outcome = sweep_fp32<SKIN, false, true>(P32, f.c, f.s, f.anc, x, so, f32it, reason, J, rho, nullptr,
+                                                    nullptr);
         CellConst<double> c;
-        double aleph, Ts0;
-        bool land;
-        ai_load(P, a, k, c, aleph, Ts0, land);
         SurfaceConst<double> s{};
-        if (SKIN) s.Ts = Ts0;
-        else surface_const(P, c, Ts0, surface_specific_humidity(P, c.pa, Ts0), s);
-        double us = 1e-4, ts = 1e-4, qst = 1e-4;
-        int f32it, f64it, reason = -1;
-        int outcome = solve_fast<SKIN>(P, P32, c, s, us, ts, qst, so, f32it, f64it, reason);
-        replay_push(rq, outcome == FAST_REPLAY, id);
+        double us = 0, ts = 0, qst = 0;
+        if (outcome != FAST_REPLAY) {
+            double aleph, Ts0;
+            bool land;
+            ai_load(P, a, k, c, aleph, Ts0, land);
+            if (SKIN) s.Ts = Ts0;
+            else surface_const(P, c, Ts0, surface_specific_humidity(P, c.pa, Ts0), s);
+            outcome = newton_fp64<SKIN>(P, c, s, x, J, rho, so, us, ts, qst, f64it, reason);
+        }
+        replay_push(rq, outcome == FAST_REPLAY, id, rpart);
         if (outcome == FAST_REPLAY) {
             if (stats) {
                 stats_add(stats, false, false, 0, false, false, 0, true, false);
@@ -296,13 +307,13 @@ __global__ void __launch_bounds__(128) ai_polish_kernel(AIArgs<S> a, DevIface<do
 // Pass 2: the queued cells, packed, through the reference's FP64 iteration. The
 // initial interface temperature is still in a.Ts: pass 1 did not write these cells.
 template <class S>
-__global__ void __launch_bounds__(128) ai_replay_kernel(AIArgs<S> a, DevIface<double> P, ReplayQueue rq,
+__global__ void __launch_bounds__(128) ai_replay_kernel(AIArgs<S> a, DevIface<double> P, ReplayQueue rq, int part,
                                                         DevStats* stats) {
     const int nxr = a.L.nx + 2;
-    const unsigned n = rq.count[0];
+    const unsigned n = rq.count[part];
     for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n && (int64_t)q < rq.capacity;
          q += gridDim.x * blockDim.x) {
-        int64_t r = rq.idx[q];
+        int64_t r = rq.idx[(int64_t)part * rq.capacity + q];
         int i = (int)(r % nxr), j = (int)(r / nxr);
         int64_t k = a.L.at(i, j);
         CellConst<double> c;
@@ -321,7 +332,7 @@ __global__ void __launch_bounds__(128) ai_replay_kernel(AIArgs<S> a, DevIface<do
 template <class S>
 static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                                SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws,
-                               DevStats* stats, cudaStream_t stream, cudaEvent_t after_solve) {
+                               DevStats* stats, cudaStream_t stream, cudaEvent_t after_solve, const TailLane* tail) {
     const int64_t ring = (int64_t)(a.L.nx + 2) * (a.L.ny + 2);
     const int block = so.block;   // <= 128: the kernels are compiled with __launch_bounds__(128)
     dim3 grid((unsigned)((ring + block - 1) / block));
@@ -332,13 +343,15 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     // iteration count is set by the temperature's clamped steps, which the network does not predict
     const bool warm = ws.mlp != nullptr && prec != NESF_PLAIN_F64 && P64.temp_form == NESF_BULK_TEMPERATURE;
     cudaError_t e = cudaMemsetAsync(wl.count, 0, sizeof(unsigned) * 2, stream);
-    if (e == cudaSuccess && prec != NESF_PLAIN_F64) e = cudaMemsetAsync(rq.count, 0, 2 * sizeof(unsigned), stream);
+    if (e == cudaSuccess && prec != NESF_PLAIN_F64) e = cudaMemsetAsync(rq.count, 0, 3 * sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
     ai_classify_kernel<S><<<grid, block, 0, stream>>>(a, P64, P32, wl, warm ? ws.feat : nullptr, stats);
+    trace_mark(so.tracer, "ai_classify", stream);
     if (warm) {
         e = mlp_pass((void*)ws.mlp, ws.feat, nullptr, ws.guess, 0, wl.count, wl.per_member, so.infer_per_sm * sms,
                      true, stream);
         if (e != cudaSuccess) return e;
+        trace_mark(so.tracer, "ai_warm_start_inference", stream);
     }
     const float* guess = warm ? ws.guess : nullptr;
     // the adaptive pass 1 keeps FP32 results up to fp32_rho; fp32_rho = 0 keeps none: the
@@ -353,29 +366,46 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
 #undef NESF_AI_SKIN
 #undef NESF_AI_LAUNCH
     e = cudaGetLastError();
+    trace_mark(so.tracer, "ai_pass1", stream);
     if (e == cudaSuccess && after_solve) e = cudaEventRecord(after_solve, stream);
     if (e != cudaSuccess || prec == NESF_PLAIN_F64) return e;
-    if (adaptive) {
-        if (skin)
-            ai_polish_kernel<S, true><<<(unsigned)(sms * so.deferred_per_sm), 128, 0, stream>>>(a, P64, P32, so, rq, stats);
-        else
-            ai_polish_kernel<S, false><<<(unsigned)(sms * so.deferred_per_sm), 128, 0, stream>>>(a, P64, P32, so, rq, stats);
-        e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
+    const unsigned g2 = (unsigned)(sms * so.deferred_per_sm);
+    if (!adaptive) {
+        ai_replay_kernel<S><<<g2, 128, 0, stream>>>(a, P64, rq, 0, stats);
+        trace_mark(so.tracer, "ai_replay", stream);
+        return cudaGetLastError();
     }
-    ai_replay_kernel<S><<<(unsigned)(sms * so.deferred_per_sm), 128, 0, stream>>>(a, P64, rq, stats);
-    return cudaGetLastError();
+    // pass 1's replays (part 0) beside the polish pass, whose own replays (part 2) follow it
+    cudaStream_t rs = stream;
+    if (tail && tail->stream) {
+        if ((e = cudaEventRecord(tail->fork, stream)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(tail->stream, tail->fork, 0)) != cudaSuccess) return e;
+        rs = tail->stream;
+    }
+    ai_replay_kernel<S><<<g2, 128, 0, rs>>>(a, P64, rq, 0, stats);
+    trace_mark(so.tracer, "ai_replay", rs);
+    if (skin) ai_polish_kernel<S, true><<<g2, 128, 0, stream>>>(a, P64, P32, so, rq, 2, stats);
+    else ai_polish_kernel<S, false><<<g2, 128, 0, stream>>>(a, P64, P32, so, rq, 2, stats);
+    trace_mark(so.tracer, "ai_polish", stream);
+    ai_replay_kernel<S><<<g2, 128, 0, stream>>>(a, P64, rq, 2, stats);
+    trace_mark(so.tracer, "ai_polish_replay", stream);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (rs != stream) {
+        if ((e = cudaEventRecord(tail->join, rs)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(stream, tail->join, 0)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_ai(const AIArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream, cudaEvent_t after_solve) {
-    return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream, after_solve);
+                      cudaStream_t stream, cudaEvent_t after_solve, const TailLane* tail) {
+    return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream, after_solve, tail);
 }
 cudaError_t launch_ai(const AIArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream, cudaEvent_t after_solve) {
-    return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream, after_solve);
+                      cudaStream_t stream, cudaEvent_t after_solve, const TailLane* tail) {
+    return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream, after_solve, tail);
 }
 
 }  // namespace nesf

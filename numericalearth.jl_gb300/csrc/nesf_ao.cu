@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(128, ENS ? 4 : 3) ao_kernel(AOArgs<S> a, DevIf
 }
 
 // Pass 1b (ADAPTIVE): the cells whose FP32 result was not kept, packed, through
-// the FP32 sweep + FP64 Newton polish; those that need it go on to the replay.
+// pass 1's FP32 sweep + FP64 Newton polish; those that need it go on to the replay.
 template <class S, bool SKIN>
 __global__ void __launch_bounds__(128) ao_polish_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
                                                         const DevIface<double>* __restrict__ P64s,
@@ -280,15 +280,26 @@ __global__ void __launch_bounds__(128) ao_polish_kernel(AOArgs<S> a, DevIface<do
         const DevIface<float>& Pf = P32s ? P32s[m] : P32;
         int i = (int)(r % nxr), j = (int)(r / nxr);
         int64_t k = a.L.at(i, j) + m * a.member_stride;
+        // pass 1's sweep from the cold start (its inputs and its strict stopping rule),
+        // then the FP64 Newton steps with the reference's FP64 cell constants
+        Fast32 f;
+        ao_load_fast<S, SKIN>(P, Pf, a, k, f);
+        float x[4] = {1e-4f, 1e-4f, 1e-4f, SKIN ? f.anc.dTi : 0.0f};
+        float J[SKIN ? 4 : 3][SKIN ? 4 : 3];
+        float rho;
+        int f32it = 0, f64it = 0, reason = -1;
+        int outcome = sweep_fp32<SKIN, false, true>(Pf, f.c, f.s, f.anc, x, so, f32it, reason, J, rho, nullptr,
+                                                    nullptr);
         CellConst<double> c;
-        bool land;
-        ao_load(P, a, k, SKIN, c, land);
-        double us = 1e-4, ts = 1e-4, qst = 1e-4;
         SurfaceConst<double> s{};
-        if (SKIN) s.Ts = c.Ti;
-        else surface_const(P, c, c.Ti, surface_specific_humidity(P, c.pa, c.Ti), s);
-        int f32it, f64it, reason = -1;
-        int outcome = solve_fast<SKIN>(P, Pf, c, s, us, ts, qst, so, f32it, f64it, reason);
+        double us = 0, ts = 0, qst = 0;
+        if (outcome != FAST_REPLAY) {
+            bool land;
+            ao_load(P, a, k, SKIN, c, land);
+            if (SKIN) s.Ts = c.Ti;
+            else surface_const(P, c, c.Ti, surface_specific_humidity(P, c.pa, c.Ti), s);
+            outcome = newton_fp64<SKIN>(P, c, s, x, J, rho, so, us, ts, qst, f64it, reason);
+        }
         replay_push(rq, outcome == FAST_REPLAY, id);
         if (outcome == FAST_REPLAY) {
             if (stats) {
@@ -353,10 +364,12 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
     if (e != cudaSuccess) return e;
     if (ens) ao_classify_kernel<S, true><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, nullptr, stats);
     else ao_classify_kernel<S, false><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, feat, stats);
+    trace_mark(so.tracer, "ao_classify", stream);
     if (warm) {
         e = mlp_pass((void*)ws.mlp, ws.feat, nullptr, ws.guess, 0, wl.count, wl.per_member, so.infer_per_sm * sms,
                      true, stream);
         if (e != cudaSuccess) return e;
+        trace_mark(so.tracer, "ao_warm_start_inference", stream);
     }
 #define NESF_AO_LAUNCH(PR, SK, EN) \
     ao_kernel<S, PR, SK, EN><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, so, wl, rq, guess, stats)
@@ -374,6 +387,7 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
 #undef NESF_AO_ENS
 #undef NESF_AO_LAUNCH
     e = cudaGetLastError();
+    trace_mark(so.tracer, "ao_pass1", stream);
     if (e != cudaSuccess || prec == NESF_PLAIN_F64) return e;
     // passes 1b and 2: enough resident blocks to sweep the queues (grid-stride)
     unsigned g2 = (unsigned)(sms * so.deferred_per_sm);
@@ -383,9 +397,11 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
         else ao_polish_kernel<S, false><<<g2, 128, 0, stream>>>(a, P64, P32, pm, ens ? P32s : nullptr, so, rq, stats);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
+        trace_mark(so.tracer, "ao_polish", stream);
     }
     if (skin) ao_replay_kernel<S, true><<<g2, 128, 0, stream>>>(a, P64, pm, rq, stats);
     else ao_replay_kernel<S, false><<<g2, 128, 0, stream>>>(a, P64, pm, rq, stats);
+    trace_mark(so.tracer, "ao_replay", stream);
     return cudaGetLastError();
 }
 

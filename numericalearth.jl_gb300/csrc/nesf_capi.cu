@@ -22,7 +22,7 @@ struct nesf_context {
     DevIface<float>* d_p32;
     int32_t capacity_members;
     uint32_t* d_replay;         // replay + polish queues of the FP32 solvers (2 x capacity)
-    unsigned int* d_replay_count;   // [2]
+    unsigned int* d_replay_count;   // [3] (see ReplayQueue)
     int64_t replay_capacity;
     uint32_t* d_work;           // compacted work lists of the solves
     unsigned int* d_work_count; // two counters per ensemble member
@@ -36,9 +36,41 @@ struct nesf_context {
     nesf_context* aux;
     cudaStream_t side;
     cudaEvent_t ev_fork, ev_ice, ev_join;
+    // the sea-ice solve's replay stream beside its polish pass, with fork/join events
+    cudaStream_t tail;
+    cudaEvent_t ev_tail_fork, ev_tail_join;
     nesf_tuning tuning;         // launch shapes and schedule (nesf_set_tuning, nesf_autotune)
+    struct TraceBuf* trace;     // kernel-boundary trace (nesf_trace_enable); the lane context borrows it
+    bool trace_owned;
     std::mutex lock;            // serialises use of the scratch above
 };
+
+// The events of a trace and the tracer hook the launchers call.
+struct TraceBuf {
+    bool on;
+    int n;
+    cudaEvent_t ev[NESF_TRACE_MAX];
+    const char* name[NESF_TRACE_MAX];
+    cudaStream_t stream[NESF_TRACE_MAX];
+    Tracer hook;
+};
+
+static void trace_record(void* self, const char* name, cudaStream_t s) {
+    TraceBuf* t = (TraceBuf*)self;
+    if (!t->on || t->n >= NESF_TRACE_MAX) return;
+    // under stream capture the record becomes an event-record node of the graph
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) return;
+    unsigned flags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
+    if (cudaEventRecordWithFlags(t->ev[t->n], s, flags) != cudaSuccess) return;
+    t->name[t->n] = name;
+    t->stream[t->n] = s;
+    t->n++;
+}
+
+static const Tracer* tracer_of(const nesf_context* ctx) {
+    return ctx && ctx->trace && ctx->trace->on ? &ctx->trace->hook : nullptr;
+}
 
 // The defaults of nesf_tuning's fields.
 static nesf_tuning default_tuning() {
@@ -108,7 +140,7 @@ int32_t nesf_struct_sizes(int64_t* sizes, int32_t n) {
         (int64_t)sizeof(nesf_atmos_grid), (int64_t)sizeof(nesf_exchange_coords), (int64_t)sizeof(nesf_interp_fields),
         (int64_t)sizeof(nesf_assembly_params), (int64_t)sizeof(nesf_assembly_fields),
         (int64_t)sizeof(nesf_coupling_step_args), (int64_t)sizeof(nesf_integral_fields),
-        (int64_t)sizeof(nesf_tuning)};
+        (int64_t)sizeof(nesf_tuning), (int64_t)sizeof(nesf_trace_entry)};
     int32_t m = (int32_t)(sizeof s / sizeof s[0]);
     for (int32_t k = 0; k < n && k < m; k++) sizes[k] = s[k];
     return m;
@@ -292,10 +324,14 @@ int nesf_context_create(int32_t device, nesf_context** out) {
     c->aux = nullptr;
     c->side = nullptr;
     c->ev_fork = c->ev_ice = c->ev_join = nullptr;
+    c->tail = nullptr;
+    c->ev_tail_fork = c->ev_tail_join = nullptr;
     c->tuning = default_tuning();
+    c->trace = nullptr;
+    c->trace_owned = false;
     cudaError_t e = cudaMalloc(&c->d_stats, sizeof(DevStats));
     if (e == cudaSuccess) e = cudaMalloc(&c->d_partials, (size_t)kIntegralBlocks * NESF_MAX_INTEGRALS * 16);
-    if (e == cudaSuccess) e = cudaMalloc(&c->d_replay_count, 2 * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_replay_count, 4 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_stats, sizeof(DevStats));
     if (e != cudaSuccess) {
         cudaFree(c->d_stats);
@@ -327,6 +363,13 @@ int nesf_context_destroy(nesf_context* c) {
         if (c->ev_fork) cudaEventDestroy(c->ev_fork);
         if (c->ev_ice) cudaEventDestroy(c->ev_ice);
         if (c->ev_join) cudaEventDestroy(c->ev_join);
+        if (c->tail) cudaStreamDestroy(c->tail);
+        if (c->ev_tail_fork) cudaEventDestroy(c->ev_tail_fork);
+        if (c->ev_tail_join) cudaEventDestroy(c->ev_tail_join);
+        if (c->trace && c->trace_owned) {
+            for (int i = 0; i < NESF_TRACE_MAX; i++) cudaEventDestroy(c->trace->ev[i]);
+            delete c->trace;
+        }
     }
     if (c->aux) nesf_context_destroy(c->aux);
     delete c;
@@ -385,7 +428,7 @@ static SolveOpts solve_opts(const nesf_solver_options& o, const nesf_context* ct
     float rho = o.precision == NESF_F32_ADAPTIVE ? (float)(o.fp32_rho < 0.99 ? o.fp32_rho : 0.99) : 0.0f;
     const nesf_tuning t = ctx ? ctx->tuning : default_tuning();
     return SolveOpts{o.polish_maxiter, (float)o.path_tolerance, rho, (float)o.fallback_ratio,
-                     t.solve_block, t.deferred_per_sm, t.infer_per_sm};
+                     t.solve_block, t.deferred_per_sm, t.infer_per_sm, tracer_of(ctx)};
 }
 
 static int check_options(const nesf_solver_options& o, const char* who) {
@@ -406,12 +449,23 @@ static int replay_queue(nesf_context* ctx, int64_t cells, ReplayQueue* q) {
         cudaFree(ctx->d_replay);
         ctx->d_replay = nullptr;
         ctx->replay_capacity = 0;
-        NESF_CUDA(cudaMalloc(&ctx->d_replay, 2 * sizeof(uint32_t) * (size_t)cells));
+        NESF_CUDA(cudaMalloc(&ctx->d_replay, 3 * sizeof(uint32_t) * (size_t)cells));
         ctx->replay_capacity = cells;
     }
     q->idx = ctx->d_replay;
     q->count = ctx->d_replay_count;
     q->capacity = ctx->replay_capacity;
+    return NESF_OK;
+}
+
+// The sea-ice solve's second stream for its deferred passes (created once; before
+// a graph capture by coupling_scratch).
+static int tail_lane(nesf_context* ctx) {
+    if (ctx->tail) return NESF_OK;
+    DeviceGuard g(ctx->device);
+    NESF_CUDA(cudaEventCreateWithFlags(&ctx->ev_tail_fork, cudaEventDisableTiming));
+    NESF_CUDA(cudaEventCreateWithFlags(&ctx->ev_tail_join, cudaEventDisableTiming));
+    NESF_CUDA(cudaStreamCreateWithFlags(&ctx->tail, cudaStreamNonBlocking));
     return NESF_OK;
 }
 
@@ -696,10 +750,16 @@ static int sea_ice_fluxes(nesf_context* ctx, const nesf_interface_params* params
     if ((r = work_list(ctx, ring, 1, &wl))) return r;
     if ((r = warm_buffers(ctx, o, ring, &ws))) return r;
     SolveOpts so = solve_opts(o, ctx);
+    // the replay of pass 1's cells beside the polish pass (the tuning's two_lanes)
+    TailLane tl{nullptr, nullptr, nullptr};
+    if (o.precision == NESF_F32_ADAPTIVE && ctx->tuning.two_lanes) {
+        if ((r = tail_lane(ctx))) return r;
+        tl = TailLane{ctx->tail, ctx->ev_tail_fork, ctx->ev_tail_join};
+    }
     return with_stats(ctx, stats, s, [&](DevStats* ds) {
         if (f->dtype == NESF_F64)
-            return launch_ai(ai_args<double>(f), P64, P32, o.precision, so, wl, rq, ws, ds, s, after_solve);
-        return launch_ai(ai_args<float>(f), P64, P32, o.precision, so, wl, rq, ws, ds, s, after_solve);
+            return launch_ai(ai_args<double>(f), P64, P32, o.precision, so, wl, rq, ws, ds, s, after_solve, &tl);
+        return launch_ai(ai_args<float>(f), P64, P32, o.precision, so, wl, rq, ws, ds, s, after_solve, &tl);
     });
 }
 
@@ -1122,6 +1182,7 @@ static int coupling_scratch(nesf_context* ctx, const nesf_coupling_step_args* a,
     int r = size_scratch(ctx, (int64_t)(a->ao->grid.nx + 2) * (a->ao->grid.ny + 2), opts);
     if (r == NESF_OK && a->ai_params && a->ai) {
         if ((r = coupling_lane(ctx))) return r;
+        if ((r = tail_lane(ctx->aux))) return r;
         r = size_scratch(ctx->aux, (int64_t)(a->ai->grid.nx + 2) * (a->ai->grid.ny + 2), opts);
     }
     return r;
@@ -1147,13 +1208,20 @@ extern "C" int nesf_coupling_step(nesf_context* ctx, const nesf_coupling_step_ar
     // both (the same state as update_state!'s order).
     // The context's tuning may put the sea-ice solve in line (one lane) and the
     // sea-ice-ocean fluxes after the solves; the outputs are the same.
-    if (a->interp && (r = nesf_interpolate_atmosphere_state(a->interp, stream))) return r;
     cudaStream_t s = (cudaStream_t)stream;
+    const Tracer* tr = tracer_of(ctx);
+    if (tr) {
+        ctx->trace->n = 0;
+        trace_mark(tr, "step", s);
+    }
+    if (a->interp && (r = nesf_interpolate_atmosphere_state(a->interp, stream))) return r;
+    if (a->interp) trace_mark(tr, "interpolate", s);
     const bool io_split = ice && a->io_params && ctx->tuning.io_overlap;
     const bool lanes = ice && ctx->tuning.two_lanes;
     if (ice) {
         if ((r = coupling_lane(ctx))) return r;
         ctx->aux->tuning = ctx->tuning;
+        ctx->aux->trace = ctx->trace;   // one timeline for both lanes
         DeviceGuard g(ctx->device);
         if (lanes) {
             NESF_CUDA(cudaEventRecord(ctx->ev_fork, s));
@@ -1162,6 +1230,7 @@ extern "C" int nesf_coupling_step(nesf_context* ctx, const nesf_coupling_step_ar
             NESF_CUDA(cudaEventRecord(ctx->ev_join, ctx->side));
         }
         if (io_split && (r = sea_ice_ocean(ctx, a->io_params, a->io, stream, 1))) return r;
+        if (io_split) trace_mark(tr, "sea_ice_ocean_fluxes", s);
         if (lanes) NESF_CUDA(cudaStreamWaitEvent(s, ctx->ev_ice, 0));
         else if ((r = sea_ice_fluxes(ctx->aux, a->ai_params, a->ai, opts, nullptr, s, nullptr))) return r;
     }
@@ -1171,6 +1240,7 @@ extern "C" int nesf_coupling_step(nesf_context* ctx, const nesf_coupling_step_ar
         NESF_CUDA(cudaStreamWaitEvent(s, ctx->ev_join, 0));
     }
     if (a->io_params && (r = sea_ice_ocean(ctx, a->io_params, a->io, stream, io_split ? 2 : 0))) return r;
+    if (a->io_params) trace_mark(tr, io_split ? "frazil_adjustment" : "sea_ice_ocean_fluxes", s);
     if (a->assembly_params) {
         if ((r = nesf_assemble_net_ocean_fluxes(a->assembly_params, a->assembly, stream))) return r;
         if (ice && (r = nesf_assemble_net_sea_ice_fluxes(a->assembly_params, a->assembly, stream))) return r;
@@ -1179,6 +1249,7 @@ extern "C" int nesf_coupling_step(nesf_context* ctx, const nesf_coupling_step_ar
             if (ice && (r = nesf_apply_air_sea_ice_radiative_fluxes(a->assembly_params, a->assembly, stream)))
                 return r;
         }
+        trace_mark(tr, "assembly", s);
     }
     return NESF_OK;
 }
@@ -1287,6 +1358,59 @@ extern "C" int nesf_graph_destroy(nesf_graph* G) {
     if (G->exec) cudaGraphExecDestroy(G->exec);
     if (G->graph) cudaGraphDestroy(G->graph);
     delete G;
+    return NESF_OK;
+}
+
+// ---------------------------------------------------------------- tracing
+extern "C" int nesf_trace_enable(nesf_context* ctx, int32_t on) {
+    int r = context_or_default(&ctx);
+    if (r) return r;
+    std::lock_guard<std::mutex> lk(ctx->lock);
+    if (on && !ctx->trace) {
+        DeviceGuard g(ctx->device);
+        TraceBuf* t = new (std::nothrow) TraceBuf();
+        if (!t) return fail(NESF_ERR_ARG, "nesf_trace_enable: out of host memory");
+        for (int i = 0; i < NESF_TRACE_MAX; i++) {
+            cudaError_t e = cudaEventCreate(&t->ev[i]);
+            if (e != cudaSuccess) {
+                for (int j = 0; j < i; j++) cudaEventDestroy(t->ev[j]);
+                delete t;
+                return cuda_fail(e, "nesf_trace_enable");
+            }
+        }
+        t->hook = Tracer{trace_record, t};
+        ctx->trace = t;
+        ctx->trace_owned = true;
+    }
+    if (ctx->trace) ctx->trace->on = on != 0;
+    return NESF_OK;
+}
+
+extern "C" int nesf_trace_read(nesf_context* ctx, nesf_trace_entry* out, int32_t max, int32_t* count) {
+    if (!out || !count || max < 0) return fail(NESF_ERR_ARG, "nesf_trace_read: null output or max < 0");
+    int r = context_or_default(&ctx);
+    if (r) return r;
+    std::lock_guard<std::mutex> lk(ctx->lock);
+    *count = 0;
+    TraceBuf* t = ctx->trace;
+    if (!t || t->n == 0) return NESF_OK;
+    DeviceGuard g(ctx->device);
+    cudaStream_t seen[NESF_TRACE_MAX];
+    int nseen = 0;
+    const int n = t->n < max ? t->n : max;
+    for (int i = 0; i < n; i++) {
+        NESF_CUDA(cudaEventSynchronize(t->ev[i]));
+        float ms = 0.0f;
+        NESF_CUDA(cudaEventElapsedTime(&ms, t->ev[0], t->ev[i]));
+        int lane = 0;
+        while (lane < nseen && seen[lane] != t->stream[i]) lane++;
+        if (lane == nseen) seen[nseen++] = t->stream[i];
+        std::memset(&out[i], 0, sizeof(out[i]));
+        std::snprintf(out[i].name, sizeof(out[i].name), "%s", t->name[i]);
+        out[i].stream = lane;
+        out[i].t_ms = ms;
+    }
+    *count = n;
     return NESF_OK;
 }
 

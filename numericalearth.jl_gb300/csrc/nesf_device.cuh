@@ -162,17 +162,16 @@ __device__ __forceinline__ R surface_atmosphere_temperature(const DevIface<R>& P
 // -------------------------------------------------------- stability functions
 // similarity_theory_turbulent_fluxes.jl. The reference evaluates both branches
 // and selects with ifelse(zeta < 0, ...); here only the selected branch is
-// evaluated, which gives the same value.
-// Division by a coefficient is multiplication by its host-derived reciprocal, sums
-// of logarithms are the logarithm of a product, and pow is exp(y log x): each
-// moves a result by about an ulp, and the FP64 division, log, atan and pow they
-// save cost 0.6k-5.8k cycles per dependent call.
+// evaluated, which gives the same value. Division by a coefficient is
+// multiplication by its host-derived reciprocal, sums of logarithms are the
+// logarithm of a product, and pow is exp(y log x): each moves a result by about an
+// ulp, and the FP64 division, log, atan and pow they save cost 0.6k-5.8k cycles per
+// dependent call.
 
-// Convective branch (zeta < 0) of Edson's momentum (MOM) and scalar functions:
-// (1 - f) psi1 + f psi2, f = zeta^2 / (1 + zeta^2).
+// Convective branch (zeta < 0) of Edson's momentum (MOM) and scalar functions
+// (:501-532, :586-618): (1 - f) psi1 + f psi2, f = zeta^2 / (1 + zeta^2).
 template <class R, bool MOM>
-__device__ __noinline__ R psi_edson_unstable(R Am, R Bm, R iBm, R Cm, R Dm, R hEm, R iEm, R sE, R isE, R Fm,
-                                             R z) {
+__device__ __forceinline__ R edson_unstable(R Am, R Bm, R iBm, R Cm, R Dm, R hEm, R iEm, R sE, R isE, R Fm, R z) {
     R zm = M<R>::fmin(R(0), z);
     R psi1;
     if (MOM) {
@@ -188,32 +187,21 @@ __device__ __noinline__ R psi_edson_unstable(R Am, R Bm, R iBm, R Cm, R Dm, R hE
     return (R(1) - f) * psi1 + f * psi2;
 }
 
-template <class R>
-__device__ __forceinline__ R psi_edson_momentum(const DevStab<R>& s, R z) {   // :501-532
+// Stable branch (zeta >= 0) of Edson's momentum (MOM) and scalar functions.
+template <class R, bool MOM>
+__device__ __forceinline__ R edson_stable(const DevStab<R>& s, R z) {
     const R* c = s.c;
-    const R* k = s.k;
-    if (z < R(0)) return psi_edson_unstable<R, true>(c[5], c[6], k[0], c[7], c[8], k[1], k[2], k[3], k[4], c[10], z);
     R zmax = c[0], Ap = c[1], Bp = c[2], Cp = c[3], Dp = c[4];
     R zp = M<R>::fmax(R(0), z);
     R dz = M<R>::fmin(zmax, Ap * zp);
-    return -Bp * zp - Cp * (zp - Dp) * M<R>::exp(-dz) - Cp * Dp;
-}
-
-template <class R>
-__device__ __forceinline__ R psi_edson_scalar(const DevStab<R>& s, R z) {     // :586-618
-    const R* c = s.c;
-    const R* k = s.k;
-    if (z < R(0)) return psi_edson_unstable<R, false>(c[6], c[7], k[0], c[8], c[9], k[1], k[2], k[3], k[4], c[11], z);
-    R zmax = c[0], Ap = c[1], Bp = c[2], Cp = c[3], Dp = c[4], Ep = c[5];
-    R zp = M<R>::fmax(R(0), z);
-    R dz = M<R>::fmin(zmax, Ap * zp);
+    if (MOM) return -Bp * zp - Cp * (zp - Dp) * M<R>::exp(-dz) - Cp * Dp;
     R x = R(1) + Bp * zp;
     R xC = Cp == R(1.5) ? x * M<R>::sqrt(x) : M<R>::exp(Cp * M<R>::log(x));   // x^Cp
-    return -xC - Bp * (zp - Dp) * M<R>::exp(-dz) - Ep;
+    return -xC - Bp * (zp - Dp) * M<R>::exp(-dz) - c[5];
 }
 
 template <class R>
-__device__ __noinline__ R psi_sheba_momentum(const R* k, R z) {     // :643-657
+__device__ __forceinline__ R sheba_momentum(const R* k, R z) {     // :643-657
     R zp = M<R>::fmax(R(0), z);
     R x = M<R>::cbrt(R(1) + zp);
     R B = k[0];
@@ -224,7 +212,7 @@ __device__ __noinline__ R psi_sheba_momentum(const R* k, R z) {     // :643-657
 }
 
 template <class R>
-__device__ __noinline__ R psi_sheba_scalar(R c, const R* k, R z) {  // :665-677
+__device__ __forceinline__ R sheba_scalar(R c, const R* k, R z) {  // :665-677
     R zp = M<R>::fmax(R(0), z);
     R P1 = k[0] * M<R>::log(R(1) + c * zp + zp * zp);
     R P2 = k[1] * (M<R>::log((R(2) * zp + k[2]) / (R(2) * zp + k[3])) - k[4]);
@@ -232,7 +220,7 @@ __device__ __noinline__ R psi_sheba_scalar(R c, const R* k, R z) {  // :665-677
 }
 
 template <class R>
-__device__ __noinline__ R psi_paulson_momentum(R a, R b, R z) {   // :688-699
+__device__ __forceinline__ R paulson_momentum(R a, R b, R z) {   // :688-699
     R zm = M<R>::fmin(R(0), z);
     R x = M<R>::sqrt(M<R>::sqrt(R(1) - a * zm));
     R u = (R(1) + x) * R(0.5);
@@ -242,7 +230,7 @@ __device__ __noinline__ R psi_paulson_momentum(R a, R b, R z) {   // :688-699
 }
 
 template <class R>
-__device__ __noinline__ R psi_paulson_scalar(R a, R z) {          // :705-710
+__device__ __forceinline__ R paulson_scalar(R a, R z) {          // :705-710
     R zm = M<R>::fmin(R(0), z);
     R x = M<R>::sqrt(M<R>::sqrt(R(1) - a * zm));
     return R(2) * M<R>::log((R(1) + x * x) * R(0.5));
@@ -254,18 +242,50 @@ __device__ __forceinline__ R psi_linear(R coef, R zmax, R z) {       // :747-752
     return -coef * M<R>::fmin(zp, zmax);
 }
 
+// One out-of-line copy of each function per kernel (the solves' loops call them from
+// several places; inlined, the kernels outgrow the instruction cache).
+template <class R, bool MOM>
+__device__ __noinline__ R psi_edson_unstable(R Am, R Bm, R iBm, R Cm, R Dm, R hEm, R iEm, R sE, R isE, R Fm, R z) {
+    return edson_unstable<R, MOM>(Am, Bm, iBm, Cm, Dm, hEm, iEm, sE, isE, Fm, z);
+}
+
+template <class R>
+__device__ __noinline__ R psi_sheba_momentum(R k0, R k1, R k2, R k3, R k4, R k5, R k6, R k7, R z) {
+    const R k[8] = {k0, k1, k2, k3, k4, k5, k6, k7};
+    return sheba_momentum(k, z);
+}
+
+template <class R>
+__device__ __noinline__ R psi_sheba_scalar(R c, R k0, R k1, R k2, R k3, R k4, R z) {
+    const R k[5] = {k0, k1, k2, k3, k4};
+    return sheba_scalar(c, k, z);
+}
+
+template <class R>
+__device__ __noinline__ R psi_paulson_momentum(R a, R b, R z) { return paulson_momentum(a, b, z); }
+
+template <class R>
+__device__ __noinline__ R psi_paulson_scalar(R a, R z) { return paulson_scalar(a, z); }
+
 // stability_profile dispatch; SplitStabilityFunction (:720-725) takes the stable
-// branch for z > 0.
+// branch for z > 0, Edson's functions select with z < 0.
 template <class R>
 __device__ __forceinline__ R stability(const DevStab<R>& s, R z) {
     const R* c = s.c;
+    const R* k = s.k;
     switch (s.kind) {
-    case NESF_PSI_EDSON_MOMENTUM: return psi_edson_momentum(s, z);
-    case NESF_PSI_EDSON_SCALAR: return psi_edson_scalar(s, z);
+    case NESF_PSI_EDSON_MOMENTUM:
+        if (z < R(0)) return psi_edson_unstable<R, true>(c[5], c[6], k[0], c[7], c[8], k[1], k[2], k[3], k[4], c[10], z);
+        return edson_stable<R, true>(s, z);
+    case NESF_PSI_EDSON_SCALAR:
+        if (z < R(0))
+            return psi_edson_unstable<R, false>(c[6], c[7], k[0], c[8], c[9], k[1], k[2], k[3], k[4], c[11], z);
+        return edson_stable<R, false>(s, z);
     case NESF_PSI_SHEBA_PAULSON_MOMENTUM:
-        return z > R(0) ? psi_sheba_momentum(s.k, z) : psi_paulson_momentum(c[2], c[3], z);
+        return z > R(0) ? psi_sheba_momentum(k[0], k[1], k[2], k[3], k[4], k[5], k[6], k[7], z)
+                        : psi_paulson_momentum(c[2], c[3], z);
     case NESF_PSI_SHEBA_PAULSON_SCALAR:
-        return z > R(0) ? psi_sheba_scalar(c[2], s.k, z) : psi_paulson_scalar(c[3], z);
+        return z > R(0) ? psi_sheba_scalar(c[2], k[0], k[1], k[2], k[3], k[4], z) : psi_paulson_scalar(c[3], z);
     case NESF_PSI_LINEAR_PAULSON_MOMENTUM:
         return z > R(0) ? psi_linear(c[0], c[1], z) : psi_paulson_momentum(c[2], c[3], z);
     case NESF_PSI_LINEAR_PAULSON_SCALAR:
@@ -274,7 +294,8 @@ __device__ __forceinline__ R stability(const DevStab<R>& s, R z) {
     }
 }
 
-// similarity_profile (:242-253), with 1 / L in place of L (h / L = h * (1 / L))
+// similarity_profile (:242-253), with 1 / L in place of L (h / L = h * (1 / L)); the
+// COARE form has no psi(l / L) term.
 template <class R>
 __device__ __forceinline__ R similarity_profile(int form, const DevStab<R>& psi, R h, R l, R invL) {
     R zeta = h * invL;

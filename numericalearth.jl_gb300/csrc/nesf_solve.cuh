@@ -24,6 +24,18 @@
 
 namespace nesf {
 
+// Kernel-boundary tracing (nesf_trace_enable): a host-side hook that the
+// launchers call after each launch, recording an event on its stream; null when
+// tracing is off.
+struct Tracer {
+    void (*mark)(void* self, const char* name, cudaStream_t s);
+    void* self;
+};
+
+inline void trace_mark(const Tracer* t, const char* name, cudaStream_t s) {
+    if (t && t->mark) t->mark(t->self, name, s);
+}
+
 // Knobs of the FP32 + FP64-polish solver.
 struct SolveOpts {
     int polish_steps;      // FP64 Newton steps
@@ -33,6 +45,7 @@ struct SolveOpts {
     // launch shapes (host side; the autotuner's choice): threads per block of pass 1,
     // blocks per SM of the packed polish/replay passes and of the warm-start inference
     int block, deferred_per_sm, infer_per_sm;
+    const Tracer* tracer;  // host side: kernel-boundary trace (null: off)
 };
 
 // Warm start of a solve: features written by the classify pass at the work-list
@@ -53,14 +66,22 @@ struct WorkList {
     int64_t per_member;
 };
 
-// Cells deferred to the packed passes. idx holds 2 * capacity entries: cells to
-// replay in FP64 at [0, capacity), cells to polish (ADAPTIVE) at [capacity, 2 *
-// capacity); count[0] and count[1] are their numbers (zeroed before the solve).
-// A cell that the polish pass sends on to the replay holds one entry in each.
+// Cells deferred to the packed passes, in parts of `capacity` entries: part 0 the
+// cells to replay in FP64, part 1 the cells to polish (ADAPTIVE), part 2 (the
+// sea-ice solve's, which replays the polish pass's cells apart so that the replay
+// of pass 1's cells runs beside the polish pass) the polish pass's replays;
+// count[part] are their numbers (zeroed before the solve). A cell that the polish
+// pass sends on to a replay holds one entry in each of two parts.
 struct ReplayQueue {
     uint32_t* idx;          // linear cell ids (member * ring + ring index)
     unsigned int* count;
     int64_t capacity;
+};
+
+// A second stream for the deferred passes and its fork/join events (null: serial).
+struct TailLane {
+    cudaStream_t stream;
+    cudaEvent_t fork, join;
 };
 
 template <class S> struct AOArgs {
@@ -387,15 +408,17 @@ __device__ __forceinline__ float spectral_bound(const float (&J)[N][N]) {
 // FP32 result is kept) or FAST_POLISH (the FP32 result needs FP64 Newton steps:
 // J and rho_est are set for them). `fp32_it` counts FP32 map evaluations.
 //
-// ACCEPT32 (ADAPTIVE): the sweep runs until every component, not just the drift
-// sum, is converged at FP32 resolution, and the FP32 result is kept when F
-// contracts by at most so.fp32_rho.
+// ACCEPT32 (ADAPTIVE): the FP32 result is kept when F contracts by at most
+// so.fp32_rho. STRICT (ADAPTIVE's passes): the sweep runs until every component,
+// not just the drift sum, is converged at FP32 resolution -- the polish pass of
+// the cells that pass 1 did not keep repeats pass 1's sweep exactly, so it reaches
+// the same decisions.
 //
 // The FP32 sweep and the 2N evaluations of the central-difference Jacobian run
 // through one loop around a single inlined copy of the map, so a warp executes
 // the same instructions for both: the kernel's hot code stays small enough for
 // the instruction cache.
-template <bool SKIN, bool ACCEPT32>
+template <bool SKIN, bool ACCEPT32, bool STRICT = ACCEPT32>
 __device__ __forceinline__ int sweep_fp32(const DevIface<float>& P32, const CellConst<float>& c32,
                                           const SurfaceConst<float>& s32, const SkinAnchor<float>& anc,
                                           float (&x)[4], const SolveOpts& so, int& fp32_it, int& reason,
@@ -488,7 +511,7 @@ __device__ __forceinline__ int sweep_fp32(const DevIface<float>& P32, const Cell
             // each component within 4 of its own ulps (ADAPTIVE), or the sum within 8
             const float u4 = 4.0f * 1.1920929e-7f;
             // (tau to 1e-7 K besides: dtheta = -tau)
-            bool quiet = ACCEPT32 ? (du <= u4 * fabsf(x[0]) && dt <= u4 * fabsf(x[1]) && dq <= u4 * fabsf(x[2]) &&
+            bool quiet = STRICT ? (du <= u4 * fabsf(x[0]) && dt <= u4 * fabsf(x[1]) && dq <= u4 * fabsf(x[2]) &&
                                      dT <= u4 * fabsf(x[3]) + 1e-7f)
                                   : drift <= 8.0f * res;
             bool done = drift < tol || quiet;
@@ -567,30 +590,20 @@ __device__ __forceinline__ int sweep_fp32(const DevIface<float>& P32, const Cell
     return FAST_POLISH;
 }
 
-// FP32 sweep + FP64 Newton polish from the reference's FP64 cell constants (c64,
-// s64). On FAST_SOLVED the solution is in us, ts, qst and, with a skin
-// temperature, s64.Ts (the interface temperature; the rest of s64 is not
-// updated); on FAST_REPLAY they are untouched. `fp32_it` counts FP32 map
-// evaluations and `fp64_it` FP64 ones.
+// FP64 Newton steps on x = F(x) from the FP32 fixed point x of sweep_fp32 (J and
+// rho_est its Jacobian and contraction bound), with the reference's FP64 cell
+// constants (c64, s64). On FAST_SOLVED the solution is in us, ts, qst and, with a
+// skin temperature, s64.Ts (the interface temperature; the rest of s64 is not
+// updated); FAST_REPLAY (I - J singular) leaves them untouched. `fp64_it` counts
+// FP64 map evaluations.
 template <bool SKIN>
-__device__ __forceinline__ int solve_fast(const DevIface<double>& P64, const DevIface<float>& P32,
-                                          const CellConst<double>& c64, SurfaceConst<double>& s64, double& us,
-                                          double& ts, double& qst, const SolveOpts& so, int& fp32_it, int& fp64_it,
-                                          int& reason, const float* xw = nullptr, bool* fell_back = nullptr) {
+__device__ __forceinline__ int newton_fp64(const DevIface<double>& P64, const CellConst<double>& c64,
+                                           SurfaceConst<double>& s64, const float (&x)[4],
+                                           const float (&J)[SKIN ? 4 : 3][SKIN ? 4 : 3], float rho_est,
+                                           const SolveOpts& so, double& us, double& ts, double& qst, int& fp64_it,
+                                           int& reason) {
     constexpr int N = SKIN ? 4 : 3;
     fp64_it = 0;
-    CellConst<float> c32;
-    SurfaceConst<float> s32;
-    convert_const(c64, c32);
-    convert_surface(s64, s32);
-    SkinAnchor<float> anc{};
-    if (SKIN) anc = skin_anchor(P64, c64.tha, c64.Ti, c64.Si, c64.qa, c64.pa, c64.sw, c64.lw);
-    float x[4] = {(float)us, (float)ts, (float)qst, SKIN ? (float)(s64.Ts - c64.tha) : 0.0f};
-    float J[N][N];
-    float rho_est;
-    if (sweep_fp32<SKIN, false>(P32, c32, s32, anc, x, so, fp32_it, reason, J, rho_est, xw, fell_back) == FAST_REPLAY)
-        return FAST_REPLAY;
-    // ---- FP64 Newton steps on x = F(x)
     float A[N][N], Ainv[N][N];
 #pragma unroll
     for (int ii = 0; ii < N; ii++)
@@ -700,6 +713,31 @@ __device__ __forceinline__ void stress_fast(float us, float du, float dv, float&
     ty = dU == 0.0f ? 0.0f : -(us * us) * dv / dU;
 }
 
+// FP32 sweep + FP64 Newton polish from the reference's FP64 cell constants (c64,
+// s64), the FP32 inputs rounded from them. Outputs as newton_fp64's; `fp32_it`
+// counts FP32 map evaluations. STRICT: the sweep of sweep_fp32<.., STRICT>.
+template <bool SKIN, bool STRICT = false>
+__device__ __forceinline__ int solve_fast(const DevIface<double>& P64, const DevIface<float>& P32,
+                                          const CellConst<double>& c64, SurfaceConst<double>& s64, double& us,
+                                          double& ts, double& qst, const SolveOpts& so, int& fp32_it, int& fp64_it,
+                                          int& reason, const float* xw = nullptr, bool* fell_back = nullptr) {
+    constexpr int N = SKIN ? 4 : 3;
+    fp64_it = 0;
+    CellConst<float> c32;
+    SurfaceConst<float> s32;
+    convert_const(c64, c32);
+    convert_surface(s64, s32);
+    SkinAnchor<float> anc{};
+    if (SKIN) anc = skin_anchor(P64, c64.tha, c64.Ti, c64.Si, c64.qa, c64.pa, c64.sw, c64.lw);
+    float x[4] = {(float)us, (float)ts, (float)qst, SKIN ? (float)(s64.Ts - c64.tha) : 0.0f};
+    float J[N][N];
+    float rho_est;
+    if (sweep_fp32<SKIN, false, STRICT>(P32, c32, s32, anc, x, so, fp32_it, reason, J, rho_est, xw, fell_back) ==
+        FAST_REPLAY)
+        return FAST_REPLAY;
+    return newton_fp64<SKIN>(P64, c64, s64, x, J, rho_est, so, us, ts, qst, fp64_it, reason);
+}
+
 // Warp-aggregated append of `id` to one side of a member's work list; returns the
 // slot it took (member * per_member + position), or -1.
 __device__ __forceinline__ int64_t worklist_push(const WorkList& w, int member, bool active, bool stable,
@@ -769,7 +807,9 @@ __device__ __forceinline__ void queue_push(const ReplayQueue& q, int part, bool 
     if ((int64_t)pos < q.capacity) q.idx[(int64_t)part * q.capacity + pos] = id;
 }
 
-__device__ __forceinline__ void replay_push(const ReplayQueue& q, bool want, uint32_t id) { queue_push(q, 0, want, id); }
+__device__ __forceinline__ void replay_push(const ReplayQueue& q, bool want, uint32_t id, int part = 0) {
+    queue_push(q, part, want, id);
+}
 __device__ __forceinline__ void polish_push(const ReplayQueue& q, bool want, uint32_t id) { queue_push(q, 1, want, id); }
 
 cudaError_t launch_ao(const AOArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32,
@@ -781,12 +821,13 @@ cudaError_t launch_ao(const AOArgs<float>& a, const DevIface<double>& P64, const
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
                       cudaStream_t stream);
 // after_solve (optional): recorded once the pass-1 solve is enqueued.
+// tail (optional): a second stream on which pass 1's replays run beside the polish pass.
 cudaError_t launch_ai(const AIArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream, cudaEvent_t after_solve = nullptr);
+                      cudaStream_t stream, cudaEvent_t after_solve = nullptr, const TailLane* tail = nullptr);
 cudaError_t launch_ai(const AIArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream, cudaEvent_t after_solve = nullptr);
+                      cudaStream_t stream, cudaEvent_t after_solve = nullptr, const TailLane* tail = nullptr);
 template <class S>
 cudaError_t launch_ao_samples(const AOArgs<S>& a, const DevIface<float>& P32, float* feat, float* targ,
                               cudaStream_t s);

@@ -241,9 +241,16 @@ class Tuning(C.Structure):
 
 TUNING_FIELDS = ("solve_block", "deferred_per_sm", "infer_per_sm", "two_lanes", "io_overlap")
 
+TRACE_MAX = 64
+
+
+class TraceEntry(C.Structure):
+    _fields_ = [("name", C.c_char * 32), ("stream", i32), ("pad_", i32), ("t_ms", d)]
+
 
 # Order of nesf_struct_sizes(): must match the library.
 STRUCTS_IN_SIZE_ORDER = (Grid, ThermodynamicsParameters, StabilityFunction, RoughnessLength,
                          SimilarityTheoryFluxesC, InterfaceParams, SolverOptions, Stats, AOFields,
                          AIFields, IOParams, IOFields, AtmosGrid, ExchangeCoords, InterpFields,
-                         AssemblyParams, AssemblyFields, CouplingStepArgs, IntegralFields, Tuning)
+                         AssemblyParams, AssemblyFields, CouplingStepArgs, IntegralFields, Tuning,
+                         TraceEntry)

@@ -65,6 +65,8 @@ SIGNATURES = {
     "nesf_set_tuning": (C.c_int, [vp, P(A.Tuning)]),
     "nesf_get_tuning": (C.c_int, [vp, P(A.Tuning)]),
     "nesf_autotune": (C.c_int, [vp, P(A.CouplingStepArgs), P(A.SolverOptions), C.c_int32, P(A.Tuning), vp]),
+    "nesf_trace_enable": (C.c_int, [vp, C.c_int32]),
+    "nesf_trace_read": (C.c_int, [vp, P(A.TraceEntry), C.c_int32, P(C.c_int32)]),
 }
 
 

@@ -350,6 +350,38 @@ def autotune(step, precision="f32_adaptive", reps=5, ctx=None, stream=None, mlp=
     return out
 
 
+def trace_enable(on=True, ctx=None):
+    """Record a kernel-boundary timeline of each coupling step (nesf_trace_enable)."""
+    lib = load()
+    ctx = ctx or default_context()
+    check(lib.nesf_trace_enable(ctx.handle, 1 if on else 0))
+
+
+def trace_read(ctx=None):
+    """The last finished step's marks (nesf_trace_read): a list of (name, stream, t_ms)."""
+    lib = load()
+    ctx = ctx or default_context()
+    buf = (A.TraceEntry * A.TRACE_MAX)()
+    n = C.c_int32()
+    check(lib.nesf_trace_read(ctx.handle, buf, A.TRACE_MAX, C.byref(n)))
+    return [(buf[i].name.decode(), int(buf[i].stream), float(buf[i].t_ms)) for i in range(n.value)]
+
+
+def timeline(marks):
+    """Per-kernel spans (name, stream, start_ms, end_ms) from trace marks: a kernel ends at
+    its mark and starts at the previous mark on its stream (the step's start for stream 0;
+    None for the first kernel of another stream, which starts when its fork event fires)."""
+    last = {}
+    spans = []
+    for name, stream, t in marks:
+        if name == "step":
+            last = {0: t}
+            continue
+        spans.append((name, stream, last.get(stream), t))
+        last[stream] = t
+    return spans
+
+
 class Graph:
     """A captured CUDA graph of one coupling step (nesf_graph_capture)."""
 
