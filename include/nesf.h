@@ -214,7 +214,7 @@ typedef struct {
     double path_tolerance;    /* replay cells whose reference stopping error may exceed
                                  this relative bound (FP32 polish); default 2e-6         */
     double fp32_rho;          /* NESF_F32_ADAPTIVE: largest contraction rate at which the
-                                 FP32 result is kept; default 0.8 (0 or less: default)  */
+                                 FP32 result is kept; default 0.9 (0 or less: default)  */
 } nesf_solver_options;
 
 /* -------------------------------------------------------------- statistics */

@@ -293,7 +293,7 @@ void nesf_default_solver_options(nesf_solver_options* o) {
     o->mlp = nullptr;
     o->fallback_ratio = 10.0;
     o->path_tolerance = 2e-6;
-    o->fp32_rho = 0.8;
+    o->fp32_rho = 0.9;
 }
 
 // ---------------------------------------------------------------- context

@@ -14,66 +14,72 @@
 namespace nesf {
 
 // ------------------------------------------------------------- sea ice - ocean
-// PART 0: the whole computation. PART 1: the fluxes alone, from the frazil-adjusted
-// column temperatures held in registers, leaving T3 unchanged; PART 2: the frazil
-// adjustment of T3 alone. PART 1 then PART 2 leave the same state as PART 0, and
-// PART 1 only reads the ocean state, so it may run beside kernels that read it.
+// Arithmetic in the storage type S, like the streaming kernels: FP64 fields as the
+// reference's Float64 kernels (bit-identical to the oracle), FP32 fields as its
+// Float32 ones. PART 0: the whole computation. PART 1: the fluxes alone, from the
+// frazil-adjusted column temperatures held in registers, leaving T3 unchanged;
+// PART 2: the frazil adjustment of T3 alone. PART 1 then PART 2 leave the same
+// state as PART 0, and PART 1 only reads the ocean state, so it may run beside
+// kernels that read it.
 template <class S, int PART>
 __global__ void __launch_bounds__(256) io_kernel(IOArgs<S> a, nesf_io_params p) {
+    using R = S;
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t n = (int64_t)a.L.nx * a.L.ny;
     if (r >= n) return;
     int i = 1 + (int)(r % a.L.nx), j = 1 + (int)(r / a.L.nx);
     int64_t k2 = a.L.at(i, j);
-    double rho = p.ocean_reference_density, cpo = p.ocean_heat_capacity;
+    const R rho = R(p.ocean_reference_density), cpo = R(p.ocean_heat_capacity);
+    const R Tfw = R(p.liquidus_freshwater_melting_temperature), slope = R(p.liquidus_slope);
     // Part 1: frazil over the column, top level first (sea_ice_ocean_fluxes.jl:153-181)
-    double dQ = 0.0, TN = 0.0;
+    R dQ = R(0), TN = R(0);
     for (int kk = p.nz; kk >= 1; kk--) {
         int64_t k3 = k2 + (int64_t)(kk - 1) * p.stride_k;
-        double Tk = (double)a.T3[k3], Sk = (double)a.S3[k3];
-        double Tm = p.liquidus_freshwater_melting_temperature - p.liquidus_slope * Sk;
+        R Tk = a.T3[k3], Sk = a.S3[k3];
+        R Tm = Tfw - slope * Sk;
         bool freezing = Tk < Tm;
-        if (PART != 1 && freezing) a.T3[k3] = (S)Tm;
+        if (PART != 1 && freezing) a.T3[k3] = Tm;
         if (PART == 2) continue;
-        double dz = a.dz[kk - 1];
-        double dE = (freezing ? 1.0 : 0.0) * rho * cpo * (Tm - Tk);
-        dQ -= dE * dz / p.dt;
-        if (kk == p.nz) TN = freezing ? (double)(S)Tm : Tk;   // the top level after the adjustment
+        R dz = R(a.dz[kk - 1]);
+        R dE = (freezing ? R(1) : R(0)) * rho * cpo * (Tm - Tk);
+        dQ -= dE * dz / R(p.dt);
+        if (kk == p.nz) TN = freezing ? Tm : Tk;   // the top level after the adjustment
     }
     if (PART == 2) return;
     st(a.frazil, k2, dQ);
     int64_t kN = k2 + (int64_t)(p.nz - 1) * p.stride_k;
-    double SN = (double)a.S3[kN];
-    double Si = ld(a.Si, k2), h = ld(a.hi, k2), aleph = ld(a.aleph, k2), hc = ld(a.hc, k2);
-    double Tsi = (p.conductive && a.Tint) ? ld(a.Tint, k2) : 0.0;
-    double Qio, Tb, Sb;
+    R SN = a.S3[kN];
+    R Si = ldr<R>(a.Si, k2), h = ldr<R>(a.hi, k2), aleph = ldr<R>(a.aleph, k2), hc = ldr<R>(a.hc, k2);
+    R Tsi = (p.conductive && a.Tint) ? ldr<R>(a.Tint, k2) : R(0);
+    R Qio, Tb, Sb;
     if (p.formulation == 1) {
-        double Tm = p.liquidus_freshwater_melting_temperature - p.liquidus_slope * SN;
-        Qio = rho * cpo * p.heat_transfer_coefficient * p.friction_velocity * (TN - Tm) * aleph;
+        R Tm = Tfw - slope * SN;
+        Qio = rho * cpo * R(p.heat_transfer_coefficient) * R(p.friction_velocity) * (TN - Tm) * aleph;
         Tb = Tm;
         Sb = SN;
     } else {
         // solve_interface_conditions (sea_ice_ocean_heat_flux_formulations.jl:280-313)
-        double E = p.reference_latent_heat;
-        double kap = 0.0, Ti = 0.0;
+        R E = R(p.reference_latent_heat);
+        R kap = R(0), Ti = R(0);
         if (p.conductive) {
-            kap = h >= hc ? p.ice_conductivity / (h * E) : 0.0;
+            kap = h >= hc ? R(p.ice_conductivity) / (h * E) : R(0);
             Ti = Tsi;
         }
-        double l1 = -p.liquidus_slope, l2 = p.liquidus_freshwater_melting_temperature;
-        double us = p.friction_velocity;
-        double eta = rho * cpo * p.heat_transfer_coefficient * us / E;
-        double gam = rho * p.salt_transfer_coefficient * us;
-        double th = eta + kap;
-        double qa = th * l1;
-        double qb = -gam - eta * TN - kap * Ti + th * (l2 - l1 * Si);
-        double qc = gam * SN + (eta * TN + kap * Ti - th * l2) * Si;
-        double xi = qa == 0 ? 0.0 : 1 / (2 * qa);
-        double D = M<double>::fmax(qb * qb - 4 * qa * qc, 0.0);   // Julia max
-        double Ss = (-qb - sqrt(D)) * xi;
-        Ss = Ss < 0 ? (-qb + sqrt(D)) * xi : Ss;
-        double Ts = l2 - p.liquidus_slope * Ss;
-        double q = eta * (TN - Ts) + kap * (Ti - Ts);
+        R l1 = -slope, l2 = Tfw;
+        R us = R(p.friction_velocity);
+        R eta = rho * cpo * R(p.heat_transfer_coefficient) * us / E;
+        R gam = rho * R(p.salt_transfer_coefficient) * us;
+        R th = eta + kap;
+        R qa = th * l1;
+        R qb = -gam - eta * TN - kap * Ti + th * (l2 - l1 * Si);
+        R qc = gam * SN + (eta * TN + kap * Ti - th * l2) * Si;
+        R xi = qa == R(0) ? R(0) : R(1) / (R(2) * qa);
+        R D = M<R>::fmax(qb * qb - R(4) * qa * qc, R(0));   // Julia max
+        R sD = M<R>::sqrt(D);
+        R Ss = (-qb - sD) * xi;
+        Ss = Ss < R(0) ? (-qb + sD) * xi : Ss;
+        R Ts = l2 - slope * Ss;
+        R q = eta * (TN - Ts) + kap * (Ti - Ts);
         Qio = E * q * aleph;
         Tb = Ts;
         Sb = Ss;
@@ -81,7 +87,7 @@ __global__ void __launch_bounds__(256) io_kernel(IOArgs<S> a, nesf_io_params p) 
         st(a.Sb, k2, Sb);
     }
     st(a.Qio, k2, Qio);
-    double Ei = ldz(a.Ei, k2), Es = ldz(a.Es, k2);
+    R Ei = ldzr<R>(a.Ei, k2), Es = ldzr<R>(a.Es, k2);
     st(a.Jw, k2, -(Ei + Es) / rho);
     st(a.Js, k2, Ei * Si / rho);
 }

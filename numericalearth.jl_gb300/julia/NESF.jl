@@ -95,7 +95,7 @@ function InterfaceComputations.compute_atmosphere_ocean_fluxes!(coupled_model, f
     params = default_params(:ocean)
     prec = fluxes.precision === :f32 ? NESF_F32_POLISH :
            fluxes.precision === :f32_adaptive ? NESF_F32_ADAPTIVE : NESF_PLAIN_F64
-    opts = SolverOptions(prec, 0, 128, 0, 0, 0, C_NULL, 10.0, 2e-6, 0.8)
+    opts = SolverOptions(prec, 0, 128, 0, 0, 0, C_NULL, 10.0, 2e-6, 0.9)
     stream = CUDA.stream().handle
     check(ccall((:nesf_compute_atmosphere_ocean_fluxes, libnesf), Cint,
                 (Ptr{Cvoid}, Ptr{UInt8}, Ref{AOFields}, Ref{SolverOptions}, Ptr{Cvoid}, Ptr{Cvoid}),

@@ -98,6 +98,42 @@ def test_sea_ice_ocean_fluxes_match_oracle(oracle, coupled64):
     assert (I(ref["frazil_heat"]) < 0).any()   # some supercooled cells formed frazil
 
 
+def test_sea_ice_ocean_fluxes_fp32_fields(oracle, coupled64):
+    """FP32 fields: the sea-ice-ocean fluxes in FP32 arithmetic (the reference's Float32
+    kernel): against the FP64 oracle on the same FP32 inputs, within 1e-5 of each output's
+    largest magnitude and 1e-4 relative on 99 % of the cells, and the frazil-adjusted
+    temperatures within 1e-6 K. The interface heat q = eta (T_N - T_b) + kappa (T_i - T_b)
+    cancels where the ocean is near its melting point, which multiplies the FP32 rounding
+    of the interface salinity (T_b = T_m(S_b)) by |T_b| / |T_N - T_b|."""
+    import torch
+    st = coupled64
+    L = st.layout
+    nz = 3
+    f32 = lambda x: np.asarray(x, dtype=np.float32)
+    T3 = f32(np.stack([st.fields["T_oc"] - 0.2 * k for k in range(nz)])[::-1])
+    S3 = f32(np.stack([st.fields["S_oc"] + 0.1 * k for k in range(nz)])[::-1])
+    dz = np.array([40.0, 20.0, 10.0])
+    spec = P.SeaIceOceanSpec()
+    inputs = {k: f32(st.fields[v]) for k, v in dict(
+        ice_salinity="ice_salinity", ice_thickness="ice_thickness", consolidation_thickness="consolidation_thickness",
+        ice_concentration="ice_concentration", internal_temperature="ice_temperature",
+        ice_mass_flux="ice_mass_flux", snow_mass_flux="snow_mass_flux").items()}
+    ref = oracle.io_fluxes(spec.to_c(nz=nz, stride_k=L.shape[0] * L.shape[1]), L, widen(inputs),
+                           T3.astype(np.float64), S3.astype(np.float64), dz)
+    dev = api.to_device(inputs)
+    out = {k: torch.zeros(L.shape, dtype=torch.float32, device="cuda") for k in F.IO_OUTPUTS}
+    T3d = torch.from_numpy(np.ascontiguousarray(T3)).cuda()
+    api.compute_sea_ice_ocean_fluxes(spec, L, dev, out, T3d, torch.from_numpy(np.ascontiguousarray(S3)).cuda(),
+                                     torch.from_numpy(dz).cuda())
+    torch.cuda.synchronize()
+    I = L.interior
+    for k in F.IO_OUTPUTS:
+        g, r = I(to_numpy(out[k])).astype(np.float64), I(ref[k])
+        assert np.abs(g - r).max() <= 1e-5 * np.abs(r).max(), k
+        assert np.percentile(rel_err(g, r, floor_frac=1e-6), 99) <= 1e-4, k
+    assert np.abs(to_numpy(T3d).astype(np.float64) - ref["T_oc"]).max() <= 1e-6
+
+
 def test_interpolation_matches_oracle(oracle):
     import torch
     st = syn.ao_quarter_land(nx=200, ny=80, dtype=np.float64)
