@@ -132,7 +132,10 @@ def make_state(small):
 #  sea-ice-ocean:          T, S, Si, h, hc, aleph, T_int, E_i, E_s read; T (frazil), 6 outputs -> 16*4 = 64 B
 #  interpolation:          9 exchange-grid outputs (+ 2 FP64 fractional indices read) -> 9*4 + 16 = 52 B
 #  assembly + radiation:   ocean 17 reads + 6 writes, ice 11 reads + 5 writes, radiation 6 diag writes
-BYTES_PER_CELL = {"interp": 52, "ao": 73, "ai": 73, "io": 64, "asm": 4 * (17 + 6 + 11 + 5 + 6 + 4) + 2}
+# DRAM bytes (read + write) per solved cell of one ao_kernel launch: ncu dram__bytes_read.sum +
+# dram__bytes_write.sum on the --small case (10,386,432 + 768 bytes for 162,402 cells), scaled to
+# the workload's launch by its cells
+AO_KERNEL_DRAM_BYTES_PER_CELL = 64.0
 
 
 def train_warm_start(seed=0):
@@ -240,6 +243,28 @@ def step_timeline(model, precision):
         model.capture(precision)
     r = lambda x: None if x is None else round(x, 3)
     return [{"kernel": n, "stream": s, "start_ms": r(b), "end_ms": r(e)} for n, s, b, e in api.timeline(marks)]
+
+
+def kernel_time(model, precision, kernel, reps=10):
+    """Mean duration (ms) of one kernel of the step, from trace events recorded on its stream
+    around it in `reps` replays of the traced graph (its span runs from the previous mark on
+    that stream)."""
+    import torch
+    from nesf import api
+    api.trace_enable(True)
+    spans = []
+    try:
+        model.capture(precision)
+        for _ in range(reps):
+            model.graph_step()
+            torch.cuda.synchronize()
+            for n, _, b, e in api.timeline(api.trace_read()):
+                if n == kernel and b is not None:
+                    spans.append(e - b)
+    finally:
+        api.trace_enable(False)
+        model.capture(precision)
+    return sum(spans) / len(spans) if spans else None
 
 
 def error_stats(model, precision):
@@ -465,18 +490,30 @@ def main():
         line["iterations_per_cell"] = {"ao": per(s_ao), "ao_cold": per(c_ao), "ai": per(s_ai), "ai_cold": per(c_ai),
                                        "ao_plain": per(p_ao), "ai_plain": per(p_ai)}
         line["errors_vs_plain_f64"] = error_stats(model, prec)
-        # roofline of the dominant kernel (HBM: algorithmic bytes / event-timed duration)
+        # roofline of the main solve kernel, the atmosphere-ocean pass 1 (ao_kernel), timed with
+        # trace events on its stream inside graph replays. It is bound by the latency of its
+        # FP32 (and FP64 anchor) arithmetic, not by HBM: the HBM fraction is small, and the
+        # work-table rate (transcendentals and flops per second, NESF_WORK_*) is given beside it.
+        from nesf import _abi as A
         peaks, kind = measured_peaks()
-        top = max(phases, key=phases.get)
-        n_cells = {"interp": (model.layout.nx + 2) * (model.layout.ny + 2),
-                   "ao": (model.layout.nx + 2) * (model.layout.ny + 2),
-                   "ai": (model.layout.nx + 2) * (model.layout.ny + 2),
-                   "io": model.layout.nx * model.layout.ny, "asm": model.layout.nx * model.layout.ny}[top]
-        alg = BYTES_PER_CELL[top] * n_cells
-        achieved = alg / (phases[top] / 1000.0) / 1e9
-        line["roofline"] = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peaks["hbm_gbs"],
-                            "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
-                            "algorithmic_bytes": alg, "peak_source": kind}
+        t_ao = kernel_time(model, prec, "ao_pass1")
+        W = A.WORK
+        alg = W["BYTES_PER_CELL_F32"] * n_ao
+        it_ao = p_ao["iterations"]   # FP64 cold-start iterations of the solved cells
+        work_t = n_ao * (W["PROLOGUE_TRANSCENDENTALS"] + W["EPILOGUE_TRANSCENDENTALS"]) + it_ao * W["ITER_TRANSCENDENTALS"]
+        work_f = n_ao * (W["PROLOGUE_FLOPS"] + W["EPILOGUE_FLOPS"]) + it_ao * W["ITER_FLOPS"]
+        achieved = alg / (t_ao / 1000.0) / 1e9 if t_ao else None
+        traffic = AO_KERNEL_DRAM_BYTES_PER_CELL * n_ao if AO_KERNEL_DRAM_BYTES_PER_CELL else None
+        line["roofline"] = {"bound": "hbm", "kernel": "ao_kernel<float, F32_ADAPTIVE> (atmosphere-ocean pass 1)",
+                            "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                            "frac": achieved / peaks["hbm_gbs"] if achieved else None, "traffic": traffic,
+                            "algorithmic_bytes": alg, "kernel_ms": t_ao, "peak_source": kind,
+                            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch "
+                                              "on the 720x320 case, scaled by cells",
+                            "compute": {"work_transcendentals": work_t, "work_flops": work_f,
+                                        "transcendentals_per_s": work_t / (t_ao / 1000.0) if t_ao else None,
+                                        "flops_per_s": work_f / (t_ao / 1000.0) if t_ao else None,
+                                        "fp64_cold_start_iterations": it_ao}}
         if not args.no_e2e:
             ms_e2e, h2d, d2h = e2e_step_time(model, prec, max(3, args.steps // 2), 1)
             line["e2e"] = {"value": cells / (ms_e2e / 1000.0), "unit": "flux cells/s", "h2d_bytes_per_step": h2d,

@@ -616,6 +616,23 @@ int nesf_get_tuning(nesf_context* ctx, nesf_tuning* tuning);
 int nesf_autotune(nesf_context* ctx, const nesf_coupling_step_args* args, const nesf_solver_options* opts,
                   int32_t reps, nesf_tuning* out, void* stream);
 
+/* ------------------------------------------------------- algorithmic work
+ * Work per unit of the similarity solve, the roofline's numerator: transcendental
+ * calls (pow counted as one; sqrt and cbrt included) and other floating-point
+ * operations, per iteration of the reference's fixed point (three similarity
+ * profiles, six psi evaluations, q_s, gustiness, roughness) and per cell for the
+ * prologue and the flux epilogue. A solve's work is the sum over its cells of
+ * PROLOGUE + iterations * ITER + EPILOGUE, the iterations those of the FP64 cold
+ * start (the reference's own count), so a warm start shows as a higher rate. */
+#define NESF_WORK_ITER_TRANSCENDENTALS 55
+#define NESF_WORK_ITER_FLOPS 300
+#define NESF_WORK_PROLOGUE_TRANSCENDENTALS 2
+#define NESF_WORK_PROLOGUE_FLOPS 20
+#define NESF_WORK_EPILOGUE_TRANSCENDENTALS 1
+#define NESF_WORK_EPILOGUE_FLOPS 35
+/* bytes per solved cell with FP32 fields: 9 inputs and 9 outputs of 4 bytes */
+#define NESF_WORK_BYTES_PER_CELL_F32 72
+
 /* ---------------------------------------------------------------- tracing
  * Kernel-boundary timeline of the coupling step: with tracing on, each
  * nesf_coupling_step (or a graph captured from one) records a CUDA event at its

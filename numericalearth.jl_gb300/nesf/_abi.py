@@ -243,6 +243,10 @@ TUNING_FIELDS = ("solve_block", "deferred_per_sm", "infer_per_sm", "two_lanes", 
 
 TRACE_MAX = 64
 
+# NESF_WORK_* of include/nesf.h (checked against the header by the tests)
+WORK = {"ITER_TRANSCENDENTALS": 55, "ITER_FLOPS": 300, "PROLOGUE_TRANSCENDENTALS": 2, "PROLOGUE_FLOPS": 20,
+        "EPILOGUE_TRANSCENDENTALS": 1, "EPILOGUE_FLOPS": 35, "BYTES_PER_CELL_F32": 72}
+
 
 class TraceEntry(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("stream", i32), ("pad_", i32), ("t_ms", d)]

@@ -93,3 +93,10 @@ def test_tuning_out_of_range_is_an_argument_error(field, value):
     t = A.Tuning(**{field: value})
     assert lib.nesf_set_tuning(None, C.byref(t)) == A.NESF_ERR_ARG
     assert field in lib.nesf_last_error().decode()
+
+
+def test_work_table_matches_header():
+    """The roofline's work-per-unit table (NESF_WORK_*) as the Python side reads it."""
+    text = open(HEADER).read()
+    found = dict(re.findall(r"#define NESF_WORK_([A-Z0-9_]+)\s+(\d+)", text))
+    assert {k: int(v) for k, v in found.items()} == A.WORK
