@@ -151,6 +151,38 @@ typedef struct {
     double tolerance;                    /* absolute drift tolerance 1e-8                      */
 } nesf_similarity_theory_fluxes;
 
+/* ---------------------------------------------------- CoefficientBasedFluxes
+ * coefficient_based_turbulent_fluxes.jl:142-371: bulk transfer coefficients,
+ * either constant (Cd, Ch, Cq) or LargeYeagerTransferCoefficients (:82-108): the
+ * PolynomialNeutralDragCoefficient (:20-54) with the Large & Yeager (2004)
+ * stability corrections (:288-340), whose stability functions are
+ * large_yeager_stability_functions (similarity_theory_turbulent_fluxes.jl:766-771).
+ * The fixed point is the same iteration (compute_interface_state.jl) with this
+ * formulation's stop criteria (ConvergenceStopCriteria(1e-8, 20) by default). */
+typedef enum { NESF_FLUXES_SIMILARITY_THEORY = 0, NESF_FLUXES_COEFFICIENT_BASED = 1 } nesf_flux_formulation;
+typedef enum { NESF_COEFFICIENTS_CONSTANT = 0, NESF_COEFFICIENTS_LARGE_YEAGER = 1 } nesf_coefficients_kind;
+
+typedef struct {
+    int32_t kind;                              /* nesf_coefficients_kind                  */
+    int32_t stop_kind;                         /* nesf_stop_kind                          */
+    int32_t maxiter;                           /* 20                                      */
+    int32_t polynomial_mask;                   /* CONSTANT: bit i set = coefficient i (Cd,
+                                                  Ch, Cq) is the PolynomialNeutralDragCoefficient
+                                                  of the wind speed (:271), not a number  */
+    double tolerance;                          /* 1e-8                                    */
+    double momentum, temperature, water_vapor; /* constant Cd, Ch, Cq (1e-3 each)        */
+    double von_karman_constant;                /* Large-Yeager: 0.4                       */
+    double drag_a, drag_b, drag_c, drag_d;     /* 2.7, 0.142, 1/13.09, 3.14807e-10        */
+    double high_wind_speed_threshold;          /* 33                                      */
+    double high_wind_drag_coefficient;         /* 2.34e-3                                 */
+    double minimum_wind_speed;                 /* 0.5                                     */
+    double reference_height;                   /* 10                                      */
+    double stable_heat_transfer_coefficient;   /* 18                                      */
+    double unstable_heat_transfer_coefficient; /* 32.7                                    */
+    double moisture_transfer_coefficient;      /* 34.6                                    */
+    nesf_stability_function stability[2];      /* momentum, scalar (linear + Paulson)     */
+} nesf_coefficient_fluxes;
+
 /* ------------------------------------------- interface + component properties */
 typedef enum { NESF_PHASE_LIQUID = 0, NESF_PHASE_ICE = 1 } nesf_phase;
 typedef enum { NESF_RELATIVE_VELOCITY = 0, NESF_WIND_VELOCITY = 1 } nesf_velocity_formulation;
@@ -185,6 +217,9 @@ typedef struct {
     double liquidus_slope;                           /* 0.054                           */
     double interior_reference_density;    /* rho_o (ocean skin temperature)             */
     double interior_heat_capacity;        /* c_o                                         */
+    int32_t flux_formulation;             /* nesf_flux_formulation (similarity theory)   */
+    int32_t pad2_;
+    nesf_coefficient_fluxes coefficients; /* when flux_formulation is coefficient-based */
 } nesf_interface_params;
 
 /* ------------------------------------------------------ solver precision */
@@ -421,6 +456,10 @@ int32_t     nesf_struct_sizes(int64_t* sizes, int32_t n);
 void nesf_default_thermodynamics(nesf_thermodynamics_parameters* p);
 void nesf_default_ao_params(nesf_interface_params* p);      /* ComponentInterfaces AO defaults */
 void nesf_default_ai_params(nesf_interface_params* p);      /* AO defaults + ice/skin changes  */
+/* CoefficientBasedFluxes defaults (coefficient_based_turbulent_fluxes.jl:30-37,92-99,215-229) for
+ * transfer coefficients of `kind`; put in params->coefficients with flux_formulation
+ * NESF_FLUXES_COEFFICIENT_BASED. */
+void nesf_default_coefficient_fluxes(nesf_coefficient_fluxes* c, int32_t kind);
 void nesf_default_io_params(nesf_io_params* p);
 void nesf_default_assembly_params(nesf_assembly_params* p);
 void nesf_default_solver_options(nesf_solver_options* o);

@@ -341,7 +341,8 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     // the learned warm start serves the bulk interface temperature: with a skin temperature the
     // iteration count is set by the temperature's clamped steps, which the network does not predict
-    const bool warm = ws.mlp != nullptr && prec != NESF_PLAIN_F64 && P64.temp_form == NESF_BULK_TEMPERATURE;
+    const bool warm = ws.mlp != nullptr && prec != NESF_PLAIN_F64 && P64.temp_form == NESF_BULK_TEMPERATURE &&
+                      P64.flux_form == NESF_FLUXES_SIMILARITY_THEORY;
     cudaError_t e = cudaMemsetAsync(wl.count, 0, sizeof(unsigned) * 2, stream);
     if (e == cudaSuccess && prec != NESF_PLAIN_F64) e = cudaMemsetAsync(rq.count, 0, 3 * sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;

@@ -356,7 +356,8 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     // warm start (FP32 modes, one member): features in pass 0, the network's guesses before pass 1
-    const bool warm = ws.mlp != nullptr && prec != NESF_PLAIN_F64 && !ens && !skin;
+    const bool warm = ws.mlp != nullptr && prec != NESF_PLAIN_F64 && !ens && !skin &&
+                      P64.flux_form == NESF_FLUXES_SIMILARITY_THEORY;   // the network predicts similarity theory
     float* feat = warm ? ws.feat : nullptr;
     const float* guess = warm ? ws.guess : nullptr;
     cudaError_t e = cudaMemsetAsync(wl.count, 0, sizeof(unsigned) * 2 * nm, stream);

@@ -140,7 +140,7 @@ int32_t nesf_struct_sizes(int64_t* sizes, int32_t n) {
         (int64_t)sizeof(nesf_atmos_grid), (int64_t)sizeof(nesf_exchange_coords), (int64_t)sizeof(nesf_interp_fields),
         (int64_t)sizeof(nesf_assembly_params), (int64_t)sizeof(nesf_assembly_fields),
         (int64_t)sizeof(nesf_coupling_step_args), (int64_t)sizeof(nesf_integral_fields),
-        (int64_t)sizeof(nesf_tuning), (int64_t)sizeof(nesf_trace_entry)};
+        (int64_t)sizeof(nesf_tuning), (int64_t)sizeof(nesf_trace_entry), (int64_t)sizeof(nesf_coefficient_fluxes)};
     int32_t m = (int32_t)(sizeof s / sizeof s[0]);
     for (int32_t k = 0; k < n && k < m; k++) sizes[k] = s[k];
     return m;
@@ -237,6 +237,36 @@ void nesf_default_ao_params(nesf_interface_params* p) {
     p->liquidus_slope = 0.054;
     p->interior_reference_density = 1020;
     p->interior_heat_capacity = 3991.86795711963;
+}
+
+void nesf_default_coefficient_fluxes(nesf_coefficient_fluxes* c, int32_t kind) {
+    memset(c, 0, sizeof *c);
+    c->kind = kind;
+    c->stop_kind = NESF_STOP_CONVERGENCE;    // coefficient_based_turbulent_fluxes.jl:215-229
+    c->maxiter = 20;
+    c->tolerance = 1e-8;
+    if (kind == NESF_COEFFICIENTS_CONSTANT) {
+        c->momentum = c->temperature = c->water_vapor = 1e-3;   // :216
+        return;
+    }
+    c->von_karman_constant = 0.4;            // :92-99
+    c->drag_a = 2.7;                         // :30-37
+    c->drag_b = 0.142;
+    c->drag_c = 1 / 13.09;
+    c->drag_d = 3.14807e-10;
+    c->high_wind_speed_threshold = 33;
+    c->high_wind_drag_coefficient = 2.34e-3;
+    c->minimum_wind_speed = 0.5;
+    c->reference_height = 10;
+    c->stable_heat_transfer_coefficient = 18;
+    c->unstable_heat_transfer_coefficient = 32.7;
+    c->moisture_transfer_coefficient = 34.6;
+    // large_yeager_stability_functions (similarity_theory_turbulent_fluxes.jl:766-771): linear
+    // stable branch (psi = -5 zeta, zeta <= 10; :742-752) + Paulson (:683-710)
+    c->stability[0].kind = NESF_PSI_LINEAR_PAULSON_MOMENTUM;
+    c->stability[0].c[0] = 5; c->stability[0].c[1] = 10; c->stability[0].c[2] = 16; c->stability[0].c[3] = M_PI / 2;
+    c->stability[1].kind = NESF_PSI_LINEAR_PAULSON_SCALAR;
+    c->stability[1].c[0] = 5; c->stability[1].c[1] = 10; c->stability[1].c[2] = 16;
 }
 
 void nesf_default_ai_params(nesf_interface_params* p) {
@@ -407,6 +437,24 @@ static int check_params(const nesf_interface_params* p, const char* who) {
         p->temperature_formulation > NESF_SKIN_TEMPERATURE_DIFFUSIVE)
         return fail(NESF_ERR_ARG, "%s: temperature formulation %d", who, p->temperature_formulation);
     if (p->surface_layer_height <= 0) return fail(NESF_ERR_ARG, "%s: surface_layer_height <= 0", who);
+    if (p->flux_formulation != NESF_FLUXES_SIMILARITY_THEORY && p->flux_formulation != NESF_FLUXES_COEFFICIENT_BASED)
+        return fail(NESF_ERR_ARG, "%s: flux formulation %d", who, p->flux_formulation);
+    if (p->flux_formulation == NESF_FLUXES_COEFFICIENT_BASED) {
+        const nesf_coefficient_fluxes& c = p->coefficients;
+        if (c.kind != NESF_COEFFICIENTS_CONSTANT && c.kind != NESF_COEFFICIENTS_LARGE_YEAGER)
+            return fail(NESF_ERR_ARG, "%s: transfer coefficients kind %d", who, c.kind);
+        if (c.maxiter < 0 || !(c.tolerance >= 0))
+            return fail(NESF_ERR_ARG, "%s: coefficient-based stop criteria (maxiter %d, tolerance %g)", who,
+                        c.maxiter, c.tolerance);
+        if (c.kind == NESF_COEFFICIENTS_LARGE_YEAGER) {
+            if (!(c.reference_height > 0) || !(c.von_karman_constant > 0))
+                return fail(NESF_ERR_ARG, "%s: Large-Yeager reference height and von Karman constant must be > 0",
+                            who);
+            for (int n = 0; n < 2; n++)
+                if (c.stability[n].kind < NESF_PSI_ZERO || c.stability[n].kind > NESF_PSI_LINEAR_PAULSON_SCALAR)
+                    return fail(NESF_ERR_ARG, "%s: stability function kind %d", who, c.stability[n].kind);
+        }
+    }
     return NESF_OK;
 }
 

@@ -98,6 +98,14 @@ template <class R> struct DevIface {
     // ln e_sat(T) = ln p_tr + esA ln(T / T_tr) + esK (1 / T_tr - 1 / T) for the interface's
     // phase: esA = (cp_v - cp_c) / R_v, esK = (L_0 - (cp_v - cp_c) T_0) / R_v; inv_Ttr = 1 / T_tr
     R esA, esK, inv_Ttr;
+    // CoefficientBasedFluxes (flux_form 1): its stop criteria are in stop_kind / maxiter / tol,
+    // Large-Yeager's von Karman constant in vk and its stability functions in psi[0] (momentum)
+    // and psi[1], psi[2] (scalar)
+    int32_t flux_form, coef_kind, poly_mask;
+    R Cd, Ch, Cq;                         // constant transfer coefficients
+    R drag_a, drag_b, drag_c, drag_d;     // PolynomialNeutralDragCoefficient
+    R U_high, Cd_high, U_min;
+    R h0, Ch_stable, Ch_unstable, Cq_ly;  // reference height, Stanton/Dalton factors
 };
 
 // ------------------------------------------------------------- thermodynamics
@@ -392,10 +400,66 @@ __device__ __forceinline__ void surface_const(const DevIface<R>& P, const CellCo
     s.nu_q = air_viscosity(P.rough[2], Ts);
 }
 
-// iterate_interface_fluxes(::SimilarityTheoryFluxes) (:315-385)
+// PolynomialNeutralDragCoefficient (coefficient_based_turbulent_fluxes.jl:48-54), U^6 as (U^3)^2.
+template <class R>
+__device__ __forceinline__ R neutral_drag(const DevIface<R>& P, R U) {
+    U = M<R>::fmax(U, P.U_min);
+    R U3 = U * U * U;
+    return U < P.U_high ? (P.drag_a / U + P.drag_b + P.drag_c * U - P.drag_d * (U3 * U3)) / R(1000) : P.Cd_high;
+}
+
+// iterate_interface_fluxes(::CoefficientBasedFluxes) (coefficient_based_turbulent_fluxes.jl:346-371)
+// with evaluate_coefficients for constants (:269-285) or Large-Yeager (:288-340). Delta h is
+// the surface layer height (compute_interface_state.jl:101). Inlined: P is a kernel parameter,
+// whose address an out-of-line call would copy to local memory.
+template <class R>
+__device__ __forceinline__ void coefficient_fluxes(const DevIface<R>& P, R dU2, R gTv, R A1, R A2, R dth, R dq, R us,
+                                                R ts, R qst, R& us_n, R& ts_n, R& qs_n) {
+    const bool ly = P.coef_kind == NESF_COEFFICIENTS_LARGE_YEAGER;
+    R dU = M<R>::fmax(M<R>::sqrt(dU2), ly ? P.U_min : R(0));
+    R Cd = P.Cd, Ch = P.Ch, Cq = P.Cq;
+    if (P.poly_mask) {   // PolynomialNeutralDragCoefficient slots of a constant SimilarityScales (:271)
+        R Cp = neutral_drag(P, dU);
+        if (P.poly_mask & 1) Cd = Cp;
+        if (P.poly_mask & 2) Ch = Cp;
+        if (P.poly_mask & 4) Cq = Cp;
+    }
+    if (ly) {
+        const R k = P.vk, dh = P.h;
+        R bs = gTv * (ts * A1 + A2 * qst);                 // buoyancy_scale (:308)
+        R zeta = bs == R(0) ? R(0) : dh * (k * bs) / (us * us);   // dh / L, L = u*^2 / (k b*)
+        R psim = stability(P.psi[0], zeta);
+        R psih = stability(P.psi[1], zeta);
+        R lg = M<R>::log(dh / P.h0);
+        R Cdp = us == R(0) ? neutral_drag(P, dU) : us * us / (dU * dU);
+        R UN10 = dU / (R(1) + M<R>::sqrt(Cdp) / k * (lg - psim));
+        UN10 = M<R>::fmax(UN10, P.U_min);
+        R CdN = neutral_drag(P, UN10);
+        R sCdN = M<R>::sqrt(CdN);
+        R ChN = sCdN / R(1000) * (zeta > R(0) ? P.Ch_stable : P.Ch_unstable);
+        R CqN = sCdN / R(1000) * P.Cq_ly;
+        R xim = sCdN / k * (lg - psim);
+        Cd = CdN / ((R(1) + xim) * (R(1) + xim));
+        R xih = sCdN / k * (lg - psih);
+        R ratio = M<R>::sqrt(Cd) / sCdN;
+        Ch = ChN * ratio / (R(1) + ChN * xih);
+        Cq = CqN * ratio / (R(1) + CqN * xih);
+    }
+    R sCd = M<R>::sqrt(Cd);
+    us_n = sCd * dU;
+    ts_n = Cd == R(0) ? R(0) : Ch / sCd * dth;
+    qs_n = Cd == R(0) ? R(0) : Cq / sCd * dq;
+}
+
+// iterate_interface_fluxes(::SimilarityTheoryFluxes) (:315-385), or the coefficient-based
+// formulation's when the interface uses it.
 template <class R>
 __device__ __forceinline__ void iterate_fluxes(const DevIface<R>& P, const CellConst<R>& c, const SurfaceConst<R>& s,
                                                R us, R ts, R qst, R& us_n, R& ts_n, R& qs_n) {
+    if (P.flux_form == NESF_FLUXES_COEFFICIENT_BASED) {
+        coefficient_fluxes(P, c.dU2, s.gTv, s.A1, s.A2, s.dth, s.dq, us, ts, qst, us_n, ts_n, qs_n);
+        return;
+    }
     R bs = s.gTv * (ts * s.A1 + s.A2 * qst);
     R Usg2 = vsgs2(P, us, bs);
     R U = M<R>::sqrt(c.dU2 + Usg2);

@@ -111,6 +111,33 @@ inline DevIface<R> make_dev_iface(const nesf_interface_params& p) {
     d.esA = R(dcp / Rv);
     d.esK = R((L0 - dcp * t.reference_temperature) / Rv);
     d.inv_Ttr = R(1.0 / t.triple_point_temperature);
+    d.flux_form = p.flux_formulation;
+    if (p.flux_formulation == NESF_FLUXES_COEFFICIENT_BASED) {
+        const nesf_coefficient_fluxes& c = p.coefficients;
+        d.coef_kind = c.kind;
+        d.poly_mask = c.kind == NESF_COEFFICIENTS_CONSTANT ? c.polynomial_mask & 7 : 0;
+        d.stop_kind = c.stop_kind;
+        d.maxiter = c.maxiter;
+        d.tol = R(c.tolerance);
+        d.Cd = R(c.momentum); d.Ch = R(c.temperature); d.Cq = R(c.water_vapor);
+        d.vk = R(c.von_karman_constant);
+        d.drag_a = R(c.drag_a); d.drag_b = R(c.drag_b); d.drag_c = R(c.drag_c); d.drag_d = R(c.drag_d);
+        d.U_high = R(c.high_wind_speed_threshold); d.Cd_high = R(c.high_wind_drag_coefficient);
+        d.U_min = R(c.minimum_wind_speed);
+        d.h0 = R(c.reference_height);
+        d.Ch_stable = R(c.stable_heat_transfer_coefficient);
+        d.Ch_unstable = R(c.unstable_heat_transfer_coefficient);
+        d.Cq_ly = R(c.moisture_transfer_coefficient);
+        // the Large-Yeager stability functions take the similarity functions' slots
+        const nesf_stability_function* sf[3] = {&c.stability[0], &c.stability[1], &c.stability[1]};
+        for (int n = 0; n < 3; n++) {
+            d.psi[n].kind = sf[n]->kind;
+            for (int k = 0; k < 12; k++) d.psi[n].c[k] = R(sf[n]->c[k]);
+            double kd[8];
+            derived_stability(*sf[n], kd);
+            for (int k = 0; k < 8; k++) d.psi[n].k[k] = R(kd[k]);
+        }
+    }
     return d;
 }
 

@@ -93,6 +93,21 @@ class SimilarityTheoryFluxesC(C.Structure):
                 ("zero_plane_displacement", d), ("stop_kind", i32), ("maxiter", i32), ("tolerance", d)]
 
 
+FLUXES_SIMILARITY_THEORY = 0
+FLUXES_COEFFICIENT_BASED = 1
+COEFFICIENTS_CONSTANT = 0
+COEFFICIENTS_LARGE_YEAGER = 1
+
+
+class CoefficientFluxes(C.Structure):
+    _fields_ = [("kind", i32), ("stop_kind", i32), ("maxiter", i32), ("polynomial_mask", i32), ("tolerance", d),
+                ("momentum", d), ("temperature", d), ("water_vapor", d), ("von_karman_constant", d),
+                ("drag_a", d), ("drag_b", d), ("drag_c", d), ("drag_d", d), ("high_wind_speed_threshold", d),
+                ("high_wind_drag_coefficient", d), ("minimum_wind_speed", d), ("reference_height", d),
+                ("stable_heat_transfer_coefficient", d), ("unstable_heat_transfer_coefficient", d),
+                ("moisture_transfer_coefficient", d), ("stability", StabilityFunction * 2)]
+
+
 class InterfaceParams(C.Structure):
     _fields_ = [("fluxes", SimilarityTheoryFluxesC), ("thermo", ThermodynamicsParameters),
                 ("humidity_phase", i32), ("has_water_mole_fraction", i32), ("water_mole_fraction", d),
@@ -104,7 +119,8 @@ class InterfaceParams(C.Structure):
                 ("has_radiation", i32), ("pad_", i32),
                 ("stefan_boltzmann_constant", d), ("albedo", d), ("emissivity", d),
                 ("liquidus_freshwater_melting_temperature", d), ("liquidus_slope", d),
-                ("interior_reference_density", d), ("interior_heat_capacity", d)]
+                ("interior_reference_density", d), ("interior_heat_capacity", d),
+                ("flux_formulation", i32), ("pad2_", i32), ("coefficients", CoefficientFluxes)]
 
 
 class SolverOptions(C.Structure):
@@ -257,4 +273,4 @@ STRUCTS_IN_SIZE_ORDER = (Grid, ThermodynamicsParameters, StabilityFunction, Roug
                          SimilarityTheoryFluxesC, InterfaceParams, SolverOptions, Stats, AOFields,
                          AIFields, IOParams, IOFields, AtmosGrid, ExchangeCoords, InterpFields,
                          AssemblyParams, AssemblyFields, CouplingStepArgs, IntegralFields, Tuning,
-                         TraceEntry)
+                         TraceEntry, CoefficientFluxes)

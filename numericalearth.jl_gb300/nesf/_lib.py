@@ -26,6 +26,7 @@ SIGNATURES = {
     "nesf_default_thermodynamics": (None, [P(A.ThermodynamicsParameters)]),
     "nesf_default_ao_params": (None, [P(A.InterfaceParams)]),
     "nesf_default_ai_params": (None, [P(A.InterfaceParams)]),
+    "nesf_default_coefficient_fluxes": (None, [P(A.CoefficientFluxes), C.c_int32]),
     "nesf_default_io_params": (None, [P(A.IOParams)]),
     "nesf_default_assembly_params": (None, [P(A.AssemblyParams)]),
     "nesf_default_solver_options": (None, [P(A.SolverOptions)]),

@@ -399,6 +399,98 @@ class SimilarityTheoryFluxes:
         return c
 
 
+# ------------------------------------------------------- CoefficientBasedFluxes
+@dataclass
+class PolynomialNeutralDragCoefficient:
+    """coefficient_based_turbulent_fluxes.jl:20-54 (Large & Yeager 2004)."""
+    a: float = 2.7
+    b: float = 0.142
+    c: float = 1 / 13.09
+    d: float = 3.14807e-10
+    high_wind_speed_threshold: float = 33.0
+    high_wind_drag_coefficient: float = 2.34e-3
+    minimum_wind_speed: float = 0.5
+
+
+@dataclass
+class LargeYeagerTransferCoefficients:
+    """coefficient_based_turbulent_fluxes.jl:82-108."""
+    von_karman_constant: float = 0.4
+    neutral_drag_coefficient: PolynomialNeutralDragCoefficient = field(
+        default_factory=PolynomialNeutralDragCoefficient)
+    stability_functions: SimilarityScales = field(default_factory=large_yeager_stability_functions)
+    reference_height: float = 10.0
+    stable_heat_transfer_coefficient: float = 18.0
+    unstable_heat_transfer_coefficient: float = 32.7
+    moisture_transfer_coefficient: float = 34.6
+
+
+@dataclass
+class CoefficientBasedFluxes:
+    """coefficient_based_turbulent_fluxes.jl:142-258 (keyword names and defaults):
+    transfer_coefficients a 3-tuple / dict of constants (momentum, temperature,
+    water_vapor) or LargeYeagerTransferCoefficients."""
+    transfer_coefficients: object = (1e-3, 1e-3, 1e-3)
+    solver_stop_criteria: object = None
+    solver_tolerance: float = 1e-8
+    solver_maxiter: int = 20
+
+    def __post_init__(self):
+        if self.solver_stop_criteria is None:
+            self.solver_stop_criteria = ConvergenceStopCriteria(self.solver_tolerance, self.solver_maxiter)
+        tc = self.transfer_coefficients
+        if isinstance(tc, dict):
+            missing = [k for k in ("momentum", "temperature", "water_vapor") if k not in tc]
+            if missing:
+                raise ValueError(f"transfer coefficients must contain momentum, temperature, water_vapor; "
+                                 f"missing {missing}")
+        elif not isinstance(tc, LargeYeagerTransferCoefficients) and len(tc) != 3:
+            raise ValueError(f"transfer coefficients must be (momentum, temperature, water_vapor), got {tc}")
+
+    def coefficients_to_c(self):
+        c = A.CoefficientFluxes()
+        sc = self.solver_stop_criteria
+        if isinstance(sc, FixedIterations):
+            c.stop_kind, c.maxiter, c.tolerance = A.STOP_FIXED_ITERATIONS, sc.iterations, 0.0
+        else:
+            c.stop_kind, c.maxiter, c.tolerance = A.STOP_CONVERGENCE, sc.maxiter, sc.tolerance
+        tc = self.transfer_coefficients
+        if isinstance(tc, LargeYeagerTransferCoefficients):
+            c.kind = A.COEFFICIENTS_LARGE_YEAGER
+            n = tc.neutral_drag_coefficient
+            c.von_karman_constant = tc.von_karman_constant
+            c.drag_a, c.drag_b, c.drag_c, c.drag_d = n.a, n.b, n.c, n.d
+            c.high_wind_speed_threshold = n.high_wind_speed_threshold
+            c.high_wind_drag_coefficient = n.high_wind_drag_coefficient
+            c.minimum_wind_speed = n.minimum_wind_speed
+            c.reference_height = tc.reference_height
+            c.stable_heat_transfer_coefficient = tc.stable_heat_transfer_coefficient
+            c.unstable_heat_transfer_coefficient = tc.unstable_heat_transfer_coefficient
+            c.moisture_transfer_coefficient = tc.moisture_transfer_coefficient
+            c.stability[0] = tc.stability_functions.momentum.to_c()
+            c.stability[1] = tc.stability_functions.temperature.to_c()
+        else:
+            c.kind = A.COEFFICIENTS_CONSTANT
+            vals = (tc["momentum"], tc["temperature"], tc["water_vapor"]) if isinstance(tc, dict) else tuple(tc)
+            poly = [v for v in vals if isinstance(v, PolynomialNeutralDragCoefficient)]
+            if any(p != poly[0] for p in poly):
+                raise NotImplementedError("one PolynomialNeutralDragCoefficient per CoefficientBasedFluxes")
+            if poly:   # evaluate_coefficient(C::PolynomialNeutralDragCoefficient, dU) = C(dU)
+                n = poly[0]
+                c.drag_a, c.drag_b, c.drag_c, c.drag_d = n.a, n.b, n.c, n.d
+                c.high_wind_speed_threshold = n.high_wind_speed_threshold
+                c.high_wind_drag_coefficient = n.high_wind_drag_coefficient
+                c.minimum_wind_speed = n.minimum_wind_speed
+            mask = 0
+            for i, v in enumerate(vals):
+                if isinstance(v, PolynomialNeutralDragCoefficient):
+                    mask |= 1 << i
+                    v = 0.0
+                setattr(c, ("momentum", "temperature", "water_vapor")[i], float(v))
+            c.polynomial_mask = mask
+        return c
+
+
 def atmosphere_sea_ice_similarity_theory(**kw):
     """similarity_theory_turbulent_fluxes.jl:791-794."""
     return SimilarityTheoryFluxes(stability_functions=atmosphere_sea_ice_stability_functions(), **kw)
@@ -484,7 +576,7 @@ class InterfaceSpec:
     """Everything the flux kernel of one interface needs: the flux formulation, the
     InterfaceProperties (interface_states.jl:8-12), atmosphere properties
     (atmosphere_ocean_fluxes.jl:8-10) and the interior properties of the surface."""
-    flux_formulation: SimilarityTheoryFluxes = field(default_factory=SimilarityTheoryFluxes)
+    flux_formulation: object = field(default_factory=SimilarityTheoryFluxes)   # or CoefficientBasedFluxes
     specific_humidity: ImpureSaturationSpecificHumidity = field(default_factory=default_ao_specific_humidity)
     temperature: object = field(default_factory=BulkTemperature)
     velocity: object = field(default_factory=RelativeVelocity)
@@ -503,7 +595,13 @@ class InterfaceSpec:
 
     def to_c(self):
         p = A.InterfaceParams()
-        p.fluxes = self.flux_formulation.to_c()
+        if isinstance(self.flux_formulation, CoefficientBasedFluxes):
+            p.fluxes = SimilarityTheoryFluxes().to_c()   # unused by the coefficient-based iteration
+            p.flux_formulation = A.FLUXES_COEFFICIENT_BASED
+            p.coefficients = self.flux_formulation.coefficients_to_c()
+        else:
+            p.fluxes = self.flux_formulation.to_c()
+            p.flux_formulation = A.FLUXES_SIMILARITY_THEORY
         p.thermo = self.thermodynamics_parameters.to_c()
         q = self.specific_humidity
         p.humidity_phase = A.PHASE_ICE if q.phase == "ice" else A.PHASE_LIQUID

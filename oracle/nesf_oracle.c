@@ -335,6 +335,62 @@ static void iterate_fluxes(const nesf_interface_params* p, const cell_in* c, dou
     *qst = chiq * dq;
 }
 
+/* PolynomialNeutralDragCoefficient (coefficient_based_turbulent_fluxes.jl:48-54) */
+double oracle_neutral_drag(const nesf_coefficient_fluxes* c, double U) {
+    U = jmax(U, c->minimum_wind_speed);
+    double U6 = pow(U, 6);
+    return U < c->high_wind_speed_threshold ? (c->drag_a / U + c->drag_b + c->drag_c * U - c->drag_d * U6) / 1000
+                                            : c->high_wind_drag_coefficient;
+}
+
+/* iterate_interface_fluxes(::CoefficientBasedFluxes) (coefficient_based_turbulent_fluxes.jl:346-371)
+ * with evaluate_coefficients: constants (:269-285) or Large-Yeager (:288-340) */
+static void iterate_coefficient_fluxes(const nesf_interface_params* p, const cell_in* c, double Ts, double qs,
+                                       double dth, double dq, double dh, const istate* prev, double* us,
+                                       double* ts, double* qst) {
+    const nesf_coefficient_fluxes* C = &p->coefficients;
+    int ly = C->kind == NESF_COEFFICIENTS_LARGE_YEAGER;
+    double du, dv;
+    if (p->velocity_formulation == NESF_WIND_VELOCITY) { du = c->ua; dv = c->va; }
+    else { du = c->ua - c->ui; dv = c->va - c->vi; }
+    double Umin = ly ? C->minimum_wind_speed : 0.0;                    /* minimum_wind_speed (:265-267) */
+    double dU = jmax(sqrt(du * du + dv * dv), Umin);
+    double Cd = C->momentum, Ch = C->temperature, Cq = C->water_vapor;
+    if (!ly && (C->polynomial_mask & 7)) {   /* evaluate_coefficient(::PolynomialNeutralDragCoefficient, dU) (:271) */
+        double Cp = oracle_neutral_drag(C, dU);
+        if (C->polynomial_mask & 1) Cd = Cp;
+        if (C->polynomial_mask & 2) Ch = Cp;
+        if (C->polynomial_mask & 4) Cq = Cp;
+    }
+    if (ly) {
+        double k = C->von_karman_constant;
+        double ustar = prev->us;
+        dU = jmax(dU, C->minimum_wind_speed);                           /* :305 */
+        double bstar = oracle_buoyancy_scale(p, prev->ts, prev->qs_, Ts, qs);
+        double L = bstar == 0 ? INFINITY : ustar * ustar / (k * bstar);
+        double zeta = dh / L;
+        double psim = oracle_stability(&C->stability[0], zeta);
+        double psih = oracle_stability(&C->stability[1], zeta);
+        double Cdp = ustar == 0 ? oracle_neutral_drag(C, dU) : ustar * ustar / (dU * dU);
+        double UN10 = dU / (1 + sqrt(Cdp) / k * (log(dh / C->reference_height) - psim));
+        UN10 = jmax(UN10, C->minimum_wind_speed);
+        double CdN = oracle_neutral_drag(C, UN10);
+        int stable = zeta > 0;
+        double ChN = sqrt(CdN) / 1000 * (stable ? C->stable_heat_transfer_coefficient
+                                                : C->unstable_heat_transfer_coefficient);
+        double CqN = sqrt(CdN) / 1000 * C->moisture_transfer_coefficient;
+        double xim = sqrt(CdN) / k * (log(dh / C->reference_height) - psim);
+        Cd = CdN / ((1 + xim) * (1 + xim));
+        double xih = sqrt(CdN) / k * (log(dh / C->reference_height) - psih);
+        double ratio = sqrt(Cd) / sqrt(CdN);
+        Ch = ChN * ratio / (1 + ChN * xih);
+        Cq = CqN * ratio / (1 + CqN * xih);
+    }
+    *us = sqrt(Cd) * dU;
+    *ts = Cd == 0 ? 0.0 : Ch / sqrt(Cd) * dth;
+    *qst = Cd == 0 ? 0.0 : Cq / sqrt(Cd) * dq;
+}
+
 /* Julia clamp: ifelse(x > hi, hi, ifelse(x < lo, lo, x)) (a NaN x stays NaN) */
 static inline double clampd(double x, double lo, double hi) { return x > hi ? hi : (x < lo ? lo : x); }
 
@@ -404,26 +460,38 @@ static istate iterate_state(const nesf_interface_params* p, const cell_in* c, co
     double dth = tha - Ts;
     double dh = p->surface_layer_height;
     istate n;
-    iterate_fluxes(p, c, Ts, qs, dth, dq, dh, prev, &n.us, &n.ts, &n.qs_);
+    if (p->flux_formulation == NESF_FLUXES_COEFFICIENT_BASED)
+        iterate_coefficient_fluxes(p, c, Ts, qs, dth, dq, dh, prev, &n.us, &n.ts, &n.qs_);
+    else
+        iterate_fluxes(p, c, Ts, qs, dth, dq, dh, prev, &n.us, &n.ts, &n.qs_);
     n.T = Ts;
     n.q = qs;
     return n;
 }
 
+/* the flux formulation's solver_stop_criteria kind */
+static int stop_kind_of(const nesf_interface_params* p) {
+    return p->flux_formulation == NESF_FLUXES_COEFFICIENT_BASED ? p->coefficients.stop_kind : p->fluxes.stop_kind;
+}
+
 /* iterating + compute_interface_state (compute_interface_state.jl:10-24,31-58) */
 static istate solve(const nesf_interface_params* p, const cell_in* c, istate s0, int* iters) {
-    const nesf_similarity_theory_fluxes* F = &p->fluxes;
+    /* the flux formulation's solver_stop_criteria */
+    const int coef = p->flux_formulation == NESF_FLUXES_COEFFICIENT_BASED;
+    const int stop_kind = coef ? p->coefficients.stop_kind : p->fluxes.stop_kind;
+    const int maxiter = coef ? p->coefficients.maxiter : p->fluxes.maxiter;
+    const double tolerance = coef ? p->coefficients.tolerance : p->fluxes.tolerance;
     istate sn = s0, sm = s0;
     int it = 0;
     for (;;) {
         int go;
-        if (F->stop_kind == NESF_STOP_FIXED_ITERATIONS) {
-            go = it < F->maxiter;
+        if (stop_kind == NESF_STOP_FIXED_ITERATIONS) {
+            go = it < maxiter;
         } else {
             int hasnt_started = it == 0;
-            int reached = it >= F->maxiter;
+            int reached = it >= maxiter;
             double drift = fabs(sn.us - sm.us) + fabs(sn.ts - sm.ts) + fabs(sn.qs_ - sm.qs_);
-            int converged = drift < F->tolerance;
+            int converged = drift < tolerance;
             go = (!(converged | reached)) | hasnt_started;
         }
         if (!go) break;
@@ -467,7 +535,7 @@ int oracle_ao_fluxes(const nesf_interface_params* p, const nesf_ao_fields* f) {
             istate s0 = {ustar0, ustar0, ustar0, c.Ti, qs0};
             istate s;
             int iters = 0;
-            int needs_to_converge = p->fluxes.stop_kind == NESF_STOP_CONVERGENCE;
+            int needs_to_converge = stop_kind_of(p) == NESF_STOP_CONVERGENCE;
             double ui = c.ui, vi = c.vi;
             if (needs_to_converge && land) {
                 istate z = {0, 0, 0, 273.15, 0};
@@ -537,7 +605,7 @@ int oracle_ai_fluxes(const nesf_interface_params* p, const nesf_ai_fields* f) {
             double qs0 = oracle_surface_specific_humidity(p, c.pa, Ts0);
             istate s0 = {ustar0, ustar0, ustar0, Ts0, qs0};
             int ice_free = aleph == 0;
-            int needs_to_converge = p->fluxes.stop_kind == NESF_STOP_CONVERGENCE;
+            int needs_to_converge = stop_kind_of(p) == NESF_STOP_CONVERGENCE;
             istate s;
             int iters = 0;
             if ((needs_to_converge && land) || ice_free) {

@@ -40,6 +40,7 @@ def load():
             "oracle_virtual_temperature": (d, [P(A.ThermodynamicsParameters), d, d]),
             "oracle_surface_specific_humidity": (d, [P(A.InterfaceParams), d, d]),
             "oracle_stability": (d, [P(A.StabilityFunction), d]),
+            "oracle_neutral_drag": (d, [P(A.CoefficientFluxes), d]),
             "oracle_vsgs2": (d, [P(A.SimilarityTheoryFluxesC), d, d, d]),
             "oracle_momentum_roughness": (d, [P(A.RoughnessLength), d, d, d]),
             "oracle_scalar_roughness": (d, [P(A.RoughnessLength), d, d, d, d]),

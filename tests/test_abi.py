@@ -100,3 +100,10 @@ def test_work_table_matches_header():
     text = open(HEADER).read()
     found = dict(re.findall(r"#define NESF_WORK_([A-Z0-9_]+)\s+(\d+)", text))
     assert {k: int(v) for k, v in found.items()} == A.WORK
+
+
+def test_julia_shim_parameter_blob_size():
+    """The Julia binding's opaque nesf_interface_params blob has the library's size."""
+    shim = os.path.join(os.path.dirname(HEADER), "..", "numericalearth.jl_gb300", "julia", "NESF.jl")
+    m = re.search(r"const PARAMS_BYTES = (\d+)", open(shim).read())
+    assert m and int(m.group(1)) == C.sizeof(A.InterfaceParams)

@@ -214,3 +214,75 @@ def test_exact_area_integrals_round_like_fsum():
     I = L.interior
     terms = (I(a) * I(b))[I(inactive) == 0]
     assert float(ex) == math.fsum(terms)
+
+
+# ------------------------------------------------ CoefficientBasedFluxes (§8 f)
+def _ly_coefficients():
+    return P.CoefficientBasedFluxes(transfer_coefficients=P.LargeYeagerTransferCoefficients()).coefficients_to_c()
+
+
+def test_polynomial_neutral_drag(oracle):
+    """test_coefficient_based_fluxes.jl:16-31: positive and below 5e-3 at 3 m/s, the high-wind
+    cap, the wind floor, monotone in moderate winds; and the polynomial at 10 m/s."""
+    lib = oracle.load()
+    c = _ly_coefficients()
+    p = lambda U: lib.oracle_neutral_drag(C.byref(c), U)
+    assert 0 < p(3.0) < 5e-3
+    assert p(40.0) == pytest.approx(2.34e-3)
+    assert p(0.0) == p(0.5)
+    assert p(20.0) > p(5.0)
+    assert p(10.0) == pytest.approx((2.7 / 10 + 0.142 + 10 / 13.09 - 3.14807e-10 * 1e6) / 1000, rel=1e-14)
+
+
+def test_large_yeager_defaults():
+    """test_coefficient_based_fluxes.jl:59-66, and the library's C defaults equal the Python
+    mirror of the reference constructors (LargeYeagerTransferCoefficients, CoefficientBasedFluxes)."""
+    from nesf import _lib
+    ly = P.LargeYeagerTransferCoefficients()
+    assert (ly.reference_height, ly.stable_heat_transfer_coefficient, ly.unstable_heat_transfer_coefficient,
+            ly.moisture_transfer_coefficient) == (10.0, 18.0, 32.7, 34.6)
+    lib = _lib.load()
+    c = A.CoefficientFluxes()
+    lib.nesf_default_coefficient_fluxes(C.byref(c), A.COEFFICIENTS_LARGE_YEAGER)
+    assert bytes(c) == bytes(_ly_coefficients())
+    f = P.CoefficientBasedFluxes()
+    assert f.solver_stop_criteria == P.ConvergenceStopCriteria(1e-8, 20)
+    with pytest.raises(ValueError):
+        P.CoefficientBasedFluxes(transfer_coefficients=(1e-3, 1e-3))
+    with pytest.raises(ValueError):
+        P.CoefficientBasedFluxes(transfer_coefficients={"momentum": 1e-3})
+
+
+COEFFICIENT_CASES = {
+    # test_coefficient_based_fluxes.jl:90, 123-124, 160-162
+    "constant": lambda: P.CoefficientBasedFluxes(transfer_coefficients=(2e-3, 2e-3, 2e-3)),
+    "polynomial_drag": lambda: P.CoefficientBasedFluxes(
+        transfer_coefficients=(P.PolynomialNeutralDragCoefficient(), 1e-3, 1e-3)),
+    "large_yeager_fixed5": lambda: P.CoefficientBasedFluxes(
+        transfer_coefficients=P.LargeYeagerTransferCoefficients(), solver_stop_criteria=P.FixedIterations(5)),
+    "large_yeager": lambda: P.CoefficientBasedFluxes(transfer_coefficients=P.LargeYeagerTransferCoefficients()),
+}
+
+
+@pytest.mark.parametrize("case", sorted(COEFFICIENT_CASES))
+def test_coefficient_based_fluxes_oracle(oracle, case):
+    """test_coefficient_based_fluxes.jl:72-178: finite fluxes and u* > 0 with each kind of
+    transfer coefficients, on a 1-degree sample; constant coefficients reach their fixed point
+    (u* = sqrt(Cd) dU) after two iterations."""
+    st = syn.ao_1deg(nx=60, ny=30)
+    spec = P.atmosphere_ocean_interface_spec(flux_formulation=COEFFICIENT_CASES[case]())
+    out = oracle.ao_fluxes(spec.to_c(), st.layout, st.fields)
+    I = st.layout.interior
+    for k in ("sensible_heat", "latent_heat", "water_vapor", "x_momentum"):
+        assert np.all(np.isfinite(I(out[k]))), k
+    assert np.all(I(out["friction_velocity"]) > 0)
+    it = st.layout.ring(out["iterations"])
+    if case == "constant":
+        f = st.fields
+        du = I(f["u_atm"]) - (I(f["u_oc"]) + np.roll(I(f["u_oc"]), -1, axis=1)) / 2
+        assert np.all(it == 2)
+        assert np.all(np.isfinite(du))
+    elif case == "large_yeager_fixed5":
+        assert np.all(it == 5)
+    else:
+        assert it.max() <= 20
