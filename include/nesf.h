@@ -183,6 +183,18 @@ typedef struct {
     nesf_stability_function stability[2];      /* momentum, scalar (linear + Paulson)     */
 } nesf_coefficient_fluxes;
 
+/* ------------------------------------------------- surface humidity models
+ * interface_states.jl:20-90 (ImpureSaturationSpecificHumidity: ocean, sea ice) and
+ * 100-230, 587-651 (land: BulkHumidity, FractionalHumidity, SkinHumidity). */
+typedef enum {
+    NESF_HUMIDITY_IMPURE_SATURATION = 0,   /* x_H2O e_sat(T_s) (the default)                     */
+    NESF_HUMIDITY_BULK = 1,                /* q_sat(T_s) where the land saturation > 0, else 0   */
+    NESF_HUMIDITY_FRACTIONAL = 2,          /* beta q_sat(T_s): beta a constant, or
+                                              min(S / S_c, 1) (CriticalSaturation)              */
+    NESF_HUMIDITY_SKIN = 3                 /* vapor-flux balance with the soil reservoir at the
+                                              bulk land temperature (iterated with the fluxes)   */
+} nesf_humidity_formulation;
+
 /* ------------------------------------------- interface + component properties */
 typedef enum { NESF_PHASE_LIQUID = 0, NESF_PHASE_ICE = 1 } nesf_phase;
 typedef enum { NESF_RELATIVE_VELOCITY = 0, NESF_WIND_VELOCITY = 1 } nesf_velocity_formulation;
@@ -220,6 +232,13 @@ typedef struct {
     int32_t flux_formulation;             /* nesf_flux_formulation (similarity theory)   */
     int32_t pad2_;
     nesf_coefficient_fluxes coefficients; /* when flux_formulation is coefficient-based */
+    int32_t humidity_formulation;         /* nesf_humidity_formulation                   */
+    int32_t pad3_;
+    double evaporation_efficiency;        /* FRACTIONAL: constant beta (used when
+                                             critical_saturation <= 0)                   */
+    double critical_saturation;           /* FRACTIONAL: CriticalSaturation S_c (> 0)    */
+    double skin_surface_thickness;        /* SKIN: saturation depth d                    */
+    double skin_vapor_diffusivity;        /* SKIN: soil vapor diffusivity kappa_q        */
 } nesf_interface_params;
 
 /* ------------------------------------------------------ solver precision */
@@ -292,6 +311,26 @@ typedef struct {
     void* interface_temperature;
     int32_t* iterations;           /* optional: iterations per cell (same layout)         */
 } nesf_ao_fields;
+
+/* ------------------------------------------------ atmosphere-land bundle
+ * _compute_atmosphere_land_interface_state! (atmosphere_land_fluxes.jl:146-251):
+ * interior cells, surface velocities zero, T_s starts at (BulkTemperature: is) the
+ * bulk land temperature, in kelvin (the interface params' temperature offsets
+ * are not applied to land). */
+typedef struct {
+    nesf_grid grid;
+    int32_t dtype;
+    int32_t pad_;
+    const void* u_atm; const void* v_atm; const void* T_atm; const void* p_atm; const void* q_atm;
+    const void* land_temperature;      /* bulk land temperature T (K)                          */
+    const void* saturation;            /* land surface saturation S (BULK, FRACTIONAL with S_c) */
+    /* outputs: AtmosphereSurfaceFluxes + T_s */
+    void* latent_heat; void* sensible_heat; void* water_vapor;
+    void* x_momentum;  void* y_momentum;
+    void* friction_velocity; void* temperature_scale; void* water_vapor_scale;
+    void* interface_temperature;
+    int32_t* iterations;
+} nesf_al_fields;
 
 /* --------------------------------------------- atmosphere-sea-ice bundle
  * _compute_atmosphere_sea_ice_interface_state! (atmosphere_sea_ice_fluxes.jl:65-185) */
@@ -460,6 +499,11 @@ void nesf_default_ai_params(nesf_interface_params* p);      /* AO defaults + ice
  * transfer coefficients of `kind`; put in params->coefficients with flux_formulation
  * NESF_FLUXES_COEFFICIENT_BASED. */
 void nesf_default_coefficient_fluxes(nesf_coefficient_fluxes* c, int32_t kind);
+/* Atmosphere-land defaults (component_interfaces.jl:404-406, 501-521):
+ * SimilarityTheoryFluxes with large_yeager_stability_functions and constant
+ * roughness lengths 0.1 m (momentum) / 0.01 m (scalars), BulkTemperature,
+ * RelativeVelocity, BulkHumidity(Liquid); temperatures in kelvin. */
+void nesf_default_al_params(nesf_interface_params* p);
 void nesf_default_io_params(nesf_io_params* p);
 void nesf_default_assembly_params(nesf_assembly_params* p);
 void nesf_default_solver_options(nesf_solver_options* o);
@@ -497,6 +541,14 @@ int nesf_compute_atmosphere_ocean_fluxes_noalloc(const nesf_interface_params* pa
 int nesf_compute_atmosphere_sea_ice_fluxes(nesf_context* ctx, const nesf_interface_params* params,
                                            const nesf_ai_fields* fields, const nesf_solver_options* opts,
                                            nesf_stats* stats, void* stream);
+/* compute_atmosphere_land_fluxes! (atmosphere_land_fluxes.jl:48-105). The FP32 modes
+ * apply to the BULK, FRACTIONAL and IMPURE_SATURATION humidity models (FP32 sweep +
+ * FP64 polish, FP64 replays in place); SKIN humidity, whose surface humidity is
+ * part of the iterated state, always runs the FP64 iteration. Default parameters:
+ * nesf_default_al_params. */
+int nesf_compute_atmosphere_land_fluxes(nesf_context* ctx, const nesf_interface_params* params,
+                                        const nesf_al_fields* fields, const nesf_solver_options* opts,
+                                        nesf_stats* stats, void* stream);
 
 /* compute_sea_ice_ocean_fluxes! (sea_ice_ocean_fluxes.jl:33-77): interior (:xy) launch */
 int nesf_compute_sea_ice_ocean_fluxes(nesf_context* ctx, const nesf_io_params* params,

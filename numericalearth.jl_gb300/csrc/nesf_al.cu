@@ -1,0 +1,123 @@
+// nesf_al.cu -- atmosphere-land similarity-theory (or coefficient-based) solve.
+//
+// _compute_atmosphere_land_interface_state! (InterfaceComputations/atmosphere_land_fluxes.jl:146-251)
+//
+// One thread per interior cell (the reference launches :xy), SoA loads of the
+// exchange-grid atmosphere state and the land state (bulk temperature in
+// kelvin, surface saturation). The surface does not move (u_s = v_s = 0), T_s is
+// the bulk land temperature (BulkTemperature) and q_s follows the interface's
+// land humidity model. PLAIN runs the reference's FP64 fixed point; the FP32
+// modes run the FP32 sweep + FP64 Newton polish and replay, in place, the cells
+// whose reference answer is path-dependent. SkinHumidity, whose q_s is iterated
+// with the fluxes, always takes the FP64 iteration.
+#include "nesf_solve.cuh"
+
+namespace nesf {
+
+template <class S>
+__device__ __forceinline__ void al_load(const DevIface<double>& P, const ALArgs<S>& a, int64_t k,
+                                        CellConst<double>& c, double& qs) {
+    c.ua = ld(a.ua, k); c.va = ld(a.va, k); c.Ta = ld(a.Ta, k); c.pa = ld(a.pa, k); c.qa = ld(a.qa, k);
+    c.ui = c.vi = 0;                      // surface velocities are zero for land (:187-189)
+    c.du = c.ua; c.dv = c.va;
+    c.dU2 = c.du * c.du + c.dv * c.dv;
+    c.Ti = ld(a.T, k);                    // bulk land temperature: the T_s of BulkTemperature (:173)
+    c.Si = 0;
+    c.hi = c.hs = c.hc = 0;
+    c.sw = c.lw = 0;
+    c.kappa = -1;
+    c.Rth = 0;
+    c.tha = surface_atmosphere_temperature(P, c.Ta, c.qa);
+    c.rho_a = air_density(P, c.Ta, c.pa, c.qa);
+    c.cp_a = c.L_s = 0;
+    c.qres = surface_specific_humidity(P, c.pa, c.Ti);   // saturated at the bulk land temperature
+    const double sat = a.sat ? ld(a.sat, k) : 1.0;
+    // the initial q_s is the saturation humidity (:200-201); BULK and FRACTIONAL recompute
+    // it from the land state every iteration (a constant at a fixed T_s), SKIN iterates it
+    qs = P.hum_form == NESF_HUMIDITY_SKIN || P.hum_form == NESF_HUMIDITY_IMPURE_SATURATION
+             ? c.qres
+             : land_humidity(P, c.pa, c.Ti, sat);
+}
+
+// The flux epilogue (atmosphere_land_fluxes.jl:216-250).
+template <class S>
+__device__ __forceinline__ void al_store(const DevIface<double>& P, const ALArgs<S>& a, int64_t k,
+                                         const CellConst<double>& c, double us, double ts, double qst, double Ts,
+                                         int iters) {
+    double dU = sqrt(c.du * c.du + c.dv * c.dv);
+    double tx = dU == 0 ? 0.0 : -(us * us) * c.du / dU;
+    double ty = dU == 0 ? 0.0 : -(us * us) * c.dv / dU;
+    double rho = c.rho_a;
+    double cp = cp_m(P, c.qa);
+    double Lv = latent_heat_vapor(P, c.Ta);
+    st(a.Qv, k, -rho * Lv * us * qst);
+    st(a.QT, k, -rho * cp * us * ts);
+    st(a.Jv, k, -rho * us * qst);
+    st(a.tx, k, rho * tx);
+    st(a.ty, k, rho * ty);
+    st(a.Ts, k, Ts);
+    st(a.us, k, us);
+    st(a.ts, k, ts);
+    st(a.qs, k, qst);
+    if (a.iters) a.iters[k] = iters;
+}
+
+template <class S, int PREC>
+__global__ void __launch_bounds__(128) al_kernel(ALArgs<S> a, DevIface<double> P64, DevIface<float> P32,
+                                                 SolveOpts so, DevStats* stats) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= (int64_t)a.L.nx * a.L.ny) return;
+    const int i = 1 + (int)(r % a.L.nx), j = 1 + (int)(r / a.L.nx);
+    const int64_t k = a.L.at(i, j);
+    const DevIface<double>& P = P64;
+    CellConst<double> c;
+    double qs0;
+    al_load(P, a, k, c, qs0);
+    SurfaceConst<double> s;
+    surface_const(P, c, c.Ti, qs0, s);
+    double us = 1e-4, ts = 1e-4, qst = 1e-4;   // :200-203
+    int iters = 0, f64it = 0;
+    bool nonconv = false, replayed = false;
+    const bool needs = P.stop_kind == NESF_STOP_CONVERGENCE;
+    if (PREC == NESF_PLAIN_F64 || !needs || P.hum_form == NESF_HUMIDITY_SKIN) {
+        iters = solve_plain<false>(P, c, s, us, ts, qst, nonconv);
+    } else {
+        int f32it = 0, reason = -1;
+        int outcome = solve_fast<false>(P, P32, c, s, us, ts, qst, so, f32it, f64it, reason);
+        iters = f32it + f64it;
+        if (outcome == FAST_REPLAY) {   // the reference's FP64 iteration from its start, in place
+            us = ts = qst = 1e-4;
+            surface_const(P, c, c.Ti, qs0, s);
+            iters = solve_plain<false>(P, c, s, us, ts, qst, nonconv);
+            f64it = iters;
+            replayed = true;
+            if (stats) stats_replay_reason(stats, reason);
+        }
+    }
+    al_store(P, a, k, c, us, ts, qst, c.Ti, iters);
+    if (stats) stats_add(stats, true, true, iters, nonconv, f64it > 0, f64it, replayed, false);
+}
+
+template <class S>
+static cudaError_t launch_al_t(const ALArgs<S>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
+                               SolveOpts so, DevStats* stats, cudaStream_t stream) {
+    const int64_t n = (int64_t)a.L.nx * a.L.ny;
+    const int block = so.block;   // <= 128: the kernel is compiled with __launch_bounds__(128)
+    const unsigned grid = (unsigned)((n + block - 1) / block);
+    if (prec == NESF_PLAIN_F64) al_kernel<S, NESF_PLAIN_F64><<<grid, block, 0, stream>>>(a, P64, P32, so, stats);
+    else al_kernel<S, NESF_F32_POLISH><<<grid, block, 0, stream>>>(a, P64, P32, so, stats);
+    cudaError_t e = cudaGetLastError();
+    trace_mark(so.tracer, "al_solve", stream);
+    return e;
+}
+
+cudaError_t launch_al(const ALArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
+                      SolveOpts so, DevStats* stats, cudaStream_t stream) {
+    return launch_al_t(a, P64, P32, prec, so, stats, stream);
+}
+cudaError_t launch_al(const ALArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
+                      SolveOpts so, DevStats* stats, cudaStream_t stream) {
+    return launch_al_t(a, P64, P32, prec, so, stats, stream);
+}
+
+}  // namespace nesf

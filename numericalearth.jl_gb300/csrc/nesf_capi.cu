@@ -140,7 +140,8 @@ int32_t nesf_struct_sizes(int64_t* sizes, int32_t n) {
         (int64_t)sizeof(nesf_atmos_grid), (int64_t)sizeof(nesf_exchange_coords), (int64_t)sizeof(nesf_interp_fields),
         (int64_t)sizeof(nesf_assembly_params), (int64_t)sizeof(nesf_assembly_fields),
         (int64_t)sizeof(nesf_coupling_step_args), (int64_t)sizeof(nesf_integral_fields),
-        (int64_t)sizeof(nesf_tuning), (int64_t)sizeof(nesf_trace_entry), (int64_t)sizeof(nesf_coefficient_fluxes)};
+        (int64_t)sizeof(nesf_tuning), (int64_t)sizeof(nesf_trace_entry), (int64_t)sizeof(nesf_coefficient_fluxes),
+        (int64_t)sizeof(nesf_al_fields)};
     int32_t m = (int32_t)(sizeof s / sizeof s[0]);
     for (int32_t k = 0; k < n && k < m; k++) sizes[k] = s[k];
     return m;
@@ -267,6 +268,32 @@ void nesf_default_coefficient_fluxes(nesf_coefficient_fluxes* c, int32_t kind) {
     c->stability[0].c[0] = 5; c->stability[0].c[1] = 10; c->stability[0].c[2] = 16; c->stability[0].c[3] = M_PI / 2;
     c->stability[1].kind = NESF_PSI_LINEAR_PAULSON_SCALAR;
     c->stability[1].c[0] = 5; c->stability[1].c[1] = 10; c->stability[1].c[2] = 16;
+}
+
+void nesf_default_al_params(nesf_interface_params* p) {
+    nesf_default_ao_params(p);
+    // default_atmosphere_land_fluxes (component_interfaces.jl:514-521): SimilarityTheoryFluxes
+    // with the Large-Yeager stability functions (atmosphere_land_stability_functions,
+    // similarity_theory_turbulent_fluxes.jl:776-777) and constant roughness lengths
+    nesf_similarity_theory_fluxes& f = p->fluxes;
+    nesf_coefficient_fluxes ly;
+    nesf_default_coefficient_fluxes(&ly, NESF_COEFFICIENTS_LARGE_YEAGER);
+    f.stability[0] = ly.stability[0];
+    f.stability[1] = ly.stability[1];
+    f.stability[2] = ly.stability[1];
+    const double rough[3] = {0.1, 0.01, 0.01};
+    for (int n = 0; n < 3; n++) {
+        memset(&f.roughness[n], 0, sizeof f.roughness[n]);
+        f.roughness[n].kind = NESF_ROUGHNESS_CONSTANT;
+        f.roughness[n].value = rough[n];
+    }
+    p->humidity_phase = NESF_PHASE_LIQUID;      // BulkHumidity(Liquid) (:501-503)
+    p->has_water_mole_fraction = 0;
+    p->water_mole_fraction = 1;
+    p->humidity_formulation = NESF_HUMIDITY_BULK;
+    p->evaporation_efficiency = 1;
+    p->interior_temperature_offset = 0;        // land temperatures in kelvin
+    p->interface_temperature_offset = 0;
 }
 
 void nesf_default_ai_params(nesf_interface_params* p) {
@@ -437,6 +464,8 @@ static int check_params(const nesf_interface_params* p, const char* who) {
         p->temperature_formulation > NESF_SKIN_TEMPERATURE_DIFFUSIVE)
         return fail(NESF_ERR_ARG, "%s: temperature formulation %d", who, p->temperature_formulation);
     if (p->surface_layer_height <= 0) return fail(NESF_ERR_ARG, "%s: surface_layer_height <= 0", who);
+    if (p->humidity_formulation < NESF_HUMIDITY_IMPURE_SATURATION || p->humidity_formulation > NESF_HUMIDITY_SKIN)
+        return fail(NESF_ERR_ARG, "%s: humidity formulation %d", who, p->humidity_formulation);
     if (p->flux_formulation != NESF_FLUXES_SIMILARITY_THEORY && p->flux_formulation != NESF_FLUXES_COEFFICIENT_BASED)
         return fail(NESF_ERR_ARG, "%s: flux formulation %d", who, p->flux_formulation);
     if (p->flux_formulation == NESF_FLUXES_COEFFICIENT_BASED) {
@@ -631,6 +660,8 @@ static AOArgs<S> ao_args(const nesf_ao_fields* f, int64_t member_stride) {
 
 static int check_ao_fields(const nesf_ao_fields* f, const nesf_interface_params* p, const char* who) {
     if (!f) return fail(NESF_ERR_ARG, "%s: null fields", who);
+    if (p->humidity_formulation != NESF_HUMIDITY_IMPURE_SATURATION)
+        return fail(NESF_ERR_UNSUPPORTED, "%s: the ocean surface humidity is ImpureSaturationSpecificHumidity", who);
     int r = check_grid(f->grid, 2, who);
     if (r) return r;
     if (f->dtype != NESF_F64 && f->dtype != NESF_F32) return fail(NESF_ERR_ARG, "%s: dtype %d", who, f->dtype);
@@ -760,6 +791,56 @@ static AIArgs<S> ai_args(const nesf_ai_fields* f) {
     return a;
 }
 
+template <class S>
+static ALArgs<S> al_args(const nesf_al_fields* f) {
+    ALArgs<S> a;
+    a.L = layout(f->grid);
+    a.ua = (const S*)f->u_atm; a.va = (const S*)f->v_atm; a.Ta = (const S*)f->T_atm;
+    a.pa = (const S*)f->p_atm; a.qa = (const S*)f->q_atm;
+    a.T = (const S*)f->land_temperature; a.sat = (const S*)f->saturation;
+    a.Qv = (S*)f->latent_heat; a.QT = (S*)f->sensible_heat; a.Jv = (S*)f->water_vapor;
+    a.tx = (S*)f->x_momentum; a.ty = (S*)f->y_momentum;
+    a.us = (S*)f->friction_velocity; a.ts = (S*)f->temperature_scale; a.qs = (S*)f->water_vapor_scale;
+    a.Ts = (S*)f->interface_temperature;
+    a.iters = f->iterations;
+    return a;
+}
+
+extern "C" int nesf_compute_atmosphere_land_fluxes(nesf_context* ctx, const nesf_interface_params* params,
+                                                   const nesf_al_fields* f, const nesf_solver_options* opts,
+                                                   nesf_stats* stats, void* stream) {
+    const char* who = "nesf_compute_atmosphere_land_fluxes";
+    int r = check_params(params, who);
+    if (r) return r;
+    if (!f) return fail(NESF_ERR_ARG, "%s: null fields", who);
+    if ((r = check_grid(f->grid, 0, who))) return r;
+    if (f->dtype != NESF_F64 && f->dtype != NESF_F32) return fail(NESF_ERR_ARG, "%s: dtype %d", who, f->dtype);
+    const void* req[] = {f->u_atm, f->v_atm, f->T_atm, f->p_atm, f->q_atm, f->land_temperature};
+    for (const void* q : req)
+        if (!q) return fail(NESF_ERR_ARG, "%s: a required array is NULL", who);
+    if (params->temperature_formulation != NESF_BULK_TEMPERATURE)
+        return fail(NESF_ERR_UNSUPPORTED, "%s: the land interface takes BulkTemperature", who);
+    const int hf = params->humidity_formulation;
+    if ((hf == NESF_HUMIDITY_BULK || (hf == NESF_HUMIDITY_FRACTIONAL && params->critical_saturation > 0)) &&
+        !f->saturation)
+        return fail(NESF_ERR_ARG, "%s: the humidity model needs the land saturation", who);
+    if (hf == NESF_HUMIDITY_SKIN && !(params->skin_surface_thickness > 0 && params->skin_vapor_diffusivity >= 0))
+        return fail(NESF_ERR_ARG, "%s: SkinHumidity needs surface_thickness > 0 and vapor_diffusivity >= 0", who);
+    nesf_solver_options o = options_or_default(opts);
+    if ((r = check_options(o, who))) return r;
+    if ((r = context_or_default(&ctx))) return r;
+    std::lock_guard<std::mutex> lk(ctx->lock);
+    DeviceGuard g(ctx->device);
+    DevIface<double> P64 = make_dev_iface<double>(*params);
+    DevIface<float> P32 = make_dev_iface<float>(*params);
+    cudaStream_t s = (cudaStream_t)stream;
+    SolveOpts so = solve_opts(o, ctx);
+    return with_stats(ctx, stats, s, [&](DevStats* ds) {
+        if (f->dtype == NESF_F64) return launch_al(al_args<double>(f), P64, P32, o.precision, so, ds, s);
+        return launch_al(al_args<float>(f), P64, P32, o.precision, so, ds, s);
+    });
+}
+
 // The sea-ice solve; `after_solve` (optional) is recorded on the stream once the
 // pass-1 solve is enqueued, before the packed polish and replay passes.
 static int sea_ice_fluxes(nesf_context* ctx, const nesf_interface_params* params, const nesf_ai_fields* f,
@@ -777,6 +858,8 @@ static int sea_ice_fluxes(nesf_context* ctx, const nesf_interface_params* params
         if (!q) return fail(NESF_ERR_ARG, "%s: a required array is NULL", who);
     if (params->temperature_formulation == NESF_SKIN_TEMPERATURE_DIFFUSIVE)
         return fail(NESF_ERR_UNSUPPORTED, "%s: diffusive skin temperature over sea ice", who);
+    if (params->humidity_formulation != NESF_HUMIDITY_IMPURE_SATURATION)
+        return fail(NESF_ERR_UNSUPPORTED, "%s: the sea-ice surface humidity is ImpureSaturationSpecificHumidity", who);
     if (params->temperature_formulation == NESF_SKIN_TEMPERATURE_CONDUCTIVE && params->snow_conductivity > 0 &&
         !f->snow_thickness)
         return fail(NESF_ERR_ARG, "%s: snow conductivity given but snow_thickness is NULL", who);

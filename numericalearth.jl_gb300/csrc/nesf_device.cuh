@@ -38,6 +38,9 @@ template <> struct M<double> {
     }
     static __device__ __forceinline__ double fabs(double a) { return ::fabs(a); }
     static __device__ __forceinline__ double inf() { return __longlong_as_double(0x7ff0000000000000LL); }
+    // products and sums rounded one at a time (no multiply-add contraction), as Julia rounds them
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
 };
 template <> struct M<float> {
     static __device__ __forceinline__ float log(float x) { return ::logf(x); }
@@ -54,6 +57,8 @@ template <> struct M<float> {
     }
     static __device__ __forceinline__ float fabs(float a) { return ::fabsf(a); }
     static __device__ __forceinline__ float inf() { return __int_as_float(0x7f800000); }
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
 };
 
 // --------------------------------------------------------- device parameters
@@ -106,6 +111,10 @@ template <class R> struct DevIface {
     R drag_a, drag_b, drag_c, drag_d;     // PolynomialNeutralDragCoefficient
     R U_high, Cd_high, U_min;
     R h0, Ch_stable, Ch_unstable, Cq_ly;  // reference height, Stanton/Dalton factors
+    // land surface humidity (nesf_humidity_formulation): constant efficiency, critical
+    // saturation (> 0: CriticalSaturation), soil vapor conductance kappa_q / d
+    int32_t hum_form;
+    R hum_beta, Sc, skin_g;
 };
 
 // ------------------------------------------------------------- thermodynamics
@@ -158,6 +167,33 @@ __device__ __forceinline__ R surface_specific_humidity(const DevIface<R>& P, R p
     R pv = P.x * (EXP ? esat_exp(P, Ts) : esat(P, Ts));
     pv = M<R>::fmin(pv, R(0.999) * pa);
     return P.einv * pv / (pa - (R(1) - P.einv) * pv);
+}
+
+// Land surface humidity at a fixed T_s (compute_interface_humidity, interface_states.jl:587-598):
+// BulkHumidity q_sat where the saturation S > 0, else 0 (:120-125); FractionalHumidity
+// beta q_sat with beta a constant or min(S / S_c, 1) (CriticalSaturation, :152-158).
+// q_sat is the pressure-based saturation humidity (:76-90): x = 1 for land.
+template <class R>
+__device__ __forceinline__ R land_humidity(const DevIface<R>& P, R pa, R Ts, R S) {
+    R qsat = surface_specific_humidity(P, pa, Ts);
+    if (P.hum_form == NESF_HUMIDITY_BULK) return S > R(0) ? qsat : R(0);
+    R beta = P.Sc > R(0) ? M<R>::fmin(S / P.Sc, R(1)) : P.hum_beta;
+    return beta * qsat;
+}
+
+// SkinHumidity's surface humidity from the previous iterate (interface_states.jl:626-651):
+// the soil flux g (q_res - q_s) balances the atmospheric flux J = -rho u* q*, written with
+// dq = q_s_prev - q_a so that it stays finite as dq -> 0.
+// The sums cancel where q_s is close to q_a; each product and sum is rounded on its own, as
+// the reference rounds them, so the FP64 path stays on the reference's iterates.
+template <class R>
+__device__ __forceinline__ R skin_humidity(const DevIface<R>& P, R rho, R qa, R qres, R qs_prev, R us, R qst) {
+    using Mr = M<R>;
+    R Ja = -Mr::mul(Mr::mul(rho, us), qst);
+    R dq = qs_prev - qa;
+    R D = Mr::add(Mr::mul(P.skin_g, dq), Ja);
+    R qs = Mr::add(Mr::mul(Mr::mul(P.skin_g, qres), dq), Mr::mul(Ja, qa)) / D;
+    return D == R(0) ? qs_prev : qs;
 }
 
 // surface_atmosphere_temperature (interface_states.jl:308-317)
@@ -367,6 +403,7 @@ template <class R> struct CellConst {
     R tha;                       // surface_atmosphere_temperature
     R rho_a, cp_a, L_s;          // air density, cp_m, latent_heat_sublim (skin only)
     R Rth;                       // conductive resistance h_s / k_s + h_i / k_i (ice skin only)
+    R qres;                      // SKIN humidity: q_sat of the soil reservoir (bulk land temperature)
 };
 
 // The ice and snow layers' thermal resistance (interface_states.jl:468-524), fixed
@@ -545,6 +582,9 @@ __device__ __forceinline__ void iterate_state(const DevIface<R>& P, const CellCo
         R Ts = skin_temperature(P, c, s.Ts, us, ts, qst, pinned);
         R qs = surface_specific_humidity(P, c.pa, Ts);
         surface_const(P, c, Ts, qs, s);
+    } else if (P.hum_form == NESF_HUMIDITY_SKIN) {   // T_s fixed, q_s iterated
+        R qs = skin_humidity(P, c.rho_a, c.qa, c.qres, s.qs, us, qst);
+        surface_const(P, c, s.Ts, qs, s);
     }
     R a, b, d;
     iterate_fluxes(P, c, s, us, ts, qst, a, b, d);

@@ -111,6 +111,11 @@ inline DevIface<R> make_dev_iface(const nesf_interface_params& p) {
     d.esA = R(dcp / Rv);
     d.esK = R((L0 - dcp * t.reference_temperature) / Rv);
     d.inv_Ttr = R(1.0 / t.triple_point_temperature);
+    d.hum_form = p.humidity_formulation;
+    d.hum_beta = R(p.evaporation_efficiency);
+    d.Sc = R(p.critical_saturation);
+    d.skin_g = p.humidity_formulation == NESF_HUMIDITY_SKIN ? R(p.skin_vapor_diffusivity / p.skin_surface_thickness)
+                                                            : R(0);
     d.flux_form = p.flux_formulation;
     if (p.flux_formulation == NESF_FLUXES_COEFFICIENT_BASED) {
         const nesf_coefficient_fluxes& c = p.coefficients;

@@ -94,6 +94,13 @@ template <class S> struct AOArgs {
     int32_t* iters;
 };
 
+template <class S> struct ALArgs {
+    Layout2 L;
+    const S *ua, *va, *Ta, *pa, *qa, *T, *sat;
+    S *Qv, *QT, *Jv, *tx, *ty, *us, *ts, *qs, *Ts;
+    int32_t* iters;
+};
+
 template <class S> struct AIArgs {
     Layout2 L;
     const S *ua, *va, *Ta, *pa, *qa, *To, *So, *hi, *hs, *hc, *aleph;
@@ -119,7 +126,7 @@ __device__ __forceinline__ void convert_const(const CellConst<R>& a, CellConst<Q
     b.ui = Q(a.ui); b.vi = Q(a.vi); b.Ti = Q(a.Ti); b.Si = Q(a.Si);
     b.hi = Q(a.hi); b.hs = Q(a.hs); b.hc = Q(a.hc); b.sw = Q(a.sw); b.lw = Q(a.lw); b.kappa = Q(a.kappa);
     b.du = Q(a.du); b.dv = Q(a.dv); b.dU2 = Q(a.dU2); b.tha = Q(a.tha);
-    b.rho_a = Q(a.rho_a); b.cp_a = Q(a.cp_a); b.L_s = Q(a.L_s); b.Rth = Q(a.Rth);
+    b.rho_a = Q(a.rho_a); b.cp_a = Q(a.cp_a); b.L_s = Q(a.L_s); b.Rth = Q(a.Rth); b.qres = Q(a.qres);
 }
 
 template <class R, class Q>
@@ -828,6 +835,10 @@ cudaError_t launch_ai(const AIArgs<double>& a, const DevIface<double>& P64, cons
 cudaError_t launch_ai(const AIArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
                       cudaStream_t stream, cudaEvent_t after_solve = nullptr, const TailLane* tail = nullptr);
+cudaError_t launch_al(const ALArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
+                      SolveOpts so, DevStats* stats, cudaStream_t stream);
+cudaError_t launch_al(const ALArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
+                      SolveOpts so, DevStats* stats, cudaStream_t stream);
 template <class S>
 cudaError_t launch_ao_samples(const AOArgs<S>& a, const DevIface<float>& P32, float* feat, float* targ,
                               cudaStream_t s);

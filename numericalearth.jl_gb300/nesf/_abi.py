@@ -120,7 +120,9 @@ class InterfaceParams(C.Structure):
                 ("stefan_boltzmann_constant", d), ("albedo", d), ("emissivity", d),
                 ("liquidus_freshwater_melting_temperature", d), ("liquidus_slope", d),
                 ("interior_reference_density", d), ("interior_heat_capacity", d),
-                ("flux_formulation", i32), ("pad2_", i32), ("coefficients", CoefficientFluxes)]
+                ("flux_formulation", i32), ("pad2_", i32), ("coefficients", CoefficientFluxes),
+                ("humidity_formulation", i32), ("pad3_", i32), ("evaporation_efficiency", d),
+                ("critical_saturation", d), ("skin_surface_thickness", d), ("skin_vapor_diffusivity", d)]
 
 
 class SolverOptions(C.Structure):
@@ -150,6 +152,19 @@ class AIFields(C.Structure):
         "consolidation_thickness", "ice_concentration", "inactive", "sw_down", "lw_down",
         "interface_temperature", "latent_heat", "sensible_heat", "water_vapor", "x_momentum",
         "y_momentum", "iterations")]
+
+
+HUMIDITY_IMPURE_SATURATION = 0
+HUMIDITY_BULK = 1
+HUMIDITY_FRACTIONAL = 2
+HUMIDITY_SKIN = 3
+
+
+class ALFields(C.Structure):
+    _fields_ = [("grid", Grid), ("dtype", i32), ("pad_", i32)] + [(n, vp) for n in (
+        "u_atm", "v_atm", "T_atm", "p_atm", "q_atm", "land_temperature", "saturation",
+        "latent_heat", "sensible_heat", "water_vapor", "x_momentum", "y_momentum", "friction_velocity",
+        "temperature_scale", "water_vapor_scale", "interface_temperature", "iterations")]
 
 
 class IOParams(C.Structure):
@@ -273,4 +288,4 @@ STRUCTS_IN_SIZE_ORDER = (Grid, ThermodynamicsParameters, StabilityFunction, Roug
                          SimilarityTheoryFluxesC, InterfaceParams, SolverOptions, Stats, AOFields,
                          AIFields, IOParams, IOFields, AtmosGrid, ExchangeCoords, InterpFields,
                          AssemblyParams, AssemblyFields, CouplingStepArgs, IntegralFields, Tuning,
-                         TraceEntry, CoefficientFluxes)
+                         TraceEntry, CoefficientFluxes, ALFields)

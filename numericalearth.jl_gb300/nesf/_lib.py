@@ -26,6 +26,7 @@ SIGNATURES = {
     "nesf_default_thermodynamics": (None, [P(A.ThermodynamicsParameters)]),
     "nesf_default_ao_params": (None, [P(A.InterfaceParams)]),
     "nesf_default_ai_params": (None, [P(A.InterfaceParams)]),
+    "nesf_default_al_params": (None, [P(A.InterfaceParams)]),
     "nesf_default_coefficient_fluxes": (None, [P(A.CoefficientFluxes), C.c_int32]),
     "nesf_default_io_params": (None, [P(A.IOParams)]),
     "nesf_default_assembly_params": (None, [P(A.AssemblyParams)]),
@@ -41,6 +42,8 @@ SIGNATURES = {
         C.c_int, [P(A.InterfaceParams), P(A.AOFields), P(A.SolverOptions), vp]),
     "nesf_compute_atmosphere_sea_ice_fluxes": (
         C.c_int, [vp, P(A.InterfaceParams), P(A.AIFields), P(A.SolverOptions), P(A.Stats), vp]),
+    "nesf_compute_atmosphere_land_fluxes": (
+        C.c_int, [vp, P(A.InterfaceParams), P(A.ALFields), P(A.SolverOptions), P(A.Stats), vp]),
     "nesf_compute_sea_ice_ocean_fluxes": (C.c_int, [vp, P(A.IOParams), P(A.IOFields), vp]),
     "nesf_compute_fractional_indices": (
         C.c_int, [P(A.Grid), P(A.ExchangeCoords), P(A.AtmosGrid), vp, vp, vp]),

@@ -147,6 +147,25 @@ def compute_atmosphere_sea_ice_fluxes(spec, layout, state, out, precision="f64",
     return stats_dict(st) if st is not None else None
 
 
+def compute_atmosphere_land_fluxes(spec, layout, state, out, precision="f64", stats=False, iterations=None,
+                                   ctx=None, stream=None):
+    """atmosphere_land_fluxes.jl:48-105: `state` holds the exchange-grid atmosphere
+    (u_atm, v_atm, T_atm, p_atm, q_atm) and the land surface (land_temperature in kelvin,
+    saturation); `out` the AtmosphereSurfaceFluxes outputs and interface_temperature."""
+    lib = load()
+    arrays = {k: state.get(k) for k in F.AL_INPUTS}
+    arrays.update({k: out.get(k) for k in F.AL_OUTPUTS})
+    arrays["iterations"] = iterations
+    f = F.pack(A.ALFields, _grid_of(layout), arrays)
+    p = spec.to_c() if hasattr(spec, "to_c") else spec
+    o = solver_options(precision)
+    st = A.Stats() if stats else None
+    ctx = ctx or default_context()
+    check(lib.nesf_compute_atmosphere_land_fluxes(ctx.handle, C.byref(p), C.byref(f), C.byref(o),
+                                                  C.byref(st) if st is not None else None, _stream_handle(stream)))
+    return stats_dict(st) if st is not None else None
+
+
 def compute_sea_ice_ocean_fluxes(spec, layout, state, out, T3, S3, dz, stream=None, ctx=None):
     """sea_ice_ocean_fluxes.jl:33-77. T3/S3: (nz, ny+2hy, nx+2hx) tensors; T3 is mutated
     by frazil formation; dz: float64 tensor of nz layer thicknesses."""

@@ -71,3 +71,5 @@ AI_INPUTS = ("u_atm", "v_atm", "T_atm", "p_atm", "q_atm", "T_oc", "S_oc", "ice_t
              "consolidation_thickness", "ice_concentration", "inactive", "sw_down", "lw_down")
 AI_OUTPUTS = ("latent_heat", "sensible_heat", "water_vapor", "x_momentum", "y_momentum")
 IO_OUTPUTS = ("interface_heat", "frazil_heat", "salt", "freshwater", "interface_T", "interface_S")
+AL_INPUTS = ("u_atm", "v_atm", "T_atm", "p_atm", "q_atm", "land_temperature", "saturation")
+AL_OUTPUTS = AO_OUTPUTS

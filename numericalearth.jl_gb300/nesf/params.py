@@ -504,6 +504,33 @@ class ImpureSaturationSpecificHumidity:
     water_mole_fraction: Optional[float] = None
 
 
+@dataclass
+class BulkHumidity:
+    """interface_states.jl:100-125: q_sat(T_s) where the land saturation > 0, else 0."""
+    phase: str = "liquid"
+
+
+@dataclass
+class CriticalSaturation:
+    """interface_states.jl:128-158: beta = min(S / S_c, 1) (Manabe 1969)."""
+    critical_saturation: float = 0.75
+
+
+@dataclass
+class FractionalHumidity:
+    """interface_states.jl:160-185: q_s = beta q_sat(T_s); efficiency a number or CriticalSaturation."""
+    efficiency: object = field(default_factory=CriticalSaturation)
+    phase: str = "liquid"
+
+
+@dataclass
+class SkinHumidity:
+    """interface_states.jl:187-229, 600-651: q_s from the soil vapor-flux balance."""
+    surface_thickness: float = 0.01
+    vapor_diffusivity: float = 2.5e-5
+    phase: str = "liquid"
+
+
 def default_ao_specific_humidity():
     """component_interfaces.jl:353-358: Liquid with x_H2O = 0.98."""
     return ImpureSaturationSpecificHumidity("liquid", 0.98)
@@ -605,8 +632,24 @@ class InterfaceSpec:
         p.thermo = self.thermodynamics_parameters.to_c()
         q = self.specific_humidity
         p.humidity_phase = A.PHASE_ICE if q.phase == "ice" else A.PHASE_LIQUID
-        p.has_water_mole_fraction = 0 if q.water_mole_fraction is None else 1
-        p.water_mole_fraction = 1.0 if q.water_mole_fraction is None else float(q.water_mole_fraction)
+        x = getattr(q, "water_mole_fraction", None)
+        p.has_water_mole_fraction = 0 if x is None else 1
+        p.water_mole_fraction = 1.0 if x is None else float(x)
+        if isinstance(q, BulkHumidity):
+            p.humidity_formulation = A.HUMIDITY_BULK
+            p.evaporation_efficiency = 1.0
+        elif isinstance(q, FractionalHumidity):
+            p.humidity_formulation = A.HUMIDITY_FRACTIONAL
+            if isinstance(q.efficiency, CriticalSaturation):
+                p.critical_saturation = q.efficiency.critical_saturation
+            else:
+                p.evaporation_efficiency = float(q.efficiency)
+        elif isinstance(q, SkinHumidity):
+            p.humidity_formulation = A.HUMIDITY_SKIN
+            p.skin_surface_thickness = q.surface_thickness
+            p.skin_vapor_diffusivity = q.vapor_diffusivity
+        else:
+            p.humidity_formulation = A.HUMIDITY_IMPURE_SATURATION
         p.velocity_formulation = A.WIND_VELOCITY if isinstance(self.velocity, WindVelocity) else A.RELATIVE_VELOCITY
         t = self.temperature
         p.max_delta_T = 5.0
@@ -651,6 +694,27 @@ def atmosphere_ocean_interface_spec(**kw):
     """ComponentInterfaces defaults for the atmosphere-ocean interface
     (component_interfaces.jl:411-414): SimilarityTheoryFluxes, BulkTemperature,
     RelativeVelocity, ImpureSaturationSpecificHumidity(Liquid, 0.98)."""
+    return InterfaceSpec(**kw)
+
+
+def default_atmosphere_land_fluxes(**kw):
+    """component_interfaces.jl:514-521: SimilarityTheoryFluxes with the Large-Yeager
+    stability functions and constant roughness lengths (0.1 m momentum, 0.01 m scalars)."""
+    kw.setdefault("stability_functions", large_yeager_stability_functions())
+    kw.setdefault("momentum_roughness_length", 0.1)
+    kw.setdefault("temperature_roughness_length", 0.01)
+    kw.setdefault("water_vapor_roughness_length", 0.01)
+    return SimilarityTheoryFluxes(**kw)
+
+
+def atmosphere_land_interface_spec(**kw):
+    """atmosphere_land_interface defaults (atmosphere_land_fluxes.jl:28-37,
+    component_interfaces.jl:404-406, 501-521): default_atmosphere_land_fluxes,
+    BulkTemperature, RelativeVelocity, BulkHumidity(Liquid); land temperatures in kelvin."""
+    kw.setdefault("flux_formulation", default_atmosphere_land_fluxes())
+    kw.setdefault("specific_humidity", BulkHumidity())
+    kw.setdefault("interior_temperature_units", "kelvin")
+    kw.setdefault("interface_temperature_units", "kelvin")
     return InterfaceSpec(**kw)
 
 

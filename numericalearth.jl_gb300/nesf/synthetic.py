@@ -166,6 +166,26 @@ def ao_1deg(seed=1000, nx=360, ny=180, dtype=np.float64, halo=HALO):
     return st
 
 
+def al_1deg(seed=1100, nx=360, ny=180, dtype=np.float64, halo=HALO, dry_fraction=0.2):
+    """Atmosphere-land, 1 degree, all land, atmosphere on the exchange grid: bulk land
+    temperature 271 + 32 cos^2(lat) + N(0, 3) K (kelvin), surface saturation U(0, 1) with
+    `dry_fraction` of the cells dry (0), the atmosphere as over the ocean."""
+    rng = np.random.default_rng(seed)
+    L = Layout(nx, ny, halo, halo)
+    c = lonlat(nx, ny, -90.0, 90.0)
+    _, lat = centres(L, c)
+    lat_int = L.interior(lat)
+    T = 271 + 32 * np.cos(np.deg2rad(lat_int)) ** 2 + rng.normal(0, 3, (ny, nx))
+    at = _atmos_interior(rng, T, nx, ny)
+    sat = rng.uniform(0, 1, (ny, nx))
+    sat[rng.uniform(0, 1, (ny, nx)) < dry_fraction] = 0.0
+    f = {"u_atm": at["u"], "v_atm": at["v"], "T_atm": at["T"], "p_atm": at["p"], "q_atm": at["q"],
+         "land_temperature": T, "saturation": sat}
+    st = SurfaceState(L, c, dtype)
+    st.fields = {k: pad(v, halo, halo).astype(dtype) for k, v in f.items()}
+    return st
+
+
 def _coarse_atmosphere(rng, nxa=640, nya=320, halo=HALO, dtype=np.float32, nt=2, dT_mean=-1.0, dT_std=2.0):
     """Global prescribed atmosphere (JRA55-like 0.5625 degree) with nt snapshots 3 h apart.
     Air temperature follows 271 + 32 cos^2(lat), cooled by up to 30 K poleward of 50 degrees."""

@@ -306,6 +306,7 @@ typedef struct {
     double hi, hs, hc;               /* ice state (skin over ice)         */
     double sw, lw;                   /* downwelling radiation             */
     double kappa;                    /* interior diffusivity              */
+    double sat;                      /* land surface saturation           */
 } cell_in;
 
 typedef struct { double us, ts, qs_, T, q; } istate;  /* u*, theta*, q*, T_s, q_s */
@@ -451,10 +452,42 @@ static double interface_temperature(const nesf_interface_params* p, const cell_i
     return Tp;
 }
 
+/* compute_interface_humidity (interface_states.jl:587-651): ImpureSaturationSpecificHumidity;
+ * BulkHumidity (:120-125); FractionalHumidity with a constant beta or CriticalSaturation
+ * (:152-158, 592-598); SkinHumidity's vapor-flux balance with the previous iterate (:626-651).
+ * saturation_specific_humidity (:76-90) is surface_specific_humidity with x = 1. */
+static double interface_humidity(const nesf_interface_params* p, const cell_in* c, double Ts, const istate* prev) {
+    switch (p->humidity_formulation) {
+    case NESF_HUMIDITY_BULK: {
+        double qsat = oracle_surface_specific_humidity(p, c->pa, Ts);
+        return c->sat > 0 ? qsat : 0.0;
+    }
+    case NESF_HUMIDITY_FRACTIONAL: {
+        double beta = p->critical_saturation > 0 ? jmin(c->sat / p->critical_saturation, 1.0)
+                                                 : p->evaporation_efficiency;
+        double qsat = oracle_surface_specific_humidity(p, c->pa, Ts);
+        return beta * qsat;
+    }
+    case NESF_HUMIDITY_SKIN: {
+        double rho = oracle_air_density(&p->thermo, c->Ta, c->pa, c->qa);
+        double Td = c->Ti;                           /* bulk land temperature at the saturation depth */
+        double qsat = oracle_surface_specific_humidity(p, c->pa, Td);
+        double g = p->skin_vapor_diffusivity / p->skin_surface_thickness;
+        double Ja = -rho * prev->us * prev->qs_;
+        double dq = prev->q - c->qa;
+        double D = g * dq + Ja;
+        double qs = (g * qsat * dq + Ja * c->qa) / D;
+        return D == 0 ? prev->q : qs;
+    }
+    default:
+        return oracle_surface_specific_humidity(p, c->pa, Ts);
+    }
+}
+
 /* iterate_interface_state (compute_interface_state.jl:69-122) */
 static istate iterate_state(const nesf_interface_params* p, const cell_in* c, const istate* prev) {
     double Ts = interface_temperature(p, c, prev);
-    double qs = oracle_surface_specific_humidity(p, c->pa, Ts);
+    double qs = interface_humidity(p, c, Ts, prev);
     double dq = c->qa - qs;
     double tha = surface_atmosphere_temperature(p, c->Ta, c->qa);
     double dth = tha - Ts;
@@ -575,6 +608,53 @@ int oracle_ao_fluxes(const nesf_interface_params* p, const nesf_ao_fields* f) {
 
 /* ---------------------------------------------------------- AI driver
  * _compute_atmosphere_sea_ice_interface_state! (atmosphere_sea_ice_fluxes.jl:65-185) */
+/* ---------------------------------------------------------- AL driver
+ * _compute_atmosphere_land_interface_state! (atmosphere_land_fluxes.jl:146-251), over the
+ * interior (:89-102); T_s = the bulk land temperature (BulkTemperature), surface at rest. */
+int oracle_al_fluxes(const nesf_interface_params* p, const nesf_al_fields* f) {
+    if (f->dtype != NESF_F64) return 1;
+    const nesf_grid* g = &f->grid;
+    const nesf_thermodynamics_parameters* t = &p->thermo;
+    int nth = oracle_get_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nth)
+    for (int j = 1; j <= g->ny; j++) {
+        for (int i = 1; i <= g->nx; i++) {
+            int64_t k = idx2(g, i, j);
+            cell_in c;
+            memset(&c, 0, sizeof c);
+            c.ua = rd(f->u_atm, k); c.va = rd(f->v_atm, k); c.Ta = rd(f->T_atm, k);
+            c.pa = rd(f->p_atm, k); c.qa = rd(f->q_atm, k);
+            c.ui = 0; c.vi = 0;
+            c.Ti = rd(f->land_temperature, k);
+            c.sat = f->saturation ? rd(f->saturation, k) : 1.0;
+            c.kappa = -1.0;
+            double ustar0 = 1e-4;
+            double qs0 = oracle_surface_specific_humidity(p, c.pa, c.Ti);   /* :200-201 */
+            istate s0 = {ustar0, ustar0, ustar0, c.Ti, qs0};
+            int iters = 0;
+            istate s = solve(p, &c, s0, &iters);
+            double du = c.ua, dv = c.va;   /* velocity_difference with u_s = v_s = 0 */
+            double dU = sqrt(du * du + dv * dv);
+            double tx = dU == 0 ? 0.0 : -(s.us * s.us) * du / dU;
+            double ty = dU == 0 ? 0.0 : -(s.us * s.us) * dv / dU;
+            double rho = oracle_air_density(t, c.Ta, c.pa, c.qa);
+            double cp = oracle_cp_m(t, c.qa);
+            double Lv = oracle_latent_heat_vapor(t, c.Ta);
+            wr(f->latent_heat, k, -rho * Lv * s.us * s.qs_);
+            wr(f->sensible_heat, k, -rho * cp * s.us * s.ts);
+            wr(f->water_vapor, k, -rho * s.us * s.qs_);
+            wr(f->x_momentum, k, rho * tx);
+            wr(f->y_momentum, k, rho * ty);
+            wr(f->interface_temperature, k, s.T);
+            wr(f->friction_velocity, k, s.us);
+            wr(f->temperature_scale, k, s.ts);
+            wr(f->water_vapor_scale, k, s.qs_);
+            if (f->iterations) f->iterations[k] = iters;
+        }
+    }
+    return 0;
+}
+
 int oracle_ai_fluxes(const nesf_interface_params* p, const nesf_ai_fields* f) {
     const nesf_grid* g = &f->grid;
     if (f->dtype != NESF_F64) return NESF_ERR_UNSUPPORTED;

@@ -34,6 +34,7 @@ double oracle_surface_specific_humidity(const nesf_interface_params* p, double p
 /* similarity-theory building blocks */
 double oracle_stability(const nesf_stability_function* psi, double zeta);
 double oracle_neutral_drag(const nesf_coefficient_fluxes* c, double U);
+int oracle_al_fluxes(const nesf_interface_params* p, const nesf_al_fields* f);
 double oracle_vsgs2(const nesf_similarity_theory_fluxes* f, double ustar, double bstar, double hbl);
 double oracle_momentum_roughness(const nesf_roughness_length* r, double ustar, double U, double Ts);
 double oracle_scalar_roughness(const nesf_roughness_length* r, double lu, double ustar, double U, double Ts);

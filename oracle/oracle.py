@@ -41,6 +41,7 @@ def load():
             "oracle_surface_specific_humidity": (d, [P(A.InterfaceParams), d, d]),
             "oracle_stability": (d, [P(A.StabilityFunction), d]),
             "oracle_neutral_drag": (d, [P(A.CoefficientFluxes), d]),
+            "oracle_al_fluxes": (C.c_int, [P(A.InterfaceParams), P(A.ALFields)]),
             "oracle_vsgs2": (d, [P(A.SimilarityTheoryFluxesC), d, d, d]),
             "oracle_momentum_roughness": (d, [P(A.RoughnessLength), d, d, d]),
             "oracle_scalar_roughness": (d, [P(A.RoughnessLength), d, d, d, d]),
@@ -93,6 +94,21 @@ def ao_fluxes(params, layout, inputs, with_iterations=True):
     if with_iterations:
         outs["iterations"] = it
     return outs
+
+
+def al_fluxes(params, layout, inputs, with_iterations=True):
+    """oracle_al_fluxes on FP64 host arrays; returns the outputs (and iterations)."""
+    lib = load()
+    arrays = {k: _f64(inputs[k]) if inputs.get(k) is not None else None for k in F.AL_INPUTS}
+    out = {k: np.zeros(layout.shape) for k in F.AL_OUTPUTS}
+    arrays.update(out)
+    its = np.zeros(layout.shape, dtype=np.int32) if with_iterations else None
+    arrays["iterations"] = its
+    f = F.pack(A.ALFields, F.make_grid(layout), arrays, dtype=A.NESF_F64)
+    _check(lib.oracle_al_fluxes(C.byref(params), C.byref(f)), "oracle_al_fluxes")
+    if with_iterations:
+        out["iterations"] = its
+    return out
 
 
 def ai_fluxes(params, layout, inputs, interface_temperature, with_iterations=True):

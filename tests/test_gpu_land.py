@@ -1,0 +1,95 @@
+"""The atmosphere-land solve (compute_atmosphere_land_fluxes!, atmosphere_land_fluxes.jl:48-251)
+on the GPU against the CPU oracle through the C ABI, for each land humidity model
+(BulkHumidity, FractionalHumidity with CriticalSaturation and with a constant efficiency,
+SkinHumidity). Bar as for the ocean: plain FP64 to 1e-12 relative on 99.99 % of the cells and
+1e-11 everywhere with identical iteration counts; the FP32 solvers within 1e-5 (SkinHumidity
+runs the FP64 iteration in every mode). Errors are relative to max(|ref|, 1e-6 max|ref|)."""
+import numpy as np
+import pytest
+
+from helpers import rel_err, to_numpy
+from nesf import api
+from nesf import fields as F
+from nesf import params as P
+from nesf import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+
+MODELS = {"bulk": P.BulkHumidity, "fractional": P.FractionalHumidity,
+          "fractional_const": lambda: P.FractionalHumidity(0.5), "skin": P.SkinHumidity}
+OUT = ("x_momentum", "y_momentum", "sensible_heat", "latent_heat", "water_vapor", "friction_velocity",
+       "temperature_scale", "water_vapor_scale", "interface_temperature")
+
+
+@pytest.fixture(scope="module")
+def state():
+    return syn.al_1deg(nx=180, ny=90)
+
+
+def run(spec, st, precision, dtype=None):
+    import torch
+    dev = api.to_device({k: st.fields[k] for k in F.AL_INPUTS}, dtype=dtype)
+    fdt = dev["u_atm"].dtype
+    out = {k: torch.zeros(st.layout.shape, dtype=fdt, device="cuda") for k in F.AL_OUTPUTS}
+    it = torch.zeros(st.layout.shape, dtype=torch.int32, device="cuda")
+    stats = api.compute_atmosphere_land_fluxes(spec, st.layout, dev, out, precision=precision, iterations=it,
+                                               stats=True)
+    torch.cuda.synchronize()
+    res = {k: to_numpy(v).astype(np.float64) for k, v in out.items()}
+    res["iterations"] = to_numpy(it)
+    return res, stats
+
+
+@pytest.mark.parametrize("model", sorted(MODELS))
+def test_plain_f64_matches_oracle(oracle, state, model):
+    spec = P.atmosphere_land_interface_spec(specific_humidity=MODELS[model]())
+    ref = oracle.al_fluxes(spec.to_c(), state.layout, state.fields)
+    gpu, stats = run(spec, state, "f64")
+    I = state.layout.interior
+    assert np.array_equal(I(gpu["iterations"]), I(ref["iterations"])), model
+    for k in OUT:
+        e = rel_err(I(gpu[k]), I(ref[k]), floor_frac=1e-6)
+        assert np.percentile(e, 99.99) <= 1e-12 and e.max() <= 1e-11, (model, k, float(e.max()))
+    assert stats["cells"] == state.layout.nx * state.layout.ny
+
+
+@pytest.mark.parametrize("precision", ["f32", "f32_adaptive"])
+@pytest.mark.parametrize("model", sorted(MODELS))
+def test_fp32_solvers_within_1e5(oracle, state, model, precision):
+    spec = P.atmosphere_land_interface_spec(specific_humidity=MODELS[model]())
+    ref = oracle.al_fluxes(spec.to_c(), state.layout, state.fields)
+    gpu, stats = run(spec, state, precision)
+    I = state.layout.interior
+    conv = I(ref["iterations"]) < 100   # where the reference stops at maxiter its answer is its 100th iterate
+    for k in OUT:
+        e = rel_err(I(gpu[k]), I(ref[k]), floor_frac=1e-6)[conv]
+        assert e.max() <= 1e-5, (model, precision, k, float(e.max()))
+    if model != "skin":
+        assert stats["polished"] > 0.5 * stats["cells"]   # the FP32 sweep + FP64 polish ran
+
+
+def test_fp32_fields(oracle, state):
+    """FP32 storage through the FP32 solver: within 1e-5 of the FP64 oracle on the same inputs."""
+    spec = P.atmosphere_land_interface_spec()
+    f32 = {k: np.asarray(v, dtype=np.float32).astype(np.float64) for k, v in state.fields.items()}
+    ref = oracle.al_fluxes(spec.to_c(), state.layout, f32)
+    import torch
+    gpu, _ = run(spec, state, "f32", dtype=torch.float32)
+    I = state.layout.interior
+    conv = I(ref["iterations"]) < 100
+    for k in OUT:
+        e = rel_err(I(gpu[k]), I(ref[k]), floor_frac=1e-6)[conv]
+        assert e.max() <= 1e-5, (k, float(e.max()))
+
+
+def test_land_rejects_ocean_only_options(state):
+    from nesf import _lib
+    spec = P.atmosphere_land_interface_spec(temperature=P.SkinTemperature(P.DiffusiveFlux()))
+    with pytest.raises(_lib.NesfError):
+        run(spec, state, "f64")
+    spec = P.atmosphere_land_interface_spec(specific_humidity=P.FractionalHumidity(P.CriticalSaturation(0.5)))
+    import torch
+    dev = api.to_device({k: state.fields[k] for k in F.AL_INPUTS if k != "saturation"})
+    out = {k: torch.zeros(state.layout.shape, dtype=torch.float64, device="cuda") for k in F.AL_OUTPUTS}
+    with pytest.raises(_lib.NesfError):
+        api.compute_atmosphere_land_fluxes(spec, state.layout, dev, out)

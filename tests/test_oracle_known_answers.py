@@ -286,3 +286,75 @@ def test_coefficient_based_fluxes_oracle(oracle, case):
         assert np.all(it == 5)
     else:
         assert it.max() <= 20
+
+
+# ------------------------------------------------ atmosphere-land interface (§8 f)
+def _land_cell(T=290.0, Ta=288.0, qa=0.008, u=5.0, sat=1.0):
+    L, a = one_cell(u_atm=u, v_atm=0.0, T_atm=Ta, p_atm=101325.0, q_atm=qa, land_temperature=T, saturation=sat)
+    return L, a
+
+
+def _land(oracle, q, **cell):
+    L, a = _land_cell(**cell)
+    spec = P.atmosphere_land_interface_spec(specific_humidity=q)
+    out = oracle.al_fluxes(spec.to_c(), L, a)
+    return {k: float(L.interior(v)[0, 0]) for k, v in out.items()}
+
+
+def test_land_defaults():
+    """nesf_default_al_params equals the Python mirror of atmosphere_land_interface's defaults."""
+    from nesf import _lib
+    lib = _lib.load()
+    p = A.InterfaceParams()
+    lib.nesf_default_al_params(C.byref(p))
+    assert bytes(p) == bytes(P.atmosphere_land_interface_spec().to_c())
+
+
+def test_bulk_humidity_dry_surface_takes_dew(oracle):
+    """interface_states.jl:100-103: a dry surface has q_s = 0, so under humid air the vapor
+    flux runs downward (dew/frost); a wet one evaporates into drier air."""
+    dry = _land(oracle, P.BulkHumidity(), sat=0.0)
+    wet = _land(oracle, P.BulkHumidity(), sat=0.3)
+    assert dry["water_vapor"] < 0 and dry["latent_heat"] < 0
+    assert wet["water_vapor"] > 0
+
+
+def test_fractional_humidity_limits(oracle):
+    """FractionalHumidity(CriticalSaturation): beta = min(S / S_c, 1); at S >= S_c it is the
+    wet BulkHumidity; with a constant beta = 0 the surface is dry."""
+    bulk = _land(oracle, P.BulkHumidity(), sat=0.9)
+    frac = _land(oracle, P.FractionalHumidity(P.CriticalSaturation(0.75)), sat=0.9)
+    for k in ("latent_heat", "sensible_heat", "water_vapor", "friction_velocity"):
+        assert frac[k] == bulk[k], k
+    dry_b = _land(oracle, P.BulkHumidity(), sat=0.0)
+    dry_f = _land(oracle, P.FractionalHumidity(0.0), sat=0.9)
+    assert dry_f["water_vapor"] == dry_b["water_vapor"]
+    half = _land(oracle, P.FractionalHumidity(P.CriticalSaturation(0.75)), sat=0.375)   # q_s = q_sat / 2
+    assert dry_b["water_vapor"] < half["water_vapor"] < bulk["water_vapor"]
+
+
+def test_skin_humidity_limits(oracle):
+    """SkinHumidity (interface_states.jl:600-651): a very conductive soil holds q_s at the
+    reservoir's saturation (the wet bulk surface); a sealed soil (kappa_q = 0) drives q_s to
+    q_a and the vapor flux to zero."""
+    wet = _land(oracle, P.BulkHumidity(), sat=1.0)
+    fast = _land(oracle, P.SkinHumidity(surface_thickness=0.01, vapor_diffusivity=1e6))
+    assert fast["water_vapor"] == pytest.approx(wet["water_vapor"], rel=1e-6)
+    sealed = _land(oracle, P.SkinHumidity(surface_thickness=0.01, vapor_diffusivity=0.0))
+    assert abs(sealed["water_vapor"]) < 1e-9 * abs(wet["water_vapor"])
+    mid = _land(oracle, P.SkinHumidity())
+    assert 0 < mid["water_vapor"] < wet["water_vapor"]
+
+
+@pytest.mark.parametrize("q", ["bulk", "fractional", "fractional_const", "skin"])
+def test_land_solve_on_1deg_sample(oracle, q):
+    """Every model gives finite fluxes and u* > 0 over a 1-degree land sample with dry cells."""
+    model = {"bulk": P.BulkHumidity(), "fractional": P.FractionalHumidity(),
+             "fractional_const": P.FractionalHumidity(0.5), "skin": P.SkinHumidity()}[q]
+    st = syn.al_1deg(nx=60, ny=30)
+    out = oracle.al_fluxes(P.atmosphere_land_interface_spec(specific_humidity=model).to_c(), st.layout, st.fields)
+    I = st.layout.interior
+    for k in ("latent_heat", "sensible_heat", "water_vapor", "x_momentum"):
+        assert np.all(np.isfinite(I(out[k]))), k
+    assert np.all(I(out["friction_velocity"]) > 0)
+    assert np.array_equal(I(out["interface_temperature"]), I(st.fields["land_temperature"]))
