@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(128) ai_classify_kernel(AIArgs<S> a, DevIface<
 
 // Pass 1: the compacted ice cells, one thread each.
 template <class S, int PREC, bool SKIN>
-__global__ void __launch_bounds__(128) ai_kernel(AIArgs<S> a, DevIface<double> P64, DevIface<float> P32,
+__global__ void __launch_bounds__(128, PREC == NESF_F32_ADAPTIVE ? 5 : 1) ai_kernel(AIArgs<S> a, DevIface<double> P64, DevIface<float> P32,
                                                  SolveOpts so, WorkList wl, ReplayQueue rq, const float* guess,
                                                  DevStats* stats) {
     const int nxr = a.L.nx + 2;

@@ -79,7 +79,9 @@ __global__ void __launch_bounds__(128) al_kernel(ALArgs<S> a, DevIface<double> P
     int iters = 0, f64it = 0;
     bool nonconv = false, replayed = false;
     const bool needs = P.stop_kind == NESF_STOP_CONVERGENCE;
-    if (PREC == NESF_PLAIN_F64 || !needs || P.hum_form == NESF_HUMIDITY_SKIN) {
+    if (P.hum_form == NESF_HUMIDITY_SKIN) {
+        iters = solve_plain<false, true>(P, c, s, us, ts, qst, nonconv);
+    } else if (PREC == NESF_PLAIN_F64 || !needs) {
         iters = solve_plain<false>(P, c, s, us, ts, qst, nonconv);
     } else {
         int f32it = 0, reason = -1;

@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(128) ao_classify_kernel(AOArgs<S> a, DevIface<
 
 // Pass 1: the compacted cells (unstable first, then stable), one thread each.
 template <class S, int PREC, bool SKIN, bool ENS>
-__global__ void __launch_bounds__(128, ENS ? 4 : 3) ao_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
+__global__ void __launch_bounds__(128, ENS ? 4 : (PREC == NESF_F32_ADAPTIVE ? 5 : 3)) ao_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
                                                               const DevIface<double>* __restrict__ P64s,
                                                               const DevIface<float>* __restrict__ P32s, SolveOpts so,
                                                               WorkList wl, ReplayQueue rq, const float* guess,

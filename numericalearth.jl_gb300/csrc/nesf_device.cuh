@@ -493,7 +493,7 @@ __device__ __forceinline__ void coefficient_fluxes(const DevIface<R>& P, R dU2, 
 template <class R>
 __device__ __forceinline__ void iterate_fluxes(const DevIface<R>& P, const CellConst<R>& c, const SurfaceConst<R>& s,
                                                R us, R ts, R qst, R& us_n, R& ts_n, R& qs_n) {
-    if (P.flux_form == NESF_FLUXES_COEFFICIENT_BASED) {
+    if (__builtin_expect(P.flux_form == NESF_FLUXES_COEFFICIENT_BASED, 0)) {   // off the hot path's layout
         coefficient_fluxes(P, c.dU2, s.gTv, s.A1, s.A2, s.dth, s.dq, us, ts, qst, us_n, ts_n, qs_n);
         return;
     }
@@ -575,14 +575,16 @@ __device__ __forceinline__ R skin_temperature(const DevIface<R>& P, const CellCo
 
 // One iterate_interface_state (compute_interface_state.jl:69-122). For the bulk
 // formulation `s` is fixed; for skin formulations it is rebuilt from the new T_s.
-template <class R, bool SKIN>
+// QSKIN (land SkinHumidity): T_s fixed, q_s iterated from the previous iterate; a template
+// flag so that the other solves carry none of its code or registers.
+template <class R, bool SKIN, bool QSKIN = false>
 __device__ __forceinline__ void iterate_state(const DevIface<R>& P, const CellConst<R>& c, SurfaceConst<R>& s,
                                               R& us, R& ts, R& qst, bool* pinned = nullptr) {
     if (SKIN) {
         R Ts = skin_temperature(P, c, s.Ts, us, ts, qst, pinned);
         R qs = surface_specific_humidity(P, c.pa, Ts);
         surface_const(P, c, Ts, qs, s);
-    } else if (P.hum_form == NESF_HUMIDITY_SKIN) {   // T_s fixed, q_s iterated
+    } else if (QSKIN) {   // T_s fixed, q_s iterated
         R qs = skin_humidity(P, c.rho_a, c.qa, c.qres, s.qs, us, qst);
         surface_const(P, c, s.Ts, qs, s);
     }
@@ -596,18 +598,18 @@ __device__ __forceinline__ void iterate_state(const DevIface<R>& P, const CellCo
 // compute_interface_state with ConvergenceStopCriteria / FixedIterations
 // (compute_interface_state.jl:10-24, 31-58). Returns the iteration count; the
 // last drift is left in `drift`.
-template <class R, bool SKIN>
+template <class R, bool SKIN, bool QSKIN = false>
 __device__ __forceinline__ int fixed_point(const DevIface<R>& P, const CellConst<R>& c, SurfaceConst<R>& s,
                                            R& us, R& ts, R& qst, int maxiter, R& drift) {
     int it = 0;
     drift = M<R>::inf();
     if (P.stop_kind == NESF_STOP_FIXED_ITERATIONS) {
-        for (; it < maxiter; it++) iterate_state<R, SKIN>(P, c, s, us, ts, qst);
+        for (; it < maxiter; it++) iterate_state<R, SKIN, QSKIN>(P, c, s, us, ts, qst);
         return it;
     }
     do {
         R u0 = us, t0 = ts, q0 = qst;
-        iterate_state<R, SKIN>(P, c, s, us, ts, qst);
+        iterate_state<R, SKIN, QSKIN>(P, c, s, us, ts, qst);
         it++;
         drift = M<R>::fabs(us - u0) + M<R>::fabs(ts - t0) + M<R>::fabs(qst - q0);
     } while (!(drift < P.tol) && it < maxiter);
