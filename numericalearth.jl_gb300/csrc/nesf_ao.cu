@@ -158,12 +158,19 @@ __global__ void __launch_bounds__(128) ao_classify_kernel(AOArgs<S> a, DevIface<
     bool needs = P.stop_kind == NESF_STOP_CONVERGENCE;
     bool active = in && !land;
     bool stable = false;
+    mlp::Features F;
     if (active) {
-        float Ts = (float)(ld(a.To, k) + P.off_int);
-        stable = stable_class(Pf, ldf(a.Ta, k), ldf(a.pa, k), ldf(a.qa, k), Ts);
+        if (feat) {
+            // the bulk Richardson number of the features has the sign of the buoyancy flux
+            F = ao_features(Pf, a, k);
+            stable = F.f[0] > 0.0f;
+        } else {
+            float Ts = (float)(ld(a.To, k) + P.off_int);
+            stable = stable_class(Pf, ldf(a.Ta, k), ldf(a.pa, k), ldf(a.qa, k), Ts);
+        }
     }
     int64_t slot = worklist_push(wl, m, active, stable, (uint32_t)r);
-    if (feat && slot >= 0) mlp::store_features(feat, slot, ao_features(Pf, a, k));
+    if (feat && slot >= 0) mlp::store_features(feat, slot, F);
     if (in && land) {
         CellConst<double> c;
         bool l;

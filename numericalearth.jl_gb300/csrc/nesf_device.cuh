@@ -161,10 +161,11 @@ template <class R> __device__ __forceinline__ R virtual_temperature(const DevIfa
 }
 
 // surface_specific_humidity(::ImpureSaturationSpecificHumidity)
-// (InterfaceComputations/interface_states.jl:55-74); EXP: e_sat from esat_exp.
+// (InterfaceComputations/interface_states.jl:55-74); EXP: e_sat from esat_exp, which FP32
+// (classification, network features) always takes.
 template <class R, bool EXP = false>
 __device__ __forceinline__ R surface_specific_humidity(const DevIface<R>& P, R pa, R Ts) {
-    R pv = P.x * (EXP ? esat_exp(P, Ts) : esat(P, Ts));
+    R pv = P.x * ((EXP || sizeof(R) == 4) ? esat_exp(P, Ts) : esat(P, Ts));
     pv = M<R>::fmin(pv, R(0.999) * pa);
     return P.einv * pv / (pa - (R(1) - P.einv) * pv);
 }
