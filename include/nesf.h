@@ -184,16 +184,26 @@ typedef struct {
 } nesf_coefficient_fluxes;
 
 /* ------------------------------------------------- surface humidity models
- * interface_states.jl:20-90 (ImpureSaturationSpecificHumidity: ocean, sea ice) and
- * 100-230, 587-651 (land: BulkHumidity, FractionalHumidity, SkinHumidity). */
+ * interface_states.jl:20-90 (ImpureSaturationSpecificHumidity: ocean, sea ice),
+ * 100-230, 587-651 (land: BulkHumidity, FractionalHumidity, SkinHumidity) and
+ * dry_layer_humidity.jl:216-366 (land: DryLayerHumidity). */
 typedef enum {
     NESF_HUMIDITY_IMPURE_SATURATION = 0,   /* x_H2O e_sat(T_s) (the default)                     */
     NESF_HUMIDITY_BULK = 1,                /* q_sat(T_s) where the land saturation > 0, else 0   */
     NESF_HUMIDITY_FRACTIONAL = 2,          /* beta q_sat(T_s): beta a constant, or
                                               min(S / S_c, 1) (CriticalSaturation)              */
-    NESF_HUMIDITY_SKIN = 3                 /* vapor-flux balance with the soil reservoir at the
+    NESF_HUMIDITY_SKIN = 3,                /* vapor-flux balance with the soil reservoir at the
                                               bulk land temperature (iterated with the fluxes)   */
+    NESF_HUMIDITY_DRY_LAYER = 4            /* vapor-flux balance across a dry surface layer whose
+                                              depth follows the land saturation, blended with the
+                                              saturated skin (iterated with the fluxes)          */
 } nesf_humidity_formulation;
+
+/* DryLayerVaporPistonVelocity's tortuosity (dry_layer_humidity.jl:111-127, 252-263). */
+typedef enum {
+    NESF_TORTUOSITY_CONSTANT = 0,          /* D_eff = D_0                                        */
+    NESF_TORTUOSITY_POWER_LAW = 1          /* Millington-Quirk: D_0 theta_g^(10/3) / nu^2        */
+} nesf_tortuosity;
 
 /* ------------------------------------------- interface + component properties */
 typedef enum { NESF_PHASE_LIQUID = 0, NESF_PHASE_ICE = 1 } nesf_phase;
@@ -239,6 +249,18 @@ typedef struct {
     double critical_saturation;           /* FRACTIONAL: CriticalSaturation S_c (> 0)    */
     double skin_surface_thickness;        /* SKIN: saturation depth d                    */
     double skin_vapor_diffusivity;        /* SKIN: soil vapor diffusivity kappa_q        */
+    /* DRY_LAYER (DryLayerHumidity with StorageBasedDryLayerDepth and
+       DryLayerVaporPistonVelocity, dry_layer_humidity.jl:81-100, 155-167, 216-235) */
+    int32_t tortuosity;                   /* nesf_tortuosity                             */
+    int32_t pad4_;
+    double maximum_dry_layer_depth;       /* delta_max (m)                               */
+    double dry_layer_onset_saturation;    /* S_c: the dry layer appears below it (> 0)   */
+    double dry_layer_exponent;            /* eta (2)                                     */
+    double minimum_dry_layer_depth;       /* delta_min (m, > 0)                          */
+    double molecular_diffusivity;         /* D_0 (m^2/s)                                 */
+    double wet_transition_width;          /* logistic blend width (5 delta_min); 0 = sharp */
+    double thermal_exchange_depth;        /* l_T (m, > 0)                                */
+    double porosity;                      /* nu (> 0 for the power-law tortuosity)       */
 } nesf_interface_params;
 
 /* ------------------------------------------------------ solver precision */

@@ -8,11 +8,54 @@
 // the bulk land temperature (BulkTemperature) and q_s follows the interface's
 // land humidity model. PLAIN runs the reference's FP64 fixed point; the FP32
 // modes run the FP32 sweep + FP64 Newton polish and replay, in place, the cells
-// whose reference answer is path-dependent. SkinHumidity, whose q_s is iterated
-// with the fluxes, always takes the FP64 iteration.
+// whose reference answer is path-dependent. SkinHumidity and DryLayerHumidity, whose
+// q_s is iterated with the fluxes, always take the FP64 iteration.
+#include <cfloat>
+
 #include "nesf_solve.cuh"
 
 namespace nesf {
+
+// theta^(10/3) correctly rounded (the Millington-Quirk power, dry_layer_humidity.jl:262). The
+// exponent is 10/3 rounded to double, p = 10/3 + d with d = 2^-51 / 3, so x^p = x^3 cbrt(x) x^d:
+// x^3 as an exact double-double (fma products), cbrt(x) refined to double-double by one Newton
+// step on c^3 = x, x^d = 1 + d ln x, and one rounding at the end. Where the vapor balance
+// cancels, the fixed point amplifies a last-place change of this power a thousandfold, so the
+// power must be the correctly rounded one that the reference's pow approximates.
+__device__ __forceinline__ double pow_ten_thirds(double x) {
+    if (!(x > 0x1p-300) || !(x < 0x1p300)) return pow(x, 10.0 / 3.0);
+    const double x2 = x * x, x2l = fma(x, x, -x2);
+    const double x3 = x2 * x, x3l = fma(x2, x, -x3) + x2l * x;
+    const double c = cbrt(x);
+    const double c2 = c * c, c2l = fma(c, c, -c2);
+    const double c3 = c2 * c, c3l = fma(c2, c, -c3) + c2l * c;
+    const double cl = -((c3 - x) + c3l) / (3.0 * c2);
+    const double ph = x3 * c;
+    double pl = fma(x3, c, -ph) + (x3 * cl + x3l * c);
+    pl += ph * ((0x1p-51 / 3.0) * log(x));
+    return ph + pl;
+}
+
+// DryLayerHumidity's per-cell constants (dry_layer_humidity.jl:317-365). The interface
+// temperature is the bulk land temperature, so the front temperature
+// T_e = T_in + chi (T_la - T_in) is T_la whatever chi = clamp(delta / l_T, 0, 1) is, and the
+// front's source humidity and the saturated skin are both q_sat(T_la) = c.qres. What is left
+// per cell is the dry layer's depth delta(S) (StorageBasedDryLayerDepth, :95-100), its
+// conductance G_e = rho D_eff / max(delta, delta_min) (:252-263, 341-345) and the logistic
+// weight of the series solution (:358-364).
+__device__ __forceinline__ void dry_layer_constants(const DevIface<double>& P, double S, CellConst<double>& c) {
+    using Md = M<double>;
+    const double s = Md::fmin(S / P.dl_Sc, 1.0);
+    const double delta = P.dl_max * pow(Md::fmax(1.0 - s, 0.0), P.dl_eta);
+    double Dv = P.dl_D0;                                            // ConstantTortuosity
+    if (P.tort == NESF_TORTUOSITY_POWER_LAW) {                      // Millington-Quirk
+        const double theta_g = Md::fmax(P.dl_nu - Md::mul(S, P.dl_nu), 0.0);
+        Dv = P.dl_D0 * pow_ten_thirds(theta_g) / (P.dl_nu * P.dl_nu);
+    }
+    c.Gq = c.rho_a * Dv / Md::fmax(delta, P.dl_min);
+    const double z = 10.0 * Md::add(delta - P.dl_min, -(P.dl_w * 0.5)) / Md::fmax(P.dl_w, DBL_EPSILON);
+    c.sig = 1.0 / (1.0 + exp(-z));
+}
 
 template <class S>
 __device__ __forceinline__ void al_load(const DevIface<double>& P, const ALArgs<S>& a, int64_t k,
@@ -32,9 +75,14 @@ __device__ __forceinline__ void al_load(const DevIface<double>& P, const ALArgs<
     c.cp_a = c.L_s = 0;
     c.qres = surface_specific_humidity(P, c.pa, c.Ti);   // saturated at the bulk land temperature
     const double sat = a.sat ? ld(a.sat, k) : 1.0;
+    c.Gq = P.skin_g;
+    c.sig = 1.0;
+    if (P.hum_form == NESF_HUMIDITY_DRY_LAYER) dry_layer_constants(P, sat, c);
     // the initial q_s is the saturation humidity (:200-201); BULK and FRACTIONAL recompute
-    // it from the land state every iteration (a constant at a fixed T_s), SKIN iterates it
-    qs = P.hum_form == NESF_HUMIDITY_SKIN || P.hum_form == NESF_HUMIDITY_IMPURE_SATURATION
+    // it from the land state every iteration (a constant at a fixed T_s), SKIN and DRY_LAYER
+    // iterate it
+    qs = P.hum_form == NESF_HUMIDITY_SKIN || P.hum_form == NESF_HUMIDITY_DRY_LAYER ||
+                 P.hum_form == NESF_HUMIDITY_IMPURE_SATURATION
              ? c.qres
              : land_humidity(P, c.pa, c.Ti, sat);
 }
@@ -79,7 +127,7 @@ __global__ void __launch_bounds__(128) al_kernel(ALArgs<S> a, DevIface<double> P
     int iters = 0, f64it = 0;
     bool nonconv = false, replayed = false;
     const bool needs = P.stop_kind == NESF_STOP_CONVERGENCE;
-    if (P.hum_form == NESF_HUMIDITY_SKIN) {
+    if (P.hum_form == NESF_HUMIDITY_SKIN || P.hum_form == NESF_HUMIDITY_DRY_LAYER) {
         iters = solve_plain<false, true>(P, c, s, us, ts, qst, nonconv);
     } else if (PREC == NESF_PLAIN_F64 || !needs) {
         iters = solve_plain<false>(P, c, s, us, ts, qst, nonconv);

@@ -2,6 +2,7 @@
 //
 // Validation, parameter conversion and dispatch to the kernels. Each entry point
 // returns an nesf_status and records a message for nesf_last_error() on failure.
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <cstdarg>
@@ -464,7 +465,7 @@ static int check_params(const nesf_interface_params* p, const char* who) {
         p->temperature_formulation > NESF_SKIN_TEMPERATURE_DIFFUSIVE)
         return fail(NESF_ERR_ARG, "%s: temperature formulation %d", who, p->temperature_formulation);
     if (p->surface_layer_height <= 0) return fail(NESF_ERR_ARG, "%s: surface_layer_height <= 0", who);
-    if (p->humidity_formulation < NESF_HUMIDITY_IMPURE_SATURATION || p->humidity_formulation > NESF_HUMIDITY_SKIN)
+    if (p->humidity_formulation < NESF_HUMIDITY_IMPURE_SATURATION || p->humidity_formulation > NESF_HUMIDITY_DRY_LAYER)
         return fail(NESF_ERR_ARG, "%s: humidity formulation %d", who, p->humidity_formulation);
     if (p->flux_formulation != NESF_FLUXES_SIMILARITY_THEORY && p->flux_formulation != NESF_FLUXES_COEFFICIENT_BASED)
         return fail(NESF_ERR_ARG, "%s: flux formulation %d", who, p->flux_formulation);
@@ -821,11 +822,28 @@ extern "C" int nesf_compute_atmosphere_land_fluxes(nesf_context* ctx, const nesf
     if (params->temperature_formulation != NESF_BULK_TEMPERATURE)
         return fail(NESF_ERR_UNSUPPORTED, "%s: the land interface takes BulkTemperature", who);
     const int hf = params->humidity_formulation;
-    if ((hf == NESF_HUMIDITY_BULK || (hf == NESF_HUMIDITY_FRACTIONAL && params->critical_saturation > 0)) &&
+    if ((hf == NESF_HUMIDITY_BULK || hf == NESF_HUMIDITY_DRY_LAYER ||
+         (hf == NESF_HUMIDITY_FRACTIONAL && params->critical_saturation > 0)) &&
         !f->saturation)
         return fail(NESF_ERR_ARG, "%s: the humidity model needs the land saturation", who);
     if (hf == NESF_HUMIDITY_SKIN && !(params->skin_surface_thickness > 0 && params->skin_vapor_diffusivity >= 0))
         return fail(NESF_ERR_ARG, "%s: SkinHumidity needs surface_thickness > 0 and vapor_diffusivity >= 0", who);
+    // DryLayerHumidity: the reference accepts any numbers; a zero minimum depth, onset saturation
+    // or exchange depth divides by zero (0/0 where the layer is wet) and a zero porosity does
+    // under the power-law tortuosity, so these are rejected rather than turned into NaN fields.
+    if (hf == NESF_HUMIDITY_DRY_LAYER) {
+        const nesf_interface_params& q = *params;
+        if (q.tortuosity != NESF_TORTUOSITY_CONSTANT && q.tortuosity != NESF_TORTUOSITY_POWER_LAW)
+            return fail(NESF_ERR_ARG, "%s: tortuosity %d", who, q.tortuosity);
+        if (!(q.maximum_dry_layer_depth >= 0 && q.dry_layer_onset_saturation > 0 && q.minimum_dry_layer_depth > 0 &&
+              q.molecular_diffusivity >= 0 && q.wet_transition_width >= 0 && q.thermal_exchange_depth > 0 &&
+              std::isfinite(q.dry_layer_exponent) &&
+              (q.tortuosity == NESF_TORTUOSITY_CONSTANT || q.porosity > 0)))
+            return fail(NESF_ERR_ARG,
+                        "%s: DryLayerHumidity needs maximum depth >= 0, onset saturation > 0, minimum depth > 0, "
+                        "diffusivity >= 0, transition width >= 0, exchange depth > 0 and (power law) porosity > 0",
+                        who);
+    }
     nesf_solver_options o = options_or_default(opts);
     if ((r = check_options(o, who))) return r;
     if ((r = context_or_default(&ctx))) return r;

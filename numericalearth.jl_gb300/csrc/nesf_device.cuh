@@ -112,9 +112,12 @@ template <class R> struct DevIface {
     R U_high, Cd_high, U_min;
     R h0, Ch_stable, Ch_unstable, Cq_ly;  // reference height, Stanton/Dalton factors
     // land surface humidity (nesf_humidity_formulation): constant efficiency, critical
-    // saturation (> 0: CriticalSaturation), soil vapor conductance kappa_q / d
-    int32_t hum_form;
+    // saturation (> 0: CriticalSaturation), soil vapor conductance kappa_q / d; DryLayerHumidity:
+    // tortuosity model, maximum depth, onset saturation, exponent, minimum depth, D_0, blend
+    // width, porosity
+    int32_t hum_form, tort;
     R hum_beta, Sc, skin_g;
+    R dl_max, dl_Sc, dl_eta, dl_min, dl_D0, dl_w, dl_nu;
 };
 
 // ------------------------------------------------------------- thermodynamics
@@ -182,19 +185,26 @@ __device__ __forceinline__ R land_humidity(const DevIface<R>& P, R pa, R Ts, R S
     return beta * qsat;
 }
 
-// SkinHumidity's surface humidity from the previous iterate (interface_states.jl:626-651):
-// the soil flux g (q_res - q_s) balances the atmospheric flux J = -rho u* q*, written with
-// dq = q_s_prev - q_a so that it stays finite as dq -> 0.
+// The land surface humidity iterated with the fluxes, from the previous iterate: a vapor
+// flux G (q_src - q_s) from a source at q_src balances the atmospheric flux J = -rho u* q*,
+// written with dq = q_s_prev - q_a so that it stays finite as dq -> 0. SkinHumidity
+// (interface_states.jl:626-651): G = kappa_q / d, q_src the reservoir's saturation.
+// DryLayerHumidity (dry_layer_humidity.jl:339-365): G = rho D_eff / max(delta, delta_min), q_src
+// the front's saturation, and the series solution is blended with the saturated skin q_wet by
+// the logistic weight sig; with the interface at the bulk land temperature q_src = q_wet.
 // The sums cancel where q_s is close to q_a; each product and sum is rounded on its own, as
 // the reference rounds them, so the FP64 path stays on the reference's iterates.
 template <class R>
-__device__ __forceinline__ R skin_humidity(const DevIface<R>& P, R rho, R qa, R qres, R qs_prev, R us, R qst) {
+__device__ __forceinline__ R balance_humidity(const DevIface<R>& P, R rho, R qa, R qsrc, R G, R sig, R qs_prev,
+                                              R us, R qst) {
     using Mr = M<R>;
     R Ja = -Mr::mul(Mr::mul(rho, us), qst);
     R dq = qs_prev - qa;
-    R D = Mr::add(Mr::mul(P.skin_g, dq), Ja);
-    R qs = Mr::add(Mr::mul(Mr::mul(P.skin_g, qres), dq), Mr::mul(Ja, qa)) / D;
-    return D == R(0) ? qs_prev : qs;
+    R D = Mr::add(Mr::mul(G, dq), Ja);
+    R qs = Mr::add(Mr::mul(Mr::mul(G, qsrc), dq), Mr::mul(Ja, qa)) / D;
+    qs = D == R(0) ? qs_prev : qs;
+    if (P.hum_form == NESF_HUMIDITY_DRY_LAYER) qs = Mr::add(qsrc, Mr::mul(sig, qs - qsrc));
+    return qs;
 }
 
 // surface_atmosphere_temperature (interface_states.jl:308-317)
@@ -404,7 +414,8 @@ template <class R> struct CellConst {
     R tha;                       // surface_atmosphere_temperature
     R rho_a, cp_a, L_s;          // air density, cp_m, latent_heat_sublim (skin only)
     R Rth;                       // conductive resistance h_s / k_s + h_i / k_i (ice skin only)
-    R qres;                      // SKIN humidity: q_sat of the soil reservoir (bulk land temperature)
+    R qres;                      // land q_sat at the bulk land temperature (SKIN, DRY_LAYER source)
+    R Gq, sig;                   // SKIN, DRY_LAYER: vapor conductance; DRY_LAYER: blend weight
 };
 
 // The ice and snow layers' thermal resistance (interface_states.jl:468-524), fixed
@@ -576,7 +587,7 @@ __device__ __forceinline__ R skin_temperature(const DevIface<R>& P, const CellCo
 
 // One iterate_interface_state (compute_interface_state.jl:69-122). For the bulk
 // formulation `s` is fixed; for skin formulations it is rebuilt from the new T_s.
-// QSKIN (land SkinHumidity): T_s fixed, q_s iterated from the previous iterate; a template
+// QSKIN (land SkinHumidity, DryLayerHumidity): T_s fixed, q_s iterated from the previous iterate; a template
 // flag so that the other solves carry none of its code or registers.
 template <class R, bool SKIN, bool QSKIN = false>
 __device__ __forceinline__ void iterate_state(const DevIface<R>& P, const CellConst<R>& c, SurfaceConst<R>& s,
@@ -586,7 +597,7 @@ __device__ __forceinline__ void iterate_state(const DevIface<R>& P, const CellCo
         R qs = surface_specific_humidity(P, c.pa, Ts);
         surface_const(P, c, Ts, qs, s);
     } else if (QSKIN) {   // T_s fixed, q_s iterated
-        R qs = skin_humidity(P, c.rho_a, c.qa, c.qres, s.qs, us, qst);
+        R qs = balance_humidity(P, c.rho_a, c.qa, c.qres, c.Gq, c.sig, s.qs, us, qst);
         surface_const(P, c, s.Ts, qs, s);
     }
     R a, b, d;

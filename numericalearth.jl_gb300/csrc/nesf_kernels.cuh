@@ -116,6 +116,10 @@ inline DevIface<R> make_dev_iface(const nesf_interface_params& p) {
     d.Sc = R(p.critical_saturation);
     d.skin_g = p.humidity_formulation == NESF_HUMIDITY_SKIN ? R(p.skin_vapor_diffusivity / p.skin_surface_thickness)
                                                             : R(0);
+    d.tort = p.tortuosity;
+    d.dl_max = R(p.maximum_dry_layer_depth); d.dl_Sc = R(p.dry_layer_onset_saturation);
+    d.dl_eta = R(p.dry_layer_exponent); d.dl_min = R(p.minimum_dry_layer_depth);
+    d.dl_D0 = R(p.molecular_diffusivity); d.dl_w = R(p.wet_transition_width); d.dl_nu = R(p.porosity);
     d.flux_form = p.flux_formulation;
     if (p.flux_formulation == NESF_FLUXES_COEFFICIENT_BASED) {
         const nesf_coefficient_fluxes& c = p.coefficients;

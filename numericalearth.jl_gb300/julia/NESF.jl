@@ -32,7 +32,7 @@ end
 # Opaque blob holding nesf_interface_params, filled by the library defaults
 # and then patched field by field through the offsets exported by the library's
 # layout (the Python binding nesf/_abi.py lists the field order).
-const PARAMS_BYTES = 1464   # sizeof(nesf_interface_params); nesf_struct_sizes() reports it
+const PARAMS_BYTES = 1536   # sizeof(nesf_interface_params); nesf_struct_sizes() reports it
 
 struct AOFields
     grid::Grid; dtype::Int32; pad::Int32

@@ -122,7 +122,11 @@ class InterfaceParams(C.Structure):
                 ("interior_reference_density", d), ("interior_heat_capacity", d),
                 ("flux_formulation", i32), ("pad2_", i32), ("coefficients", CoefficientFluxes),
                 ("humidity_formulation", i32), ("pad3_", i32), ("evaporation_efficiency", d),
-                ("critical_saturation", d), ("skin_surface_thickness", d), ("skin_vapor_diffusivity", d)]
+                ("critical_saturation", d), ("skin_surface_thickness", d), ("skin_vapor_diffusivity", d),
+                ("tortuosity", i32), ("pad4_", i32), ("maximum_dry_layer_depth", d),
+                ("dry_layer_onset_saturation", d), ("dry_layer_exponent", d), ("minimum_dry_layer_depth", d),
+                ("molecular_diffusivity", d), ("wet_transition_width", d), ("thermal_exchange_depth", d),
+                ("porosity", d)]
 
 
 class SolverOptions(C.Structure):
@@ -158,6 +162,9 @@ HUMIDITY_IMPURE_SATURATION = 0
 HUMIDITY_BULK = 1
 HUMIDITY_FRACTIONAL = 2
 HUMIDITY_SKIN = 3
+HUMIDITY_DRY_LAYER = 4
+TORTUOSITY_CONSTANT = 0
+TORTUOSITY_POWER_LAW = 1
 
 
 class ALFields(C.Structure):

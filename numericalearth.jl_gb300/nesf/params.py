@@ -531,6 +531,46 @@ class SkinHumidity:
     phase: str = "liquid"
 
 
+@dataclass
+class StorageBasedDryLayerDepth:
+    """dry_layer_humidity.jl:81-100: delta(S) = delta_max (1 - min(S / S_c, 1))^eta."""
+    maximum_dry_layer_depth: float
+    dry_layer_onset_saturation: float
+    dry_layer_exponent: float = 2.0
+
+
+class ConstantTortuosity:
+    """dry_layer_humidity.jl:111-118, 255-256: D_eff = D_0."""
+
+
+class PowerLawTortuosity:
+    """dry_layer_humidity.jl:120-127, 258-263: D_eff = D_0 theta_g^(10/3) / nu^2 (Millington-Quirk)."""
+
+
+@dataclass
+class DryLayerVaporPistonVelocity:
+    """dry_layer_humidity.jl:155-167 (wet_transition_width None = 5 minimum_dry_layer_depth)."""
+    minimum_dry_layer_depth: float
+    molecular_diffusivity: float
+    wet_transition_width: Optional[float] = None
+    tortuosity: object = field(default_factory=ConstantTortuosity)
+
+    def __post_init__(self):
+        if self.wet_transition_width is None:
+            self.wet_transition_width = 5 * self.minimum_dry_layer_depth
+
+
+@dataclass
+class DryLayerHumidity:
+    """dry_layer_humidity.jl:216-235, 317-366: q_s from the vapor-flux balance across a dry
+    surface layer, blended with the saturated skin."""
+    dry_layer_depth: StorageBasedDryLayerDepth
+    vapor_exchange: DryLayerVaporPistonVelocity
+    thermal_exchange_depth: float
+    porosity: float
+    phase: str = "liquid"
+
+
 def default_ao_specific_humidity():
     """component_interfaces.jl:353-358: Liquid with x_H2O = 0.98."""
     return ImpureSaturationSpecificHumidity("liquid", 0.98)
@@ -648,6 +688,19 @@ class InterfaceSpec:
             p.humidity_formulation = A.HUMIDITY_SKIN
             p.skin_surface_thickness = q.surface_thickness
             p.skin_vapor_diffusivity = q.vapor_diffusivity
+        elif isinstance(q, DryLayerHumidity):
+            p.humidity_formulation = A.HUMIDITY_DRY_LAYER
+            d, v = q.dry_layer_depth, q.vapor_exchange
+            p.maximum_dry_layer_depth = d.maximum_dry_layer_depth
+            p.dry_layer_onset_saturation = d.dry_layer_onset_saturation
+            p.dry_layer_exponent = d.dry_layer_exponent
+            p.minimum_dry_layer_depth = v.minimum_dry_layer_depth
+            p.molecular_diffusivity = v.molecular_diffusivity
+            p.wet_transition_width = v.wet_transition_width
+            p.tortuosity = A.TORTUOSITY_POWER_LAW if isinstance(v.tortuosity, PowerLawTortuosity) \
+                else A.TORTUOSITY_CONSTANT
+            p.thermal_exchange_depth = q.thermal_exchange_depth
+            p.porosity = q.porosity
         else:
             p.humidity_formulation = A.HUMIDITY_IMPURE_SATURATION
         p.velocity_formulation = A.WIND_VELOCITY if isinstance(self.velocity, WindVelocity) else A.RELATIVE_VELOCITY

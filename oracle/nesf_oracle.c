@@ -20,6 +20,7 @@
  */
 #include "nesf_oracle.h"
 
+#include <float.h>
 #include <math.h>
 #include <stddef.h>
 #include <string.h>
@@ -30,6 +31,18 @@
 static int g_threads = 0;
 
 void oracle_set_threads(int32_t n) { g_threads = n; }
+
+/* Conditioning probe for the parity tests: each iterate's interface humidity is moved by n
+ * units in the last place (0 = the reference's arithmetic), either only where the flux
+ * evaluation sees it (carry = 0) or also in the iterate handed on (carry = 1). Where q_s - q_a
+ * cancels, the reference's vapor fluxes respond to a last-place change of q_s (of any of its
+ * ingredients) by ulp(q_a) / |q_s - q_a|, and the fixed point feeds the change back with the
+ * slope of the q_s map; the two forms measure the response without and with that feedback. */
+static int32_t g_humidity_ulp_shift = 0, g_humidity_shift_carry = 0;
+void oracle_set_humidity_ulp_shift(int32_t n, int32_t carry) {
+    g_humidity_ulp_shift = n;
+    g_humidity_shift_carry = carry;
+}
 int32_t oracle_get_threads(void) {
 #ifdef _OPENMP
     return g_threads > 0 ? g_threads : omp_get_max_threads();
@@ -452,9 +465,65 @@ static double interface_temperature(const nesf_interface_params* p, const cell_i
     return Tp;
 }
 
+/* theta^(10/3) (the Millington-Quirk power, dry_layer_humidity.jl:262), correctly rounded: the
+ * exponent is 10/3 rounded to double, p = 10/3 + d with d = 2^-51 / 3, so
+ * x^p = x^3 cbrt(x) x^d, with x^3 an exact double-double (Dekker products through fma), cbrt(x)
+ * refined to double-double by one Newton step on c^3 = x, and x^d = 1 + d ln x to 1e-32. The
+ * fixed point amplifies a last-place change of this power a thousandfold where the vapor
+ * balance cancels, so the power is rounded once from a near-exact value rather than taken from
+ * a libm pow (within about half an ulp, and misrounded in some cases). */
+double oracle_pow_ten_thirds(double x) {
+    if (!(x > 0x1p-300) || !(x < 0x1p300)) return pow(x, 10.0 / 3.0);
+    double x2 = x * x, x2l = fma(x, x, -x2);
+    double x3 = x2 * x, x3l = fma(x2, x, -x3) + x2l * x;
+    double c = cbrt(x);
+    double c2 = c * c, c2l = fma(c, c, -c2);
+    double c3 = c2 * c, c3l = fma(c2, c, -c3) + c2l * c;
+    double cl = -((c3 - x) + c3l) / (3.0 * c2);
+    double ph = x3 * c;
+    double pl = fma(x3, c, -ph) + (x3 * cl + x3l * c);
+    pl += ph * ((0x1p-51 / 3.0) * log(x));
+    return ph + pl;
+}
+
+/* DryLayerHumidity's compute_interface_humidity (dry_layer_humidity.jl:317-366) with
+ * StorageBasedDryLayerDepth (:95-100) and the tortuosity models (:252-263). The dry layer's
+ * depth follows the land saturation S; vapor leaves the front (saturated at
+ * Te = Tin + chi (Tla - Tin)) by a Fick flux of conductance Ge and the atmosphere carries it
+ * away at the previous iterate's flux Ja = -rho u* q*, linearised about q_prev; the series
+ * solution is blended with the saturated skin q_sat(Tin) by a logistic weight in the depth.
+ * Tin is the current interface-temperature iterate, Tla the bulk land temperature. */
+double oracle_dry_layer_humidity(const nesf_interface_params* p, double Tin, double Tla, double S, double Ta,
+                                 double pa, double qa, double us, double qst, double qprev) {
+    double rho = oracle_air_density(&p->thermo, Ta, pa, qa);
+    double s = jmin(S / p->dry_layer_onset_saturation, 1.0);
+    double delta = p->maximum_dry_layer_depth * pow(jmax(1.0 - s, 0.0), p->dry_layer_exponent);
+    double dmin = p->minimum_dry_layer_depth;
+    double chi = clampd(delta / p->thermal_exchange_depth, 0.0, 1.0);
+    double Te = Tin + chi * (Tla - Tin);
+    double qe = oracle_surface_specific_humidity(p, pa, Te);
+    double theta_l = S * p->porosity;                 /* pore liquid fraction ~ S nu */
+    double Dv = p->molecular_diffusivity;             /* ConstantTortuosity */
+    if (p->tortuosity == NESF_TORTUOSITY_POWER_LAW) { /* Millington-Quirk */
+        double theta_g = jmax(p->porosity - theta_l, 0.0);
+        Dv = p->molecular_diffusivity * oracle_pow_ten_thirds(theta_g) / (p->porosity * p->porosity);
+    }
+    double Ge = rho * Dv / jmax(delta, dmin);
+    double Ja = -rho * us * qst;
+    double dq = qprev - qa;
+    double D = Ge * dq + Ja;
+    double qseries = D == 0 ? qprev : (Ge * qe * dq + Ja * qa) / D;
+    double qwet = oracle_surface_specific_humidity(p, pa, Tin);
+    double w = p->wet_transition_width;
+    double z = 10 * (delta - dmin - w / 2) / jmax(w, DBL_EPSILON);
+    double sigma = 1 / (1 + exp(-z));
+    return qwet + sigma * (qseries - qwet);
+}
+
 /* compute_interface_humidity (interface_states.jl:587-651): ImpureSaturationSpecificHumidity;
  * BulkHumidity (:120-125); FractionalHumidity with a constant beta or CriticalSaturation
- * (:152-158, 592-598); SkinHumidity's vapor-flux balance with the previous iterate (:626-651).
+ * (:152-158, 592-598); SkinHumidity's vapor-flux balance with the previous iterate (:626-651);
+ * DryLayerHumidity (oracle_dry_layer_humidity).
  * saturation_specific_humidity (:76-90) is surface_specific_humidity with x = 1. */
 static double interface_humidity(const nesf_interface_params* p, const cell_in* c, double Ts, const istate* prev) {
     switch (p->humidity_formulation) {
@@ -479,6 +548,8 @@ static double interface_humidity(const nesf_interface_params* p, const cell_in* 
         double qs = (g * qsat * dq + Ja * c->qa) / D;
         return D == 0 ? prev->q : qs;
     }
+    case NESF_HUMIDITY_DRY_LAYER:
+        return oracle_dry_layer_humidity(p, Ts, c->Ti, c->sat, c->Ta, c->pa, c->qa, prev->us, prev->qs_, prev->q);
     default:
         return oracle_surface_specific_humidity(p, c->pa, Ts);
     }
@@ -487,7 +558,10 @@ static double interface_humidity(const nesf_interface_params* p, const cell_in* 
 /* iterate_interface_state (compute_interface_state.jl:69-122) */
 static istate iterate_state(const nesf_interface_params* p, const cell_in* c, const istate* prev) {
     double Ts = interface_temperature(p, c, prev);
-    double qs = interface_humidity(p, c, Ts, prev);
+    double q_iter = interface_humidity(p, c, Ts, prev);
+    double qs = q_iter;
+    for (int32_t k = 0; k < g_humidity_ulp_shift; k++) qs = nextafter(qs, INFINITY);
+    if (g_humidity_shift_carry) q_iter = qs;
     double dq = c->qa - qs;
     double tha = surface_atmosphere_temperature(p, c->Ta, c->qa);
     double dth = tha - Ts;
@@ -498,7 +572,7 @@ static istate iterate_state(const nesf_interface_params* p, const cell_in* c, co
     else
         iterate_fluxes(p, c, Ts, qs, dth, dq, dh, prev, &n.us, &n.ts, &n.qs_);
     n.T = Ts;
-    n.q = qs;
+    n.q = q_iter;
     return n;
 }
 

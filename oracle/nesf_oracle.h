@@ -30,6 +30,9 @@ double oracle_latent_heat_vapor(const nesf_thermodynamics_parameters* th, double
 double oracle_latent_heat_sublim(const nesf_thermodynamics_parameters* th, double T);
 double oracle_virtual_temperature(const nesf_thermodynamics_parameters* th, double T, double q);
 double oracle_surface_specific_humidity(const nesf_interface_params* p, double pa, double Ts);
+double oracle_pow_ten_thirds(double x);
+double oracle_dry_layer_humidity(const nesf_interface_params* p, double Tin, double Tla, double S, double Ta,
+                                 double pa, double qa, double us, double qst, double qprev);
 
 /* similarity-theory building blocks */
 double oracle_stability(const nesf_stability_function* psi, double zeta);
@@ -57,6 +60,7 @@ int oracle_apply_air_sea_radiative_fluxes(const nesf_assembly_params* p, const n
 int oracle_apply_air_sea_ice_radiative_fluxes(const nesf_assembly_params* p, const nesf_assembly_fields* f);
 
 void oracle_set_threads(int32_t n);
+void oracle_set_humidity_ulp_shift(int32_t n, int32_t carry);   /* conditioning probe for tests; 0 = off */
 int32_t oracle_get_threads(void);
 
 #ifdef __cplusplus

@@ -5,6 +5,7 @@ CPU-baseline leg of bench.py as the checker. The product path never calls it.
 Inputs are numpy arrays; FP32 workloads are widened to FP64 before the call
 (every FP32 value is exact in FP64), so the oracle always computes in FP64.
 """
+import contextlib
 import ctypes as C
 import os
 import sys
@@ -39,6 +40,8 @@ def load():
             "oracle_latent_heat_sublim": (d, [P(A.ThermodynamicsParameters), d]),
             "oracle_virtual_temperature": (d, [P(A.ThermodynamicsParameters), d, d]),
             "oracle_surface_specific_humidity": (d, [P(A.InterfaceParams), d, d]),
+            "oracle_dry_layer_humidity": (d, [P(A.InterfaceParams)] + [d] * 9),
+            "oracle_pow_ten_thirds": (d, [d]),
             "oracle_stability": (d, [P(A.StabilityFunction), d]),
             "oracle_neutral_drag": (d, [P(A.CoefficientFluxes), d]),
             "oracle_al_fluxes": (C.c_int, [P(A.InterfaceParams), P(A.ALFields)]),
@@ -57,6 +60,7 @@ def load():
             "oracle_apply_air_sea_radiative_fluxes": (C.c_int, [P(A.AssemblyParams), P(A.AssemblyFields)]),
             "oracle_apply_air_sea_ice_radiative_fluxes": (C.c_int, [P(A.AssemblyParams), P(A.AssemblyFields)]),
             "oracle_set_threads": (None, [C.c_int32]),
+            "oracle_set_humidity_ulp_shift": (None, [C.c_int32, C.c_int32]),
             "oracle_get_threads": (C.c_int32, []),
         }
         for name, (res, args) in sig.items():
@@ -109,6 +113,19 @@ def al_fluxes(params, layout, inputs, with_iterations=True):
     if with_iterations:
         out["iterations"] = its
     return out
+
+
+@contextlib.contextmanager
+def humidity_ulp_shift(n, carry):
+    """Within the block every iterate's interface humidity is moved n units in the last place
+    where its flux evaluation sees it, and with carry also in the iterate handed on
+    (oracle_set_humidity_ulp_shift): the conditioning probe of the parity tests."""
+    lib = load()
+    lib.oracle_set_humidity_ulp_shift(n, 1 if carry else 0)
+    try:
+        yield
+    finally:
+        lib.oracle_set_humidity_ulp_shift(0, 0)
 
 
 def ai_fluxes(params, layout, inputs, interface_temperature, with_iterations=True):

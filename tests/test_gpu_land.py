@@ -1,9 +1,19 @@
 """The atmosphere-land solve (compute_atmosphere_land_fluxes!, atmosphere_land_fluxes.jl:48-251)
 on the GPU against the CPU oracle through the C ABI, for each land humidity model
 (BulkHumidity, FractionalHumidity with CriticalSaturation and with a constant efficiency,
-SkinHumidity). Bar as for the ocean: plain FP64 to 1e-12 relative on 99.99 % of the cells and
-1e-11 everywhere with identical iteration counts; the FP32 solvers within 1e-5 (SkinHumidity
-runs the FP64 iteration in every mode). Errors are relative to max(|ref|, 1e-6 max|ref|)."""
+SkinHumidity, DryLayerHumidity with either tortuosity and with the sharp wet switch). Bar as
+for the ocean: plain FP64 to 1e-12 relative on 99.99 % of the cells and 1e-11 everywhere with
+identical iteration counts; the FP32 solvers within 1e-5 (SkinHumidity and DryLayerHumidity
+run the FP64 iteration in every mode). Errors are relative to max(|ref|, 1e-6 max|ref|).
+
+SkinHumidity and DryLayerHumidity iterate q_s from a vapor balance, and where the vapor flux
+nearly vanishes q_s - q_a cancels: there a one-ulp difference of q_s (from any libm-computed
+ingredient: e_sat, the air density, the stability functions) moves the reference's own vapor
+fluxes by ulp(q_a) / |q_s - q_a|, up to 1e-10 relative in this sample, and the fixed point
+feeds it back with the slope of the q_s map. For those fields the bar is per cell: 4 times the
+oracle's response per ulp of q_s (the larger of its responses to a 1024-ulp shift, with and
+without the feedback, oracle.humidity_ulp_shift, over 1024: a single ulp rounds away in some
+cells), and 1e-12 where that response is smaller. The GPU lands within 2 such units."""
 import numpy as np
 import pytest
 
@@ -15,8 +25,22 @@ from nesf import synthetic as syn
 
 pytestmark = pytest.mark.gpu
 
+
+def dry_layer(tortuosity=P.ConstantTortuosity, width=None):
+    """DryLayerHumidity with the parameters of the reference's dry-layer tests."""
+    return P.DryLayerHumidity(P.StorageBasedDryLayerDepth(0.05, 0.5, 2.0),
+                              P.DryLayerVaporPistonVelocity(1e-4, 2.5e-5, wet_transition_width=width,
+                                                            tortuosity=tortuosity()),
+                              thermal_exchange_depth=0.10, porosity=0.4)
+
+
 MODELS = {"bulk": P.BulkHumidity, "fractional": P.FractionalHumidity,
-          "fractional_const": lambda: P.FractionalHumidity(0.5), "skin": P.SkinHumidity}
+          "fractional_const": lambda: P.FractionalHumidity(0.5), "skin": P.SkinHumidity,
+          "dry_layer": dry_layer, "dry_layer_power_law": lambda: dry_layer(P.PowerLawTortuosity),
+          "dry_layer_sharp": lambda: dry_layer(width=0.0)}
+ITERATED_HUMIDITY = ("skin", "dry_layer", "dry_layer_power_law", "dry_layer_sharp")
+VAPOR = ("latent_heat", "water_vapor", "water_vapor_scale")
+SHIFT_ULPS = 1024
 OUT = ("x_momentum", "y_momentum", "sensible_heat", "latent_heat", "water_vapor", "friction_velocity",
        "temperature_scale", "water_vapor_scale", "interface_temperature")
 
@@ -47,9 +71,19 @@ def test_plain_f64_matches_oracle(oracle, state, model):
     gpu, stats = run(spec, state, "f64")
     I = state.layout.interior
     assert np.array_equal(I(gpu["iterations"]), I(ref["iterations"])), model
+    shifted = []
+    if model in ITERATED_HUMIDITY:
+        for carry in (False, True):
+            with oracle.humidity_ulp_shift(SHIFT_ULPS, carry):
+                shifted.append(oracle.al_fluxes(spec.to_c(), state.layout, state.fields))
     for k in OUT:
         e = rel_err(I(gpu[k]), I(ref[k]), floor_frac=1e-6)
-        assert np.percentile(e, 99.99) <= 1e-12 and e.max() <= 1e-11, (model, k, float(e.max()))
+        if shifted and k in VAPOR:
+            s = np.maximum(*(rel_err(I(sh[k]), I(ref[k]), floor_frac=1e-6) for sh in shifted)) / SHIFT_ULPS
+            bar = np.maximum(1e-12, 4 * s)
+            assert np.all(e <= bar), (model, k, float((e / bar).max()), float(e.max()))
+        else:
+            assert np.percentile(e, 99.99) <= 1e-12 and e.max() <= 1e-11, (model, k, float(e.max()))
     assert stats["cells"] == state.layout.nx * state.layout.ny
 
 
@@ -64,7 +98,7 @@ def test_fp32_solvers_within_1e5(oracle, state, model, precision):
     for k in OUT:
         e = rel_err(I(gpu[k]), I(ref[k]), floor_frac=1e-6)[conv]
         assert e.max() <= 1e-5, (model, precision, k, float(e.max()))
-    if model != "skin":
+    if model not in ITERATED_HUMIDITY:
         assert stats["polished"] > 0.5 * stats["cells"]   # the FP32 sweep + FP64 polish ran
 
 
@@ -93,3 +127,24 @@ def test_land_rejects_ocean_only_options(state):
     out = {k: torch.zeros(state.layout.shape, dtype=torch.float64, device="cuda") for k in F.AL_OUTPUTS}
     with pytest.raises(_lib.NesfError):
         api.compute_atmosphere_land_fluxes(spec, state.layout, dev, out)
+
+
+def test_dry_layer_rejects_degenerate_parameters(state):
+    """Parameters under which the reference divides by zero are refused (NESF_ERR_ARG), and the
+    dry-layer model needs the land saturation."""
+    from nesf import _lib
+    import torch
+    for attr in ("minimum_dry_layer_depth", "thermal_exchange_depth"):
+        q = dry_layer()
+        setattr(q.vapor_exchange if attr == "minimum_dry_layer_depth" else q, attr, 0.0)
+        with pytest.raises(_lib.NesfError):
+            run(P.atmosphere_land_interface_spec(specific_humidity=q), state, "f64")
+    q = dry_layer(P.PowerLawTortuosity)
+    q.porosity = 0.0
+    with pytest.raises(_lib.NesfError):
+        run(P.atmosphere_land_interface_spec(specific_humidity=q), state, "f64")
+    dev = api.to_device({k: state.fields[k] for k in F.AL_INPUTS if k != "saturation"})
+    out = {k: torch.zeros(state.layout.shape, dtype=torch.float64, device="cuda") for k in F.AL_OUTPUTS}
+    with pytest.raises(_lib.NesfError):
+        api.compute_atmosphere_land_fluxes(P.atmosphere_land_interface_spec(specific_humidity=dry_layer()),
+                                           state.layout, dev, out)

@@ -346,11 +346,15 @@ def test_skin_humidity_limits(oracle):
     assert 0 < mid["water_vapor"] < wet["water_vapor"]
 
 
-@pytest.mark.parametrize("q", ["bulk", "fractional", "fractional_const", "skin"])
+@pytest.mark.parametrize("q", ["bulk", "fractional", "fractional_const", "skin", "dry_layer"])
 def test_land_solve_on_1deg_sample(oracle, q):
     """Every model gives finite fluxes and u* > 0 over a 1-degree land sample with dry cells."""
     model = {"bulk": P.BulkHumidity(), "fractional": P.FractionalHumidity(),
-             "fractional_const": P.FractionalHumidity(0.5), "skin": P.SkinHumidity()}[q]
+             "fractional_const": P.FractionalHumidity(0.5), "skin": P.SkinHumidity(),
+             "dry_layer": P.DryLayerHumidity(P.StorageBasedDryLayerDepth(0.05, 0.5),
+                                             P.DryLayerVaporPistonVelocity(1e-4, 2.5e-5,
+                                                                           tortuosity=P.PowerLawTortuosity()),
+                                             thermal_exchange_depth=0.1, porosity=0.4)}[q]
     st = syn.al_1deg(nx=60, ny=30)
     out = oracle.al_fluxes(P.atmosphere_land_interface_spec(specific_humidity=model).to_c(), st.layout, st.fields)
     I = st.layout.interior
@@ -358,3 +362,109 @@ def test_land_solve_on_1deg_sample(oracle, q):
         assert np.all(np.isfinite(I(out[k]))), k
     assert np.all(I(out["friction_velocity"]) > 0)
     assert np.array_equal(I(out["interface_temperature"]), I(st.fields["land_temperature"]))
+
+
+# ------------------------------------------------ DryLayerHumidity (dry_layer_humidity.jl)
+# The cases of the reference's test/test_dry_layer_humidity.jl: the humidity function called on
+# one state (T_in = 300 K or 310 K against a 290 K bulk land, p = 1e5 Pa, q_a = 0.01,
+# T_a = 295 K, u* = 0.3, q* = -2e-4, previous q_s = 0.005), with delta_max = 0.05,
+# S_c = 0.5, delta_min = 1e-4, D_0 = 2.5e-5, l_T = 0.1, nu = 0.4.
+def _dry_layer_params(exponent=2.0, D0=2.5e-5, width=None, tortuosity=None):
+    v = P.DryLayerVaporPistonVelocity(minimum_dry_layer_depth=1e-4, molecular_diffusivity=D0,
+                                      wet_transition_width=width, tortuosity=tortuosity or P.ConstantTortuosity())
+    q = P.DryLayerHumidity(P.StorageBasedDryLayerDepth(0.05, 0.5, exponent), v, thermal_exchange_depth=0.10,
+                           porosity=0.4)
+    return P.atmosphere_land_interface_spec(specific_humidity=q).to_c()
+
+
+def _q_dry(oracle, params, S, Tin=300.0, Tla=290.0, pa=1.0e5, qa=1.0e-2, Ta=295.0, us=0.3, qst=-2.0e-4, qprev=0.005):
+    return oracle.load().oracle_dry_layer_humidity(C.byref(params), Tin, Tla, S, Ta, pa, qa, us, qst, qprev)
+
+
+def _qsat(oracle, params, T, pa=1.0e5):
+    return oracle.load().oracle_surface_specific_humidity(C.byref(params), pa, T)
+
+
+def test_dry_layer_wet_branch(oracle):
+    """S = S_c: delta = 0, and with the sharp switch q_s is q_sat(T_in)."""
+    p = _dry_layer_params(exponent=2.0, width=0.0)
+    assert _q_dry(oracle, p, 0.5) == pytest.approx(_qsat(oracle, p, 300.0), abs=1e-15)
+
+
+def test_dry_layer_vapor_divider(oracle):
+    """S = 0: delta = delta_max, chi = 1/2, and q_s is the conductance-weighted mean of the
+    front's q_sat((T_in + T_la) / 2) and q_a."""
+    p = _dry_layer_params(exponent=1.0)
+    lib = oracle.load()
+    qe = _qsat(oracle, p, (300.0 + 290.0) / 2)
+    rho = lib.oracle_air_density(C.byref(p.thermo), 295.0, 1.0e5, 1.0e-2)
+    Ge = rho * 2.5e-5 / 0.05
+    dq = 0.005 - 1.0e-2
+    Ja = -rho * 0.3 * -2.0e-4
+    Ga = Ja / dq
+    expected = (Ge * qe + Ga * 1.0e-2) / (Ge + Ga)
+    assert _q_dry(oracle, p, 0.0) == pytest.approx(expected, abs=1e-15)
+
+
+def test_dry_layer_front_temperature(oracle):
+    """A dry layer draws its vapor from a colder front (T_la < T_in): drier than the wet skin."""
+    p = _dry_layer_params(exponent=1.0, width=0.0)
+    wet = _q_dry(oracle, p, 0.5, Tin=310.0)
+    assert wet == pytest.approx(_qsat(oracle, p, 310.0), rel=1e-15)
+    assert _q_dry(oracle, p, 0.0, Tin=310.0) < wet
+
+
+def test_dry_layer_sealed_layer_takes_air_humidity(oracle):
+    """G_e -> 0 (D_0 = 1e-14): q_s -> q_a."""
+    p = _dry_layer_params(exponent=1.0, D0=1e-14)
+    assert _q_dry(oracle, p, 0.0) == pytest.approx(1.0e-2, abs=1e-6)
+
+
+def test_dry_layer_wet_transition_blend(oracle):
+    """The logistic blend: default width 5 delta_min; the sharp switch is exactly wet at S_c;
+    the blend stays within 1e-3 of wet there, equals the sharp series solution deep in the dry
+    side, and gives the midpoint of wet and series at its centre."""
+    assert P.DryLayerVaporPistonVelocity(minimum_dry_layer_depth=1e-4,
+                                         molecular_diffusivity=2.5e-5).wet_transition_width == pytest.approx(5e-4)
+    sharp = _dry_layer_params(exponent=1.0, width=0.0)
+    blend = _dry_layer_params(exponent=1.0, width=1e-2)
+    qsat = _qsat(oracle, sharp, 300.0)
+    assert _q_dry(oracle, sharp, 0.5) == pytest.approx(qsat, abs=1e-15)
+    assert _q_dry(oracle, blend, 0.5) == pytest.approx(qsat, rel=1e-3)
+    assert _q_dry(oracle, blend, 0.0) == pytest.approx(_q_dry(oracle, sharp, 0.0), rel=1e-14)
+    delta = 1e-4 + 1e-2 / 2
+    S_mid = 0.5 * (1 - delta / 0.05)
+    assert _q_dry(oracle, blend, S_mid) == pytest.approx((qsat + _q_dry(oracle, sharp, S_mid)) / 2, rel=1e-12)
+
+
+def test_dry_layer_power_law_tortuosity(oracle):
+    """Millington-Quirk (dry_layer_humidity.jl:258-263): at S = 0.2 (eta = 1) the layer is
+    delta = 0.03 deep, the front at T_in + 0.3 (T_la - T_in), and D_eff = D_0 theta_g^(10/3) / nu^2
+    with theta_g = nu - S nu; q_s is the divider of the two conductances."""
+    p = _dry_layer_params(exponent=1.0, tortuosity=P.PowerLawTortuosity())
+    lib = oracle.load()
+    S, nu = 0.2, 0.4
+    delta = 0.05 * (1 - S / 0.5)
+    qe = _qsat(oracle, p, 300.0 + min(delta / 0.10, 1.0) * (290.0 - 300.0))
+    rho = lib.oracle_air_density(C.byref(p.thermo), 295.0, 1.0e5, 1.0e-2)
+    Ge = rho * (2.5e-5 * (nu - S * nu) ** (10 / 3) / nu ** 2) / delta
+    Ja = -rho * 0.3 * -2.0e-4
+    Ga = Ja / (0.005 - 1.0e-2)
+    expected = (Ge * qe + Ga * 1.0e-2) / (Ge + Ga)
+    assert _q_dry(oracle, p, S) == pytest.approx(expected, abs=1e-15)
+    const = _dry_layer_params(exponent=1.0)
+    assert _q_dry(oracle, const, S) != _q_dry(oracle, p, S)
+
+
+def test_pow_ten_thirds_is_correctly_rounded(oracle):
+    """The Millington-Quirk power theta^(10/3) that the oracle (and the kernel, by the same
+    construction) takes: the correctly rounded power, checked against 300-bit mpmath."""
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.prec = 300
+    f = oracle.load().oracle_pow_ten_thirds
+    rng = np.random.default_rng(7)
+    xs = np.concatenate([rng.uniform(0, 0.4, 3000), 10 ** rng.uniform(-20, 2, 1000), [1.0, 0.4, 0.125, 1e-300]])
+    p = mpmath.mpf(10.0 / 3.0)
+    for x in xs:
+        assert f(float(x)) == float(mpmath.power(mpmath.mpf(float(x)), p)), float(x)
+    assert f(0.0) == 0.0
