@@ -480,6 +480,38 @@ typedef struct {
     void* ice_upwelling_longwave; void* ice_downwelling_longwave; void* ice_downwelling_shortwave;
 } nesf_assembly_fields;
 
+/* ------------------------------------------ land net-flux assembly and radiation
+ * update_net_fluxes!(model, land::SlabLand) (Lands/slab_land.jl:285-329) and
+ * apply_air_land_radiative_fluxes! (Radiations/apply_air_land_radiative_fluxes.jl:22-95)
+ * over the land exchange grid's interior. */
+typedef struct {
+    double stefan_boltzmann_constant;     /* 5.670374419e-8                               */
+    double land_albedo, land_emissivity;  /* the radiation's land SurfaceRadiationProperties
+                                             (the reference has no default: land_surface =
+                                             nothing means no land radiation)             */
+} nesf_land_radiation_params;
+
+typedef struct {
+    nesf_grid grid;                       /* the land grid                                */
+    int32_t dtype;
+    int32_t pad_;
+    const uint8_t* inactive;              /* radiation only; NULL = every cell active     */
+    const void* rain;                     /* the atmosphere exchanger's rainfall; NULL = 0 */
+    /* atmosphere-land fluxes (nesf_compute_atmosphere_land_fluxes outputs) */
+    const void* al_sensible; const void* al_latent; const void* al_water_vapor;
+    const void* al_interface_temperature; /* T_s (kelvin)                                  */
+    const void* sw_down; const void* lw_down;   /* radiation                              */
+    /* outputs, the SlabLand flux accumulators (NULL skips one) */
+    void* surface_energy_flux;            /* Q_T + Q_v, positive upward; the radiation adds
+                                             sigma eps T_s^4 - eps LW - (1 - alpha) SW    */
+    void* precipitation;                  /* rain + max(0, -J_v)                          */
+    void* evaporation;                    /* max(0, J_v)                                  */
+    void* vapor_flux;                     /* J_v                                          */
+    void* liquid_precipitation_flux;      /* rain                                         */
+    /* radiation diagnostics (InterfaceRadiationFlux of the land; NULL skips one) */
+    void* upwelling_longwave; void* downwelling_longwave; void* downwelling_shortwave;
+} nesf_land_flux_fields;
+
 /* ------------------------------------------------ area integrals (FP64)
  * The global flux integrals behind the reference's conservation checks,
  * int dA(a) = sum(a) * A_z and int dA(a, b) = sum(a .* b) * A_z
@@ -598,6 +630,13 @@ int nesf_apply_air_sea_radiative_fluxes(const nesf_assembly_params* params, cons
 /* apply_air_sea_ice_radiative_fluxes! (apply_air_sea_ice_radiative_fluxes.jl:15-90) */
 int nesf_apply_air_sea_ice_radiative_fluxes(const nesf_assembly_params* params, const nesf_assembly_fields* fields,
                                             void* stream);
+/* update_net_fluxes!(model, land::SlabLand) (Lands/slab_land.jl:285-329): the SlabLand flux
+   accumulators from the atmosphere-land fluxes and the rainfall */
+int nesf_assemble_net_land_fluxes(const nesf_land_flux_fields* fields, void* stream);
+/* apply_air_land_radiative_fluxes! (Radiations/apply_air_land_radiative_fluxes.jl:22-95): the
+   radiative part added in place to surface_energy_flux, and the diagnostics */
+int nesf_apply_air_land_radiative_fluxes(const nesf_land_radiation_params* params, const nesf_land_flux_fields* fields,
+                                         void* stream);
 
 /* int dA of up to 16 fields; result: device memory, 2 n doubles (sum, residual) per
  * integral, written on `stream`. */

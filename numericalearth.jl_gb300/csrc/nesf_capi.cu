@@ -142,7 +142,8 @@ int32_t nesf_struct_sizes(int64_t* sizes, int32_t n) {
         (int64_t)sizeof(nesf_assembly_params), (int64_t)sizeof(nesf_assembly_fields),
         (int64_t)sizeof(nesf_coupling_step_args), (int64_t)sizeof(nesf_integral_fields),
         (int64_t)sizeof(nesf_tuning), (int64_t)sizeof(nesf_trace_entry), (int64_t)sizeof(nesf_coefficient_fluxes),
-        (int64_t)sizeof(nesf_al_fields)};
+        (int64_t)sizeof(nesf_al_fields), (int64_t)sizeof(nesf_land_radiation_params),
+        (int64_t)sizeof(nesf_land_flux_fields)};
     int32_t m = (int32_t)(sizeof s / sizeof s[0]);
     for (int32_t k = 0; k < n && k < m; k++) sizes[k] = s[k];
     return m;
@@ -1087,6 +1088,51 @@ extern "C" int nesf_apply_air_sea_radiative_fluxes(const nesf_assembly_params* p
 extern "C" int nesf_apply_air_sea_ice_radiative_fluxes(const nesf_assembly_params* p, const nesf_assembly_fields* f,
                                                        void* stream) {
     return run_assembly(p, f, 3, stream, "nesf_apply_air_sea_ice_radiative_fluxes");
+}
+
+template <class S>
+static LandArgs<S> land_args(const nesf_land_flux_fields* f) {
+    LandArgs<S> a;
+    a.L = layout(f->grid);
+    a.inactive = f->inactive;
+    a.rain = (const S*)f->rain;
+    a.QT = (const S*)f->al_sensible; a.Qv = (const S*)f->al_latent; a.Jv = (const S*)f->al_water_vapor;
+    a.Ts = (const S*)f->al_interface_temperature;
+    a.sw = (const S*)f->sw_down; a.lw = (const S*)f->lw_down;
+    a.Es = (S*)f->surface_energy_flux; a.P = (S*)f->precipitation; a.E = (S*)f->evaporation;
+    a.Jvo = (S*)f->vapor_flux; a.Pl = (S*)f->liquid_precipitation_flux;
+    a.up_lw = (S*)f->upwelling_longwave; a.dn_lw = (S*)f->downwelling_longwave;
+    a.dn_sw = (S*)f->downwelling_shortwave;
+    return a;
+}
+
+static int run_land(const nesf_land_radiation_params* p, const nesf_land_flux_fields* f, bool radiation, void* stream,
+                    const char* who) {
+    if (!f || (radiation && !p)) return fail(NESF_ERR_ARG, "%s: null argument", who);
+    int r = check_grid(f->grid, 0, who);
+    if (r) return r;
+    if (f->dtype != NESF_F64 && f->dtype != NESF_F32) return fail(NESF_ERR_ARG, "%s: dtype %d", who, f->dtype);
+    if (radiation) {
+        if (!f->al_interface_temperature || !f->sw_down || !f->lw_down || !f->surface_energy_flux)
+            return fail(NESF_ERR_ARG, "%s: T_s, radiation and surface_energy_flux are required", who);
+    } else if (!f->al_sensible || !f->al_latent || !f->al_water_vapor) {
+        return fail(NESF_ERR_ARG, "%s: the atmosphere-land fluxes are required", who);
+    }
+    nesf_land_radiation_params q = {};
+    if (p) q = *p;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = f->dtype == NESF_F64 ? launch_land(land_args<double>(f), q, radiation, s)
+                                         : launch_land(land_args<float>(f), q, radiation, s);
+    if (e != cudaSuccess) return cuda_fail(e, who);
+    return NESF_OK;
+}
+
+extern "C" int nesf_assemble_net_land_fluxes(const nesf_land_flux_fields* f, void* stream) {
+    return run_land(nullptr, f, false, stream, "nesf_assemble_net_land_fluxes");
+}
+extern "C" int nesf_apply_air_land_radiative_fluxes(const nesf_land_radiation_params* p, const nesf_land_flux_fields* f,
+                                                    void* stream) {
+    return run_land(p, f, true, stream, "nesf_apply_air_land_radiative_fluxes");
 }
 
 // ------------------------------------------------ allocation-free variant

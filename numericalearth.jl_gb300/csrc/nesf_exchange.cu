@@ -294,6 +294,47 @@ __global__ void __launch_bounds__(256) radiation_kernel(AsmArgs<S> a, nesf_assem
     }
 }
 
+// _assemble_slab_land_fluxes! (Lands/slab_land.jl:316-329): every interior cell of the land
+// grid, masked or not, as the reference writes them.
+template <class S>
+__global__ void __launch_bounds__(256) land_assemble_kernel(LandArgs<S> a) {
+    using R = S;
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= (int64_t)a.L.nx * a.L.ny) return;
+    int i = 1 + (int)(r % a.L.nx), j = 1 + (int)(r / a.L.nx);
+    int64_t k = a.L.at(i, j);
+    R QT = ldr<R>(a.QT, k), Qv = ldr<R>(a.Qv, k), Jv = ldr<R>(a.Jv, k);
+    R rain = ldzr<R>(a.rain, k);
+    st(a.Es, k, QT + Qv);
+    st(a.P, k, rain + M<R>::fmax(R(0), -Jv));
+    st(a.E, k, M<R>::fmax(R(0), Jv));
+    st(a.Jvo, k, Jv);
+    st(a.Pl, k, rain);
+}
+
+// _apply_air_land_radiative_fluxes! (Radiations/apply_air_land_radiative_fluxes.jl:60-95):
+// sum_rad = -sigma eps T^4 - (-eps LW - (1 - alpha) SW), positive into the land, enters the
+// upward surface_energy_flux with its sign flipped.
+template <class S>
+__global__ void __launch_bounds__(256) land_radiation_kernel(LandArgs<S> a, nesf_land_radiation_params p) {
+    using R = S;
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= (int64_t)a.L.nx * a.L.ny) return;
+    int i = 1 + (int)(r % a.L.nx), j = 1 + (int)(r / a.L.nx);
+    int64_t k = a.L.at(i, j);
+    R Ts = ldr<R>(a.Ts, k);
+    R T2 = Ts * Ts;
+    R Iup = R(p.stefan_boltzmann_constant) * R(p.land_emissivity) * (T2 * T2);
+    R Ia = -R(p.land_emissivity) * ldr<R>(a.lw, k);
+    R It = -(1 - R(p.land_albedo)) * ldr<R>(a.sw, k);
+    R SQ = -Iup - (Ia + It);
+    bool inactive = a.inactive ? a.inactive[k] != 0 : false;
+    a.Es[k] = a.Es[k] + (inactive ? R(0) : -SQ);
+    st(a.up_lw, k, Iup);
+    st(a.dn_lw, k, -Ia);
+    st(a.dn_sw, k, -It);
+}
+
 // ------------------------------------------------------------------ launchers
 static inline unsigned blocks_for(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
 
@@ -341,5 +382,15 @@ cudaError_t launch_assemble(const AsmArgs<S>& a, const nesf_assembly_params& p, 
 }
 template cudaError_t launch_assemble<double>(const AsmArgs<double>&, const nesf_assembly_params&, int, cudaStream_t);
 template cudaError_t launch_assemble<float>(const AsmArgs<float>&, const nesf_assembly_params&, int, cudaStream_t);
+
+template <class S>
+cudaError_t launch_land(const LandArgs<S>& a, const nesf_land_radiation_params& p, bool radiation, cudaStream_t s) {
+    int64_t n = (int64_t)a.L.nx * a.L.ny;
+    if (radiation) land_radiation_kernel<S><<<blocks_for(n, 256), 256, 0, s>>>(a, p);
+    else land_assemble_kernel<S><<<blocks_for(n, 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+template cudaError_t launch_land<double>(const LandArgs<double>&, const nesf_land_radiation_params&, bool, cudaStream_t);
+template cudaError_t launch_land<float>(const LandArgs<float>&, const nesf_land_radiation_params&, bool, cudaStream_t);
 
 }  // namespace nesf

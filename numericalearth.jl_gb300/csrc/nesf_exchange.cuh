@@ -43,6 +43,14 @@ template <class S> struct AsmArgs {
     AsmFields<S> f;
 };
 
+template <class S> struct LandArgs {
+    Layout2 L;
+    const uint8_t* inactive;
+    const S *rain, *QT, *Qv, *Jv, *Ts, *sw, *lw;
+    S *Es, *P, *E, *Jvo, *Pl;       // SlabLand accumulators
+    S *up_lw, *dn_lw, *dn_sw;       // radiation diagnostics
+};
+
 // part 0: fluxes + frazil adjustment of T3; 1: the fluxes alone (T3 read only); 2: the adjustment alone.
 template <class S> cudaError_t launch_io(const IOArgs<S>& a, const nesf_io_params& p, cudaStream_t s, int part = 0);
 cudaError_t launch_frac(const Layout2& L, const nesf_exchange_coords& c, const nesf_atmos_grid& ag, double* fi,
@@ -53,5 +61,9 @@ const void* interp_kernel_address(bool fp64);
 // which: 0 net ocean, 1 net sea ice, 2 ocean radiation, 3 sea-ice radiation
 template <class S>
 cudaError_t launch_assemble(const AsmArgs<S>& a, const nesf_assembly_params& p, int which, cudaStream_t s);
+
+// radiation false: the SlabLand accumulators; true: the radiative part added to surface_energy_flux
+template <class S>
+cudaError_t launch_land(const LandArgs<S>& a, const nesf_land_radiation_params& p, bool radiation, cudaStream_t s);
 
 }  // namespace nesf

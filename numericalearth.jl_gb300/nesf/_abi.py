@@ -229,6 +229,20 @@ class AssemblyFields(C.Structure):
     _fields_ = [("grid", Grid), ("dtype", i32), ("pad_", i32)] + [(n, vp) for n in ASSEMBLY_FIELD_NAMES]
 
 
+class LandRadiationParams(C.Structure):
+    _fields_ = [("stefan_boltzmann_constant", d), ("land_albedo", d), ("land_emissivity", d)]
+
+
+LAND_FLUX_FIELD_NAMES = (
+    "inactive", "rain", "al_sensible", "al_latent", "al_water_vapor", "al_interface_temperature",
+    "sw_down", "lw_down", "surface_energy_flux", "precipitation", "evaporation", "vapor_flux",
+    "liquid_precipitation_flux", "upwelling_longwave", "downwelling_longwave", "downwelling_shortwave")
+
+
+class LandFluxFields(C.Structure):
+    _fields_ = [("grid", Grid), ("dtype", i32), ("pad_", i32)] + [(n, vp) for n in LAND_FLUX_FIELD_NAMES]
+
+
 class CouplingStepArgs(C.Structure):
     _fields_ = [("ao_params", C.POINTER(InterfaceParams)), ("ao", C.POINTER(AOFields)),
                 ("ai_params", C.POINTER(InterfaceParams)), ("ai", C.POINTER(AIFields)),
@@ -295,4 +309,4 @@ STRUCTS_IN_SIZE_ORDER = (Grid, ThermodynamicsParameters, StabilityFunction, Roug
                          SimilarityTheoryFluxesC, InterfaceParams, SolverOptions, Stats, AOFields,
                          AIFields, IOParams, IOFields, AtmosGrid, ExchangeCoords, InterpFields,
                          AssemblyParams, AssemblyFields, CouplingStepArgs, IntegralFields, Tuning,
-                         TraceEntry, CoefficientFluxes, ALFields)
+                         TraceEntry, CoefficientFluxes, ALFields, LandRadiationParams, LandFluxFields)

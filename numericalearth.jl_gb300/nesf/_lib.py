@@ -52,6 +52,8 @@ SIGNATURES = {
     "nesf_assemble_net_sea_ice_fluxes": (C.c_int, [P(A.AssemblyParams), P(A.AssemblyFields), vp]),
     "nesf_apply_air_sea_radiative_fluxes": (C.c_int, [P(A.AssemblyParams), P(A.AssemblyFields), vp]),
     "nesf_apply_air_sea_ice_radiative_fluxes": (C.c_int, [P(A.AssemblyParams), P(A.AssemblyFields), vp]),
+    "nesf_assemble_net_land_fluxes": (C.c_int, [P(A.LandFluxFields), vp]),
+    "nesf_apply_air_land_radiative_fluxes": (C.c_int, [P(A.LandRadiationParams), P(A.LandFluxFields), vp]),
     "nesf_area_integrals": (C.c_int, [vp, P(A.IntegralFields), vp, vp]),
     "nesf_mlp_selftest": (C.c_int, [vp, vp, vp, C.c_int32, vp]),
     "nesf_mlp_bytes": (C.c_int64, []),

@@ -251,6 +251,23 @@ def apply_air_sea_ice_radiative_fluxes(spec, layout, arrays, stream=None):
     _assembly("nesf_apply_air_sea_ice_radiative_fluxes", spec, layout, arrays, stream)
 
 
+def assemble_net_land_fluxes(layout, arrays, stream=None):
+    """update_net_fluxes!(model, land::SlabLand) (Lands/slab_land.jl:285-329): `arrays` maps
+    nesf_land_flux_fields names to device tensors."""
+    lib = load()
+    f = F.pack(A.LandFluxFields, _grid_of(layout), arrays)
+    check(lib.nesf_assemble_net_land_fluxes(C.byref(f), _stream_handle(stream)))
+
+
+def apply_air_land_radiative_fluxes(radiation, layout, arrays, stream=None):
+    """apply_air_land_radiative_fluxes! (Radiations/apply_air_land_radiative_fluxes.jl:22-95);
+    `radiation` is a params.LandRadiation (or an nesf_land_radiation_params)."""
+    lib = load()
+    f = F.pack(A.LandFluxFields, _grid_of(layout), arrays)
+    p = radiation.to_c() if hasattr(radiation, "to_c") else radiation
+    check(lib.nesf_apply_air_land_radiative_fluxes(C.byref(p), C.byref(f), _stream_handle(stream)))
+
+
 def area_integrals(layout, fields, factors=None, inactive=None, area=None, row_area=None, uniform_area=1.0,
                    ctx=None, stream=None):
     """Compensated FP64 area integrals (int dA(a) / int dA(a, b) of the reference's conservation

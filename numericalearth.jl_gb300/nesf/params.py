@@ -864,3 +864,19 @@ class AssemblySpec:
         p.ice_albedo = self.sea_ice_surface.albedo
         p.ice_emissivity = self.sea_ice_surface.emissivity
         return p
+
+
+@dataclass
+class LandRadiation:
+    """The land surface of PrescribedRadiation (prescribed_radiation.jl:56, land_surface): the
+    reference has no default (nothing: no land radiation); its coupled dry-layer test uses
+    SurfaceRadiationProperties(0.2, 0.95)."""
+    land_surface: SurfaceRadiationProperties
+    stefan_boltzmann_constant: float = default_stefan_boltzmann_constant
+
+    def to_c(self):
+        p = A.LandRadiationParams()
+        p.stefan_boltzmann_constant = self.stefan_boltzmann_constant
+        p.land_albedo = self.land_surface.albedo
+        p.land_emissivity = self.land_surface.emissivity
+        return p

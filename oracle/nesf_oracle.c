@@ -1050,6 +1050,47 @@ int oracle_apply_air_sea_radiative_fluxes(const nesf_assembly_params* p, const n
     return NESF_OK;
 }
 
+/* _assemble_slab_land_fluxes! (Lands/slab_land.jl:316-329): the SlabLand accumulators */
+int oracle_assemble_net_land_fluxes(const nesf_land_flux_fields* f) {
+    const nesf_grid* g = &f->grid;
+    if (f->dtype != NESF_F64) return NESF_ERR_UNSUPPORTED;
+    for (int j = 1; j <= g->ny; j++) {
+        for (int i = 1; i <= g->nx; i++) {
+            int64_t k = idx2(g, i, j);
+            double QT = rd(f->al_sensible, k), Qv = rd(f->al_latent, k), Jv = rd(f->al_water_vapor, k);
+            double rain = rdz(f->rain, k);
+            wr(f->surface_energy_flux, k, QT + Qv);
+            wr(f->precipitation, k, rain + jmax(0.0, -Jv));
+            wr(f->evaporation, k, jmax(0.0, Jv));
+            wr(f->vapor_flux, k, Jv);
+            wr(f->liquid_precipitation_flux, k, rain);
+        }
+    }
+    return NESF_OK;
+}
+
+/* _apply_air_land_radiative_fluxes! (Radiations/apply_air_land_radiative_fluxes.jl:60-95) */
+int oracle_apply_air_land_radiative_fluxes(const nesf_land_radiation_params* p, const nesf_land_flux_fields* f) {
+    const nesf_grid* g = &f->grid;
+    if (f->dtype != NESF_F64) return NESF_ERR_UNSUPPORTED;
+    for (int j = 1; j <= g->ny; j++) {
+        for (int i = 1; i <= g->nx; i++) {
+            int64_t k = idx2(g, i, j);
+            double Ts = rd(f->al_interface_temperature, k);
+            double Iup = emitted_lw(Ts, p->stefan_boltzmann_constant, p->land_emissivity);
+            double Ia = absorbed_lw(p->land_emissivity, rd(f->lw_down, k));
+            double It = transmitted_sw(p->land_albedo, rd(f->sw_down, k));
+            double SQ = -Iup - (Ia + It);   /* positive into the land */
+            int inactive = f->inactive ? f->inactive[k] != 0 : 0;
+            ((double*)f->surface_energy_flux)[k] += inactive ? 0.0 : -SQ;
+            wr(f->upwelling_longwave, k, Iup);
+            wr(f->downwelling_longwave, k, -Ia);
+            wr(f->downwelling_shortwave, k, -It);
+        }
+    }
+    return NESF_OK;
+}
+
 /* _apply_air_sea_ice_radiative_fluxes! (apply_air_sea_ice_radiative_fluxes.jl:55-90) */
 int oracle_apply_air_sea_ice_radiative_fluxes(const nesf_assembly_params* p, const nesf_assembly_fields* f) {
     const nesf_grid* g = &f->grid;

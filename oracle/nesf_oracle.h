@@ -58,6 +58,8 @@ int oracle_assemble_net_ocean_fluxes(const nesf_assembly_params* p, const nesf_a
 int oracle_assemble_net_sea_ice_fluxes(const nesf_assembly_params* p, const nesf_assembly_fields* f);
 int oracle_apply_air_sea_radiative_fluxes(const nesf_assembly_params* p, const nesf_assembly_fields* f);
 int oracle_apply_air_sea_ice_radiative_fluxes(const nesf_assembly_params* p, const nesf_assembly_fields* f);
+int oracle_assemble_net_land_fluxes(const nesf_land_flux_fields* f);
+int oracle_apply_air_land_radiative_fluxes(const nesf_land_radiation_params* p, const nesf_land_flux_fields* f);
 
 void oracle_set_threads(int32_t n);
 void oracle_set_humidity_ulp_shift(int32_t n, int32_t carry);   /* conditioning probe for tests; 0 = off */

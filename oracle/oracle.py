@@ -59,6 +59,8 @@ def load():
             "oracle_assemble_net_sea_ice_fluxes": (C.c_int, [P(A.AssemblyParams), P(A.AssemblyFields)]),
             "oracle_apply_air_sea_radiative_fluxes": (C.c_int, [P(A.AssemblyParams), P(A.AssemblyFields)]),
             "oracle_apply_air_sea_ice_radiative_fluxes": (C.c_int, [P(A.AssemblyParams), P(A.AssemblyFields)]),
+            "oracle_assemble_net_land_fluxes": (C.c_int, [P(A.LandFluxFields)]),
+            "oracle_apply_air_land_radiative_fluxes": (C.c_int, [P(A.LandRadiationParams), P(A.LandFluxFields)]),
             "oracle_set_threads": (None, [C.c_int32]),
             "oracle_set_humidity_ulp_shift": (None, [C.c_int32, C.c_int32]),
             "oracle_get_threads": (C.c_int32, []),
@@ -197,6 +199,22 @@ def assemble(params, layout, arrays, which):
           "ocean_radiation": lib.oracle_apply_air_sea_radiative_fluxes,
           "sea_ice_radiation": lib.oracle_apply_air_sea_ice_radiative_fluxes}[which]
     _check(fn(C.byref(params), C.byref(f)), "oracle assembly")
+    return arrs
+
+
+def land_assembly(layout, arrays, radiation=None):
+    """oracle_assemble_net_land_fluxes (radiation None) or oracle_apply_air_land_radiative_fluxes
+    (radiation an nesf_land_radiation_params). Output arrays in `arrays` are updated in place
+    (they must be float64 numpy arrays)."""
+    lib = load()
+    arrs = {k: (_f64(v) if not (isinstance(v, np.ndarray) and v.dtype == np.float64 and v.flags["C_CONTIGUOUS"])
+                else v) for k, v in arrays.items()}
+    f = F.pack(A.LandFluxFields, F.make_grid(layout), arrs, dtype=A.NESF_F64)
+    if radiation is None:
+        _check(lib.oracle_assemble_net_land_fluxes(C.byref(f)), "oracle_assemble_net_land_fluxes")
+    else:
+        _check(lib.oracle_apply_air_land_radiative_fluxes(C.byref(radiation), C.byref(f)),
+               "oracle_apply_air_land_radiative_fluxes")
     return arrs
 
 

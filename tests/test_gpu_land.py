@@ -148,3 +148,54 @@ def test_dry_layer_rejects_degenerate_parameters(state):
     with pytest.raises(_lib.NesfError):
         api.compute_atmosphere_land_fluxes(P.atmosphere_land_interface_spec(specific_humidity=dry_layer()),
                                            state.layout, dev, out)
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_land_assembly_and_radiation(oracle, state, dtype):
+    """nesf_assemble_net_land_fluxes then nesf_apply_air_land_radiative_fluxes against the oracle,
+    on the fluxes of the 1-degree land solve with rainfall, radiation and a 10 % mask. FP64 fields:
+    identical to the oracle (both built without multiply-add contraction); FP32 fields (FP32
+    arithmetic): within 1e-6 of each output's largest magnitude."""
+    import torch
+    flux = oracle.al_fluxes(P.atmosphere_land_interface_spec().to_c(), state.layout, state.fields)
+    rng = np.random.default_rng(5)
+    shp = state.layout.shape
+    host = {"al_sensible": flux["sensible_heat"], "al_latent": flux["latent_heat"],
+            "al_water_vapor": flux["water_vapor"], "al_interface_temperature": flux["interface_temperature"],
+            "rain": rng.uniform(0, 1e-4, shp), "sw_down": rng.uniform(0, 1000, shp),
+            "lw_down": rng.uniform(250, 450, shp)}
+    tdt = torch.float64 if dtype == "f64" else torch.float32
+    host = {k: np.asarray(v, dtype=np.float64) if dtype == "f64" else
+            np.asarray(v, dtype=np.float32).astype(np.float64) for k, v in host.items()}
+    mask = (rng.uniform(size=shp) < 0.1).astype(np.uint8)
+    outs = ("surface_energy_flux", "precipitation", "evaporation", "vapor_flux", "liquid_precipitation_flux",
+            "upwelling_longwave", "downwelling_longwave", "downwelling_shortwave")
+    rad = P.LandRadiation(P.SurfaceRadiationProperties(0.2, 0.95))
+    ref = {**{k: v.copy() for k, v in host.items()}, **{k: np.zeros(shp) for k in outs}, "inactive": mask}
+    ref = oracle.land_assembly(state.layout, ref)
+    ref = oracle.land_assembly(state.layout, ref, rad.to_c())
+    dev = {k: torch.tensor(v, dtype=tdt, device="cuda") for k, v in host.items()}
+    dev.update({k: torch.zeros(shp, dtype=tdt, device="cuda") for k in outs})
+    dev["inactive"] = torch.tensor(mask, device="cuda")
+    api.assemble_net_land_fluxes(state.layout, dev)
+    api.apply_air_land_radiative_fluxes(rad, state.layout, dev)
+    torch.cuda.synchronize()
+    I = state.layout.interior
+    for k in outs:
+        g, r = I(to_numpy(dev[k]).astype(np.float64)), I(ref[k])
+        if dtype == "f64":
+            assert np.array_equal(g, r), k
+        else:
+            assert np.abs(g - r).max() <= 1e-6 * np.abs(r).max(), (k, float(np.abs(g - r).max()))
+
+
+def test_land_assembly_rejects_missing_inputs(state):
+    from nesf import _lib
+    import torch
+    shp = state.layout.shape
+    z = lambda: torch.zeros(shp, dtype=torch.float64, device="cuda")
+    with pytest.raises(_lib.NesfError):
+        api.assemble_net_land_fluxes(state.layout, {"al_sensible": z(), "surface_energy_flux": z()})
+    with pytest.raises(_lib.NesfError):   # radiation needs T_s, SW, LW and the flux it adds to
+        api.apply_air_land_radiative_fluxes(P.LandRadiation(P.SurfaceRadiationProperties(0.2, 0.95)), state.layout,
+                                            {"al_interface_temperature": z(), "sw_down": z(), "lw_down": z()})

@@ -468,3 +468,51 @@ def test_pow_ten_thirds_is_correctly_rounded(oracle):
     for x in xs:
         assert f(float(x)) == float(mpmath.power(mpmath.mpf(float(x)), p)), float(x)
     assert f(0.0) == 0.0
+
+
+# ------------------------------------------------ SlabLand flux assembly and land radiation
+def _land_assembly(oracle, radiation=None, inactive=None, **values):
+    L, a = one_cell(**values)
+    if inactive is not None:
+        a["inactive"] = np.full(L.shape, inactive, dtype=np.uint8)
+    for k in ("surface_energy_flux", "precipitation", "evaporation", "vapor_flux", "liquid_precipitation_flux",
+              "upwelling_longwave", "downwelling_longwave", "downwelling_shortwave"):
+        a.setdefault(k, np.zeros(L.shape))
+    out = oracle.land_assembly(L, a, radiation)
+    return {k: float(L.interior(v)[0, 0]) for k, v in out.items()}
+
+
+def test_slab_land_assembly_cases(oracle):
+    """The cases of the reference's test/test_slab_land.jl: evaporation, dew, rain with dew,
+    and the turbulent surface energy flux (positive upward)."""
+    z = dict(al_sensible=0.0, al_latent=0.0, rain=0.0)
+    up = _land_assembly(oracle, **z, al_water_vapor=0.5)
+    assert (up["precipitation"], up["evaporation"]) == (0.0, 0.5)
+    dew = _land_assembly(oracle, **z, al_water_vapor=-0.5)
+    assert (dew["precipitation"], dew["evaporation"]) == (0.5, 0.0)
+    wet = _land_assembly(oracle, al_sensible=0.0, al_latent=0.0, al_water_vapor=-0.2, rain=1.5)
+    assert wet["precipitation"] == pytest.approx(1.7, abs=1e-12) and wet["evaporation"] == 0.0
+    assert wet["liquid_precipitation_flux"] == 1.5 and wet["vapor_flux"] == -0.2
+    es = _land_assembly(oracle, al_sensible=2.0, al_latent=-5.0, al_water_vapor=0.0, rain=0.0)
+    assert es["surface_energy_flux"] == -3.0
+
+
+def test_land_radiation_adds_to_surface_energy_flux(oracle):
+    """Radiations/apply_air_land_radiative_fluxes.jl as the reference's coupled tests check it:
+    the radiation is added to the turbulent surface_energy_flux as -sum_rad, with sum_rad rebuilt
+    from the stored diagnostics (downwelling positive into the land, upwelling out); a black
+    surface (alpha 0, eps 1) with no incoming radiation raises the flux by sigma T^4."""
+    rad = P.LandRadiation(P.SurfaceRadiationProperties(0.2, 0.95)).to_c()
+    cell = dict(al_interface_temperature=295.0, sw_down=600.0, lw_down=350.0, surface_energy_flux=-3.0)
+    r = _land_assembly(oracle, rad, **cell)
+    sum_rad = r["downwelling_longwave"] + r["downwelling_shortwave"] - r["upwelling_longwave"]
+    assert r["surface_energy_flux"] == pytest.approx(-3.0 - sum_rad, rel=1e-15)
+    assert r["downwelling_shortwave"] == pytest.approx(0.8 * 600.0, rel=1e-15)
+    assert r["downwelling_longwave"] == pytest.approx(0.95 * 350.0, rel=1e-15)
+    black = P.LandRadiation(P.SurfaceRadiationProperties(0.0, 1.0)).to_c()
+    b = _land_assembly(oracle, black, al_interface_temperature=300.0, sw_down=0.0, lw_down=0.0,
+                       surface_energy_flux=0.0)
+    assert b["upwelling_longwave"] > 0 and b["surface_energy_flux"] == b["upwelling_longwave"]
+    assert b["upwelling_longwave"] == pytest.approx(5.670374419e-8 * 300.0 ** 4, rel=1e-15)
+    masked = _land_assembly(oracle, rad, **cell, inactive=1)
+    assert masked["surface_energy_flux"] == -3.0
