@@ -418,6 +418,7 @@ def cpu_baseline(state, target_s=12.0):
     threads = oracle.get_threads()
     done_cells = 0
     elapsed = 0.0
+    hist = {}
     ao = P.atmosphere_ocean_interface_spec().to_c()
     ai = P.atmosphere_sea_ice_interface_spec().to_c()
     sub = syn.Layout(L.nx, rows, L.hx, L.hy)
@@ -437,16 +438,44 @@ def cpu_baseline(state, target_s=12.0):
             for n, k in (("u", "u_atm"), ("v", "v_atm"), ("T", "T_atm"), ("q", "q_atm"), ("p", "p_atm"),
                          ("sw", "sw_down"), ("lw", "lw_down")):
                 band[k] = out[n]
-        oracle.ao_fluxes(ao, sub, band, with_iterations=False)
-        oracle.ai_fluxes(ai, sub, band, band["ice_temperature"], with_iterations=False)
+        ro = oracle.ao_fluxes(ao, sub, band)
+        ri = oracle.ai_fluxes(ai, sub, band, band["ice_temperature"])
         elapsed += time.perf_counter() - t0
         water = sub.interior(band["inactive"]) == 0
         ice = sub.interior(band["ice_concentration"]) > 0
         done_cells += int(water.sum() + (water & ice).sum())
+        for name, its, sel in (("ao", ro["iterations"], water), ("ai", ri["iterations"], water & ice)):
+            h = hist.setdefault(name, np.zeros(len(ITER_BINS) - 1, dtype=np.int64))
+            h += np.histogram(sub.interior(its)[sel], bins=ITER_BINS)[0]
         bands += 1
     return {"value": done_cells / elapsed, "unit": "flux cells/s", "cores": threads, "kind": "port",
+            "nproc": os.cpu_count(), "cpu_model": cpu_model(),
+            "iteration_histogram": {"bins": ITER_BINS.tolist(), **{k: v.tolist() for k, v in hist.items()}},
             "sample": f"{bands} bands of {rows} rows x {L.nx} cells spread over the domain ({done_cells} "
                       f"solved cells): interpolation + AO + AI solves, {elapsed:.1f} s of CPU work"}
+
+
+ITER_BINS = np.array([1, 3, 5, 8, 12, 16, 20, 30, 50, 100, 101])
+
+
+def cpu_model():
+    """The host CPU's model name (/proc/cpuinfo; on Arm the implementer and part numbers)."""
+    try:
+        with open("/proc/cpuinfo") as fh:
+            info = fh.read()
+    except OSError:
+        return "unknown"
+    for key in ("model name", "Model"):
+        for line in info.splitlines():
+            if line.startswith(key) and ":" in line:
+                return line.split(":", 1)[1].strip()
+    parts = {}
+    for line in info.splitlines():
+        if ":" in line:
+            k, v = (x.strip() for x in line.split(":", 1))
+            if k in ("CPU implementer", "CPU part") and k not in parts:
+                parts[k] = v
+    return ", ".join(f"{k} {v}" for k, v in parts.items()) or "unknown"
 
 
 def run_reference(args):
@@ -468,6 +497,8 @@ def run_reference(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "sample": "row bands of the workload", "parallelism": "openmp"},
             "cpu_baseline": {"value": v, "unit": "flux cells/s", "cores": oracle.get_threads(), "kind": "port",
+                             "nproc": vals[-1]["nproc"], "cpu_model": vals[-1]["cpu_model"],
+                             "iteration_histogram": vals[-1]["iteration_histogram"],
                              "sample": vals[-1]["sample"] + " (the reference is Julia; no Julia toolchain here)"},
             "e2e": {"value": v, "unit": "flux cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
