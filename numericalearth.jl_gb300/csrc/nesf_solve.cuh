@@ -421,17 +421,28 @@ __device__ __forceinline__ float spectral_bound(const float (&J)[N][N]) {
 // the cells that pass 1 did not keep repeats pass 1's sweep exactly, so it reaches
 // the same decisions.
 //
-// The FP32 sweep and the 2N evaluations of the central-difference Jacobian run
-// through one loop around a single inlined copy of the map, so a warp executes
-// the same instructions for both: the kernel's hot code stays small enough for
-// the instruction cache.
-template <bool SKIN, bool ACCEPT32, bool STRICT = ACCEPT32>
+// Bulk temperature (N = 3): J is a forward difference around the sweep's last
+// evaluated point x_b (whose image y_b = F(x_b) the sweep already has), N map
+// evaluations, enough for the decisions (rho, the replay rules, ADAPTIVE's
+// acceptance), which tolerate its O(h) bias. CENTRAL (the cells that go on to FP64
+// Newton steps): after the decisions the N mirrored points are evaluated too and J
+// becomes the central difference, O(h^2), which the Newton steps' convergence needs
+// on slowly contracting cells. Pass 1 of ADAPTIVE takes no CENTRAL: its polish
+// pass repeats the sweep (same decisions) with CENTRAL. Skin temperature (N = 4):
+// the central difference around x from the start, 2N evaluations (the forward
+// scheme's extra state costs these kernels more in spills than it saves).
+//
+// The FP32 sweep and the Jacobian's evaluations run through one loop around a
+// single inlined copy of the map, so a warp executes the same instructions for
+// all of them: the kernel's hot code stays small enough for the instruction cache.
+template <bool SKIN, bool ACCEPT32, bool STRICT = ACCEPT32, bool CENTRAL = !ACCEPT32>
 __device__ __forceinline__ int sweep_fp32(const DevIface<float>& P32, const CellConst<float>& c32,
                                           const SurfaceConst<float>& s32, const SkinAnchor<float>& anc,
                                           float (&x)[4], const SolveOpts& so, int& fp32_it, int& reason,
                                           float (&J)[SKIN ? 4 : 3][SKIN ? 4 : 3], float& rho_est,
                                           const float* xw, bool* fell_back) {
     constexpr int N = SKIN ? 4 : 3;
+    constexpr bool FWD = !SKIN;   // forward-difference J (bulk temperature)
     const float tol = P32.tol;
     const float x0[4] = {x[0], x[1], x[2], x[3]};
     // warm start: the network's (u*, theta*, q*) replaces the reference's start; T_s keeps its own
@@ -440,7 +451,10 @@ __device__ __forceinline__ int sweep_fp32(const DevIface<float>& P32, const Cell
     float yw[4] = {0, 0, 0, 0};   // first iterate from the warm start while the cold start is probed
     float rw = 0.0f;
     int probes = 0;
-    float yp[4] = {0, 0, 0, 0};   // F(x + h e_j) of the column in progress
+    float xb[4] = {0, 0, 0, 0};   // FWD: the last sweep point and its image, the Jacobian's base
+    float yb[4] = {0, 0, 0, 0};
+    float yp[4] = {0, 0, 0, 0};   // !FWD: F(x + h e_j) of the column in progress
+    bool decided = false;         // FWD: the decisions are made; CENTRAL's mirrored points follow
     SweepTrace tr;
     tr.d[0] = tr.d[1] = tr.d[2] = 0.0f;
     tr.lam = 1.0f;
@@ -448,10 +462,12 @@ __device__ __forceinline__ int sweep_fp32(const DevIface<float>& P32, const Cell
     int rising = 0;
     bool stalled = false;  // the sweep ended on the rising-drift rule
     int it = 0;            // sweep iterations
-    int phase = 0;         // 0 sweep; 1 cold-start probe; 2 + 2j / 3 + 2j: F(x + h e_j) / F(x - h e_j)
+    int phase = 0;         // 0 sweep; 1 cold-start probe; FWD: 2 + j: F(x_b + h e_j), N + 2 + j:
+                           // F(x_b - h e_j); !FWD: 2 + 2j / 3 + 2j: F(x + h e_j) / F(x - h e_j)
     float h = 0.0f;
     float cond = 1.0f;     // condition of the anchored differences at the last sweep iterate
     const int limit = P32.maxiter;
+sweep:
 #pragma unroll 1
     for (;;) {
         float xin[4] = {x[0], x[1], x[2], x[3]};
@@ -460,11 +476,13 @@ __device__ __forceinline__ int sweep_fp32(const DevIface<float>& P32, const Cell
             for (int k = 0; k < 4; k++) xin[k] = x0[k];
         }
         if (phase >= 2) {
-            const int jj = (phase - 2) >> 1;
-            const float sgn = (phase & 1) ? -1.0f : 1.0f;
+            const bool minus = FWD ? phase >= N + 2 : (phase & 1) != 0;
+            const int jj = FWD ? phase - (minus ? N + 2 : 2) : (phase - 2) >> 1;
 #pragma unroll
-            for (int k = 0; k < 4; k++)
-                if (k == jj) { h = jac_step(k, x[k]); xin[k] += sgn * h; }
+            for (int k = 0; k < 4; k++) {
+                if (FWD) xin[k] = xb[k];
+                if (k == jj) { h = jac_step(k, xin[k]); xin[k] += minus ? -h : h; }
+            }
         }
         float yu = xin[0], yt = xin[1], yq = xin[2], yT = xin[3];
         if (SKIN) {
@@ -508,7 +526,10 @@ __device__ __forceinline__ int sweep_fp32(const DevIface<float>& P32, const Cell
                 continue;
             }
 #pragma unroll
-            for (int k = 0; k < 4; k++) x[k] = y[k];
+            for (int k = 0; k < 4; k++) {
+                if (FWD) { xb[k] = xin[k]; yb[k] = y[k]; }
+                x[k] = y[k];
+            }
             // FP32 resolution of the drift sum: the ulps of the scales themselves
             float res = 1.1920929e-7f * (fabsf(x[0]) + fabsf(x[1]) + fabsf(x[2]));
             if (drift > 64.0f * res || it <= 2) {
@@ -534,11 +555,11 @@ __device__ __forceinline__ int sweep_fp32(const DevIface<float>& P32, const Cell
                 reason = REPLAY_NO_FP32;
                 return FAST_REPLAY;                       // no FP32 convergence
             }
-        } else if (!(phase & 1)) {
+        } else if (!FWD && !(phase & 1)) {
 #pragma unroll
             for (int k = 0; k < 4; k++) yp[k] = y[k];
             phase++;
-        } else {
+        } else if (!FWD) {
             // central difference: column (phase - 3) / 2
             const int jj = (phase - 3) >> 1;
             const float inv2h = 0.5f / h;
@@ -548,9 +569,34 @@ __device__ __forceinline__ int sweep_fp32(const DevIface<float>& P32, const Cell
                 for (int k = 0; k < N; k++)
                     if (k == jj) J[ii][k] = (yp[ii] - y[ii]) * inv2h;
             if (++phase == 2 * N + 2) break;
+        } else if (phase < N + 2) {
+            // forward difference: column phase - 2
+            const int jj = phase - 2;
+            const float invh = 1.0f / h;
+#pragma unroll
+            for (int ii = 0; ii < N; ii++)
+#pragma unroll
+                for (int k = 0; k < N; k++)
+                    if (k == jj) J[ii][k] = (y[ii] - yb[ii]) * invh;
+            if (++phase == N + 2) break;
+        } else {
+            // the mirrored point of column phase - N - 2: the forward column becomes the central
+            // difference (F(x_b + h e_j) - F(x_b - h e_j)) / 2h, F(x_b + h e_j) = y_b + h J e_j
+            const int jj = phase - (N + 2);
+            const float inv2h = 0.5f / h;
+#pragma unroll
+            for (int ii = 0; ii < N; ii++)
+#pragma unroll
+                for (int k = 0; k < N; k++)
+                    if (k == jj) J[ii][k] = (J[ii][k] * h + yb[ii] - y[ii]) * inv2h;
+            if (++phase == 2 * N + 2) break;
         }
     }
-    fp32_it = it + probes + 2 * N;
+    if (FWD && decided) {   // CENTRAL: the mirrored points are in J; the decisions were made before them
+        fp32_it += N;
+        return FAST_POLISH;
+    }
+    fp32_it = it + probes + (FWD ? N : 2 * N);
     // ---- contraction rate of F at the solution
     rho_est = spectral_bound<N>(J);
     if (!(rho_est < 0.995f)) { reason = REPLAY_SLOW; return FAST_REPLAY; }
@@ -594,6 +640,10 @@ __device__ __forceinline__ int sweep_fp32(const DevIface<float>& P32, const Cell
     // cancellation and by 1 / (1 - rho), must stay within path_tol
     if (ACCEPT32 && !stalled && rho_est <= so.fp32_rho && cond * 1.2e-7f <= so.path_tol * (1.0f - rho_est))
         return FAST_SOLVED;
+    if (FWD && CENTRAL) {   // back into the loop for the mirrored points (one copy of the map)
+        decided = true;
+        goto sweep;
+    }
     return FAST_POLISH;
 }
 
