@@ -345,7 +345,8 @@ typedef struct {
     int32_t pad_;
     const void* u_atm; const void* v_atm; const void* T_atm; const void* p_atm; const void* q_atm;
     const void* land_temperature;      /* bulk land temperature T (K)                          */
-    const void* saturation;            /* land surface saturation S (BULK, FRACTIONAL with S_c) */
+    const void* saturation;            /* land surface saturation S (BULK, DRY_LAYER,
+                                          FRACTIONAL with S_c)                                 */
     /* outputs: AtmosphereSurfaceFluxes + T_s */
     void* latent_heat; void* sensible_heat; void* water_vapor;
     void* x_momentum;  void* y_momentum;
