@@ -442,6 +442,24 @@ typedef struct {
     const double* frac_i; const double* frac_j;
 } nesf_interp_fields;
 
+/* ----------------------------------------------- time interpolation of forcing
+ * The time indexing of Oceananigans' FieldTimeSeries, which PrescribedAtmosphere holds its
+ * forcing in (cpu_interpolating_time_indices, as interpolate_atmospheric_state.jl:57-60
+ * calls it; the JRA55 atmosphere cycles its repeat year,
+ * JRA55_prescribed_atmosphere.jl:37). Host-only: no device work. */
+typedef enum {
+    NESF_TIME_CYCLICAL = 0,   /* t wrapped into [t_0, t_0 + period); between t_last and
+                                 t_0 + period the last snapshot blends into the first        */
+    NESF_TIME_LINEAR = 1,     /* the bracketing interval, extrapolated beyond the ends        */
+    NESF_TIME_CLAMP = 2       /* the first / last snapshot outside the range                  */
+} nesf_time_indexing;
+
+/* The snapshots n1, n2 (0-based) that bracket time t and the weight of n2 (the
+   interpolation's time_weight). times: nt strictly increasing values; period: the cycle
+   length for NESF_TIME_CYCLICAL (<= 0: t_last - t_0 plus the last interval). */
+int nesf_time_indices(const double* times, int32_t nt, int32_t indexing, double period, double t, int32_t* n1,
+                      int32_t* n2, double* weight);
+
 /* ------------------------------------------------------- net-flux assembly */
 typedef struct {
     double ocean_reference_density;   /* rho_o */
@@ -542,6 +560,9 @@ typedef struct nesf_context nesf_context;   /* library-owned scratch per device 
 
 int32_t     nesf_abi_version(void);
 const char* nesf_version(void);
+/* Per-device set-up ahead of the first call (the default context that calls with a
+   null context use); optional, the first call does it otherwise. */
+int nesf_init(int32_t device);
 const char* nesf_last_error(void);
 /* sizes of the public structs, for binding checks: fills n entries */
 int32_t     nesf_struct_sizes(int64_t* sizes, int32_t n);

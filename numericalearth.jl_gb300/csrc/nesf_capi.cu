@@ -610,6 +610,67 @@ static int context_or_default(nesf_context** ctx) {
     return NESF_OK;
 }
 
+// cpu_interpolating_time_indices of a FieldTimeSeries (interpolate_atmospheric_state.jl:57-60):
+// the bracketing snapshots of t and the weight of the second, on the host.
+int nesf_time_indices(const double* times, int32_t nt, int32_t indexing, double period, double t, int32_t* n1,
+                      int32_t* n2, double* weight) {
+    const char* who = "nesf_time_indices";
+    if (!times || !n1 || !n2 || !weight || nt < 1) return fail(NESF_ERR_ARG, "%s: null argument or nt < 1", who);
+    if (indexing < NESF_TIME_CYCLICAL || indexing > NESF_TIME_CLAMP)
+        return fail(NESF_ERR_ARG, "%s: time indexing %d", who, indexing);
+    if (!std::isfinite(t)) return fail(NESF_ERR_ARG, "%s: time %g", who, t);
+    for (int32_t n = 1; n < nt; n++)
+        if (!(times[n] > times[n - 1])) return fail(NESF_ERR_ARG, "%s: times not strictly increasing at %d", who, n);
+    if (nt == 1) {
+        *n1 = *n2 = 0;
+        *weight = 0;
+        return NESF_OK;
+    }
+    const double t0 = times[0], tl = times[nt - 1];
+    if (indexing == NESF_TIME_CYCLICAL) {
+        const double P = period > 0 ? period : (tl - t0) + (tl - times[nt - 2]);
+        if (!(P > tl - t0)) return fail(NESF_ERR_ARG, "%s: period %g does not exceed the times' span", who, P);
+        double tau = std::fmod(t - t0, P);
+        if (tau < 0) tau += P;
+        t = t0 + tau;
+        if (t >= tl) {   // between the last snapshot and the first one's next cycle
+            *n1 = nt - 1;
+            *n2 = 0;
+            *weight = (t - tl) / (t0 + P - tl);
+            return NESF_OK;
+        }
+    } else if (indexing == NESF_TIME_CLAMP && (t <= t0 || t >= tl)) {
+        *n1 = *n2 = t <= t0 ? 0 : nt - 1;
+        *weight = 0;
+        return NESF_OK;
+    }
+    // the last snapshot at or before t, within [0, nt - 2]
+    int32_t lo = 0, hi = nt - 1;
+    if (t < t0) hi = 0;
+    while (hi - lo > 1) {
+        const int32_t mid = lo + (hi - lo) / 2;
+        if (times[mid] <= t) lo = mid;
+        else hi = mid;
+    }
+    const int32_t n = lo < nt - 2 ? lo : nt - 2;
+    *n1 = n;
+    *n2 = n + 1;
+    *weight = (t - times[n]) / (times[n + 1] - times[n]);
+    return NESF_OK;
+}
+
+// The library's per-device set-up done ahead of the first call: the default context of
+// `device` (its streams, events and scratch), which the calls that take a null context
+// use. The caller's current device is left as it was.
+int nesf_init(int32_t device) {
+    int n = 0;
+    NESF_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n || device >= 64) return fail(NESF_ERR_ARG, "nesf_init: device %d of %d", device, n);
+    std::lock_guard<std::mutex> lk(g_default_lock);
+    if (!g_default_ctx[device]) return nesf_context_create(device, &g_default_ctx[device]);
+    return NESF_OK;
+}
+
 static void stats_to_public(const DevStats& d, nesf_stats* s) {
     s->cells = (int64_t)d.cells;
     s->solved = (int64_t)d.solved;

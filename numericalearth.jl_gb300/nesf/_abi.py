@@ -163,6 +163,9 @@ HUMIDITY_BULK = 1
 HUMIDITY_FRACTIONAL = 2
 HUMIDITY_SKIN = 3
 HUMIDITY_DRY_LAYER = 4
+TIME_CYCLICAL = 0
+TIME_LINEAR = 1
+TIME_CLAMP = 2
 TORTUOSITY_CONSTANT = 0
 TORTUOSITY_POWER_LAW = 1
 

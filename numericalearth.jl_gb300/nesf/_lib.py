@@ -29,6 +29,9 @@ SIGNATURES = {
     "nesf_default_al_params": (None, [P(A.InterfaceParams)]),
     "nesf_default_coefficient_fluxes": (None, [P(A.CoefficientFluxes), C.c_int32]),
     "nesf_default_io_params": (None, [P(A.IOParams)]),
+    "nesf_time_indices": (C.c_int, [P(C.c_double), C.c_int32, C.c_int32, C.c_double, C.c_double, P(C.c_int32),
+                                          P(C.c_int32), P(C.c_double)]),
+    "nesf_init": (C.c_int, [C.c_int32]),
     "nesf_default_assembly_params": (None, [P(A.AssemblyParams)]),
     "nesf_default_solver_options": (None, [P(A.SolverOptions)]),
     "nesf_context_create": (C.c_int, [C.c_int32, P(vp)]),

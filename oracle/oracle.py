@@ -250,3 +250,31 @@ def area_integrals(layout, fields, factors=None, inactive=None, area=None, row_a
             total *= Fraction(float(uniform_area))
         out.append(total)
     return out
+
+
+def time_indices(times, indexing, period, t):
+    """The bracketing snapshots (0-based n1, n2) of time t and the weight of n2, restated from
+    the time indexing of Oceananigans' FieldTimeSeries (Cyclical / Linear / Clamp), which
+    NumericalEarth's atmosphere interpolation calls (interpolate_atmospheric_state.jl:57-60;
+    the package is not vendored with the reference, so this follows its documented behaviour:
+    Cyclical wraps t into [t_0, t_0 + period) and blends the last snapshot into the first past
+    t_last, its default period being the span plus the last interval; Linear extrapolates the
+    end intervals; Clamp holds the end snapshots)."""
+    times = np.asarray(times, dtype=np.float64)
+    nt = len(times)
+    if nt == 1:
+        return 0, 0, 0.0
+    t0, tl = float(times[0]), float(times[-1])
+    if indexing == "cyclical":
+        P = period if period and period > 0 else (tl - t0) + (tl - float(times[-2]))
+        t = t0 + float(np.mod(t - t0, P))
+        if t >= tl:
+            return nt - 1, 0, (t - tl) / (t0 + P - tl)
+    elif indexing == "clamp":
+        if t <= t0:
+            return 0, 0, 0.0
+        if t >= tl:
+            return nt - 1, nt - 1, 0.0
+    n = int(np.searchsorted(times, t, side="right")) - 1
+    n = min(max(n, 0), nt - 2)
+    return n, n + 1, (t - float(times[n])) / (float(times[n + 1]) - float(times[n]))
