@@ -756,6 +756,12 @@ int nesf_graph_capture(nesf_context* ctx, const nesf_coupling_step_args* args, c
                        nesf_graph** out);
 int nesf_graph_set_time_weight(nesf_graph* graph, double time_weight);
 int nesf_graph_launch(nesf_graph* graph, void* stream);
+/* The snapshot pair the captured interpolation reads, for a forcing window whose pair moves
+   between device slots: src[9] (u v T q p rain snow sw lw; NULL keeps the captured array,
+   and only variables interpolated at capture can be set) is each variable's first snapshot,
+   stride_t the elements from it to the second (negative allowed), time_weight the pair's
+   weight (nesf_time_indices). The arrays keep the captured atmosphere grid and dtype. */
+int nesf_graph_set_forcing(nesf_graph* graph, const void* const* src, int64_t stride_t, double time_weight);
 int nesf_graph_destroy(nesf_graph* graph);
 
 /* ------------------------------------------------------------ the autotuner

@@ -1601,6 +1601,41 @@ extern "C" int nesf_graph_set_time_weight(nesf_graph* G, double tn) {
     return NESF_OK;
 }
 
+// The snapshot pair a captured step's interpolation reads, for a forcing window that moves
+// the pair between device slots: per variable the first snapshot (NULL keeps the captured
+// pointer), the stride to the second one and the pair's time weight.
+template <class S>
+static int set_forcing_args(InterpArgs<S>* a, const void* const* src, int64_t stride_t, double tn) {
+    for (int n = 0; n < 9; n++) {
+        if (!src || !src[n]) continue;
+        if (!a->src[n])
+            return fail(NESF_ERR_ARG, "nesf_graph_set_forcing: variable %d was not interpolated at capture", n);
+        if (((uintptr_t)src[n]) % sizeof(S))
+            return fail(NESF_ERR_ARG, "nesf_graph_set_forcing: variable %d is not aligned to its type", n);
+    }
+    for (int n = 0; n < 9; n++)
+        if (src && src[n]) a->src[n] = (const S*)src[n];
+    a->atmos.stride_t = stride_t;
+    a->tn = tn;
+    return NESF_OK;
+}
+
+extern "C" int nesf_graph_set_forcing(nesf_graph* G, const void* const* src, int64_t stride_t, double tn) {
+    if (!G) return fail(NESF_ERR_ARG, "nesf_graph_set_forcing: null graph");
+    if (!G->interp_node) return fail(NESF_ERR_ARG, "nesf_graph_set_forcing: the graph has no interpolation");
+    if (!(tn >= 0.0 && tn <= 1.0)) return fail(NESF_ERR_ARG, "nesf_graph_set_forcing: weight %g", tn);
+    DeviceGuard g(G->device);
+    int r = G->interp_fp64 ? set_forcing_args((InterpArgs<double>*)G->interp_args, src, stride_t, tn)
+                           : set_forcing_args((InterpArgs<float>*)G->interp_args, src, stride_t, tn);
+    if (r) return r;
+    void* args[1] = {G->interp_args};
+    cudaKernelNodeParams kp = G->interp_params;
+    kp.kernelParams = args;
+    kp.extra = nullptr;
+    NESF_CUDA(cudaGraphExecKernelNodeSetParams(G->exec, G->interp_node, &kp));
+    return NESF_OK;
+}
+
 extern "C" int nesf_graph_launch(nesf_graph* G, void* stream) {
     if (!G) return fail(NESF_ERR_ARG, "nesf_graph_launch: null graph");
     DeviceGuard g(G->device);

@@ -69,6 +69,7 @@ SIGNATURES = {
     "nesf_coupling_step": (C.c_int, [vp, P(A.CouplingStepArgs), P(A.SolverOptions), vp]),
     "nesf_graph_capture": (C.c_int, [vp, P(A.CouplingStepArgs), P(A.SolverOptions), P(vp)]),
     "nesf_graph_set_time_weight": (C.c_int, [vp, C.c_double]),
+    "nesf_graph_set_forcing": (C.c_int, [vp, P(vp), C.c_int64, C.c_double]),
     "nesf_graph_launch": (C.c_int, [vp, vp]),
     "nesf_graph_destroy": (C.c_int, [vp]),
     "nesf_set_tuning": (C.c_int, [vp, P(A.Tuning)]),

@@ -192,6 +192,7 @@ def exchange_coords(c):
     return A.ExchangeCoords(c.lon0, c.dlon, c.lat0, c.dlat)
 
 
+INTERP_ORDER = ("u", "v", "T", "q", "p", "rain", "snow", "sw", "lw")   # nesf_interp_fields' order
 INTERP_SRC = {"u": "u", "v": "v", "T": "T", "q": "q", "p": "p", "rain": "rain", "snow": "snow", "sw": "sw_down",
               "lw": "lw_down"}
 INTERP_DST = {"u": "u_out", "v": "v_out", "T": "T_out", "q": "q_out", "p": "p_out", "rain": "rain_out",
@@ -433,6 +434,12 @@ class Graph:
 
     def set_time_weight(self, tn):
         check(self.lib.nesf_graph_set_time_weight(self.handle, float(tn)))
+
+    def set_forcing(self, arrays, stride_t, tn):
+        """nesf_graph_set_forcing: `arrays` maps u v T q p rain snow sw lw to each variable's
+        first snapshot (device tensors; absent names keep the captured arrays)."""
+        ptrs = (C.c_void_p * 9)(*[(arrays[n].data_ptr() if n in arrays else None) for n in INTERP_ORDER])
+        check(self.lib.nesf_graph_set_forcing(self.handle, ptrs, int(stride_t), float(tn)))
 
     def launch(self, stream=None):
         check(self.lib.nesf_graph_launch(self.handle, _stream_handle(stream)))

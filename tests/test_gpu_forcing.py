@@ -6,6 +6,7 @@ the first (11 snapshots in 5 slots: with slot = index mod 5 both would share a s
 import numpy as np
 import pytest
 
+from helpers import to_numpy
 from nesf import api
 from nesf import forcing
 from nesf import synthetic as syn
@@ -44,3 +45,39 @@ def test_window_interpolation_matches_explicit_pairs(oracle, tmp_path):
         assert win.uploads < 2 * len(ts)   # the window reuses and prefetches its slots
     finally:
         win.close()
+
+
+def test_graph_follows_the_window(tmp_path):
+    """A captured coupling step fed by the window through nesf_graph_set_forcing: after each
+    replay the exchange-grid atmosphere equals the interpolation of the explicit pair."""
+    import torch
+    from nesf.coupled import ATMOS_NAMES, EXCHANGE_ATMOS, CoupledModel
+    st = syn.coupled(seed=21, nx=240, ny=120, lat_s=-80, lat_n=80, land=0.3, interpolate=True)
+    base = st.atmos["arrays"]
+    nt, dt = 7, 10800.0
+    series = {n: np.stack([base[n][k % 2] * (1 + 0.01 * k) if n not in ("u", "v") else base[n][k % 2] + 0.3 * k
+                           for k in range(nt)]).astype(base[n].dtype) for n in base}
+    times = np.arange(nt) * dt
+    m = CoupledModel(st)
+    m.capture("f32_adaptive")
+    dtype = torch.from_numpy(series["T"][:1]).dtype
+    win = forcing.FieldTimeSeriesWindow(forcing.ArraySource(series), times, st.atmos["layout"], slots=3, dtype=dtype)
+    try:
+        for t in (0.0, 0.4 * dt, 2.5 * dt, 6.5 * dt, 7.25 * dt, 13.0 * dt):
+            arrays, stride, w = win.update(t)
+            m.graph.set_forcing(arrays, stride, w)
+            m.reset()
+            m.graph_step()
+            win.release()
+            n1, n2, _ = forcing.time_indices(times, t)
+            pair = {n: torch.tensor(np.stack([series[n][n1], series[n][n2]]), device="cuda") for n in series}
+            ref = {n: torch.zeros_like(m.x[EXCHANGE_ATMOS[n]]) for n in ATMOS_NAMES}
+            api.interpolate_atmosphere_state(m.layout, m.coords, st.atmos, pair, ref, w, frac=(m.fi, m.fj))
+            torch.cuda.synchronize()
+            R = m.layout.ring   # the interpolation writes the interior and its one-cell ring
+            for n in ATMOS_NAMES:
+                assert np.array_equal(R(to_numpy(m.x[EXCHANGE_ATMOS[n]])), R(to_numpy(ref[n]))), (t, n)
+            assert torch.isfinite(m.ao["latent_heat"]).all()
+    finally:
+        win.close()
+        m.graph.close()
