@@ -398,15 +398,21 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     return cudaSuccess;
 }
 
+// The build compiles this file once per storage type (NESF_STORAGE = 64, then 32), so the
+// two halves of the kernel instantiations compile in parallel; undefined builds both.
+#if !defined(NESF_STORAGE) || NESF_STORAGE == 64
 cudaError_t launch_ai(const AIArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
                       cudaStream_t stream, cudaEvent_t after_solve, const TailLane* tail) {
     return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream, after_solve, tail);
 }
+#endif
+#if !defined(NESF_STORAGE) || NESF_STORAGE == 32
 cudaError_t launch_ai(const AIArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
                       cudaStream_t stream, cudaEvent_t after_solve, const TailLane* tail) {
     return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream, after_solve, tail);
 }
+#endif
 
 }  // namespace nesf

@@ -161,13 +161,19 @@ static cudaError_t launch_al_t(const ALArgs<S>& a, const DevIface<double>& P64, 
     return e;
 }
 
+// The build compiles this file once per storage type (NESF_STORAGE = 64, then 32), so the
+// two halves of the kernel instantiations compile in parallel; undefined builds both.
+#if !defined(NESF_STORAGE) || NESF_STORAGE == 64
 cudaError_t launch_al(const ALArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, DevStats* stats, cudaStream_t stream) {
     return launch_al_t(a, P64, P32, prec, so, stats, stream);
 }
+#endif
+#if !defined(NESF_STORAGE) || NESF_STORAGE == 32
 cudaError_t launch_al(const ALArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, DevStats* stats, cudaStream_t stream) {
     return launch_al_t(a, P64, P32, prec, so, stats, stream);
 }
+#endif
 
 }  // namespace nesf

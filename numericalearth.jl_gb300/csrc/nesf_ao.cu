@@ -413,18 +413,24 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
     return cudaGetLastError();
 }
 
+// The build compiles this file once per storage type (NESF_STORAGE = 64, then 32), so the
+// two halves of the kernel instantiations compile in parallel; undefined builds both.
+#if !defined(NESF_STORAGE) || NESF_STORAGE == 64
 cudaError_t launch_ao(const AOArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
                       cudaStream_t stream) {
     return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, ws, stats, stream);
 }
+#endif
+#if !defined(NESF_STORAGE) || NESF_STORAGE == 32
 cudaError_t launch_ao(const AOArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
                       cudaStream_t stream) {
     return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, ws, stats, stream);
 }
+#endif
 
 }  // namespace nesf
 
@@ -461,9 +467,13 @@ cudaError_t launch_ao_samples(const AOArgs<S>& a, const DevIface<float>& P32, fl
     ao_samples_kernel<S><<<(unsigned)((ring + 255) / 256), 256, 0, s>>>(a, P32, feat, targ);
     return cudaGetLastError();
 }
+#if !defined(NESF_STORAGE) || NESF_STORAGE == 64
 template cudaError_t launch_ao_samples<double>(const AOArgs<double>&, const DevIface<float>&, float*, float*,
                                                cudaStream_t);
+#endif
+#if !defined(NESF_STORAGE) || NESF_STORAGE == 32
 template cudaError_t launch_ao_samples<float>(const AOArgs<float>&, const DevIface<float>&, float*, float*,
                                               cudaStream_t);
+#endif
 
 }  // namespace nesf

@@ -23,6 +23,9 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-r
 # The streaming kernels (interpolation, sea-ice-ocean fluxes, assembly) are HBM-bound:
 # without contracted multiply-adds they round exactly like the CPU restatement.
 PER_FILE_FLAGS = {"nesf_exchange.cu": ["-fmad=false"]}
+# The solve files instantiate every kernel for FP64 and FP32 storage: each is compiled
+# twice, one storage type per object, so the slowest translation unit takes half as long.
+SPLIT_BY_STORAGE = ("nesf_ao.cu", "nesf_ai.cu", "nesf_al.cu")
 
 
 def nvcc():
@@ -58,9 +61,19 @@ def build(force=False, verbose=False, jobs=None):
     exe = nvcc()
     srcs = sources()
 
-    def compile_one(src):
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
-        cmd = [exe, *ARCH, *NVCC_FLAGS, *PER_FILE_FLAGS.get(os.path.basename(src), []), "-I", INCLUDE, "-c", src, "-o", obj]
+    units = []
+    for src in srcs:
+        base = os.path.basename(src)[:-3]
+        if os.path.basename(src) in SPLIT_BY_STORAGE:
+            units += [(src, [f"-DNESF_STORAGE={b}"], f"{base}.f{b}.o") for b in (64, 32)]
+        else:
+            units.append((src, [], base + ".o"))
+
+    def compile_one(unit):
+        src, defs, name = unit
+        obj = os.path.join(BUILD, name)
+        cmd = [exe, *ARCH, *NVCC_FLAGS, *PER_FILE_FLAGS.get(os.path.basename(src), []), *defs, "-I", INCLUDE, "-c",
+               src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")
@@ -68,8 +81,10 @@ def build(force=False, verbose=False, jobs=None):
             sys.stderr.write(r.stderr)
         return obj
 
-    with ThreadPoolExecutor(max_workers=jobs or max(1, min(len(srcs), os.cpu_count() or 1))) as ex:
-        objs = list(ex.map(compile_one, srcs))
+    # slowest first, so the long units start at once when there are fewer cores than units
+    units.sort(key=lambda u: os.path.basename(u[0]) not in SPLIT_BY_STORAGE)
+    with ThreadPoolExecutor(max_workers=jobs or max(1, min(len(units), os.cpu_count() or 1))) as ex:
+        objs = list(ex.map(compile_one, units))
     tmp = LIB + ".tmp"
     cmd = [exe, *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs]
     r = subprocess.run(cmd, capture_output=True, text=True)
