@@ -552,7 +552,8 @@ def main():
             "vs_baseline": None, "dtype": {"f32": "f32+f64polish", "f32_adaptive": "f32 (f64 polish where ill-conditioned)"}.get(prec, "f64"), "data": "synthetic",
             "config": {"workload": WORKLOAD, "cells_ao": n_ao, "cells_ai": n_ai, "fields": "fp32",
                        "warm_start": model.mlp is not None,
-                       "schedule": "one thread per cell, compacted work lists, packed polish/replay passes; "
+                       "schedule": "one thread per cell (sea-ice pass 1: resident warps taking 32 work-list "
+                                   "entries at a time), compacted work lists, packed polish/replay passes; "
                                    "sea-ice and ocean solves on two lanes (the ocean solve overlaps the sea-ice "
                                    "polish/replay tail); the step replayed as one CUDA graph",
                        "l2": "working set > L2 (no flush needed)", "parallelism": f"replicas x{world}",

@@ -777,7 +777,9 @@ typedef struct {
     int32_t infer_per_sm;     /* blocks per SM of the warm-start inference pass, 1..8 (4)             */
     int32_t two_lanes;        /* coupling step: sea-ice solve on a second stream beside the ocean's (1) */
     int32_t io_overlap;       /* coupling step: sea-ice-ocean fluxes beside the sea-ice pass 1 (1)      */
-    int32_t pad_;
+    int32_t pass1_fetch;      /* pass 1 of the FP32 solvers: 1 one thread per work-list entry; 2 in the
+                                 sea-ice solve, 3 in the sea-ice and ocean solves, the resident blocks
+                                 only, each warp taking 32 entries at a time (2)                       */
     double step_ms;           /* nesf_autotune: the chosen configuration's mean step time            */
 } nesf_tuning;
 

@@ -179,13 +179,12 @@ __global__ void __launch_bounds__(128) ai_classify_kernel(AIArgs<S> a, DevIface<
     }
 }
 
-// Pass 1: the compacted ice cells, one thread each.
+// One entry of pass 1: the w-th cell of the work list.
 template <class S, int PREC, bool SKIN>
-__global__ void __launch_bounds__(128, PREC == NESF_F32_ADAPTIVE ? 5 : 1) ai_kernel(AIArgs<S> a, DevIface<double> P64, DevIface<float> P32,
-                                                 SolveOpts so, WorkList wl, ReplayQueue rq, const float* guess,
-                                                 DevStats* stats) {
+__device__ __forceinline__ void ai_cell(const AIArgs<S>& a, const DevIface<double>& P64, const DevIface<float>& P32,
+                                        const SolveOpts& so, const WorkList& wl, const ReplayQueue& rq,
+                                        const float* guess, DevStats* stats, int64_t w) {
     const int nxr = a.L.nx + 2;
-    const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int64_t r = worklist_get(wl, 0, w);
     if (r < 0) return;
     float xw[3];
@@ -254,6 +253,28 @@ __global__ void __launch_bounds__(128, PREC == NESF_F32_ADAPTIVE ? 5 : 1) ai_ker
     }
     ai_store(P, a, k, c, us, ts, qst, Ts, iters);
     if (stats) stats_add(stats, true, true, iters, nonconv, f64it > 0, f64it, false, fallback);
+}
+
+// Pass 1: the compacted ice cells, one thread each; with NESF_FETCH_SEA_ICE (FP32 solvers) the
+// resident blocks only, each warp taking the next 32 entries of the list (counter
+// rq.count[3]) until it is exhausted, as in the atmosphere-ocean pass 1.
+template <class S, int PREC, bool SKIN>
+__global__ void __launch_bounds__(128, PREC == NESF_F32_ADAPTIVE ? 5 : 1) ai_kernel(AIArgs<S> a, DevIface<double> P64, DevIface<float> P32,
+                                                 SolveOpts so, WorkList wl, ReplayQueue rq, const float* guess,
+                                                 DevStats* stats) {
+    const bool fetch = PREC != NESF_PLAIN_F64 && (so.fetch & NESF_FETCH_SEA_ICE);
+    int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (;;) {
+        if (fetch) {
+            unsigned base = 0;
+            if ((threadIdx.x & 31) == 0) base = atomicAdd(&rq.count[3], 32u);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= wl.count[0] + wl.count[1]) return;
+            w = (int64_t)base + (threadIdx.x & 31);
+        }
+        ai_cell<S, PREC, SKIN>(a, P64, P32, so, wl, rq, guess, stats, w);
+        if (!fetch) return;
+    }
 }
 
 // Pass 1b (ADAPTIVE): the cells whose FP32 result was not kept, packed, through pass
@@ -344,7 +365,8 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     const bool warm = ws.mlp != nullptr && prec != NESF_PLAIN_F64 && P64.temp_form == NESF_BULK_TEMPERATURE &&
                       P64.flux_form == NESF_FLUXES_SIMILARITY_THEORY;
     cudaError_t e = cudaMemsetAsync(wl.count, 0, sizeof(unsigned) * 2, stream);
-    if (e == cudaSuccess && prec != NESF_PLAIN_F64) e = cudaMemsetAsync(rq.count, 0, 3 * sizeof(unsigned), stream);
+    // rq.count: [0, 2] the deferred queues, [3] pass 1's fetch counter
+    if (e == cudaSuccess && prec != NESF_PLAIN_F64) e = cudaMemsetAsync(rq.count, 0, 4 * sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
     ai_classify_kernel<S><<<grid, block, 0, stream>>>(a, P64, P32, wl, warm ? ws.feat : nullptr, stats);
     trace_mark(so.tracer, "ai_classify", stream);
@@ -359,7 +381,9 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     // POLISH pass 1, which polishes every cell in place
     const bool adaptive = prec == NESF_F32_ADAPTIVE && so.fp32_rho > 0.0f;
     const bool skin = P64.temp_form != NESF_BULK_TEMPERATURE;
-#define NESF_AI_LAUNCH(PR, SK, G) ai_kernel<S, PR, SK><<<grid, block, 0, stream>>>(a, P64, P32, so, wl, rq, G, stats)
+#define NESF_AI_LAUNCH(PR, SK, G)                                                                          \
+    ai_kernel<S, PR, SK><<<pass1_grid(ai_kernel<S, PR, SK>, grid, block, sms, PR != NESF_PLAIN_F64 && (so.fetch & NESF_FETCH_SEA_ICE)), \
+                           block, 0, stream>>>(a, P64, P32, so, wl, rq, G, stats)
 #define NESF_AI_SKIN(PR, G) do { if (skin) NESF_AI_LAUNCH(PR, true, G); else NESF_AI_LAUNCH(PR, false, G); } while (0)
     if (prec == NESF_PLAIN_F64) NESF_AI_SKIN(NESF_PLAIN_F64, nullptr);
     else if (adaptive) NESF_AI_SKIN(NESF_F32_ADAPTIVE, guess);

@@ -180,28 +180,13 @@ __global__ void __launch_bounds__(128) ao_classify_kernel(AOArgs<S> a, DevIface<
     if (stats && in && land) stats_add(stats, true, false, 0, false, false, 0, false, false);
 }
 
-// Pass 1: the compacted cells (unstable first, then stable), one thread each.
-template <class S, int PREC, bool SKIN, bool ENS>
-__global__ void __launch_bounds__(128, ENS ? 4 : (PREC == NESF_F32_ADAPTIVE ? 5 : 3)) ao_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
-                                                              const DevIface<double>* __restrict__ P64s,
-                                                              const DevIface<float>* __restrict__ P32s, SolveOpts so,
-                                                              WorkList wl, ReplayQueue rq, const float* guess,
-                                                              DevStats* stats) {
+// One entry of pass 1: the w-th cell of member m's work list.
+template <class S, int PREC, bool SKIN>
+__device__ __forceinline__ void ao_cell(const AOArgs<S>& a, const DevIface<double>& Pd, const DevIface<float>& Pf,
+                                        const SolveOpts& so, const WorkList& wl, const ReplayQueue& rq,
+                                        const float* guess, DevStats* stats, int m, int64_t w) {
     const int nxr = a.L.nx + 2;
     const int64_t ring = (int64_t)nxr * (a.L.ny + 2);
-    const int m = blockIdx.y;
-    __shared__ DevIface<double> sP64;
-    __shared__ DevIface<float> sP32;
-    if (ENS) {
-        if (threadIdx.x == 0) {
-            sP64 = P64s[m];
-            sP32 = P32s[m];
-        }
-        __syncthreads();
-    }
-    const DevIface<double>& Pd = ENS ? sP64 : P64;
-    const DevIface<float>& Pf = ENS ? sP32 : P32;
-    const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int64_t r = worklist_get(wl, m, w);
     if (r < 0) return;
     int i = (int)(r % nxr), j = (int)(r / nxr);
@@ -267,6 +252,45 @@ __global__ void __launch_bounds__(128, ENS ? 4 : (PREC == NESF_F32_ADAPTIVE ? 5 
     }
     ao_store(Pd, a, k, c, false, us, ts, qst, s.Ts, iters);
     if (stats) stats_add(stats, true, true, iters, nonconv, f64it > 0, f64it, false, fallback);
+}
+
+// Pass 1: the compacted cells (unstable first, then stable), one thread each. With
+// NESF_FETCH_OCEAN (FP32 solvers, one member) the grid is the resident blocks only and each
+// warp takes the next 32 entries of the list (counter rq.count[3]) until it is
+// exhausted: a warp that finishes early starts on new cells instead of holding its
+// block's slot until the block's slowest warp is done. Each cell's arithmetic is the
+// same under both schedules.
+template <class S, int PREC, bool SKIN, bool ENS>
+__global__ void __launch_bounds__(128, ENS ? 4 : (PREC == NESF_F32_ADAPTIVE ? 5 : 3)) ao_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
+                                                              const DevIface<double>* __restrict__ P64s,
+                                                              const DevIface<float>* __restrict__ P32s, SolveOpts so,
+                                                              WorkList wl, ReplayQueue rq, const float* guess,
+                                                              DevStats* stats) {
+    const int m = blockIdx.y;
+    __shared__ DevIface<double> sP64;
+    __shared__ DevIface<float> sP32;
+    if (ENS) {
+        if (threadIdx.x == 0) {
+            sP64 = P64s[m];
+            sP32 = P32s[m];
+        }
+        __syncthreads();
+    }
+    const DevIface<double>& Pd = ENS ? sP64 : P64;
+    const DevIface<float>& Pf = ENS ? sP32 : P32;
+    const bool fetch = !ENS && PREC != NESF_PLAIN_F64 && (so.fetch & NESF_FETCH_OCEAN);
+    int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (;;) {
+        if (fetch) {
+            unsigned base = 0;
+            if ((threadIdx.x & 31) == 0) base = atomicAdd(&rq.count[3], 32u);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= wl.count[0] + wl.count[1]) return;
+            w = (int64_t)base + (threadIdx.x & 31);
+        }
+        ao_cell<S, PREC, SKIN>(a, Pd, Pf, so, wl, rq, guess, stats, m, w);
+        if (!fetch) return;
+    }
 }
 
 // Pass 1b (ADAPTIVE): the cells whose FP32 result was not kept, packed, through
@@ -368,7 +392,8 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
     float* feat = warm ? ws.feat : nullptr;
     const float* guess = warm ? ws.guess : nullptr;
     cudaError_t e = cudaMemsetAsync(wl.count, 0, sizeof(unsigned) * 2 * nm, stream);
-    if (e == cudaSuccess && prec != NESF_PLAIN_F64) e = cudaMemsetAsync(rq.count, 0, 2 * sizeof(unsigned), stream);
+    // rq.count: [0, 1] the deferred queues, [3] pass 1's fetch counter
+    if (e == cudaSuccess && prec != NESF_PLAIN_F64) e = cudaMemsetAsync(rq.count, 0, 4 * sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
     if (ens) ao_classify_kernel<S, true><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, nullptr, stats);
     else ao_classify_kernel<S, false><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, feat, stats);
@@ -380,7 +405,9 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
         trace_mark(so.tracer, "ao_warm_start_inference", stream);
     }
 #define NESF_AO_LAUNCH(PR, SK, EN) \
-    ao_kernel<S, PR, SK, EN><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, so, wl, rq, guess, stats)
+    ao_kernel<S, PR, SK, EN><<<pass1_grid(ao_kernel<S, PR, SK, EN>, grid, threads, sms,                       \
+                                          !EN && PR != NESF_PLAIN_F64 && (so.fetch & NESF_FETCH_OCEAN)),     \
+                               threads, 0, stream>>>(a, P64, P32, P64s, P32s, so, wl, rq, guess, stats)
 #define NESF_AO_ENS(PR, SK) \
     do { if (ens) NESF_AO_LAUNCH(PR, SK, true); else NESF_AO_LAUNCH(PR, SK, false); } while (0)
 #define NESF_AO_SKIN(PR) \

@@ -23,7 +23,7 @@ struct nesf_context {
     DevIface<float>* d_p32;
     int32_t capacity_members;
     uint32_t* d_replay;         // replay + polish queues of the FP32 solvers (2 x capacity)
-    unsigned int* d_replay_count;   // [3] (see ReplayQueue)
+    unsigned int* d_replay_count;   // [4]: the deferred queues [0..2], pass 1's fetch counter [3]
     int64_t replay_capacity;
     uint32_t* d_work;           // compacted work lists of the solves
     unsigned int* d_work_count; // two counters per ensemble member
@@ -81,6 +81,7 @@ static nesf_tuning default_tuning() {
     t.infer_per_sm = 4;
     t.two_lanes = 1;
     t.io_overlap = 1;
+    t.pass1_fetch = 2;
     return t;
 }
 
@@ -507,7 +508,9 @@ static SolveOpts solve_opts(const nesf_solver_options& o, const nesf_context* ct
     float rho = o.precision == NESF_F32_ADAPTIVE ? (float)(o.fp32_rho < 0.99 ? o.fp32_rho : 0.99) : 0.0f;
     const nesf_tuning t = ctx ? ctx->tuning : default_tuning();
     return SolveOpts{o.polish_maxiter, (float)o.path_tolerance, rho, (float)o.fallback_ratio,
-                     t.solve_block, t.deferred_per_sm, t.infer_per_sm, tracer_of(ctx)};
+                     t.solve_block, t.deferred_per_sm, t.infer_per_sm,
+                     (t.pass1_fetch >= 2 ? NESF_FETCH_SEA_ICE : 0) | (t.pass1_fetch == 3 ? NESF_FETCH_OCEAN : 0),
+                     tracer_of(ctx)};
 }
 
 static int check_options(const nesf_solver_options& o, const char* who) {
@@ -1715,6 +1718,8 @@ static int check_tuning(const nesf_tuning& t, const char* who) {
         return fail(NESF_ERR_ARG, "%s: infer_per_sm %d (1..8)", who, t.infer_per_sm);
     if (t.two_lanes < 0 || t.two_lanes > 1 || t.io_overlap < 0 || t.io_overlap > 1)
         return fail(NESF_ERR_ARG, "%s: two_lanes and io_overlap are 0 or 1", who);
+    if (t.pass1_fetch < 0 || t.pass1_fetch > 3)
+        return fail(NESF_ERR_ARG, "%s: pass1_fetch %d (1, 2 or 3)", who, t.pass1_fetch);
     return NESF_OK;
 }
 
@@ -1724,7 +1729,7 @@ static nesf_tuning complete_tuning(const nesf_tuning& t) {
     if (!r.solve_block) r.solve_block = d.solve_block;
     if (!r.deferred_per_sm) r.deferred_per_sm = d.deferred_per_sm;
     if (!r.infer_per_sm) r.infer_per_sm = d.infer_per_sm;
-    r.pad_ = 0;
+    if (!r.pass1_fetch) r.pass1_fetch = d.pass1_fetch;
     return r;
 }
 
@@ -1796,6 +1801,7 @@ extern "C" int nesf_autotune(nesf_context* ctx, const nesf_coupling_step_args* a
         {&nesf_tuning::solve_block, {128, 96, 64, 32}, true},
         {&nesf_tuning::deferred_per_sm, {2, 4, 8, 16}, fast},
         {&nesf_tuning::infer_per_sm, {2, 4, 8}, warm},
+        {&nesf_tuning::pass1_fetch, {2, 1, 3}, fast},
         {&nesf_tuning::two_lanes, {1, 0}, ice},
         {&nesf_tuning::io_overlap, {1, 0}, ice && a->io_params != nullptr},
     };

@@ -37,6 +37,8 @@ inline void trace_mark(const Tracer* t, const char* name, cudaStream_t s) {
 }
 
 // Knobs of the FP32 + FP64-polish solver.
+enum { NESF_FETCH_OCEAN = 1, NESF_FETCH_SEA_ICE = 2 };
+
 struct SolveOpts {
     int polish_steps;      // FP64 Newton steps
     float path_tol;        // replay threshold on the reference's stopping-error bound
@@ -45,6 +47,8 @@ struct SolveOpts {
     // launch shapes (host side; the autotuner's choice): threads per block of pass 1,
     // blocks per SM of the packed polish/replay passes and of the warm-start inference
     int block, deferred_per_sm, infer_per_sm;
+    int fetch;             // pass 1 of the FP32 solvers where resident warps take 32 work-list entries
+                           // at a time: NESF_FETCH_OCEAN | NESF_FETCH_SEA_ICE bits
     const Tracer* tracer;  // host side: kernel-boundary trace (null: off)
 };
 
@@ -70,8 +74,9 @@ struct WorkList {
 // cells to replay in FP64, part 1 the cells to polish (ADAPTIVE), part 2 (the
 // sea-ice solve's, which replays the polish pass's cells apart so that the replay
 // of pass 1's cells runs beside the polish pass) the polish pass's replays;
-// count[part] are their numbers (zeroed before the solve). A cell that the polish
-// pass sends on to a replay holds one entry in each of two parts.
+// count[part] are their numbers (zeroed before the solve), and count[3] is pass 1's
+// fetch counter (SolveOpts::fetch). A cell that the polish pass sends on to a replay
+// holds one entry in each of two parts.
 struct ReplayQueue {
     uint32_t* idx;          // linear cell ids (member * ring + ring index)
     unsigned int* count;
@@ -868,6 +873,21 @@ __device__ __forceinline__ void replay_push(const ReplayQueue& q, bool want, uin
     queue_push(q, part, want, id);
 }
 __device__ __forceinline__ void polish_push(const ReplayQueue& q, bool want, uint32_t id) { queue_push(q, 1, want, id); }
+
+// Grid of a pass-1 launch: with warp fetching, the blocks that can be resident at
+// once (at most the one-thread-per-entry grid); otherwise that grid unchanged.
+template <class K>
+inline dim3 pass1_grid(K kernel, dim3 grid, int threads, int sms, bool fetch) {
+    if (!fetch) return grid;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess || per_sm < 1) {
+        (void)cudaGetLastError();
+        per_sm = 1;
+    }
+    const unsigned g = (unsigned)sms * (unsigned)per_sm;
+    if (g < grid.x) grid.x = g;
+    return grid;
+}
 
 cudaError_t launch_ao(const AOArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,

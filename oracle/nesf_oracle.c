@@ -15,6 +15,13 @@
  *     bilinear-in-space and linear-in-time interpolation;
  *   - ClimaSeaIce.jl (compat "0.5, 0.6"): LinearLiquidus melting temperature
  *     T_m = T_fw - slope * S.
+ * Pinning: the reference is Julia and cannot run here, and its tests hold no
+ * golden flux vectors. This restatement is pinned by the known answers those
+ * tests do hold (zero fluxes, the neutral log-law closed form, gustiness bit
+ * identity, Large-Yeager stability values, the three-equation interface
+ * properties, the dry-layer and slab-land cases, e_sat at the triple point).
+ * Parity unpinned: the restated Thermodynamics.jl, Oceananigans.jl and
+ * ClimaSeaIce.jl functions above beyond those identities.
  * Build with -ffp-contract=off so that no fused multiply-add changes the
  * rounding between machines.
  */
