@@ -279,9 +279,11 @@ typedef struct {
     int32_t precision;        /* nesf_precision                                        */
     int32_t polish_maxiter;   /* FP64 Newton polish steps at most (default 3; 1-3 are
                                  used by contraction rate)                            */
-    int32_t block_size;       /* threads per block; 0 = library default                */
-    int32_t schedule;         /* 0: one thread per cell; 1: persistent lane refill      */
-    int32_t ctas_per_sm;      /* persistent schedule: CTAs per SM (0 = occupancy)       */
+    int32_t block_size;       /* reserved, ignored: the launch shapes and the pass-1
+                                 schedule are the context's tuning (nesf_set_tuning,
+                                 nesf_autotune)                                         */
+    int32_t schedule;         /* reserved, ignored (see block_size)                     */
+    int32_t ctas_per_sm;      /* reserved, ignored (see block_size)                     */
     int32_t warm_start;       /* 1: MLP initial guess (needs mlp weights)              */
     const void* mlp;          /* device pointer to packed MLP weights (nesf_mlp_*)      */
     double fallback_ratio;    /* warm start: back to the cold start when the first residual

@@ -47,6 +47,8 @@ struct AOFields
     interface_temperature::Ptr{Cvoid}; iterations::Ptr{Int32}
 end
 
+# nesf_solver_options; block_size, schedule and ctas_per_sm are reserved (the launch shapes are
+# the library context's tuning, nesf_set_tuning / nesf_autotune).
 struct SolverOptions
     precision::Int32; polish_maxiter::Int32; block_size::Int32; schedule::Int32
     ctas_per_sm::Int32; warm_start::Int32; mlp::Ptr{Cvoid}; fallback_ratio::Float64; path_tolerance::Float64

@@ -66,14 +66,13 @@ def default_context(device=None):
     return _DEFAULT_CTX[dev]
 
 
-def solver_options(precision="f64", polish_maxiter=0, block_size=128, schedule=0, mlp=None):
-    """nesf_solver_options; `mlp` (a warm.WarmStartNetwork) turns on the learned warm start."""
+def solver_options(precision="f64", polish_maxiter=0, mlp=None):
+    """nesf_solver_options; `mlp` (a warm.WarmStartNetwork) turns on the learned warm start.
+    Launch shapes are the context's tuning (set_tuning, autotune), not options of a call."""
     o = A.SolverOptions()
     load().nesf_default_solver_options(C.byref(o))
     o.precision = PRECISIONS[precision]
     o.polish_maxiter = polish_maxiter
-    o.block_size = block_size
-    o.schedule = schedule
     if mlp is not None:
         o.warm_start = 1
         o.mlp = mlp.ptr
