@@ -132,3 +132,36 @@ def test_julia_shim_humidity_offsets(tmp_path):
                                                       text=True).stdout.splitlines())
     for k, v in offsets.items():
         assert int(out[k]) == v == getattr(A.InterfaceParams, k).offset, k
+
+
+# include/nesf.h's structs in the order of nesf_struct_sizes() and of A.STRUCTS_IN_SIZE_ORDER
+C_STRUCT_NAMES = (
+    "nesf_grid", "nesf_thermodynamics_parameters", "nesf_stability_function", "nesf_roughness_length",
+    "nesf_similarity_theory_fluxes", "nesf_interface_params", "nesf_solver_options", "nesf_stats",
+    "nesf_ao_fields", "nesf_ai_fields", "nesf_io_params", "nesf_io_fields", "nesf_atmos_grid",
+    "nesf_exchange_coords", "nesf_interp_fields", "nesf_assembly_params", "nesf_assembly_fields",
+    "nesf_coupling_step_args", "nesf_integral_fields", "nesf_tuning", "nesf_trace_entry",
+    "nesf_coefficient_fluxes", "nesf_al_fields", "nesf_land_radiation_params", "nesf_land_flux_fields")
+
+
+@pytest.mark.parametrize("k", range(len(C_STRUCT_NAMES)))
+def test_struct_field_offsets_match_header(tmp_path, k):
+    """Every field of each ctypes mirror sits at offsetof() of include/nesf.h (compiled here)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    assert len(C_STRUCT_NAMES) == len(A.STRUCTS_IN_SIZE_ORDER)
+    c_name, mirror = C_STRUCT_NAMES[k], A.STRUCTS_IN_SIZE_ORDER[k]
+    names = [f[0] for f in mirror._fields_]
+    src = tmp_path / "off.c"
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "nesf.h"\nint main(void) {\n' +
+                   "".join(f'    printf("{k} %zu\\n", offsetof({c_name}, {k}));\n' for k in names) +
+                   "    return 0;\n}\n")
+    exe = tmp_path / "off"
+    subprocess.run([cc, "-I", os.path.dirname(HEADER), "-o", str(exe), str(src)], check=True)
+    out = dict(line.split() for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                      text=True).stdout.splitlines())
+    for k in names:
+        assert int(out[k]) == getattr(mirror, k).offset, (c_name, k)
