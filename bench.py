@@ -75,7 +75,7 @@ class ClockSampler:
         try:
             self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.file,
                                          stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -106,8 +106,21 @@ class ClockSampler:
         mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        hist = {}
+        for v in sm:
+            hist[str(int(v))] = hist.get(str(int(v)), 0) + 1
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows), "sm_mhz_histogram": hist,
+                "power_w_median": float(np.median([float(r[3]) for r in rows if _num(r[3])]))
+                if any(_num(r[3]) for r in rows) else None}
+
+
+def _num(x):
+    try:
+        float(x)
+        return True
+    except ValueError:
+        return False
 
 
 def measured_peaks():
@@ -195,6 +208,68 @@ def phase_times(model, precision, reps=3):
         for k, n in enumerate(names):
             acc[n] += ev[k].elapsed_time(ev[k + 1]) / reps
     return acc
+
+
+REPEAT_ROUNDS = 5
+
+# ncu pipe utilisation of the two pass-1 solve kernels (--set full, one launch each on the
+# 720 x 320 coupled case): the profile summary named here holds the command and the figures.
+NCU_PIPES = {
+    "source": "profiles/solve_kernels_f32adaptive_coupled_720x320.md",
+    "ao_kernel": {"issue_active": 0.497, "fma_pipe": 0.226, "xu_pipe": 0.070, "fp64_pipe": 0.194,
+                  "warps_active": 0.256, "lanes_active_per_warp_instruction": 21.9},
+    "ai_kernel": {"issue_active": 0.305, "fma_pipe": 0.122, "xu_pipe": 0.046, "fp64_pipe": 0.189,
+                  "warps_active": 0.129, "lanes_active_per_warp_instruction": 18.2},
+}
+
+
+def compute_roofline(work_t, work_f, t_ms, fp64_iters, clk):
+    """The compute side of the main solve kernel's roofline: the work table's rates
+    (NESF_WORK_*: transcendentals and flops of the reference's FP64 cold-start iterations)
+    against peaks DERIVED from the SM count and the sampled SM clock (FP32: 128 lanes x 2
+    flops per SM per cycle; MUFU: 16 per SM per cycle), beside the ncu pipe fractions."""
+    import torch
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz") or 2070.0
+    fp32_peak = sms * 128 * 2 * mhz * 1e6
+    mufu_peak = sms * 16 * mhz * 1e6
+    sec = t_ms / 1000.0 if t_ms else None
+    flops = work_f / sec if sec else None
+    trans = work_t / sec if sec else None
+    return {"work_transcendentals": work_t, "work_flops": work_f, "transcendentals_per_s": trans,
+            "flops_per_s": flops, "fp64_cold_start_iterations": fp64_iters,
+            "fp32_peak_flops_derived": fp32_peak, "mufu_peak_ops_derived": mufu_peak,
+            "frac_fp32_work_table": flops / fp32_peak if flops else None,
+            "frac_mufu_work_table": trans / mufu_peak if trans else None,
+            "peak_note": f"derived: {sms} SMs x 128 FP32 lanes x 2 flops (FMA) x {mhz:.0f} MHz; MUFU 16 / SM / "
+                         "cycle. The work table counts the reference's FP64 cold-start iterations, so a "
+                         "fraction above the pipes' own ncu fractions means iterations saved.",
+            "ncu_pipes": NCU_PIPES}
+
+
+def replay_round(model, steps, world):
+    """One more timed round of `steps` replays of the captured step (already warm)."""
+    import torch
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(steps):
+        model.graph_step()
+    e1.record(s)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms
 
 
 def time_steps(model, precision, steps, warmup, world):
@@ -302,6 +377,89 @@ def error_stats(model, precision):
     return res
 
 
+HEADLINE_FLUXES = ("latent_heat", "sensible_heat", "water_vapor", "x_momentum", "y_momentum")
+
+
+def step_snapshot(model, precision, row_index):
+    """One coupling step from the initial state (the captured graph of `precision`), and the
+    band rows `row_index` of every output it writes (interpolated atmosphere, the three
+    interfaces, the net fluxes), as host FP64 arrays."""
+    import torch
+    from nesf.coupled import EXCHANGE_ATMOS
+    model.capture(precision)
+    model.reset()
+    model.graph_step()
+    torch.cuda.synchronize()
+    grab = lambda t: t.index_select(0, row_index).double().cpu().numpy()
+    snap = {"ao": {k: grab(v) for k, v in model.ao.items()}, "ai": {k: grab(v) for k, v in model.ai.items()},
+            "io": {k: grab(v) for k, v in model.io.items()}, "net": {k: grab(v) for k, v in model.net.items()},
+            "io_T": {"T_oc": grab(model.x["T_oc"])}}
+    if model.atmos is not None:
+        snap["atmos"] = {k: grab(model.x[k]) for k in EXCHANGE_ATMOS.values()}
+    model.reset()
+    return snap
+
+
+def oracle_errors(model, precisions, bands=48, rows=8):
+    """Max / p99 relative error of each precision's coupling step against the FP64 oracle
+    (oracle/band.py: interpolation, the three interfaces, assembly and radiation restated on
+    the CPU) on `bands` bands of `rows` rows spread over the workload, per output. Relative
+    error = |gpu - oracle| / max(|oracle|, 1e-6 max|oracle|). Cells where the oracle's
+    atmosphere-ocean or atmosphere-sea-ice iteration stops at maxiter are excluded and counted:
+    there the reference's answer is its 100th iterate, which the warm-started path need not
+    follow. The net momentum fluxes also read the west / south neighbours' interface stress,
+    so they exclude the neighbours of such cells too."""
+    import torch
+    from oracle import band as OB
+    st = model.state
+    L = model.layout
+    h = rows + 2 * L.hy
+    pos = OB.band_positions(st, rows, bands)
+    row_index = torch.cat([torch.arange(int(p), int(p) + h) for p in pos]).cuda()
+    snaps = {p: step_snapshot(model, p, row_index) for p in precisions}
+    tables = {p: OB.ErrorTable() for p in precisions}
+    maxit = {"ao": model.ao_spec.flux_formulation.solver_stop_criteria.maxiter,
+             "ai": model.ai_spec.flux_formulation.solver_stop_criteria.maxiter}
+    excluded = 0
+    t0 = time.perf_counter()
+    for b, lo in enumerate(pos):
+        sub, ref = OB.step_band(st, int(lo), rows, model.ao_spec, model.ai_spec, model.io_spec, model.asm_spec)
+        I = sub.interior
+        stopped = (I(ref["ao"]["iterations"]) >= maxit["ao"]) | (I(ref["ai"]["iterations"]) >= maxit["ai"])
+        excluded += int(stopped.sum())
+        near = stopped.copy()
+        near[:, 1:] |= stopped[:, :-1]
+        near[1:, :] |= stopped[:-1, :]
+        keep, keep_net = ~stopped, ~near
+        for p, snap in snaps.items():
+            part = lambda a: I(a[b * h:(b + 1) * h])
+            for group in ("atmos", "ao", "ai", "io", "net"):
+                if group not in ref or group not in snap:
+                    continue
+                for k, r in ref[group].items():
+                    if k == "iterations" or k not in snap[group]:
+                        continue
+                    kk = keep_net if group == "net" else keep
+                    tables[p].add(f"{group}.{k}", part(snap[group][k]), I(r), kk)
+            tables[p].add("io.ocean_T_after_frazil", part(snap["io_T"]["T_oc"]), I(ref["io"]["T_oc"][0]), keep)
+    oracle_s = time.perf_counter() - t0
+    out = {}
+    for p, t in tables.items():
+        s = t.summary()
+        head = [s[f"{g}.{k}"] for g in ("ao", "ai") for k in HEADLINE_FLUXES if f"{g}.{k}" in s]
+        out[p] = {"max_headline_fluxes": max(x["max"] for x in head),
+                  "p99_headline_fluxes": max(x["p99"] for x in head), "per_output": s}
+    out["sample"] = (f"{len(pos)} bands of {rows} rows x {L.nx} cells spread over the domain; "
+                     f"{excluded} cells where the oracle stops at maxiter excluded; oracle {oracle_s:.1f} s "
+                     f"on {_oracle_threads()} threads")
+    return out
+
+
+def _oracle_threads():
+    from oracle import oracle
+    return oracle.get_threads()
+
+
 def e2e_step_time(model, precision, steps, warmup):
     """Same step through the public API with host buffers: pinned H2D of the step's inputs
     (ocean and sea-ice surface state + the two atmosphere snapshots) into the model's
@@ -406,11 +564,12 @@ def e2e_pipelined_step_time(models, precision, steps, warmup):
 
 def cpu_baseline(state, target_s=12.0):
     """The oracle (C restatement, OpenMP over all host threads) on bands of rows of the same
-    workload: interpolation of the prescribed atmosphere onto the band, then the
-    atmosphere-ocean and atmosphere-sea-ice solves; returns solved cells/s and the sample."""
-    from nesf import api
+    workload, every phase of the GPU step (oracle/band.py): interpolation of the prescribed
+    atmosphere onto the band, the atmosphere-ocean, atmosphere-sea-ice and sea-ice-ocean
+    fluxes, the net ocean and sea-ice assembly with radiation; returns solved cells/s (the
+    GPU step's unit) and the sample."""
     from nesf import params as P
-    from nesf import synthetic as syn
+    from oracle import band as OB
     from oracle import oracle
     L = state.layout
     f = state.fields
@@ -419,40 +578,28 @@ def cpu_baseline(state, target_s=12.0):
     done_cells = 0
     elapsed = 0.0
     hist = {}
-    ao = P.atmosphere_ocean_interface_spec().to_c()
-    ai = P.atmosphere_sea_ice_interface_spec().to_c()
-    sub = syn.Layout(L.nx, rows, L.hx, L.hy)
-    height = rows + 2 * L.hy
-    positions = np.linspace(0, L.shape[0] - height, 97).astype(int)
-    atmos = state.atmos
+    specs = dict(ao_spec=P.atmosphere_ocean_interface_spec(), ai_spec=P.atmosphere_sea_ice_interface_spec(),
+                 io_spec=P.SeaIceOceanSpec(), asm_spec=P.AssemblySpec())
+    positions = OB.band_positions(state, rows, 97)
     bands = 0
     while elapsed < target_s and bands < 10 * len(positions):
         lo = int(positions[bands % len(positions)])
-        band = {k: np.ascontiguousarray(v[lo:lo + height].astype(np.float64) if v.dtype != np.uint8
-                                        else v[lo:lo + height]) for k, v in f.items() if v.ndim == 2}
         t0 = time.perf_counter()
-        if "u_atm" not in band:
-            c = state.coords
-            bc = api.exchange_coords(syn.LonLat(c.lon0, c.dlon, c.lat0 + lo * c.dlat, c.dlat))
-            out = oracle.interpolate(sub, bc, api.atmos_grid_struct(atmos), atmos["arrays"], atmos["time_weight"])
-            for n, k in (("u", "u_atm"), ("v", "v_atm"), ("T", "T_atm"), ("q", "q_atm"), ("p", "p_atm"),
-                         ("sw", "sw_down"), ("lw", "lw_down")):
-                band[k] = out[n]
-        ro = oracle.ao_fluxes(ao, sub, band)
-        ri = oracle.ai_fluxes(ai, sub, band, band["ice_temperature"])
+        sub, res = OB.step_band(state, lo, rows, **specs)
         elapsed += time.perf_counter() - t0
-        water = sub.interior(band["inactive"]) == 0
-        ice = sub.interior(band["ice_concentration"]) > 0
+        water = sub.interior(OB.band_of(f["inactive"], state, lo, rows)) == 0
+        ice = sub.interior(OB.band_of(f["ice_concentration"], state, lo, rows)) > 0
         done_cells += int(water.sum() + (water & ice).sum())
-        for name, its, sel in (("ao", ro["iterations"], water), ("ai", ri["iterations"], water & ice)):
+        for name, sel in (("ao", water), ("ai", water & ice)):
             h = hist.setdefault(name, np.zeros(len(ITER_BINS) - 1, dtype=np.int64))
-            h += np.histogram(sub.interior(its)[sel], bins=ITER_BINS)[0]
+            h += np.histogram(sub.interior(res[name]["iterations"])[sel], bins=ITER_BINS)[0]
         bands += 1
     return {"value": done_cells / elapsed, "unit": "flux cells/s", "cores": threads, "kind": "port",
             "nproc": os.cpu_count(), "cpu_model": cpu_model(),
             "iteration_histogram": {"bins": ITER_BINS.tolist(), **{k: v.tolist() for k, v in hist.items()}},
             "sample": f"{bands} bands of {rows} rows x {L.nx} cells spread over the domain ({done_cells} "
-                      f"solved cells): interpolation + AO + AI solves, {elapsed:.1f} s of CPU work"}
+                      f"solved cells): the whole step (interpolation, AO + AI + IO fluxes, assembly and "
+                      f"radiation), {elapsed:.1f} s of CPU work"}
 
 
 ITER_BINS = np.array([1, 3, 5, 8, 12, 16, 20, 30, 50, 100, 101])
@@ -530,9 +677,11 @@ def main():
     # launch shapes and schedule from the autotuner (nesf_autotune), on this workload
     tuning = model.autotune(prec, reps=3) if not args.no_autotune else None
 
-    # warm-up both solvers, then the timed region (fast path) with clock sampling
+    # warm-up, then the timed region (fast path: exactly `steps` replays, the headline), then
+    # REPEAT_ROUNDS - 1 more rounds of `steps` replays for the spread; clocks sampled throughout
     with ClockSampler(local) as clocks:
         ms, launches = time_steps(model, prec, args.steps, args.warmup, world)
+        rounds = [ms] + [replay_round(model, args.steps, world) for _ in range(REPEAT_ROUNDS - 1)]
     clk = clocks.summary()
     if args.no_plain:
         print(json.dumps({"metric": METRIC, "value": cells * world / (ms / 1000.0), "unit": "flux cells/s",
@@ -560,6 +709,10 @@ def main():
                        "tuning": tuning},
             "gpu_launches": launches,
             "clocks": clk,
+            "repeat_rounds": {"rounds": len(rounds), "steps_per_round": args.steps,
+                              "ms_per_step": [round(x, 4) for x in rounds], "median": float(np.median(rounds)),
+                              "min": min(rounds), "max": max(rounds),
+                              "note": "the headline ms_per_step is the first round"},
             "plain_f64": {"value": cells * world / (ms_plain / 1000.0), "ms_per_step": ms_plain,
                           "phases_ms": phases_plain},
             "f32_polish_ms_per_step": ms_polish,
@@ -585,6 +738,9 @@ def main():
         line["iterations_per_cell"] = {"ao": per(s_ao), "ao_cold": per(c_ao), "ai": per(s_ai), "ai_cold": per(c_ai),
                                        "ao_plain": per(p_ao), "ai_plain": per(p_ai)}
         line["errors_vs_plain_f64"] = error_stats(model, prec)
+        ev = oracle_errors(model, [prec, "f64"])
+        line["errors_vs_oracle"] = {"fast": ev[prec], "plain_f64": ev["f64"], "sample": ev["sample"]}
+        line["max_rel_err_vs_oracle"] = ev[prec]["max_headline_fluxes"]
         # roofline of the main solve kernel, the atmosphere-ocean pass 1 (ao_kernel), timed with
         # trace events on its stream inside graph replays. It is bound by the latency of its
         # FP32 (and FP64 anchor) arithmetic, not by HBM: the HBM fraction is small, and the
@@ -605,10 +761,7 @@ def main():
                             "algorithmic_bytes": alg, "kernel_ms": t_ao, "peak_source": kind,
                             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch "
                                               "on the 720x320 case, scaled by cells",
-                            "compute": {"work_transcendentals": work_t, "work_flops": work_f,
-                                        "transcendentals_per_s": work_t / (t_ao / 1000.0) if t_ao else None,
-                                        "flops_per_s": work_f / (t_ao / 1000.0) if t_ao else None,
-                                        "fp64_cold_start_iterations": it_ao}}
+                            "compute": compute_roofline(work_t, work_f, t_ao, it_ao, clk)}
         if not args.no_e2e:
             ms_ser, h2d, d2h = e2e_step_time(model, prec, max(3, args.steps // 2), 1)
             twin = CoupledModel(state)                 # the second slot of the double buffer

@@ -610,10 +610,19 @@ int nesf_compute_atmosphere_ocean_fluxes_ensemble(nesf_context* ctx, const nesf_
  * counterpart in the reference. Its scratch is a fixed 24 MiB array in the
  * library, shared by every call: grids of more than 2,097,152 cells (halo ring
  * (nx+2) x (ny+2)) are rejected with NESF_ERR_CAPACITY; calls that overlap on the
- * GPU race on the scratch. The first call on a device sets up the scratch address
- * (make it before any stream capture). No statistics. */
+ * GPU race on the scratch. The device must have been prepared with
+ * nesf_noalloc_prepare (else NESF_ERR_ARG). No warm start (NESF_ERR_ARG if
+ * requested), no statistics; the context's tuning is not used (default launch
+ * shapes). */
 int nesf_compute_atmosphere_ocean_fluxes_noalloc(const nesf_interface_params* params, const nesf_ao_fields* fields,
                                                  const nesf_solver_options* opts, void* stream);
+/* Set-up of the allocation-free solve on `device`, once, at the caller's set-up:
+ * it loads the library's module holding the 24 MiB scratch array (under lazy
+ * module loading a device reserves that memory only then) and every kernel the
+ * solve can launch, and resolves the array's device address. Call it before the
+ * host's memory pool reserves the device and before any stream capture; the
+ * device holds the array until the process exits. No counterpart in the reference. */
+int nesf_noalloc_prepare(int32_t device);
 
 /* compute_atmosphere_sea_ice_fluxes! (atmosphere_sea_ice_fluxes.jl:18-62) */
 int nesf_compute_atmosphere_sea_ice_fluxes(nesf_context* ctx, const nesf_interface_params* params,
@@ -671,6 +680,10 @@ int nesf_area_integrals(nesf_context* ctx, const nesf_integral_fields* fields, d
  * three operand arrangements it uses (BF16 in, FP32 out; a, b, d device memory,
  * row-major): which = 0: d[128x64] = a[128x64] b[64x64]^T; which = 1:
  * d[128x64] = a[128x64] b[64x64]; which = 2: d[128x16] = a[128x128]^T b[128x16].
+ * which = 3 checks the failure path instead: no MMA is issued, so the kernel's
+ * bounded wait on its mbarrier gives up after 64 polls, records the error, frees
+ * its TMEM and returns; the call returns NESF_ERR_TIMEOUT and the context stays
+ * usable (d is not written).
  * Synchronises the stream; NESF_ERR_TIMEOUT if the MMA did not complete. */
 int nesf_mlp_selftest(const void* a, const void* b, float* d, int32_t which, void* stream);
 

@@ -440,6 +440,24 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
     return cudaGetLastError();
 }
 
+template <class S>
+static cudaError_t preload_ao_t() {
+    const void* kernels[] = {
+        (const void*)ao_classify_kernel<S, false>,
+        (const void*)ao_kernel<S, NESF_PLAIN_F64, false, false>, (const void*)ao_kernel<S, NESF_PLAIN_F64, true, false>,
+        (const void*)ao_kernel<S, NESF_F32_POLISH, false, false>, (const void*)ao_kernel<S, NESF_F32_POLISH, true, false>,
+        (const void*)ao_kernel<S, NESF_F32_ADAPTIVE, false, false>,
+        (const void*)ao_kernel<S, NESF_F32_ADAPTIVE, true, false>,
+        (const void*)ao_polish_kernel<S, false>, (const void*)ao_polish_kernel<S, true>,
+        (const void*)ao_replay_kernel<S, false>, (const void*)ao_replay_kernel<S, true>};
+    for (const void* k : kernels) {
+        cudaFuncAttributes fa;
+        cudaError_t e = cudaFuncGetAttributes(&fa, k);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 // The build compiles this file once per storage type (NESF_STORAGE = 64, then 32), so the
 // two halves of the kernel instantiations compile in parallel; undefined builds both.
 #if !defined(NESF_STORAGE) || NESF_STORAGE == 64
@@ -449,6 +467,7 @@ cudaError_t launch_ao(const AOArgs<double>& a, const DevIface<double>& P64, cons
                       cudaStream_t stream) {
     return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, ws, stats, stream);
 }
+cudaError_t preload_ao_kernels(const AOArgs<double>*) { return preload_ao_t<double>(); }
 #endif
 #if !defined(NESF_STORAGE) || NESF_STORAGE == 32
 cudaError_t launch_ao(const AOArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32,
@@ -457,6 +476,7 @@ cudaError_t launch_ao(const AOArgs<float>& a, const DevIface<double>& P64, const
                       cudaStream_t stream) {
     return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, ws, stats, stream);
 }
+cudaError_t preload_ao_kernels(const AOArgs<float>*) { return preload_ao_t<float>(); }
 #endif
 
 }  // namespace nesf

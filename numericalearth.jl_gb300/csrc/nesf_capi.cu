@@ -1207,31 +1207,37 @@ extern "C" int nesf_apply_air_land_radiative_fluxes(const nesf_land_radiation_pa
 // budget that must not enter the driver's allocator. For them,
 // nesf_compute_atmosphere_ocean_fluxes_noalloc runs the atmosphere-ocean solve
 // without allocating anything: its scratch -- the compacted work list, the queues
-// of cells to replay and to polish, and their counters -- is this file-scope array,
-// which every GPU that loads the library holds until the process exits: 64
-// counters (256 B) + three lists of NESF_NOALLOC_MAX_CELLS uint32 entries, 24 MiB
-// + 256 B in all.
+// of cells to replay and to polish, and their counters -- is this file-scope array:
+// 64 counters (256 B) + three lists of NESF_NOALLOC_MAX_CELLS uint32 entries, 24 MiB
+// + 256 B in all. Under lazy module loading (the CUDA default) a device holds the
+// array from the moment this file's module is loaded on it, which
+// nesf_noalloc_prepare does; from then until the process exits.
 #define NESF_NOALLOC_MAX_CELLS (1 << 21)
 static __device__ __align__(256) uint32_t g_noalloc_scratch[64 + 3 * (size_t)NESF_NOALLOC_MAX_CELLS];
 
-static uint32_t* g_noalloc_ptr[64];   // device address of the array, per device
+static uint32_t* g_noalloc_ptr[64];   // device address of the array, per prepared device
 static std::mutex g_noalloc_lock;
 
-// Set-up, once per device, with that device current: the array's device address.
-// In host code the symbol names a host-side stand-in, not device memory, so only
-// this address may be handed to a kernel.
-static int noalloc_scratch(uint32_t** out) {
-    int dev = 0;
-    NESF_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 64) return fail(NESF_ERR_ARG, "nesf_compute_atmosphere_ocean_fluxes_noalloc: device %d", dev);
+// Set-up, once per device, with that device current: the array's device address
+// (in host code the symbol names a host-side stand-in, not device memory, so only
+// this address may be handed to a kernel), and every kernel the entry point can
+// launch loaded, so that its calls load no module (loading one allocates).
+extern "C" int nesf_noalloc_prepare(int32_t device) {
+    const char* who = "nesf_noalloc_prepare";
+    int n = 0;
+    NESF_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n || device >= 64) return fail(NESF_ERR_ARG, "%s: device %d of %d", who, device, n);
     std::lock_guard<std::mutex> lk(g_noalloc_lock);
-    if (!g_noalloc_ptr[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
-        g_noalloc_ptr[dev] = (uint32_t*)p;
-    }
-    *out = g_noalloc_ptr[dev];
+    if (g_noalloc_ptr[device]) return NESF_OK;
+    DeviceGuard g(device);
+    if (!g.ok) return fail(NESF_ERR_CUDA, "%s: cannot make device %d current", who, device);
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
+    if ((e = preload_ao_kernels((const AOArgs<double>*)nullptr)) != cudaSuccess ||
+        (e = preload_ao_kernels((const AOArgs<float>*)nullptr)) != cudaSuccess)
+        return cuda_fail(e, "nesf_noalloc_prepare: loading the solve kernels");
+    g_noalloc_ptr[device] = (uint32_t*)p;
     return NESF_OK;
 }
 
@@ -1244,15 +1250,25 @@ extern "C" int nesf_compute_atmosphere_ocean_fluxes_noalloc(const nesf_interface
     if ((r = check_ao_fields(f, params, who))) return r;
     nesf_solver_options o = options_or_default(opts);
     if ((r = check_options(o, who))) return r;
+    if (o.warm_start) return fail(NESF_ERR_ARG, "%s: no warm start (its buffers would be allocated)", who);
     int64_t ring = (int64_t)(f->grid.nx + 2) * (f->grid.ny + 2);
     if (ring > NESF_NOALLOC_MAX_CELLS)
         return fail(NESF_ERR_CAPACITY,
                     "%s: %lld cells (halo ring included) exceed the fixed scratch of %d cells; "
                     "use nesf_compute_atmosphere_ocean_fluxes", who, (long long)ring, NESF_NOALLOC_MAX_CELLS);
+    int dev = 0;
+    NESF_CUDA(cudaGetDevice(&dev));
     uint32_t* base = nullptr;
-    if ((r = noalloc_scratch(&base))) return r;
-    // counters: [0, 1] work list (unstable, stable), [2, 3] replay and polish
-    // queues; the launch clears them before the first pass reads them
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_lock);
+        if (dev >= 0 && dev < 64) base = g_noalloc_ptr[dev];
+    }
+    if (!base) return fail(NESF_ERR_ARG, "%s: device %d not prepared (call nesf_noalloc_prepare(%d) at set-up)", who,
+                            dev, dev);
+    // counters: base[0..1] the work list's counts (unstable, stable); base[2..5] the
+    // queue counters rq.count[0..3] (replays, polishes, the sea-ice solve's polish
+    // replays (unused here), pass 1's fetch counter); the launch clears the counters a
+    // precision uses before its first pass reads them
     WorkList wl{base + 64, base, ring};
     ReplayQueue rq{base + 64 + NESF_NOALLOC_MAX_CELLS, base + 2, NESF_NOALLOC_MAX_CELLS};
     DevIface<double> P64 = make_dev_iface<double>(*params);
@@ -1278,7 +1294,7 @@ cudaError_t launch_tc_selftest(const void* A, const void* B, float* D, int which
 extern "C" int nesf_mlp_selftest(const void* a, const void* b, float* d, int32_t which, void* stream) {
     const char* who = "nesf_mlp_selftest";
     if (!a || !b || !d) return fail(NESF_ERR_ARG, "%s: null argument", who);
-    if (which < 0 || which > 2) return fail(NESF_ERR_ARG, "%s: which = %d", who, which);
+    if (which < 0 || which > 3) return fail(NESF_ERR_ARG, "%s: which = %d", who, which);
     unsigned int* st = nullptr;
     NESF_CUDA(cudaMalloc(&st, sizeof(unsigned int)));
     cudaStream_t s = (cudaStream_t)stream;

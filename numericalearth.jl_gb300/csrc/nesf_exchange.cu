@@ -14,6 +14,50 @@
 namespace nesf {
 
 // ------------------------------------------------------------- sea ice - ocean
+// The interface heat flux, temperature and salinity of one cell in arithmetic R
+// (sea_ice_ocean_fluxes.jl:183-205): the bulk formulation, or the three-equation
+// interface conditions (solve_interface_conditions,
+// sea_ice_ocean_heat_flux_formulations.jl:280-313) with the MITgcm root choice.
+template <class R, class S>
+__device__ __forceinline__ void io_interface(const IOArgs<S>& a, const nesf_io_params& p, int64_t k2, R TN, R SN,
+                                             S& Qio_out, S& Tb_out, S& Sb_out) {
+    const R rho = R(p.ocean_reference_density), cpo = R(p.ocean_heat_capacity);
+    const R Tfw = R(p.liquidus_freshwater_melting_temperature), slope = R(p.liquidus_slope);
+    R Si = ldr<R>(a.Si, k2), h = ldr<R>(a.hi, k2), aleph = ldr<R>(a.aleph, k2), hc = ldr<R>(a.hc, k2);
+    R Tsi = (p.conductive && a.Tint) ? ldr<R>(a.Tint, k2) : R(0);
+    if (p.formulation == 1) {
+        R Tm = Tfw - slope * SN;
+        Qio_out = S(rho * cpo * R(p.heat_transfer_coefficient) * R(p.friction_velocity) * (TN - Tm) * aleph);
+        Tb_out = S(Tm);
+        Sb_out = S(SN);
+        return;
+    }
+    R E = R(p.reference_latent_heat);
+    R kap = R(0), Ti = R(0);
+    if (p.conductive) {
+        kap = h >= hc ? R(p.ice_conductivity) / (h * E) : R(0);
+        Ti = Tsi;
+    }
+    R l1 = -slope, l2 = Tfw;
+    R us = R(p.friction_velocity);
+    R eta = rho * cpo * R(p.heat_transfer_coefficient) * us / E;
+    R gam = rho * R(p.salt_transfer_coefficient) * us;
+    R th = eta + kap;
+    R qa = th * l1;
+    R qb = -gam - eta * TN - kap * Ti + th * (l2 - l1 * Si);
+    R qc = gam * SN + (eta * TN + kap * Ti - th * l2) * Si;
+    R xi = qa == R(0) ? R(0) : R(1) / (R(2) * qa);
+    R D = M<R>::fmax(qb * qb - R(4) * qa * qc, R(0));   // Julia max
+    R sD = M<R>::sqrt(D);
+    R Ss = (-qb - sD) * xi;
+    Ss = Ss < R(0) ? (-qb + sD) * xi : Ss;
+    R Ts = l2 - slope * Ss;
+    R q = eta * (TN - Ts) + kap * (Ti - Ts);
+    Qio_out = S(E * q * aleph);
+    Tb_out = S(Ts);
+    Sb_out = S(Ss);
+}
+
 // Arithmetic in the storage type S, like the streaming kernels: FP64 fields as the
 // reference's Float64 kernels (bit-identical to the oracle), FP32 fields as its
 // Float32 ones. PART 0: the whole computation. PART 1: the fluxes alone, from the
@@ -33,6 +77,7 @@ __global__ void __launch_bounds__(256) io_kernel(IOArgs<S> a, nesf_io_params p) 
     const R Tfw = R(p.liquidus_freshwater_melting_temperature), slope = R(p.liquidus_slope);
     // Part 1: frazil over the column, top level first (sea_ice_ocean_fluxes.jl:153-181)
     R dQ = R(0), TN = R(0);
+    bool top_frozen = false;
     for (int kk = p.nz; kk >= 1; kk--) {
         int64_t k3 = k2 + (int64_t)(kk - 1) * p.stride_k;
         R Tk = a.T3[k3], Sk = a.S3[k3];
@@ -43,50 +88,35 @@ __global__ void __launch_bounds__(256) io_kernel(IOArgs<S> a, nesf_io_params p) 
         R dz = R(a.dz[kk - 1]);
         R dE = (freezing ? R(1) : R(0)) * rho * cpo * (Tm - Tk);
         dQ -= dE * dz / R(p.dt);
-        if (kk == p.nz) TN = freezing ? Tm : Tk;   // the top level after the adjustment
+        if (kk == p.nz) {                         // the top level after the adjustment
+            TN = freezing ? Tm : Tk;
+            top_frozen = freezing;
+        }
     }
     if (PART == 2) return;
     st(a.frazil, k2, dQ);
     int64_t kN = k2 + (int64_t)(p.nz - 1) * p.stride_k;
     R SN = a.S3[kN];
-    R Si = ldr<R>(a.Si, k2), h = ldr<R>(a.hi, k2), aleph = ldr<R>(a.aleph, k2), hc = ldr<R>(a.hc, k2);
-    R Tsi = (p.conductive && a.Tint) ? ldr<R>(a.Tint, k2) : R(0);
+    R aleph = ldr<R>(a.aleph, k2);
     R Qio, Tb, Sb;
-    if (p.formulation == 1) {
-        R Tm = Tfw - slope * SN;
-        Qio = rho * cpo * R(p.heat_transfer_coefficient) * R(p.friction_velocity) * (TN - Tm) * aleph;
-        Tb = Tm;
-        Sb = SN;
+    // FP32 fields: where the ice covers part of the cell, the interface heat
+    // eta (T_N - T_b) + kappa (T_i - T_b) cancels near the melting point and would
+    // multiply FP32's rounding of S_b by |T_b| / |T_N - T_b|; the interface
+    // conditions are solved in FP64 there, from the FP32 inputs (exact in FP64),
+    // with a frozen top level at its melting point T_m(S_N) in FP64.
+    if (sizeof(S) < sizeof(double) && aleph > R(0)) {
+        double SN64 = (double)SN;
+        double TN64 = top_frozen ? p.liquidus_freshwater_melting_temperature - p.liquidus_slope * SN64 : (double)TN;
+        io_interface<double>(a, p, k2, TN64, SN64, Qio, Tb, Sb);
     } else {
-        // solve_interface_conditions (sea_ice_ocean_heat_flux_formulations.jl:280-313)
-        R E = R(p.reference_latent_heat);
-        R kap = R(0), Ti = R(0);
-        if (p.conductive) {
-            kap = h >= hc ? R(p.ice_conductivity) / (h * E) : R(0);
-            Ti = Tsi;
-        }
-        R l1 = -slope, l2 = Tfw;
-        R us = R(p.friction_velocity);
-        R eta = rho * cpo * R(p.heat_transfer_coefficient) * us / E;
-        R gam = rho * R(p.salt_transfer_coefficient) * us;
-        R th = eta + kap;
-        R qa = th * l1;
-        R qb = -gam - eta * TN - kap * Ti + th * (l2 - l1 * Si);
-        R qc = gam * SN + (eta * TN + kap * Ti - th * l2) * Si;
-        R xi = qa == R(0) ? R(0) : R(1) / (R(2) * qa);
-        R D = M<R>::fmax(qb * qb - R(4) * qa * qc, R(0));   // Julia max
-        R sD = M<R>::sqrt(D);
-        R Ss = (-qb - sD) * xi;
-        Ss = Ss < R(0) ? (-qb + sD) * xi : Ss;
-        R Ts = l2 - slope * Ss;
-        R q = eta * (TN - Ts) + kap * (Ti - Ts);
-        Qio = E * q * aleph;
-        Tb = Ts;
-        Sb = Ss;
+        io_interface<R>(a, p, k2, TN, SN, Qio, Tb, Sb);
+    }
+    if (p.formulation != 1) {
         st(a.Tb, k2, Tb);
         st(a.Sb, k2, Sb);
     }
     st(a.Qio, k2, Qio);
+    R Si = ldr<R>(a.Si, k2);
     R Ei = ldzr<R>(a.Ei, k2), Es = ldzr<R>(a.Es, k2);
     st(a.Jw, k2, -(Ei + Es) / rho);
     st(a.Js, k2, Ei * Si / rho);

@@ -28,6 +28,12 @@ __device__ __forceinline__ void to_blocked(const __nv_bfloat16* __restrict__ g, 
 }
 
 // D = A x B^T (case 0), A x B (case 1), A^T x B (case 2); see nesf_mlp_selftest.
+// Case 3 checks the failure path of the bounded wait: no MMA is issued and nothing
+// arrives on the mbarrier, so the wait gives up after kTimeoutCheckPolls polls, the
+// status word records the error and the kernel frees its TMEM (nothing is in
+// flight) and returns.
+constexpr int kTimeoutCheckPolls = 64;
+
 __global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const __nv_bfloat16* __restrict__ A,
                                                              const __nv_bfloat16* __restrict__ B, float* __restrict__ D,
                                                              int which, TcStatus* status) {
@@ -47,6 +53,9 @@ __global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const __nv_bfloat16
     } else if (which == 1) {   // A [128 x 64] K-major, B [64 (K) x 64 (N)]: N contiguous
         RA = 128; RB = 64; to_blocked(A, sa, 128, 64); to_blocked(B, sb, 64, 64);
         N = 64; ksteps = 4; a_kcol = true; b_kcol = false;
+    } else if (which == 3) {   // the wait-timeout check: no operands
+        RA = 128; RB = 64;
+        N = 64; ksteps = 4; a_kcol = true; b_kcol = true;
     } else {                   // A [128 (K) x 128 (M)], B [128 (K) x 16 (N)]: both MN-major
         RA = 128; RB = 128; to_blocked(A, sa, 128, 128); to_blocked(B, sb, 128, 16);
         N = 16; ksteps = 8; a_kcol = false; b_kcol = false;
@@ -62,16 +71,18 @@ __global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const __nv_bfloat16
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tbase = tslot;
-    if (threadIdx.x == 0) {
+    const bool issue = which != 3;
+    if (threadIdx.x == 0 && issue) {
         uint32_t id = tc::idesc_bf16(128, N, a_mn, b_mn);
         tc::mma_chain(tbase, tc::smem_addr(sa), a_lbo, a_sbo, a_step, tc::smem_addr(sb), b_lbo, b_sbo, b_step, id,
                       ksteps, false);
         tc::mma_commit(&bar);
     }
-    bool ok = __all_sync(0xffffffffu, tc::mbar_wait(&bar, 0));   // warp-uniform: tcgen05.ld is .aligned
+    const int limit = issue ? tc::kSpinLimit : kTimeoutCheckPolls;
+    bool ok = __all_sync(0xffffffffu, tc::mbar_wait(&bar, 0, limit));   // warp-uniform: tcgen05.ld is .aligned
     if (!ok) {
         if (lane == 0) atomicExch(&status->error, 1u);
-        tc::mbar_wait(&bar, 0);   // give the MMA a second bounded chance to drain before TMEM is freed
+        tc::mbar_wait(&bar, 0, limit);   // give the MMA a second bounded chance to drain before TMEM is freed
     }
     tc::fence_after_sync();
     if (ok) {

@@ -897,6 +897,10 @@ cudaError_t launch_ao(const AOArgs<float>& a, const DevIface<double>& P64, const
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
                       cudaStream_t stream);
+// Loads (under lazy module loading) every kernel that the one-member atmosphere-ocean
+// solve of storage S can launch, so that a later launch loads no module.
+cudaError_t preload_ao_kernels(const AOArgs<double>*);
+cudaError_t preload_ao_kernels(const AOArgs<float>*);
 // after_solve (optional): recorded once the pass-1 solve is enqueued.
 // tail (optional): a second stream on which pass 1's replays run beside the polish pass.
 cudaError_t launch_ai(const AIArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,

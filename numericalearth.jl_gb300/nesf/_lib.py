@@ -43,6 +43,7 @@ SIGNATURES = {
                   P(A.Stats), vp]),
     "nesf_compute_atmosphere_ocean_fluxes_noalloc": (
         C.c_int, [P(A.InterfaceParams), P(A.AOFields), P(A.SolverOptions), vp]),
+    "nesf_noalloc_prepare": (C.c_int, [C.c_int32]),
     "nesf_compute_atmosphere_sea_ice_fluxes": (
         C.c_int, [vp, P(A.InterfaceParams), P(A.AIFields), P(A.SolverOptions), P(A.Stats), vp]),
     "nesf_compute_atmosphere_land_fluxes": (

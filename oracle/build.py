@@ -29,7 +29,7 @@ def build(force=False):
     if cc is None:
         raise RuntimeError("no C compiler for the oracle")
     tmp = LIB + ".tmp"
-    cmd = [cc, "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared", "-o", tmp, *SRC, "-lm"]
+    cmd = [cc, "-O3", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared", "-o", tmp, *SRC, "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stderr}")

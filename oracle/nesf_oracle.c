@@ -627,7 +627,7 @@ int oracle_ao_fluxes(const nesf_interface_params* p, const nesf_ao_fields* f) {
     const nesf_thermodynamics_parameters* t = &p->thermo;
     int nth = oracle_get_threads();
     (void)nth;
-#pragma omp parallel for schedule(dynamic, 1) num_threads(nth)
+#pragma omp parallel for collapse(2) schedule(dynamic, 128) num_threads(nth)
     for (int j = 0; j <= g->ny + 1; j++) {
         for (int i = 0; i <= g->nx + 1; i++) {
             int64_t k = idx2(g, i, j);
@@ -697,7 +697,7 @@ int oracle_al_fluxes(const nesf_interface_params* p, const nesf_al_fields* f) {
     const nesf_grid* g = &f->grid;
     const nesf_thermodynamics_parameters* t = &p->thermo;
     int nth = oracle_get_threads();
-#pragma omp parallel for schedule(dynamic, 1) num_threads(nth)
+#pragma omp parallel for collapse(2) schedule(dynamic, 128) num_threads(nth)
     for (int j = 1; j <= g->ny; j++) {
         for (int i = 1; i <= g->nx; i++) {
             int64_t k = idx2(g, i, j);
@@ -743,7 +743,7 @@ int oracle_ai_fluxes(const nesf_interface_params* p, const nesf_ai_fields* f) {
     const nesf_thermodynamics_parameters* t = &p->thermo;
     int nth = oracle_get_threads();
     (void)nth;
-#pragma omp parallel for schedule(dynamic, 1) num_threads(nth)
+#pragma omp parallel for collapse(2) schedule(dynamic, 128) num_threads(nth)
     for (int j = 0; j <= g->ny + 1; j++) {
         for (int i = 0; i <= g->nx + 1; i++) {
             int64_t k = idx2(g, i, j);

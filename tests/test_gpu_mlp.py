@@ -34,6 +34,27 @@ def test_tcgen05_gemm_layouts(which):
     assert err < 1e-5, (which, err)
 
 
+def test_tcgen05_wait_timeout_is_reported_and_the_context_survives():
+    """The failure path of the tensor-core kernels' bounded mbarrier waits, without a
+    fault: in self-test mode 3 no MMA is issued and nothing arrives on the barrier, so
+    the wait gives up after a short limit; the kernel records the error, frees its TMEM
+    and returns, the call reports NESF_ERR_TIMEOUT, and a GEMM afterwards on the same
+    context is still correct."""
+    import torch
+    from nesf import _abi as A
+    lib = _lib.load()
+    a = torch.zeros((128, 64), dtype=torch.bfloat16, device="cuda")
+    b = torch.zeros((64, 64), dtype=torch.bfloat16, device="cuda")
+    d = torch.full((128, 64), 7.0, dtype=torch.float32, device="cuda")
+    code = lib.nesf_mlp_selftest(C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()), C.c_void_p(d.data_ptr()), 3,
+                                 None)
+    assert code == A.NESF_ERR_TIMEOUT, (code, lib.nesf_last_error())
+    assert b"did not complete" in lib.nesf_last_error()
+    assert torch.all(d == 7.0)          # no result was read out of TMEM
+    torch.cuda.synchronize()            # the context is intact
+    test_tcgen05_gemm_layouts(0)
+
+
 def _samples(rng, n):
     """Features in the ranges the solver produces and targets with masks."""
     x = np.zeros((n, 8), np.float32)
