@@ -404,11 +404,20 @@ def oracle_errors(model, precisions, bands=48, rows=8):
     """Max / p99 relative error of each precision's coupling step against the FP64 oracle
     (oracle/band.py: interpolation, the three interfaces, assembly and radiation restated on
     the CPU) on `bands` bands of `rows` rows spread over the workload, per output. Relative
-    error = |gpu - oracle| / max(|oracle|, 1e-6 max|oracle|). Cells where the oracle's
-    atmosphere-ocean or atmosphere-sea-ice iteration stops at maxiter are excluded and counted:
-    there the reference's answer is its 100th iterate, which the warm-started path need not
-    follow. The net momentum fluxes also read the west / south neighbours' interface stress,
-    so they exclude the neighbours of such cells too."""
+    error = |gpu - oracle| / max(|oracle|, 1e-6 max|oracle|); interface temperatures in kelvin.
+
+    Three tables per precision:
+      solver       the oracle solves from the atmosphere the GPU interpolated (the FP32
+                   values the GPU's solves read): the solvers' and the assembly's error on
+                   the same inputs -- the accuracy the metric states;
+      interpolation the GPU's FP32 interpolation (FP32 arithmetic, as the reference's Float32
+                   kernels) against the oracle's FP64 one;
+      end_to_end   everything from the oracle's own FP64 interpolation: the solves then
+                   amplify the interpolated inputs' FP32 rounding where differences cancel.
+    Cells where the oracle's atmosphere-ocean or atmosphere-sea-ice iteration stops at maxiter
+    are excluded and counted: there the reference's answer is its 100th iterate, which the
+    warm-started path need not follow. The net momentum fluxes also read the west / south
+    neighbours' interface stress, so they exclude the neighbours of such cells too."""
     import torch
     from oracle import band as OB
     st = model.state
@@ -417,38 +426,46 @@ def oracle_errors(model, precisions, bands=48, rows=8):
     pos = OB.band_positions(st, rows, bands)
     row_index = torch.cat([torch.arange(int(p), int(p) + h) for p in pos]).cuda()
     snaps = {p: step_snapshot(model, p, row_index) for p in precisions}
-    tables = {p: OB.ErrorTable() for p in precisions}
+    tables = {p: {t: OB.ErrorTable() for t in ("solver", "interpolation", "end_to_end")} for p in precisions}
     maxit = {"ao": model.ao_spec.flux_formulation.solver_stop_criteria.maxiter,
              "ai": model.ai_spec.flux_formulation.solver_stop_criteria.maxiter}
+    kelvin = lambda k, a: a + 273.15 if k == "interface_temperature" else a
+    specs = (model.ao_spec, model.ai_spec, model.io_spec, model.asm_spec)
     excluded = 0
     t0 = time.perf_counter()
     for b, lo in enumerate(pos):
-        sub, ref = OB.step_band(st, int(lo), rows, model.ao_spec, model.ai_spec, model.io_spec, model.asm_spec)
-        I = sub.interior
-        stopped = (I(ref["ao"]["iterations"]) >= maxit["ao"]) | (I(ref["ai"]["iterations"]) >= maxit["ai"])
-        excluded += int(stopped.sum())
-        near = stopped.copy()
-        near[:, 1:] |= stopped[:, :-1]
-        near[1:, :] |= stopped[:-1, :]
-        keep, keep_net = ~stopped, ~near
+        part = lambda a: a[b * h:(b + 1) * h]
+        _, own = OB.step_band(st, int(lo), rows, *specs)
         for p, snap in snaps.items():
-            part = lambda a: I(a[b * h:(b + 1) * h])
-            for group in ("atmos", "ao", "ai", "io", "net"):
-                if group not in ref or group not in snap:
-                    continue
-                for k, r in ref[group].items():
-                    if k == "iterations" or k not in snap[group]:
+            sub, same = OB.step_band(st, int(lo), rows, *specs,
+                                     atmos={k: part(v) for k, v in snap.get("atmos", {}).items()})
+            I = sub.interior
+            for table, ref in (("solver", same), ("end_to_end", own)):
+                stopped = (I(ref["ao"]["iterations"]) >= maxit["ao"]) | (I(ref["ai"]["iterations"]) >= maxit["ai"])
+                if table == "solver" and p == precisions[0]:
+                    excluded += int(stopped.sum())
+                near = stopped.copy()
+                near[:, 1:] |= stopped[:, :-1]
+                near[1:, :] |= stopped[:-1, :]
+                for group in ("ao", "ai", "io", "net"):
+                    if group not in ref or group not in snap:
                         continue
-                    kk = keep_net if group == "net" else keep
-                    tables[p].add(f"{group}.{k}", part(snap[group][k]), I(r), kk)
-            tables[p].add("io.ocean_T_after_frazil", part(snap["io_T"]["T_oc"]), I(ref["io"]["T_oc"][0]), keep)
+                    for k, r in ref[group].items():
+                        if k == "iterations" or k not in snap[group]:
+                            continue
+                        tables[p][table].add(f"{group}.{k}", kelvin(k, I(part(snap[group][k]))), kelvin(k, I(r)),
+                                             ~near if group == "net" else ~stopped)
+                tables[p][table].add("io.ocean_T_after_frazil", I(part(snap["io_T"]["T_oc"])),
+                                     I(ref["io"]["T_oc"][0]), ~stopped)
+            for k, r in own.get("atmos", {}).items():
+                tables[p]["interpolation"].add(f"atmos.{k}", I(part(snap["atmos"][k])), I(r))
     oracle_s = time.perf_counter() - t0
     out = {}
     for p, t in tables.items():
-        s = t.summary()
-        head = [s[f"{g}.{k}"] for g in ("ao", "ai") for k in HEADLINE_FLUXES if f"{g}.{k}" in s]
+        s = {name: tab.summary() for name, tab in t.items()}
+        head = [s["solver"][f"{g}.{k}"] for g in ("ao", "ai") for k in HEADLINE_FLUXES if f"{g}.{k}" in s["solver"]]
         out[p] = {"max_headline_fluxes": max(x["max"] for x in head),
-                  "p99_headline_fluxes": max(x["p99"] for x in head), "per_output": s}
+                  "p99_headline_fluxes": max(x["p99"] for x in head), **s}
     out["sample"] = (f"{len(pos)} bands of {rows} rows x {L.nx} cells spread over the domain; "
                      f"{excluded} cells where the oracle stops at maxiter excluded; oracle {oracle_s:.1f} s "
                      f"on {_oracle_threads()} threads")

@@ -307,6 +307,21 @@ def ensemble_params(seed, members):
                  nu_scale=rng.uniform(0.8, 1.2)) for _ in range(members)]
 
 
+def ensemble_member_spec(pert):
+    """The atmosphere-ocean interface of one ensemble member: SimilarityTheoryFluxes with the
+    member's Charnock parameter, minimum gustiness, smooth-wall parameter (0.11 scaled) and
+    Reynolds-scaling A, b (5.85e-5, 0.72 scaled) for both scalar roughness lengths."""
+    from . import params as P
+    mom = P.MomentumRoughnessLength(wave_formulation=pert["charnock"],
+                                    smooth_wall_parameter=0.11 * pert["nu_scale"])
+    sc = P.ScalarRoughnessLength(reynolds_number_scaling_function=P.ReynoldsScalingFunction(
+        5.85e-5 * pert["A_scale"], 0.72 * pert["b_scale"]))
+    flux = P.SimilarityTheoryFluxes(subgrid_velocities=P.ConvectiveGustiness(1.2, pert["minimum_gustiness"]),
+                                    momentum_roughness_length=mom, temperature_roughness_length=sc,
+                                    water_vapor_roughness_length=sc)
+    return P.atmosphere_ocean_interface_spec(flux_formulation=flux)
+
+
 def ensemble(seed=1003, members=32, nx=720, ny=360, dtype=np.float32, halo=HALO):
     """`members` AO problems back to back (member stride = one parent array)."""
     states = [ao_1deg(seed * 100 + m, nx, ny, dtype, halo) for m in range(members)]

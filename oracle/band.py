@@ -53,22 +53,33 @@ def band_of(array, state, lo, rows):
 
 
 def step_band(state, lo, rows, ao_spec, ai_spec=None, io_spec=None, asm_spec=None, time_weight=None,
-              dz_top=10.0):
+              dz_top=10.0, atmos=None):
     """The oracle's coupling step on rows lo+1..lo+rows; returns (layout, results) with
-    results = {"atmos": {...}, "ao": {...}, "ai": {...}, "io": {...}, "net": {...}} of
-    band-sized FP64 parent arrays ("ao"/"ai" include "iterations")."""
+    results = {"atmos": {...}, "ao": {...}, "ai": {...}, "io": {...}, "net": {...},
+    "inputs": {...}} of band-sized FP64 parent arrays ("ao"/"ai" include "iterations";
+    "inputs" holds the band's inputs, the interpolated atmosphere included).
+
+    `atmos` (optional): the band's exchange-grid atmosphere (u_atm, ..., lw_down: band-sized
+    parent arrays) to solve from instead of the oracle's own interpolation -- e.g. the
+    values a GPU step with FP32 fields interpolated in FP32 arithmetic and then read, so
+    that the solves are compared on the same inputs; "atmos" in the results is still the
+    oracle's interpolation."""
     sub, _ = band_rows(state, lo, rows)
     band = {k: band_of(v, state, lo, rows) for k, v in state.fields.items() if v.ndim == 2}
-    res = {}
+    res = {"inputs": band}
     if state.atmos is not None:
         at = state.atmos
         c = state.coords
         bc = api.exchange_coords(syn.LonLat(c.lon0, c.dlon, c.lat0 + lo * c.dlat, c.dlat))
         tw = at["time_weight"] if time_weight is None else time_weight
         out = oracle.interpolate(sub, bc, api.atmos_grid_struct(at), at["arrays"], tw)
+        res["atmos"] = {k: out[n] for n, k in ATMOS_TO_EXCHANGE}
         for n, k in ATMOS_TO_EXCHANGE:
             band[k] = out[n]
-        res["atmos"] = {k: band[k] for _, k in ATMOS_TO_EXCHANGE}
+    if atmos is not None:
+        for _, k in ATMOS_TO_EXCHANGE:
+            if k in atmos:
+                band[k] = np.ascontiguousarray(atmos[k], dtype=np.float64)
     res["ao"] = oracle.ao_fluxes(ao_spec.to_c(), sub, band)
     ice = ai_spec is not None and "ice_concentration" in band
     if ice:
@@ -122,7 +133,10 @@ def relative_errors(got, ref, floor):
 class ErrorTable:
     """Max and 99th-percentile relative error per output over many bands. Each output's
     floor is 1e-6 of its largest oracle magnitude over all bands (cells where the flux
-    nearly vanishes are compared on that absolute scale)."""
+    nearly vanishes are compared on that absolute scale). "normwise" is the largest
+    absolute error over the largest oracle magnitude: the measure for sums of terms that
+    cancel (the net fluxes), whose per-cell relative error grows without bound where
+    the sum vanishes."""
 
     def __init__(self):
         self.pairs = {}
@@ -143,6 +157,10 @@ class ErrorTable:
             finite = np.abs(r[np.isfinite(r)])
             floor = 1e-6 * finite.max() if finite.size else 0.0
             e = relative_errors(g, r, floor)
+            ok = np.isfinite(g) & np.isfinite(r)
+            norm = float(np.abs(g - r)[ok].max() / finite.max()) if ok.any() and finite.size and finite.max() > 0 \
+                else 0.0
             out[name] = {"max": float(e.max()) if e.size else 0.0,
-                         "p99": float(np.percentile(e, 99)) if e.size else 0.0, "cells": int(e.size)}
+                         "p99": float(np.percentile(e, 99)) if e.size else 0.0,
+                         "normwise": norm, "cells": int(e.size)}
         return out

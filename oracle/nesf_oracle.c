@@ -50,6 +50,11 @@ void oracle_set_humidity_ulp_shift(int32_t n, int32_t carry) {
     g_humidity_ulp_shift = n;
     g_humidity_shift_carry = carry;
 }
+/* The same probe on the air's potential temperature theta_a (surface_atmosphere_temperature,
+ * its ulp differs between a CPU and a GPU that contracts its multiply-add): where theta_a - T_s
+ * cancels, the sensible heat responds to it by ulp(theta_a) / |theta_a - T_s|. */
+static int32_t g_theta_ulp_shift = 0;
+void oracle_set_temperature_ulp_shift(int32_t n) { g_theta_ulp_shift = n; }
 int32_t oracle_get_threads(void) {
 #ifdef _OPENMP
     return g_threads > 0 ? g_threads : omp_get_max_threads();
@@ -571,6 +576,7 @@ static istate iterate_state(const nesf_interface_params* p, const cell_in* c, co
     if (g_humidity_shift_carry) q_iter = qs;
     double dq = c->qa - qs;
     double tha = surface_atmosphere_temperature(p, c->Ta, c->qa);
+    for (int32_t k = 0; k < g_theta_ulp_shift; k++) tha = nextafter(tha, INFINITY);
     double dth = tha - Ts;
     double dh = p->surface_layer_height;
     istate n;

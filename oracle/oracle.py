@@ -63,6 +63,7 @@ def load():
             "oracle_apply_air_land_radiative_fluxes": (C.c_int, [P(A.LandRadiationParams), P(A.LandFluxFields)]),
             "oracle_set_threads": (None, [C.c_int32]),
             "oracle_set_humidity_ulp_shift": (None, [C.c_int32, C.c_int32]),
+            "oracle_set_temperature_ulp_shift": (None, [C.c_int32]),
             "oracle_get_threads": (C.c_int32, []),
         }
         for name, (res, args) in sig.items():
@@ -128,6 +129,42 @@ def humidity_ulp_shift(n, carry):
         yield
     finally:
         lib.oracle_set_humidity_ulp_shift(0, 0)
+
+
+@contextlib.contextmanager
+def temperature_ulp_shift(n):
+    """Within the block every iterate's air potential temperature theta_a is moved n units in
+    the last place (oracle_set_temperature_ulp_shift): the temperature side of the probe."""
+    lib = load()
+    lib.oracle_set_temperature_ulp_shift(n)
+    try:
+        yield
+    finally:
+        lib.oracle_set_temperature_ulp_shift(0)
+
+
+def conditioning_response(run, ref, keys, shift=1024, view=None):
+    """Per-cell response of the oracle's outputs to one unit in the last place of its interface
+    humidity (with and without carrying the change into the next iterate) and of theta_a: the
+    largest relative change over the three probes, each under a `shift`-ulp move, divided by
+    `shift` (a single ulp rounds away in some cells). `run()` returns the oracle's outputs;
+    `view(key, array)` selects the cells compared (default: all)."""
+    view = view or (lambda k, a: a)
+    outs = []
+    for carry in (False, True):
+        with humidity_ulp_shift(shift, carry):
+            outs.append(run())
+    with temperature_ulp_shift(shift):
+        outs.append(run())
+    resp = {}
+    for k in keys:
+        r = np.asarray(view(k, ref[k]), np.float64)
+        scale = np.abs(r)
+        finite = scale[np.isfinite(scale)]
+        den = np.maximum(scale, 1e-6 * finite.max() if finite.size else 0.0)
+        den = np.where(den > 0, den, 1.0)
+        resp[k] = np.max([np.abs(np.asarray(view(k, o[k]), np.float64) - r) / den for o in outs], axis=0) / shift
+    return resp
 
 
 def ai_fluxes(params, layout, inputs, interface_temperature, with_iterations=True):

@@ -34,3 +34,21 @@ def widen(arrays):
         else:
             out[k] = v
     return out
+
+
+def assert_conditioned(gpu, ref, keys, response, label="", units=4.0):
+    """The plain FP64 parity bar, per cell: relative error (floor 1e-6 of the field's largest
+    magnitude) <= 1e-12, or `units` times the oracle's own response to one unit in the last
+    place of its interface humidity or of theta_a where that is larger (oracle
+    conditioning_response). Where q_a - q_s or theta_a - T_s nearly cancels, a last-place
+    difference of a libm result or of a contracted multiply-add between the CPU and the GPU
+    moves the reference's own answer by that much; elsewhere the bar is 1e-12."""
+    for k in keys:
+        e = rel_err(gpu[k], ref[k], floor_frac=1e-6)
+        bar = np.maximum(1e-12, units * np.asarray(response[k]))
+        ok = e <= bar
+        if not np.all(ok):
+            worst = int(np.argmax(np.where(ok, 0.0, e / bar)))
+            raise AssertionError((label, k, "cells over the bar:", int((~ok).sum()), "of", e.size,
+                                  "worst error / bar:", float((e / bar).ravel()[worst]),
+                                  "error:", float(e.ravel()[worst]), "cells > 1e-12:", int((e > 1e-12).sum())))

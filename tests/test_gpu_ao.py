@@ -2,7 +2,9 @@
 
 Bar: the plain FP64 kernel matches the oracle to 1e-12 relative on tau_x, tau_y,
 Q_sensible, Q_latent and evaporation (and u*, theta*, q*, T_s) with identical
-iteration counts; the FP32 + FP64-polish kernel stays within 1e-5 relative.
+iteration counts -- per cell, where q_a - q_s or theta_a - T_s cancels, to 4 x the
+oracle's own response to one ulp of its humidity or theta_a when that exceeds
+1e-12; the FP32 + FP64-polish kernel stays within 1e-5 relative.
 Relative errors are |gpu - ref| / max(|ref|, 1e-6 max|ref|): where a flux
 crosses zero it is the small difference of two large terms (q_a - q_s,
 theta_a - T_s), a 1-ulp difference of the CPU and GPU libm there is amplified
@@ -12,7 +14,7 @@ field's scale (an absolute bar of 1e-18 max|ref| for the plain kernel).
 import numpy as np
 import pytest
 
-from helpers import rel_err, to_numpy, widen
+from helpers import assert_conditioned, rel_err, to_numpy, widen
 from nesf import api
 from nesf import fields as F
 from nesf import params as P
@@ -50,20 +52,20 @@ def ao1(oracle):
     return st, spec, ref
 
 
-def assert_parity(gpu, ref, keys, label=""):
-    """1e-12 relative on 99.99 % of the cells and 1e-11 on every cell: the few cells
-    above 1e-12 are those where q_a - q_s or theta_a - T_s nearly cancels, which
-    multiplies the last-bit difference of the CPU and GPU pow/exp by |q_s / dq|."""
-    for k in keys:
-        e = rel_err(gpu[k], ref[k], floor_frac=1e-6)
-        n_bad = int((e > 1e-12).sum())
-        assert np.percentile(e, 99.99) <= 1e-12 and e.max() <= 1e-11, (label, k, float(e.max()), n_bad, e.size)
+def assert_parity(oracle, spec, st, gpu, ref, keys, label="", view=None):
+    """Per cell, 1e-12 relative, or 4 x the oracle's own response to one ulp of its interface
+    humidity or of theta_a where q_a - q_s or theta_a - T_s nearly cancels (helpers.
+    assert_conditioned); `view(key, array)` selects the cells compared."""
+    view = view or (lambda k, a: a)
+    resp = oracle.conditioning_response(lambda: oracle.ao_fluxes(spec.to_c(), st.layout, st.fields), ref, keys,
+                                        view=view)
+    assert_conditioned({k: view(k, gpu[k]) for k in keys}, {k: view(k, ref[k]) for k in keys}, keys, resp, label)
 
 
-def test_plain_f64_matches_oracle_1deg(ao1):
+def test_plain_f64_matches_oracle_1deg(oracle, ao1):
     st, spec, ref = ao1
     gpu, stats = run_gpu_ao(spec, st, "f64", stats=True)
-    assert_parity({k: ring(st, gpu[k]) for k in ALL_OUT}, {k: ring(st, ref[k]) for k in ALL_OUT}, ALL_OUT)
+    assert_parity(oracle, spec, st, gpu, ref, ALL_OUT, view=lambda k, a: ring(st, a))
     assert np.array_equal(ring(st, gpu["iterations"]), ring(st, ref["iterations"]))
     n = (st.layout.nx + 2) * (st.layout.ny + 2)
     assert stats["cells"] == n and stats["solved"] == n
@@ -161,7 +163,7 @@ def test_ragged_sizes(oracle, nx, ny):
     spec = P.atmosphere_ocean_interface_spec()
     ref = oracle.ao_fluxes(spec.to_c(), st.layout, st.fields)
     gpu, _ = run_gpu_ao(spec, st, "f64")
-    assert_parity({k: ring(st, gpu[k]) for k in FLUXES}, {k: ring(st, ref[k]) for k in FLUXES}, FLUXES)
+    assert_parity(oracle, spec, st, gpu, ref, FLUXES, view=lambda k, a: ring(st, a))
     assert np.array_equal(ring(st, gpu["iterations"]), ring(st, ref["iterations"]))
 
 
@@ -200,17 +202,10 @@ def test_formulation_variants(oracle, variant):
     it = ring(st, ref["iterations"])
     conv = it < spec.flux_formulation.solver_stop_criteria.__dict__.get("maxiter", 10 ** 9)
     # a skin temperature feeds T_s back into dtheta = theta_a - T_s every iteration, where a
-    # 1-ulp libm difference is amplified by the cancellation; 1e-10 bounds it there
-    g = {k: ring(st, gpu[k])[conv] for k in ALL_OUT}
-    r = {k: ring(st, ref[k])[conv] for k in ALL_OUT}
-    g["interface_temperature"] = g["interface_temperature"] + 273.15
-    r["interface_temperature"] = r["interface_temperature"] + 273.15
-    if variant == "skin_diffusive":
-        for k in ALL_OUT:
-            e = rel_err(g[k], r[k], floor_frac=1e-6)
-            assert e.max() <= 1e-10, (variant, k, float(e.max()))
-    else:
-        assert_parity(g, r, ALL_OUT, variant)
+    # last-place difference is amplified by the cancellation: the per-cell bar measures that
+    # amplification on the oracle itself
+    view = lambda k, a: ring(st, a)[conv] + (273.15 if k == "interface_temperature" else 0.0)
+    assert_parity(oracle, spec, st, gpu, ref, ALL_OUT, variant, view=view)
     assert np.array_equal(ring(st, gpu["iterations"])[conv], it[conv]), variant
     # the COARE form lacks psi(l/L) and its profile turns negative for a few percent of
     # very unstable cells, which never converge (NaN, as in the reference)
@@ -246,6 +241,6 @@ def test_nonfinite_inputs_stay_contained(oracle):
     gpu, stats = run_gpu_ao(spec, st, "f64", stats=True)
     assert stats["nonconverged"] >= 1
     ok = np.isfinite(ref["latent_heat"])
-    assert_parity({k: gpu[k][ok] for k in FLUXES}, {k: ref[k][ok] for k in FLUXES}, FLUXES)
+    assert_parity(oracle, spec, st, gpu, ref, FLUXES, view=lambda k, a: a[ok])
     for k in FLUXES:
         assert np.array_equal(np.isnan(gpu[k]), np.isnan(ref[k]))

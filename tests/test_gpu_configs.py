@@ -1,0 +1,278 @@
+"""Each benchmark workload at its stated size on the GPU, against the FP64 oracle.
+
+The GPU runs the whole grid; the oracle, which restates the reference in plain C, runs
+on bands of rows spread over the grid (oracle/band.py: a band with its halos gives the
+whole grid's answer on its interior, checked bit for bit on the CPU by
+test_oracle_bands.py). Relative error = |gpu - oracle| / max(|oracle|, 1e-6 max|oracle|).
+
+1. 1440 x 560 (latitude -70..70), 30 % land, the prescribed atmosphere on a 640 x 320 grid
+   at two 3-hourly snapshots interpolated in space and time onto the exchange grid, then
+   the atmosphere-ocean solve (interpolate_state! + compute_atmosphere_ocean_fluxes!).
+   FP64 fields, plain FP64: the interpolation to 1e-13, the fluxes to the per-cell
+   conditioning bar (helpers.assert_conditioned), identical iteration counts. FP32 fields,
+   the adaptive FP32 solver: within 1e-5.
+2. 1440 x 600 (latitude -75..75) ocean + sea ice, the atmosphere-ocean, atmosphere-sea-ice
+   and sea-ice-ocean fluxes and the net-flux assembly with radiation in one coupling step.
+   FP32 fields, the adaptive solver, the step replayed as a CUDA graph: the interface
+   fluxes within 1e-5; the sea-ice-ocean fluxes within 1e-5 (p99) and 1e-6 under the ice;
+   the net fluxes within 1e-5 of their largest magnitude. FP64 fields, plain FP64: the
+   solves at the conditioning bar with identical iteration counts, the rest to 1e-12.
+3. 32 members x 720 x 360 in one ensemble launch, each member with its own Charnock
+   parameter, gustiness and roughness coefficients: per member two bands against the
+   oracle with that member's parameters (plain FP64 arithmetic on FP32 fields within 1e-6,
+   the FP32 output rounding; the adaptive solver within 1e-5), and per-member compensated
+   FP64 area integrals of the fluxes equal to the exact sums of the GPU's cell values.
+
+Cells where the oracle stops at maxiter (its 100th iterate, which a path that is not the
+reference's FP64 iteration need not follow) are excluded from the FP32 comparisons and
+counted; the plain FP64 path must match them too.
+"""
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+from helpers import assert_conditioned, rel_err, to_numpy
+from nesf import api
+from nesf import fields as F
+from nesf import params as P
+from nesf import synthetic as syn
+from nesf.coupled import EXCHANGE_ATMOS, CoupledModel
+
+pytestmark = pytest.mark.gpu
+
+FLUXES = ("x_momentum", "y_momentum", "sensible_heat", "latent_heat", "water_vapor")
+AO_ALL = FLUXES + ("friction_velocity", "temperature_scale", "water_vapor_scale", "interface_temperature")
+ROWS = 8
+
+
+def kelvin_view(k, a):
+    """Interface temperatures in kelvin, so that their relative error is meaningful."""
+    return a + 273.15 if k == "interface_temperature" else a
+
+
+def bands_of(state, count):
+    from oracle import band as OB
+    return [int(x) for x in OB.band_positions(state, ROWS, count)]
+
+
+def band_part(full, state, lo):
+    from oracle import band as OB
+    sub, rs = OB.band_rows(state, lo, ROWS)
+    return sub.interior(np.asarray(full)[rs])
+
+
+# --------------------------------------------------------------------- 1
+@pytest.fixture(scope="module")
+def quarter64():
+    return syn.ao_quarter_land(dtype=np.float64)
+
+
+def test_config1_quarter_degree_plain_f64(oracle, quarter64):
+    import torch
+    from oracle import band as OB
+    st = quarter64
+    assert (st.layout.nx, st.layout.ny) == (1440, 560) and st.atmos is not None
+    spec = P.atmosphere_ocean_interface_spec()
+    m = CoupledModel(st, ao_spec=spec)
+    m.interpolate_state()
+    it = torch.zeros(st.layout.shape, dtype=torch.int32, device="cuda")
+    api.compute_atmosphere_ocean_fluxes(spec, st.layout, m.x, m.ao, precision="f64", iterations=it)
+    torch.cuda.synchronize()
+    gpu = {k: to_numpy(v) for k, v in m.ao.items()}
+    atm = {k: to_numpy(m.x[k]) for k in EXCHANGE_ATMOS.values()}
+    its = to_numpy(it)
+    water = 0
+    for lo in bands_of(st, 12):
+        sub, ref = OB.step_band(st, lo, ROWS, spec)
+        I = sub.interior
+        for k, r in ref["atmos"].items():
+            e = rel_err(band_part(atm[k], st, lo), I(r), floor_frac=1e-6)
+            assert e.max() <= 1e-13, ("interpolation", lo, k, float(e.max()))
+        band_in = ref["inputs"]
+        resp = oracle.conditioning_response(lambda: oracle.ao_fluxes(spec.to_c(), sub, band_in), ref["ao"], AO_ALL,
+                                            view=lambda k, a: kelvin_view(k, I(a)))
+        g = {k: kelvin_view(k, band_part(gpu[k], st, lo)) for k in AO_ALL}
+        r = {k: kelvin_view(k, I(ref["ao"][k])) for k in AO_ALL}
+        assert_conditioned(g, r, AO_ALL, resp, f"band {lo}")
+        assert np.array_equal(band_part(its, st, lo), I(ref["ao"]["iterations"])), lo
+        water += int((I(band_in["inactive"]) == 0).sum())
+    assert water > 0.5 * 12 * ROWS * 1440
+
+
+def test_config1_quarter_degree_fp32_adaptive(oracle):
+    """FP32 fields interpolate in FP32 arithmetic (the reference's Float32 kernels): within 1e-6
+    of each field's largest magnitude, and 1e-6 relative for the positive fields, of the
+    oracle's FP64 interpolation. The adaptive solve is compared with the oracle solving from
+    the same interpolated (FP32) atmosphere: within 1e-5."""
+    import torch
+    from oracle import band as OB
+    st = syn.ao_quarter_land()
+    spec = P.atmosphere_ocean_interface_spec()
+    m = CoupledModel(st, ao_spec=spec)
+    m.interpolate_state()
+    api.compute_atmosphere_ocean_fluxes(spec, st.layout, m.x, m.ao, precision="f32_adaptive")
+    torch.cuda.synchronize()
+    gpu = {k: to_numpy(v).astype(np.float64) for k, v in m.ao.items()}
+    atm = {k: to_numpy(m.x[k]).astype(np.float64) for k in EXCHANGE_ATMOS.values()}
+    excluded = 0
+    for lo in bands_of(st, 12):
+        _, rs = OB.band_rows(st, lo, ROWS)
+        sub, ref = OB.step_band(st, lo, ROWS, spec, atmos={k: v[rs] for k, v in atm.items()})
+        I = sub.interior
+        for k, r in ref["atmos"].items():
+            g = band_part(atm[k], st, lo)
+            assert np.abs(g - I(r)).max() <= 1e-6 * np.abs(r).max(), ("interpolation", lo, k)
+            if k not in ("u_atm", "v_atm"):
+                assert rel_err(g, I(r), floor_frac=1e-6).max() <= 1e-6, ("interpolation", lo, k)
+        keep = I(ref["ao"]["iterations"]) < 100
+        excluded += int((~keep).sum())
+        for k in AO_ALL:
+            e = rel_err(kelvin_view(k, band_part(gpu[k], st, lo)), kelvin_view(k, I(ref["ao"][k])),
+                        floor_frac=1e-6)[keep]
+            assert e.max() <= 1e-5, (lo, k, float(e.max()))
+    assert excluded < 0.001 * 12 * ROWS * 1440
+
+
+# --------------------------------------------------------------------- 2
+def _snapshot(m):
+    snap = {"ao": {k: to_numpy(v).astype(np.float64) for k, v in m.ao.items()},
+            "ai": {k: to_numpy(v).astype(np.float64) for k, v in m.ai.items()},
+            "io": {k: to_numpy(v).astype(np.float64) for k, v in m.io.items()},
+            "net": {k: to_numpy(v).astype(np.float64) for k, v in m.net.items()}}
+    snap["io"]["T_oc"] = to_numpy(m.x["T_oc"]).astype(np.float64)
+    return snap
+
+
+def _specs():
+    return dict(ao_spec=P.atmosphere_ocean_interface_spec(), ai_spec=P.atmosphere_sea_ice_interface_spec(),
+                io_spec=P.SeaIceOceanSpec(), asm_spec=P.AssemblySpec())
+
+
+def test_config2_coupled_step_fp32_graph(oracle):
+    import torch
+    from oracle import band as OB
+    st = syn.coupled_1440()
+    assert (st.layout.nx, st.layout.ny) == (1440, 600)
+    sp = _specs()
+    m = CoupledModel(st, **sp)
+    m.capture("f32_adaptive")
+    m.reset()
+    m.graph_step()
+    torch.cuda.synchronize()
+    snap = _snapshot(m)
+    excluded = 0
+    tables = OB.ErrorTable()
+    for lo in bands_of(st, 16):
+        sub, ref = OB.step_band(st, lo, ROWS, **sp)
+        I = sub.interior
+        stopped = (I(ref["ao"]["iterations"]) >= 100) | (I(ref["ai"]["iterations"]) >= 100)
+        excluded += int(stopped.sum())
+        near = stopped.copy()
+        near[:, 1:] |= stopped[:, :-1]
+        near[1:, :] |= stopped[:-1, :]
+        for group in ("ao", "ai"):
+            for k in (AO_ALL if group == "ao" else FLUXES + ("interface_temperature",)):
+                e = rel_err(kelvin_view(k, band_part(snap[group][k], st, lo)), kelvin_view(k, I(ref[group][k])),
+                            floor_frac=1e-6)[~stopped]
+                assert e.max() <= 1e-5, (group, lo, k, float(e.max()))
+        ice = I(ref["inputs"]["ice_concentration"]) > 0
+        for k in F.IO_OUTPUTS + ("T_oc",):
+            r = I(ref["io"][k][0] if k == "T_oc" else ref["io"][k])
+            tables.add("io." + k, band_part(snap["io"][k], st, lo), r)
+            if k in ("interface_heat", "interface_T", "interface_S"):
+                tables.add("io_ice." + k, band_part(snap["io"][k], st, lo), r, ice)
+        for k, r in ref["net"].items():
+            tables.add("net." + k, band_part(snap["net"][k], st, lo), I(r), ~near)
+    s = tables.summary()
+    for k, v in s.items():
+        if k.startswith("io_ice."):
+            assert v["max"] <= 1e-6, (k, v)
+        elif k.startswith("io."):
+            assert v["p99"] <= 1e-5 and v["normwise"] <= 1e-5, (k, v)
+        else:
+            assert v["normwise"] <= 1e-5, (k, v)
+    assert excluded < 0.001 * 16 * ROWS * 1440
+
+
+def test_config2_coupled_step_plain_f64(oracle):
+    import torch
+    from oracle import band as OB
+    st = syn.coupled_1440(dtype=np.float64)
+    sp = _specs()
+    m = CoupledModel(st, **sp)
+    m.iterations = {k: torch.zeros(st.layout.shape, dtype=torch.int32, device="cuda") for k in ("ao", "ai")}
+    m.reset()
+    m.update_state("f64")
+    torch.cuda.synchronize()
+    snap = _snapshot(m)
+    its = {k: to_numpy(v) for k, v in m.iterations.items()}
+    for lo in bands_of(st, 10):
+        sub, ref = OB.step_band(st, lo, ROWS, **sp)
+        I = sub.interior
+        band_in = ref["inputs"]
+        view = lambda k, a: kelvin_view(k, I(a))
+        resp = oracle.conditioning_response(lambda: oracle.ao_fluxes(sp["ao_spec"].to_c(), sub, band_in), ref["ao"],
+                                            AO_ALL, view=view)
+        assert_conditioned({k: kelvin_view(k, band_part(snap["ao"][k], st, lo)) for k in AO_ALL},
+                           {k: view(k, ref["ao"][k]) for k in AO_ALL}, AO_ALL, resp, f"ao band {lo}")
+        ai_keys = FLUXES + ("interface_temperature",)
+        resp = oracle.conditioning_response(
+            lambda: oracle.ai_fluxes(sp["ai_spec"].to_c(), sub, band_in, band_in["ice_temperature"]), ref["ai"],
+            ai_keys, view=view)
+        assert_conditioned({k: kelvin_view(k, band_part(snap["ai"][k], st, lo)) for k in ai_keys},
+                           {k: view(k, ref["ai"][k]) for k in ai_keys}, ai_keys, resp, f"ai band {lo}")
+        for g in ("ao", "ai"):
+            assert np.array_equal(band_part(its[g], st, lo), I(ref[g]["iterations"])), (g, lo)
+        # the sea-ice-ocean fluxes and the assembly read the solves' outputs: compared where
+        # those are within 1e-12 of the oracle's (every cell but a few cancelling ones)
+        for k in F.IO_OUTPUTS:
+            e = rel_err(band_part(snap["io"][k], st, lo), I(ref["io"][k]), floor_frac=1e-6)
+            assert e.max() <= 1e-12, ("io", lo, k, float(e.max()))
+        for k, r in ref["net"].items():
+            e = rel_err(band_part(snap["net"][k], st, lo), I(r), floor_frac=1e-6)
+            assert np.percentile(e, 99.9) <= 1e-12, ("net", lo, k, float(e.max()))
+
+
+# --------------------------------------------------------------------- 3
+def test_config3_ensemble_32_members(oracle):
+    import torch
+    from oracle import band as OB
+    members = 32
+    st = syn.ensemble()
+    L = st.layout
+    assert st.members == members and (L.nx, L.ny) == (720, 360)
+    specs = [syn.ensemble_member_spec(p) for p in st.perturbations]
+    assert len({s.flux_formulation.momentum_roughness_length.wave_formulation for s in specs}) == members
+    dev = api.to_device({k: st.fields[k] for k in F.AO_INPUTS if k in st.fields})
+    out = {k: torch.zeros((members,) + L.shape, dtype=torch.float32, device="cuda") for k in F.AO_OUTPUTS}
+    positions = bands_of(syn.SurfaceState(L, st.coords, st.dtype), 2 * members)
+    for prec, bar in (("f64", 1e-6), ("f32_adaptive", 1e-5)):
+        for v in out.values():
+            v.fill_(float("nan"))
+        api.compute_atmosphere_ocean_fluxes_ensemble(specs, L, dev, out, precision=prec)
+        torch.cuda.synchronize()
+        host = {k: to_numpy(v).astype(np.float64) for k, v in out.items()}
+        for mbr in range(members):
+            ms = syn.SurfaceState(L, st.coords, st.dtype, fields={k: v[mbr] for k, v in st.fields.items()})
+            for lo in positions[2 * mbr:2 * mbr + 2]:
+                sub, ref = OB.step_band(ms, lo, ROWS, specs[mbr])
+                I = sub.interior
+                keep = I(ref["ao"]["iterations"]) < 100
+                for k in AO_ALL:
+                    e = rel_err(kelvin_view(k, band_part(host[k][mbr], ms, lo)), kelvin_view(k, I(ref["ao"][k])),
+                                floor_frac=1e-6)[keep]
+                    assert e.max() <= bar, (prec, mbr, lo, k, float(e.max()))
+    # per-member compensated FP64 area integrals of the (last) fluxes: the exact sums
+    lat = st.coords.lat0 + np.arange(L.ny) * st.coords.dlat
+    rows = np.cos(np.radians(lat)) * 1e10
+    rows_dev = torch.from_numpy(rows).cuda()
+    for mbr in (0, 13, 31):
+        flds = [out[k][mbr] for k in ("sensible_heat", "latent_heat", "x_momentum")]
+        got = api.area_integrals(L, flds, row_area=rows_dev).cpu().numpy()
+        exact = oracle.area_integrals(L, [to_numpy(f) for f in flds], row_area=rows)
+        for n, f in enumerate(flds):
+            hi, lo_ = float(got[n][0]), float(got[n][1])
+            assert hi == float(exact[n]), (mbr, n)
+            scale = np.abs(L.interior(to_numpy(f)).astype(np.float64)).sum() * rows.max()
+            assert abs(Fraction(hi) + Fraction(lo_) - exact[n]) <= Fraction(scale) * Fraction(2) ** -100

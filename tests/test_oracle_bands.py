@@ -31,8 +31,8 @@ def test_band_equals_whole_grid_rows(workload, lo, rows):
     L = st.layout
     full_layout, full = OB.step_band(st, 0, L.ny, **specs())
     sub, part = OB.step_band(st, lo, rows, **specs())
-    assert set(part) == {"atmos", "ao", "ai", "io", "net"}
-    for group in part:
+    assert set(part) == {"atmos", "ao", "ai", "io", "net", "inputs"}
+    for group in ("atmos", "ao", "ai", "io", "net"):
         for k, v in part[group].items():
             if k == "T_oc":
                 v, w = v[0], full[group][k][0]

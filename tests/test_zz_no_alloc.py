@@ -37,14 +37,16 @@ pytestmark = pytest.mark.gpu
 MAX_CELLS = 1 << 21
 
 
-def _noalloc(lib, spec, layout, dev, out, precision, warm_start=0):
+def _noalloc(lib, spec, layout, dev, out, precision, mlp=None):
     import torch
     arrays = {k: dev.get(k) for k in F.AO_INPUTS}
     arrays.update({k: out[k] for k in F.AO_OUTPUTS})
     f = F.pack(A.AOFields, F.make_grid(layout), arrays)
     p = spec.to_c()
     o = api.solver_options(precision)
-    o.warm_start = warm_start
+    if mlp is not None:
+        o.warm_start = 1
+        o.mlp = mlp.data_ptr()
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     return lib.nesf_compute_atmosphere_ocean_fluxes_noalloc(C.byref(p), C.byref(f), C.byref(o), stream)
 
@@ -137,6 +139,7 @@ def test_noalloc_refuses_a_warm_start():
     spec = P.atmosphere_ocean_interface_spec()
     dev = api.to_device({k: st.fields[k] for k in F.AO_INPUTS if k in st.fields})
     out = {k: torch.zeros(st.layout.shape, dtype=torch.float64, device="cuda") for k in F.AO_OUTPUTS}
-    code = _noalloc(lib, spec, st.layout, dev, out, "f32_adaptive", warm_start=1)
+    blob = torch.zeros(lib.nesf_mlp_bytes(), dtype=torch.uint8, device="cuda")   # never read: refused first
+    code = _noalloc(lib, spec, st.layout, dev, out, "f32_adaptive", mlp=blob)
     assert code == A.NESF_ERR_ARG
     assert b"warm start" in lib.nesf_last_error()
