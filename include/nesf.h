@@ -794,7 +794,12 @@ typedef struct {
     int32_t io_overlap;       /* coupling step: sea-ice-ocean fluxes beside the sea-ice pass 1 (1)      */
     int32_t pass1_fetch;      /* pass 1 of the FP32 solvers: 1 one thread per work-list entry; 2 in the
                                  sea-ice solve, 3 in the sea-ice and ocean solves, the resident blocks
-                                 only, each warp taking 32 entries at a time (2)                       */
+                                 only, each warp taking 32 entries at a time; 4 as 3, and the adaptive
+                                 solver's pass 1 with lane refill: each lane advances its own cell one
+                                 map evaluation at a time and takes a new cell when it is done (2)    */
+    int32_t refill_cadence;   /* pass1_fetch 4: every refill_cadence map evaluations the lanes whose
+                                 cell is done decide, store or queue it together and take new cells
+                                 together, 1..16 (2)                                                    */
     double step_ms;           /* nesf_autotune: the chosen configuration's mean step time            */
 } nesf_tuning;
 

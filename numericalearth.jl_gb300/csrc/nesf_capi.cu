@@ -82,6 +82,7 @@ static nesf_tuning default_tuning() {
     t.two_lanes = 1;
     t.io_overlap = 1;
     t.pass1_fetch = 2;
+    t.refill_cadence = 2;
     return t;
 }
 
@@ -509,8 +510,8 @@ static SolveOpts solve_opts(const nesf_solver_options& o, const nesf_context* ct
     const nesf_tuning t = ctx ? ctx->tuning : default_tuning();
     return SolveOpts{o.polish_maxiter, (float)o.path_tolerance, rho, (float)o.fallback_ratio,
                      t.solve_block, t.deferred_per_sm, t.infer_per_sm,
-                     (t.pass1_fetch >= 2 ? NESF_FETCH_SEA_ICE : 0) | (t.pass1_fetch == 3 ? NESF_FETCH_OCEAN : 0),
-                     tracer_of(ctx)};
+                     (t.pass1_fetch >= 2 ? NESF_FETCH_SEA_ICE : 0) | (t.pass1_fetch >= 3 ? NESF_FETCH_OCEAN : 0),
+                     t.pass1_fetch == 4 ? (t.refill_cadence > 0 ? t.refill_cadence : 2) : 0, tracer_of(ctx)};
 }
 
 static int check_options(const nesf_solver_options& o, const char* who) {
@@ -1734,8 +1735,10 @@ static int check_tuning(const nesf_tuning& t, const char* who) {
         return fail(NESF_ERR_ARG, "%s: infer_per_sm %d (1..8)", who, t.infer_per_sm);
     if (t.two_lanes < 0 || t.two_lanes > 1 || t.io_overlap < 0 || t.io_overlap > 1)
         return fail(NESF_ERR_ARG, "%s: two_lanes and io_overlap are 0 or 1", who);
-    if (t.pass1_fetch < 0 || t.pass1_fetch > 3)
-        return fail(NESF_ERR_ARG, "%s: pass1_fetch %d (1, 2 or 3)", who, t.pass1_fetch);
+    if (t.pass1_fetch < 0 || t.pass1_fetch > 4)
+        return fail(NESF_ERR_ARG, "%s: pass1_fetch %d (1, 2, 3 or 4)", who, t.pass1_fetch);
+    if (t.refill_cadence < 0 || t.refill_cadence > 16)
+        return fail(NESF_ERR_ARG, "%s: refill_cadence %d (1..16)", who, t.refill_cadence);
     return NESF_OK;
 }
 
@@ -1746,6 +1749,7 @@ static nesf_tuning complete_tuning(const nesf_tuning& t) {
     if (!r.deferred_per_sm) r.deferred_per_sm = d.deferred_per_sm;
     if (!r.infer_per_sm) r.infer_per_sm = d.infer_per_sm;
     if (!r.pass1_fetch) r.pass1_fetch = d.pass1_fetch;
+    if (!r.refill_cadence) r.refill_cadence = d.refill_cadence;
     return r;
 }
 
@@ -1807,6 +1811,7 @@ extern "C" int nesf_autotune(nesf_context* ctx, const nesf_coupling_step_args* a
     const bool ice = a->ai_params != nullptr;
     const bool warm = o.warm_start && o.mlp && o.precision != NESF_PLAIN_F64;
     const bool fast = o.precision != NESF_PLAIN_F64;
+    const bool adaptive = o.precision == NESF_F32_ADAPTIVE;
     nesf_tuning best = complete_tuning(start);
     double best_ms = 0.0;
     r = timed(best, &best_ms);
@@ -1817,7 +1822,8 @@ extern "C" int nesf_autotune(nesf_context* ctx, const nesf_coupling_step_args* a
         {&nesf_tuning::solve_block, {128, 96, 64, 32}, true},
         {&nesf_tuning::deferred_per_sm, {2, 4, 8, 16}, fast},
         {&nesf_tuning::infer_per_sm, {2, 4, 8}, warm},
-        {&nesf_tuning::pass1_fetch, {2, 1, 3}, fast},
+        {&nesf_tuning::pass1_fetch, {2, 1, 3, 4}, fast},
+        {&nesf_tuning::refill_cadence, {1, 2, 4, 8}, adaptive},
         {&nesf_tuning::two_lanes, {1, 0}, ice},
         {&nesf_tuning::io_overlap, {1, 0}, ice && a->io_params != nullptr},
     };

@@ -75,26 +75,48 @@ __global__ void __launch_bounds__(256) io_kernel(IOArgs<S> a, nesf_io_params p) 
     int64_t k2 = a.L.at(i, j);
     const R rho = R(p.ocean_reference_density), cpo = R(p.ocean_heat_capacity);
     const R Tfw = R(p.liquidus_freshwater_melting_temperature), slope = R(p.liquidus_slope);
-    // Part 1: frazil over the column, top level first (sea_ice_ocean_fluxes.jl:153-181)
-    R dQ = R(0), TN = R(0);
+    // Part 1: frazil over the column, top level first (sea_ice_ocean_fluxes.jl:153-181).
+    // FP32 fields: T_m - T_k cancels in a freezing level, so a level whose FP32 test is
+    // within a few ulps of T_m, or that freezes, is decided, adjusted and charged in FP64
+    // from its FP32 values (exact in FP64); dQ accumulates in FP64.
+    double dQ = 0.0;
+    R TN = R(0);
     bool top_frozen = false;
     for (int kk = p.nz; kk >= 1; kk--) {
         int64_t k3 = k2 + (int64_t)(kk - 1) * p.stride_k;
         R Tk = a.T3[k3], Sk = a.S3[k3];
         R Tm = Tfw - slope * Sk;
         bool freezing = Tk < Tm;
+        double dE = 0.0;
+        bool charged = true;
+        if (sizeof(R) < sizeof(double)) {
+            // (T_k - T_m is exact in FP32 when the two are that close)
+            const bool near = !(M<R>::fabs(Tk - Tm) > R(4.0 * 1.1920929e-7) * M<R>::fabs(Tm));
+            charged = freezing || near;
+            if (charged) {
+                const double Tm64 = p.liquidus_freshwater_melting_temperature - p.liquidus_slope * (double)Sk;
+                freezing = (double)Tk < Tm64;
+                Tm = (R)Tm64;
+                dE = (freezing ? 1.0 : 0.0) * p.ocean_reference_density * p.ocean_heat_capacity *
+                     (Tm64 - (double)Tk);
+            }
+        } else {
+            dE = (double)((freezing ? R(1) : R(0)) * rho * cpo * (Tm - Tk));
+        }
         if (PART != 1 && freezing) a.T3[k3] = Tm;
         if (PART == 2) continue;
-        R dz = R(a.dz[kk - 1]);
-        R dE = (freezing ? R(1) : R(0)) * rho * cpo * (Tm - Tk);
-        dQ -= dE * dz / R(p.dt);
+        if (sizeof(R) < sizeof(double)) {
+            if (charged) dQ -= dE * a.dz[kk - 1] / p.dt;
+        } else {
+            dQ = (double)((R)dQ - (R)dE * R(a.dz[kk - 1]) / R(p.dt));
+        }
         if (kk == p.nz) {                         // the top level after the adjustment
             TN = freezing ? Tm : Tk;
             top_frozen = freezing;
         }
     }
     if (PART == 2) return;
-    st(a.frazil, k2, dQ);
+    st(a.frazil, k2, (R)dQ);
     int64_t kN = k2 + (int64_t)(p.nz - 1) * p.stride_k;
     R SN = a.S3[kN];
     R aleph = ldr<R>(a.aleph, k2);

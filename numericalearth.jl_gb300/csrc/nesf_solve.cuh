@@ -49,6 +49,7 @@ struct SolveOpts {
     int block, deferred_per_sm, infer_per_sm;
     int fetch;             // pass 1 of the FP32 solvers where resident warps take 32 work-list entries
                            // at a time: NESF_FETCH_OCEAN | NESF_FETCH_SEA_ICE bits
+    int refill;            // adaptive pass 1 with lane refill every `refill` map evaluations (0: off)
     const Tracer* tracer;  // host side: kernel-boundary trace (null: off)
 };
 
@@ -414,11 +415,15 @@ __device__ __forceinline__ float spectral_bound(const float (&J)[N][N]) {
 
 // The FP32 sweep of a cell over the FP32 inputs of the map (c32, s32; with a skin
 // temperature the anchors `anc` and the state's fourth component tau = T_s -
-// theta_a, the delta form). x holds the start (u*, theta*, q*, tau) on entry and
-// the FP32 fixed point on return. Returns FAST_REPLAY (the cell must follow the
-// reference's FP64 iteration; `reason` says why), FAST_SOLVED (ACCEPT32 only: the
-// FP32 result is kept) or FAST_POLISH (the FP32 result needs FP64 Newton steps:
-// J and rho_est are set for them). `fp32_it` counts FP32 map evaluations.
+// theta_a, the delta form), as a state machine that one map evaluation at a time
+// advances (struct Sweep), so that a kernel can run the evaluations of cells that
+// are at different stages of their sweeps in lockstep (the refill pass 1).
+// sweep_fp32 runs one cell's machine to its end. x holds the start (u*, theta*,
+// q*, tau) and, at the end, the FP32 fixed point. Outcomes: FAST_REPLAY (the cell
+// must follow the reference's FP64 iteration; `reason` says why), FAST_SOLVED
+// (ACCEPT32 only: the FP32 result is kept) or FAST_POLISH (the FP32 result needs
+// FP64 Newton steps: J and rho_est are set for them). `fp32_it` counts FP32 map
+// evaluations.
 //
 // ACCEPT32 (ADAPTIVE): the FP32 result is kept when F contracts by at most
 // so.fp32_rho. STRICT (ADAPTIVE's passes): the sweep runs until every component,
@@ -440,46 +445,53 @@ __device__ __forceinline__ float spectral_bound(const float (&J)[N][N]) {
 // The FP32 sweep and the Jacobian's evaluations run through one loop around a
 // single inlined copy of the map, so a warp executes the same instructions for
 // all of them: the kernel's hot code stays small enough for the instruction cache.
+enum { SWEEP_CONTINUE = -1, SWEEP_DECIDE = -2 };
+
 template <bool SKIN, bool ACCEPT32, bool STRICT = ACCEPT32, bool CENTRAL = !ACCEPT32>
-__device__ __forceinline__ int sweep_fp32(const DevIface<float>& P32, const CellConst<float>& c32,
-                                          const SurfaceConst<float>& s32, const SkinAnchor<float>& anc,
-                                          float (&x)[4], const SolveOpts& so, int& fp32_it, int& reason,
-                                          float (&J)[SKIN ? 4 : 3][SKIN ? 4 : 3], float& rho_est,
-                                          const float* xw, bool* fell_back) {
-    constexpr int N = SKIN ? 4 : 3;
-    constexpr bool FWD = !SKIN;   // forward-difference J (bulk temperature)
-    const float tol = P32.tol;
-    const float x0[4] = {x[0], x[1], x[2], x[3]};
-    // warm start: the network's (u*, theta*, q*) replaces the reference's start; T_s keeps its own
-    const bool warm = xw != nullptr && isfinite(xw[0]) && isfinite(xw[1]) && isfinite(xw[2]) && xw[0] > 0.0f;
-    if (warm) { x[0] = xw[0]; x[1] = xw[1]; x[2] = xw[2]; }
-    float yw[4] = {0, 0, 0, 0};   // first iterate from the warm start while the cold start is probed
-    float rw = 0.0f;
-    int probes = 0;
-    float xb[4] = {0, 0, 0, 0};   // FWD: the last sweep point and its image, the Jacobian's base
-    float yb[4] = {0, 0, 0, 0};
-    float yp[4] = {0, 0, 0, 0};   // !FWD: F(x + h e_j) of the column in progress
-    bool decided = false;         // FWD: the decisions are made; CENTRAL's mirrored points follow
+struct Sweep {
+    static constexpr int N = SKIN ? 4 : 3;
+    static constexpr bool FWD = !SKIN;   // forward-difference J (bulk temperature)
+    float x[4], x0[4];
+    float yw[4];          // first iterate from the warm start while the cold start is probed
+    float rw;
+    float xb[4], yb[4];   // FWD: the last sweep point and its image, the Jacobian's base
+    float yp[4];          // !FWD: F(x + h e_j) of the column in progress
+    float J[N][N];
     SweepTrace tr;
-    tr.d[0] = tr.d[1] = tr.d[2] = 0.0f;
-    tr.lam = 1.0f;
-    float prev = M<float>::inf();
-    int rising = 0;
-    bool stalled = false;  // the sweep ended on the rising-drift rule
-    int it = 0;            // sweep iterations
-    int phase = 0;         // 0 sweep; 1 cold-start probe; FWD: 2 + j: F(x_b + h e_j), N + 2 + j:
-                           // F(x_b - h e_j); !FWD: 2 + 2j / 3 + 2j: F(x + h e_j) / F(x - h e_j)
-    float h = 0.0f;
-    float cond = 1.0f;     // condition of the anchored differences at the last sweep iterate
-    const int limit = P32.maxiter;
-sweep:
-#pragma unroll 1
-    for (;;) {
-        float xin[4] = {x[0], x[1], x[2], x[3]};
-        if (phase == 1) {
+    float prev, h, cond, rho_est;
+    int probes, rising, it, phase, fp32_it, reason;
+    // phase 0 sweep; 1 cold-start probe; FWD: 2 + j: F(x_b + h e_j), N + 2 + j: F(x_b - h e_j);
+    // !FWD: 2 + 2j / 3 + 2j: F(x + h e_j) / F(x - h e_j)
+    bool warm, decided, stalled, fell_back;   // decided (FWD): CENTRAL's mirrored points follow;
+                                              // stalled: the sweep ended on the rising-drift rule
+
+    // Start from x (the reference's start) or, with a warm start, the network's (u*, theta*,
+    // q*) guess xw; T_s keeps its own.
+    __device__ __forceinline__ void begin(const float (&start)[4], const float* xw) {
 #pragma unroll
-            for (int k = 0; k < 4; k++) xin[k] = x0[k];
+        for (int k = 0; k < 4; k++) {
+            x[k] = x0[k] = start[k];
+            yw[k] = xb[k] = yb[k] = yp[k] = 0.0f;
         }
+        warm = xw != nullptr && isfinite(xw[0]) && isfinite(xw[1]) && isfinite(xw[2]) && xw[0] > 0.0f;
+        if (warm) { x[0] = xw[0]; x[1] = xw[1]; x[2] = xw[2]; }
+        rw = 0.0f;
+        probes = 0;
+        decided = stalled = fell_back = false;
+        tr.d[0] = tr.d[1] = tr.d[2] = 0.0f;
+        tr.lam = 1.0f;
+        prev = M<float>::inf();
+        rising = it = phase = fp32_it = 0;
+        reason = -1;
+        h = 0.0f;
+        cond = 1.0f;      // condition of the anchored differences at the last sweep iterate
+        rho_est = 0.0f;
+    }
+
+    // The point the map is evaluated at next.
+    __device__ __forceinline__ void input(float (&xin)[4]) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) xin[k] = phase == 1 ? x0[k] : x[k];
         if (phase >= 2) {
             const bool minus = FWD ? phase >= N + 2 : (phase & 1) != 0;
             const int jj = FWD ? phase - (minus ? N + 2 : 2) : (phase - 2) >> 1;
@@ -489,16 +501,15 @@ sweep:
                 if (k == jj) { h = jac_step(k, xin[k]); xin[k] += minus ? -h : h; }
             }
         }
-        float yu = xin[0], yt = xin[1], yq = xin[2], yT = xin[3];
-        if (SKIN) {
-            float cd = 1.0f;
-            iterate_skin_delta<float>(P32, c32, anc, yu, yt, yq, yT, &cd);
-            if (phase == 0) cond = cd;
-        } else {
-            SurfaceConst<float> sv = s32;
-            iterate_state<float, false>(P32, c32, sv, yu, yt, yq);
-        }
-        float y[4] = {yu, yt, yq, yT};
+    }
+
+    // Takes y = F(xin) (cd: the condition of the anchored differences of that evaluation).
+    // Returns SWEEP_CONTINUE (evaluate the next input), SWEEP_DECIDE (the Jacobian is
+    // complete: call decide) or an outcome.
+    __device__ __forceinline__ int advance(const float (&xin)[4], const float (&y)[4], float cd,
+                                           const DevIface<float>& P32, const SolveOpts& so) {
+        const float tol = P32.tol;
+        if (SKIN && phase == 0) cond = cd;
         if (phase == 1) {
             // cold-start fallback: keep the warm start unless its first residual, relative to
             // its state, exceeds fallback_ratio times the cold start's relative first residual
@@ -506,16 +517,17 @@ sweep:
             float rc = fabsf(y[0] - x0[0]) + fabsf(y[1] - x0[1]) + fabsf(y[2] - x0[2]);
             float nw = fabsf(x[0]) + fabsf(x[1]) + fabsf(x[2]), nc = fabsf(x0[0]) + fabsf(x0[1]) + fabsf(x0[2]);
             const bool cold = !(rw * nc <= so.fallback_ratio * rc * nw);
-            if (cold && fell_back) *fell_back = true;
-            const float* from = cold ? x0 : x;
-            const float* to = cold ? y : yw;
-            tr.d[0] = fabsf(to[0] - from[0]); tr.d[1] = fabsf(to[1] - from[1]); tr.d[2] = fabsf(to[2] - from[2]);
+            if (cold) fell_back = true;
+            // from (cold ? x0 : x) to (cold ? y : yw), element by element (no pointer to a
+            // member array, which would keep the whole state out of registers)
+#pragma unroll
+            for (int k = 0; k < 3; k++) tr.d[k] = fabsf((cold ? y[k] : yw[k]) - (cold ? x0[k] : x[k]));
             tr.lam = 1.0f;
             prev = cold ? rc : rw;
 #pragma unroll
-            for (int k = 0; k < 4; k++) x[k] = to[k];
+            for (int k = 0; k < 4; k++) x[k] = cold ? y[k] : yw[k];
             phase = 0;
-            continue;
+            return SWEEP_CONTINUE;
         }
         if (phase == 0) {
             it++;
@@ -528,7 +540,7 @@ sweep:
                 for (int k = 0; k < 4; k++) yw[k] = y[k];
                 rw = drift;
                 phase = 1;
-                continue;
+                return SWEEP_CONTINUE;
             }
 #pragma unroll
             for (int k = 0; k < 4; k++) {
@@ -555,16 +567,20 @@ sweep:
                 // calm cells: the reference's absolute drift rule leaves tol / u* of relative room
                 if (fabsf(x[0]) * so.path_tol < tol) { fp32_it = it; reason = REPLAY_CALM; return FAST_REPLAY; }
                 phase = 2;
-            } else if (it >= limit) {
+            } else if (it >= P32.maxiter) {
                 fp32_it = it;
                 reason = REPLAY_NO_FP32;
                 return FAST_REPLAY;                       // no FP32 convergence
             }
-        } else if (!FWD && !(phase & 1)) {
+            return SWEEP_CONTINUE;
+        }
+        if (!FWD && !(phase & 1)) {
 #pragma unroll
             for (int k = 0; k < 4; k++) yp[k] = y[k];
             phase++;
-        } else if (!FWD) {
+            return SWEEP_CONTINUE;
+        }
+        if (!FWD) {
             // central difference: column (phase - 3) / 2
             const int jj = (phase - 3) >> 1;
             const float inv2h = 0.5f / h;
@@ -573,8 +589,9 @@ sweep:
 #pragma unroll
                 for (int k = 0; k < N; k++)
                     if (k == jj) J[ii][k] = (yp[ii] - y[ii]) * inv2h;
-            if (++phase == 2 * N + 2) break;
-        } else if (phase < N + 2) {
+            return ++phase == 2 * N + 2 ? SWEEP_DECIDE : SWEEP_CONTINUE;
+        }
+        if (phase < N + 2) {
             // forward difference: column phase - 2
             const int jj = phase - 2;
             const float invh = 1.0f / h;
@@ -583,73 +600,127 @@ sweep:
 #pragma unroll
                 for (int k = 0; k < N; k++)
                     if (k == jj) J[ii][k] = (y[ii] - yb[ii]) * invh;
-            if (++phase == N + 2) break;
-        } else {
-            // the mirrored point of column phase - N - 2: the forward column becomes the central
-            // difference (F(x_b + h e_j) - F(x_b - h e_j)) / 2h, F(x_b + h e_j) = y_b + h J e_j
-            const int jj = phase - (N + 2);
-            const float inv2h = 0.5f / h;
-#pragma unroll
-            for (int ii = 0; ii < N; ii++)
-#pragma unroll
-                for (int k = 0; k < N; k++)
-                    if (k == jj) J[ii][k] = (J[ii][k] * h + yb[ii] - y[ii]) * inv2h;
-            if (++phase == 2 * N + 2) break;
+            return ++phase == N + 2 ? SWEEP_DECIDE : SWEEP_CONTINUE;
         }
-    }
-    if (FWD && decided) {   // CENTRAL: the mirrored points are in J; the decisions were made before them
+        // the mirrored point of column phase - N - 2: the forward column becomes the central
+        // difference (F(x_b + h e_j) - F(x_b - h e_j)) / 2h, F(x_b + h e_j) = y_b + h J e_j
+        const int jj = phase - (N + 2);
+        const float inv2h = 0.5f / h;
+#pragma unroll
+        for (int ii = 0; ii < N; ii++)
+#pragma unroll
+            for (int k = 0; k < N; k++)
+                if (k == jj) J[ii][k] = (J[ii][k] * h + yb[ii] - y[ii]) * inv2h;
+        if (++phase < 2 * N + 2) return SWEEP_CONTINUE;
+        // CENTRAL: the mirrored points are in J; the decisions were made before them
         fp32_it += N;
         return FAST_POLISH;
     }
-    fp32_it = it + probes + (FWD ? N : 2 * N);
-    // ---- contraction rate of F at the solution
-    rho_est = spectral_bound<N>(J);
-    if (!(rho_est < 0.995f)) { reason = REPLAY_SLOW; return FAST_REPLAY; }
-    // ---- the reference's stopping error along its slowest mode: e = rho / (1 - rho) d, |d|_1 < tol.
-    // Mode shape: power iteration from the last drift (each component's largest share over the
-    // last two iterates, which a rotating complex mode alternates between), or the last drift.
-    float v[4] = {tr.d[0], tr.d[1], tr.d[2], 0.0f};
-    float vn = v[0] + v[1] + v[2];
-    if (vn > 0.0f) {
-        float frac[3] = {v[0] / vn, v[1] / vn, v[2] / vn};
+
+    // The decisions once the Jacobian is complete: an outcome, or SWEEP_CONTINUE when
+    // CENTRAL's mirrored points are to be evaluated first.
+    __device__ __forceinline__ int decide(const SolveOpts& so, const DevIface<float>& P32) {
+        const float tol = P32.tol;
+        fp32_it = it + probes + (FWD ? N : 2 * N);
+        // ---- contraction rate of F at the solution
+        rho_est = spectral_bound<N>(J);
+        if (!(rho_est < 0.995f)) { reason = REPLAY_SLOW; return FAST_REPLAY; }
+        // ---- the reference's stopping error along its slowest mode: e = rho / (1 - rho) d, |d|_1 < tol.
+        // Mode shape: power iteration from the last drift (each component's largest share over the
+        // last two iterates, which a rotating complex mode alternates between), or the last drift.
+        float v[4] = {tr.d[0], tr.d[1], tr.d[2], 0.0f};
+        float vn = v[0] + v[1] + v[2];
+        if (vn > 0.0f) {
+            float frac[3] = {v[0] / vn, v[1] / vn, v[2] / vn};
 #pragma unroll
-        for (int k = 0; k < 8; k++) {
-            float w[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            for (int k = 0; k < 8; k++) {
+                float w[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
-            for (int ii = 0; ii < N; ii++)
+                for (int ii = 0; ii < N; ii++)
 #pragma unroll
-                for (int jj = 0; jj < N; jj++) w[ii] += J[ii][jj] * v[jj];
-            float wn = 0.0f;
+                    for (int jj = 0; jj < N; jj++) w[ii] += J[ii][jj] * v[jj];
+                float wn = 0.0f;
 #pragma unroll
-            for (int ii = 0; ii < N; ii++) wn += fabsf(w[ii]);
-            if (!(wn > 0.0f)) break;          // J nilpotent on the drift: keep the drift's shape
-            float inv = 1.0f / wn;
+                for (int ii = 0; ii < N; ii++) wn += fabsf(w[ii]);
+                if (!(wn > 0.0f)) break;          // J nilpotent on the drift: keep the drift's shape
+                float inv = 1.0f / wn;
 #pragma unroll
-            for (int ii = 0; ii < N; ii++) v[ii] = w[ii] * inv;   // signed: J's modes, not |J|'s
-            float mn = fabsf(v[0]) + fabsf(v[1]) + fabsf(v[2]);
-            if (k >= 6 && mn > 0.0f) {
+                for (int ii = 0; ii < N; ii++) v[ii] = w[ii] * inv;   // signed: J's modes, not |J|'s
+                float mn = fabsf(v[0]) + fabsf(v[1]) + fabsf(v[2]);
+                if (k >= 6 && mn > 0.0f) {
 #pragma unroll
-                for (int ii = 0; ii < 3; ii++) frac[ii] = k == 6 ? fabsf(v[ii]) / mn : fmaxf(frac[ii], fabsf(v[ii]) / mn);
+                    for (int ii = 0; ii < 3; ii++)
+                        frac[ii] = k == 6 ? fabsf(v[ii]) / mn : fmaxf(frac[ii], fabsf(v[ii]) / mn);
+                }
             }
+            float kb = rho_est / (1.0f - rho_est) * tol;
+#pragma unroll
+            for (int ii = 0; ii < 3; ii++)
+                if (!(kb * frac[ii] <= so.path_tol * fmaxf(fabsf(x[ii]), state_floor(ii)))) {
+                    reason = REPLAY_BOUND;
+                    return FAST_REPLAY;
+                }
         }
-        float kb = rho_est / (1.0f - rho_est) * tol;
+        // ---- ADAPTIVE: keep the FP32 result of a quiet, well-contracting cell
+        // FP32 rounding of the anchored terms (~1e-7 of each), amplified by their
+        // cancellation and by 1 / (1 - rho), must stay within path_tol
+        if (ACCEPT32 && !stalled && rho_est <= so.fp32_rho && cond * 1.2e-7f <= so.path_tol * (1.0f - rho_est))
+            return FAST_SOLVED;
+        if (FWD && CENTRAL) {   // back to the map for the mirrored points (one copy of the map)
+            decided = true;
+            return SWEEP_CONTINUE;
+        }
+        return FAST_POLISH;
+    }
+};
+
+// One FP32 evaluation of the map at xin (the sweep's inputs); cd receives the
+// condition number of the anchored differences (skin temperature; 1 otherwise).
+template <bool SKIN>
+__device__ __forceinline__ void sweep_map(const DevIface<float>& P32, const CellConst<float>& c32,
+                                          const SurfaceConst<float>& s32, const SkinAnchor<float>& anc,
+                                          const float (&xin)[4], float (&y)[4], float& cd) {
+    float yu = xin[0], yt = xin[1], yq = xin[2], yT = xin[3];
+    cd = 1.0f;
+    if (SKIN) {
+        iterate_skin_delta<float>(P32, c32, anc, yu, yt, yq, yT, &cd);
+    } else {
+        SurfaceConst<float> sv = s32;
+        iterate_state<float, false>(P32, c32, sv, yu, yt, yq);
+    }
+    y[0] = yu; y[1] = yt; y[2] = yq; y[3] = yT;
+}
+
+template <bool SKIN, bool ACCEPT32, bool STRICT = ACCEPT32, bool CENTRAL = !ACCEPT32>
+__device__ __forceinline__ int sweep_fp32(const DevIface<float>& P32, const CellConst<float>& c32,
+                                          const SurfaceConst<float>& s32, const SkinAnchor<float>& anc,
+                                          float (&x)[4], const SolveOpts& so, int& fp32_it, int& reason,
+                                          float (&J)[SKIN ? 4 : 3][SKIN ? 4 : 3], float& rho_est,
+                                          const float* xw, bool* fell_back) {
+    constexpr int N = SKIN ? 4 : 3;
+    Sweep<SKIN, ACCEPT32, STRICT, CENTRAL> sw;
+    sw.begin(x, xw);
+    int out;
+#pragma unroll 1
+    for (;;) {
+        float xin[4], y[4], cd;
+        sw.input(xin);
+        sweep_map<SKIN>(P32, c32, s32, anc, xin, y, cd);
+        out = sw.advance(xin, y, cd, P32, so);
+        if (out == SWEEP_DECIDE) out = sw.decide(so, P32);
+        if (out != SWEEP_CONTINUE) break;
+    }
 #pragma unroll
-        for (int ii = 0; ii < 3; ii++)
-            if (!(kb * frac[ii] <= so.path_tol * fmaxf(fabsf(x[ii]), state_floor(ii)))) {
-                reason = REPLAY_BOUND;
-                return FAST_REPLAY;
-            }
-    }
-    // ---- ADAPTIVE: keep the FP32 result of a quiet, well-contracting cell
-    // FP32 rounding of the anchored terms (~1e-7 of each), amplified by their
-    // cancellation and by 1 / (1 - rho), must stay within path_tol
-    if (ACCEPT32 && !stalled && rho_est <= so.fp32_rho && cond * 1.2e-7f <= so.path_tol * (1.0f - rho_est))
-        return FAST_SOLVED;
-    if (FWD && CENTRAL) {   // back into the loop for the mirrored points (one copy of the map)
-        decided = true;
-        goto sweep;
-    }
-    return FAST_POLISH;
+    for (int k = 0; k < 4; k++) x[k] = sw.x[k];
+#pragma unroll
+    for (int ii = 0; ii < N; ii++)
+#pragma unroll
+        for (int jj = 0; jj < N; jj++) J[ii][jj] = sw.J[ii][jj];
+    fp32_it = sw.fp32_it;
+    if (sw.reason >= 0) reason = sw.reason;
+    rho_est = sw.rho_est;
+    if (fell_back && sw.fell_back) *fell_back = true;
+    return out;
 }
 
 // FP64 Newton steps on x = F(x) from the FP32 fixed point x of sweep_fp32 (J and

@@ -55,6 +55,10 @@ void oracle_set_humidity_ulp_shift(int32_t n, int32_t carry) {
  * cancels, the sensible heat responds to it by ulp(theta_a) / |theta_a - T_s|. */
 static int32_t g_theta_ulp_shift = 0;
 void oracle_set_temperature_ulp_shift(int32_t n) { g_theta_ulp_shift = n; }
+/* ... and on each iterate's interface temperature T_s (a skin temperature's balance is
+ * rounded differently by a GPU that contracts its multiply-adds). */
+static int32_t g_ts_ulp_shift = 0;
+void oracle_set_interface_temperature_ulp_shift(int32_t n) { g_ts_ulp_shift = n; }
 int32_t oracle_get_threads(void) {
 #ifdef _OPENMP
     return g_threads > 0 ? g_threads : omp_get_max_threads();
@@ -570,6 +574,7 @@ static double interface_humidity(const nesf_interface_params* p, const cell_in* 
 /* iterate_interface_state (compute_interface_state.jl:69-122) */
 static istate iterate_state(const nesf_interface_params* p, const cell_in* c, const istate* prev) {
     double Ts = interface_temperature(p, c, prev);
+    for (int32_t k = 0; k < g_ts_ulp_shift; k++) Ts = nextafter(Ts, INFINITY);
     double q_iter = interface_humidity(p, c, Ts, prev);
     double qs = q_iter;
     for (int32_t k = 0; k < g_humidity_ulp_shift; k++) qs = nextafter(qs, INFINITY);

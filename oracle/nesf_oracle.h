@@ -64,6 +64,7 @@ int oracle_apply_air_land_radiative_fluxes(const nesf_land_radiation_params* p, 
 void oracle_set_threads(int32_t n);
 void oracle_set_humidity_ulp_shift(int32_t n, int32_t carry);   /* conditioning probe for tests; 0 = off */
 void oracle_set_temperature_ulp_shift(int32_t n);
+void oracle_set_interface_temperature_ulp_shift(int32_t n);
 int32_t oracle_get_threads(void);
 
 #ifdef __cplusplus

@@ -64,6 +64,7 @@ def load():
             "oracle_set_threads": (None, [C.c_int32]),
             "oracle_set_humidity_ulp_shift": (None, [C.c_int32, C.c_int32]),
             "oracle_set_temperature_ulp_shift": (None, [C.c_int32]),
+            "oracle_set_interface_temperature_ulp_shift": (None, [C.c_int32]),
             "oracle_get_threads": (C.c_int32, []),
         }
         for name, (res, args) in sig.items():
@@ -132,30 +133,35 @@ def humidity_ulp_shift(n, carry):
 
 
 @contextlib.contextmanager
-def temperature_ulp_shift(n):
-    """Within the block every iterate's air potential temperature theta_a is moved n units in
-    the last place (oracle_set_temperature_ulp_shift): the temperature side of the probe."""
+def temperature_ulp_shift(n, interface=False):
+    """Within the block every iterate's air potential temperature theta_a (or, with interface,
+    its interface temperature T_s) is moved n units in the last place
+    (oracle_set_temperature_ulp_shift / oracle_set_interface_temperature_ulp_shift): the
+    temperature side of the probe."""
     lib = load()
-    lib.oracle_set_temperature_ulp_shift(n)
+    setter = lib.oracle_set_interface_temperature_ulp_shift if interface else lib.oracle_set_temperature_ulp_shift
+    setter(n)
     try:
         yield
     finally:
-        lib.oracle_set_temperature_ulp_shift(0)
+        setter(0)
 
 
 def conditioning_response(run, ref, keys, shift=1024, view=None):
     """Per-cell response of the oracle's outputs to one unit in the last place of its interface
-    humidity (with and without carrying the change into the next iterate) and of theta_a: the
-    largest relative change over the three probes, each under a `shift`-ulp move, divided by
-    `shift` (a single ulp rounds away in some cells). `run()` returns the oracle's outputs;
-    `view(key, array)` selects the cells compared (default: all)."""
+    humidity (with and without carrying the change into the next iterate), of theta_a and of
+    the interface temperature T_s: the largest relative change over the four probes, each
+    under a `shift`-ulp move, divided by `shift` (a single ulp rounds away in some cells).
+    `run()` returns the oracle's outputs; `view(key, array)` selects the cells compared
+    (default: all)."""
     view = view or (lambda k, a: a)
     outs = []
     for carry in (False, True):
         with humidity_ulp_shift(shift, carry):
             outs.append(run())
-    with temperature_ulp_shift(shift):
-        outs.append(run())
+    for interface in (False, True):
+        with temperature_ulp_shift(shift, interface):
+            outs.append(run())
     resp = {}
     for k in keys:
         r = np.asarray(view(k, ref[k]), np.float64)

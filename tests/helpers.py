@@ -39,7 +39,7 @@ def widen(arrays):
 def assert_conditioned(gpu, ref, keys, response, label="", units=4.0):
     """The plain FP64 parity bar, per cell: relative error (floor 1e-6 of the field's largest
     magnitude) <= 1e-12, or `units` times the oracle's own response to one unit in the last
-    place of its interface humidity or of theta_a where that is larger (oracle
+    place of its interface humidity, of theta_a or of T_s where that is larger (oracle
     conditioning_response). Where q_a - q_s or theta_a - T_s nearly cancels, a last-place
     difference of a libm result or of a contracted multiply-add between the CPU and the GPU
     moves the reference's own answer by that much; elsewhere the bar is 1e-12."""

@@ -155,7 +155,8 @@ def test_config2_coupled_step_fp32_graph(oracle):
     st = syn.coupled_1440()
     assert (st.layout.nx, st.layout.ny) == (1440, 600)
     sp = _specs()
-    m = CoupledModel(st, **sp)
+    m = CoupledModel(st, ao_spec=sp["ao_spec"], ai_spec=sp["ai_spec"], io_spec=sp["io_spec"],
+                     assembly_spec=sp["asm_spec"])
     m.capture("f32_adaptive")
     m.reset()
     m.graph_step()
@@ -200,7 +201,8 @@ def test_config2_coupled_step_plain_f64(oracle):
     from oracle import band as OB
     st = syn.coupled_1440(dtype=np.float64)
     sp = _specs()
-    m = CoupledModel(st, **sp)
+    m = CoupledModel(st, ao_spec=sp["ao_spec"], ai_spec=sp["ai_spec"], io_spec=sp["io_spec"],
+                     assembly_spec=sp["asm_spec"])
     m.iterations = {k: torch.zeros(st.layout.shape, dtype=torch.int32, device="cuda") for k in ("ao", "ai")}
     m.reset()
     m.update_state("f64")
