@@ -794,12 +794,11 @@ typedef struct {
     int32_t io_overlap;       /* coupling step: sea-ice-ocean fluxes beside the sea-ice pass 1 (1)      */
     int32_t pass1_fetch;      /* pass 1 of the FP32 solvers: 1 one thread per work-list entry; 2 in the
                                  sea-ice solve, 3 in the sea-ice and ocean solves, the resident blocks
-                                 only, each warp taking 32 entries at a time; 4 as 3, and the adaptive
-                                 solver's pass 1 with lane refill: each lane advances its own cell one
-                                 map evaluation at a time and takes a new cell when it is done (2)    */
-    int32_t refill_cadence;   /* pass1_fetch 4: every refill_cadence map evaluations the lanes whose
-                                 cell is done decide, store or queue it together and take new cells
-                                 together, 1..16 (2)                                                    */
+                                 only, each warp taking 32 entries at a time; 4 as 3 with lane refill
+                                 in the adaptive solver's pass 1: a warp takes new entries for its
+                                 idle lanes as soon as refill_lanes of them are idle (2)              */
+    int32_t refill_lanes;     /* pass1_fetch 4: idle lanes that make a warp take new entries, 1..32
+                                 (32: warp fetching) (8)                                                */
     double step_ms;           /* nesf_autotune: the chosen configuration's mean step time            */
 } nesf_tuning;
 

@@ -277,77 +277,37 @@ __global__ void __launch_bounds__(128, PREC == NESF_F32_ADAPTIVE ? 5 : 1) ai_ker
     }
 }
 
-// Pass 1 of the adaptive solver with lane refill (SolveOpts::refill = D > 0, convergence
-// stopping rule): as ao_refill_kernel -- each lane advances its cell's FP32 sweep one map
-// evaluation per trip; every D trips the finished lanes decide, store or queue their
-// cells together and the empty lanes take the next work-list entries together. Each
-// cell's arithmetic is that of ai_kernel<ADAPTIVE>.
+// The atmosphere-sea-ice cell of the adaptive pass 1 (adaptive_pass1's adapter).
 template <class S, bool SKIN>
-__global__ void __launch_bounds__(128, 5) ai_refill_kernel(AIArgs<S> a, DevIface<double> P64, DevIface<float> P32,
-                                                           SolveOpts so, WorkList wl, ReplayQueue rq,
-                                                           const float* guess, DevStats* stats) {
-    const int nxr = a.L.nx + 2;
-    const int lane = threadIdx.x & 31;
-    const unsigned total = wl.count[0] + wl.count[1];
-    const int cadence = so.refill;
-    Sweep<SKIN, true> sw;
+struct AIAdaptiveCell {
+    const AIArgs<S>& a;
+    const DevIface<double>& P64;
+    const DevIface<float>& P32;
     Fast32 f;
-    int64_t k = 0;
-    uint32_t id = 0;
-    bool have = false, pending = false, alive = true;
-    int outcome = SWEEP_CONTINUE;
-#pragma unroll 1
-    for (int trip = 0;; trip++) {
-        if (trip % cadence == 0) {
-            if (pending) {
-                if (outcome == SWEEP_DECIDE) outcome = sw.decide(so, P32);
-                replay_push(rq, outcome == FAST_REPLAY, id);
-                polish_push(rq, outcome == FAST_POLISH, id);
-                if (outcome == FAST_SOLVED) {
-                    ai_store_fast(P64, a, k, f, sw.x[0], sw.x[1], sw.x[2], SKIN ? f.tha + (double)sw.x[3] : f.Ts0,
-                                  sw.fp32_it);
-                    if (stats) stats_add(stats, true, true, sw.fp32_it, false, false, 0, false, sw.fell_back);
-                } else if (stats) {
-                    stats_add(stats, true, false, 0, false, false, 0, outcome == FAST_REPLAY, sw.fell_back);
-                    if (outcome == FAST_REPLAY) stats_replay_reason(stats, sw.reason);
-                }
-                have = pending = false;
-            }
-            const bool need = alive && !have;
-            const unsigned nb = __ballot_sync(0xffffffffu, need);
-            if (nb) {
-                const int leader = __ffs(nb) - 1;
-                unsigned base = 0;
-                if (lane == leader) base = atomicAdd(&rq.count[3], (unsigned)__popc(nb));
-                base = __shfl_sync(0xffffffffu, base, leader);
-                if (need) {
-                    const unsigned w = base + __popc(nb & ((1u << lane) - 1u));
-                    if (w < total) {
-                        const int64_t r = worklist_get(wl, 0, w);
-                        const int i = (int)(r % nxr), j = (int)(r / nxr);
-                        k = a.L.at(i, j);
-                        id = (uint32_t)r;
-                        float xw[3];
-                        const float* warm = mlp::guess_at(guess, worklist_slot(wl, 0, w), xw);
-                        ai_load_fast<S, SKIN>(P64, P32, a, k, f);
-                        const float start[4] = {1e-4f, 1e-4f, 1e-4f, SKIN ? (float)(f.Ts0 - f.tha) : 0.0f};  // :127
-                        sw.begin(start, warm);
-                        have = true;
-                    } else {
-                        alive = false;
-                    }
-                }
-            }
-            if (!__any_sync(0xffffffffu, have)) break;
-        }
-        if (have && !pending) {
-            float xin[4], y[4], cd;
-            sw.input(xin);
-            sweep_map<SKIN>(P32, f.c, f.s, f.anc, xin, y, cd);
-            outcome = sw.advance(xin, y, cd, P32, so);
-            pending = outcome != SWEEP_CONTINUE;
-        }
+    int64_t k;
+    uint32_t id;
+    __device__ __forceinline__ void load(int64_t r, float (&start)[4]) {
+        const int nxr = a.L.nx + 2;
+        const int i = (int)(r % nxr), j = (int)(r / nxr);
+        k = a.L.at(i, j);
+        id = (uint32_t)r;
+        ai_load_fast<S, SKIN>(P64, P32, a, k, f);
+        start[0] = start[1] = start[2] = 1e-4f;   // atmosphere_sea_ice_fluxes.jl:127
+        start[3] = SKIN ? (float)(f.Ts0 - f.tha) : 0.0f;
     }
+    __device__ __forceinline__ void store(const float (&x)[4], int iters) {
+        ai_store_fast(P64, a, k, f, x[0], x[1], x[2], SKIN ? f.tha + (double)x[3] : f.Ts0, iters);
+    }
+};
+
+// Pass 1 of the adaptive solver under the convergence stopping rule: adaptive_pass1 with the
+// schedule of SolveOpts::fetch / refill.
+template <class S, bool SKIN>
+__global__ void __launch_bounds__(128, 5) ai_adaptive_kernel(AIArgs<S> a, DevIface<double> P64, DevIface<float> P32,
+                                                             SolveOpts so, WorkList wl, ReplayQueue rq,
+                                                             const float* guess, DevStats* stats) {
+    AIAdaptiveCell<S, SKIN> cell{a, P64, P32};
+    adaptive_pass1<SKIN>(cell, P32, so, wl, rq, guess, stats, (so.fetch & NESF_FETCH_SEA_ICE) != 0);
 }
 
 // Pass 1b (ADAPTIVE): the cells whose FP32 result was not kept, packed, through pass
@@ -458,15 +418,16 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     ai_kernel<S, PR, SK><<<pass1_grid(ai_kernel<S, PR, SK>, grid, block, sms, PR != NESF_PLAIN_F64 && (so.fetch & NESF_FETCH_SEA_ICE)), \
                            block, 0, stream>>>(a, P64, P32, so, wl, rq, G, stats)
 #define NESF_AI_SKIN(PR, G) do { if (skin) NESF_AI_LAUNCH(PR, true, G); else NESF_AI_LAUNCH(PR, false, G); } while (0)
-    // lane refill: the adaptive pass 1 under the convergence stopping rule
-    const bool refill = adaptive && so.refill > 0 && P64.stop_kind == NESF_STOP_CONVERGENCE;
+    // the adaptive pass 1 under the convergence stopping rule: every schedule in one kernel
+    const bool one = adaptive && P64.stop_kind == NESF_STOP_CONVERGENCE;
+    const bool fetch_ai = (so.fetch & NESF_FETCH_SEA_ICE) != 0;
     if (prec == NESF_PLAIN_F64) NESF_AI_SKIN(NESF_PLAIN_F64, nullptr);
-    else if (refill && skin)
-        ai_refill_kernel<S, true><<<pass1_grid(ai_refill_kernel<S, true>, grid, block, sms, true), block, 0,
-                                    stream>>>(a, P64, P32, so, wl, rq, guess, stats);
-    else if (refill)
-        ai_refill_kernel<S, false><<<pass1_grid(ai_refill_kernel<S, false>, grid, block, sms, true), block, 0,
-                                     stream>>>(a, P64, P32, so, wl, rq, guess, stats);
+    else if (one && skin)
+        ai_adaptive_kernel<S, true><<<pass1_grid(ai_adaptive_kernel<S, true>, grid, block, sms, fetch_ai), block, 0,
+                                      stream>>>(a, P64, P32, so, wl, rq, guess, stats);
+    else if (one)
+        ai_adaptive_kernel<S, false><<<pass1_grid(ai_adaptive_kernel<S, false>, grid, block, sms, fetch_ai), block,
+                                       0, stream>>>(a, P64, P32, so, wl, rq, guess, stats);
     else if (adaptive) NESF_AI_SKIN(NESF_F32_ADAPTIVE, guess);
     else NESF_AI_SKIN(NESF_F32_POLISH, guess);
 #undef NESF_AI_SKIN

@@ -293,81 +293,37 @@ __global__ void __launch_bounds__(128, ENS ? 4 : (PREC == NESF_F32_ADAPTIVE ? 5 
     }
 }
 
-// Pass 1 of the adaptive solver with lane refill (SolveOpts::refill = D > 0; one member,
-// convergence stopping rule): the resident blocks only. Each lane holds one cell and
-// advances its FP32 sweep one map evaluation per trip, whatever stage (sweep,
-// cold-start probe, Jacobian column) the cell is at, so the lanes of a warp evaluate
-// the map in lockstep on cells at different stages. Every D trips the lanes whose
-// sweep is done take the decisions, store or queue their cells together, and the
-// empty lanes take the next work-list entries (counter rq.count[3]) together: a cell
-// that converges early frees its lane for a new cell instead of idling it until the
-// warp's slowest cell is done. Each cell's arithmetic is that of ao_kernel<ADAPTIVE>.
+// The atmosphere-ocean cell of the adaptive pass 1 (adaptive_pass1's adapter).
 template <class S, bool SKIN>
-__global__ void __launch_bounds__(128, 5) ao_refill_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
-                                                           SolveOpts so, WorkList wl, ReplayQueue rq,
-                                                           const float* guess, DevStats* stats) {
-    const int nxr = a.L.nx + 2;
-    const int lane = threadIdx.x & 31;
-    const unsigned total = wl.count[0] + wl.count[1];
-    const int cadence = so.refill;
-    Sweep<SKIN, true> sw;
+struct AOAdaptiveCell {
+    const AOArgs<S>& a;
+    const DevIface<double>& P64;
+    const DevIface<float>& P32;
     Fast32 f;
-    int64_t k = 0;
-    uint32_t id = 0;
-    bool have = false, pending = false, alive = true;
-    int outcome = SWEEP_CONTINUE;
-#pragma unroll 1
-    for (int trip = 0;; trip++) {
-        if (trip % cadence == 0) {
-            if (pending) {
-                if (outcome == SWEEP_DECIDE) outcome = sw.decide(so, P32);
-                replay_push(rq, outcome == FAST_REPLAY, id);
-                polish_push(rq, outcome == FAST_POLISH, id);
-                if (outcome == FAST_SOLVED) {
-                    ao_store_fast(P64, P32, a, k, f, sw.x[0], sw.x[1], sw.x[2],
-                                  SKIN ? f.tha + (double)sw.x[3] : f.Ts0, sw.fp32_it);
-                    if (stats) stats_add(stats, true, true, sw.fp32_it, false, false, 0, false, sw.fell_back);
-                } else if (stats) {
-                    stats_add(stats, true, false, 0, false, false, 0, outcome == FAST_REPLAY, sw.fell_back);
-                    if (outcome == FAST_REPLAY) stats_replay_reason(stats, sw.reason);
-                }
-                have = pending = false;
-            }
-            const bool need = alive && !have;
-            const unsigned nb = __ballot_sync(0xffffffffu, need);
-            if (nb) {
-                const int leader = __ffs(nb) - 1;
-                unsigned base = 0;
-                if (lane == leader) base = atomicAdd(&rq.count[3], (unsigned)__popc(nb));
-                base = __shfl_sync(0xffffffffu, base, leader);
-                if (need) {
-                    const unsigned w = base + __popc(nb & ((1u << lane) - 1u));
-                    if (w < total) {
-                        const int64_t r = worklist_get(wl, 0, w);
-                        const int i = (int)(r % nxr), j = (int)(r / nxr);
-                        k = a.L.at(i, j);
-                        id = (uint32_t)r;
-                        float xw[3];
-                        const float* warm = mlp::guess_at(guess, worklist_slot(wl, 0, w), xw);
-                        ao_load_fast<S, SKIN>(P64, P32, a, k, f);
-                        const float start[4] = {1e-4f, 1e-4f, 1e-4f, SKIN ? f.anc.dTi : 0.0f};   // :132
-                        sw.begin(start, warm);
-                        have = true;
-                    } else {
-                        alive = false;
-                    }
-                }
-            }
-            if (!__any_sync(0xffffffffu, have)) break;
-        }
-        if (have && !pending) {
-            float xin[4], y[4], cd;
-            sw.input(xin);
-            sweep_map<SKIN>(P32, f.c, f.s, f.anc, xin, y, cd);
-            outcome = sw.advance(xin, y, cd, P32, so);
-            pending = outcome != SWEEP_CONTINUE;
-        }
+    int64_t k;
+    uint32_t id;
+    __device__ __forceinline__ void load(int64_t r, float (&start)[4]) {
+        const int nxr = a.L.nx + 2;
+        const int i = (int)(r % nxr), j = (int)(r / nxr);
+        k = a.L.at(i, j);
+        id = (uint32_t)r;
+        ao_load_fast<S, SKIN>(P64, P32, a, k, f);
+        start[0] = start[1] = start[2] = 1e-4f;   // atmosphere_ocean_fluxes.jl:132
+        start[3] = SKIN ? f.anc.dTi : 0.0f;
     }
+    __device__ __forceinline__ void store(const float (&x)[4], int iters) {
+        ao_store_fast(P64, P32, a, k, f, x[0], x[1], x[2], SKIN ? f.tha + (double)x[3] : f.Ts0, iters);
+    }
+};
+
+// Pass 1 of the adaptive solver, one member, convergence stopping rule: adaptive_pass1
+// with the schedule of SolveOpts::fetch / refill.
+template <class S, bool SKIN>
+__global__ void __launch_bounds__(128, 5) ao_adaptive_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
+                                                             SolveOpts so, WorkList wl, ReplayQueue rq,
+                                                             const float* guess, DevStats* stats) {
+    AOAdaptiveCell<S, SKIN> cell{a, P64, P32};
+    adaptive_pass1<SKIN>(cell, P32, so, wl, rq, guess, stats, (so.fetch & NESF_FETCH_OCEAN) != 0);
 }
 
 // Pass 1b (ADAPTIVE): the cells whose FP32 result was not kept, packed, through
@@ -492,15 +448,17 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
     // the adaptive pass 1 keeps FP32 results up to fp32_rho; fp32_rho = 0 keeps none: the
     // POLISH pass 1, which polishes every cell in place
     const bool adaptive = prec == NESF_F32_ADAPTIVE && so.fp32_rho > 0.0f;
-    // lane refill: the adaptive pass 1 of one member under the convergence stopping rule
-    const bool refill = adaptive && !ens && so.refill > 0 && P64.stop_kind == NESF_STOP_CONVERGENCE;
+    // the adaptive pass 1 of one member under the convergence stopping rule: every schedule in
+    // one kernel (ao_adaptive_kernel)
+    const bool one = adaptive && !ens && P64.stop_kind == NESF_STOP_CONVERGENCE;
+    const bool fetch_ao = (so.fetch & NESF_FETCH_OCEAN) != 0;
     if (prec == NESF_PLAIN_F64) NESF_AO_SKIN(NESF_PLAIN_F64);
-    else if (refill && skin)
-        ao_refill_kernel<S, true><<<pass1_grid(ao_refill_kernel<S, true>, grid, threads, sms, true), threads, 0,
-                                    stream>>>(a, P64, P32, so, wl, rq, guess, stats);
-    else if (refill)
-        ao_refill_kernel<S, false><<<pass1_grid(ao_refill_kernel<S, false>, grid, threads, sms, true), threads, 0,
-                                     stream>>>(a, P64, P32, so, wl, rq, guess, stats);
+    else if (one && skin)
+        ao_adaptive_kernel<S, true><<<pass1_grid(ao_adaptive_kernel<S, true>, grid, threads, sms, fetch_ao), threads,
+                                      0, stream>>>(a, P64, P32, so, wl, rq, guess, stats);
+    else if (one)
+        ao_adaptive_kernel<S, false><<<pass1_grid(ao_adaptive_kernel<S, false>, grid, threads, sms, fetch_ao),
+                                       threads, 0, stream>>>(a, P64, P32, so, wl, rq, guess, stats);
     else if (adaptive) NESF_AO_SKIN(NESF_F32_ADAPTIVE);
     else NESF_AO_SKIN(NESF_F32_POLISH);
 #undef NESF_AO_SKIN
@@ -533,7 +491,7 @@ static cudaError_t preload_ao_t() {
         (const void*)ao_kernel<S, NESF_F32_POLISH, false, false>, (const void*)ao_kernel<S, NESF_F32_POLISH, true, false>,
         (const void*)ao_kernel<S, NESF_F32_ADAPTIVE, false, false>,
         (const void*)ao_kernel<S, NESF_F32_ADAPTIVE, true, false>,
-        (const void*)ao_refill_kernel<S, false>, (const void*)ao_refill_kernel<S, true>,
+        (const void*)ao_adaptive_kernel<S, false>, (const void*)ao_adaptive_kernel<S, true>,
         (const void*)ao_polish_kernel<S, false>, (const void*)ao_polish_kernel<S, true>,
         (const void*)ao_replay_kernel<S, false>, (const void*)ao_replay_kernel<S, true>};
     for (const void* k : kernels) {

@@ -82,7 +82,7 @@ static nesf_tuning default_tuning() {
     t.two_lanes = 1;
     t.io_overlap = 1;
     t.pass1_fetch = 2;
-    t.refill_cadence = 2;
+    t.refill_lanes = 8;
     return t;
 }
 
@@ -511,7 +511,7 @@ static SolveOpts solve_opts(const nesf_solver_options& o, const nesf_context* ct
     return SolveOpts{o.polish_maxiter, (float)o.path_tolerance, rho, (float)o.fallback_ratio,
                      t.solve_block, t.deferred_per_sm, t.infer_per_sm,
                      (t.pass1_fetch >= 2 ? NESF_FETCH_SEA_ICE : 0) | (t.pass1_fetch >= 3 ? NESF_FETCH_OCEAN : 0),
-                     t.pass1_fetch == 4 ? (t.refill_cadence > 0 ? t.refill_cadence : 2) : 0, tracer_of(ctx)};
+                     t.pass1_fetch == 4 ? (t.refill_lanes > 0 ? t.refill_lanes : 8) : 32, tracer_of(ctx)};
 }
 
 static int check_options(const nesf_solver_options& o, const char* who) {
@@ -1574,7 +1574,6 @@ extern "C" int nesf_graph_capture(nesf_context* ctx, const nesf_coupling_step_ar
     // the interpolation node, whose time weight changes every step
     if (a->interp) {
         G->interp_fp64 = a->interp->dtype == NESF_F64;
-        const void* fn = interp_kernel_address(G->interp_fp64);
         size_t n = 0;
         e = cudaGraphGetNodes(graph, nullptr, &n);
         cudaGraphNode_t nodes[256];
@@ -1583,7 +1582,8 @@ extern "C" int nesf_graph_capture(nesf_context* ctx, const nesf_coupling_step_ar
             cudaGraphNodeType t;
             if (cudaGraphNodeGetType(nodes[k], &t) != cudaSuccess || t != cudaGraphNodeTypeKernel) continue;
             cudaKernelNodeParams kp;
-            if (cudaGraphKernelNodeGetParams(nodes[k], &kp) != cudaSuccess || kp.func != fn) continue;
+            if (cudaGraphKernelNodeGetParams(nodes[k], &kp) != cudaSuccess || !is_interp_kernel(kp.func, G->interp_fp64))
+                continue;
             G->interp_node = nodes[k];
             G->interp_params = kp;
             memcpy(G->interp_args, kp.kernelParams[0],
@@ -1737,8 +1737,8 @@ static int check_tuning(const nesf_tuning& t, const char* who) {
         return fail(NESF_ERR_ARG, "%s: two_lanes and io_overlap are 0 or 1", who);
     if (t.pass1_fetch < 0 || t.pass1_fetch > 4)
         return fail(NESF_ERR_ARG, "%s: pass1_fetch %d (1, 2, 3 or 4)", who, t.pass1_fetch);
-    if (t.refill_cadence < 0 || t.refill_cadence > 16)
-        return fail(NESF_ERR_ARG, "%s: refill_cadence %d (1..16)", who, t.refill_cadence);
+    if (t.refill_lanes < 0 || t.refill_lanes > 32)
+        return fail(NESF_ERR_ARG, "%s: refill_lanes %d (1..32)", who, t.refill_lanes);
     return NESF_OK;
 }
 
@@ -1749,7 +1749,7 @@ static nesf_tuning complete_tuning(const nesf_tuning& t) {
     if (!r.deferred_per_sm) r.deferred_per_sm = d.deferred_per_sm;
     if (!r.infer_per_sm) r.infer_per_sm = d.infer_per_sm;
     if (!r.pass1_fetch) r.pass1_fetch = d.pass1_fetch;
-    if (!r.refill_cadence) r.refill_cadence = d.refill_cadence;
+    if (!r.refill_lanes) r.refill_lanes = d.refill_lanes;
     return r;
 }
 
@@ -1823,7 +1823,7 @@ extern "C" int nesf_autotune(nesf_context* ctx, const nesf_coupling_step_args* a
         {&nesf_tuning::deferred_per_sm, {2, 4, 8, 16}, fast},
         {&nesf_tuning::infer_per_sm, {2, 4, 8}, warm},
         {&nesf_tuning::pass1_fetch, {2, 1, 3, 4}, fast},
-        {&nesf_tuning::refill_cadence, {1, 2, 4, 8}, adaptive},
+        {&nesf_tuning::refill_lanes, {8, 4, 16}, adaptive},
         {&nesf_tuning::two_lanes, {1, 0}, ice},
         {&nesf_tuning::io_overlap, {1, 0}, ice && a->io_params != nullptr},
     };

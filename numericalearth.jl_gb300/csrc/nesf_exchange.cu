@@ -11,6 +11,8 @@
 // All are HBM-bound: one thread per cell, i fastest, read-once/write-once.
 #include "nesf_exchange.cuh"
 
+#include <climits>
+
 namespace nesf {
 
 // ------------------------------------------------------------- sea ice - ocean
@@ -214,6 +216,122 @@ __global__ void __launch_bounds__(256) interp_kernel(InterpArgs<S> a) {
     }
 }
 
+// Tiled interpolation for a regular longitude-latitude exchange grid without fractional
+// index caches: a block of 256 threads covers 256 ring columns x tile_rows ring rows. The
+// fractional indices depend on the column (longitude) and on the row (latitude) alone, so
+// the block computes them once per column and once per row, in FP64 with the gather
+// kernel's expressions (the same values), and stages the coarse footprint of its tile --
+// the atmosphere columns and rows its cells' bilinear stencils touch, both snapshots of
+// all nine variables -- in shared memory with coalesced loads; each cell then reads its
+// four corners there. The interpolation arithmetic is the gather kernel's (same
+// expressions, same order: bit-identical outputs). A tile whose footprint would exceed
+// the staged bounds (fp_w x fp_h, sized on the host) reads its corners from global memory.
+constexpr int kInterpTileCols = 256;
+constexpr int kInterpMaxTileRows = 32;
+
+template <class S>
+__global__ void __launch_bounds__(kInterpTileCols) interp_tile_kernel(InterpArgs<S> a) {
+    extern __shared__ __align__(16) unsigned char interp_smem[];
+    S* stage = (S*)interp_smem;
+    __shared__ int s_jm[kInterpMaxTileRows];
+    __shared__ S s_eta[kInterpMaxTileRows];
+    __shared__ int s_bounds[4];   // smallest and largest stencil column (unwrapped), row (clamped)
+    const int nxr = a.L.nx + 2, nyr = a.L.ny + 2;
+    const nesf_atmos_grid& ag = a.atmos;
+    const int i = blockIdx.x * kInterpTileCols + threadIdx.x;   // ring column 0..nx+1
+    const int jt = blockIdx.y * a.tile_rows;                     // first ring row of the tile
+    const int nj = min(a.tile_rows, nyr - jt);
+    const bool col = i < nxr;
+    int im = 0;
+    S xi = S(0);
+    if (col) {
+        double lon = a.coords.lon0 + (i - 1) * a.coords.dlon;
+        double fi = (lon - ag.lon0) / ag.dlon + 1;
+        double fli = floor(fi);
+        // |fi| beyond 2^28 means coordinates far outside the atmosphere's: the clamp keeps the
+        // footprint arithmetic below from overflowing (wrap_i gives such cells a column anyway)
+        im = (int)fmin(fmax(fli, -268435456.0), 268435456.0);
+        xi = (S)(fi - fli);
+    }
+    if (threadIdx.x == 0) {
+        s_bounds[0] = INT_MAX; s_bounds[1] = INT_MIN; s_bounds[2] = INT_MAX; s_bounds[3] = INT_MIN;
+    }
+    __syncthreads();
+    if (threadIdx.x < nj) {
+        int j = jt + threadIdx.x;
+        double lat = a.coords.lat0 + (j - 1) * a.coords.dlat;
+        double fj = (lat - ag.lat0) / ag.dlat + 1;
+        double flj = floor(fj);
+        int jm = (int)flj;
+        s_jm[threadIdx.x] = jm;
+        s_eta[threadIdx.x] = (S)(fj - flj);
+        atomicMin(&s_bounds[2], clamp_j(jm, ag.ny));
+        atomicMax(&s_bounds[3], clamp_j(jm + 1, ag.ny));
+    }
+    if (col) {
+        atomicMin(&s_bounds[0], im);
+        atomicMax(&s_bounds[1], im + 1);
+    }
+    __syncthreads();
+    const int imin = s_bounds[0], jmin = s_bounds[2];
+    const int64_t W64 = (int64_t)s_bounds[1] - imin + 1, H64 = (int64_t)s_bounds[3] - jmin + 1;
+    const bool staged = W64 >= 2 && H64 >= 1 && W64 <= a.fp_w && H64 <= a.fp_h;   // block-uniform
+    const int W = staged ? (int)W64 : 0, H = staged ? (int)H64 : 0;
+    const int plane = W * H;
+    if (staged) {
+        const int total = 18 * plane;
+        for (int e = threadIdx.x; e < total; e += kInterpTileCols) {
+            const int var = e / (2 * plane), t = (e / plane) & 1, rc = e % plane;
+            const int r = rc / W, c = rc % W;
+            const S* b = a.src[var];
+            S v = S(0);
+            if (b) {
+                const int ii = wrap_i(imin + c, ag.nx), jj = jmin + r;
+                v = __ldg(b + (int64_t)t * ag.stride_t + (int64_t)(ii - 1 + ag.hx) + (int64_t)(jj - 1 + ag.hy) * ag.stride_j);
+            }
+            stage[e] = v;
+        }
+    }
+    __syncthreads();
+    if (!col) return;
+    const int i0 = wrap_i(im, ag.nx), i1 = wrap_i(im + 1, ag.nx);
+    const int c0 = im - imin, c1 = c0 + 1;
+    const S tn = (S)a.tn;
+    for (int r = 0; r < nj; r++) {
+        const int j = jt + r;
+        const int jm = s_jm[r];
+        const S eta = s_eta[r];
+        const int j0 = clamp_j(jm, ag.ny), j1 = clamp_j(jm + 1, ag.ny);
+        const int64_t k = a.L.at(i, j);
+        if (staged) {
+            const int r0 = j0 - jmin, r1 = j1 - jmin;
+#pragma unroll
+            for (int n = 0; n < 9; n++) {
+                if (!a.dst[n]) continue;
+                S out = S(0);
+                if (a.src[n]) {
+                    S v[2];
+#pragma unroll
+                    for (int t = 0; t < 2; t++) {
+                        const S* q = stage + (2 * n + t) * plane;
+                        auto at = [&](int cc, int rr) { return q[rr * W + cc]; };
+                        v[t] = (1 - xi) * (1 - eta) * at(c0, r0) + (1 - xi) * eta * at(c0, r1) +
+                               xi * (1 - eta) * at(c1, r0) + xi * eta * at(c1, r1);
+                    }
+                    out = v[1] * tn + v[0] * (1 - tn);
+                }
+                a.dst[n][k] = out;
+            }
+        } else {
+#pragma unroll
+            for (int n = 0; n < 9; n++) {
+                if (!a.dst[n]) continue;
+                a.dst[n][k] = a.src[n] ? interp_one<S>(ag, a.src[n], i0, i1, j0, j1, xi, eta, tn) : S(0);
+            }
+        }
+    }
+}
+
 // ------------------------------------------------------------------ assembly
 // Arithmetic in the storage type S, as the interpolation.
 template <class S>
@@ -408,17 +526,50 @@ cudaError_t launch_frac(const Layout2& L, const nesf_exchange_coords& c, const n
     return cudaGetLastError();
 }
 
+// The tiled kernel serves a regular grid without caches when a tile's coarse footprint fits
+// in kInterpStageBytes of shared memory: tile rows are halved from kInterpMaxTileRows until
+// it does (the per-cell gather kernel otherwise). Footprint bounds: a tile's columns span
+// (kInterpTileCols - 1) |dlon / dlon_atmos| fractional indices, its rows (rows - 1) |dlat /
+// dlat_atmos|; + 1 for the stencil's second point and + 1 for the floors.
+constexpr size_t kInterpStageBytes = 64 * 1024;
+
 template <class S>
-cudaError_t launch_interp(const InterpArgs<S>& a, cudaStream_t s) {
-    int64_t n = (int64_t)(a.L.nx + 2) * (a.L.ny + 2);
-    interp_kernel<S><<<blocks_for(n, 256), 256, 0, s>>>(a);
+cudaError_t launch_interp(const InterpArgs<S>& a0, cudaStream_t s) {
+    InterpArgs<S> a = a0;
+    a.tile_rows = a.fp_w = a.fp_h = 0;
+    const int64_t nyr = a.L.ny + 2;
+    if (!a.frac_i) {
+        const double rx = fabs(a.coords.dlon / a.atmos.dlon), ry = fabs(a.coords.dlat / a.atmos.dlat);
+        const double w = ceil((kInterpTileCols - 1) * rx) + 3;
+        for (int rows = kInterpMaxTileRows; rows >= 1 && !a.tile_rows; rows /= 2) {
+            const double h = ceil((rows - 1) * ry) + 3;
+            if (w <= 4096 && h <= 4096 && 18.0 * w * h * sizeof(S) <= (double)kInterpStageBytes) {
+                a.tile_rows = rows;
+                a.fp_w = (int)w;
+                a.fp_h = (int)h;
+            }
+        }
+    }
+    if (!a.tile_rows) {
+        int64_t n = (int64_t)(a.L.nx + 2) * nyr;
+        interp_kernel<S><<<blocks_for(n, 256), 256, 0, s>>>(a);
+        return cudaGetLastError();
+    }
+    const size_t bytes = (size_t)18 * a.fp_w * a.fp_h * sizeof(S);
+    cudaError_t e = cudaFuncSetAttribute(interp_tile_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kInterpStageBytes);
+    if (e != cudaSuccess) return e;
+    dim3 grid((unsigned)((a.L.nx + 2 + kInterpTileCols - 1) / kInterpTileCols),
+              (unsigned)((nyr + a.tile_rows - 1) / a.tile_rows));
+    interp_tile_kernel<S><<<grid, kInterpTileCols, bytes, s>>>(a);
     return cudaGetLastError();
 }
 template cudaError_t launch_interp<double>(const InterpArgs<double>&, cudaStream_t);
 template cudaError_t launch_interp<float>(const InterpArgs<float>&, cudaStream_t);
 
-const void* interp_kernel_address(bool fp64) {
-    return fp64 ? (const void*)interp_kernel<double> : (const void*)interp_kernel<float>;
+bool is_interp_kernel(const void* fn, bool fp64) {
+    return fp64 ? (fn == (const void*)interp_kernel<double> || fn == (const void*)interp_tile_kernel<double>)
+                : (fn == (const void*)interp_kernel<float> || fn == (const void*)interp_tile_kernel<float>);
 }
 
 template <class S>

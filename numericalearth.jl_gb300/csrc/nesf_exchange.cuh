@@ -23,6 +23,9 @@ template <class S> struct InterpArgs {
     const S* src[9];          // u v T q p rain snow sw lw (atmosphere grid, 2 snapshots)
     S* dst[9];                // exchange-grid outputs
     const double *frac_i, *frac_j;
+    // the tiled kernel (regular grids, no caches): exchange rows per tile and the largest
+    // coarse footprint (columns x rows) a tile stages; 0: the per-cell gather kernel
+    int tile_rows, fp_w, fp_h;
 };
 
 template <class S> struct AsmFields {
@@ -56,8 +59,9 @@ template <class S> cudaError_t launch_io(const IOArgs<S>& a, const nesf_io_param
 cudaError_t launch_frac(const Layout2& L, const nesf_exchange_coords& c, const nesf_atmos_grid& ag, double* fi,
                         double* fj, cudaStream_t s);
 template <class S> cudaError_t launch_interp(const InterpArgs<S>& a, cudaStream_t s);
-// The interpolation kernel's address, to find its node in a captured graph.
-const void* interp_kernel_address(bool fp64);
+// Whether `fn` is one of the interpolation kernels of the storage type, to find its node
+// in a captured graph.
+bool is_interp_kernel(const void* fn, bool fp64);
 // which: 0 net ocean, 1 net sea ice, 2 ocean radiation, 3 sea-ice radiation
 template <class S>
 cudaError_t launch_assemble(const AsmArgs<S>& a, const nesf_assembly_params& p, int which, cudaStream_t s);

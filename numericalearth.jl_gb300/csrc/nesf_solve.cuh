@@ -49,7 +49,8 @@ struct SolveOpts {
     int block, deferred_per_sm, infer_per_sm;
     int fetch;             // pass 1 of the FP32 solvers where resident warps take 32 work-list entries
                            // at a time: NESF_FETCH_OCEAN | NESF_FETCH_SEA_ICE bits
-    int refill;            // adaptive pass 1 with lane refill every `refill` map evaluations (0: off)
+    int refill;            // adaptive pass 1 with warp fetching: lanes idle before a warp takes new
+                           // entries for them (32: all, the warp fetching; fewer: lane refill)
     const Tracer* tracer;  // host side: kernel-boundary trace (null: off)
 };
 
@@ -701,13 +702,21 @@ __device__ __forceinline__ int sweep_fp32(const DevIface<float>& P32, const Cell
     Sweep<SKIN, ACCEPT32, STRICT, CENTRAL> sw;
     sw.begin(x, xw);
     int out;
+    // the decisions run after the evaluation loop, where the lanes of a warp that left it
+    // at different iterations are together again (inside it each lane would take them
+    // alone); CENTRAL's mirrored points go back into the loop
 #pragma unroll 1
     for (;;) {
-        float xin[4], y[4], cd;
-        sw.input(xin);
-        sweep_map<SKIN>(P32, c32, s32, anc, xin, y, cd);
-        out = sw.advance(xin, y, cd, P32, so);
-        if (out == SWEEP_DECIDE) out = sw.decide(so, P32);
+#pragma unroll 1
+        for (;;) {
+            float xin[4], y[4], cd;
+            sw.input(xin);
+            sweep_map<SKIN>(P32, c32, s32, anc, xin, y, cd);
+            out = sw.advance(xin, y, cd, P32, so);
+            if (out != SWEEP_CONTINUE) break;
+        }
+        if (out != SWEEP_DECIDE) break;
+        out = sw.decide(so, P32);
         if (out != SWEEP_CONTINUE) break;
     }
 #pragma unroll
@@ -944,6 +953,91 @@ __device__ __forceinline__ void replay_push(const ReplayQueue& q, bool want, uin
     queue_push(q, part, want, id);
 }
 __device__ __forceinline__ void polish_push(const ReplayQueue& q, bool want, uint32_t id) { queue_push(q, 1, want, id); }
+
+// Pass 1 of the adaptive solver (one member, convergence stopping rule), every schedule in
+// one loop: each lane holds a cell and advances its FP32 sweep one map evaluation per trip
+// (Sweep), whatever stage -- sweep, cold-start probe, Jacobian column -- the cell is at, so
+// the lanes of a warp evaluate the map in lockstep. The decisions, the epilogue (store or
+// queue) and the taking of new cells happen at warp events only, together for the lanes
+// concerned: an event comes when no lane is sweeping, or, with lane refill, when `refill`
+// lanes are done or empty. Schedules:
+//   fetch = false: one work-list entry per thread (the grid covers the list), no refill;
+//   fetch, refill = 32: the resident warps take the next 32 entries (counter rq.count[3])
+//     when all their cells are done -- warp fetching;
+//   fetch, refill < 32: a warp takes new entries for its idle lanes as soon as `refill` of
+//     them are idle -- lane refill: a cell that converges early frees its lane for a new
+//     cell instead of holding it until the warp's slowest cell is done.
+// Every schedule runs the same instructions on a cell (one kernel, one inlined copy of the
+// map), so the outputs do not depend on it. `Cell` is the interface's adapter: load(r,
+// start) reads ring cell r's inputs into `f` and the start state, store(x, iterations)
+// writes the fluxes of a kept FP32 result; `id` names the cell in the queues.
+template <bool SKIN, class Cell>
+__device__ __forceinline__ void adaptive_pass1(Cell& cell, const DevIface<float>& P32, const SolveOpts& so,
+                                               const WorkList& wl, const ReplayQueue& rq, const float* guess,
+                                               DevStats* stats, bool fetch) {
+    const int lane = threadIdx.x & 31;
+    const unsigned total = wl.count[0] + wl.count[1];
+    const int refill = fetch ? (so.refill > 0 && so.refill < 32 ? so.refill : 32) : 32;
+    Sweep<SKIN, true> sw;
+    bool have = false, pending = false, alive = true, first = true;
+    int outcome = SWEEP_CONTINUE;
+#pragma unroll 1
+    for (;;) {
+        const unsigned running = __ballot_sync(0xffffffffu, have && !pending);
+        const unsigned idle = __ballot_sync(0xffffffffu, pending || (!have && alive));
+        if (running == 0u || (fetch && refill < 32 && __popc(idle) >= refill)) {
+            if (pending) {   // the decisions and the epilogue of the lanes whose sweep is done
+                if (outcome == SWEEP_DECIDE) outcome = sw.decide(so, P32);
+                replay_push(rq, outcome == FAST_REPLAY, cell.id);
+                polish_push(rq, outcome == FAST_POLISH, cell.id);
+                if (outcome == FAST_SOLVED) {
+                    cell.store(sw.x, sw.fp32_it);
+                    if (stats) stats_add(stats, true, true, sw.fp32_it, false, false, 0, false, sw.fell_back);
+                } else if (stats) {
+                    stats_add(stats, true, false, 0, false, false, 0, outcome == FAST_REPLAY, sw.fell_back);
+                    if (outcome == FAST_REPLAY) stats_replay_reason(stats, sw.reason);
+                }
+                have = pending = false;
+            }
+            int64_t w = -1;
+            if (fetch) {
+                const bool need = alive && !have;
+                const unsigned nb = __ballot_sync(0xffffffffu, need);
+                if (nb) {
+                    const int leader = __ffs(nb) - 1;
+                    unsigned base = 0;
+                    if (lane == leader) base = atomicAdd(&rq.count[3], (unsigned)__popc(nb));
+                    base = __shfl_sync(0xffffffffu, base, leader);
+                    if (need) {
+                        const unsigned pos = base + __popc(nb & ((1u << lane) - 1u));
+                        if (pos < total) w = pos;
+                        else alive = false;
+                    }
+                }
+            } else if (first) {
+                const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+                w = t < (int64_t)total ? t : -1;
+                alive = false;
+            }
+            first = false;
+            if (w >= 0) {
+                float xw[3], start[4];
+                const float* warm = mlp::guess_at(guess, worklist_slot(wl, 0, w), xw);
+                cell.load(worklist_get(wl, 0, w), start);
+                sw.begin(start, warm);
+                have = true;
+            }
+            if (!__any_sync(0xffffffffu, have)) break;
+        }
+        if (have && !pending) {
+            float xin[4], y[4], cd;
+            sw.input(xin);
+            sweep_map<SKIN>(P32, cell.f.c, cell.f.s, cell.f.anc, xin, y, cd);
+            outcome = sw.advance(xin, y, cd, P32, so);
+            pending = outcome != SWEEP_CONTINUE;
+        }
+    }
+}
 
 // Grid of a pass-1 launch: with warp fetching, the blocks that can be resident at
 // once (at most the one-thread-per-entry grid); otherwise that grid unchanged.

@@ -56,10 +56,12 @@ class CoupledModel:
             self.atmos_src = {n: torch.from_numpy(state.atmos["arrays"][n]).to(device) for n in ATMOS_NAMES}
             for n in ATMOS_NAMES:
                 self.x[EXCHANGE_ATMOS[n]] = z()
-            self.fi = torch.zeros(L.shape, dtype=torch.float64, device=device)
-            self.fj = torch.zeros_like(self.fi)
-            # initialize!(exchanger): fractional indices once (prescribed_atmosphere_regridder.jl:41-49)
-            api.compute_fractional_indices(L, self.coords, self.atmos, self.fi, self.fj)
+            # initialize!(exchanger) computes the fractional indices once
+            # (prescribed_atmosphere_regridder.jl:41-49). On this regular longitude-latitude exchange
+            # grid they depend on the column and on the row alone, so the interpolation computes them
+            # per tile from the coordinates (the same values) instead of reading two FP64 caches per
+            # cell; `fractional_indices()` computes the caches for a caller that wants them.
+            self.fi = self.fj = None
         self.ai_T = self.x["ice_temperature"].clone()     # AI interface (top surface) temperature, in/out
         self.ao = {k: z() for k in F.AO_OUTPUTS}
         self.ai = {k: z() for k in F.AI_OUTPUTS}
@@ -77,8 +79,17 @@ class CoupledModel:
             return 0
         out = {n: self.x[EXCHANGE_ATMOS[n]] for n in ATMOS_NAMES}
         api.interpolate_atmosphere_state(self.layout, self.coords, self.atmos, self.atmos_src, out,
-                                         self.atmos["time_weight"], frac=(self.fi, self.fj), stream=stream)
+                                         self.atmos["time_weight"], stream=stream)
         return 1
+
+    def fractional_indices(self):
+        """The exchanger's fractional-index fields (nesf_compute_fractional_indices), FP64 on the
+        device: what initialize!(exchanger) stores."""
+        torch = self.torch
+        fi = torch.zeros(self.layout.shape, dtype=torch.float64, device=self.device)
+        fj = torch.zeros_like(fi)
+        api.compute_fractional_indices(self.layout, self.coords, self.atmos, fi, fj)
+        return fi, fj
 
     def compute_fluxes(self, precision="f64", polish_maxiter=0, stats=False, stream=None):
         x = self.x
@@ -158,8 +169,7 @@ class CoupledModel:
             interp = None
             if self.atmos is not None:
                 out = {n: self.x[EXCHANGE_ATMOS[n]] for n in ATMOS_NAMES}
-                interp = (self.coords, self.atmos, self.atmos_src, out, (self.fi, self.fj),
-                          self.atmos["time_weight"])
+                interp = (self.coords, self.atmos, self.atmos_src, out, None, self.atmos["time_weight"])
             L = self.layout
             self._step = api.CouplingStep(self.ao_spec, L, ao_arrays, self.ai_spec, ai_arrays, self.io_spec,
                                           io_arrays, (self.T3.shape[0], L.shape[0] * L.shape[1]), interp,

@@ -87,8 +87,8 @@ def test_network_blob_layout_matches_binding():
 
 @pytest.mark.parametrize("field,value", [("solve_block", 48), ("solve_block", 160), ("deferred_per_sm", 17),
                                          ("infer_per_sm", -1), ("two_lanes", 2), ("io_overlap", -1),
-                                         ("pass1_fetch", 5), ("pass1_fetch", -1), ("refill_cadence", 17),
-                                         ("refill_cadence", -2)])
+                                         ("pass1_fetch", 5), ("pass1_fetch", -1), ("refill_lanes", 33),
+                                         ("refill_lanes", -2)])
 def test_tuning_out_of_range_is_an_argument_error(field, value):
     """nesf_set_tuning checks its fields before it touches a device."""
     lib = _lib.load()

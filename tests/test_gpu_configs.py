@@ -16,7 +16,9 @@ test_oracle_bands.py). Relative error = |gpu - oracle| / max(|oracle|, 1e-6 max|
    FP32 fields, the adaptive solver, the step replayed as a CUDA graph: the interface
    fluxes within 1e-5; the sea-ice-ocean fluxes within 1e-5 (p99) and 1e-6 under the ice;
    the net fluxes within 1e-5 of their largest magnitude. FP64 fields, plain FP64: the
-   solves at the conditioning bar with identical iteration counts, the rest to 1e-12.
+   solves at the conditioning bar with identical iteration counts, the sea-ice-ocean
+   fluxes to 1e-12, the net fluxes (sums whose terms can cancel) to 1e-12 of their largest
+   magnitude and 1e-12 relative on 99 % of the cells.
 3. 32 members x 720 x 360 in one ensemble launch, each member with its own Charnock
    parameter, gustiness and roughness coefficients: per member two bands against the
    oracle with that member's parameters (plain FP64 arithmetic on FP32 fields within 1e-6,
@@ -231,9 +233,13 @@ def test_config2_coupled_step_plain_f64(oracle):
         for k in F.IO_OUTPUTS:
             e = rel_err(band_part(snap["io"][k], st, lo), I(ref["io"][k]), floor_frac=1e-6)
             assert e.max() <= 1e-12, ("io", lo, k, float(e.max()))
+        # the net fluxes sum terms that can cancel (the sea-ice top heat: turbulent against
+        # radiative): held to 1e-12 of their largest magnitude and per cell on 99 % of the cells
         for k, r in ref["net"].items():
-            e = rel_err(band_part(snap["net"][k], st, lo), I(r), floor_frac=1e-6)
-            assert np.percentile(e, 99.9) <= 1e-12, ("net", lo, k, float(e.max()))
+            g, rr = band_part(snap["net"][k], st, lo), I(r)
+            assert np.abs(g - rr).max() <= 1e-12 * np.abs(rr).max(), ("net", lo, k)
+            e = rel_err(g, rr, floor_frac=1e-6)
+            assert np.percentile(e, 99) <= 1e-12, ("net", lo, k, float(e.max()))
 
 
 # --------------------------------------------------------------------- 3

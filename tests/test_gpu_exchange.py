@@ -163,6 +163,41 @@ def test_interpolation_matches_oracle(oracle):
         assert np.array_equal(to_numpy(out[n]), to_numpy(out2[n])), n
 
 
+@pytest.mark.parametrize("nx,ny,lon_w,lon_e,lat_s,lat_n,dtype", [
+    (720, 96, -10.0, 350.0, -70.0, 70.0, np.float64),    # longitudes across the periodic seam
+    (300, 70, 0.0, 360.0, 80.0, -80.0, np.float64),      # latitude decreasing with j
+    (1440, 40, 0.0, 360.0, -70.0, 70.0, np.float32),     # quarter degree, FP32 fields
+    (100, 50, 0.0, 360.0, -80.0, 80.0, np.float64),      # coarser than the atmosphere (gather kernel)
+    (37, 5, 33.0, 47.0, 61.0, 62.0, np.float64),         # one partial tile
+])
+def test_interpolation_tiles_match_the_gather_kernel(oracle, nx, ny, lon_w, lon_e, lat_s, lat_n, dtype):
+    """On a regular grid without caches the interpolation stages each tile's coarse stencil in
+    shared memory (or, when the footprint is too large, gathers per cell): bit-identical to the
+    gather kernel reading the fractional-index caches, and to the oracle to 1e-13 (FP64)."""
+    import torch
+    st = syn.ao_quarter_land(nx=nx, ny=ny, dtype=dtype)
+    c = syn.lonlat(nx, ny, lat_s, lat_n, lon_w, lon_e)
+    at = st.atmos
+    src = api.to_device(at["arrays"])
+    tdt = src["T"].dtype
+    out = {n: torch.full(st.layout.shape, float("nan"), dtype=tdt, device="cuda") for n in src}
+    api.interpolate_atmosphere_state(st.layout, c, at, src, out, at["time_weight"])
+    fi = torch.zeros(st.layout.shape, dtype=torch.float64, device="cuda")
+    fj = torch.zeros_like(fi)
+    api.compute_fractional_indices(st.layout, c, at, fi, fj)
+    out2 = {n: torch.full_like(out[n], float("nan")) for n in src}
+    api.interpolate_atmosphere_state(st.layout, c, at, src, out2, at["time_weight"], frac=(fi, fj))
+    torch.cuda.synchronize()
+    R = st.layout.ring
+    for n in src:
+        assert np.array_equal(R(to_numpy(out[n])), R(to_numpy(out2[n]))), n
+    if dtype == np.float64:
+        ref = oracle.interpolate(st.layout, api.exchange_coords(c), api.atmos_grid_struct(at), at["arrays"],
+                                 at["time_weight"])
+        for n in src:
+            assert rel_err(R(to_numpy(out[n])), R(ref[n]), floor_frac=1e-6).max() <= 1e-13, n
+
+
 def test_interpolation_fp32_fields(oracle):
     """FP32 fields interpolate in FP32 arithmetic, like the reference's Float32 kernels: against
     the FP64 oracle on the same (FP32) atmosphere, positive fields (T, p, q, radiation) are within

@@ -60,6 +60,7 @@ def test_graph_follows_the_window(tmp_path):
     times = np.arange(nt) * dt
     m = CoupledModel(st)
     m.capture("f32_adaptive")
+    caches = m.fractional_indices()   # the direct call interpolates with the caches (the gather kernel)
     dtype = torch.from_numpy(series["T"][:1]).dtype
     win = forcing.FieldTimeSeriesWindow(forcing.ArraySource(series), times, st.atmos["layout"], slots=3, dtype=dtype)
     try:
@@ -72,7 +73,7 @@ def test_graph_follows_the_window(tmp_path):
             n1, n2, _ = forcing.time_indices(times, t)
             pair = {n: torch.tensor(np.stack([series[n][n1], series[n][n2]]), device="cuda") for n in series}
             ref = {n: torch.zeros_like(m.x[EXCHANGE_ATMOS[n]]) for n in ATMOS_NAMES}
-            api.interpolate_atmosphere_state(m.layout, m.coords, st.atmos, pair, ref, w, frac=(m.fi, m.fj))
+            api.interpolate_atmosphere_state(m.layout, m.coords, st.atmos, pair, ref, w, frac=caches)
             torch.cuda.synchronize()
             R = m.layout.ring   # the interpolation writes the interior and its one-cell ring
             for n in ATMOS_NAMES:
