@@ -104,37 +104,6 @@ def test_work_table_matches_header():
     assert {k: int(v) for k, v in found.items()} == A.WORK
 
 
-def test_julia_shim_parameter_blob_size():
-    """The Julia binding's opaque nesf_interface_params blob has the library's size."""
-    shim = os.path.join(os.path.dirname(HEADER), "..", "numericalearth.jl_gb300", "julia", "NESF.jl")
-    m = re.search(r"const PARAMS_BYTES = (\d+)", open(shim).read())
-    assert m and int(m.group(1)) == C.sizeof(A.InterfaceParams)
-
-
-def test_julia_shim_humidity_offsets(tmp_path):
-    """The byte offsets the Julia binding writes the land humidity model at are offsetof() of
-    include/nesf.h (compiled here) and the ctypes mirror's."""
-    import shutil
-    import subprocess
-    cc = shutil.which("gcc") or shutil.which("cc")
-    if cc is None:
-        pytest.skip("no C compiler")
-    shim = os.path.join(os.path.dirname(HEADER), "..", "numericalearth.jl_gb300", "julia", "NESF.jl")
-    block = re.search(r"const HUMIDITY_OFFSETS = \((.*?)\)", open(shim).read(), re.S).group(1)
-    offsets = {k: int(v) for k, v in re.findall(r"(\w+) = (\d+)", block)}
-    assert len(offsets) == 14
-    src = tmp_path / "off.c"
-    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "nesf.h"\nint main(void) {\n' +
-                   "".join(f'    printf("{k} %zu\\n", offsetof(nesf_interface_params, {k}));\n' for k in offsets) +
-                   "    return 0;\n}\n")
-    exe = tmp_path / "off"
-    subprocess.run([cc, "-I", os.path.dirname(HEADER), "-o", str(exe), str(src)], check=True)
-    out = dict(line.split() for line in subprocess.run([str(exe)], check=True, capture_output=True,
-                                                      text=True).stdout.splitlines())
-    for k, v in offsets.items():
-        assert int(out[k]) == v == getattr(A.InterfaceParams, k).offset, k
-
-
 # include/nesf.h's structs in the order of nesf_struct_sizes() and of A.STRUCTS_IN_SIZE_ORDER
 C_STRUCT_NAMES = (
     "nesf_grid", "nesf_thermodynamics_parameters", "nesf_stability_function", "nesf_roughness_length",
