@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="time only --precision (profiling captures)")
     ap.add_argument("--cold", action="store_true", help="no learned warm start")
     ap.add_argument("--no-autotune", action="store_true", help="default launch shapes (no nesf_autotune)")
+    ap.add_argument("--no-configs", action="store_true", help="skip the measurements of configurations 0-3")
     return ap.parse_args()
 
 
@@ -472,6 +473,194 @@ def oracle_errors(model, precisions, bands=48, rows=8):
     return out
 
 
+# ------------------------------------------------------------ the other configurations
+CONFIG_WORKLOADS = {
+    0: "ao_1deg: 360x180 (1 degree) atmosphere-ocean, no land, atmosphere on the exchange grid, FP64 fields",
+    1: "ao_quarter_land: 1440x560 (lat -70..70) atmosphere-ocean, 30% land, 640x320x2 prescribed atmosphere "
+       "interpolated onto the grid, FP32 fields",
+    2: "coupled_1440: 1440x600 (lat -75..75) atmosphere-ocean + atmosphere-sea-ice + sea-ice-ocean fluxes and "
+       "the net-flux assembly with radiation in one coupling step (CUDA graph), FP32 fields",
+    3: "ensemble_32: 32 members x 720x360 atmosphere-ocean in one launch, each member with its own Charnock "
+       "parameter, gustiness and roughness coefficients, per-member FP64 compensated integrals, FP32 fields",
+}
+
+
+class AOStep:
+    """An atmosphere-ocean step (with the interpolation of a prescribed atmosphere when the
+    workload has one) on the device, captured as one coupling-step graph."""
+
+    def __init__(self, state):
+        import torch
+        from nesf import api
+        from nesf import fields as F
+        from nesf import params as P
+        from nesf.coupled import ATMOS_NAMES, EXCHANGE_ATMOS
+        self.state, self.layout = state, state.layout
+        self.spec = P.atmosphere_ocean_interface_spec()
+        self.x = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in state.fields.items()}
+        dt = self.x["u_oc"].dtype
+        interp = None
+        if state.atmos is not None:
+            self.src = {n: torch.from_numpy(state.atmos["arrays"][n]).cuda() for n in ATMOS_NAMES}
+            for n in ATMOS_NAMES:
+                self.x[EXCHANGE_ATMOS[n]] = torch.zeros(self.layout.shape, dtype=dt, device="cuda")
+            interp = (state.coords, state.atmos, self.src, {n: self.x[EXCHANGE_ATMOS[n]] for n in ATMOS_NAMES},
+                      None, state.atmos["time_weight"])
+        self.ao = {k: torch.zeros(self.layout.shape, dtype=dt, device="cuda") for k in F.AO_OUTPUTS}
+        arrays = {k: self.x.get(k) for k in F.AO_INPUTS}
+        arrays.update(self.ao)
+        self.step = api.CouplingStep(self.spec, self.layout, arrays, interp=interp)
+        self.graphs = {}
+
+    def cells(self):
+        return int((self.layout.interior(self.state.fields["inactive"]) == 0).sum())
+
+    def graph(self, precision):
+        from nesf import api
+        if precision not in self.graphs:
+            self.graphs[precision] = api.Graph(self.step, precision)
+        return self.graphs[precision]
+
+
+def time_graph(launch, steps, warmup):
+    """ms per launch of `launch()`, CUDA events on the current stream after `warmup` launches."""
+    import torch
+    for _ in range(warmup):
+        launch()
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(steps):
+        launch()
+    e1.record(s)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def _ao_band_errors(table, got, state, lo, rows, ref, keep):
+    from oracle import band as OB
+    sub, rs = OB.band_rows(state, lo, rows)
+    kelvin = lambda k, a: a + 273.15 if k == "interface_temperature" else a
+    for k in HEADLINE_FLUXES + ("friction_velocity", "temperature_scale", "water_vapor_scale",
+                                "interface_temperature"):
+        table.add(f"ao.{k}", kelvin(k, sub.interior(np.asarray(got[k])[rs])), kelvin(k, sub.interior(ref[k])), keep)
+
+
+def _summary(table):
+    s = table.summary()
+    head = [v for k, v in s.items() if k.split(".")[1] in HEADLINE_FLUXES]
+    return {"max_headline_fluxes": max(v["max"] for v in head), "p99_headline_fluxes": max(v["p99"] for v in head),
+            "per_output": s}
+
+
+def config_entry(n, steps=20):
+    """Throughput, accuracy against the oracle and the oracle's CPU rate for configuration n
+    (0-3), whose workload CONFIG_WORKLOADS names: the adaptive FP32 solver (no warm start) and
+    the plain FP64 solver on the GPU, the oracle on bands of rows on the host cores."""
+    import torch
+    from nesf import api
+    from nesf import fields as F
+    from nesf import params as P
+    from nesf import synthetic as syn
+    from nesf.coupled import CoupledModel, EXCHANGE_ATMOS
+    from oracle import band as OB
+    from oracle import oracle
+    rows = 8
+    out = {"workload": CONFIG_WORKLOADS[n]}
+    if n == 3:
+        st = syn.ensemble()
+        L = st.layout
+        specs = [syn.ensemble_member_spec(p) for p in st.perturbations]
+        dev = api.to_device({k: st.fields[k] for k in F.AO_INPUTS if k in st.fields})
+        res = {k: torch.zeros((st.members,) + L.shape, dtype=torch.float32, device="cuda") for k in F.AO_OUTPUTS}
+        cells = int((np.stack([L.interior(m) for m in st.fields["inactive"]]) == 0).sum())
+        run = lambda prec: (lambda: api.compute_atmosphere_ocean_fluxes_ensemble(specs, L, dev, res, precision=prec))
+        ms = {p: time_graph(run(p), steps if p != "f64" else max(3, steps // 4), 2) for p in ("f32_adaptive", "f64")}
+        lat = st.coords.lat0 + np.arange(L.ny) * st.coords.dlat
+        rows_dev = torch.from_numpy(np.cos(np.radians(lat)) * 1.0e10).cuda()
+        tables = {}
+        for prec in ("f32_adaptive", "f64"):
+            run(prec)()
+            torch.cuda.synchronize()
+            got = {k: v.double().cpu().numpy() for k, v in res.items()}
+            t = OB.ErrorTable()
+            cpu_s, cpu_cells = 0.0, 0
+            for mbr in range(st.members):
+                ms_state = syn.SurfaceState(L, st.coords, st.dtype, fields={k: v[mbr] for k, v in st.fields.items()})
+                lo = int(OB.band_positions(ms_state, rows, st.members)[mbr])
+                t0 = time.perf_counter()
+                sub, ref = OB.step_band(ms_state, lo, rows, specs[mbr])
+                cpu_s += time.perf_counter() - t0
+                cpu_cells += int((sub.interior(ref["inputs"]["inactive"]) == 0).sum())
+                keep = sub.interior(ref["ao"]["iterations"]) < 100
+                _ao_band_errors(t, {k: v[mbr] for k, v in got.items()}, ms_state, lo, rows, ref["ao"], keep)
+            tables[prec] = _summary(t)
+        integrals = []
+        for mbr in range(st.members):
+            r = api.area_integrals(L, [res["sensible_heat"][mbr], res["latent_heat"][mbr]],
+                                   row_area=rows_dev).cpu().numpy()
+            integrals.append([float(r[0][0]), float(r[1][0])])
+        out.update(cells=cells, members=st.members, integrals_sensible_latent=integrals[:4],
+                   integrals_note="per-member compensated FP64 sums (sum, residual pairs on the device) of the "
+                                  "last solve's sensible and latent heat, rows weighted by cos(lat); first 4 shown")
+    elif n in (0, 1):
+        st = syn.ao_1deg() if n == 0 else syn.ao_quarter_land()
+        m = AOStep(st)
+        cells = m.cells()
+        ms = {p: time_graph(m.graph(p).launch, steps if p != "f64" else max(3, steps // 4), 3)
+              for p in ("f32_adaptive", "f64")}
+        tables = {}
+        cpu_s, cpu_cells = 0.0, 0
+        for prec in ("f32_adaptive", "f64"):
+            m.graph(prec).launch()
+            torch.cuda.synchronize()
+            got = {k: v.double().cpu().numpy() for k, v in m.ao.items()}
+            atm = {k: m.x[k].double().cpu().numpy() for k in EXCHANGE_ATMOS.values()} if st.atmos is not None else None
+            t = OB.ErrorTable()
+            for lo in OB.band_positions(st, rows, 16):
+                _, rs = OB.band_rows(st, int(lo), rows)
+                t0 = time.perf_counter()
+                sub, ref = OB.step_band(st, int(lo), rows, m.spec,
+                                        atmos=None if atm is None else {k: v[rs] for k, v in atm.items()})
+                if prec == "f64":
+                    cpu_s += time.perf_counter() - t0
+                    cpu_cells += int((sub.interior(ref["inputs"]["inactive"]) == 0).sum())
+                keep = sub.interior(ref["ao"]["iterations"]) < 100
+                _ao_band_errors(t, got, st, int(lo), rows, ref["ao"], keep)
+            tables[prec] = _summary(t)
+    else:
+        st = syn.coupled_1440()
+        m = CoupledModel(st)
+        n_ao, n_ai = m.active_cells()
+        cells = n_ao + n_ai
+        ms = {}
+        for p in ("f32_adaptive", "f64"):
+            m.capture(p)
+            ms[p] = time_graph(m.graph_step, steps if p != "f64" else max(3, steps // 4), 3)
+        ev = oracle_errors(m, ["f32_adaptive", "f64"], bands=16, rows=rows)
+        tables = {p: {"max_headline_fluxes": ev[p]["max_headline_fluxes"],
+                      "p99_headline_fluxes": ev[p]["p99_headline_fluxes"],
+                      "per_output": ev[p]["solver"]} for p in ("f32_adaptive", "f64")}
+        t0 = time.perf_counter()
+        cpu_cells = 0
+        sp = (m.ao_spec, m.ai_spec, m.io_spec, m.asm_spec)
+        for lo in OB.band_positions(st, rows, 16):
+            sub, ref = OB.step_band(st, int(lo), rows, *sp)
+            water = sub.interior(ref["inputs"]["inactive"]) == 0
+            ice = sub.interior(ref["inputs"]["ice_concentration"]) > 0
+            cpu_cells += int(water.sum() + (water & ice).sum())
+        cpu_s = time.perf_counter() - t0
+    out.update(cells=cells, fast_ms_per_step=ms["f32_adaptive"], plain_f64_ms_per_step=ms["f64"],
+               fast_cells_per_s=cells / (ms["f32_adaptive"] / 1000.0), plain_f64_cells_per_s=cells / (ms["f64"] / 1000.0),
+               speedup_vs_plain_f64=ms["f64"] / ms["f32_adaptive"],
+               errors_vs_oracle={"fast": tables["f32_adaptive"], "plain_f64": tables["f64"]},
+               cpu_oracle={"cells_per_s": cpu_cells / cpu_s if cpu_s > 0 else None, "cores": oracle.get_threads(),
+                           "sample": f"{cpu_cells} solved cells on bands of {rows} rows, {cpu_s:.2f} s"})
+    torch.cuda.synchronize()
+    return out
+
+
 def _oracle_threads():
     from oracle import oracle
     return oracle.get_threads()
@@ -792,6 +981,9 @@ def main():
                            "serial_ms_per_step": ms_ser}
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(state)
+        if not args.no_configs:
+            # the other configurations of the same metric, beside this one (configuration 4)
+            line["configs"] = {str(n): config_entry(n) for n in (0, 1, 2, 3)}
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()

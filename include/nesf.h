@@ -293,6 +293,12 @@ typedef struct {
                                  this relative bound (FP32 polish); default 2e-6         */
     double fp32_rho;          /* NESF_F32_ADAPTIVE: largest contraction rate at which the
                                  FP32 result is kept; default 0.9 (0 or less: default)  */
+    double calm_replay_wind;  /* NESF_F32_ADAPTIVE, atmosphere-sea-ice solve: cells whose
+                                 10 m wind speed is below it go from the classify pass
+                                 straight to the reference's FP64 iteration, on a stream
+                                 of their own beside pass 1 (in calm air the fixed point
+                                 converges slowly: these are the solve's longest FP64
+                                 chains); default 0.7 m/s, 0: none                     */
 } nesf_solver_options;
 
 /* -------------------------------------------------------------- statistics */
@@ -799,6 +805,8 @@ typedef struct {
                                  idle lanes as soon as refill_lanes of them are idle (2)              */
     int32_t refill_lanes;     /* pass1_fetch 4: idle lanes that make a warp take new entries, 1..32
                                  (32: warp fetching) (8)                                                */
+    int32_t early_ocean_classify; /* coupling step with two lanes: the ocean's classify pass and warm-
+                                 start inference beside the sea-ice pass 1, its pass 1 after it (1) */
     double step_ms;           /* nesf_autotune: the chosen configuration's mean step time            */
 } nesf_tuning;
 

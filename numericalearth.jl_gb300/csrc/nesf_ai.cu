@@ -143,10 +143,16 @@ __device__ __forceinline__ void ai_store_zero(const DevIface<double>& P, const D
 }
 
 // Pass 0: ice-free and land cells get the zero state with the ocean temperature
-// (atmosphere_sea_ice_fluxes.jl:141-142); the others go to the work list.
+// (atmosphere_sea_ice_fluxes.jl:141-142); the others go to the work list, or, with
+// calm2 > 0, those whose wind speed squared is below calm2 to the early replay (queue
+// part 3): in calm air the reference's fixed point converges slowly (40 to 100
+// iterations), the FP32 sweep's acceptance tests often send such a cell to the FP64
+// replay anyway, and its replay, the longest chain of dependent FP64 iterations of the
+// solve, can then start at once, beside pass 1, instead of after it.
 template <class S>
 __global__ void __launch_bounds__(128) ai_classify_kernel(AIArgs<S> a, DevIface<double> P, DevIface<float> Pf,
-                                                          WorkList wl, float* feat, DevStats* stats) {
+                                                          WorkList wl, ReplayQueue rq, float calm2, float* feat,
+                                                          DevStats* stats) {
     const int nxr = a.L.nx + 2;
     const int64_t ring = (int64_t)nxr * (a.L.ny + 2);
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -166,6 +172,14 @@ __global__ void __launch_bounds__(128) ai_classify_kernel(AIArgs<S> a, DevIface<
             stable = stable_class(Pf, Ta, pa, qa, Ts0);
         }
     }
+    bool calm = false;
+    if (active && calm2 > 0.0f) {
+        float ua = ldf(a.ua, k), va = ldf(a.va, k);
+        calm = ua * ua + va * va < calm2;
+    }
+    queue_push(rq, 3, calm, (uint32_t)r);
+    if (calm && stats) stats_add(stats, true, false, 0, false, false, 0, true, false);
+    active = active && !calm;
     int64_t slot = worklist_push(wl, 0, active, stable, (uint32_t)r);
     if (feat && slot >= 0) {
         // warm-start features (FP32) from the state before the iteration
@@ -257,7 +271,7 @@ __device__ __forceinline__ void ai_cell(const AIArgs<S>& a, const DevIface<doubl
 
 // Pass 1: the compacted ice cells, one thread each; with NESF_FETCH_SEA_ICE (FP32 solvers) the
 // resident blocks only, each warp taking the next 32 entries of the list (counter
-// rq.count[3]) until it is exhausted, as in the atmosphere-ocean pass 1.
+// rq.count[kFetchCounter]) until it is exhausted, as in the atmosphere-ocean pass 1.
 template <class S, int PREC, bool SKIN>
 __global__ void __launch_bounds__(128, PREC == NESF_F32_ADAPTIVE ? 5 : 1) ai_kernel(AIArgs<S> a, DevIface<double> P64, DevIface<float> P32,
                                                  SolveOpts so, WorkList wl, ReplayQueue rq, const float* guess,
@@ -267,7 +281,7 @@ __global__ void __launch_bounds__(128, PREC == NESF_F32_ADAPTIVE ? 5 : 1) ai_ker
     for (;;) {
         if (fetch) {
             unsigned base = 0;
-            if ((threadIdx.x & 31) == 0) base = atomicAdd(&rq.count[3], 32u);
+            if ((threadIdx.x & 31) == 0) base = atomicAdd(&rq.count[kFetchCounter], 32u);
             base = __shfl_sync(0xffffffffu, base, 0);
             if (base >= wl.count[0] + wl.count[1]) return;
             w = (int64_t)base + (threadIdx.x & 31);
@@ -386,7 +400,8 @@ __global__ void __launch_bounds__(128) ai_replay_kernel(AIArgs<S> a, DevIface<do
 template <class S>
 static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                                SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws,
-                               DevStats* stats, cudaStream_t stream, cudaEvent_t after_solve, const TailLane* tail) {
+                               DevStats* stats, cudaStream_t stream, cudaEvent_t after_solve, const TailLane* tail,
+                               const TailLane* early) {
     const int64_t ring = (int64_t)(a.L.nx + 2) * (a.L.ny + 2);
     const int block = so.block;   // <= 128: the kernels are compiled with __launch_bounds__(128)
     dim3 grid((unsigned)((ring + block - 1) / block));
@@ -398,11 +413,24 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     const bool warm = ws.mlp != nullptr && prec != NESF_PLAIN_F64 && P64.temp_form == NESF_BULK_TEMPERATURE &&
                       P64.flux_form == NESF_FLUXES_SIMILARITY_THEORY;
     cudaError_t e = cudaMemsetAsync(wl.count, 0, sizeof(unsigned) * 2, stream);
-    // rq.count: [0, 2] the deferred queues, [3] pass 1's fetch counter
-    if (e == cudaSuccess && prec != NESF_PLAIN_F64) e = cudaMemsetAsync(rq.count, 0, 4 * sizeof(unsigned), stream);
+    // rq.count: [0, 3] the deferred queues, [kFetchCounter] pass 1's fetch counter
+    if (e == cudaSuccess && prec != NESF_PLAIN_F64)
+        e = cudaMemsetAsync(rq.count, 0, kQueueCounters * sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
-    ai_classify_kernel<S><<<grid, block, 0, stream>>>(a, P64, P32, wl, warm ? ws.feat : nullptr, stats);
+    // calm cells straight to the FP64 replay on the early lane (the adaptive solver under the
+    // convergence stopping rule; the queue's part 3 holds them)
+    const bool adaptive_conv = prec == NESF_F32_ADAPTIVE && so.fp32_rho > 0.0f && P64.stop_kind == NESF_STOP_CONVERGENCE;
+    const bool calm = adaptive_conv && so.calm_wind > 0.0f && early && early->stream;
+    ai_classify_kernel<S><<<grid, block, 0, stream>>>(a, P64, P32, wl, rq, calm ? so.calm_wind * so.calm_wind : 0.0f,
+                                                      warm ? ws.feat : nullptr, stats);
     trace_mark(so.tracer, "ai_classify", stream);
+    if (calm) {
+        if ((e = cudaEventRecord(early->fork, stream)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(early->stream, early->fork, 0)) != cudaSuccess) return e;
+        ai_replay_kernel<S><<<(unsigned)(sms * so.deferred_per_sm), 128, 0, early->stream>>>(a, P64, rq, 3, stats);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        trace_mark(so.tracer, "ai_calm_replay", early->stream);
+    }
     if (warm) {
         e = mlp_pass((void*)ws.mlp, ws.feat, nullptr, ws.guess, 0, wl.count, wl.per_member, so.infer_per_sm * sms,
                      true, stream);
@@ -442,6 +470,7 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
         trace_mark(so.tracer, "ai_replay", stream);
         return cudaGetLastError();
     }
+
     // pass 1's replays (part 0) beside the polish pass, whose own replays (part 2) follow it
     cudaStream_t rs = stream;
     if (tail && tail->stream) {
@@ -461,6 +490,10 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
         if ((e = cudaEventRecord(tail->join, rs)) != cudaSuccess) return e;
         if ((e = cudaStreamWaitEvent(stream, tail->join, 0)) != cudaSuccess) return e;
     }
+    if (calm) {   // the early lane (only on this path: calm needs the adaptive solver) joins last
+        if ((e = cudaEventRecord(early->join, early->stream)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(stream, early->join, 0)) != cudaSuccess) return e;
+    }
     return cudaSuccess;
 }
 
@@ -469,15 +502,15 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
 #if !defined(NESF_STORAGE) || NESF_STORAGE == 64
 cudaError_t launch_ai(const AIArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream, cudaEvent_t after_solve, const TailLane* tail) {
-    return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream, after_solve, tail);
+                      cudaStream_t stream, cudaEvent_t after_solve, const TailLane* tail, const TailLane* early) {
+    return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream, after_solve, tail, early);
 }
 #endif
 #if !defined(NESF_STORAGE) || NESF_STORAGE == 32
 cudaError_t launch_ai(const AIArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream, cudaEvent_t after_solve, const TailLane* tail) {
-    return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream, after_solve, tail);
+                      cudaStream_t stream, cudaEvent_t after_solve, const TailLane* tail, const TailLane* early) {
+    return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream, after_solve, tail, early);
 }
 #endif
 

@@ -256,7 +256,7 @@ __device__ __forceinline__ void ao_cell(const AOArgs<S>& a, const DevIface<doubl
 
 // Pass 1: the compacted cells (unstable first, then stable), one thread each. With
 // NESF_FETCH_OCEAN (FP32 solvers, one member) the grid is the resident blocks only and each
-// warp takes the next 32 entries of the list (counter rq.count[3]) until it is
+// warp takes the next 32 entries of the list (counter rq.count[kFetchCounter]) until it is
 // exhausted: a warp that finishes early starts on new cells instead of holding its
 // block's slot until the block's slowest warp is done. Each cell's arithmetic is the
 // same under both schedules.
@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(128, ENS ? 4 : (PREC == NESF_F32_ADAPTIVE ? 5 
     for (;;) {
         if (fetch) {
             unsigned base = 0;
-            if ((threadIdx.x & 31) == 0) base = atomicAdd(&rq.count[3], 32u);
+            if ((threadIdx.x & 31) == 0) base = atomicAdd(&rq.count[kFetchCounter], 32u);
             base = __shfl_sync(0xffffffffu, base, 0);
             if (base >= wl.count[0] + wl.count[1]) return;
             w = (int64_t)base + (threadIdx.x & 31);
@@ -410,7 +410,8 @@ template <class S>
 static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                                const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec,
                                bool skin, SolveOpts so, const WorkList& wl, const ReplayQueue& rq,
-                               const WarmStart& ws, DevStats* stats, cudaStream_t stream) {
+                               const WarmStart& ws, DevStats* stats, cudaStream_t stream,
+                               cudaEvent_t before_pass1) {
     const int64_t ring = (int64_t)(a.L.nx + 2) * (a.L.ny + 2);
     const int threads = so.block;   // <= 128: the kernels are compiled with __launch_bounds__(128)
     const int nm = members > 1 ? members : 1;
@@ -425,8 +426,9 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
     float* feat = warm ? ws.feat : nullptr;
     const float* guess = warm ? ws.guess : nullptr;
     cudaError_t e = cudaMemsetAsync(wl.count, 0, sizeof(unsigned) * 2 * nm, stream);
-    // rq.count: [0, 1] the deferred queues, [3] pass 1's fetch counter
-    if (e == cudaSuccess && prec != NESF_PLAIN_F64) e = cudaMemsetAsync(rq.count, 0, 4 * sizeof(unsigned), stream);
+    // rq.count: [0, 1] the deferred queues, [kFetchCounter] pass 1's fetch counter
+    if (e == cudaSuccess && prec != NESF_PLAIN_F64)
+        e = cudaMemsetAsync(rq.count, 0, kQueueCounters * sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
     if (ens) ao_classify_kernel<S, true><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, nullptr, stats);
     else ao_classify_kernel<S, false><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, feat, stats);
@@ -437,6 +439,7 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
         if (e != cudaSuccess) return e;
         trace_mark(so.tracer, "ao_warm_start_inference", stream);
     }
+    if (before_pass1 && (e = cudaStreamWaitEvent(stream, before_pass1, 0)) != cudaSuccess) return e;
 #define NESF_AO_LAUNCH(PR, SK, EN) \
     ao_kernel<S, PR, SK, EN><<<pass1_grid(ao_kernel<S, PR, SK, EN>, grid, threads, sms,                       \
                                           !EN && PR != NESF_PLAIN_F64 && (so.fetch & NESF_FETCH_OCEAN)),     \
@@ -508,8 +511,8 @@ static cudaError_t preload_ao_t() {
 cudaError_t launch_ao(const AOArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream) {
-    return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, ws, stats, stream);
+                      cudaStream_t stream, cudaEvent_t before_pass1) {
+    return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, ws, stats, stream, before_pass1);
 }
 cudaError_t preload_ao_kernels(const AOArgs<double>*) { return preload_ao_t<double>(); }
 #endif
@@ -517,8 +520,8 @@ cudaError_t preload_ao_kernels(const AOArgs<double>*) { return preload_ao_t<doub
 cudaError_t launch_ao(const AOArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream) {
-    return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, ws, stats, stream);
+                      cudaStream_t stream, cudaEvent_t before_pass1) {
+    return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, ws, stats, stream, before_pass1);
 }
 cudaError_t preload_ao_kernels(const AOArgs<float>*) { return preload_ao_t<float>(); }
 #endif

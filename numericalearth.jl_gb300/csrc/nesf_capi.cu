@@ -22,8 +22,8 @@ struct nesf_context {
     DevIface<double>* d_p64;    // per-member parameters (ensemble)
     DevIface<float>* d_p32;
     int32_t capacity_members;
-    uint32_t* d_replay;         // replay + polish queues of the FP32 solvers (2 x capacity)
-    unsigned int* d_replay_count;   // [4]: the deferred queues [0..2], pass 1's fetch counter [3]
+    uint32_t* d_replay;         // the deferred-cell queues of the FP32 solvers (4 parts x capacity)
+    unsigned int* d_replay_count;   // [8]: the queue parts [0..3], pass 1's fetch counter [4]
     int64_t replay_capacity;
     uint32_t* d_work;           // compacted work lists of the solves
     unsigned int* d_work_count; // two counters per ensemble member
@@ -37,9 +37,12 @@ struct nesf_context {
     nesf_context* aux;
     cudaStream_t side;
     cudaEvent_t ev_fork, ev_ice, ev_join;
-    // the sea-ice solve's replay stream beside its polish pass, with fork/join events
+    // the sea-ice solve's replay stream beside its polish pass, with fork/join events, and its
+    // early lane (the calm cells' replays beside pass 1)
     cudaStream_t tail;
     cudaEvent_t ev_tail_fork, ev_tail_join;
+    cudaStream_t early;
+    cudaEvent_t ev_early_fork, ev_early_join;
     nesf_tuning tuning;         // launch shapes and schedule (nesf_set_tuning, nesf_autotune)
     struct TraceBuf* trace;     // kernel-boundary trace (nesf_trace_enable); the lane context borrows it
     bool trace_owned;
@@ -83,6 +86,7 @@ static nesf_tuning default_tuning() {
     t.io_overlap = 1;
     t.pass1_fetch = 2;
     t.refill_lanes = 8;
+    t.early_ocean_classify = 1;
     return t;
 }
 
@@ -355,6 +359,7 @@ void nesf_default_solver_options(nesf_solver_options* o) {
     o->fallback_ratio = 10.0;
     o->path_tolerance = 2e-6;
     o->fp32_rho = 0.9;
+    o->calm_replay_wind = 0.7;
 }
 
 // ---------------------------------------------------------------- context
@@ -387,12 +392,14 @@ int nesf_context_create(int32_t device, nesf_context** out) {
     c->ev_fork = c->ev_ice = c->ev_join = nullptr;
     c->tail = nullptr;
     c->ev_tail_fork = c->ev_tail_join = nullptr;
+    c->early = nullptr;
+    c->ev_early_fork = c->ev_early_join = nullptr;
     c->tuning = default_tuning();
     c->trace = nullptr;
     c->trace_owned = false;
     cudaError_t e = cudaMalloc(&c->d_stats, sizeof(DevStats));
     if (e == cudaSuccess) e = cudaMalloc(&c->d_partials, (size_t)kIntegralBlocks * NESF_MAX_INTEGRALS * 16);
-    if (e == cudaSuccess) e = cudaMalloc(&c->d_replay_count, 4 * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_replay_count, 8 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_stats, sizeof(DevStats));
     if (e != cudaSuccess) {
         cudaFree(c->d_stats);
@@ -427,6 +434,9 @@ int nesf_context_destroy(nesf_context* c) {
         if (c->tail) cudaStreamDestroy(c->tail);
         if (c->ev_tail_fork) cudaEventDestroy(c->ev_tail_fork);
         if (c->ev_tail_join) cudaEventDestroy(c->ev_tail_join);
+        if (c->early) cudaStreamDestroy(c->early);
+        if (c->ev_early_fork) cudaEventDestroy(c->ev_early_fork);
+        if (c->ev_early_join) cudaEventDestroy(c->ev_early_join);
         if (c->trace && c->trace_owned) {
             for (int i = 0; i < NESF_TRACE_MAX; i++) cudaEventDestroy(c->trace->ev[i]);
             delete c->trace;
@@ -511,7 +521,8 @@ static SolveOpts solve_opts(const nesf_solver_options& o, const nesf_context* ct
     return SolveOpts{o.polish_maxiter, (float)o.path_tolerance, rho, (float)o.fallback_ratio,
                      t.solve_block, t.deferred_per_sm, t.infer_per_sm,
                      (t.pass1_fetch >= 2 ? NESF_FETCH_SEA_ICE : 0) | (t.pass1_fetch >= 3 ? NESF_FETCH_OCEAN : 0),
-                     t.pass1_fetch == 4 ? (t.refill_lanes > 0 ? t.refill_lanes : 8) : 32, tracer_of(ctx)};
+                     t.pass1_fetch == 4 ? (t.refill_lanes > 0 ? t.refill_lanes : 8) : 32, tracer_of(ctx),
+                     (float)o.calm_replay_wind};
 }
 
 static int check_options(const nesf_solver_options& o, const char* who) {
@@ -519,6 +530,8 @@ static int check_options(const nesf_solver_options& o, const char* who) {
         return fail(NESF_ERR_ARG, "%s: precision %d", who, o.precision);
     if (o.warm_start && !o.mlp) return fail(NESF_ERR_ARG, "%s: warm_start without a network (mlp)", who);
     if (o.warm_start && !(o.fallback_ratio > 0)) return fail(NESF_ERR_ARG, "%s: fallback_ratio must be > 0", who);
+    if (!(o.calm_replay_wind >= 0) || o.calm_replay_wind > 1e3)
+        return fail(NESF_ERR_ARG, "%s: calm_replay_wind %g (0..1000 m/s)", who, o.calm_replay_wind);
     return NESF_OK;
 }
 
@@ -532,7 +545,7 @@ static int replay_queue(nesf_context* ctx, int64_t cells, ReplayQueue* q) {
         cudaFree(ctx->d_replay);
         ctx->d_replay = nullptr;
         ctx->replay_capacity = 0;
-        NESF_CUDA(cudaMalloc(&ctx->d_replay, 3 * sizeof(uint32_t) * (size_t)cells));
+        NESF_CUDA(cudaMalloc(&ctx->d_replay, 4 * sizeof(uint32_t) * (size_t)cells));
         ctx->replay_capacity = cells;
     }
     q->idx = ctx->d_replay;
@@ -541,14 +554,19 @@ static int replay_queue(nesf_context* ctx, int64_t cells, ReplayQueue* q) {
     return NESF_OK;
 }
 
-// The sea-ice solve's second stream for its deferred passes (created once; before
-// a graph capture by coupling_scratch).
+// The sea-ice solve's second and third streams for its deferred passes and its calm
+// cells' early replays (created once; before a graph capture by coupling_scratch).
 static int tail_lane(nesf_context* ctx) {
-    if (ctx->tail) return NESF_OK;
+    if (ctx->tail && ctx->early) return NESF_OK;
     DeviceGuard g(ctx->device);
-    NESF_CUDA(cudaEventCreateWithFlags(&ctx->ev_tail_fork, cudaEventDisableTiming));
-    NESF_CUDA(cudaEventCreateWithFlags(&ctx->ev_tail_join, cudaEventDisableTiming));
-    NESF_CUDA(cudaStreamCreateWithFlags(&ctx->tail, cudaStreamNonBlocking));
+    if (!ctx->tail) {
+        NESF_CUDA(cudaEventCreateWithFlags(&ctx->ev_tail_fork, cudaEventDisableTiming));
+        NESF_CUDA(cudaEventCreateWithFlags(&ctx->ev_tail_join, cudaEventDisableTiming));
+        NESF_CUDA(cudaStreamCreateWithFlags(&ctx->tail, cudaStreamNonBlocking));
+    }
+    NESF_CUDA(cudaEventCreateWithFlags(&ctx->ev_early_fork, cudaEventDisableTiming));
+    NESF_CUDA(cudaEventCreateWithFlags(&ctx->ev_early_join, cudaEventDisableTiming));
+    NESF_CUDA(cudaStreamCreateWithFlags(&ctx->early, cudaStreamNonBlocking));
     return NESF_OK;
 }
 
@@ -743,9 +761,10 @@ static int check_ao_fields(const nesf_ao_fields* f, const nesf_interface_params*
     return NESF_OK;
 }
 
-extern "C" int nesf_compute_atmosphere_ocean_fluxes(nesf_context* ctx, const nesf_interface_params* params,
-                                                    const nesf_ao_fields* f, const nesf_solver_options* opts,
-                                                    nesf_stats* stats, void* stream) {
+// The atmosphere-ocean solve; before_pass1 (optional): an event its stream waits for after the
+// classify pass and the warm-start inference, before pass 1.
+static int ocean_fluxes(nesf_context* ctx, const nesf_interface_params* params, const nesf_ao_fields* f,
+                        const nesf_solver_options* opts, nesf_stats* stats, void* stream, cudaEvent_t before_pass1) {
     const char* who = "nesf_compute_atmosphere_ocean_fluxes";
     int r = check_params(params, who);
     if (r) return r;
@@ -770,10 +789,16 @@ extern "C" int nesf_compute_atmosphere_ocean_fluxes(nesf_context* ctx, const nes
     return with_stats(ctx, stats, s, [&](DevStats* ds) {
         if (f->dtype == NESF_F64)
             return launch_ao(ao_args<double>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl, rq, ws,
-                             ds, s);
+                             ds, s, before_pass1);
         return launch_ao(ao_args<float>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl, rq, ws, ds,
-                         s);
+                         s, before_pass1);
     });
+}
+
+extern "C" int nesf_compute_atmosphere_ocean_fluxes(nesf_context* ctx, const nesf_interface_params* params,
+                                                    const nesf_ao_fields* f, const nesf_solver_options* opts,
+                                                    nesf_stats* stats, void* stream) {
+    return ocean_fluxes(ctx, params, f, opts, stats, stream, nullptr);
 }
 
 extern "C" int nesf_compute_atmosphere_ocean_fluxes_ensemble(nesf_context* ctx, const nesf_interface_params* params,
@@ -965,16 +990,19 @@ static int sea_ice_fluxes(nesf_context* ctx, const nesf_interface_params* params
     if ((r = work_list(ctx, ring, 1, &wl))) return r;
     if ((r = warm_buffers(ctx, o, ring, &ws))) return r;
     SolveOpts so = solve_opts(o, ctx);
-    // the replay of pass 1's cells beside the polish pass (the tuning's two_lanes)
-    TailLane tl{nullptr, nullptr, nullptr};
+    // the replay of pass 1's cells beside the polish pass and the calm cells' replays beside
+    // pass 1 (the tuning's two_lanes)
+    TailLane tl{nullptr, nullptr, nullptr}, el{nullptr, nullptr, nullptr};
     if (o.precision == NESF_F32_ADAPTIVE && ctx->tuning.two_lanes) {
         if ((r = tail_lane(ctx))) return r;
         tl = TailLane{ctx->tail, ctx->ev_tail_fork, ctx->ev_tail_join};
+        el = TailLane{ctx->early, ctx->ev_early_fork, ctx->ev_early_join};
     }
     return with_stats(ctx, stats, s, [&](DevStats* ds) {
         if (f->dtype == NESF_F64)
-            return launch_ai(ai_args<double>(f), P64, P32, o.precision, so, wl, rq, ws, ds, s, after_solve, &tl);
-        return launch_ai(ai_args<float>(f), P64, P32, o.precision, so, wl, rq, ws, ds, s, after_solve, &tl);
+            return launch_ai(ai_args<double>(f), P64, P32, o.precision, so, wl, rq, ws, ds, s, after_solve, &tl,
+                             &el);
+        return launch_ai(ai_args<float>(f), P64, P32, o.precision, so, wl, rq, ws, ds, s, after_solve, &tl, &el);
     });
 }
 
@@ -1266,10 +1294,10 @@ extern "C" int nesf_compute_atmosphere_ocean_fluxes_noalloc(const nesf_interface
     }
     if (!base) return fail(NESF_ERR_ARG, "%s: device %d not prepared (call nesf_noalloc_prepare(%d) at set-up)", who,
                             dev, dev);
-    // counters: base[0..1] the work list's counts (unstable, stable); base[2..5] the
-    // queue counters rq.count[0..3] (replays, polishes, the sea-ice solve's polish
-    // replays (unused here), pass 1's fetch counter); the launch clears the counters a
-    // precision uses before its first pass reads them
+    // counters: base[0..1] the work list's counts (unstable, stable); base[2..6] the
+    // queue counters rq.count[0..4] (replays, polishes, the sea-ice solve's polish and
+    // calm replays (unused here), pass 1's fetch counter); the launch clears the counters
+    // a precision uses before its first pass reads them
     WorkList wl{base + 64, base, ring};
     ReplayQueue rq{base + 64 + NESF_NOALLOC_MAX_CELLS, base + 2, NESF_NOALLOC_MAX_CELLS};
     DevIface<double> P64 = make_dev_iface<double>(*params);
@@ -1507,10 +1535,13 @@ extern "C" int nesf_coupling_step(nesf_context* ctx, const nesf_coupling_step_ar
         }
         if (io_split && (r = sea_ice_ocean(ctx, a->io_params, a->io, stream, 1))) return r;
         if (io_split) trace_mark(tr, "sea_ice_ocean_fluxes", s);
-        if (lanes) NESF_CUDA(cudaStreamWaitEvent(s, ctx->ev_ice, 0));
-        else if ((r = sea_ice_fluxes(ctx->aux, a->ai_params, a->ai, opts, nullptr, s, nullptr))) return r;
+        if (lanes && !ctx->tuning.early_ocean_classify) NESF_CUDA(cudaStreamWaitEvent(s, ctx->ev_ice, 0));
+        else if (!lanes && (r = sea_ice_fluxes(ctx->aux, a->ai_params, a->ai, opts, nullptr, s, nullptr))) return r;
     }
-    if ((r = nesf_compute_atmosphere_ocean_fluxes(ctx, a->ao_params, a->ao, opts, nullptr, stream))) return r;
+    // with early_ocean_classify the ocean's classify pass and warm-start inference run beside the
+    // sea-ice pass 1, and its pass 1 waits for the sea-ice pass 1 instead
+    cudaEvent_t before_pass1 = lanes && ctx->tuning.early_ocean_classify ? ctx->ev_ice : nullptr;
+    if ((r = ocean_fluxes(ctx, a->ao_params, a->ao, opts, nullptr, stream, before_pass1))) return r;
     if (lanes) {
         DeviceGuard g(ctx->device);
         NESF_CUDA(cudaStreamWaitEvent(s, ctx->ev_join, 0));
@@ -1739,6 +1770,8 @@ static int check_tuning(const nesf_tuning& t, const char* who) {
         return fail(NESF_ERR_ARG, "%s: pass1_fetch %d (1, 2, 3 or 4)", who, t.pass1_fetch);
     if (t.refill_lanes < 0 || t.refill_lanes > 32)
         return fail(NESF_ERR_ARG, "%s: refill_lanes %d (1..32)", who, t.refill_lanes);
+    if (t.early_ocean_classify < 0 || t.early_ocean_classify > 1)
+        return fail(NESF_ERR_ARG, "%s: early_ocean_classify is 0 or 1", who);
     return NESF_OK;
 }
 
@@ -1826,6 +1859,7 @@ extern "C" int nesf_autotune(nesf_context* ctx, const nesf_coupling_step_args* a
         {&nesf_tuning::refill_lanes, {8, 4, 16}, adaptive},
         {&nesf_tuning::two_lanes, {1, 0}, ice},
         {&nesf_tuning::io_overlap, {1, 0}, ice && a->io_params != nullptr},
+        {&nesf_tuning::early_ocean_classify, {1, 0}, ice},
     };
     for (const Axis& ax : axes) {
         if (r || !ax.used) continue;

@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(256) interp_kernel(InterpArgs<S> a) {
 // expressions, same order: bit-identical outputs). A tile whose footprint would exceed
 // the staged bounds (fp_w x fp_h, sized on the host) reads its corners from global memory.
 constexpr int kInterpTileCols = 256;
-constexpr int kInterpMaxTileRows = 32;
+constexpr int kInterpMaxTileRows = 16;
 
 template <class S>
 __global__ void __launch_bounds__(kInterpTileCols) interp_tile_kernel(InterpArgs<S> a) {
@@ -279,17 +279,15 @@ __global__ void __launch_bounds__(kInterpTileCols) interp_tile_kernel(InterpArgs
     const int W = staged ? (int)W64 : 0, H = staged ? (int)H64 : 0;
     const int plane = W * H;
     if (staged) {
-        const int total = 18 * plane;
-        for (int e = threadIdx.x; e < total; e += kInterpTileCols) {
-            const int var = e / (2 * plane), t = (e / plane) & 1, rc = e % plane;
-            const int r = rc / W, c = rc % W;
-            const S* b = a.src[var];
-            S v = S(0);
-            if (b) {
-                const int ii = wrap_i(imin + c, ag.nx), jj = jmin + r;
-                v = __ldg(b + (int64_t)t * ag.stride_t + (int64_t)(ii - 1 + ag.hx) + (int64_t)(jj - 1 + ag.hy) * ag.stride_j);
+        // one (row, column) per element of the footprint, the 18 planes (variable, snapshot) in turn
+        for (int e = threadIdx.x; e < plane; e += kInterpTileCols) {
+            const int r = e / W, c = e - r * W;
+            const int64_t at = (int64_t)(wrap_i(imin + c, ag.nx) - 1 + ag.hx) + (int64_t)(jmin + r - 1 + ag.hy) * ag.stride_j;
+#pragma unroll
+            for (int q = 0; q < 18; q++) {
+                const S* b = a.src[q >> 1];
+                stage[q * plane + e] = b ? __ldg(b + (int64_t)(q & 1) * ag.stride_t + at) : S(0);
             }
-            stage[e] = v;
         }
     }
     __syncthreads();

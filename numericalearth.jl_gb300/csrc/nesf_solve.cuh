@@ -52,6 +52,8 @@ struct SolveOpts {
     int refill;            // adaptive pass 1 with warp fetching: lanes idle before a warp takes new
                            // entries for them (32: all, the warp fetching; fewer: lane refill)
     const Tracer* tracer;  // host side: kernel-boundary trace (null: off)
+    float calm_wind;       // adaptive sea-ice solve with an early lane: wind speed below which the
+                           // classify pass sends a cell straight to the FP64 replay (0: none)
 };
 
 // Warm start of a solve: features written by the classify pass at the work-list
@@ -75,10 +77,13 @@ struct WorkList {
 // Cells deferred to the packed passes, in parts of `capacity` entries: part 0 the
 // cells to replay in FP64, part 1 the cells to polish (ADAPTIVE), part 2 (the
 // sea-ice solve's, which replays the polish pass's cells apart so that the replay
-// of pass 1's cells runs beside the polish pass) the polish pass's replays;
-// count[part] are their numbers (zeroed before the solve), and count[3] is pass 1's
-// fetch counter (SolveOpts::fetch). A cell that the polish pass sends on to a replay
-// holds one entry in each of two parts.
+// of pass 1's cells runs beside the polish pass) the polish pass's replays, part 3
+// (the sea-ice solve's) the calm cells its classify pass sends straight to the
+// replay (SolveOpts::calm_wind); count[part] are their numbers (zeroed before the
+// solve), and count[kFetchCounter] is pass 1's fetch counter (SolveOpts::fetch). A
+// cell that the polish pass sends on to a replay holds one entry in each of two parts.
+constexpr int kFetchCounter = 4;
+constexpr int kQueueCounters = 5;
 struct ReplayQueue {
     uint32_t* idx;          // linear cell ids (member * ring + ring index)
     unsigned int* count;
@@ -962,7 +967,7 @@ __device__ __forceinline__ void polish_push(const ReplayQueue& q, bool want, uin
 // concerned: an event comes when no lane is sweeping, or, with lane refill, when `refill`
 // lanes are done or empty. Schedules:
 //   fetch = false: one work-list entry per thread (the grid covers the list), no refill;
-//   fetch, refill = 32: the resident warps take the next 32 entries (counter rq.count[3])
+//   fetch, refill = 32: the resident warps take the next 32 entries (rq.count[kFetchCounter])
 //     when all their cells are done -- warp fetching;
 //   fetch, refill < 32: a warp takes new entries for its idle lanes as soon as `refill` of
 //     them are idle -- lane refill: a cell that converges early frees its lane for a new
@@ -1006,7 +1011,7 @@ __device__ __forceinline__ void adaptive_pass1(Cell& cell, const DevIface<float>
                 if (nb) {
                     const int leader = __ffs(nb) - 1;
                     unsigned base = 0;
-                    if (lane == leader) base = atomicAdd(&rq.count[3], (unsigned)__popc(nb));
+                    if (lane == leader) base = atomicAdd(&rq.count[kFetchCounter], (unsigned)__popc(nb));
                     base = __shfl_sync(0xffffffffu, base, leader);
                     if (need) {
                         const unsigned pos = base + __popc(nb & ((1u << lane) - 1u));
@@ -1054,26 +1059,32 @@ inline dim3 pass1_grid(K kernel, dim3 grid, int threads, int sms, bool fetch) {
     return grid;
 }
 
+// before_pass1 (optional): an event the stream waits for after the classify pass and the
+// warm-start inference, before pass 1.
 cudaError_t launch_ao(const AOArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream);
+                      cudaStream_t stream, cudaEvent_t before_pass1 = nullptr);
 cudaError_t launch_ao(const AOArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream);
+                      cudaStream_t stream, cudaEvent_t before_pass1 = nullptr);
 // Loads (under lazy module loading) every kernel that the one-member atmosphere-ocean
 // solve of storage S can launch, so that a later launch loads no module.
 cudaError_t preload_ao_kernels(const AOArgs<double>*);
 cudaError_t preload_ao_kernels(const AOArgs<float>*);
 // after_solve (optional): recorded once the pass-1 solve is enqueued.
 // tail (optional): a second stream on which pass 1's replays run beside the polish pass.
+// early (optional): a third stream on which the calm cells' replays run from the classify
+// pass on, beside pass 1 (SolveOpts::calm_wind; without it no cell is sent early).
 cudaError_t launch_ai(const AIArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream, cudaEvent_t after_solve = nullptr, const TailLane* tail = nullptr);
+                      cudaStream_t stream, cudaEvent_t after_solve = nullptr, const TailLane* tail = nullptr,
+                      const TailLane* early = nullptr);
 cudaError_t launch_ai(const AIArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream, cudaEvent_t after_solve = nullptr, const TailLane* tail = nullptr);
+                      cudaStream_t stream, cudaEvent_t after_solve = nullptr, const TailLane* tail = nullptr,
+                      const TailLane* early = nullptr);
 cudaError_t launch_al(const ALArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, DevStats* stats, cudaStream_t stream);
 cudaError_t launch_al(const ALArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,

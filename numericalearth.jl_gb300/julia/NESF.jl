@@ -136,7 +136,7 @@ end
 struct SolverOptions
     precision::Int32; polish_maxiter::Int32; block_size::Int32; schedule::Int32
     ctas_per_sm::Int32; warm_start::Int32; mlp::Ptr{Cvoid}
-    fallback_ratio::Float64; path_tolerance::Float64; fp32_rho::Float64
+    fallback_ratio::Float64; path_tolerance::Float64; fp32_rho::Float64; calm_replay_wind::Float64
 end
 
 struct AOFields
@@ -263,7 +263,7 @@ precision_code(f::GB300SimilarityTheoryFluxes) = f.precision === :f32 ? NESF_F32
                                                   f.precision === :f32_adaptive ? NESF_F32_ADAPTIVE : NESF_PLAIN_F64
 solver_options(model::GB300Model) =
     SolverOptions(precision_code(model.interfaces.atmosphere_ocean_interface.flux_formulation), 0, 0, 0, 0, 0,
-                  C_NULL, 10.0, 2e-6, 0.9)
+                  C_NULL, 10.0, 2e-6, 0.9, 0.7)
 
 # ---------------------------------------------------------------- plumbing
 check(code) = code == NESF_OK ||
@@ -877,7 +877,7 @@ function al_fluxes!(model, interface)
                       devptr(out.x_momentum), devptr(out.y_momentum),
                       devptr(out.friction_velocity), devptr(out.temperature_scale), devptr(out.water_vapor_scale),
                       devptr(interface.temperature), C_NULL)
-    opts = SolverOptions(precision_code(interface.flux_formulation), 0, 0, 0, 0, 0, C_NULL, 10.0, 2e-6, 0.9)
+    opts = SolverOptions(precision_code(interface.flux_formulation), 0, 0, 0, 0, 0, C_NULL, 10.0, 2e-6, 0.9, 0.7)
     check(ccall((:nesf_compute_atmosphere_land_fluxes, libnesf), Cint,
                 (Ptr{Cvoid}, Ref{InterfaceParams}, Ref{ALFields}, Ref{SolverOptions}, Ptr{Cvoid}, Ptr{Cvoid}),
                 C_NULL, r, fields, opts, C_NULL, stream()))

@@ -132,7 +132,7 @@ class InterfaceParams(C.Structure):
 class SolverOptions(C.Structure):
     _fields_ = [("precision", i32), ("polish_maxiter", i32), ("block_size", i32), ("schedule", i32),
                 ("ctas_per_sm", i32), ("warm_start", i32), ("mlp", vp), ("fallback_ratio", d), ("path_tolerance", d),
-                ("fp32_rho", d)]
+                ("fp32_rho", d), ("calm_replay_wind", d)]
 
 
 class Stats(C.Structure):
@@ -291,11 +291,12 @@ class IntegralFields(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("solve_block", i32), ("deferred_per_sm", i32), ("infer_per_sm", i32), ("two_lanes", i32),
-                ("io_overlap", i32), ("pass1_fetch", i32), ("refill_lanes", i32), ("step_ms", d)]
+                ("io_overlap", i32), ("pass1_fetch", i32), ("refill_lanes", i32), ("early_ocean_classify", i32),
+                ("step_ms", d)]
 
 
 TUNING_FIELDS = ("solve_block", "deferred_per_sm", "infer_per_sm", "two_lanes", "io_overlap", "pass1_fetch",
-                 "refill_lanes")
+                 "refill_lanes", "early_ocean_classify")
 
 TRACE_MAX = 64
 

@@ -66,13 +66,16 @@ def default_context(device=None):
     return _DEFAULT_CTX[dev]
 
 
-def solver_options(precision="f64", polish_maxiter=0, mlp=None):
-    """nesf_solver_options; `mlp` (a warm.WarmStartNetwork) turns on the learned warm start.
+def solver_options(precision="f64", polish_maxiter=0, mlp=None, calm_replay_wind=None):
+    """nesf_solver_options; `mlp` (a warm.WarmStartNetwork) turns on the learned warm start;
+    `calm_replay_wind` (m/s) overrides the library's default for the sea-ice solve's calm cells.
     Launch shapes are the context's tuning (set_tuning, autotune), not options of a call."""
     o = A.SolverOptions()
     load().nesf_default_solver_options(C.byref(o))
     o.precision = PRECISIONS[precision]
     o.polish_maxiter = polish_maxiter
+    if calm_replay_wind is not None:
+        o.calm_replay_wind = float(calm_replay_wind)
     if mlp is not None:
         o.warm_start = 1
         o.mlp = mlp.ptr
@@ -99,7 +102,7 @@ def compute_atmosphere_ocean_fluxes(spec, layout, state, out, precision="f64", p
     arrays["iterations"] = iterations
     f = F.pack(A.AOFields, _grid_of(layout), arrays)
     p = spec.to_c() if hasattr(spec, "to_c") else spec
-    o = solver_options(precision, polish_maxiter, mlp=mlp)
+    o = solver_options(precision, polish_maxiter, mlp=mlp, calm_replay_wind=calm_replay_wind)
     st = A.Stats() if stats else None
     ctx = ctx or default_context()
     check(lib.nesf_compute_atmosphere_ocean_fluxes(ctx.handle, C.byref(p), C.byref(f), C.byref(o),
@@ -128,7 +131,7 @@ def compute_atmosphere_ocean_fluxes_ensemble(specs, layout, state, out, precisio
 
 
 def compute_atmosphere_sea_ice_fluxes(spec, layout, state, out, precision="f64", polish_maxiter=0, stats=False,
-                                      iterations=None, ctx=None, stream=None, mlp=None):
+                                      iterations=None, ctx=None, stream=None, mlp=None, calm_replay_wind=None):
     """atmosphere_sea_ice_fluxes.jl:18-62; `out['interface_temperature']` is read as the
     initial skin temperature and overwritten with the solved one."""
     lib = load()

@@ -305,6 +305,38 @@ def test_assembly_and_radiation_match_oracle(oracle, coupled64):
     assert np.all(I(to_numpy(dev["ocean_T"]))[land] == 0)
 
 
+@pytest.mark.parametrize("wind", [0.0, 0.7, 1000.0])
+def test_sea_ice_calm_cells_replay_from_the_classify_pass(oracle, coupled64, wind):
+    """The adaptive sea-ice solve sends the cells whose wind is below calm_replay_wind from its
+    classify pass straight to the reference's FP64 iteration, on a stream of their own beside
+    pass 1: none (0), the calm ones (0.7 m/s, the default) or every ice cell (1000 m/s). The
+    fluxes stay within 1e-5 of the oracle, every cell is counted once, and with every cell
+    replayed all of them are solved by the FP64 iteration."""
+    import torch
+    st = coupled64
+    spec = P.atmosphere_sea_ice_interface_spec()
+    ref = oracle.ai_fluxes(spec.to_c(), st.layout, st.fields, st.fields["ice_temperature"])
+    dev = api.to_device({k: st.fields.get(k) for k in F.AI_INPUTS if k in st.fields})
+    out = {k: torch.zeros(st.layout.shape, dtype=torch.float64, device="cuda") for k in F.AI_OUTPUTS}
+    out["interface_temperature"] = torch.from_numpy(st.fields["ice_temperature"].copy()).cuda()
+    s = api.compute_atmosphere_sea_ice_fluxes(spec, st.layout, dev, out, precision="f32_adaptive", stats=True,
+                                              calm_replay_wind=wind)
+    torch.cuda.synchronize()
+    R = st.layout.ring
+    conv = R(ref["iterations"]) < 100
+    for k in F.AI_OUTPUTS + ("interface_temperature",):
+        g, r = R(to_numpy(out[k])), R(ref[k])
+        if k == "interface_temperature":
+            g, r = g + 273.15, r + 273.15
+        e = rel_err(g, r, floor_frac=1e-6)[conv]
+        assert e.max() <= 1e-5, (wind, k, float(e.max()))
+    ice = int(((R(st.fields["ice_concentration"]) > 0) & (R(st.fields["inactive"]) == 0)).sum())
+    assert s["cells"] == R(st.fields["ice_concentration"]).size
+    assert s["solved"] == ice
+    if wind > 100:
+        assert s["fp64_redo"] == ice and s["polished"] == 0
+
+
 def test_ensemble_members_use_their_own_parameters(oracle):
     import torch
     members = 4
