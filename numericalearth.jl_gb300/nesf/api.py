@@ -424,12 +424,12 @@ def timeline(marks):
 class Graph:
     """A captured CUDA graph of one coupling step (nesf_graph_capture)."""
 
-    def __init__(self, step, precision="f32_adaptive", ctx=None, mlp=None):
+    def __init__(self, step, precision="f32_adaptive", ctx=None, mlp=None, calm_replay_wind=None):
         self.lib = load()
         self.step = step                     # keeps the captured pointers' owners alive
         self.mlp = mlp                       # and the network the graph reads
         self.ctx = ctx or default_context()
-        o = solver_options(precision, mlp=mlp)
+        o = solver_options(precision, mlp=mlp, calm_replay_wind=calm_replay_wind)
         h = C.c_void_p()
         check(self.lib.nesf_graph_capture(self.ctx.handle, C.byref(step.args), C.byref(o), C.byref(h)))
         self.handle = h

@@ -188,9 +188,10 @@ class CoupledModel:
         self.reset()
         return t
 
-    def capture(self, precision="f32_adaptive"):
-        """Capture one coupling step as a CUDA graph (nesf_graph_capture)."""
-        self.graph = api.Graph(self.step_args(), precision, mlp=self.mlp)
+    def capture(self, precision="f32_adaptive", calm_replay_wind=None):
+        """Capture one coupling step as a CUDA graph (nesf_graph_capture); `calm_replay_wind`
+        overrides the library's default for the sea-ice solve's calm cells."""
+        self.graph = api.Graph(self.step_args(), precision, mlp=self.mlp, calm_replay_wind=calm_replay_wind)
         self.graph_precision = precision
         return self.graph
 
