@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--small", action="store_true", help="small grid (profiling captures)")
     ap.add_argument("--no-plain", action="store_true", help="time only --precision (profiling captures)")
     ap.add_argument("--cold", action="store_true", help="no learned warm start")
+    ap.add_argument("--warm-samples", default="1e7", choices=["1e7", "4e5"], help="warm-start training set")
     ap.add_argument("--no-autotune", action="store_true", help="default launch shapes (no nesf_autotune)")
     ap.add_argument("--no-configs", action="store_true", help="skip the measurements of configurations 0-3")
     return ap.parse_args()
@@ -152,28 +153,54 @@ def make_state(small):
 AO_KERNEL_DRAM_BYTES_PER_CELL = 64.0
 
 
-def train_warm_start(seed=0):
+# warm-start training sets: "1e7" -- about 1e7 solver-generated samples, the scale the
+# 1/8-degree workload's configuration names: two open-ocean states of 2880 x 1280 with 0-40 m/s
+# winds and -15..+10 K air-sea differences (7.4 M cells) and four coupled 1440 x 720 states
+# like the workload's (2.9 M water cells); "4e5" -- the small set (four 360 x 180 open-ocean
+# states, three coupled 360 x 180 states)
+WARM_SETS = {
+    "1e7": dict(open_ocean=[(2880, 1280)] * 2, coupled=[(1440, 720)] * 4,
+                schedule=((2, 2e-3), (1, 5e-4), (1, 1e-4)), batch=4096),
+    "4e5": dict(open_ocean=[(360, 180)] * 4, coupled=[(360, 180)] * 3,
+                schedule=((12, 2e-3), (8, 5e-4), (5, 1e-4)), batch=2048),
+}
+
+
+def train_warm_start(seed=0, samples="1e7"):
     """Train the warm-start network on solver-generated samples (open-ocean states with 0-40 m/s
     winds and -15..+10 K air-sea differences, and coupled states like the workload's), on the
-    tensor cores; returns the network and a summary."""
+    tensor cores; returns the network and a summary (sample count, epochs, losses, seconds
+    for the samples and for the training)."""
     import torch
     from nesf import params as P
     from nesf import synthetic as syn
     from nesf import warm
+    cfg = WARM_SETS[samples]
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
     spec = P.atmosphere_ocean_interface_spec()
-    states = [syn.warm_training_state(seed=7000 + k, nx=360, ny=180) for k in range(4)]
-    states += [syn.coupled(seed=7100 + k, nx=360, ny=180, lat_s=-80, lat_n=80, land=0.3, interpolate=False)
-               for k in range(3)]
-    x, t = warm.training_set(spec, states)
+
+    def states():
+        for k, (nx, ny) in enumerate(cfg["open_ocean"]):
+            yield syn.warm_training_state(seed=7000 + k, nx=nx, ny=ny)
+        for k, (nx, ny) in enumerate(cfg["coupled"]):
+            yield syn.coupled(seed=7100 + k, nx=nx, ny=ny, lat_s=-80, lat_n=80, land=0.3, interpolate=False)
+
+    x, t = warm.training_set(spec, states(), shuffle_seed=seed + 11)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
     net = warm.WarmStartNetwork(seed=seed)
     net.fit_normalization(x, t)
     losses = []
-    for epochs, lr in ((12, 2e-3), (8, 5e-4), (5, 1e-4)):
-        losses += net.train(x, t, epochs=epochs, batch=2048, lr=lr)
+    for epochs, lr in cfg["schedule"]:
+        losses += net.train(x, t, epochs=epochs, batch=cfg["batch"], lr=lr)
     torch.cuda.synchronize()
-    return net, {"samples": int(x.shape[0]), "epochs": len(losses), "loss_first": losses[0],
-                 "loss_last": losses[-1], "seconds": time.perf_counter() - t0}
+    t2 = time.perf_counter()
+    n = int(x.shape[0])
+    del x, t
+    return net, {"samples": n, "set": samples, "epochs": len(losses), "batch": cfg["batch"],
+                 "loss_first": losses[0], "loss_last": losses[-1], "seconds_samples": t1 - t0,
+                 "seconds_training": t2 - t1, "seconds": t2 - t0}
 
 
 def phase_times(model, precision, reps=3):
@@ -879,7 +906,7 @@ def main():
     prec = args.precision
     warm_info = None
     if prec != "f64" and not args.cold:
-        model.mlp, warm_info = train_warm_start()
+        model.mlp, warm_info = train_warm_start(samples=args.warm_samples)
     # launch shapes and schedule from the autotuner (nesf_autotune), on this workload
     tuning = model.autotune(prec, reps=3) if not args.no_autotune else None
 

@@ -825,6 +825,50 @@ int nesf_get_tuning(nesf_context* ctx, nesf_tuning* tuning);
 int nesf_autotune(nesf_context* ctx, const nesf_coupling_step_args* args, const nesf_solver_options* opts,
                   int32_t reps, nesf_tuning* out, void* stream);
 
+/* The autotuner's results on disk, so that a model is tuned once per device and
+ * workload rather than once per run. A key names what a tuning was measured on; a
+ * cache file (any path the caller picks) holds one tuning per key. Format, every
+ * integer little-endian whatever the host:
+ *   "NESFTUNE" (8 bytes), uint32 format version (NESF_TUNING_VERSION), uint32 key
+ *   bytes (108), uint32 tuning fields (8), uint32 record count, then per record the
+ *   key (device name, 64 bytes NUL-padded, then its eleven int32 fields) and the
+ *   tuning (its eight int32 fields in declaration order, then step_ms as the
+ *   IEEE-754 bits of a double).
+ * A file of another format version or tuning-field count holds nothing for this
+ * library: find reports no entry and store starts the file afresh. A file that does
+ * not start with the magic, or is cut short, is an argument error (store does not
+ * overwrite it). Store writes `path`.tmp and renames it over `path`; concurrent
+ * writers of one path may lose each other's entries. No reference counterpart (the
+ * reference has no autotuner). */
+#define NESF_TUNING_VERSION 1
+typedef struct {
+    char device[64];              /* cudaDeviceProp::name, NUL-padded                         */
+    int32_t sm_count;             /* multiprocessors                                          */
+    int32_t compute_capability;   /* major * 10 + minor                                       */
+    int32_t nx, ny;               /* interior grid of the atmosphere-ocean fields             */
+    int32_t hx, hy;               /* their halo widths                                        */
+    int32_t dtype;                /* nesf_dtype of the fields                                 */
+    int32_t precision;            /* nesf_solver_options.precision                            */
+    int32_t warm_start;           /* 1: the step runs with a warm-start network               */
+    int32_t parts;                /* bit 0 sea ice, 1 sea-ice-ocean fluxes, 2 interpolation,
+                                     3 net-flux assembly, 4 radiative add-ons                 */
+    int32_t flux_formulation;     /* the atmosphere-ocean params' flux_formulation            */
+} nesf_tuning_key;
+
+/* The key of a coupling step on the context's device. */
+int nesf_tuning_key_of(nesf_context* ctx, const nesf_coupling_step_args* args, const nesf_solver_options* opts,
+                       nesf_tuning_key* key);
+/* The cached tuning of `key`: *found = 1 and the tuning in `out`, or *found = 0 (no
+ * file, a stale file, or no record of the key). Host only. */
+int nesf_tuning_cache_find(const char* path, const nesf_tuning_key* key, nesf_tuning* out, int32_t* found);
+/* Record `tuning` for `key` (replacing an earlier record of the key). Host only. */
+int nesf_tuning_cache_store(const char* path, const nesf_tuning_key* key, const nesf_tuning* tuning);
+/* nesf_autotune through the cache: the cached tuning of this step's key is set on the
+ * context without running a step (*from_cache = 1); otherwise the search runs and its
+ * result is stored (*from_cache = 0). */
+int nesf_autotune_cached(nesf_context* ctx, const nesf_coupling_step_args* args, const nesf_solver_options* opts,
+                         int32_t reps, const char* path, nesf_tuning* out, int32_t* from_cache, void* stream);
+
 /* ------------------------------------------------------- algorithmic work
  * Work per unit of the similarity solve, the roofline's numerator: transcendental
  * calls (pow counted as one; sqrt and cbrt included) and other floating-point

@@ -7,6 +7,7 @@
 #include <cstring>
 #include <cstdarg>
 #include <mutex>
+#include <string>
 #include <vector>
 #include <new>
 
@@ -149,7 +150,7 @@ int32_t nesf_struct_sizes(int64_t* sizes, int32_t n) {
         (int64_t)sizeof(nesf_coupling_step_args), (int64_t)sizeof(nesf_integral_fields),
         (int64_t)sizeof(nesf_tuning), (int64_t)sizeof(nesf_trace_entry), (int64_t)sizeof(nesf_coefficient_fluxes),
         (int64_t)sizeof(nesf_al_fields), (int64_t)sizeof(nesf_land_radiation_params),
-        (int64_t)sizeof(nesf_land_flux_fields)};
+        (int64_t)sizeof(nesf_land_flux_fields), (int64_t)sizeof(nesf_tuning_key)};
     int32_t m = (int32_t)(sizeof s / sizeof s[0]);
     for (int32_t k = 0; k < n && k < m; k++) sizes[k] = s[k];
     return m;
@@ -1886,4 +1887,228 @@ extern "C" int nesf_autotune(nesf_context* ctx, const nesf_coupling_step_args* a
     ctx->tuning = best;
     if (out) *out = best;
     return NESF_OK;
+}
+
+// ------------------------------------------------------- the tuning cache on disk
+// Explicit little-endian serialisation (no struct dumps), so that a file is read the
+// same on any host.
+namespace {
+
+constexpr char kTuneMagic[8] = {'N', 'E', 'S', 'F', 'T', 'U', 'N', 'E'};
+constexpr int kKeyInts = 11;
+constexpr uint32_t kKeyBytes = 64 + 4 * kKeyInts;
+constexpr int kTuneInts = 8;
+constexpr size_t kRecordBytes = kKeyBytes + 4 * kTuneInts + 8;
+constexpr size_t kHeaderBytes = 8 + 4 * 4;
+
+void put_u32(std::vector<unsigned char>& b, uint32_t v) {
+    for (int i = 0; i < 4; i++) b.push_back((unsigned char)(v >> (8 * i)));
+}
+void put_u64(std::vector<unsigned char>& b, uint64_t v) {
+    for (int i = 0; i < 8; i++) b.push_back((unsigned char)(v >> (8 * i)));
+}
+uint32_t get_u32(const unsigned char* p) {
+    return (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
+}
+uint64_t get_u64(const unsigned char* p) {
+    return (uint64_t)get_u32(p) | ((uint64_t)get_u32(p + 4) << 32);
+}
+
+void key_ints(const nesf_tuning_key& k, int32_t* v) {
+    const int32_t w[kKeyInts] = {k.sm_count, k.compute_capability, k.nx, k.ny, k.hx, k.hy,
+                                 k.dtype, k.precision, k.warm_start, k.parts, k.flux_formulation};
+    std::memcpy(v, w, sizeof(w));
+}
+void tune_ints(const nesf_tuning& t, int32_t* v) {
+    const int32_t w[kTuneInts] = {t.solve_block, t.deferred_per_sm, t.infer_per_sm, t.two_lanes,
+                                  t.io_overlap, t.pass1_fetch, t.refill_lanes, t.early_ocean_classify};
+    std::memcpy(v, w, sizeof(w));
+}
+
+void put_key(std::vector<unsigned char>& b, const nesf_tuning_key& k) {
+    char name[64];
+    std::memset(name, 0, sizeof(name));
+    std::memcpy(name, k.device, strnlen(k.device, sizeof(k.device)));
+    b.insert(b.end(), name, name + 64);
+    int32_t v[kKeyInts];
+    key_ints(k, v);
+    for (int32_t x : v) put_u32(b, (uint32_t)x);
+}
+
+void put_tuning(std::vector<unsigned char>& b, const nesf_tuning& t) {
+    int32_t v[kTuneInts];
+    tune_ints(t, v);
+    for (int32_t x : v) put_u32(b, (uint32_t)x);
+    uint64_t bits;
+    std::memcpy(&bits, &t.step_ms, 8);
+    put_u64(b, bits);
+}
+
+nesf_tuning get_tuning_record(const unsigned char* p) {
+    int32_t v[kTuneInts];
+    for (int i = 0; i < kTuneInts; i++) v[i] = (int32_t)get_u32(p + 4 * i);
+    nesf_tuning t;
+    std::memset(&t, 0, sizeof(t));
+    t.solve_block = v[0]; t.deferred_per_sm = v[1]; t.infer_per_sm = v[2]; t.two_lanes = v[3];
+    t.io_overlap = v[4]; t.pass1_fetch = v[5]; t.refill_lanes = v[6]; t.early_ocean_classify = v[7];
+    const uint64_t bits = get_u64(p + 4 * kTuneInts);
+    std::memcpy(&t.step_ms, &bits, 8);
+    return t;
+}
+
+// The records of a cache file: NESF_OK with `stale` set when the file is missing or
+// of another version (no records); an argument error when it is not a cache file.
+int read_cache(const char* path, const char* who, std::vector<unsigned char>& records, bool& stale) {
+    records.clear();
+    stale = false;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) {
+        stale = true;
+        return NESF_OK;
+    }
+    std::vector<unsigned char> all;
+    unsigned char buf[4096];
+    size_t n;
+    while ((n = std::fread(buf, 1, sizeof(buf), f)) > 0) all.insert(all.end(), buf, buf + n);
+    const bool err = std::ferror(f) != 0;
+    std::fclose(f);
+    if (err) return fail(NESF_ERR_ARG, "%s: cannot read %s", who, path);
+    if (all.size() < 8 || std::memcmp(all.data(), kTuneMagic, 8) != 0)
+        return fail(NESF_ERR_ARG, "%s: %s is not a tuning cache (no NESFTUNE header)", who, path);
+    if (all.size() < kHeaderBytes) return fail(NESF_ERR_ARG, "%s: %s is cut short (header)", who, path);
+    const uint32_t version = get_u32(&all[8]), key_bytes = get_u32(&all[12]), fields = get_u32(&all[16]),
+                   count = get_u32(&all[20]);
+    if (version != NESF_TUNING_VERSION || key_bytes != kKeyBytes || fields != (uint32_t)kTuneInts) {
+        stale = true;
+        return NESF_OK;
+    }
+    if (all.size() != kHeaderBytes + (size_t)count * kRecordBytes)
+        return fail(NESF_ERR_ARG, "%s: %s holds %zu bytes for %u records (%zu expected)", who, path, all.size(),
+                    count, kHeaderBytes + (size_t)count * kRecordBytes);
+    records.assign(all.begin() + kHeaderBytes, all.end());
+    return NESF_OK;
+}
+
+int check_key(const nesf_tuning_key* key, const char* who) {
+    if (!key) return fail(NESF_ERR_ARG, "%s: null key", who);
+    if (strnlen(key->device, sizeof(key->device)) == sizeof(key->device))
+        return fail(NESF_ERR_ARG, "%s: the key's device name is not NUL-terminated", who);
+    return NESF_OK;
+}
+
+}  // namespace
+
+extern "C" int nesf_tuning_key_of(nesf_context* ctx, const nesf_coupling_step_args* a, const nesf_solver_options* opts,
+                                  nesf_tuning_key* key) {
+    const char* who = "nesf_tuning_key_of";
+    if (!a || !a->ao || !a->ao_params || !key) return fail(NESF_ERR_ARG, "%s: null arguments", who);
+    int r = context_or_default(&ctx);
+    if (r) return r;
+    cudaDeviceProp p;
+    NESF_CUDA(cudaGetDeviceProperties(&p, ctx->device));
+    const nesf_solver_options o = options_or_default(opts);
+    std::memset(key, 0, sizeof(*key));
+    std::snprintf(key->device, sizeof(key->device), "%s", p.name);
+    key->sm_count = p.multiProcessorCount;
+    key->compute_capability = p.major * 10 + p.minor;
+    key->nx = a->ao->grid.nx;
+    key->ny = a->ao->grid.ny;
+    key->hx = a->ao->grid.hx;
+    key->hy = a->ao->grid.hy;
+    key->dtype = a->ao->dtype;
+    key->precision = o.precision;
+    key->warm_start = (o.warm_start && o.mlp && o.precision != NESF_PLAIN_F64) ? 1 : 0;
+    key->parts = (a->ai_params ? 1 : 0) | (a->io_params ? 2 : 0) | (a->interp ? 4 : 0) |
+                 (a->assembly_params ? 8 : 0) | (a->radiation ? 16 : 0);
+    key->flux_formulation = a->ao_params->flux_formulation;
+    return NESF_OK;
+}
+
+extern "C" int nesf_tuning_cache_find(const char* path, const nesf_tuning_key* key, nesf_tuning* out,
+                                      int32_t* found) {
+    const char* who = "nesf_tuning_cache_find";
+    if (!path || !out || !found) return fail(NESF_ERR_ARG, "%s: null arguments", who);
+    int r = check_key(key, who);
+    if (r) return r;
+    *found = 0;
+    std::vector<unsigned char> rec;
+    bool stale = false;
+    if ((r = read_cache(path, who, rec, stale))) return r;
+    std::vector<unsigned char> want;
+    put_key(want, *key);
+    for (size_t off = 0; off + kRecordBytes <= rec.size(); off += kRecordBytes) {
+        if (std::memcmp(&rec[off], want.data(), kKeyBytes) != 0) continue;
+        *out = get_tuning_record(&rec[off + kKeyBytes]);
+        *found = 1;
+    }
+    return NESF_OK;
+}
+
+extern "C" int nesf_tuning_cache_store(const char* path, const nesf_tuning_key* key, const nesf_tuning* tuning) {
+    const char* who = "nesf_tuning_cache_store";
+    if (!path || !tuning) return fail(NESF_ERR_ARG, "%s: null arguments", who);
+    int r = check_key(key, who);
+    if (r || (r = check_tuning(*tuning, who))) return r;
+    std::vector<unsigned char> rec;
+    bool stale = false;
+    if ((r = read_cache(path, who, rec, stale))) return r;
+    std::vector<unsigned char> want, out;
+    put_key(want, *key);
+    out.insert(out.end(), kTuneMagic, kTuneMagic + 8);
+    put_u32(out, NESF_TUNING_VERSION);
+    put_u32(out, kKeyBytes);
+    put_u32(out, (uint32_t)kTuneInts);
+    put_u32(out, 0);                         // record count, set below
+    uint32_t count = 0;
+    for (size_t off = 0; off + kRecordBytes <= rec.size(); off += kRecordBytes) {
+        if (std::memcmp(&rec[off], want.data(), kKeyBytes) == 0) continue;   // replaced
+        out.insert(out.end(), rec.begin() + off, rec.begin() + off + kRecordBytes);
+        count++;
+    }
+    out.insert(out.end(), want.begin(), want.end());
+    put_tuning(out, *tuning);
+    count++;
+    for (int i = 0; i < 4; i++) out[20 + i] = (unsigned char)(count >> (8 * i));
+    std::string tmp = std::string(path) + ".tmp";
+    FILE* f = std::fopen(tmp.c_str(), "wb");
+    if (!f) return fail(NESF_ERR_ARG, "%s: cannot write %s", who, tmp.c_str());
+    const bool ok = std::fwrite(out.data(), 1, out.size(), f) == out.size();
+    if (std::fclose(f) != 0 || !ok) {
+        std::remove(tmp.c_str());
+        return fail(NESF_ERR_ARG, "%s: cannot write %s", who, tmp.c_str());
+    }
+    if (std::rename(tmp.c_str(), path) != 0) {
+        std::remove(tmp.c_str());
+        return fail(NESF_ERR_ARG, "%s: cannot rename %s over %s", who, tmp.c_str(), path);
+    }
+    return NESF_OK;
+}
+
+extern "C" int nesf_autotune_cached(nesf_context* ctx, const nesf_coupling_step_args* a,
+                                    const nesf_solver_options* opts, int32_t reps, const char* path,
+                                    nesf_tuning* out, int32_t* from_cache, void* stream) {
+    const char* who = "nesf_autotune_cached";
+    if (!path || !from_cache) return fail(NESF_ERR_ARG, "%s: null arguments", who);
+    int r = context_or_default(&ctx);
+    if (r) return r;
+    nesf_tuning_key key;
+    if ((r = nesf_tuning_key_of(ctx, a, opts, &key))) return r;
+    nesf_tuning t;
+    int32_t found = 0;
+    if ((r = nesf_tuning_cache_find(path, &key, &t, &found))) return r;
+    if (found) {
+        if ((r = check_tuning(t, who))) return r;
+        {
+            std::lock_guard<std::mutex> lk(ctx->lock);
+            ctx->tuning = complete_tuning(t);
+            ctx->tuning.step_ms = t.step_ms;
+        }
+        if (out) *out = ctx->tuning;
+        *from_cache = 1;
+        return NESF_OK;
+    }
+    *from_cache = 0;
+    if ((r = nesf_autotune(ctx, a, opts, reps, &t, stream))) return r;
+    if (out) *out = t;
+    return nesf_tuning_cache_store(path, &key, &t);
 }

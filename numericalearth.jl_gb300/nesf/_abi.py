@@ -298,6 +298,15 @@ class Tuning(C.Structure):
 TUNING_FIELDS = ("solve_block", "deferred_per_sm", "infer_per_sm", "two_lanes", "io_overlap", "pass1_fetch",
                  "refill_lanes", "early_ocean_classify")
 
+TUNING_VERSION = 1
+
+
+class TuningKey(C.Structure):
+    _fields_ = [("device", C.c_char * 64), ("sm_count", i32), ("compute_capability", i32), ("nx", i32), ("ny", i32),
+                ("hx", i32), ("hy", i32), ("dtype", i32), ("precision", i32), ("warm_start", i32), ("parts", i32),
+                ("flux_formulation", i32)]
+
+
 TRACE_MAX = 64
 
 # NESF_WORK_* of include/nesf.h (checked against the header by the tests)
@@ -314,4 +323,4 @@ STRUCTS_IN_SIZE_ORDER = (Grid, ThermodynamicsParameters, StabilityFunction, Roug
                          SimilarityTheoryFluxesC, InterfaceParams, SolverOptions, Stats, AOFields,
                          AIFields, IOParams, IOFields, AtmosGrid, ExchangeCoords, InterpFields,
                          AssemblyParams, AssemblyFields, CouplingStepArgs, IntegralFields, Tuning,
-                         TraceEntry, CoefficientFluxes, ALFields, LandRadiationParams, LandFluxFields)
+                         TraceEntry, CoefficientFluxes, ALFields, LandRadiationParams, LandFluxFields, TuningKey)

@@ -76,6 +76,11 @@ SIGNATURES = {
     "nesf_set_tuning": (C.c_int, [vp, P(A.Tuning)]),
     "nesf_get_tuning": (C.c_int, [vp, P(A.Tuning)]),
     "nesf_autotune": (C.c_int, [vp, P(A.CouplingStepArgs), P(A.SolverOptions), C.c_int32, P(A.Tuning), vp]),
+    "nesf_tuning_key_of": (C.c_int, [vp, P(A.CouplingStepArgs), P(A.SolverOptions), P(A.TuningKey)]),
+    "nesf_tuning_cache_find": (C.c_int, [C.c_char_p, P(A.TuningKey), P(A.Tuning), P(C.c_int32)]),
+    "nesf_tuning_cache_store": (C.c_int, [C.c_char_p, P(A.TuningKey), P(A.Tuning)]),
+    "nesf_autotune_cached": (C.c_int, [vp, P(A.CouplingStepArgs), P(A.SolverOptions), C.c_int32, C.c_char_p,
+                                       P(A.Tuning), P(C.c_int32), vp]),
     "nesf_trace_enable": (C.c_int, [vp, C.c_int32]),
     "nesf_trace_read": (C.c_int, [vp, P(A.TraceEntry), C.c_int32, P(C.c_int32)]),
 }

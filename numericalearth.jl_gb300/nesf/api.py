@@ -375,18 +375,62 @@ def set_tuning(ctx=None, **fields):
     return get_tuning(ctx)
 
 
-def autotune(step, precision="f32_adaptive", reps=5, ctx=None, stream=None, mlp=None):
+def _tuning_dict(t):
+    out = {k: int(getattr(t, k)) for k in A.TUNING_FIELDS}
+    out["step_ms"] = float(t.step_ms)
+    return out
+
+
+def autotune(step, precision="f32_adaptive", reps=5, ctx=None, stream=None, mlp=None, cache=None):
     """Coordinate search of the context's tuning on one coupling step (nesf_autotune); returns
-    the chosen tuning (a dict with its mean step time, step_ms). The steps run for real."""
+    the chosen tuning (a dict with its mean step time, step_ms). The steps run for real.
+
+    `cache`: a tuning-cache file (nesf_autotune_cached). A tuning recorded there for this
+    step's key (device, grid, dtype, precision, warm start, phases) is set without running a
+    step; otherwise the search runs and its result is recorded. The dict then carries
+    "from_cache"."""
     lib = load()
     o = solver_options(precision, mlp=mlp)
     ctx = ctx or default_context()
     t = A.Tuning()
-    check(lib.nesf_autotune(ctx.handle, C.byref(step.args), C.byref(o), int(reps), C.byref(t),
-                            _stream_handle(stream)))
-    out = {k: int(getattr(t, k)) for k in A.TUNING_FIELDS}
-    out["step_ms"] = float(t.step_ms)
+    if cache is None:
+        check(lib.nesf_autotune(ctx.handle, C.byref(step.args), C.byref(o), int(reps), C.byref(t),
+                                _stream_handle(stream)))
+        return _tuning_dict(t)
+    hit = C.c_int32(0)
+    check(lib.nesf_autotune_cached(ctx.handle, C.byref(step.args), C.byref(o), int(reps), str(cache).encode(),
+                                   C.byref(t), C.byref(hit), _stream_handle(stream)))
+    out = _tuning_dict(t)
+    out["from_cache"] = bool(hit.value)
     return out
+
+
+def tuning_key(step, precision="f32_adaptive", ctx=None, mlp=None):
+    """The tuning-cache key of a coupling step on the context's device (nesf_tuning_key_of)."""
+    lib = load()
+    o = solver_options(precision, mlp=mlp)
+    ctx = ctx or default_context()
+    k = A.TuningKey()
+    check(lib.nesf_tuning_key_of(ctx.handle, C.byref(step.args), C.byref(o), C.byref(k)))
+    return k
+
+
+def tuning_cache_find(path, key):
+    """The tuning a cache file records for `key` (a dict), or None (nesf_tuning_cache_find)."""
+    lib = load()
+    t = A.Tuning()
+    found = C.c_int32(0)
+    check(lib.nesf_tuning_cache_find(str(path).encode(), C.byref(key), C.byref(t), C.byref(found)))
+    return _tuning_dict(t) if found.value else None
+
+
+def tuning_cache_store(path, key, tuning):
+    """Record `tuning` (a dict of the tuning fields, step_ms optional) for `key`
+    (nesf_tuning_cache_store)."""
+    lib = load()
+    t = A.Tuning(**{k: int(tuning.get(k, 0)) for k in A.TUNING_FIELDS})
+    t.step_ms = float(tuning.get("step_ms", 0.0))
+    check(lib.nesf_tuning_cache_store(str(path).encode(), C.byref(key), C.byref(t)))
 
 
 def trace_enable(on=True, ctx=None):

@@ -181,10 +181,11 @@ class CoupledModel:
         api.coupling_step(self.step_args(), precision, stream=stream, mlp=self.mlp)
         return self.kernels_per_step(precision, native=True)
 
-    def autotune(self, precision="f32_adaptive", reps=5):
+    def autotune(self, precision="f32_adaptive", reps=5, cache=None):
         """Tune the default context's launch shapes and schedule on this model's step
-        (nesf_autotune). The steps run for real; the state is reset afterwards."""
-        t = api.autotune(self.step_args(), precision, reps=reps, mlp=self.mlp)
+        (nesf_autotune; through the tuning-cache file `cache` when given). The steps run for
+        real; the state is reset afterwards."""
+        t = api.autotune(self.step_args(), precision, reps=reps, mlp=self.mlp, cache=cache)
         self.reset()
         return t
 

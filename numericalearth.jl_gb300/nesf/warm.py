@@ -112,9 +112,12 @@ def ao_samples(spec, layout, state, solved, stream=None):
     return feat, targ
 
 
-def training_set(spec, states, stream=None):
+def training_set(spec, states, stream=None, shuffle_seed=None):
     """Solver-generated samples: each synthetic state solved by the plain FP64 solver, then
-    its (features, targets) pairs with a valid u* target, concatenated."""
+    its (features, targets) pairs with a valid u* target, concatenated. `states` may be a
+    generator (each state's host arrays are dropped once its samples are on the device).
+    With `shuffle_seed` the samples are put in a seeded random order, so that contiguous
+    mini-batches mix cells of every state."""
     torch = _torch()
     from . import api
     feats, targs = [], []
@@ -127,4 +130,11 @@ def training_set(spec, states, stream=None):
         keep = (t[:, 3].to(torch.int32) & 1) != 0
         feats.append(f[keep])
         targs.append(t[keep])
-    return torch.cat(feats).contiguous(), torch.cat(targs).contiguous()
+        del dev, out, f, t
+    x, t = torch.cat(feats), torch.cat(targs)
+    if shuffle_seed is not None:
+        g = torch.Generator(device=x.device)
+        g.manual_seed(int(shuffle_seed))
+        order = torch.randperm(x.shape[0], generator=g, device=x.device)
+        x, t = x[order], t[order]
+    return x.contiguous(), t.contiguous()

@@ -111,7 +111,8 @@ C_STRUCT_NAMES = (
     "nesf_ao_fields", "nesf_ai_fields", "nesf_io_params", "nesf_io_fields", "nesf_atmos_grid",
     "nesf_exchange_coords", "nesf_interp_fields", "nesf_assembly_params", "nesf_assembly_fields",
     "nesf_coupling_step_args", "nesf_integral_fields", "nesf_tuning", "nesf_trace_entry",
-    "nesf_coefficient_fluxes", "nesf_al_fields", "nesf_land_radiation_params", "nesf_land_flux_fields")
+    "nesf_coefficient_fluxes", "nesf_al_fields", "nesf_land_radiation_params", "nesf_land_flux_fields",
+    "nesf_tuning_key")
 
 
 @pytest.mark.parametrize("k", range(len(C_STRUCT_NAMES)))

@@ -100,3 +100,29 @@ def test_graph_keeps_its_tuning(model):
     got = outputs(model)
     for k in ref:
         assert np.array_equal(ref[k], got[k], equal_nan=True), k
+
+
+def test_autotune_through_the_cache(model, tmp_path):
+    """The first cached autotune searches and records; the second sets the recorded tuning
+    without a step; the key names this device and step."""
+    import torch
+    path = tmp_path / "tuning.bin"
+    api.set_tuning(**DEFAULT)
+    first = model.autotune("f32_adaptive", reps=1, cache=path)
+    assert first["from_cache"] is False and first["step_ms"] > 0
+    api.set_tuning(**dict(DEFAULT, solve_block=32, two_lanes=0))
+    second = model.autotune("f32_adaptive", reps=1, cache=path)
+    assert second["from_cache"] is True
+    assert {k: second[k] for k in DEFAULT} == {k: first[k] for k in DEFAULT}
+    cur = api.get_tuning()
+    assert {k: cur[k] for k in DEFAULT} == {k: first[k] for k in DEFAULT}
+    k = api.tuning_key(model.step_args(), "f32_adaptive")
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    assert k.device.decode() == props.name and k.sm_count == props.multi_processor_count
+    assert k.compute_capability == props.major * 10 + props.minor
+    assert (k.nx, k.ny) == (model.layout.nx, model.layout.ny) and k.parts == 31 and k.warm_start == 0
+    assert api.tuning_cache_find(path, k) is not None
+    # another precision is another key: searched afresh
+    third = model.autotune("f32", reps=1, cache=path)
+    assert third["from_cache"] is False
+    api.set_tuning(**DEFAULT)
