@@ -296,9 +296,12 @@ typedef struct {
     double calm_replay_wind;  /* NESF_F32_ADAPTIVE, atmosphere-sea-ice solve: cells whose
                                  10 m wind speed is below it go from the classify pass
                                  straight to the reference's FP64 iteration, on a stream
-                                 of their own beside pass 1 (in calm air the fixed point
-                                 converges slowly: these are the solve's longest FP64
-                                 chains); default 0.7 m/s, 0: none                     */
+                                 of their own beside pass 1 when the tuning's two_lanes
+                                 is on, else with pass 1's replays (in calm air the fixed
+                                 point converges slowly: these are the solve's longest
+                                 FP64 chains); default 0: none (measured on the 1/8-degree
+                                 step: 0.7 m/s replays more cells in FP64 than pass 1
+                                 would, beside pass 1, and the step takes 0.5 ms longer)   */
 } nesf_solver_options;
 
 /* -------------------------------------------------------------- statistics */
@@ -806,7 +809,10 @@ typedef struct {
     int32_t refill_lanes;     /* pass1_fetch 4: idle lanes that make a warp take new entries, 1..32
                                  (32: warp fetching) (8)                                                */
     int32_t early_ocean_classify; /* coupling step with two lanes: the ocean's classify pass and warm-
-                                 start inference beside the sea-ice pass 1, its pass 1 after it (1) */
+                                 start inference beside the sea-ice pass 1, its pass 1 after it (0) */
+    int32_t ice_deferred_per_sm; /* blocks per SM of the sea-ice solve's packed polish and replay
+                                 passes, 1..16; 0: deferred_per_sm. Fewer leave registers to the
+                                 ocean solve's kernels that run beside them (0)              */
     double step_ms;           /* nesf_autotune: the chosen configuration's mean step time            */
 } nesf_tuning;
 
@@ -830,9 +836,9 @@ int nesf_autotune(nesf_context* ctx, const nesf_coupling_step_args* args, const 
  * cache file (any path the caller picks) holds one tuning per key. Format, every
  * integer little-endian whatever the host:
  *   "NESFTUNE" (8 bytes), uint32 format version (NESF_TUNING_VERSION), uint32 key
- *   bytes (108), uint32 tuning fields (8), uint32 record count, then per record the
+ *   bytes (108), uint32 tuning fields (9), uint32 record count, then per record the
  *   key (device name, 64 bytes NUL-padded, then its eleven int32 fields) and the
- *   tuning (its eight int32 fields in declaration order, then step_ms as the
+ *   tuning (its nine int32 fields in declaration order, then step_ms as the
  *   IEEE-754 bits of a double).
  * A file of another format version or tuning-field count holds nothing for this
  * library: find reports no entry and store starts the file afresh. A file that does

@@ -317,7 +317,7 @@ struct AIAdaptiveCell {
 // Pass 1 of the adaptive solver under the convergence stopping rule: adaptive_pass1 with the
 // schedule of SolveOpts::fetch / refill.
 template <class S, bool SKIN>
-__global__ void __launch_bounds__(128, 5) ai_adaptive_kernel(AIArgs<S> a, DevIface<double> P64, DevIface<float> P32,
+__global__ void __launch_bounds__(128, NESF_ADAPTIVE_MIN_BLOCKS) ai_adaptive_kernel(AIArgs<S> a, DevIface<double> P64, DevIface<float> P32,
                                                              SolveOpts so, WorkList wl, ReplayQueue rq,
                                                              const float* guess, DevStats* stats) {
     AIAdaptiveCell<S, SKIN> cell{a, P64, P32};
@@ -417,17 +417,20 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     if (e == cudaSuccess && prec != NESF_PLAIN_F64)
         e = cudaMemsetAsync(rq.count, 0, kQueueCounters * sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
-    // calm cells straight to the FP64 replay on the early lane (the adaptive solver under the
-    // convergence stopping rule; the queue's part 3 holds them)
+    // calm cells straight to the FP64 replay (the adaptive solver under the convergence
+    // stopping rule; the queue's part 3 holds them): on the early lane beside pass 1 when
+    // there is one, else with pass 1's replays. The choice is the solver's, the lane only
+    // the schedule: every tuning replays the same cells.
     const bool adaptive_conv = prec == NESF_F32_ADAPTIVE && so.fp32_rho > 0.0f && P64.stop_kind == NESF_STOP_CONVERGENCE;
-    const bool calm = adaptive_conv && so.calm_wind > 0.0f && early && early->stream;
+    const bool calm = adaptive_conv && so.calm_wind > 0.0f;
+    const bool early_lane = calm && early && early->stream;
     ai_classify_kernel<S><<<grid, block, 0, stream>>>(a, P64, P32, wl, rq, calm ? so.calm_wind * so.calm_wind : 0.0f,
                                                       warm ? ws.feat : nullptr, stats);
     trace_mark(so.tracer, "ai_classify", stream);
-    if (calm) {
+    if (early_lane) {
         if ((e = cudaEventRecord(early->fork, stream)) != cudaSuccess) return e;
         if ((e = cudaStreamWaitEvent(early->stream, early->fork, 0)) != cudaSuccess) return e;
-        ai_replay_kernel<S><<<(unsigned)(sms * so.deferred_per_sm), 128, 0, early->stream>>>(a, P64, rq, 3, stats);
+        ai_replay_kernel<S><<<(unsigned)(sms * so.deferred_ice), 128, 0, early->stream>>>(a, P64, rq, 3, stats);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         trace_mark(so.tracer, "ai_calm_replay", early->stream);
     }
@@ -464,7 +467,7 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     trace_mark(so.tracer, "ai_pass1", stream);
     if (e == cudaSuccess && after_solve) e = cudaEventRecord(after_solve, stream);
     if (e != cudaSuccess || prec == NESF_PLAIN_F64) return e;
-    const unsigned g2 = (unsigned)(sms * so.deferred_per_sm);
+    const unsigned g2 = (unsigned)(sms * so.deferred_ice);
     if (!adaptive) {
         ai_replay_kernel<S><<<g2, 128, 0, stream>>>(a, P64, rq, 0, stats);
         trace_mark(so.tracer, "ai_replay", stream);
@@ -480,6 +483,10 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     }
     ai_replay_kernel<S><<<g2, 128, 0, rs>>>(a, P64, rq, 0, stats);
     trace_mark(so.tracer, "ai_replay", rs);
+    if (calm && !early_lane) {
+        ai_replay_kernel<S><<<g2, 128, 0, rs>>>(a, P64, rq, 3, stats);
+        trace_mark(so.tracer, "ai_calm_replay", rs);
+    }
     if (skin) ai_polish_kernel<S, true><<<g2, 128, 0, stream>>>(a, P64, P32, so, rq, 2, stats);
     else ai_polish_kernel<S, false><<<g2, 128, 0, stream>>>(a, P64, P32, so, rq, 2, stats);
     trace_mark(so.tracer, "ai_polish", stream);
@@ -490,7 +497,7 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
         if ((e = cudaEventRecord(tail->join, rs)) != cudaSuccess) return e;
         if ((e = cudaStreamWaitEvent(stream, tail->join, 0)) != cudaSuccess) return e;
     }
-    if (calm) {   // the early lane (only on this path: calm needs the adaptive solver) joins last
+    if (early_lane) {   // the early lane (only on this path: calm needs the adaptive solver) joins last
         if ((e = cudaEventRecord(early->join, early->stream)) != cudaSuccess) return e;
         if ((e = cudaStreamWaitEvent(stream, early->join, 0)) != cudaSuccess) return e;
     }

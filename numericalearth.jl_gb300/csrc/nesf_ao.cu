@@ -72,6 +72,49 @@ __device__ __forceinline__ void ao_store(const DevIface<double>& P, const AOArgs
     if (a.iters) a.iters[k] = iters;
 }
 
+// A land cell's zero interface state (zero_interface_state, interface_states.jl:800-803)
+// through ao_store's epilogue without its FP64 divisions and square root: with u* =
+// theta* = q* = 0 every output is a zero whose sign follows the signs of the air density
+// p / (R_m T), of cp_m, of L_v and of the wind components. The guards keep each factor
+// finite and clear of the rounding that a contracted multiply-add could move (R_m's and
+// the heat capacities' sums far from cancelling, the density's quotient within range),
+// so the signs are ao_store's; other cells take ao_store. rho is replaced by +-1 of its
+// sign, and the division by |dU| > 0 leaves a zero unchanged.
+template <class S>
+__device__ __forceinline__ void ao_store_land(const DevIface<double>& P, const AOArgs<S>& a, int64_t k, int iters) {
+    const double ua = ld(a.ua, k), va = ld(a.va, k), Ta = ld(a.Ta, k), pa = ld(a.pa, k), qa = ld(a.qa, k);
+    const double f = 1.0 + (P.eps - 1.0) * qa;
+    const double den = gas_constant_air(P, qa) * Ta;
+    const double cp = cp_m(P, qa), Lv = latent_heat_vapor(P, Ta);
+    const bool clear = fabs(f) > 1e-6 * (1.0 + fabs(P.eps - 1.0) * fabs(qa)) &&
+                       fabs(cp) > 1e-6 * (fabs(P.cpd) + fabs(P.cpv - P.cpd) * fabs(qa)) &&
+                       fabs(Lv) > 1e-6 * (fabs(P.Lv0) + fabs(P.cpv - P.cpl) * fabs(Ta - P.T0)) &&
+                       fabs(pa) > 1e-30 && fabs(pa) < 1e30 && fabs(den) > 1e-30 && fabs(den) < 1e30 &&
+                       fabs(cp) < 1e30 && fabs(Lv) < 1e30 && isfinite(ua) && isfinite(va);
+    if (!clear) {
+        CellConst<double> c;
+        bool land;
+        ao_load(P, a, k, false, c, land);
+        ao_store(P, a, k, c, true, 0.0, 0.0, 0.0, 273.15, iters);
+        return;
+    }
+    const double r = copysign(1.0, pa) * copysign(1.0, den);   // the sign of the air density
+    const double z = 0.0;
+    const bool calm = ua * ua + va * va == 0.0;                  // |dU| = 0 (surface at rest)
+    const double tx = calm ? 0.0 : -(z * z) * ua;
+    const double ty = calm ? 0.0 : -(z * z) * va;
+    st(a.Qv, k, -r * Lv * z * z);
+    st(a.QT, k, -r * cp * z * z);
+    st(a.Jv, k, -r * z * z);
+    st(a.tx, k, r * tx);
+    st(a.ty, k, r * ty);
+    st(a.Ts, k, 273.15 - P.off_ifc);
+    st(a.us, k, z);
+    st(a.ts, k, z);
+    st(a.qs, k, z);
+    if (a.iters) a.iters[k] = iters;
+}
+
 // The adaptive pass-1 prologue: the cell's FP32 inputs with FP64 only where
 // differences cancel (ao_load's quantities, rounded to FP32).
 template <class S, bool SKIN>
@@ -171,12 +214,7 @@ __global__ void __launch_bounds__(128) ao_classify_kernel(AOArgs<S> a, DevIface<
     }
     int64_t slot = worklist_push(wl, m, active, stable, (uint32_t)r);
     if (feat && slot >= 0) mlp::store_features(feat, slot, F);
-    if (in && land) {
-        CellConst<double> c;
-        bool l;
-        ao_load(P, a, k, false, c, l);
-        ao_store(P, a, k, c, true, 0.0, 0.0, 0.0, 273.15, needs ? 0 : P.maxiter);
-    }
+    if (in && land) ao_store_land(P, a, k, needs ? 0 : P.maxiter);
     if (stats && in && land) stats_add(stats, true, false, 0, false, false, 0, false, false);
 }
 
@@ -319,7 +357,7 @@ struct AOAdaptiveCell {
 // Pass 1 of the adaptive solver, one member, convergence stopping rule: adaptive_pass1
 // with the schedule of SolveOpts::fetch / refill.
 template <class S, bool SKIN>
-__global__ void __launch_bounds__(128, 5) ao_adaptive_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
+__global__ void __launch_bounds__(128, NESF_ADAPTIVE_MIN_BLOCKS) ao_adaptive_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
                                                              SolveOpts so, WorkList wl, ReplayQueue rq,
                                                              const float* guess, DevStats* stats) {
     AOAdaptiveCell<S, SKIN> cell{a, P64, P32};

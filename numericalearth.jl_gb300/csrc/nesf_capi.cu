@@ -87,7 +87,8 @@ static nesf_tuning default_tuning() {
     t.io_overlap = 1;
     t.pass1_fetch = 2;
     t.refill_lanes = 8;
-    t.early_ocean_classify = 1;
+    t.early_ocean_classify = 0;
+    t.ice_deferred_per_sm = 0;
     return t;
 }
 
@@ -360,7 +361,7 @@ void nesf_default_solver_options(nesf_solver_options* o) {
     o->fallback_ratio = 10.0;
     o->path_tolerance = 2e-6;
     o->fp32_rho = 0.9;
-    o->calm_replay_wind = 0.7;
+    o->calm_replay_wind = 0.0;
 }
 
 // ---------------------------------------------------------------- context
@@ -523,7 +524,7 @@ static SolveOpts solve_opts(const nesf_solver_options& o, const nesf_context* ct
                      t.solve_block, t.deferred_per_sm, t.infer_per_sm,
                      (t.pass1_fetch >= 2 ? NESF_FETCH_SEA_ICE : 0) | (t.pass1_fetch >= 3 ? NESF_FETCH_OCEAN : 0),
                      t.pass1_fetch == 4 ? (t.refill_lanes > 0 ? t.refill_lanes : 8) : 32, tracer_of(ctx),
-                     (float)o.calm_replay_wind};
+                     (float)o.calm_replay_wind, t.ice_deferred_per_sm > 0 ? t.ice_deferred_per_sm : t.deferred_per_sm};
 }
 
 static int check_options(const nesf_solver_options& o, const char* who) {
@@ -1773,6 +1774,8 @@ static int check_tuning(const nesf_tuning& t, const char* who) {
         return fail(NESF_ERR_ARG, "%s: refill_lanes %d (1..32)", who, t.refill_lanes);
     if (t.early_ocean_classify < 0 || t.early_ocean_classify > 1)
         return fail(NESF_ERR_ARG, "%s: early_ocean_classify is 0 or 1", who);
+    if (t.ice_deferred_per_sm < 0 || t.ice_deferred_per_sm > 16)
+        return fail(NESF_ERR_ARG, "%s: ice_deferred_per_sm %d (0..16)", who, t.ice_deferred_per_sm);
     return NESF_OK;
 }
 
@@ -1861,6 +1864,7 @@ extern "C" int nesf_autotune(nesf_context* ctx, const nesf_coupling_step_args* a
         {&nesf_tuning::two_lanes, {1, 0}, ice},
         {&nesf_tuning::io_overlap, {1, 0}, ice && a->io_params != nullptr},
         {&nesf_tuning::early_ocean_classify, {1, 0}, ice},
+        {&nesf_tuning::ice_deferred_per_sm, {0, 1, 2}, ice && fast},
     };
     for (const Axis& ax : axes) {
         if (r || !ax.used) continue;
@@ -1897,7 +1901,7 @@ namespace {
 constexpr char kTuneMagic[8] = {'N', 'E', 'S', 'F', 'T', 'U', 'N', 'E'};
 constexpr int kKeyInts = 11;
 constexpr uint32_t kKeyBytes = 64 + 4 * kKeyInts;
-constexpr int kTuneInts = 8;
+constexpr int kTuneInts = 9;
 constexpr size_t kRecordBytes = kKeyBytes + 4 * kTuneInts + 8;
 constexpr size_t kHeaderBytes = 8 + 4 * 4;
 
@@ -1921,7 +1925,8 @@ void key_ints(const nesf_tuning_key& k, int32_t* v) {
 }
 void tune_ints(const nesf_tuning& t, int32_t* v) {
     const int32_t w[kTuneInts] = {t.solve_block, t.deferred_per_sm, t.infer_per_sm, t.two_lanes,
-                                  t.io_overlap, t.pass1_fetch, t.refill_lanes, t.early_ocean_classify};
+                                  t.io_overlap, t.pass1_fetch, t.refill_lanes, t.early_ocean_classify,
+                                  t.ice_deferred_per_sm};
     std::memcpy(v, w, sizeof(w));
 }
 
@@ -1951,6 +1956,7 @@ nesf_tuning get_tuning_record(const unsigned char* p) {
     std::memset(&t, 0, sizeof(t));
     t.solve_block = v[0]; t.deferred_per_sm = v[1]; t.infer_per_sm = v[2]; t.two_lanes = v[3];
     t.io_overlap = v[4]; t.pass1_fetch = v[5]; t.refill_lanes = v[6]; t.early_ocean_classify = v[7];
+    t.ice_deferred_per_sm = v[8];
     const uint64_t bits = get_u64(p + 4 * kTuneInts);
     std::memcpy(&t.step_ms, &bits, 8);
     return t;

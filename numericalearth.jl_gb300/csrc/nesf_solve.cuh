@@ -54,6 +54,7 @@ struct SolveOpts {
     const Tracer* tracer;  // host side: kernel-boundary trace (null: off)
     float calm_wind;       // adaptive sea-ice solve with an early lane: wind speed below which the
                            // classify pass sends a cell straight to the FP64 replay (0: none)
+    int deferred_ice;      // blocks per SM of the sea-ice solve's packed polish and replay passes
 };
 
 // Warm start of a solve: features written by the classify pass at the work-list
@@ -83,6 +84,12 @@ struct WorkList {
 // solve), and count[kFetchCounter] is pass 1's fetch counter (SolveOpts::fetch). A
 // cell that the polish pass sends on to a replay holds one entry in each of two parts.
 constexpr int kFetchCounter = 4;
+
+// Blocks of 128 threads per SM that the adaptive pass-1 kernels are compiled for (their
+// register budget: 65536 / (128 x this), rounded down to a multiple of 8).
+#ifndef NESF_ADAPTIVE_MIN_BLOCKS
+#define NESF_ADAPTIVE_MIN_BLOCKS 5
+#endif
 constexpr int kQueueCounters = 5;
 struct ReplayQueue {
     uint32_t* idx;          // linear cell ids (member * ring + ring index)

@@ -102,7 +102,7 @@ def compute_atmosphere_ocean_fluxes(spec, layout, state, out, precision="f64", p
     arrays["iterations"] = iterations
     f = F.pack(A.AOFields, _grid_of(layout), arrays)
     p = spec.to_c() if hasattr(spec, "to_c") else spec
-    o = solver_options(precision, polish_maxiter, mlp=mlp, calm_replay_wind=calm_replay_wind)
+    o = solver_options(precision, polish_maxiter, mlp=mlp)
     st = A.Stats() if stats else None
     ctx = ctx or default_context()
     check(lib.nesf_compute_atmosphere_ocean_fluxes(ctx.handle, C.byref(p), C.byref(f), C.byref(o),
@@ -141,7 +141,7 @@ def compute_atmosphere_sea_ice_fluxes(spec, layout, state, out, precision="f64",
     arrays["iterations"] = iterations
     f = F.pack(A.AIFields, _grid_of(layout), arrays)
     p = spec.to_c() if hasattr(spec, "to_c") else spec
-    o = solver_options(precision, polish_maxiter, mlp=mlp)
+    o = solver_options(precision, polish_maxiter, mlp=mlp, calm_replay_wind=calm_replay_wind)
     st = A.Stats() if stats else None
     ctx = ctx or default_context()
     check(lib.nesf_compute_atmosphere_sea_ice_fluxes(ctx.handle, C.byref(p), C.byref(f), C.byref(o),

@@ -224,8 +224,12 @@ def test_config2_coupled_step_plain_f64(oracle):
         resp = oracle.conditioning_response(
             lambda: oracle.ai_fluxes(sp["ai_spec"].to_c(), sub, band_in, band_in["ice_temperature"]), ref["ai"],
             ai_keys, view=view)
+        # the skin temperature's balance is re-rounded every iteration from several ingredients
+        # (the radiative term, the conductive resistance, q_s(T_s)) whose last places differ
+        # between the CPU and the GPU independently, so the sea-ice solve is held to 8 units of
+        # its response (measured: every cell within 5 units on this workload)
         assert_conditioned({k: kelvin_view(k, band_part(snap["ai"][k], st, lo)) for k in ai_keys},
-                           {k: view(k, ref["ai"][k]) for k in ai_keys}, ai_keys, resp, f"ai band {lo}")
+                           {k: view(k, ref["ai"][k]) for k in ai_keys}, ai_keys, resp, f"ai band {lo}", units=8.0)
         for g in ("ao", "ai"):
             assert np.array_equal(band_part(its[g], st, lo), I(ref[g]["iterations"])), (g, lo)
         # the sea-ice-ocean fluxes and the assembly read the solves' outputs: compared where

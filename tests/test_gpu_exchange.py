@@ -309,7 +309,7 @@ def test_assembly_and_radiation_match_oracle(oracle, coupled64):
 def test_sea_ice_calm_cells_replay_from_the_classify_pass(oracle, coupled64, wind):
     """The adaptive sea-ice solve sends the cells whose wind is below calm_replay_wind from its
     classify pass straight to the reference's FP64 iteration, on a stream of their own beside
-    pass 1: none (0), the calm ones (0.7 m/s, the default) or every ice cell (1000 m/s). The
+    pass 1: none (0, the default), the calm ones (0.7 m/s) or every ice cell (1000 m/s). The
     fluxes stay within 1e-5 of the oracle, every cell is counted once, and with every cell
     replayed all of them are solved by the FP64 iteration."""
     import torch
