@@ -974,7 +974,7 @@ def main():
         ev = oracle_errors(model, [prec, "f64"])
         line["errors_vs_oracle"] = {"fast": ev[prec], "plain_f64": ev["f64"], "sample": ev["sample"]}
         line["max_rel_err_vs_oracle"] = ev[prec]["max_headline_fluxes"]
-        # roofline of the main solve kernel, the atmosphere-ocean pass 1 (ao_kernel), timed with
+        # roofline of the main solve kernel, the atmosphere-ocean pass 1 (ao_adaptive_kernel), timed with
         # trace events on its stream inside graph replays. It is bound by the latency of its
         # FP32 (and FP64 anchor) arithmetic, not by HBM: the HBM fraction is small, and the
         # work-table rate (transcendentals and flops per second, NESF_WORK_*) is given beside it.
@@ -988,7 +988,7 @@ def main():
         work_f = n_ao * (W["PROLOGUE_FLOPS"] + W["EPILOGUE_FLOPS"]) + it_ao * W["ITER_FLOPS"]
         achieved = alg / (t_ao / 1000.0) / 1e9 if t_ao else None
         traffic = AO_KERNEL_DRAM_BYTES_PER_CELL * n_ao if AO_KERNEL_DRAM_BYTES_PER_CELL else None
-        line["roofline"] = {"bound": "hbm", "kernel": "ao_kernel<float, F32_ADAPTIVE> (atmosphere-ocean pass 1)",
+        line["roofline"] = {"bound": "hbm", "kernel": "ao_adaptive_kernel<float, bulk> (atmosphere-ocean pass 1)",
                             "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                             "frac": achieved / peaks["hbm_gbs"] if achieved else None, "traffic": traffic,
                             "algorithmic_bytes": alg, "kernel_ms": t_ao, "peak_source": kind,

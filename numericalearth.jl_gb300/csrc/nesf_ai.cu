@@ -327,7 +327,8 @@ __global__ void __launch_bounds__(128, NESF_ADAPTIVE_MIN_BLOCKS) ai_adaptive_ker
 // Pass 1b (ADAPTIVE): the cells whose FP32 result was not kept, packed, through pass
 // 1's FP32 sweep + FP64 Newton polish; those that need it go on to the replay. The
 // initial interface temperature is still in a.Ts: pass 1 did not write these cells.
-template <class S, bool SKIN>
+// STATE: pass 1 left each entry's sweep state (rq.pstate; with a skin temperature).
+template <class S, bool SKIN, bool STATE>
 __global__ void __launch_bounds__(128) ai_polish_kernel(AIArgs<S> a, DevIface<double> P, DevIface<float> P32,
                                                         SolveOpts so, ReplayQueue rq, int rpart, DevStats* stats) {
     const int nxr = a.L.nx + 2;
@@ -338,16 +339,24 @@ __global__ void __launch_bounds__(128) ai_polish_kernel(AIArgs<S> a, DevIface<do
         int64_t r = id;
         int i = (int)(r % nxr), j = (int)(r / nxr);
         int64_t k = a.L.at(i, j);
-        // pass 1's sweep (the same inputs, start and strict stopping rule: the same
-        // decisions), then the FP64 Newton steps with the reference's FP64 cell constants
-        Fast32 f;
-        ai_load_fast<S, SKIN>(P, P32, a, k, f);
-        float x[4] = {1e-4f, 1e-4f, 1e-4f, SKIN ? (float)(f.Ts0 - f.tha) : 0.0f};
+        // pass 1's sweep: its state when pass 1 left it (a skin temperature), else the sweep
+        // again (the same inputs, start and strict stopping rule: the same decisions); then
+        // the FP64 Newton steps with the reference's FP64 cell constants
+        float x[4];
         float J[SKIN ? 4 : 3][SKIN ? 4 : 3];
         float rho;
-        int f32it = 0, f64it = 0, reason = -1;
-        int outcome = sweep_fp32<SKIN, false, true>(P32, f.c, f.s, f.anc, x, so, f32it, reason, J, rho, nullptr,
+        int f32it = 0, f64it = 0, reason = -1, outcome;
+        if constexpr (STATE) {
+            polish_state_load(rq, (int64_t)q, x, J, rho, f32it);
+            outcome = FAST_POLISH;
+        } else {
+            Fast32 f;
+            ai_load_fast<S, SKIN>(P, P32, a, k, f);
+            x[0] = x[1] = x[2] = 1e-4f;
+            x[3] = SKIN ? (float)(f.Ts0 - f.tha) : 0.0f;
+            outcome = sweep_fp32<SKIN, false, true>(P32, f.c, f.s, f.anc, x, so, f32it, reason, J, rho, nullptr,
                                                     nullptr);
+        }
         CellConst<double> c;
         SurfaceConst<double> s{};
         double us = 0, ts = 0, qst = 0;
@@ -487,8 +496,9 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
         ai_replay_kernel<S><<<g2, 128, 0, rs>>>(a, P64, rq, 3, stats);
         trace_mark(so.tracer, "ai_calm_replay", rs);
     }
-    if (skin) ai_polish_kernel<S, true><<<g2, 128, 0, stream>>>(a, P64, P32, so, rq, 2, stats);
-    else ai_polish_kernel<S, false><<<g2, 128, 0, stream>>>(a, P64, P32, so, rq, 2, stats);
+    if (skin && rq.pstate) ai_polish_kernel<S, true, true><<<g2, 128, 0, stream>>>(a, P64, P32, so, rq, 2, stats);
+    else if (skin) ai_polish_kernel<S, true, false><<<g2, 128, 0, stream>>>(a, P64, P32, so, rq, 2, stats);
+    else ai_polish_kernel<S, false, false><<<g2, 128, 0, stream>>>(a, P64, P32, so, rq, 2, stats);
     trace_mark(so.tracer, "ai_polish", stream);
     ai_replay_kernel<S><<<g2, 128, 0, stream>>>(a, P64, rq, 2, stats);
     trace_mark(so.tracer, "ai_polish_replay", stream);

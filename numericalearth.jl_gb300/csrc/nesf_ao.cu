@@ -370,7 +370,7 @@ template <class S, bool SKIN>
 __global__ void __launch_bounds__(128) ao_polish_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
                                                         const DevIface<double>* __restrict__ P64s,
                                                         const DevIface<float>* __restrict__ P32s, SolveOpts so,
-                                                        ReplayQueue rq, DevStats* stats) {
+                                                        ReplayQueue rq, int rpart, DevStats* stats) {
     const int nxr = a.L.nx + 2;
     const int64_t ring = (int64_t)nxr * (a.L.ny + 2);
     const unsigned n = rq.count[1];
@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(128) ao_polish_kernel(AOArgs<S> a, DevIface<do
             else surface_const(P, c, c.Ti, surface_specific_humidity(P, c.pa, c.Ti), s);
             outcome = newton_fp64<SKIN>(P, c, s, x, J, rho, so, us, ts, qst, f64it, reason);
         }
-        replay_push(rq, outcome == FAST_REPLAY, id);
+        replay_push(rq, outcome == FAST_REPLAY, id, rpart);
         if (outcome == FAST_REPLAY) {
             if (stats) {
                 stats_add(stats, false, false, 0, false, false, 0, true, false);
@@ -415,17 +415,17 @@ __global__ void __launch_bounds__(128) ao_polish_kernel(AOArgs<S> a, DevIface<do
     }
 }
 
-// Pass 2: the queued cells, packed, through the reference's FP64 iteration.
+// Pass 2: the cells queued in `part`, packed, through the reference's FP64 iteration.
 template <class S, bool SKIN>
 __global__ void __launch_bounds__(128) ao_replay_kernel(AOArgs<S> a, DevIface<double> P64,
                                                         const DevIface<double>* __restrict__ P64s, ReplayQueue rq,
-                                                        DevStats* stats) {
+                                                        int part, DevStats* stats) {
     const int nxr = a.L.nx + 2;
     const int64_t ring = (int64_t)nxr * (a.L.ny + 2);
-    const unsigned n = rq.count[0];
+    const unsigned n = rq.count[part];
     for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n && (int64_t)q < rq.capacity;
          q += gridDim.x * blockDim.x) {
-        uint32_t id = rq.idx[q];
+        uint32_t id = rq.idx[(int64_t)part * rq.capacity + q];
         int64_t m = (int64_t)id / ring, r = (int64_t)id % ring;
         const DevIface<double>& P = P64s ? P64s[m] : P64;
         int i = (int)(r % nxr), j = (int)(r / nxr);
@@ -449,7 +449,7 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
                                const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec,
                                bool skin, SolveOpts so, const WorkList& wl, const ReplayQueue& rq,
                                const WarmStart& ws, DevStats* stats, cudaStream_t stream,
-                               cudaEvent_t before_pass1) {
+                               cudaEvent_t before_pass1, const TailLane* tail) {
     const int64_t ring = (int64_t)(a.L.nx + 2) * (a.L.ny + 2);
     const int threads = so.block;   // <= 128: the kernels are compiled with __launch_bounds__(128)
     const int nm = members > 1 ? members : 1;
@@ -511,17 +511,36 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
     // passes 1b and 2: enough resident blocks to sweep the queues (grid-stride)
     unsigned g2 = (unsigned)(sms * so.deferred_per_sm);
     const DevIface<double>* pm = ens ? P64s : nullptr;
+    // with a second lane, pass 1's replays (part 0) run beside the polish pass, whose own
+    // replays (part 2) follow it; without, the polish pass's replays join part 0
+    const bool split = adaptive && tail && tail->stream;
+    cudaStream_t rs = stream;
+    if (split) {
+        if ((e = cudaEventRecord(tail->fork, stream)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(tail->stream, tail->fork, 0)) != cudaSuccess) return e;
+        rs = tail->stream;
+        if (skin) ao_replay_kernel<S, true><<<g2, 128, 0, rs>>>(a, P64, pm, rq, 0, stats);
+        else ao_replay_kernel<S, false><<<g2, 128, 0, rs>>>(a, P64, pm, rq, 0, stats);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        trace_mark(so.tracer, "ao_replay", rs);
+    }
+    const int rpart = split ? 2 : 0;
     if (adaptive) {
-        if (skin) ao_polish_kernel<S, true><<<g2, 128, 0, stream>>>(a, P64, P32, pm, ens ? P32s : nullptr, so, rq, stats);
-        else ao_polish_kernel<S, false><<<g2, 128, 0, stream>>>(a, P64, P32, pm, ens ? P32s : nullptr, so, rq, stats);
+        if (skin) ao_polish_kernel<S, true><<<g2, 128, 0, stream>>>(a, P64, P32, pm, ens ? P32s : nullptr, so, rq, rpart, stats);
+        else ao_polish_kernel<S, false><<<g2, 128, 0, stream>>>(a, P64, P32, pm, ens ? P32s : nullptr, so, rq, rpart, stats);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         trace_mark(so.tracer, "ao_polish", stream);
     }
-    if (skin) ao_replay_kernel<S, true><<<g2, 128, 0, stream>>>(a, P64, pm, rq, stats);
-    else ao_replay_kernel<S, false><<<g2, 128, 0, stream>>>(a, P64, pm, rq, stats);
-    trace_mark(so.tracer, "ao_replay", stream);
-    return cudaGetLastError();
+    if (skin) ao_replay_kernel<S, true><<<g2, 128, 0, stream>>>(a, P64, pm, rq, rpart, stats);
+    else ao_replay_kernel<S, false><<<g2, 128, 0, stream>>>(a, P64, pm, rq, rpart, stats);
+    trace_mark(so.tracer, split ? "ao_polish_replay" : "ao_replay", stream);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (split) {
+        if ((e = cudaEventRecord(tail->join, rs)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(stream, tail->join, 0)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 template <class S>
@@ -549,8 +568,9 @@ static cudaError_t preload_ao_t() {
 cudaError_t launch_ao(const AOArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream, cudaEvent_t before_pass1) {
-    return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, ws, stats, stream, before_pass1);
+                      cudaStream_t stream, cudaEvent_t before_pass1, const TailLane* tail) {
+    return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, ws, stats, stream, before_pass1,
+                       tail);
 }
 cudaError_t preload_ao_kernels(const AOArgs<double>*) { return preload_ao_t<double>(); }
 #endif
@@ -558,8 +578,9 @@ cudaError_t preload_ao_kernels(const AOArgs<double>*) { return preload_ao_t<doub
 cudaError_t launch_ao(const AOArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream, cudaEvent_t before_pass1) {
-    return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, ws, stats, stream, before_pass1);
+                      cudaStream_t stream, cudaEvent_t before_pass1, const TailLane* tail) {
+    return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, ws, stats, stream, before_pass1,
+                       tail);
 }
 cudaError_t preload_ao_kernels(const AOArgs<float>*) { return preload_ao_t<float>(); }
 #endif

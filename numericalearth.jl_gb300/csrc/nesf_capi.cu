@@ -24,6 +24,8 @@ struct nesf_context {
     DevIface<float>* d_p32;
     int32_t capacity_members;
     uint32_t* d_replay;         // the deferred-cell queues of the FP32 solvers (4 parts x capacity)
+    float* d_pstate;            // pass 1's state of the polish queue's entries (sea-ice solves)
+    int64_t pstate_capacity;
     unsigned int* d_replay_count;   // [8]: the queue parts [0..3], pass 1's fetch counter [4]
     int64_t replay_capacity;
     uint32_t* d_work;           // compacted work lists of the solves
@@ -381,6 +383,8 @@ int nesf_context_create(int32_t device, nesf_context** out) {
     c->d_p32 = nullptr;
     c->d_replay = nullptr;
     c->replay_capacity = 0;
+    c->d_pstate = nullptr;
+    c->pstate_capacity = 0;
     c->d_work = nullptr;
     c->d_work_count = nullptr;
     c->work_capacity = 0;
@@ -423,6 +427,7 @@ int nesf_context_destroy(nesf_context* c) {
         cudaFree(c->d_p64);
         cudaFree(c->d_p32);
         cudaFree(c->d_replay);
+        cudaFree(c->d_pstate);
         cudaFree(c->d_replay_count);
         cudaFree(c->d_work);
         cudaFree(c->d_work_count);
@@ -540,7 +545,7 @@ static int check_options(const nesf_solver_options& o, const char* who) {
 // The context's queues of deferred cells (replay and polish), grown to `cells`
 // entries each (caller holds ctx->lock). Growing synchronises the device: size
 // the first call for the largest grid.
-static int replay_queue(nesf_context* ctx, int64_t cells, ReplayQueue* q) {
+static int replay_queue(nesf_context* ctx, int64_t cells, ReplayQueue* q, bool with_state = false) {
     if (cells > ctx->replay_capacity) {
         cudaError_t e = cudaDeviceSynchronize();
         if (e != cudaSuccess) return cuda_fail(e, "replay queue");
@@ -550,9 +555,21 @@ static int replay_queue(nesf_context* ctx, int64_t cells, ReplayQueue* q) {
         NESF_CUDA(cudaMalloc(&ctx->d_replay, 4 * sizeof(uint32_t) * (size_t)cells));
         ctx->replay_capacity = cells;
     }
+    // the polish state (sea-ice solves): one entry per polish-queue entry, so that every
+    // polished cell takes the same path whatever its position in the queue
+    if (with_state && ctx->pstate_capacity < ctx->replay_capacity) {
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) return cuda_fail(e, "polish state");
+        cudaFree(ctx->d_pstate);
+        ctx->d_pstate = nullptr;
+        ctx->pstate_capacity = 0;
+        NESF_CUDA(cudaMalloc(&ctx->d_pstate, sizeof(float) * kPolishStateFloats * (size_t)ctx->replay_capacity));
+        ctx->pstate_capacity = ctx->replay_capacity;
+    }
     q->idx = ctx->d_replay;
     q->count = ctx->d_replay_count;
     q->capacity = ctx->replay_capacity;
+    q->pstate = with_state ? ctx->d_pstate : nullptr;
     return NESF_OK;
 }
 
@@ -788,12 +805,18 @@ static int ocean_fluxes(nesf_context* ctx, const nesf_interface_params* params, 
     if ((r = work_list(ctx, ring, 1, &wl))) return r;
     if ((r = warm_buffers(ctx, o, ring, &ws))) return r;
     SolveOpts so = solve_opts(o, ctx);
+    // pass 1's replays beside the polish pass (the tuning's two_lanes)
+    TailLane tl{nullptr, nullptr, nullptr};
+    if (o.precision == NESF_F32_ADAPTIVE && ctx->tuning.two_lanes) {
+        if ((r = tail_lane(ctx))) return r;
+        tl = TailLane{ctx->tail, ctx->ev_tail_fork, ctx->ev_tail_join};
+    }
     return with_stats(ctx, stats, s, [&](DevStats* ds) {
         if (f->dtype == NESF_F64)
             return launch_ao(ao_args<double>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl, rq, ws,
-                             ds, s, before_pass1);
+                             ds, s, before_pass1, &tl);
         return launch_ao(ao_args<float>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl, rq, ws, ds,
-                         s, before_pass1);
+                         s, before_pass1, &tl);
     });
 }
 
@@ -988,7 +1011,7 @@ static int sea_ice_fluxes(nesf_context* ctx, const nesf_interface_params* params
     ReplayQueue rq;
     WorkList wl;
     WarmStart ws;
-    if ((r = replay_queue(ctx, ring, &rq))) return r;
+    if ((r = replay_queue(ctx, ring, &rq, true))) return r;
     if ((r = work_list(ctx, ring, 1, &wl))) return r;
     if ((r = warm_buffers(ctx, o, ring, &ws))) return r;
     SolveOpts so = solve_opts(o, ctx);
@@ -1301,7 +1324,7 @@ extern "C" int nesf_compute_atmosphere_ocean_fluxes_noalloc(const nesf_interface
     // calm replays (unused here), pass 1's fetch counter); the launch clears the counters
     // a precision uses before its first pass reads them
     WorkList wl{base + 64, base, ring};
-    ReplayQueue rq{base + 64 + NESF_NOALLOC_MAX_CELLS, base + 2, NESF_NOALLOC_MAX_CELLS};
+    ReplayQueue rq{base + 64 + NESF_NOALLOC_MAX_CELLS, base + 2, NESF_NOALLOC_MAX_CELLS, nullptr};
     DevIface<double> P64 = make_dev_iface<double>(*params);
     DevIface<float> P32 = make_dev_iface<float>(*params);
     bool skin = params->temperature_formulation != NESF_BULK_TEMPERATURE;
@@ -1458,13 +1481,13 @@ extern "C" int nesf_area_integrals(nesf_context* ctx, const nesf_integral_fields
 // ------------------------------------------------------------ coupling step
 // Scratch for the solves of a step, sized before any capture (growing it
 // synchronises the device, which a stream capture forbids).
-static int size_scratch(nesf_context* ctx, int64_t cells, const nesf_solver_options* opts) {
+static int size_scratch(nesf_context* ctx, int64_t cells, const nesf_solver_options* opts, bool sea_ice = false) {
     std::lock_guard<std::mutex> lk(ctx->lock);
     DeviceGuard g(ctx->device);
     ReplayQueue rq;
     WorkList wl;
     WarmStart ws;
-    int r = replay_queue(ctx, cells, &rq);
+    int r = replay_queue(ctx, cells, &rq, sea_ice);
     if (r == NESF_OK) r = work_list(ctx, cells, 1, &wl);
     if (r == NESF_OK) r = warm_buffers(ctx, options_or_default(opts), cells, &ws);
     return r;
@@ -1486,10 +1509,11 @@ static int coupling_lane(nesf_context* ctx) {
 
 static int coupling_scratch(nesf_context* ctx, const nesf_coupling_step_args* a, const nesf_solver_options* opts) {
     int r = size_scratch(ctx, (int64_t)(a->ao->grid.nx + 2) * (a->ao->grid.ny + 2), opts);
+    if (r == NESF_OK) r = tail_lane(ctx);   // the ocean solve's replay lane
     if (r == NESF_OK && a->ai_params && a->ai) {
         if ((r = coupling_lane(ctx))) return r;
         if ((r = tail_lane(ctx->aux))) return r;
-        r = size_scratch(ctx->aux, (int64_t)(a->ai->grid.nx + 2) * (a->ai->grid.ny + 2), opts);
+        r = size_scratch(ctx->aux, (int64_t)(a->ai->grid.nx + 2) * (a->ai->grid.ny + 2), opts, true);
     }
     return r;
 }

@@ -95,7 +95,17 @@ struct ReplayQueue {
     uint32_t* idx;          // linear cell ids (member * ring + ring index)
     unsigned int* count;
     int64_t capacity;
+    float* pstate;          // pass 1's state of each part-1 entry (null: the polish pass repeats
+                            // pass 1's sweep); kPolishStateFloats floats per entry
 };
+
+// Pass 1's state of a cell it sends to the polish pass (the adaptive solver with a skin
+// temperature, whose pass 1 takes the central-difference Jacobian before its decisions, as
+// the polish pass's own sweep does): the FP32 fixed point x, the Jacobian J (4 x 4), the
+// contraction bound and the FP32 map evaluations, at the cell's polish-queue position, so
+// that the polish pass goes straight to its FP64 Newton steps instead of repeating the
+// sweep. Six float4 per entry.
+constexpr int kPolishStateFloats = 24;
 
 // A second stream for the deferred passes and its fork/join events (null: serial).
 struct TailLane {
@@ -948,23 +958,69 @@ __device__ __forceinline__ bool stable_class(const DevIface<float>& P, float Ta,
 
 // Warp-aggregated append of `id` to one part of the deferred-cell queue (lanes
 // with want = true): part 0 the FP64 replays, part 1 the FP64 polishes.
-__device__ __forceinline__ void queue_push(const ReplayQueue& q, int part, bool want, uint32_t id) {
+// Warp-aggregated append of `id` to a queue part; returns its position there, or -1.
+__device__ __forceinline__ int64_t queue_push(const ReplayQueue& q, int part, bool want, uint32_t id) {
     unsigned mask = __activemask();
     unsigned ballot = __ballot_sync(mask, want);
-    if (!want) return;
+    if (!want) return -1;
     int lane = threadIdx.x & 31;
     int leader = __ffs(ballot) - 1;
     unsigned base = 0;
     if (lane == leader) base = atomicAdd(&q.count[part], (unsigned)__popc(ballot));
     base = __shfl_sync(ballot, base, leader);
     unsigned pos = base + __popc(ballot & ((1u << lane) - 1u));
-    if ((int64_t)pos < q.capacity) q.idx[(int64_t)part * q.capacity + pos] = id;
+    if ((int64_t)pos >= q.capacity) return -1;
+    q.idx[(int64_t)part * q.capacity + pos] = id;
+    return (int64_t)pos;
 }
 
 __device__ __forceinline__ void replay_push(const ReplayQueue& q, bool want, uint32_t id, int part = 0) {
     queue_push(q, part, want, id);
 }
-__device__ __forceinline__ void polish_push(const ReplayQueue& q, bool want, uint32_t id) { queue_push(q, 1, want, id); }
+__device__ __forceinline__ int64_t polish_push(const ReplayQueue& q, bool want, uint32_t id) {
+    return queue_push(q, 1, want, id);
+}
+
+// The polish state of part-1 entry `pos` (kPolishStateFloats): x, J row by row, rho, the
+// FP32 map evaluations.
+template <int N>
+__device__ __forceinline__ void polish_state_store(const ReplayQueue& q, int64_t pos, const float (&x)[4],
+                                                   const float (&J)[N][N], float rho, int fp32_it) {
+    float v[kPolishStateFloats];
+#pragma unroll
+    for (int k = 0; k < kPolishStateFloats; k++) v[k] = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 4; k++) v[k] = x[k];
+#pragma unroll
+    for (int i = 0; i < N; i++)
+#pragma unroll
+        for (int j = 0; j < N; j++) v[4 + 4 * i + j] = J[i][j];
+    v[20] = rho;
+    v[21] = __int_as_float(fp32_it);
+    float4* p = reinterpret_cast<float4*>(q.pstate + pos * kPolishStateFloats);
+#pragma unroll
+    for (int k = 0; k < kPolishStateFloats / 4; k++) p[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+}
+
+template <int N>
+__device__ __forceinline__ void polish_state_load(const ReplayQueue& q, int64_t pos, float (&x)[4], float (&J)[N][N],
+                                                  float& rho, int& fp32_it) {
+    float v[kPolishStateFloats];
+    const float4* p = reinterpret_cast<const float4*>(q.pstate + pos * kPolishStateFloats);
+#pragma unroll
+    for (int k = 0; k < kPolishStateFloats / 4; k++) {
+        const float4 w = p[k];
+        v[4 * k] = w.x; v[4 * k + 1] = w.y; v[4 * k + 2] = w.z; v[4 * k + 3] = w.w;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) x[k] = v[k];
+#pragma unroll
+    for (int i = 0; i < N; i++)
+#pragma unroll
+        for (int j = 0; j < N; j++) J[i][j] = v[4 + 4 * i + j];
+    rho = v[20];
+    fp32_it = __float_as_int(v[21]);
+}
 
 // Pass 1 of the adaptive solver (one member, convergence stopping rule), every schedule in
 // one loop: each lane holds a cell and advances its FP32 sweep one map evaluation per trip
@@ -1001,7 +1057,8 @@ __device__ __forceinline__ void adaptive_pass1(Cell& cell, const DevIface<float>
             if (pending) {   // the decisions and the epilogue of the lanes whose sweep is done
                 if (outcome == SWEEP_DECIDE) outcome = sw.decide(so, P32);
                 replay_push(rq, outcome == FAST_REPLAY, cell.id);
-                polish_push(rq, outcome == FAST_POLISH, cell.id);
+                const int64_t ps = polish_push(rq, outcome == FAST_POLISH, cell.id);
+                if (SKIN && ps >= 0 && rq.pstate) polish_state_store(rq, ps, sw.x, sw.J, sw.rho_est, sw.fp32_it);
                 if (outcome == FAST_SOLVED) {
                     cell.store(sw.x, sw.fp32_it);
                     if (stats) stats_add(stats, true, true, sw.fp32_it, false, false, 0, false, sw.fell_back);
@@ -1067,15 +1124,16 @@ inline dim3 pass1_grid(K kernel, dim3 grid, int threads, int sms, bool fetch) {
 }
 
 // before_pass1 (optional): an event the stream waits for after the classify pass and the
-// warm-start inference, before pass 1.
+// warm-start inference, before pass 1. tail (optional): a second lane on which pass 1's
+// replays run beside the polish pass (the queue's part 2 then holds the polish pass's).
 cudaError_t launch_ao(const AOArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream, cudaEvent_t before_pass1 = nullptr);
+                      cudaStream_t stream, cudaEvent_t before_pass1 = nullptr, const TailLane* tail = nullptr);
 cudaError_t launch_ao(const AOArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream, cudaEvent_t before_pass1 = nullptr);
+                      cudaStream_t stream, cudaEvent_t before_pass1 = nullptr, const TailLane* tail = nullptr);
 // Loads (under lazy module loading) every kernel that the one-member atmosphere-ocean
 // solve of storage S can launch, so that a later launch loads no module.
 cudaError_t preload_ao_kernels(const AOArgs<double>*);

@@ -22,7 +22,16 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 # The streaming kernels (interpolation, sea-ice-ocean fluxes, assembly) are HBM-bound:
 # without contracted multiply-adds they round exactly like the CPU restatement.
-PER_FILE_FLAGS = {"nesf_exchange.cu": ["-fmad=false"]}
+# The interface solves' FP32 arithmetic -- the adaptive solver's FP32 sweep, its FP32 flux
+# epilogue, the classify passes' features -- uses the hardware's approximate division,
+# square root, logarithm and exponential (FP32 denormals flushed): the sweep's own
+# tests of convergence and conditioning decide which FP32 results are kept, and the
+# cells they do not keep are polished or replayed in FP64, whose arithmetic these flags
+# do not touch (the plain FP64 path, the polish's Newton steps and the replays are
+# unchanged). Measured on the 1/8-degree step: 6.70 -> 5.77 ms, the largest error
+# against the FP64 oracle 4.3e-6 both ways.
+FAST_FP32 = ["--use_fast_math"]
+PER_FILE_FLAGS = {"nesf_exchange.cu": ["-fmad=false"], "nesf_ao.cu": FAST_FP32, "nesf_ai.cu": FAST_FP32}
 # The solve files instantiate every kernel for FP64 and FP32 storage: each is compiled
 # twice, one storage type per object, so the slowest translation unit takes half as long.
 SPLIT_BY_STORAGE = ("nesf_ao.cu", "nesf_ai.cu", "nesf_al.cu")
