@@ -79,9 +79,47 @@ __device__ __forceinline__ void ao_store(const DevIface<double>& P, const AOArgs
 // finite and clear of the rounding that a contracted multiply-add could move (R_m's and
 // the heat capacities' sums far from cancelling, the density's quotient within range),
 // so the signs are ao_store's; other cells take ao_store. rho is replaced by +-1 of its
-// sign, and the division by |dU| > 0 leaves a zero unchanged.
+// sign, and the division by |dU| > 0 leaves a zero unchanged. FP32 fields decide in FP32
+// (Pf: the parameters rounded to FP32) with margins ten times wider, which the FP32
+// rounding of each factor stays far inside; FP64 operations and conversions run at 1/64
+// of the FP32 rate, and land is a third of the grid.
 template <class S>
-__device__ __forceinline__ void ao_store_land(const DevIface<double>& P, const AOArgs<S>& a, int64_t k, int iters) {
+__device__ __forceinline__ void ao_store_land(const DevIface<double>& P, const DevIface<float>& Pf, const AOArgs<S>& a,
+                                              int64_t k, int iters) {
+    if constexpr (sizeof(S) == sizeof(float)) {
+        const float ua = a.ua[k], va = a.va[k], Ta = a.Ta[k], pa = a.pa[k], qa = a.qa[k];
+        const float f = 1.0f + (Pf.eps - 1.0f) * qa;
+        const float den = gas_constant_air(Pf, qa) * Ta;
+        const float cp = cp_m(Pf, qa), Lv = latent_heat_vapor(Pf, Ta);
+        const bool clear = fabsf(f) > 1e-5f * (1.0f + fabsf(Pf.eps - 1.0f) * fabsf(qa)) &&
+                           fabsf(cp) > 1e-5f * (fabsf(Pf.cpd) + fabsf(Pf.cpv - Pf.cpd) * fabsf(qa)) &&
+                           fabsf(Lv) > 1e-5f * (fabsf(Pf.Lv0) + fabsf(Pf.cpv - Pf.cpl) * fabsf(Ta - Pf.T0)) &&
+                           fabsf(pa) > 1e-30f && fabsf(pa) < 1e30f && fabsf(den) > 1e-30f && fabsf(den) < 1e30f &&
+                           fabsf(cp) < 1e30f && fabsf(Lv) < 1e30f && isfinite(ua) && isfinite(va);
+        if (clear) {
+            const float r = copysignf(1.0f, pa) * copysignf(1.0f, den);
+            const float z = 0.0f;
+            const bool calm = ua == 0.0f && va == 0.0f;
+            const float tx = calm ? 0.0f : -(z * z) * ua;
+            const float ty = calm ? 0.0f : -(z * z) * va;
+            st(a.Qv, k, -r * Lv * z * z);
+            st(a.QT, k, -r * cp * z * z);
+            st(a.Jv, k, -r * z * z);
+            st(a.tx, k, r * tx);
+            st(a.ty, k, r * ty);
+            st(a.Ts, k, (S)(273.15 - P.off_ifc));
+            st(a.us, k, z);
+            st(a.ts, k, z);
+            st(a.qs, k, z);
+            if (a.iters) a.iters[k] = iters;
+            return;
+        }
+        CellConst<double> c;
+        bool land;
+        ao_load(P, a, k, false, c, land);
+        ao_store(P, a, k, c, true, 0.0, 0.0, 0.0, 273.15, iters);
+        return;
+    }
     const double ua = ld(a.ua, k), va = ld(a.va, k), Ta = ld(a.Ta, k), pa = ld(a.pa, k), qa = ld(a.qa, k);
     const double f = 1.0 + (P.eps - 1.0) * qa;
     const double den = gas_constant_air(P, qa) * Ta;
@@ -214,7 +252,7 @@ __global__ void __launch_bounds__(128) ao_classify_kernel(AOArgs<S> a, DevIface<
     }
     int64_t slot = worklist_push(wl, m, active, stable, (uint32_t)r);
     if (feat && slot >= 0) mlp::store_features(feat, slot, F);
-    if (in && land) ao_store_land(P, a, k, needs ? 0 : P.maxiter);
+    if (in && land) ao_store_land(P, Pf, a, k, needs ? 0 : P.maxiter);
     if (stats && in && land) stats_add(stats, true, false, 0, false, false, 0, false, false);
 }
 

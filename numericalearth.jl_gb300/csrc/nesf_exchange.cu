@@ -16,34 +16,47 @@
 namespace nesf {
 
 // ------------------------------------------------------------- sea ice - ocean
+// The parameters in arithmetic R, converted once on the host: a conversion from FP64
+// inside the kernel runs on the FP64 pipe, at 1/64 of the FP32 rate on this part, and
+// with FP32 fields it was most of the streaming kernels' time.
+template <class R> struct IOConsts {
+    R rho, cpo, Tfw, slope, ht, us, st, E, kice;
+};
+template <class R> static IOConsts<R> io_consts(const nesf_io_params& p) {
+    return IOConsts<R>{R(p.ocean_reference_density), R(p.ocean_heat_capacity),
+                       R(p.liquidus_freshwater_melting_temperature), R(p.liquidus_slope),
+                       R(p.heat_transfer_coefficient), R(p.friction_velocity), R(p.salt_transfer_coefficient),
+                       R(p.reference_latent_heat), R(p.ice_conductivity)};
+}
+
 // The interface heat flux, temperature and salinity of one cell in arithmetic R
 // (sea_ice_ocean_fluxes.jl:183-205): the bulk formulation, or the three-equation
 // interface conditions (solve_interface_conditions,
 // sea_ice_ocean_heat_flux_formulations.jl:280-313) with the MITgcm root choice.
 template <class R, class S>
-__device__ __forceinline__ void io_interface(const IOArgs<S>& a, const nesf_io_params& p, int64_t k2, R TN, R SN,
-                                             S& Qio_out, S& Tb_out, S& Sb_out) {
-    const R rho = R(p.ocean_reference_density), cpo = R(p.ocean_heat_capacity);
-    const R Tfw = R(p.liquidus_freshwater_melting_temperature), slope = R(p.liquidus_slope);
+__device__ __forceinline__ void io_interface(const IOArgs<S>& a, const nesf_io_params& p, const IOConsts<R>& C,
+                                             int64_t k2, R TN, R SN, S& Qio_out, S& Tb_out, S& Sb_out) {
+    const R rho = C.rho, cpo = C.cpo;
+    const R Tfw = C.Tfw, slope = C.slope;
     R Si = ldr<R>(a.Si, k2), h = ldr<R>(a.hi, k2), aleph = ldr<R>(a.aleph, k2), hc = ldr<R>(a.hc, k2);
     R Tsi = (p.conductive && a.Tint) ? ldr<R>(a.Tint, k2) : R(0);
     if (p.formulation == 1) {
         R Tm = Tfw - slope * SN;
-        Qio_out = S(rho * cpo * R(p.heat_transfer_coefficient) * R(p.friction_velocity) * (TN - Tm) * aleph);
+        Qio_out = S(rho * cpo * C.ht * C.us * (TN - Tm) * aleph);
         Tb_out = S(Tm);
         Sb_out = S(SN);
         return;
     }
-    R E = R(p.reference_latent_heat);
+    R E = C.E;
     R kap = R(0), Ti = R(0);
     if (p.conductive) {
-        kap = h >= hc ? R(p.ice_conductivity) / (h * E) : R(0);
+        kap = h >= hc ? C.kice / (h * E) : R(0);
         Ti = Tsi;
     }
     R l1 = -slope, l2 = Tfw;
-    R us = R(p.friction_velocity);
-    R eta = rho * cpo * R(p.heat_transfer_coefficient) * us / E;
-    R gam = rho * R(p.salt_transfer_coefficient) * us;
+    R us = C.us;
+    R eta = rho * cpo * C.ht * us / E;
+    R gam = rho * C.st * us;
     R th = eta + kap;
     R qa = th * l1;
     R qb = -gam - eta * TN - kap * Ti + th * (l2 - l1 * Si);
@@ -68,22 +81,22 @@ __device__ __forceinline__ void io_interface(const IOArgs<S>& a, const nesf_io_p
 // state as PART 0, and PART 1 only reads the ocean state, so it may run beside
 // kernels that read it.
 template <class S, int PART>
-__global__ void __launch_bounds__(256) io_kernel(IOArgs<S> a, nesf_io_params p) {
+__global__ void __launch_bounds__(256) io_kernel(IOArgs<S> a, nesf_io_params p, IOConsts<S> C, IOConsts<double> C64) {
     using R = S;
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t n = (int64_t)a.L.nx * a.L.ny;
     if (r >= n) return;
     int i = 1 + (int)(r % a.L.nx), j = 1 + (int)(r / a.L.nx);
     int64_t k2 = a.L.at(i, j);
-    const R rho = R(p.ocean_reference_density), cpo = R(p.ocean_heat_capacity);
-    const R Tfw = R(p.liquidus_freshwater_melting_temperature), slope = R(p.liquidus_slope);
+    const R rho = C.rho, cpo = C.cpo;
+    const R Tfw = C.Tfw, slope = C.slope;
     // Part 1: frazil over the column, top level first (sea_ice_ocean_fluxes.jl:153-181).
     // FP32 fields: T_m - T_k cancels in a freezing level, so a level whose FP32 test is
     // within a few ulps of T_m, or that freezes, is decided, adjusted and charged in FP64
     // from its FP32 values (exact in FP64); dQ accumulates in FP64.
     double dQ = 0.0;
     R TN = R(0);
-    bool top_frozen = false;
+    bool top_frozen = false, any_charged = false;
     for (int kk = p.nz; kk >= 1; kk--) {
         int64_t k3 = k2 + (int64_t)(kk - 1) * p.stride_k;
         R Tk = a.T3[k3], Sk = a.S3[k3];
@@ -109,6 +122,7 @@ __global__ void __launch_bounds__(256) io_kernel(IOArgs<S> a, nesf_io_params p) 
         if (PART == 2) continue;
         if (sizeof(R) < sizeof(double)) {
             if (charged) dQ -= dE * a.dz[kk - 1] / p.dt;
+            any_charged = any_charged || charged;
         } else {
             dQ = (double)((R)dQ - (R)dE * R(a.dz[kk - 1]) / R(p.dt));
         }
@@ -118,7 +132,8 @@ __global__ void __launch_bounds__(256) io_kernel(IOArgs<S> a, nesf_io_params p) 
         }
     }
     if (PART == 2) return;
-    st(a.frazil, k2, (R)dQ);
+    // FP32 fields: dQ is still its +0 unless a level was charged (no FP64 conversion then)
+    st(a.frazil, k2, (sizeof(R) < sizeof(double) && !any_charged) ? R(0) : (R)dQ);
     int64_t kN = k2 + (int64_t)(p.nz - 1) * p.stride_k;
     R SN = a.S3[kN];
     R aleph = ldr<R>(a.aleph, k2);
@@ -131,9 +146,9 @@ __global__ void __launch_bounds__(256) io_kernel(IOArgs<S> a, nesf_io_params p) 
     if (sizeof(S) < sizeof(double) && aleph > R(0)) {
         double SN64 = (double)SN;
         double TN64 = top_frozen ? p.liquidus_freshwater_melting_temperature - p.liquidus_slope * SN64 : (double)TN;
-        io_interface<double>(a, p, k2, TN64, SN64, Qio, Tb, Sb);
+        io_interface<double>(a, p, C64, k2, TN64, SN64, Qio, Tb, Sb);
     } else {
-        io_interface<R>(a, p, k2, TN, SN, Qio, Tb, Sb);
+        io_interface<R>(a, p, C, k2, TN, SN, Qio, Tb, Sb);
     }
     if (p.formulation != 1) {
         st(a.Tb, k2, Tb);
@@ -331,16 +346,26 @@ __global__ void __launch_bounds__(kInterpTileCols) interp_tile_kernel(InterpArgs
 }
 
 // ------------------------------------------------------------------ assembly
-// Arithmetic in the storage type S, as the interpolation.
+// Arithmetic in the storage type S, as the interpolation; the parameters converted to S
+// once on the host (as the sea-ice-ocean kernel's).
+template <class R> struct AsmConsts {
+    R rho, cpo, off, sigma, eps_o, alb_o, eps_i, alb_i;
+};
+template <class R> static AsmConsts<R> asm_consts(const nesf_assembly_params& p) {
+    return AsmConsts<R>{R(p.ocean_reference_density), R(p.ocean_heat_capacity), R(p.interface_temperature_offset),
+                        R(p.stefan_boltzmann_constant), R(p.ocean_emissivity), R(p.ocean_albedo),
+                        R(p.ice_emissivity), R(p.ice_albedo)};
+}
+
 template <class S>
-__global__ void __launch_bounds__(256) assemble_ocean_kernel(AsmArgs<S> a, nesf_assembly_params p) {
+__global__ void __launch_bounds__(256) assemble_ocean_kernel(AsmArgs<S> a, AsmConsts<S> p) {
     using R = S;
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= (int64_t)a.L.nx * a.L.ny) return;
     int i = 1 + (int)(r % a.L.nx), j = 1 + (int)(r / a.L.nx);
     int64_t k = a.L.at(i, j), kw = k - 1, ks = k - a.L.sj;
-    const R rinv = R(1) / R(p.ocean_reference_density);
-    const R cinv = R(1) / R(p.ocean_heat_capacity);
+    const R rinv = R(1) / p.rho;
+    const R cinv = R(1) / p.cpo;
     R al = ldzr<R>(a.f.aleph, k);
     R To = ldr<R>(a.f.To, k);
     R Jr = ldzr<R>(a.f.rain, k), Js = ldzr<R>(a.f.snow, k), Ps = ldzr<R>(a.f.isnow, k), Jl = ldzr<R>(a.f.land_fw, k);
@@ -366,11 +391,11 @@ __global__ void __launch_bounds__(256) assemble_ocean_kernel(AsmArgs<S> a, nesf_
     R JT = inactive ? R(0) : JTao + JTio;
     if (a.with_radiation) {
         // apply_air_sea_radiative_fluxes fused: J_T += radiative part
-        R Ts = ldr<R>(a.f.ao_Ts, k) + R(p.interface_temperature_offset);
+        R Ts = ldr<R>(a.f.ao_Ts, k) + p.off;
         R T2 = Ts * Ts;
-        R Iup = R(p.stefan_boltzmann_constant) * R(p.ocean_emissivity) * (T2 * T2);
-        R Ia = -R(p.ocean_emissivity) * ldr<R>(a.f.lw, k);
-        R It = -(1 - R(p.ocean_albedo)) * ldr<R>(a.f.sw, k);
+        R Iup = p.sigma * p.eps_o * (T2 * T2);
+        R Ia = -p.eps_o * ldr<R>(a.f.lw, k);
+        R It = -(1 - p.alb_o) * ldr<R>(a.f.sw, k);
         Ia *= (1 - al);
         It *= (1 - al);
         R Iup_o = Iup * (1 - al);
@@ -388,7 +413,7 @@ __global__ void __launch_bounds__(256) assemble_ocean_kernel(AsmArgs<S> a, nesf_
 }
 
 template <class S>
-__global__ void __launch_bounds__(256) assemble_ice_kernel(AsmArgs<S> a, nesf_assembly_params p) {
+__global__ void __launch_bounds__(256) assemble_ice_kernel(AsmArgs<S> a, AsmConsts<S> p) {
     using R = S;
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= (int64_t)a.L.nx * a.L.ny) return;
@@ -403,11 +428,11 @@ __global__ void __launch_bounds__(256) assemble_ice_kernel(AsmArgs<S> a, nesf_as
     bool inactive = a.f.inactive ? a.f.inactive[k] != 0 : false;
     R top = inactive ? R(0) : SQt;
     if (a.with_radiation) {
-        R Ts = ldr<R>(a.f.ai_Ts, k) + R(p.interface_temperature_offset);
+        R Ts = ldr<R>(a.f.ai_Ts, k) + p.off;
         R T2 = Ts * Ts;
-        R Iup = R(p.stefan_boltzmann_constant) * R(p.ice_emissivity) * (T2 * T2);
-        R Ia = -R(p.ice_emissivity) * ldr<R>(a.f.lw, k);
-        R It = -(1 - R(p.ice_albedo)) * ldr<R>(a.f.sw, k);
+        R Iup = p.sigma * p.eps_i * (T2 * T2);
+        R Ia = -p.eps_i * ldr<R>(a.f.lw, k);
+        R It = -(1 - p.alb_i) * ldr<R>(a.f.sw, k);
         R SQ = (Iup + Ia + It) * al;
         top += inactive ? R(0) : SQ;
         st(a.f.i_up_lw, k, Iup);
@@ -423,7 +448,7 @@ __global__ void __launch_bounds__(256) assemble_ice_kernel(AsmArgs<S> a, nesf_as
 
 // Radiation alone, added in place to an already assembled J_T / top heat flux.
 template <class S, bool ICE>
-__global__ void __launch_bounds__(256) radiation_kernel(AsmArgs<S> a, nesf_assembly_params p) {
+__global__ void __launch_bounds__(256) radiation_kernel(AsmArgs<S> a, AsmConsts<S> p) {
     using R = S;
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= (int64_t)a.L.nx * a.L.ny) return;
@@ -431,13 +456,13 @@ __global__ void __launch_bounds__(256) radiation_kernel(AsmArgs<S> a, nesf_assem
     int64_t k = a.L.at(i, j);
     bool inactive = a.f.inactive ? a.f.inactive[k] != 0 : false;
     if (!ICE) {
-        const R rinv = R(1) / R(p.ocean_reference_density), cinv = R(1) / R(p.ocean_heat_capacity);
+        const R rinv = R(1) / p.rho, cinv = R(1) / p.cpo;
         R al = ldzr<R>(a.f.aleph, k);
-        R Ts = ldr<R>(a.f.ao_Ts, k) + R(p.interface_temperature_offset);
+        R Ts = ldr<R>(a.f.ao_Ts, k) + p.off;
         R T2 = Ts * Ts;
-        R Iup = R(p.stefan_boltzmann_constant) * R(p.ocean_emissivity) * (T2 * T2);
-        R Ia = -R(p.ocean_emissivity) * ldr<R>(a.f.lw, k);
-        R It = -(1 - R(p.ocean_albedo)) * ldr<R>(a.f.sw, k);
+        R Iup = p.sigma * p.eps_o * (T2 * T2);
+        R Ia = -p.eps_o * ldr<R>(a.f.lw, k);
+        R It = -(1 - p.alb_o) * ldr<R>(a.f.sw, k);
         Ia *= (1 - al);
         It *= (1 - al);
         R Iup_o = Iup * (1 - al);
@@ -449,11 +474,11 @@ __global__ void __launch_bounds__(256) radiation_kernel(AsmArgs<S> a, nesf_assem
         st(a.f.o_dn_sw, k, -It);
     } else {
         R al = ldr<R>(a.f.aleph, k);
-        R Ts = ldr<R>(a.f.ai_Ts, k) + R(p.interface_temperature_offset);
+        R Ts = ldr<R>(a.f.ai_Ts, k) + p.off;
         R T2 = Ts * Ts;
-        R Iup = R(p.stefan_boltzmann_constant) * R(p.ice_emissivity) * (T2 * T2);
-        R Ia = -R(p.ice_emissivity) * ldr<R>(a.f.lw, k);
-        R It = -(1 - R(p.ice_albedo)) * ldr<R>(a.f.sw, k);
+        R Iup = p.sigma * p.eps_i * (T2 * T2);
+        R Ia = -p.eps_i * ldr<R>(a.f.lw, k);
+        R It = -(1 - p.alb_i) * ldr<R>(a.f.sw, k);
         R SQ = (Iup + Ia + It) * al;
         a.f.i_top[k] = a.f.i_top[k] + (inactive ? R(0) : SQ);
         st(a.f.i_up_lw, k, Iup);
@@ -509,9 +534,11 @@ static inline unsigned blocks_for(int64_t n, int b) { return (unsigned)((n + b -
 template <class S>
 cudaError_t launch_io(const IOArgs<S>& a, const nesf_io_params& p, cudaStream_t s, int part) {
     int64_t n = (int64_t)a.L.nx * a.L.ny;
-    if (part == 1) io_kernel<S, 1><<<blocks_for(n, 256), 256, 0, s>>>(a, p);
-    else if (part == 2) io_kernel<S, 2><<<blocks_for(n, 256), 256, 0, s>>>(a, p);
-    else io_kernel<S, 0><<<blocks_for(n, 256), 256, 0, s>>>(a, p);
+    const IOConsts<S> C = io_consts<S>(p);
+    const IOConsts<double> C64 = io_consts<double>(p);
+    if (part == 1) io_kernel<S, 1><<<blocks_for(n, 256), 256, 0, s>>>(a, p, C, C64);
+    else if (part == 2) io_kernel<S, 2><<<blocks_for(n, 256), 256, 0, s>>>(a, p, C, C64);
+    else io_kernel<S, 0><<<blocks_for(n, 256), 256, 0, s>>>(a, p, C, C64);
     return cudaGetLastError();
 }
 template cudaError_t launch_io<double>(const IOArgs<double>&, const nesf_io_params&, cudaStream_t, int);
@@ -573,11 +600,12 @@ bool is_interp_kernel(const void* fn, bool fp64) {
 template <class S>
 cudaError_t launch_assemble(const AsmArgs<S>& a, const nesf_assembly_params& p, int which, cudaStream_t s) {
     int64_t n = (int64_t)a.L.nx * a.L.ny;
+    const AsmConsts<S> C = asm_consts<S>(p);
     switch (which) {
-    case 0: assemble_ocean_kernel<S><<<blocks_for(n, 256), 256, 0, s>>>(a, p); break;
-    case 1: assemble_ice_kernel<S><<<blocks_for(n, 256), 256, 0, s>>>(a, p); break;
-    case 2: radiation_kernel<S, false><<<blocks_for(n, 256), 256, 0, s>>>(a, p); break;
-    default: radiation_kernel<S, true><<<blocks_for(n, 256), 256, 0, s>>>(a, p); break;
+    case 0: assemble_ocean_kernel<S><<<blocks_for(n, 256), 256, 0, s>>>(a, C); break;
+    case 1: assemble_ice_kernel<S><<<blocks_for(n, 256), 256, 0, s>>>(a, C); break;
+    case 2: radiation_kernel<S, false><<<blocks_for(n, 256), 256, 0, s>>>(a, C); break;
+    default: radiation_kernel<S, true><<<blocks_for(n, 256), 256, 0, s>>>(a, C); break;
     }
     return cudaGetLastError();
 }
