@@ -244,10 +244,10 @@ REPEAT_ROUNDS = 5
 # 720 x 320 coupled case): the profile summary named here holds the command and the figures.
 NCU_PIPES = {
     "source": "profiles/solve_kernels_f32adaptive_coupled_720x320.md",
-    "ao_kernel": {"issue_active": 0.497, "fma_pipe": 0.226, "xu_pipe": 0.070, "fp64_pipe": 0.194,
-                  "warps_active": 0.256, "lanes_active_per_warp_instruction": 21.9},
-    "ai_kernel": {"issue_active": 0.305, "fma_pipe": 0.122, "xu_pipe": 0.046, "fp64_pipe": 0.189,
-                  "warps_active": 0.129, "lanes_active_per_warp_instruction": 18.2},
+    "ao_adaptive_kernel": {"issue_active": 0.423, "fma_pipe": 0.168, "alu_pipe": 0.220, "xu_inst": 0.089,
+                           "fp64_pipe": 0.289, "warps_active": 0.256, "lanes_active_per_warp_instruction": 24.5},
+    "ai_adaptive_kernel": {"issue_active": 0.349, "fma_pipe": 0.110, "alu_pipe": 0.161, "xu_inst": 0.065,
+                           "fp64_pipe": 0.068, "warps_active": 0.152, "lanes_active_per_warp_instruction": 19.1},
 }
 
 

@@ -704,8 +704,10 @@ int nesf_mlp_selftest(const void* a, const void* b, float* d, int32_t which, voi
  * in one device blob of nesf_mlp_bytes() bytes (FP32 masters, BF16 copies, the
  * gradient and the Adam moments); inference and training run on the tensor cores
  * (tcgen05, BF16 operands, FP32 accumulation). Features are 8 floats per sample
- * (6 used), targets 4 (c_u, c_theta, c_q, and a bit mask of the valid ones as a
- * float), outputs 4 (c_u, c_theta, c_q, 1). The solvers take a trained blob through
+ * (6 used; the feature array 16-byte aligned), targets 4 (c_u, c_theta, c_q, and a
+ * bit mask of the valid ones as a float), outputs 4 (c_u, c_theta, c_q, 1); inference
+ * evaluates GELU with the hardware's tanh approximation (its activations are BF16
+ * anyway), training with tanhf. The solvers take a trained blob through
  * nesf_solver_options.mlp with warm_start = 1 (FP32 modes, single member, bulk
  * interface temperature: a skin temperature keeps the reference's start). No
  * counterpart in the reference. */

@@ -1395,8 +1395,12 @@ extern "C" int nesf_mlp_fit_normalization(void* mlp, const float* x, const float
     return NESF_OK;
 }
 
+// The tile pass reads each sample's 8 features as two 16-byte vectors.
+static bool features_aligned(const float* x) { return ((uintptr_t)x & 15u) == 0; }
+
 extern "C" int nesf_mlp_gradient(void* mlp, const float* x, const float* t, int64_t n, void* stream) {
     if (!mlp || !x || !t || n <= 0) return fail(NESF_ERR_ARG, "nesf_mlp_gradient: bad argument");
+    if (!features_aligned(x)) return fail(NESF_ERR_ARG, "nesf_mlp_gradient: features not 16-byte aligned");
     int64_t tiles = (n + 127) / 128;
     int grid = (int)(tiles < sm_count() ? tiles : sm_count());
     cudaError_t e = mlp_pass(mlp, x, t, nullptr, n, nullptr, 0, grid, false, (cudaStream_t)stream);
@@ -1408,6 +1412,7 @@ extern "C" int nesf_mlp_train(void* mlp, const float* x, const float* t, int64_t
                               float* loss, void* stream) {
     const char* who = "nesf_mlp_train";
     if (!mlp || !x || !t || !o || n <= 0) return fail(NESF_ERR_ARG, "%s: bad argument", who);
+    if (!features_aligned(x)) return fail(NESF_ERR_ARG, "%s: features not 16-byte aligned", who);
     if (o->batch <= 0 || o->batch % 128 != 0) return fail(NESF_ERR_ARG, "%s: batch %d not a multiple of 128", who, o->batch);
     if (o->epochs <= 0 || !(o->learning_rate > 0)) return fail(NESF_ERR_ARG, "%s: epochs / learning rate", who);
     cudaStream_t s = (cudaStream_t)stream;
@@ -1435,6 +1440,7 @@ extern "C" int nesf_mlp_train(void* mlp, const float* x, const float* t, int64_t
 
 extern "C" int nesf_mlp_infer(void* mlp, const float* x, int64_t n, float* out, void* stream) {
     if (!mlp || !x || !out || n <= 0) return fail(NESF_ERR_ARG, "nesf_mlp_infer: bad argument");
+    if (!features_aligned(x)) return fail(NESF_ERR_ARG, "nesf_mlp_infer: features not 16-byte aligned");
     int64_t tiles = (n + 127) / 128;
     int grid = (int)(tiles < sm_count() ? tiles : sm_count());
     cudaError_t e = mlp_pass(mlp, x, nullptr, out, n, nullptr, 0, grid, false, (cudaStream_t)stream);

@@ -315,8 +315,11 @@ __global__ void __launch_bounds__(128, TRAIN ? 1 : 4) pass_kernel(Blob* __restri
 #pragma unroll
             for (int k = 0; k < 16; k++) v[k] = 0.0f;
             if (valid) {
+                const float4* xs = reinterpret_cast<const float4*>(io.x + slot * 8);   // 32-byte rows
+                const float4 a = xs[0], b = xs[1];
+                const float f[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
 #pragma unroll
-                for (int k = 0; k < kIn; k++) v[k] = (io.x[slot * 8 + k] - in_mu[k]) / in_sig[k];
+                for (int k = 0; k < kIn; k++) v[k] = (f[k] - in_mu[k]) / in_sig[k];
             }
             store_row16(sm + oX, 128, r, 0, v);
         }
@@ -329,7 +332,10 @@ __global__ void __launch_bounds__(128, TRAIN ? 1 : 4) pass_kernel(Blob* __restri
             float v[16];
             tc::tmem_ld16(tc::tmem_at(tm + tD, warp, c0), v);
 #pragma unroll
-            for (int k = 0; k < 16; k++) { Z1[c0 + k] = v[k] + sb1[c0 + k]; v[k] = gelu(Z1[c0 + k]); }
+            for (int k = 0; k < 16; k++) {
+                Z1[c0 + k] = v[k] + sb1[c0 + k];
+                v[k] = TRAIN ? gelu(Z1[c0 + k]) : gelu_approx(Z1[c0 + k]);
+            }
             store_row16(sm + oH1, 128, r, c0, v);
         }
         // ---- layer 2: D = H1 W2^T
@@ -340,7 +346,10 @@ __global__ void __launch_bounds__(128, TRAIN ? 1 : 4) pass_kernel(Blob* __restri
             float v[16];
             tc::tmem_ld16(tc::tmem_at(tm + tD, warp, c0), v);
 #pragma unroll
-            for (int k = 0; k < 16; k++) { Z2[c0 + k] = v[k] + sb2[c0 + k]; v[k] = gelu(Z2[c0 + k]); }
+            for (int k = 0; k < 16; k++) {
+                Z2[c0 + k] = v[k] + sb2[c0 + k];
+                v[k] = TRAIN ? gelu(Z2[c0 + k]) : gelu_approx(Z2[c0 + k]);
+            }
             store_row16(sm + oH2, 128, r, c0, v);
         }
         // ---- layer 3: D = H2 W3^T (16 columns, 3 used)

@@ -98,6 +98,17 @@ __device__ __forceinline__ float gelu(float x) {
     return 0.5f * x * (1.0f + tanhf(u));
 }
 
+// The same GELU with the hardware's tanh approximation (tanh.approx.f32, relative error
+// about 2^-11): for inference only, whose activations are rounded to BF16 (2^-8) before the
+// next layer anyway; training keeps tanhf, so that its gradients follow the restatement.
+__device__ __forceinline__ float gelu_approx(float x) {
+    const float k = 0.7978845608028654f;          // sqrt(2 / pi)
+    float u = k * (x + 0.044715f * x * x * x);
+    float t;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
+    return 0.5f * x * (1.0f + t);
+}
+
 __device__ __forceinline__ float gelu_grad(float x) {
     const float k = 0.7978845608028654f;
     float u = k * (x + 0.044715f * x * x * x);
