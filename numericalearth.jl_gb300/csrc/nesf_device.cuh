@@ -395,7 +395,10 @@ __device__ __forceinline__ R vsgs2(const DevIface<R>& P, R us, R bs) {
         conv = P.const_sg * P.const_sg;
     } else if (P.subgrid_kind == NESF_SUBGRID_CONVECTIVE) {
         R Jb = -us * bs;
-        R UG = M<R>::fmax(P.min_gust, P.beta * M<R>::cbrt(M<R>::fmax(R(0), Jb) * P.hbl));
+        // a stable or neutral cell has no buoyancy flux to take the cube root of: cbrt(0) = 0
+        // exactly, and the cube root is the iteration's dearest call after pow in FP64
+        R wb = M<R>::fmax(R(0), Jb) * P.hbl;
+        R UG = M<R>::fmax(P.min_gust, P.beta * (wb != R(0) ? M<R>::cbrt(wb) : wb));
         conv = UG * UG;
     }
     return conv + P.meso_sg * P.meso_sg;
