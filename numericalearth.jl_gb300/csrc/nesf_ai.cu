@@ -101,14 +101,15 @@ __device__ __forceinline__ void ai_store_fast(const DevIface<double>& P, const A
     if (a.iters) a.iters[k] = iters;
 }
 
-template <bool SKIN>
+template <bool SKIN, bool PAIR = false>
 __device__ __forceinline__ int ai_plain(const DevIface<double>& P, const CellConst<double>& c, double Ts0,
-                                        double& us, double& ts, double& qst, double& Ts, bool& nonconv) {
+                                        double& us, double& ts, double& qst, double& Ts, bool& nonconv,
+                                        LanePair lp = LanePair{0u, 0}) {
     double qs0 = surface_specific_humidity(P, c.pa, Ts0);
     SurfaceConst<double> s;
     surface_const(P, c, Ts0, qs0, s);
     us = ts = qst = 1e-4;   // initial guess (atmosphere_sea_ice_fluxes.jl:127)
-    int it = solve_plain<SKIN>(P, c, s, us, ts, qst, nonconv);
+    int it = solve_plain<SKIN, false, PAIR>(P, c, s, us, ts, qst, nonconv, lp);
     Ts = s.Ts;
     return it;
 }
@@ -381,15 +382,17 @@ __global__ void __launch_bounds__(128) ai_polish_kernel(AIArgs<S> a, DevIface<do
     }
 }
 
-// Pass 2: the queued cells, packed, through the reference's FP64 iteration. The
+// Pass 2: the queued cells, packed, through the reference's FP64 iteration, two lanes per
+// cell (LanePair: the profiles' stability functions and logarithms split between them). The
 // initial interface temperature is still in a.Ts: pass 1 did not write these cells.
 template <class S>
 __global__ void __launch_bounds__(128) ai_replay_kernel(AIArgs<S> a, DevIface<double> P, ReplayQueue rq, int part,
                                                         DevStats* stats) {
     const int nxr = a.L.nx + 2;
     const unsigned n = rq.count[part];
-    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n && (int64_t)q < rq.capacity;
-         q += gridDim.x * blockDim.x) {
+    const LanePair lp{3u << ((threadIdx.x & 31u) & ~1u), (int)(threadIdx.x & 1u)};
+    for (unsigned q = (blockIdx.x * blockDim.x + threadIdx.x) >> 1; q < n && (int64_t)q < rq.capacity;
+         q += (gridDim.x * blockDim.x) >> 1) {
         int64_t r = rq.idx[(int64_t)part * rq.capacity + q];
         int i = (int)(r % nxr), j = (int)(r / nxr);
         int64_t k = a.L.at(i, j);
@@ -399,10 +402,11 @@ __global__ void __launch_bounds__(128) ai_replay_kernel(AIArgs<S> a, DevIface<do
         ai_load(P, a, k, c, aleph, Ts0, land);
         double us, ts, qst, Ts;
         bool nonconv;
-        int it = P.temp_form != NESF_BULK_TEMPERATURE ? ai_plain<true>(P, c, Ts0, us, ts, qst, Ts, nonconv)
-                                                      : ai_plain<false>(P, c, Ts0, us, ts, qst, Ts, nonconv);
-        ai_store(P, a, k, c, us, ts, qst, Ts, it);
-        if (stats) stats_add(stats, false, true, it, nonconv, false, it, false, false);
+        int it = P.temp_form != NESF_BULK_TEMPERATURE ? ai_plain<true, true>(P, c, Ts0, us, ts, qst, Ts, nonconv, lp)
+                                                      : ai_plain<false, true>(P, c, Ts0, us, ts, qst, Ts, nonconv, lp);
+        const bool mine = lp.half == 0;   // lane 0 of the pair stores and counts
+        if (mine) ai_store(P, a, k, c, us, ts, qst, Ts, it);
+        if (stats) stats_add(stats, false, mine, it, mine && nonconv, false, mine ? it : 0, false, false);
     }
 }
 

@@ -453,7 +453,8 @@ __global__ void __launch_bounds__(128) ao_polish_kernel(AOArgs<S> a, DevIface<do
     }
 }
 
-// Pass 2: the cells queued in `part`, packed, through the reference's FP64 iteration.
+// Pass 2: the cells queued in `part`, packed, through the reference's FP64 iteration, two
+// lanes per cell (LanePair: the profiles' stability functions and logarithms split between them).
 template <class S, bool SKIN>
 __global__ void __launch_bounds__(128) ao_replay_kernel(AOArgs<S> a, DevIface<double> P64,
                                                         const DevIface<double>* __restrict__ P64s, ReplayQueue rq,
@@ -461,8 +462,9 @@ __global__ void __launch_bounds__(128) ao_replay_kernel(AOArgs<S> a, DevIface<do
     const int nxr = a.L.nx + 2;
     const int64_t ring = (int64_t)nxr * (a.L.ny + 2);
     const unsigned n = rq.count[part];
-    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n && (int64_t)q < rq.capacity;
-         q += gridDim.x * blockDim.x) {
+    const LanePair lp{3u << ((threadIdx.x & 31u) & ~1u), (int)(threadIdx.x & 1u)};
+    for (unsigned q = (blockIdx.x * blockDim.x + threadIdx.x) >> 1; q < n && (int64_t)q < rq.capacity;
+         q += (gridDim.x * blockDim.x) >> 1) {
         uint32_t id = rq.idx[(int64_t)part * rq.capacity + q];
         int64_t m = (int64_t)id / ring, r = (int64_t)id % ring;
         const DevIface<double>& P = P64s ? P64s[m] : P64;
@@ -476,9 +478,10 @@ __global__ void __launch_bounds__(128) ao_replay_kernel(AOArgs<S> a, DevIface<do
         SurfaceConst<double> s;
         surface_const(P, c, c.Ti, qs0, s);
         bool nonconv;
-        int it = solve_plain<SKIN>(P, c, s, us, ts, qst, nonconv);
-        ao_store(P, a, k, c, false, us, ts, qst, s.Ts, it);
-        if (stats) stats_add(stats, false, true, it, nonconv, false, it, false, false);
+        int it = solve_plain<SKIN, false, true>(P, c, s, us, ts, qst, nonconv, lp);
+        const bool mine = lp.half == 0;   // lane 0 of the pair stores and counts
+        if (mine) ao_store(P, a, k, c, false, us, ts, qst, s.Ts, it);
+        if (stats) stats_add(stats, false, mine, it, mine && nonconv, false, mine ? it : 0, false, false);
     }
 }
 

@@ -503,11 +503,23 @@ __device__ __forceinline__ void coefficient_fluxes(const DevIface<R>& P, R dU2, 
     qs_n = Cd == R(0) ? R(0) : Cq / sCd * dq;
 }
 
+// Two lanes of a warp on one cell (the FP64 replays): `half` 0 or 1, `mask` the pair's lanes.
+struct LanePair {
+    unsigned mask;
+    int half;
+};
+
 // iterate_interface_fluxes(::SimilarityTheoryFluxes) (:315-385), or the coefficient-based
-// formulation's when the interface uses it.
-template <class R>
+// formulation's when the interface uses it. PAIR: the two lanes of `lp` iterate the same
+// cell and split the logarithmic profiles' four stability-function values and two
+// logarithms between them -- lane 0 psi(h / L) and log(h / l_u), lane 1 psi(l / L) and
+// log(h / l_t) -- each by the same function and expression as the single-lane path, then
+// exchange them: a dependent FP64 chain (one cell's iterations, ~64 cycles per dependent
+// FP64 instruction) shortens by the split part.
+template <class R, bool PAIR = false>
 __device__ __forceinline__ void iterate_fluxes(const DevIface<R>& P, const CellConst<R>& c, const SurfaceConst<R>& s,
-                                               R us, R ts, R qst, R& us_n, R& ts_n, R& qs_n) {
+                                               R us, R ts, R qst, R& us_n, R& ts_n, R& qs_n,
+                                               LanePair lp = LanePair{0u, 0}) {
     if (__builtin_expect(P.flux_form == NESF_FLUXES_COEFFICIENT_BASED, 0)) {   // off the hot path's layout
         coefficient_fluxes(P, c.dU2, s.gTv, s.A1, s.A2, s.dth, s.dq, us, ts, qst, us_n, ts_n, qs_n);
         return;
@@ -520,8 +532,22 @@ __device__ __forceinline__ void iterate_fluxes(const DevIface<R>& P, const CellC
     R h = M<R>::fmax(P.h - P.d0, R(2) * lu);
     // 1 / L, L = u*^2 / (kappa b*) (Inf when b* = 0)
     R invL = bs == R(0) ? R(0) : (P.vk * bs) / (us * us);
-    R chiu = P.vk / similarity_profile(P.form, P.psi[0], h, lu, invL);
-    R chit = P.vk / similarity_profile(P.form, P.psi[1], h, lt, invL);
+    R chiu, chit;
+    if (PAIR && P.form != NESF_PROFILE_COARE) {
+        const bool hi = lp.half != 0;
+        const R pm = stability(P.psi[0], (hi ? lu : h) * invL);
+        const R ph = stability(P.psi[1], (hi ? lt : h) * invL);
+        const R lg = M<R>::log(h / (hi ? lt : lu));
+        const R pm2 = __shfl_xor_sync(lp.mask, pm, 1);
+        const R ph2 = __shfl_xor_sync(lp.mask, ph, 1);
+        const R lg2 = __shfl_xor_sync(lp.mask, lg, 1);
+        // similarity_profile's log(h / l) - psi(h / L) + psi(l / L), in its order
+        chiu = P.vk / ((hi ? lg2 : lg) - (hi ? pm2 : pm) + (hi ? pm : pm2));
+        chit = P.vk / ((hi ? lg : lg2) - (hi ? ph2 : ph) + (hi ? ph : ph2));
+    } else {
+        chiu = P.vk / similarity_profile(P.form, P.psi[0], h, lu, invL);
+        chit = P.vk / similarity_profile(P.form, P.psi[1], h, lt, invL);
+    }
     R chiq;
     if (P.scalar_same) {
         chiq = chit;
@@ -592,9 +618,10 @@ __device__ __forceinline__ R skin_temperature(const DevIface<R>& P, const CellCo
 // formulation `s` is fixed; for skin formulations it is rebuilt from the new T_s.
 // QSKIN (land SkinHumidity, DryLayerHumidity): T_s fixed, q_s iterated from the previous iterate; a template
 // flag so that the other solves carry none of its code or registers.
-template <class R, bool SKIN, bool QSKIN = false>
+template <class R, bool SKIN, bool QSKIN = false, bool PAIR = false>
 __device__ __forceinline__ void iterate_state(const DevIface<R>& P, const CellConst<R>& c, SurfaceConst<R>& s,
-                                              R& us, R& ts, R& qst, bool* pinned = nullptr) {
+                                              R& us, R& ts, R& qst, bool* pinned = nullptr,
+                                              LanePair lp = LanePair{0u, 0}) {
     if (SKIN) {
         R Ts = skin_temperature(P, c, s.Ts, us, ts, qst, pinned);
         R qs = surface_specific_humidity(P, c.pa, Ts);
@@ -604,7 +631,7 @@ __device__ __forceinline__ void iterate_state(const DevIface<R>& P, const CellCo
         surface_const(P, c, s.Ts, qs, s);
     }
     R a, b, d;
-    iterate_fluxes(P, c, s, us, ts, qst, a, b, d);
+    iterate_fluxes<R, PAIR>(P, c, s, us, ts, qst, a, b, d, lp);
     us = a;
     ts = b;
     qst = d;
@@ -613,18 +640,19 @@ __device__ __forceinline__ void iterate_state(const DevIface<R>& P, const CellCo
 // compute_interface_state with ConvergenceStopCriteria / FixedIterations
 // (compute_interface_state.jl:10-24, 31-58). Returns the iteration count; the
 // last drift is left in `drift`.
-template <class R, bool SKIN, bool QSKIN = false>
+template <class R, bool SKIN, bool QSKIN = false, bool PAIR = false>
 __device__ __forceinline__ int fixed_point(const DevIface<R>& P, const CellConst<R>& c, SurfaceConst<R>& s,
-                                           R& us, R& ts, R& qst, int maxiter, R& drift) {
+                                           R& us, R& ts, R& qst, int maxiter, R& drift,
+                                           LanePair lp = LanePair{0u, 0}) {
     int it = 0;
     drift = M<R>::inf();
     if (P.stop_kind == NESF_STOP_FIXED_ITERATIONS) {
-        for (; it < maxiter; it++) iterate_state<R, SKIN, QSKIN>(P, c, s, us, ts, qst);
+        for (; it < maxiter; it++) iterate_state<R, SKIN, QSKIN, PAIR>(P, c, s, us, ts, qst, nullptr, lp);
         return it;
     }
     do {
         R u0 = us, t0 = ts, q0 = qst;
-        iterate_state<R, SKIN, QSKIN>(P, c, s, us, ts, qst);
+        iterate_state<R, SKIN, QSKIN, PAIR>(P, c, s, us, ts, qst, nullptr, lp);
         it++;
         drift = M<R>::fabs(us - u0) + M<R>::fabs(ts - t0) + M<R>::fabs(qst - q0);
     } while (!(drift < P.tol) && it < maxiter);

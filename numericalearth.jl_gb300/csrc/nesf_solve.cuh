@@ -353,12 +353,12 @@ __device__ __forceinline__ bool invert(float (&a)[N][N], float (&inv)[N][N]) {
 }
 
 // The reference's FP64 fixed point from (us, ts, qst) and s64. Returns iterations.
-template <bool SKIN, bool QSKIN = false>
+template <bool SKIN, bool QSKIN = false, bool PAIR = false>
 __device__ __forceinline__ int solve_plain(const DevIface<double>& P64, const CellConst<double>& c64,
                                            SurfaceConst<double>& s64, double& us, double& ts, double& qst,
-                                           bool& nonconv) {
+                                           bool& nonconv, LanePair lp = LanePair{0u, 0}) {
     double drift;
-    int it = fixed_point<double, SKIN, QSKIN>(P64, c64, s64, us, ts, qst, P64.maxiter, drift);
+    int it = fixed_point<double, SKIN, QSKIN, PAIR>(P64, c64, s64, us, ts, qst, P64.maxiter, drift, lp);
     nonconv = P64.stop_kind == NESF_STOP_CONVERGENCE && !(drift < P64.tol);
     return it;
 }
