@@ -811,7 +811,7 @@ typedef struct {
     int32_t refill_lanes;     /* pass1_fetch 4: idle lanes that make a warp take new entries, 1..32
                                  (32: warp fetching) (8)                                                */
     int32_t early_ocean_classify; /* coupling step with two lanes: the ocean's classify pass and warm-
-                                 start inference beside the sea-ice pass 1, its pass 1 after it (0) */
+                                 start inference beside the sea-ice pass 1, its pass 1 after it (1) */
     int32_t ice_deferred_per_sm; /* blocks per SM of the sea-ice solve's packed polish and replay
                                  passes, 1..16; 0: deferred_per_sm. Fewer leave registers to the
                                  ocean solve's kernels that run beside them (0)              */
@@ -824,8 +824,9 @@ typedef struct {
 int nesf_set_tuning(nesf_context* ctx, const nesf_tuning* tuning);
 int nesf_get_tuning(nesf_context* ctx, nesf_tuning* tuning);
 /* Coordinate search over the tuning on the caller's workload: for each field in
- * turn, each candidate value is timed (CUDA events on `stream`, one untimed step,
- * then `reps` steps) with the others at their best so far; the fastest setting is
+ * turn, each candidate value is timed (the step captured as a graph under it, CUDA
+ * events on `stream`, one untimed replay, then `reps` replays) with the others at
+ * their best so far; the fastest setting is
  * kept. The chosen tuning is set on the context and written to `out` with its
  * step time. The steps run for real: the outputs and the in/out state (sea-ice
  * surface temperature, frazil-adjusted ocean temperature) are left as that many

@@ -89,7 +89,7 @@ static nesf_tuning default_tuning() {
     t.io_overlap = 1;
     t.pass1_fetch = 2;
     t.refill_lanes = 8;
-    t.early_ocean_classify = 0;
+    t.early_ocean_classify = 1;
     t.ice_deferred_per_sm = 0;
     return t;
 }
@@ -1858,21 +1858,27 @@ extern "C" int nesf_autotune(nesf_context* ctx, const nesf_coupling_step_args* a
             return cuda_fail(e, who);
         }
     }
-    // mean step time of a tuning: one untimed step (it also sizes the scratch), then `reps`
+    // mean step time of a tuning, as the model runs the step: captured as a graph under the
+    // tuning, one untimed replay, then `reps` replays (the lanes of a graph schedule
+    // differently from the same kernels launched one call at a time)
     auto timed = [&](const nesf_tuning& t, double* ms) -> int {
         ctx->tuning = t;
-        int q = nesf_coupling_step(ctx, a, opts, stream);
+        nesf_graph* G = nullptr;
+        int q = nesf_graph_capture(ctx, a, opts, &G);
         if (q) return q;
+        auto done = [&](int rc) { nesf_graph_destroy(G); return rc; };
+        if ((q = nesf_graph_launch(G, stream))) return done(q);
         DeviceGuard g(ctx->device);
-        NESF_CUDA(cudaEventRecord(e0, s));
-        for (int i = 0; i < reps; i++)
-            if ((q = nesf_coupling_step(ctx, a, opts, stream))) return q;
-        NESF_CUDA(cudaEventRecord(e1, s));
-        NESF_CUDA(cudaEventSynchronize(e1));
+        cudaError_t e = cudaEventRecord(e0, s);
+        for (int i = 0; e == cudaSuccess && i < reps; i++)
+            if ((q = nesf_graph_launch(G, stream))) return done(q);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
         float f = 0.0f;
-        NESF_CUDA(cudaEventElapsedTime(&f, e0, e1));
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&f, e0, e1);
+        if (e != cudaSuccess) return done(cuda_fail(e, "nesf_autotune"));
         *ms = (double)f / reps;
-        return NESF_OK;
+        return done(NESF_OK);
     };
     const nesf_solver_options o = options_or_default(opts);
     const bool ice = a->ai_params != nullptr;

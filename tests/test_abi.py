@@ -136,3 +136,18 @@ def test_struct_field_offsets_match_header(tmp_path, k):
                                                       text=True).stdout.splitlines())
     for k in names:
         assert int(out[k]) == getattr(mirror, k).offset, (c_name, k)
+
+
+def test_mlp_entry_points_refuse_misaligned_features():
+    """The network's passes read each sample's 8 features as two 16-byte vectors: a feature
+    pointer off a 16-byte boundary is refused before any device work (checked here with
+    placeholder addresses that are never dereferenced)."""
+    import ctypes as C
+    lib = _lib.load()
+    blob, out, targets = C.c_void_p(0x10000), C.c_void_p(0x20000), C.c_void_p(0x30000)
+    misaligned = C.c_void_p(0x40004)
+    assert lib.nesf_mlp_infer(blob, misaligned, 128, out, None) == A.NESF_ERR_ARG
+    assert b"16-byte" in lib.nesf_last_error()
+    assert lib.nesf_mlp_gradient(blob, misaligned, targets, 128, None) == A.NESF_ERR_ARG
+    o = A.MlpTrainOptions(1, 128, 1e-3, 0.9, 0.999, 1e-8)
+    assert lib.nesf_mlp_train(blob, misaligned, targets, 128, C.byref(o), None, None) == A.NESF_ERR_ARG

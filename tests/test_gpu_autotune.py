@@ -13,7 +13,7 @@ from nesf.coupled import CoupledModel, ICE_NET, OCEAN_NET, RAD_DIAG
 pytestmark = pytest.mark.gpu
 
 DEFAULT = dict(solve_block=128, deferred_per_sm=4, infer_per_sm=4, two_lanes=1, io_overlap=1, pass1_fetch=2,
-               refill_lanes=8, early_ocean_classify=0, ice_deferred_per_sm=0)
+               refill_lanes=8, early_ocean_classify=1, ice_deferred_per_sm=0)
 
 
 @pytest.fixture(scope="module")
@@ -51,7 +51,7 @@ def test_every_tuning_gives_the_same_outputs(model, precision):
                    dict(pass1_fetch=1), dict(pass1_fetch=3), dict(pass1_fetch=3, solve_block=64),
                    dict(pass1_fetch=2, solve_block=32), dict(pass1_fetch=4), dict(pass1_fetch=4, refill_lanes=1),
                    dict(pass1_fetch=4, refill_lanes=16, solve_block=64), dict(pass1_fetch=4, refill_lanes=3),
-                   dict(early_ocean_classify=1), dict(early_ocean_classify=1, two_lanes=0),
+                   dict(early_ocean_classify=0), dict(early_ocean_classify=0, two_lanes=0),
                    dict(ice_deferred_per_sm=1), dict(ice_deferred_per_sm=2, deferred_per_sm=8)):
         got = step(model, precision, **tuning)
         for k in ref:
@@ -64,7 +64,7 @@ def test_warm_start_inference_grid(model):
     try:
         ref = step(model, "f32_adaptive")
         for tuning in (dict(infer_per_sm=1), dict(infer_per_sm=2), dict(infer_per_sm=8), dict(pass1_fetch=4),
-                       dict(pass1_fetch=4, refill_lanes=5), dict(early_ocean_classify=1)):
+                       dict(pass1_fetch=4, refill_lanes=5), dict(early_ocean_classify=0)):
             got = step(model, "f32_adaptive", **tuning)
             for k in ref:
                 assert np.array_equal(ref[k], got[k], equal_nan=True), (tuning, k)
