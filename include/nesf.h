@@ -815,6 +815,10 @@ typedef struct {
     int32_t ice_deferred_per_sm; /* blocks per SM of the sea-ice solve's packed polish and replay
                                  passes, 1..16; 0: deferred_per_sm. Fewer leave registers to the
                                  ocean solve's kernels that run beside them (0)              */
+    int32_t cells_per_thread; /* pass 1 of the adaptive solver, 1..8: work-list entries a thread
+                                 takes one after another -- with one thread per entry the grid
+                                 shrinks by this factor; with fetching each lane reserves this
+                                 many entries per fetch (fewer atomic adds, a longer tail) (1)  */
     double step_ms;           /* nesf_autotune: the chosen configuration's mean step time            */
 } nesf_tuning;
 
@@ -839,9 +843,9 @@ int nesf_autotune(nesf_context* ctx, const nesf_coupling_step_args* args, const 
  * cache file (any path the caller picks) holds one tuning per key. Format, every
  * integer little-endian whatever the host:
  *   "NESFTUNE" (8 bytes), uint32 format version (NESF_TUNING_VERSION), uint32 key
- *   bytes (108), uint32 tuning fields (9), uint32 record count, then per record the
+ *   bytes (108), uint32 tuning fields (10), uint32 record count, then per record the
  *   key (device name, 64 bytes NUL-padded, then its eleven int32 fields) and the
- *   tuning (its nine int32 fields in declaration order, then step_ms as the
+ *   tuning (its ten int32 fields in declaration order, then step_ms as the
  *   IEEE-754 bits of a double).
  * A file of another format version or tuning-field count holds nothing for this
  * library: find reports no entry and store starts the file afresh. A file that does
@@ -849,7 +853,7 @@ int nesf_autotune(nesf_context* ctx, const nesf_coupling_step_args* args, const 
  * overwrite it). Store writes `path`.tmp and renames it over `path`; concurrent
  * writers of one path may lose each other's entries. No reference counterpart (the
  * reference has no autotuner). */
-#define NESF_TUNING_VERSION 1
+#define NESF_TUNING_VERSION 2
 typedef struct {
     char device[64];              /* cudaDeviceProp::name, NUL-padded                         */
     int32_t sm_count;             /* multiprocessors                                          */

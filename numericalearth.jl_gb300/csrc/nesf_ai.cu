@@ -467,10 +467,10 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     const bool fetch_ai = (so.fetch & NESF_FETCH_SEA_ICE) != 0;
     if (prec == NESF_PLAIN_F64) NESF_AI_SKIN(NESF_PLAIN_F64, nullptr);
     else if (one && skin)
-        ai_adaptive_kernel<S, true><<<pass1_grid(ai_adaptive_kernel<S, true>, grid, block, sms, fetch_ai), block, 0,
+        ai_adaptive_kernel<S, true><<<pass1_grid(ai_adaptive_kernel<S, true>, grid, block, sms, fetch_ai, so.cells), block, 0,
                                       stream>>>(a, P64, P32, so, wl, rq, guess, stats);
     else if (one)
-        ai_adaptive_kernel<S, false><<<pass1_grid(ai_adaptive_kernel<S, false>, grid, block, sms, fetch_ai), block,
+        ai_adaptive_kernel<S, false><<<pass1_grid(ai_adaptive_kernel<S, false>, grid, block, sms, fetch_ai, so.cells), block,
                                        0, stream>>>(a, P64, P32, so, wl, rq, guess, stats);
     else if (adaptive) NESF_AI_SKIN(NESF_F32_ADAPTIVE, guess);
     else NESF_AI_SKIN(NESF_F32_POLISH, guess);

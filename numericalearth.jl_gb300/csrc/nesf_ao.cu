@@ -536,10 +536,10 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
     const bool fetch_ao = (so.fetch & NESF_FETCH_OCEAN) != 0;
     if (prec == NESF_PLAIN_F64) NESF_AO_SKIN(NESF_PLAIN_F64);
     else if (one && skin)
-        ao_adaptive_kernel<S, true><<<pass1_grid(ao_adaptive_kernel<S, true>, grid, threads, sms, fetch_ao), threads,
+        ao_adaptive_kernel<S, true><<<pass1_grid(ao_adaptive_kernel<S, true>, grid, threads, sms, fetch_ao, so.cells), threads,
                                       0, stream>>>(a, P64, P32, so, wl, rq, guess, stats);
     else if (one)
-        ao_adaptive_kernel<S, false><<<pass1_grid(ao_adaptive_kernel<S, false>, grid, threads, sms, fetch_ao),
+        ao_adaptive_kernel<S, false><<<pass1_grid(ao_adaptive_kernel<S, false>, grid, threads, sms, fetch_ao, so.cells),
                                        threads, 0, stream>>>(a, P64, P32, so, wl, rq, guess, stats);
     else if (adaptive) NESF_AO_SKIN(NESF_F32_ADAPTIVE);
     else NESF_AO_SKIN(NESF_F32_POLISH);

@@ -91,6 +91,7 @@ static nesf_tuning default_tuning() {
     t.refill_lanes = 8;
     t.early_ocean_classify = 1;
     t.ice_deferred_per_sm = 0;
+    t.cells_per_thread = 1;
     return t;
 }
 
@@ -529,7 +530,8 @@ static SolveOpts solve_opts(const nesf_solver_options& o, const nesf_context* ct
                      t.solve_block, t.deferred_per_sm, t.infer_per_sm,
                      (t.pass1_fetch >= 2 ? NESF_FETCH_SEA_ICE : 0) | (t.pass1_fetch >= 3 ? NESF_FETCH_OCEAN : 0),
                      t.pass1_fetch == 4 ? (t.refill_lanes > 0 ? t.refill_lanes : 8) : 32, tracer_of(ctx),
-                     (float)o.calm_replay_wind, t.ice_deferred_per_sm > 0 ? t.ice_deferred_per_sm : t.deferred_per_sm};
+                     (float)o.calm_replay_wind, t.ice_deferred_per_sm > 0 ? t.ice_deferred_per_sm : t.deferred_per_sm,
+                     t.cells_per_thread > 0 ? t.cells_per_thread : 1};
 }
 
 static int check_options(const nesf_solver_options& o, const char* who) {
@@ -1806,6 +1808,8 @@ static int check_tuning(const nesf_tuning& t, const char* who) {
         return fail(NESF_ERR_ARG, "%s: early_ocean_classify is 0 or 1", who);
     if (t.ice_deferred_per_sm < 0 || t.ice_deferred_per_sm > 16)
         return fail(NESF_ERR_ARG, "%s: ice_deferred_per_sm %d (0..16)", who, t.ice_deferred_per_sm);
+    if (t.cells_per_thread < 0 || t.cells_per_thread > 8)
+        return fail(NESF_ERR_ARG, "%s: cells_per_thread %d (1..8)", who, t.cells_per_thread);
     return NESF_OK;
 }
 
@@ -1817,6 +1821,7 @@ static nesf_tuning complete_tuning(const nesf_tuning& t) {
     if (!r.infer_per_sm) r.infer_per_sm = d.infer_per_sm;
     if (!r.pass1_fetch) r.pass1_fetch = d.pass1_fetch;
     if (!r.refill_lanes) r.refill_lanes = d.refill_lanes;
+    if (!r.cells_per_thread) r.cells_per_thread = d.cells_per_thread;
     return r;
 }
 
@@ -1901,6 +1906,7 @@ extern "C" int nesf_autotune(nesf_context* ctx, const nesf_coupling_step_args* a
         {&nesf_tuning::io_overlap, {1, 0}, ice && a->io_params != nullptr},
         {&nesf_tuning::early_ocean_classify, {1, 0}, ice},
         {&nesf_tuning::ice_deferred_per_sm, {0, 1, 2}, ice && fast},
+        {&nesf_tuning::cells_per_thread, {1, 2, 4}, adaptive},
     };
     for (const Axis& ax : axes) {
         if (r || !ax.used) continue;
@@ -1937,7 +1943,7 @@ namespace {
 constexpr char kTuneMagic[8] = {'N', 'E', 'S', 'F', 'T', 'U', 'N', 'E'};
 constexpr int kKeyInts = 11;
 constexpr uint32_t kKeyBytes = 64 + 4 * kKeyInts;
-constexpr int kTuneInts = 9;
+constexpr int kTuneInts = 10;
 constexpr size_t kRecordBytes = kKeyBytes + 4 * kTuneInts + 8;
 constexpr size_t kHeaderBytes = 8 + 4 * 4;
 
@@ -1962,7 +1968,7 @@ void key_ints(const nesf_tuning_key& k, int32_t* v) {
 void tune_ints(const nesf_tuning& t, int32_t* v) {
     const int32_t w[kTuneInts] = {t.solve_block, t.deferred_per_sm, t.infer_per_sm, t.two_lanes,
                                   t.io_overlap, t.pass1_fetch, t.refill_lanes, t.early_ocean_classify,
-                                  t.ice_deferred_per_sm};
+                                  t.ice_deferred_per_sm, t.cells_per_thread};
     std::memcpy(v, w, sizeof(w));
 }
 
@@ -1992,7 +1998,7 @@ nesf_tuning get_tuning_record(const unsigned char* p) {
     std::memset(&t, 0, sizeof(t));
     t.solve_block = v[0]; t.deferred_per_sm = v[1]; t.infer_per_sm = v[2]; t.two_lanes = v[3];
     t.io_overlap = v[4]; t.pass1_fetch = v[5]; t.refill_lanes = v[6]; t.early_ocean_classify = v[7];
-    t.ice_deferred_per_sm = v[8];
+    t.ice_deferred_per_sm = v[8]; t.cells_per_thread = v[9];
     const uint64_t bits = get_u64(p + 4 * kTuneInts);
     std::memcpy(&t.step_ms, &bits, 8);
     return t;

@@ -242,7 +242,8 @@ __global__ void __launch_bounds__(256) interp_kernel(InterpArgs<S> a) {
 // expressions, same order: bit-identical outputs). A tile whose footprint would exceed
 // the staged bounds (fp_w x fp_h, sized on the host) reads its corners from global memory.
 constexpr int kInterpTileCols = 256;
-constexpr int kInterpMaxTileRows = 16;
+constexpr int kInterpTileRows = 16;      // rows of a tile unless one wave of taller tiles covers the grid
+constexpr int kInterpMaxTileRows = 32;
 
 template <class S>
 __global__ void __launch_bounds__(kInterpTileCols) interp_tile_kernel(InterpArgs<S> a) {
@@ -552,11 +553,26 @@ cudaError_t launch_frac(const Layout2& L, const nesf_exchange_coords& c, const n
 }
 
 // The tiled kernel serves a regular grid without caches when a tile's coarse footprint fits
-// in kInterpStageBytes of shared memory: tile rows are halved from kInterpMaxTileRows until
+// in kInterpStageBytes of shared memory: tile rows are halved from kInterpTileRows until
 // it does (the per-cell gather kernel otherwise). Footprint bounds: a tile's columns span
 // (kInterpTileCols - 1) |dlon / dlon_atmos| fractional indices, its rows (rows - 1) |dlat /
 // dlat_atmos|; + 1 for the stencil's second point and + 1 for the floors.
+// Wave: a tile's blocks run their phases (indices, staging, outputs) one after the other,
+// so a grid slightly larger than the blocks that fit on the GPU at once leaves a second
+// wave of a few blocks, each alone on its SM, after the first. Where tiles of up to
+// kInterpMaxTileRows rows fit the grid into one wave (and their footprint into shared
+// memory), the rows are the fewest that do.
 constexpr size_t kInterpStageBytes = 64 * 1024;
+
+template <class S>
+static bool interp_footprint(const InterpArgs<S>& a, int rows, int& w, int& h) {
+    const double rx = fabs(a.coords.dlon / a.atmos.dlon), ry = fabs(a.coords.dlat / a.atmos.dlat);
+    const double fw = ceil((kInterpTileCols - 1) * rx) + 3, fh = ceil((rows - 1) * ry) + 3;
+    if (!(fw <= 4096 && fh <= 4096 && 18.0 * fw * fh * sizeof(S) <= (double)kInterpStageBytes)) return false;
+    w = (int)fw;
+    h = (int)fh;
+    return true;
+}
 
 template <class S>
 cudaError_t launch_interp(const InterpArgs<S>& a0, cudaStream_t s) {
@@ -564,14 +580,31 @@ cudaError_t launch_interp(const InterpArgs<S>& a0, cudaStream_t s) {
     a.tile_rows = a.fp_w = a.fp_h = 0;
     const int64_t nyr = a.L.ny + 2;
     if (!a.frac_i) {
-        const double rx = fabs(a.coords.dlon / a.atmos.dlon), ry = fabs(a.coords.dlat / a.atmos.dlat);
-        const double w = ceil((kInterpTileCols - 1) * rx) + 3;
-        for (int rows = kInterpMaxTileRows; rows >= 1 && !a.tile_rows; rows /= 2) {
-            const double h = ceil((rows - 1) * ry) + 3;
-            if (w <= 4096 && h <= 4096 && 18.0 * w * h * sizeof(S) <= (double)kInterpStageBytes) {
-                a.tile_rows = rows;
-                a.fp_w = (int)w;
-                a.fp_h = (int)h;
+        int w = 0, h = 0;
+        for (int rows = kInterpTileRows; rows >= 1 && !a.tile_rows; rows /= 2)
+            if (interp_footprint(a, rows, w, h)) { a.tile_rows = rows; a.fp_w = w; a.fp_h = h; }
+        if (a.tile_rows == kInterpTileRows) {
+            cudaError_t e = cudaFuncSetAttribute(interp_tile_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)kInterpStageBytes);
+            if (e != cudaSuccess) return e;
+            int dev = 0, sms = 0, per_sm = 0;
+            const int64_t col_tiles = (a.L.nx + 2 + kInterpTileCols - 1) / kInterpTileCols;
+            if (cudaGetDevice(&dev) == cudaSuccess &&
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess) {
+                for (int rows = kInterpTileRows; rows <= kInterpMaxTileRows; rows++) {
+                    if (!interp_footprint(a, rows, w, h)) break;
+                    const size_t bytes = (size_t)18 * w * h * sizeof(S);
+                    if (cudaOccupancyMaxActiveBlocksPerMultiprocessorWithFlags(
+                            &per_sm, interp_tile_kernel<S>, kInterpTileCols, bytes, cudaOccupancyDefault) !=
+                        cudaSuccess) {
+                        (void)cudaGetLastError();
+                        break;
+                    }
+                    if (col_tiles * ((nyr + rows - 1) / rows) <= (int64_t)per_sm * sms) {
+                        a.tile_rows = rows; a.fp_w = w; a.fp_h = h;
+                        break;
+                    }
+                }
             }
         }
     }

@@ -55,6 +55,8 @@ struct SolveOpts {
     float calm_wind;       // adaptive sea-ice solve with an early lane: wind speed below which the
                            // classify pass sends a cell straight to the FP64 replay (0: none)
     int deferred_ice;      // blocks per SM of the sea-ice solve's packed polish and replay passes
+    int cells;             // adaptive pass 1: work-list entries a thread takes in turn (one thread per
+                           // entry: the grid shrinks by this factor) or a lane reserves per fetch
 };
 
 // Warm start of a solve: features written by the classify pass at the work-list
@@ -1029,12 +1031,17 @@ __device__ __forceinline__ void polish_state_load(const ReplayQueue& q, int64_t 
 // queue) and the taking of new cells happen at warp events only, together for the lanes
 // concerned: an event comes when no lane is sweeping, or, with lane refill, when `refill`
 // lanes are done or empty. Schedules:
-//   fetch = false: one work-list entry per thread (the grid covers the list), no refill;
-//   fetch, refill = 32: the resident warps take the next 32 entries (rq.count[kFetchCounter])
+//   fetch = false: so.cells work-list entries per thread (the grid covers the list once the
+//     cells are counted: thread t takes entries t, t + T, ..., T the grid's threads), the next
+//     one when all of the warp's cells are done, no refill;
+//   fetch, refill = 32: the resident warps take the next entries (rq.count[kFetchCounter])
 //     when all their cells are done -- warp fetching;
 //   fetch, refill < 32: a warp takes new entries for its idle lanes as soon as `refill` of
 //     them are idle -- lane refill: a cell that converges early frees its lane for a new
 //     cell instead of holding it until the warp's slowest cell is done.
+//   With fetching, each lane that needs entries reserves so.cells of them with the warp's one
+//   atomic add (a warp of n such lanes advances the counter by n * cells; lane l of them owns
+//   base + l, base + l + n, ...) and takes its reserved entries without another atomic.
 // Every schedule runs the same instructions on a cell (one kernel, one inlined copy of the
 // map), so the outputs do not depend on it. `Cell` is the interface's adapter: load(r,
 // start) reads ring cell r's inputs into `f` and the start state, store(x, iterations)
@@ -1046,8 +1053,12 @@ __device__ __forceinline__ void adaptive_pass1(Cell& cell, const DevIface<float>
     const int lane = threadIdx.x & 31;
     const unsigned total = wl.count[0] + wl.count[1];
     const int refill = fetch ? (so.refill > 0 && so.refill < 32 ? so.refill : 32) : 32;
+    const int cells = so.cells > 1 ? so.cells : 1;
+    int taken = 0;                  // without fetching: entries this thread has taken
+    unsigned rnext = 0, rstep = 0;  // with fetching: the lane's next reserved entry and its stride
+    int rleft = 0;                  // and how many reserved entries are left
     Sweep<SKIN, true> sw;
-    bool have = false, pending = false, alive = true, first = true;
+    bool have = false, pending = false, alive = true;
     int outcome = SWEEP_CONTINUE;
 #pragma unroll 1
     for (;;) {
@@ -1071,24 +1082,36 @@ __device__ __forceinline__ void adaptive_pass1(Cell& cell, const DevIface<float>
             int64_t w = -1;
             if (fetch) {
                 const bool need = alive && !have;
-                const unsigned nb = __ballot_sync(0xffffffffu, need);
+                const unsigned nb = __ballot_sync(0xffffffffu, need && rleft == 0);
                 if (nb) {
                     const int leader = __ffs(nb) - 1;
+                    const unsigned n = (unsigned)__popc(nb);
                     unsigned base = 0;
-                    if (lane == leader) base = atomicAdd(&rq.count[kFetchCounter], (unsigned)__popc(nb));
+                    if (lane == leader) base = atomicAdd(&rq.count[kFetchCounter], n * (unsigned)cells);
                     base = __shfl_sync(0xffffffffu, base, leader);
-                    if (need) {
-                        const unsigned pos = base + __popc(nb & ((1u << lane) - 1u));
-                        if (pos < total) w = pos;
-                        else alive = false;
+                    if (need && rleft == 0) {
+                        rnext = base + (unsigned)__popc(nb & ((1u << lane) - 1u));
+                        rstep = n;
+                        rleft = cells;
                     }
                 }
-            } else if (first) {
-                const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-                w = t < (int64_t)total ? t : -1;
-                alive = false;
+                if (need) {   // a reserved entry is at hand
+                    const unsigned pos = rnext;
+                    rnext += rstep;
+                    rleft--;
+                    if (pos < total) w = pos;
+                    else {      // the later reserved entries lie beyond the list too
+                        alive = false;
+                        rleft = 0;
+                    }
+                }
+            } else if (!have && taken < cells) {
+                const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x +
+                                  (int64_t)taken * gridDim.x * blockDim.x;
+                taken++;
+                if (t < (int64_t)total) w = t;
+                if (w < 0 || taken == cells) alive = false;
             }
-            first = false;
             if (w >= 0) {
                 float xw[3], start[4];
                 const float* warm = mlp::guess_at(guess, worklist_slot(wl, 0, w), xw);
@@ -1109,10 +1132,14 @@ __device__ __forceinline__ void adaptive_pass1(Cell& cell, const DevIface<float>
 }
 
 // Grid of a pass-1 launch: with warp fetching, the blocks that can be resident at
-// once (at most the one-thread-per-entry grid); otherwise that grid unchanged.
+// once (at most the one-thread-per-entry grid); otherwise that grid, divided by the
+// cells each thread takes (adaptive pass 1).
 template <class K>
-inline dim3 pass1_grid(K kernel, dim3 grid, int threads, int sms, bool fetch) {
-    if (!fetch) return grid;
+inline dim3 pass1_grid(K kernel, dim3 grid, int threads, int sms, bool fetch, int cells = 1) {
+    if (!fetch) {
+        if (cells > 1) grid.x = (grid.x + (unsigned)cells - 1) / (unsigned)cells;
+        return grid;
+    }
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess || per_sm < 1) {
         (void)cudaGetLastError();

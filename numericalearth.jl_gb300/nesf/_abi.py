@@ -292,13 +292,13 @@ class IntegralFields(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("solve_block", i32), ("deferred_per_sm", i32), ("infer_per_sm", i32), ("two_lanes", i32),
                 ("io_overlap", i32), ("pass1_fetch", i32), ("refill_lanes", i32), ("early_ocean_classify", i32),
-                ("ice_deferred_per_sm", i32), ("step_ms", d)]
+                ("ice_deferred_per_sm", i32), ("cells_per_thread", i32), ("step_ms", d)]
 
 
 TUNING_FIELDS = ("solve_block", "deferred_per_sm", "infer_per_sm", "two_lanes", "io_overlap", "pass1_fetch",
-                 "refill_lanes", "early_ocean_classify", "ice_deferred_per_sm")
+                 "refill_lanes", "early_ocean_classify", "ice_deferred_per_sm", "cells_per_thread")
 
-TUNING_VERSION = 1
+TUNING_VERSION = 2
 
 
 class TuningKey(C.Structure):

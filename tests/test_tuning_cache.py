@@ -15,7 +15,7 @@ from nesf import _abi as A
 from nesf import _lib, api
 
 TUNING = dict(solve_block=96, deferred_per_sm=8, infer_per_sm=2, two_lanes=1, io_overlap=0, pass1_fetch=3,
-              refill_lanes=8, early_ocean_classify=1, ice_deferred_per_sm=2, step_ms=7.125)
+              refill_lanes=8, early_ocean_classify=1, ice_deferred_per_sm=2, cells_per_thread=2, step_ms=7.125)
 
 
 def key(**kw):
@@ -48,13 +48,13 @@ def test_byte_layout(tmp_path):
     b = path.read_bytes()
     assert b[:8] == b"NESFTUNE"
     version, key_bytes, fields, count = struct.unpack_from("<4I", b, 8)
-    assert (version, key_bytes, fields, count) == (A.TUNING_VERSION, 108, 9, 1)
-    assert len(b) == 24 + 108 + 9 * 4 + 8
+    assert (version, key_bytes, fields, count) == (A.TUNING_VERSION, 108, 10, 1)
+    assert len(b) == 24 + 108 + 10 * 4 + 8
     rec = b[24:]
     assert rec[:64] == b"NVIDIA GB300".ljust(64, b"\0")
     assert struct.unpack_from("<11i", rec, 64) == (152, 103, 2880, 1280, 3, 3, 1, 2, 1, 31, 0)
-    assert struct.unpack_from("<9i", rec, 108) == tuple(TUNING[k] for k in A.TUNING_FIELDS)
-    assert struct.unpack_from("<d", rec, 144)[0] == TUNING["step_ms"]
+    assert struct.unpack_from("<10i", rec, 108) == tuple(TUNING[k] for k in A.TUNING_FIELDS)
+    assert struct.unpack_from("<d", rec, 148)[0] == TUNING["step_ms"]
 
 
 def test_stale_version_reads_empty_and_is_rewritten(tmp_path):
