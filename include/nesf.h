@@ -684,6 +684,20 @@ int nesf_apply_air_land_radiative_fluxes(const nesf_land_radiation_params* param
  * integral, written on `stream`. */
 int nesf_area_integrals(nesf_context* ctx, const nesf_integral_fields* fields, double* result, void* stream);
 
+/* ------------------------------------------------------ double-float check
+ * The adaptive solver's FP64 replays of the cells its FP32 sweep does not keep run in
+ * double-float arithmetic (a value as the unevaluated sum of two FP32 numbers, 48
+ * significant bits) on the FP32 pipes: this GPU issues one FP64 warp instruction per
+ * ~64 cycles per SM sub-partition. This entry point checks that arithmetic: out[i] =
+ * op(x[i], y[i]) (y only for the binary operations) with the arguments rounded to
+ * double-float and the result widened to FP64; x, y, out device arrays of n doubles,
+ * launched on `stream` (not synchronised). No counterpart in the reference. */
+enum {
+    NESF_DF_ADD = 0, NESF_DF_SUB = 1, NESF_DF_MUL = 2, NESF_DF_DIV = 3, NESF_DF_SQRT = 4, NESF_DF_CBRT = 5,
+    NESF_DF_EXP = 6, NESF_DF_LOG = 7, NESF_DF_POW = 8, NESF_DF_ATAN = 9
+};
+int nesf_double_float_check(const double* x, const double* y, double* out, int64_t n, int32_t op, void* stream);
+
 /* ------------------------------------------------------ tensor-core check
  * Self-check of the tcgen05 GEMM building blocks of the warm-start network in the
  * three operand arrangements it uses (BF16 in, FP32 out; a, b, d device memory,

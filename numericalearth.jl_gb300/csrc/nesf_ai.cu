@@ -10,25 +10,27 @@
 
 namespace nesf {
 
-template <class S>
-__device__ __forceinline__ void ai_load(const DevIface<double>& P, const AIArgs<S>& a, int64_t k,
-                                        CellConst<double>& c, double& aleph, double& Ts0, bool& land) {
-    c.ua = ld(a.ua, k); c.va = ld(a.va, k); c.Ta = ld(a.Ta, k); c.pa = ld(a.pa, k); c.qa = ld(a.qa, k);
-    c.Ti = ld(a.To, k) + P.off_int;      // ocean below the ice (atmosphere_sea_ice_fluxes.jl:92-94)
-    c.Si = ld(a.So, k);
-    c.ui = 0; c.vi = 0;                  // sea-ice velocities are not used (:97-98)
-    c.hi = ld(a.hi, k);
-    c.hs = ldz(a.hs, k);
-    c.hc = ld(a.hc, k);
+// R: double (the reference's FP64 iteration) or df (the adaptive solver's replays).
+template <class S, class R>
+__device__ __forceinline__ void ai_load(const DevIface<R>& P, const AIArgs<S>& a, int64_t k,
+                                        CellConst<R>& c, R& aleph, R& Ts0, bool& land) {
+    c.ua = ldr<R>(a.ua, k); c.va = ldr<R>(a.va, k); c.Ta = ldr<R>(a.Ta, k); c.pa = ldr<R>(a.pa, k);
+    c.qa = ldr<R>(a.qa, k);
+    c.Ti = ldr<R>(a.To, k) + P.off_int;   // ocean below the ice (atmosphere_sea_ice_fluxes.jl:92-94)
+    c.Si = ldr<R>(a.So, k);
+    c.ui = R(0); c.vi = R(0);            // sea-ice velocities are not used (:97-98)
+    c.hi = ldr<R>(a.hi, k);
+    c.hs = ldzr<R>(a.hs, k);
+    c.hc = ldr<R>(a.hc, k);
     c.Rth = conductive_resistance(P, c.hs, c.hi);
-    aleph = ld(a.aleph, k);
-    Ts0 = ld(a.Ts, k) + P.off_ifc;
-    c.sw = ldz(a.sw, k);
-    c.lw = ldz(a.lw, k);
-    c.kappa = -1.0;
+    aleph = ldr<R>(a.aleph, k);
+    Ts0 = ldr<R>(a.Ts, k) + P.off_ifc;
+    c.sw = ldzr<R>(a.sw, k);
+    c.lw = ldzr<R>(a.lw, k);
+    c.kappa = R(-1.0);
     land = a.inactive ? a.inactive[k] != 0 : false;
     if (P.vel_form == NESF_WIND_VELOCITY) { c.du = c.ua; c.dv = c.va; }
-    else { c.du = c.ua - 0.0; c.dv = c.va - 0.0; }
+    else { c.du = c.ua - R(0.0); c.dv = c.va - R(0.0); }
     c.dU2 = c.du * c.du + c.dv * c.dv;
     c.tha = surface_atmosphere_temperature(P, c.Ta, c.qa);
     c.rho_a = air_density(P, c.Ta, c.pa, c.qa);
@@ -37,15 +39,14 @@ __device__ __forceinline__ void ai_load(const DevIface<double>& P, const AIArgs<
 }
 
 // The flux epilogue (atmosphere_sea_ice_fluxes.jl:154-184).
-template <class S>
-__device__ __forceinline__ void ai_store(const DevIface<double>& P, const AIArgs<S>& a, int64_t k,
-                                         const CellConst<double>& c, double us, double ts, double qst, double Ts,
-                                         int iters) {
-    double du = c.du, dv = c.dv;
-    double dU = sqrt(du * du + dv * dv);
-    double tx = dU == 0 ? 0.0 : -(us * us) * du / dU;
-    double ty = dU == 0 ? 0.0 : -(us * us) * dv / dU;
-    double rho = c.rho_a, cp = c.cp_a, Li = c.L_s;
+template <class S, class R>
+__device__ __forceinline__ void ai_store(const DevIface<R>& P, const AIArgs<S>& a, int64_t k,
+                                         const CellConst<R>& c, R us, R ts, R qst, R Ts, int iters) {
+    R du = c.du, dv = c.dv;
+    R dU = M<R>::sqrt(du * du + dv * dv);
+    R tx = dU == R(0) ? R(0) : -(us * us) * du / dU;
+    R ty = dU == R(0) ? R(0) : -(us * us) * dv / dU;
+    R rho = c.rho_a, cp = c.cp_a, Li = c.L_s;
     st(a.Qv, k, -rho * us * qst * Li);
     st(a.QT, k, -rho * cp * us * ts);
     st(a.Jv, k, -rho * us * qst);
@@ -101,15 +102,14 @@ __device__ __forceinline__ void ai_store_fast(const DevIface<double>& P, const A
     if (a.iters) a.iters[k] = iters;
 }
 
-template <bool SKIN, bool PAIR = false>
-__device__ __forceinline__ int ai_plain(const DevIface<double>& P, const CellConst<double>& c, double Ts0,
-                                        double& us, double& ts, double& qst, double& Ts, bool& nonconv,
-                                        LanePair lp = LanePair{0u, 0}) {
-    double qs0 = surface_specific_humidity(P, c.pa, Ts0);
-    SurfaceConst<double> s;
+template <bool SKIN, bool PAIR = false, class R = double>
+__device__ __forceinline__ int ai_plain(const DevIface<R>& P, const CellConst<R>& c, R Ts0, R& us, R& ts, R& qst,
+                                        R& Ts, bool& nonconv, LanePair lp = LanePair{0u, 0}) {
+    R qs0 = surface_specific_humidity(P, c.pa, Ts0);
+    SurfaceConst<R> s;
     surface_const(P, c, Ts0, qs0, s);
-    us = ts = qst = 1e-4;   // initial guess (atmosphere_sea_ice_fluxes.jl:127)
-    int it = solve_plain<SKIN, false, PAIR>(P, c, s, us, ts, qst, nonconv, lp);
+    us = ts = qst = R(1e-4);   // initial guess (atmosphere_sea_ice_fluxes.jl:127)
+    int it = solve_plain<SKIN, false, PAIR, R>(P, c, s, us, ts, qst, nonconv, lp);
     Ts = s.Ts;
     return it;
 }
@@ -329,9 +329,12 @@ __global__ void __launch_bounds__(128, NESF_ADAPTIVE_MIN_BLOCKS) ai_adaptive_ker
 // 1's FP32 sweep + FP64 Newton polish; those that need it go on to the replay. The
 // initial interface temperature is still in a.Ts: pass 1 did not write these cells.
 // STATE: pass 1 left each entry's sweep state (rq.pstate; with a skin temperature).
-template <class S, bool SKIN, bool STATE>
+// R: the Newton steps' arithmetic, with the parameters Pr (double, the drop-in's FP64; the
+// double-float instantiation measured slower than FP64 on these throughput passes).
+template <class S, bool SKIN, bool STATE, class R = double>
 __global__ void __launch_bounds__(128) ai_polish_kernel(AIArgs<S> a, DevIface<double> P, DevIface<float> P32,
-                                                        SolveOpts so, ReplayQueue rq, int rpart, DevStats* stats) {
+                                                        DevIface<R> Pr, SolveOpts so, ReplayQueue rq, int rpart,
+                                                        DevStats* stats) {
     const int nxr = a.L.nx + 2;
     const unsigned n = rq.count[1];
     for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n && (int64_t)q < rq.capacity;
@@ -358,16 +361,16 @@ __global__ void __launch_bounds__(128) ai_polish_kernel(AIArgs<S> a, DevIface<do
             outcome = sweep_fp32<SKIN, false, true>(P32, f.c, f.s, f.anc, x, so, f32it, reason, J, rho, nullptr,
                                                     nullptr);
         }
-        CellConst<double> c;
-        SurfaceConst<double> s{};
-        double us = 0, ts = 0, qst = 0;
+        CellConst<R> c;
+        SurfaceConst<R> s{};
+        R us = R(0), ts = R(0), qst = R(0);
         if (outcome != FAST_REPLAY) {
-            double aleph, Ts0;
+            R aleph, Ts0;
             bool land;
-            ai_load(P, a, k, c, aleph, Ts0, land);
+            ai_load(Pr, a, k, c, aleph, Ts0, land);
             if (SKIN) s.Ts = Ts0;
-            else surface_const(P, c, Ts0, surface_specific_humidity(P, c.pa, Ts0), s);
-            outcome = newton_fp64<SKIN>(P, c, s, x, J, rho, so, us, ts, qst, f64it, reason);
+            else surface_const(Pr, c, Ts0, surface_specific_humidity(Pr, c.pa, Ts0), s);
+            outcome = newton_fp64<SKIN, R>(Pr, c, s, x, J, rho, so, us, ts, qst, f64it, reason);
         }
         replay_push(rq, outcome == FAST_REPLAY, id, rpart);
         if (outcome == FAST_REPLAY) {
@@ -377,7 +380,7 @@ __global__ void __launch_bounds__(128) ai_polish_kernel(AIArgs<S> a, DevIface<do
             }
             continue;
         }
-        ai_store(P, a, k, c, us, ts, qst, s.Ts, f32it + f64it);
+        ai_store(Pr, a, k, c, us, ts, qst, s.Ts, f32it + f64it);
         if (stats) stats_add(stats, false, true, f32it + f64it, false, true, f64it, false, false);
     }
 }
@@ -385,8 +388,8 @@ __global__ void __launch_bounds__(128) ai_polish_kernel(AIArgs<S> a, DevIface<do
 // Pass 2: the queued cells, packed, through the reference's FP64 iteration, two lanes per
 // cell (LanePair: the profiles' stability functions and logarithms split between them). The
 // initial interface temperature is still in a.Ts: pass 1 did not write these cells.
-template <class S>
-__global__ void __launch_bounds__(128) ai_replay_kernel(AIArgs<S> a, DevIface<double> P, ReplayQueue rq, int part,
+template <class S, class R = double>
+__global__ void __launch_bounds__(128) ai_replay_kernel(AIArgs<S> a, DevIface<R> P, ReplayQueue rq, int part,
                                                         DevStats* stats) {
     const int nxr = a.L.nx + 2;
     const unsigned n = rq.count[part];
@@ -396,14 +399,15 @@ __global__ void __launch_bounds__(128) ai_replay_kernel(AIArgs<S> a, DevIface<do
         int64_t r = rq.idx[(int64_t)part * rq.capacity + q];
         int i = (int)(r % nxr), j = (int)(r / nxr);
         int64_t k = a.L.at(i, j);
-        CellConst<double> c;
-        double aleph, Ts0;
+        CellConst<R> c;
+        R aleph, Ts0;
         bool land;
         ai_load(P, a, k, c, aleph, Ts0, land);
-        double us, ts, qst, Ts;
+        R us, ts, qst, Ts;
         bool nonconv;
-        int it = P.temp_form != NESF_BULK_TEMPERATURE ? ai_plain<true, true>(P, c, Ts0, us, ts, qst, Ts, nonconv, lp)
-                                                      : ai_plain<false, true>(P, c, Ts0, us, ts, qst, Ts, nonconv, lp);
+        int it = P.temp_form != NESF_BULK_TEMPERATURE
+                     ? ai_plain<true, true, R>(P, c, Ts0, us, ts, qst, Ts, nonconv, lp)
+                     : ai_plain<false, true, R>(P, c, Ts0, us, ts, qst, Ts, nonconv, lp);
         const bool mine = lp.half == 0;   // lane 0 of the pair stores and counts
         if (mine) ai_store(P, a, k, c, us, ts, qst, Ts, it);
         if (stats) stats_add(stats, false, mine, it, mine && nonconv, false, mine ? it : 0, false, false);
@@ -418,6 +422,12 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     const int64_t ring = (int64_t)(a.L.nx + 2) * (a.L.ny + 2);
     const int block = so.block;   // <= 128: the kernels are compiled with __launch_bounds__(128)
     dim3 grid((unsigned)((ring + block - 1) / block));
+    // the replays in double-float arithmetic when the caller provides the parameters (so.pdf),
+    // else in FP64
+    auto ai_replay = [&](unsigned g, cudaStream_t st, int part) {
+        if (so.pdf) (void)launch_ai_replay_df(a, *so.pdf, rq, part, stats, g, st);
+        else ai_replay_kernel<S><<<g, 128, 0, st>>>(a, P64, rq, part, stats);
+    };
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -443,7 +453,7 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     if (early_lane) {
         if ((e = cudaEventRecord(early->fork, stream)) != cudaSuccess) return e;
         if ((e = cudaStreamWaitEvent(early->stream, early->fork, 0)) != cudaSuccess) return e;
-        ai_replay_kernel<S><<<(unsigned)(sms * so.deferred_ice), 128, 0, early->stream>>>(a, P64, rq, 3, stats);
+        ai_replay((unsigned)(sms * so.deferred_ice), early->stream, 3);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         trace_mark(so.tracer, "ai_calm_replay", early->stream);
     }
@@ -482,7 +492,7 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     if (e != cudaSuccess || prec == NESF_PLAIN_F64) return e;
     const unsigned g2 = (unsigned)(sms * so.deferred_ice);
     if (!adaptive) {
-        ai_replay_kernel<S><<<g2, 128, 0, stream>>>(a, P64, rq, 0, stats);
+        ai_replay(g2, stream, 0);
         trace_mark(so.tracer, "ai_replay", stream);
         return cudaGetLastError();
     }
@@ -494,17 +504,17 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
         if ((e = cudaStreamWaitEvent(tail->stream, tail->fork, 0)) != cudaSuccess) return e;
         rs = tail->stream;
     }
-    ai_replay_kernel<S><<<g2, 128, 0, rs>>>(a, P64, rq, 0, stats);
+    ai_replay(g2, rs, 0);
     trace_mark(so.tracer, "ai_replay", rs);
     if (calm && !early_lane) {
-        ai_replay_kernel<S><<<g2, 128, 0, rs>>>(a, P64, rq, 3, stats);
+        ai_replay(g2, rs, 3);
         trace_mark(so.tracer, "ai_calm_replay", rs);
     }
-    if (skin && rq.pstate) ai_polish_kernel<S, true, true><<<g2, 128, 0, stream>>>(a, P64, P32, so, rq, 2, stats);
-    else if (skin) ai_polish_kernel<S, true, false><<<g2, 128, 0, stream>>>(a, P64, P32, so, rq, 2, stats);
-    else ai_polish_kernel<S, false, false><<<g2, 128, 0, stream>>>(a, P64, P32, so, rq, 2, stats);
+    if (skin && rq.pstate) ai_polish_kernel<S, true, true><<<g2, 128, 0, stream>>>(a, P64, P32, P64, so, rq, 2, stats);
+    else if (skin) ai_polish_kernel<S, true, false><<<g2, 128, 0, stream>>>(a, P64, P32, P64, so, rq, 2, stats);
+    else ai_polish_kernel<S, false, false><<<g2, 128, 0, stream>>>(a, P64, P32, P64, so, rq, 2, stats);
     trace_mark(so.tracer, "ai_polish", stream);
-    ai_replay_kernel<S><<<g2, 128, 0, stream>>>(a, P64, rq, 2, stats);
+    ai_replay(g2, stream, 2);
     trace_mark(so.tracer, "ai_polish_replay", stream);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (rs != stream) {
@@ -518,8 +528,27 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     return cudaSuccess;
 }
 
-// The build compiles this file once per storage type (NESF_STORAGE = 64, then 32), so the
-// two halves of the kernel instantiations compile in parallel; undefined builds both.
+// The build compiles this file once per storage type (NESF_STORAGE = 64, then 32) and per
+// part (NESF_DF_PART = 0: every kernel but the double-float replay, 1: that one, whose
+// inlined arithmetic takes the compiler longest), so that the parts compile in parallel;
+// undefined builds everything.
+#if !defined(NESF_DF_PART) || NESF_DF_PART == 1
+#if !defined(NESF_STORAGE) || NESF_STORAGE == 64
+cudaError_t launch_ai_replay_df(const AIArgs<double>& a, const DevIface<df>& P, const ReplayQueue& rq, int part,
+                                DevStats* stats, unsigned grid, cudaStream_t s) {
+    ai_replay_kernel<double, df><<<grid, 128, 0, s>>>(a, P, rq, part, stats);
+    return cudaGetLastError();
+}
+#endif
+#if !defined(NESF_STORAGE) || NESF_STORAGE == 32
+cudaError_t launch_ai_replay_df(const AIArgs<float>& a, const DevIface<df>& P, const ReplayQueue& rq, int part,
+                                DevStats* stats, unsigned grid, cudaStream_t s) {
+    ai_replay_kernel<float, df><<<grid, 128, 0, s>>>(a, P, rq, part, stats);
+    return cudaGetLastError();
+}
+#endif
+#endif
+#if !defined(NESF_DF_PART) || NESF_DF_PART == 0
 #if !defined(NESF_STORAGE) || NESF_STORAGE == 64
 cudaError_t launch_ai(const AIArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
@@ -533,6 +562,7 @@ cudaError_t launch_ai(const AIArgs<float>& a, const DevIface<double>& P64, const
                       cudaStream_t stream, cudaEvent_t after_solve, const TailLane* tail, const TailLane* early) {
     return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream, after_solve, tail, early);
 }
+#endif
 #endif
 
 }  // namespace nesf

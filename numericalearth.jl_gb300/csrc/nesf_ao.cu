@@ -13,19 +13,21 @@
 namespace nesf {
 
 // assemble_interior_state + the atmosphere reads (atmosphere_ocean_fluxes.jl:62-71, 97-128)
-template <class S>
-__device__ __forceinline__ void ao_load(const DevIface<double>& P, const AOArgs<S>& a, int64_t k, bool skin,
-                                        CellConst<double>& c, bool& land) {
-    c.ua = ld(a.ua, k); c.va = ld(a.va, k); c.Ta = ld(a.Ta, k); c.pa = ld(a.pa, k); c.qa = ld(a.qa, k);
-    c.ui = (ld(a.uo, k) + ld(a.uo, k + 1)) / 2;          // centre average of the x-face velocity
-    c.vi = (ld(a.vo, k) + ld(a.vo, k + a.L.sj)) / 2;     // centre average of the y-face velocity
-    c.Ti = ld(a.To, k) + P.off_int;
-    c.Si = ld(a.So, k);
-    c.hi = c.hs = c.hc = 0;
-    c.Rth = 0;
-    c.sw = ldz(a.sw, k);
-    c.lw = ldz(a.lw, k);
-    c.kappa = a.kappa ? ld(a.kappa, k) : -1.0;
+// R: double (the reference's FP64 iteration) or df (the adaptive solver's replays).
+template <class S, class R>
+__device__ __forceinline__ void ao_load(const DevIface<R>& P, const AOArgs<S>& a, int64_t k, bool skin,
+                                        CellConst<R>& c, bool& land) {
+    c.ua = ldr<R>(a.ua, k); c.va = ldr<R>(a.va, k); c.Ta = ldr<R>(a.Ta, k); c.pa = ldr<R>(a.pa, k);
+    c.qa = ldr<R>(a.qa, k);
+    c.ui = (ldr<R>(a.uo, k) + ldr<R>(a.uo, k + 1)) / R(2);         // centre average of the x-face velocity
+    c.vi = (ldr<R>(a.vo, k) + ldr<R>(a.vo, k + a.L.sj)) / R(2);    // centre average of the y-face velocity
+    c.Ti = ldr<R>(a.To, k) + P.off_int;
+    c.Si = ldr<R>(a.So, k);
+    c.hi = c.hs = c.hc = R(0);
+    c.Rth = R(0);
+    c.sw = ldzr<R>(a.sw, k);
+    c.lw = ldzr<R>(a.lw, k);
+    c.kappa = a.kappa ? ldr<R>(a.kappa, k) : R(-1.0);
     land = a.inactive ? a.inactive[k] != 0 : false;
     if (P.vel_form == NESF_WIND_VELOCITY) { c.du = c.ua; c.dv = c.va; }
     else { c.du = c.ua - c.ui; c.dv = c.va - c.vi; }
@@ -36,30 +38,29 @@ __device__ __forceinline__ void ao_load(const DevIface<double>& P, const AOArgs<
         c.cp_a = cp_m(P, c.qa);
         c.L_s = latent_heat_sublim(P, c.Ta);
     } else {
-        c.rho_a = c.cp_a = c.L_s = 0;
+        c.rho_a = c.cp_a = c.L_s = R(0);
     }
 }
 
 // The flux epilogue (atmosphere_ocean_fluxes.jl:157-196).
-template <class S>
-__device__ __forceinline__ void ao_store(const DevIface<double>& P, const AOArgs<S>& a, int64_t k,
-                                         const CellConst<double>& c, bool land, double us, double ts, double qst,
-                                         double Ts, int iters) {
-    double ui = c.ui, vi = c.vi;
+template <class S, class R>
+__device__ __forceinline__ void ao_store(const DevIface<R>& P, const AOArgs<S>& a, int64_t k,
+                                         const CellConst<R>& c, bool land, R us, R ts, R qst, R Ts, int iters) {
+    R ui = c.ui, vi = c.vi;
     if (land) {   // zero_interface_state (interface_states.jl:800-803)
-        us = ts = qst = 0;
-        Ts = 273.15;
-        ui = vi = 0;
+        us = ts = qst = R(0);
+        Ts = R(273.15);
+        ui = vi = R(0);
     }
-    double du, dv;
+    R du, dv;
     if (P.vel_form == NESF_WIND_VELOCITY) { du = c.ua; dv = c.va; }
     else { du = c.ua - ui; dv = c.va - vi; }
-    double dU = sqrt(du * du + dv * dv);
-    double tx = dU == 0 ? 0.0 : -(us * us) * du / dU;
-    double ty = dU == 0 ? 0.0 : -(us * us) * dv / dU;
-    double rho = air_density(P, c.Ta, c.pa, c.qa);
-    double cp = cp_m(P, c.qa);
-    double Lv = latent_heat_vapor(P, c.Ta);
+    R dU = M<R>::sqrt(du * du + dv * dv);
+    R tx = dU == R(0) ? R(0) : -(us * us) * du / dU;
+    R ty = dU == R(0) ? R(0) : -(us * us) * dv / dU;
+    R rho = air_density(P, c.Ta, c.pa, c.qa);
+    R cp = cp_m(P, c.qa);
+    R Lv = latent_heat_vapor(P, c.Ta);
     st(a.Qv, k, -rho * Lv * us * qst);
     st(a.QT, k, -rho * cp * us * ts);
     st(a.Jv, k, -rho * us * qst);
@@ -117,7 +118,7 @@ __device__ __forceinline__ void ao_store_land(const DevIface<double>& P, const D
         CellConst<double> c;
         bool land;
         ao_load(P, a, k, false, c, land);
-        ao_store(P, a, k, c, true, 0.0, 0.0, 0.0, 273.15, iters);
+        ao_store<S, double>(P, a, k, c, true, 0.0, 0.0, 0.0, 273.15, iters);
         return;
     }
     const double ua = ld(a.ua, k), va = ld(a.va, k), Ta = ld(a.Ta, k), pa = ld(a.pa, k), qa = ld(a.qa, k);
@@ -133,7 +134,7 @@ __device__ __forceinline__ void ao_store_land(const DevIface<double>& P, const D
         CellConst<double> c;
         bool land;
         ao_load(P, a, k, false, c, land);
-        ao_store(P, a, k, c, true, 0.0, 0.0, 0.0, 273.15, iters);
+        ao_store<S, double>(P, a, k, c, true, 0.0, 0.0, 0.0, 273.15, iters);
         return;
     }
     const double r = copysign(1.0, pa) * copysign(1.0, den);   // the sign of the air density
@@ -404,9 +405,12 @@ __global__ void __launch_bounds__(128, NESF_ADAPTIVE_MIN_BLOCKS) ao_adaptive_ker
 
 // Pass 1b (ADAPTIVE): the cells whose FP32 result was not kept, packed, through
 // pass 1's FP32 sweep + FP64 Newton polish; those that need it go on to the replay.
-template <class S, bool SKIN>
+// R: the Newton steps' arithmetic, with the parameters Pr (or per member P64s): double, the
+// drop-in's FP64 (the double-float instantiation measured slower than FP64 on these
+// throughput passes).
+template <class S, bool SKIN, class R = double>
 __global__ void __launch_bounds__(128) ao_polish_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
-                                                        const DevIface<double>* __restrict__ P64s,
+                                                        DevIface<R> Pr, const DevIface<double>* __restrict__ P64s,
                                                         const DevIface<float>* __restrict__ P32s, SolveOpts so,
                                                         ReplayQueue rq, int rpart, DevStats* stats) {
     const int nxr = a.L.nx + 2;
@@ -430,15 +434,16 @@ __global__ void __launch_bounds__(128) ao_polish_kernel(AOArgs<S> a, DevIface<do
         int f32it = 0, f64it = 0, reason = -1;
         int outcome = sweep_fp32<SKIN, false, true>(Pf, f.c, f.s, f.anc, x, so, f32it, reason, J, rho, nullptr,
                                                     nullptr);
-        CellConst<double> c;
-        SurfaceConst<double> s{};
-        double us = 0, ts = 0, qst = 0;
+        const DevIface<R>& PR = member_params(Pr, P64s, m);
+        CellConst<R> c;
+        SurfaceConst<R> s{};
+        R us = R(0), ts = R(0), qst = R(0);
         if (outcome != FAST_REPLAY) {
             bool land;
-            ao_load(P, a, k, SKIN, c, land);
+            ao_load(PR, a, k, SKIN, c, land);
             if (SKIN) s.Ts = c.Ti;
-            else surface_const(P, c, c.Ti, surface_specific_humidity(P, c.pa, c.Ti), s);
-            outcome = newton_fp64<SKIN>(P, c, s, x, J, rho, so, us, ts, qst, f64it, reason);
+            else surface_const(PR, c, c.Ti, surface_specific_humidity(PR, c.pa, c.Ti), s);
+            outcome = newton_fp64<SKIN, R>(PR, c, s, x, J, rho, so, us, ts, qst, f64it, reason);
         }
         replay_push(rq, outcome == FAST_REPLAY, id, rpart);
         if (outcome == FAST_REPLAY) {
@@ -448,16 +453,17 @@ __global__ void __launch_bounds__(128) ao_polish_kernel(AOArgs<S> a, DevIface<do
             }
             continue;
         }
-        ao_store(P, a, k, c, false, us, ts, qst, s.Ts, f32it + f64it);
+        ao_store(PR, a, k, c, false, us, ts, qst, s.Ts, f32it + f64it);
         if (stats) stats_add(stats, false, true, f32it + f64it, false, true, f64it, false, false);
     }
 }
 
 // Pass 2: the cells queued in `part`, packed, through the reference's FP64 iteration, two
 // lanes per cell (LanePair: the profiles' stability functions and logarithms split between them).
-template <class S, bool SKIN>
-__global__ void __launch_bounds__(128) ao_replay_kernel(AOArgs<S> a, DevIface<double> P64,
-                                                        const DevIface<double>* __restrict__ P64s, ReplayQueue rq,
+// R: double, or df for one member (the parameters in Pr; ensembles' members' parameters are FP64).
+template <class S, bool SKIN, class R = double>
+__global__ void __launch_bounds__(128) ao_replay_kernel(AOArgs<S> a, DevIface<R> Pr,
+                                                        const DevIface<R>* __restrict__ Ps, ReplayQueue rq,
                                                         int part, DevStats* stats) {
     const int nxr = a.L.nx + 2;
     const int64_t ring = (int64_t)nxr * (a.L.ny + 2);
@@ -467,18 +473,18 @@ __global__ void __launch_bounds__(128) ao_replay_kernel(AOArgs<S> a, DevIface<do
          q += (gridDim.x * blockDim.x) >> 1) {
         uint32_t id = rq.idx[(int64_t)part * rq.capacity + q];
         int64_t m = (int64_t)id / ring, r = (int64_t)id % ring;
-        const DevIface<double>& P = P64s ? P64s[m] : P64;
+        const DevIface<R>& P = Ps ? Ps[m] : Pr;
         int i = (int)(r % nxr), j = (int)(r / nxr);
         int64_t k = a.L.at(i, j) + m * a.member_stride;
-        CellConst<double> c;
+        CellConst<R> c;
         bool land;
         ao_load(P, a, k, SKIN, c, land);
-        double us = 1e-4, ts = 1e-4, qst = 1e-4;
-        double qs0 = surface_specific_humidity(P, c.pa, c.Ti);
-        SurfaceConst<double> s;
+        R us = R(1e-4), ts = R(1e-4), qst = R(1e-4);
+        R qs0 = surface_specific_humidity(P, c.pa, c.Ti);
+        SurfaceConst<R> s;
         surface_const(P, c, c.Ti, qs0, s);
         bool nonconv;
-        int it = solve_plain<SKIN, false, true>(P, c, s, us, ts, qst, nonconv, lp);
+        int it = solve_plain<SKIN, false, true, R>(P, c, s, us, ts, qst, nonconv, lp);
         const bool mine = lp.half == 0;   // lane 0 of the pair stores and counts
         if (mine) ao_store(P, a, k, c, false, us, ts, qst, s.Ts, it);
         if (stats) stats_add(stats, false, mine, it, mine && nonconv, false, mine ? it : 0, false, false);
@@ -556,25 +562,34 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
     // replays (part 2) follow it; without, the polish pass's replays join part 0
     const bool split = adaptive && tail && tail->stream;
     cudaStream_t rs = stream;
+    // the replays of one member in double-float arithmetic when the caller provides its
+    // parameters (so.pdf), else in FP64
+    auto replay = [&](cudaStream_t st, int part) {
+        if (so.pdf && !ens) {
+            (void)launch_ao_replay_df(a, *so.pdf, rq, part, skin, stats, g2, st);
+        } else {
+            if (skin) ao_replay_kernel<S, true><<<g2, 128, 0, st>>>(a, P64, pm, rq, part, stats);
+            else ao_replay_kernel<S, false><<<g2, 128, 0, st>>>(a, P64, pm, rq, part, stats);
+        }
+    };
     if (split) {
         if ((e = cudaEventRecord(tail->fork, stream)) != cudaSuccess) return e;
         if ((e = cudaStreamWaitEvent(tail->stream, tail->fork, 0)) != cudaSuccess) return e;
         rs = tail->stream;
-        if (skin) ao_replay_kernel<S, true><<<g2, 128, 0, rs>>>(a, P64, pm, rq, 0, stats);
-        else ao_replay_kernel<S, false><<<g2, 128, 0, rs>>>(a, P64, pm, rq, 0, stats);
+        replay(rs, 0);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         trace_mark(so.tracer, "ao_replay", rs);
     }
     const int rpart = split ? 2 : 0;
     if (adaptive) {
-        if (skin) ao_polish_kernel<S, true><<<g2, 128, 0, stream>>>(a, P64, P32, pm, ens ? P32s : nullptr, so, rq, rpart, stats);
-        else ao_polish_kernel<S, false><<<g2, 128, 0, stream>>>(a, P64, P32, pm, ens ? P32s : nullptr, so, rq, rpart, stats);
-        e = cudaGetLastError();
+        if (skin)
+            ao_polish_kernel<S, true><<<g2, 128, 0, stream>>>(a, P64, P32, P64, pm, ens ? P32s : nullptr, so, rq, rpart, stats);
+        else ao_polish_kernel<S, false><<<g2, 128, 0, stream>>>(a, P64, P32, P64, pm, ens ? P32s : nullptr, so, rq, rpart, stats);
+        if (e == cudaSuccess) e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         trace_mark(so.tracer, "ao_polish", stream);
     }
-    if (skin) ao_replay_kernel<S, true><<<g2, 128, 0, stream>>>(a, P64, pm, rq, rpart, stats);
-    else ao_replay_kernel<S, false><<<g2, 128, 0, stream>>>(a, P64, pm, rq, rpart, stats);
+    replay(stream, rpart);
     trace_mark(so.tracer, split ? "ao_polish_replay" : "ao_replay", stream);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (split) {
@@ -603,8 +618,43 @@ static cudaError_t preload_ao_t() {
     return cudaSuccess;
 }
 
-// The build compiles this file once per storage type (NESF_STORAGE = 64, then 32), so the
-// two halves of the kernel instantiations compile in parallel; undefined builds both.
+// The build compiles this file once per storage type (NESF_STORAGE = 64, then 32) and per
+// part (NESF_DF_PART = 0: every kernel but the double-float replays, 1: those, whose
+// inlined arithmetic takes the compiler longest), so that the parts compile in parallel;
+// undefined builds everything.
+template <class S>
+static cudaError_t launch_ao_replay_df_t(const AOArgs<S>& a, const DevIface<df>& P, const ReplayQueue& rq, int part,
+                                         bool skin, DevStats* stats, unsigned grid, cudaStream_t s) {
+    if (skin) ao_replay_kernel<S, true, df><<<grid, 128, 0, s>>>(a, P, nullptr, rq, part, stats);
+    else ao_replay_kernel<S, false, df><<<grid, 128, 0, s>>>(a, P, nullptr, rq, part, stats);
+    return cudaGetLastError();
+}
+
+// Loads the double-float replays (under lazy module loading), for preload_ao_kernels.
+template <class S>
+static cudaError_t preload_ao_replay_df_t() {
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, (const void*)ao_replay_kernel<S, false, df>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void*)ao_replay_kernel<S, true, df>);
+    return e;
+}
+#if !defined(NESF_DF_PART) || NESF_DF_PART == 1
+#if !defined(NESF_STORAGE) || NESF_STORAGE == 64
+cudaError_t launch_ao_replay_df(const AOArgs<double>& a, const DevIface<df>& P, const ReplayQueue& rq, int part,
+                                bool skin, DevStats* stats, unsigned grid, cudaStream_t s) {
+    return launch_ao_replay_df_t(a, P, rq, part, skin, stats, grid, s);
+}
+cudaError_t preload_ao_replay_df(const AOArgs<double>*) { return preload_ao_replay_df_t<double>(); }
+#endif
+#if !defined(NESF_STORAGE) || NESF_STORAGE == 32
+cudaError_t launch_ao_replay_df(const AOArgs<float>& a, const DevIface<df>& P, const ReplayQueue& rq, int part,
+                                bool skin, DevStats* stats, unsigned grid, cudaStream_t s) {
+    return launch_ao_replay_df_t(a, P, rq, part, skin, stats, grid, s);
+}
+cudaError_t preload_ao_replay_df(const AOArgs<float>*) { return preload_ao_replay_df_t<float>(); }
+#endif
+#endif
+#if !defined(NESF_DF_PART) || NESF_DF_PART == 0
 #if !defined(NESF_STORAGE) || NESF_STORAGE == 64
 cudaError_t launch_ao(const AOArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
@@ -613,7 +663,10 @@ cudaError_t launch_ao(const AOArgs<double>& a, const DevIface<double>& P64, cons
     return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, ws, stats, stream, before_pass1,
                        tail);
 }
-cudaError_t preload_ao_kernels(const AOArgs<double>*) { return preload_ao_t<double>(); }
+cudaError_t preload_ao_kernels(const AOArgs<double>* p) {
+    cudaError_t e = preload_ao_t<double>();
+    return e == cudaSuccess ? preload_ao_replay_df(p) : e;
+}
 #endif
 #if !defined(NESF_STORAGE) || NESF_STORAGE == 32
 cudaError_t launch_ao(const AOArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32,
@@ -623,7 +676,11 @@ cudaError_t launch_ao(const AOArgs<float>& a, const DevIface<double>& P64, const
     return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, ws, stats, stream, before_pass1,
                        tail);
 }
-cudaError_t preload_ao_kernels(const AOArgs<float>*) { return preload_ao_t<float>(); }
+cudaError_t preload_ao_kernels(const AOArgs<float>* p) {
+    cudaError_t e = preload_ao_t<float>();
+    return e == cudaSuccess ? preload_ao_replay_df(p) : e;
+}
+#endif
 #endif
 
 }  // namespace nesf

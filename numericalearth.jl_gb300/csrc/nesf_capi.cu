@@ -807,6 +807,8 @@ static int ocean_fluxes(nesf_context* ctx, const nesf_interface_params* params, 
     if ((r = work_list(ctx, ring, 1, &wl))) return r;
     if ((r = warm_buffers(ctx, o, ring, &ws))) return r;
     SolveOpts so = solve_opts(o, ctx);
+    const DevIface<df> Pdf = make_dev_iface<df>(*params);
+    so.pdf = &Pdf;
     // pass 1's replays beside the polish pass (the tuning's two_lanes)
     TailLane tl{nullptr, nullptr, nullptr};
     if (o.precision == NESF_F32_ADAPTIVE && ctx->tuning.two_lanes) {
@@ -1017,6 +1019,8 @@ static int sea_ice_fluxes(nesf_context* ctx, const nesf_interface_params* params
     if ((r = work_list(ctx, ring, 1, &wl))) return r;
     if ((r = warm_buffers(ctx, o, ring, &ws))) return r;
     SolveOpts so = solve_opts(o, ctx);
+    const DevIface<df> Pdf = make_dev_iface<df>(*params);
+    so.pdf = &Pdf;
     // the replay of pass 1's cells beside the polish pass and the calm cells' replays beside
     // pass 1 (the tuning's two_lanes)
     TailLane tl{nullptr, nullptr, nullptr}, el{nullptr, nullptr, nullptr};
@@ -1331,12 +1335,33 @@ extern "C" int nesf_compute_atmosphere_ocean_fluxes_noalloc(const nesf_interface
     DevIface<float> P32 = make_dev_iface<float>(*params);
     bool skin = params->temperature_formulation != NESF_BULK_TEMPERATURE;
     SolveOpts so = solve_opts(o);
+    const DevIface<df> Pdf = make_dev_iface<df>(*params);
+    so.pdf = &Pdf;
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = f->dtype == NESF_F64
                         ? launch_ao(ao_args<double>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl,
                                     rq, WarmStart{}, nullptr, s)
                         : launch_ao(ao_args<float>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl,
                                     rq, WarmStart{}, nullptr, s);
+    if (e != cudaSuccess) return cuda_fail(e, who);
+    return NESF_OK;
+}
+
+// ------------------------------------------------ double-float check
+namespace nesf {
+cudaError_t launch_df_check(const double* x, const double* y, double* out, int64_t n, int op, cudaStream_t s);
+}
+
+extern "C" int nesf_double_float_check(const double* x, const double* y, double* out, int64_t n, int32_t op,
+                                       void* stream) {
+    const char* who = "nesf_double_float_check";
+    if (op < NESF_DF_ADD || op > NESF_DF_ATAN) return fail(NESF_ERR_ARG, "%s: operation %d", who, op);
+    const bool binary = op == NESF_DF_ADD || op == NESF_DF_SUB || op == NESF_DF_MUL || op == NESF_DF_DIV ||
+                        op == NESF_DF_POW;
+    if (n < 0 || n > ((int64_t)1 << 31)) return fail(NESF_ERR_ARG, "%s: n = %lld", who, (long long)n);
+    if (n > 0 && (!x || !out || (binary && !y))) return fail(NESF_ERR_ARG, "%s: null array", who);
+    if (n == 0) return NESF_OK;
+    cudaError_t e = nesf::launch_df_check(x, binary ? y : nullptr, out, n, op, (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(e, who);
     return NESF_OK;
 }

@@ -1,7 +1,8 @@
 // nesf_device.cuh -- per-cell similarity-theory physics for the interface-flux kernels.
 //
 // Everything here is templated on the compute type R (double for the drop-in
-// FP64 solver and the polish step, float for the FP32 sweep). The formulas
+// FP64 solver, float for the FP32 sweep, df -- double-float, nesf_df.cuh -- for the
+// adaptive solver's deferred passes). The formulas
 // restate NumericalEarth.jl v0.6.2 (paths below are inside that project) and
 // keep its operation order, with three kinds of exception, each moving a value
 // by about an ulp (the FP64 path stays within 1e-12 of the reference): quantities
@@ -14,9 +15,11 @@
 
 #include <cstdint>
 #include <cmath>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #include "../../include/nesf.h"
+#include "nesf_df.cuh"
 
 namespace nesf {
 
@@ -59,6 +62,24 @@ template <> struct M<float> {
     static __device__ __forceinline__ float inf() { return __int_as_float(0x7f800000); }
     static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
     static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+};
+template <> struct M<df> {
+    static __device__ __forceinline__ df log(df x) { return dfx::log(x); }
+    static __device__ __forceinline__ df exp(df x) { return dfx::exp(x); }
+    static __device__ __forceinline__ df pow(df x, df y) { return dfx::pow(x, y); }
+    static __device__ __forceinline__ df atan(df x) { return dfx::atan(x); }
+    static __device__ __forceinline__ df cbrt(df x) { return dfx::cbrt(x); }
+    static __device__ __forceinline__ df sqrt(df x) { return dfx::sqrt(x); }
+    static __device__ __forceinline__ df fmin(df x, df y) {
+        return (isnan(x) || isnan(y)) ? x + y : (x == y ? (signbit(x) ? x : y) : (x < y ? x : y));
+    }
+    static __device__ __forceinline__ df fmax(df x, df y) {
+        return (isnan(x) || isnan(y)) ? x + y : (x == y ? (signbit(x) ? y : x) : (x > y ? x : y));
+    }
+    static __device__ __forceinline__ df fabs(df a) { return signbit(a) ? -a : a; }
+    static __device__ __forceinline__ df inf() { return df(__int_as_float(0x7f800000), 0.0f); }
+    static __device__ __forceinline__ df mul(df a, df b) { return a * b; }
+    static __device__ __forceinline__ df add(df a, df b) { return a + b; }
 };
 
 // --------------------------------------------------------- device parameters
@@ -165,10 +186,10 @@ template <class R> __device__ __forceinline__ R virtual_temperature(const DevIfa
 
 // surface_specific_humidity(::ImpureSaturationSpecificHumidity)
 // (InterfaceComputations/interface_states.jl:55-74); EXP: e_sat from esat_exp, which FP32
-// (classification, network features) always takes.
+// (classification, network features) and double-float (the replays) always take.
 template <class R, bool EXP = false>
 __device__ __forceinline__ R surface_specific_humidity(const DevIface<R>& P, R pa, R Ts) {
-    R pv = P.x * ((EXP || sizeof(R) == 4) ? esat_exp(P, Ts) : esat(P, Ts));
+    R pv = P.x * ((EXP || !std::is_same<R, double>::value) ? esat_exp(P, Ts) : esat(P, Ts));
     pv = M<R>::fmin(pv, R(0.999) * pa);
     return P.einv * pv / (pa - (R(1) - P.einv) * pv);
 }

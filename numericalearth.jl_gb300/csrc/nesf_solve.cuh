@@ -57,6 +57,8 @@ struct SolveOpts {
     int deferred_ice;      // blocks per SM of the sea-ice solve's packed polish and replay passes
     int cells;             // adaptive pass 1: work-list entries a thread takes in turn (one thread per
                            // entry: the grid shrinks by this factor) or a lane reserves per fetch
+    const DevIface<df>* pdf;   // host side: the parameters in double-float, for the deferred passes
+                               // of one member (null: FP64)
 };
 
 // Warm start of a solve: features written by the classify pass at the work-list
@@ -355,12 +357,12 @@ __device__ __forceinline__ bool invert(float (&a)[N][N], float (&inv)[N][N]) {
 }
 
 // The reference's FP64 fixed point from (us, ts, qst) and s64. Returns iterations.
-template <bool SKIN, bool QSKIN = false, bool PAIR = false>
-__device__ __forceinline__ int solve_plain(const DevIface<double>& P64, const CellConst<double>& c64,
-                                           SurfaceConst<double>& s64, double& us, double& ts, double& qst,
+template <bool SKIN, bool QSKIN = false, bool PAIR = false, class R = double>
+__device__ __forceinline__ int solve_plain(const DevIface<R>& P64, const CellConst<R>& c64,
+                                           SurfaceConst<R>& s64, R& us, R& ts, R& qst,
                                            bool& nonconv, LanePair lp = LanePair{0u, 0}) {
-    double drift;
-    int it = fixed_point<double, SKIN, QSKIN, PAIR>(P64, c64, s64, us, ts, qst, P64.maxiter, drift, lp);
+    R drift;
+    int it = fixed_point<R, SKIN, QSKIN, PAIR>(P64, c64, s64, us, ts, qst, P64.maxiter, drift, lp);
     nonconv = P64.stop_kind == NESF_STOP_CONVERGENCE && !(drift < P64.tol);
     return it;
 }
@@ -761,12 +763,12 @@ __device__ __forceinline__ int sweep_fp32(const DevIface<float>& P32, const Cell
 // constants (c64, s64). On FAST_SOLVED the solution is in us, ts, qst and, with a
 // skin temperature, s64.Ts (the interface temperature; the rest of s64 is not
 // updated); FAST_REPLAY (I - J singular) leaves them untouched. `fp64_it` counts
-// FP64 map evaluations.
-template <bool SKIN>
-__device__ __forceinline__ int newton_fp64(const DevIface<double>& P64, const CellConst<double>& c64,
-                                           SurfaceConst<double>& s64, const float (&x)[4],
+// FP64 map evaluations. R: double, or df (the steps in double-float arithmetic).
+template <bool SKIN, class R = double>
+__device__ __forceinline__ int newton_fp64(const DevIface<R>& P64, const CellConst<R>& c64,
+                                           SurfaceConst<R>& s64, const float (&x)[4],
                                            const float (&J)[SKIN ? 4 : 3][SKIN ? 4 : 3], float rho_est,
-                                           const SolveOpts& so, double& us, double& ts, double& qst, int& fp64_it,
+                                           const SolveOpts& so, R& us, R& ts, R& qst, int& fp64_it,
                                            int& reason) {
     constexpr int N = SKIN ? 4 : 3;
     fp64_it = 0;
@@ -785,7 +787,7 @@ __device__ __forceinline__ int newton_fp64(const DevIface<double>& P64, const Ce
             for (int jj = 0; jj < 3; jj++) A3[ii][jj] = (ii == jj ? 1.0f : 0.0f) - J[ii][jj];
         if (!invert<3>(A3, A3i)) { reason = REPLAY_SINGULAR; return FAST_REPLAY; }
     }
-    double xd[4] = {(double)x[0], (double)x[1], (double)x[2], SKIN ? c64.tha + (double)x[3] : 0.0};
+    R xd[4] = {R(x[0]), R(x[1]), R(x[2]), SKIN ? c64.tha + R(x[3]) : R(0.0)};
     // a Newton step with an approximate J shrinks the error by about |dJ| / (1 - rho):
     // slowly contracting cells take more steps, up to polish_steps
     const int want = 1 + (rho_est > 0.5f ? 1 : 0) + (rho_est > 0.8f ? 1 : 0);
@@ -793,9 +795,9 @@ __device__ __forceinline__ int newton_fp64(const DevIface<double>& P64, const Ce
     const int steps = want < cap ? want : cap;
 #pragma unroll 1
     for (int n = 0; n < steps; n++) {
-        double y[4];
+        R y[4];
         bool pinned = false;
-        eval_map<double, SKIN>(P64, c64, s64, xd, y, &pinned);
+        eval_map<R, SKIN>(P64, c64, s64, xd, y, &pinned);
         fp64_it++;
         float r[4];
 #pragma unroll
@@ -815,8 +817,8 @@ __device__ __forceinline__ int newton_fp64(const DevIface<double>& P64, const Ce
                 for (int jj = 0; jj < N; jj++) dl[ii] += Ainv[ii][jj] * r[jj];
         }
 #pragma unroll
-        for (int ii = 0; ii < 3; ii++) xd[ii] += (double)dl[ii];
-        if (SKIN) xd[3] = pinned ? y[3] : xd[3] + (double)dl[3];
+        for (int ii = 0; ii < 3; ii++) xd[ii] += R(dl[ii]);
+        if (SKIN) xd[3] = pinned ? y[3] : xd[3] + R(dl[3]);
     }
     us = xd[0]; ts = xd[1]; qst = xd[2];
     if (SKIN) s64.Ts = xd[3];   // the callers read the interface temperature alone
@@ -1184,6 +1186,26 @@ cudaError_t launch_al(const ALArgs<float>& a, const DevIface<double>& P64, const
 template <class S>
 cudaError_t launch_ao_samples(const AOArgs<S>& a, const DevIface<float>& P32, float* feat, float* targ,
                               cudaStream_t s);
+// The adaptive solvers' replays in double-float arithmetic (one member), compiled apart
+// (NESF_DF_PART 1 of the solve files).
+cudaError_t launch_ai_replay_df(const AIArgs<double>& a, const DevIface<df>& P, const ReplayQueue& rq, int part,
+                                DevStats* stats, unsigned grid, cudaStream_t s);
+cudaError_t launch_ai_replay_df(const AIArgs<float>& a, const DevIface<df>& P, const ReplayQueue& rq, int part,
+                                DevStats* stats, unsigned grid, cudaStream_t s);
+cudaError_t launch_ao_replay_df(const AOArgs<double>& a, const DevIface<df>& P, const ReplayQueue& rq, int part,
+                                bool skin, DevStats* stats, unsigned grid, cudaStream_t s);
+cudaError_t launch_ao_replay_df(const AOArgs<float>& a, const DevIface<df>& P, const ReplayQueue& rq, int part,
+                                bool skin, DevStats* stats, unsigned grid, cudaStream_t s);
+cudaError_t preload_ao_replay_df(const AOArgs<double>*);
+cudaError_t preload_ao_replay_df(const AOArgs<float>*);
+// A solve's parameters in the arithmetic R of its deferred passes: member m's FP64 ones for an
+// ensemble (ps), else p.
+template <class R>
+__device__ __forceinline__ const DevIface<R>& member_params(const DevIface<R>& p, const DevIface<double>* ps,
+                                                            int64_t m) {
+    if constexpr (std::is_same<R, double>::value) return ps ? ps[m] : p;
+    else return p;
+}
 // The warm-start network's inference pass over a work list (nesf_mlp.cu).
 cudaError_t mlp_pass(void* blob, const float* x, const float* t, float* y, int64_t n, const unsigned int* count,
                      int64_t per_member, int grid, bool state, cudaStream_t s);

@@ -60,6 +60,7 @@ SIGNATURES = {
     "nesf_apply_air_land_radiative_fluxes": (C.c_int, [P(A.LandRadiationParams), P(A.LandFluxFields), vp]),
     "nesf_area_integrals": (C.c_int, [vp, P(A.IntegralFields), vp, vp]),
     "nesf_mlp_selftest": (C.c_int, [vp, vp, vp, C.c_int32, vp]),
+    "nesf_double_float_check": (C.c_int, [vp, vp, vp, C.c_int64, C.c_int32, vp]),
     "nesf_mlp_bytes": (C.c_int64, []),
     "nesf_mlp_init": (C.c_int, [vp, C.c_uint64, vp]),
     "nesf_mlp_fit_normalization": (C.c_int, [vp, vp, vp, C.c_int64, vp]),

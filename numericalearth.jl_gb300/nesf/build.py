@@ -31,10 +31,14 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-r
 # unchanged). Measured on the 1/8-degree step: 6.70 -> 5.77 ms, the largest error
 # against the FP64 oracle 4.3e-6 both ways.
 FAST_FP32 = ["--use_fast_math"]
-PER_FILE_FLAGS = {"nesf_exchange.cu": ["-fmad=false"], "nesf_ao.cu": FAST_FP32, "nesf_ai.cu": FAST_FP32}
+PER_FILE_FLAGS = {"nesf_exchange.cu": ["-fmad=false"], "nesf_ao.cu": FAST_FP32, "nesf_ai.cu": FAST_FP32,
+                  "nesf_df.cu": FAST_FP32}
 # The solve files instantiate every kernel for FP64 and FP32 storage: each is compiled
 # twice, one storage type per object, so the slowest translation unit takes half as long.
 SPLIT_BY_STORAGE = ("nesf_ao.cu", "nesf_ai.cu", "nesf_al.cu")
+# The two interface solves are split once more: their double-float replay kernels
+# (NESF_DF_PART 1) compile apart from the other kernels (NESF_DF_PART 0).
+SPLIT_DF_PART = ("nesf_ao.cu", "nesf_ai.cu")
 
 
 def nvcc():
@@ -73,7 +77,10 @@ def build(force=False, verbose=False, jobs=None):
     units = []
     for src in srcs:
         base = os.path.basename(src)[:-3]
-        if os.path.basename(src) in SPLIT_BY_STORAGE:
+        if os.path.basename(src) in SPLIT_DF_PART:
+            units += [(src, [f"-DNESF_STORAGE={b}", f"-DNESF_DF_PART={d}"], f"{base}.f{b}.p{d}.o")
+                      for b in (64, 32) for d in (0, 1)]
+        elif os.path.basename(src) in SPLIT_BY_STORAGE:
             units += [(src, [f"-DNESF_STORAGE={b}"], f"{base}.f{b}.o") for b in (64, 32)]
         else:
             units.append((src, [], base + ".o"))
@@ -91,7 +98,7 @@ def build(force=False, verbose=False, jobs=None):
         return obj
 
     # slowest first, so the long units start at once when there are fewer cores than units
-    units.sort(key=lambda u: os.path.basename(u[0]) not in SPLIT_BY_STORAGE)
+    units.sort(key=lambda u: (os.path.basename(u[0]) not in SPLIT_BY_STORAGE, "-DNESF_DF_PART=1" not in u[1]))
     with ThreadPoolExecutor(max_workers=jobs or max(1, min(len(units), os.cpu_count() or 1))) as ex:
         objs = list(ex.map(compile_one, units))
     tmp = LIB + ".tmp"
