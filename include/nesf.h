@@ -824,8 +824,11 @@ typedef struct {
                                  idle lanes as soon as refill_lanes of them are idle (2)              */
     int32_t refill_lanes;     /* pass1_fetch 4: idle lanes that make a warp take new entries, 1..32
                                  (32: warp fetching) (8)                                                */
-    int32_t early_ocean_classify; /* coupling step with two lanes: the ocean's classify pass and warm-
-                                 start inference beside the sea-ice pass 1, its pass 1 after it (1) */
+    int32_t early_ocean_classify; /* coupling step with two lanes: the ocean's classify pass and
+                                 warm-start inference 0 after the sea-ice pass 1, 1 beside it, 2
+                                 before it (the sea-ice pass 1 waits for them), 3 after it with the
+                                 sea-ice polish pass waiting for them; the ocean's pass 1 follows
+                                 the sea-ice pass 1 in each (0)                                   */
     int32_t ice_deferred_per_sm; /* blocks per SM of the sea-ice solve's packed polish and replay
                                  passes, 1..16; 0: deferred_per_sm. Fewer leave registers to the
                                  ocean solve's kernels that run beside them (0)              */

@@ -418,7 +418,7 @@ template <class S>
 static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                                SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws,
                                DevStats* stats, cudaStream_t stream, cudaEvent_t after_solve, const TailLane* tail,
-                               const TailLane* early) {
+                               const TailLane* early, cudaEvent_t before_pass1, MidHook* mid) {
     const int64_t ring = (int64_t)(a.L.nx + 2) * (a.L.ny + 2);
     const int block = so.block;   // <= 128: the kernels are compiled with __launch_bounds__(128)
     dim3 grid((unsigned)((ring + block - 1) / block));
@@ -464,6 +464,7 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
         trace_mark(so.tracer, "ai_warm_start_inference", stream);
     }
     const float* guess = warm ? ws.guess : nullptr;
+    if (before_pass1 && (e = cudaStreamWaitEvent(stream, before_pass1, 0)) != cudaSuccess) return e;
     // the adaptive pass 1 keeps FP32 results up to fp32_rho; fp32_rho = 0 keeps none: the
     // POLISH pass 1, which polishes every cell in place
     const bool adaptive = prec == NESF_F32_ADAPTIVE && so.fp32_rho > 0.0f;
@@ -489,6 +490,7 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     e = cudaGetLastError();
     trace_mark(so.tracer, "ai_pass1", stream);
     if (e == cudaSuccess && after_solve) e = cudaEventRecord(after_solve, stream);
+    if (e == cudaSuccess && mid && mid->fn && (mid->status = mid->fn(mid->arg)) != NESF_OK) return cudaErrorLaunchFailure;
     if (e != cudaSuccess || prec == NESF_PLAIN_F64) return e;
     const unsigned g2 = (unsigned)(sms * so.deferred_ice);
     if (!adaptive) {
@@ -510,6 +512,7 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
         ai_replay(g2, rs, 3);
         trace_mark(so.tracer, "ai_calm_replay", rs);
     }
+    if (mid && mid->wait && (e = cudaStreamWaitEvent(stream, mid->wait, 0)) != cudaSuccess) return e;
     if (skin && rq.pstate) ai_polish_kernel<S, true, true><<<g2, 128, 0, stream>>>(a, P64, P32, P64, so, rq, 2, stats);
     else if (skin) ai_polish_kernel<S, true, false><<<g2, 128, 0, stream>>>(a, P64, P32, P64, so, rq, 2, stats);
     else ai_polish_kernel<S, false, false><<<g2, 128, 0, stream>>>(a, P64, P32, P64, so, rq, 2, stats);
@@ -552,15 +555,17 @@ cudaError_t launch_ai_replay_df(const AIArgs<float>& a, const DevIface<df>& P, c
 #if !defined(NESF_STORAGE) || NESF_STORAGE == 64
 cudaError_t launch_ai(const AIArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream, cudaEvent_t after_solve, const TailLane* tail, const TailLane* early) {
-    return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream, after_solve, tail, early);
+                      cudaStream_t stream, cudaEvent_t after_solve, const TailLane* tail, const TailLane* early,
+                      cudaEvent_t before_pass1, MidHook* mid) {
+    return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream, after_solve, tail, early, before_pass1, mid);
 }
 #endif
 #if !defined(NESF_STORAGE) || NESF_STORAGE == 32
 cudaError_t launch_ai(const AIArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream, cudaEvent_t after_solve, const TailLane* tail, const TailLane* early) {
-    return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream, after_solve, tail, early);
+                      cudaStream_t stream, cudaEvent_t after_solve, const TailLane* tail, const TailLane* early,
+                      cudaEvent_t before_pass1, MidHook* mid) {
+    return launch_ai_t(a, P64, P32, prec, so, wl, rq, ws, stats, stream, after_solve, tail, early, before_pass1, mid);
 }
 #endif
 #endif

@@ -496,7 +496,7 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
                                const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec,
                                bool skin, SolveOpts so, const WorkList& wl, const ReplayQueue& rq,
                                const WarmStart& ws, DevStats* stats, cudaStream_t stream,
-                               cudaEvent_t before_pass1, const TailLane* tail) {
+                               cudaEvent_t before_pass1, const TailLane* tail, MidHook* mid) {
     const int64_t ring = (int64_t)(a.L.nx + 2) * (a.L.ny + 2);
     const int threads = so.block;   // <= 128: the kernels are compiled with __launch_bounds__(128)
     const int nm = members > 1 ? members : 1;
@@ -523,6 +523,10 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
                      true, stream);
         if (e != cudaSuccess) return e;
         trace_mark(so.tracer, "ao_warm_start_inference", stream);
+    }
+    if (mid) {
+        if (mid->ready && (e = cudaEventRecord(mid->ready, stream)) != cudaSuccess) return e;
+        if (mid->fn && (mid->status = mid->fn(mid->arg)) != NESF_OK) return cudaErrorLaunchFailure;
     }
     if (before_pass1 && (e = cudaStreamWaitEvent(stream, before_pass1, 0)) != cudaSuccess) return e;
 #define NESF_AO_LAUNCH(PR, SK, EN) \
@@ -659,9 +663,9 @@ cudaError_t preload_ao_replay_df(const AOArgs<float>*) { return preload_ao_repla
 cudaError_t launch_ao(const AOArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream, cudaEvent_t before_pass1, const TailLane* tail) {
+                      cudaStream_t stream, cudaEvent_t before_pass1, const TailLane* tail, MidHook* mid) {
     return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, ws, stats, stream, before_pass1,
-                       tail);
+                       tail, mid);
 }
 cudaError_t preload_ao_kernels(const AOArgs<double>* p) {
     cudaError_t e = preload_ao_t<double>();
@@ -672,9 +676,9 @@ cudaError_t preload_ao_kernels(const AOArgs<double>* p) {
 cudaError_t launch_ao(const AOArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream, cudaEvent_t before_pass1, const TailLane* tail) {
+                      cudaStream_t stream, cudaEvent_t before_pass1, const TailLane* tail, MidHook* mid) {
     return launch_ao_t(a, P64, P32, P64s, P32s, members, prec, skin, so, wl, rq, ws, stats, stream, before_pass1,
-                       tail);
+                       tail, mid);
 }
 cudaError_t preload_ao_kernels(const AOArgs<float>* p) {
     cudaError_t e = preload_ao_t<float>();

@@ -39,7 +39,7 @@ struct nesf_context {
     // the coupling step's second lane: scratch of the sea-ice solve, its stream, fork/join events
     nesf_context* aux;
     cudaStream_t side;
-    cudaEvent_t ev_fork, ev_ice, ev_join;
+    cudaEvent_t ev_fork, ev_ice, ev_join, ev_ocean;
     // the sea-ice solve's replay stream beside its polish pass, with fork/join events, and its
     // early lane (the calm cells' replays beside pass 1)
     cudaStream_t tail;
@@ -89,7 +89,7 @@ static nesf_tuning default_tuning() {
     t.io_overlap = 1;
     t.pass1_fetch = 2;
     t.refill_lanes = 8;
-    t.early_ocean_classify = 1;
+    t.early_ocean_classify = 0;
     t.ice_deferred_per_sm = 0;
     t.cells_per_thread = 1;
     return t;
@@ -396,7 +396,7 @@ int nesf_context_create(int32_t device, nesf_context** out) {
     c->warm_capacity = 0;
     c->aux = nullptr;
     c->side = nullptr;
-    c->ev_fork = c->ev_ice = c->ev_join = nullptr;
+    c->ev_fork = c->ev_ice = c->ev_join = c->ev_ocean = nullptr;
     c->tail = nullptr;
     c->ev_tail_fork = c->ev_tail_join = nullptr;
     c->early = nullptr;
@@ -438,6 +438,7 @@ int nesf_context_destroy(nesf_context* c) {
         if (c->side) cudaStreamDestroy(c->side);
         if (c->ev_fork) cudaEventDestroy(c->ev_fork);
         if (c->ev_ice) cudaEventDestroy(c->ev_ice);
+        if (c->ev_ocean) cudaEventDestroy(c->ev_ocean);
         if (c->ev_join) cudaEventDestroy(c->ev_join);
         if (c->tail) cudaStreamDestroy(c->tail);
         if (c->ev_tail_fork) cudaEventDestroy(c->ev_tail_fork);
@@ -783,9 +784,12 @@ static int check_ao_fields(const nesf_ao_fields* f, const nesf_interface_params*
 }
 
 // The atmosphere-ocean solve; before_pass1 (optional): an event its stream waits for after the
-// classify pass and the warm-start inference, before pass 1.
+// classify pass and the warm-start inference, before pass 1; mid (optional): recorded on the
+// stream after the inference, then its hook enqueues work of another lane (which may wait for
+// the event), before the wait for before_pass1 is enqueued.
 static int ocean_fluxes(nesf_context* ctx, const nesf_interface_params* params, const nesf_ao_fields* f,
-                        const nesf_solver_options* opts, nesf_stats* stats, void* stream, cudaEvent_t before_pass1) {
+                        const nesf_solver_options* opts, nesf_stats* stats, void* stream, cudaEvent_t before_pass1,
+                        MidHook* mid = nullptr) {
     const char* who = "nesf_compute_atmosphere_ocean_fluxes";
     int r = check_params(params, who);
     if (r) return r;
@@ -818,9 +822,9 @@ static int ocean_fluxes(nesf_context* ctx, const nesf_interface_params* params, 
     return with_stats(ctx, stats, s, [&](DevStats* ds) {
         if (f->dtype == NESF_F64)
             return launch_ao(ao_args<double>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl, rq, ws,
-                             ds, s, before_pass1, &tl);
+                             ds, s, before_pass1, &tl, mid);
         return launch_ao(ao_args<float>(f, 0), P64, P32, nullptr, nullptr, 1, o.precision, skin, so, wl, rq, ws, ds,
-                         s, before_pass1, &tl);
+                         s, before_pass1, &tl, mid);
     });
 }
 
@@ -980,10 +984,11 @@ extern "C" int nesf_compute_atmosphere_land_fluxes(nesf_context* ctx, const nesf
 }
 
 // The sea-ice solve; `after_solve` (optional) is recorded on the stream once the
-// pass-1 solve is enqueued, before the packed polish and replay passes.
+// pass-1 solve is enqueued, before the packed polish and replay passes; `before_pass1`
+// (optional) is waited for before pass 1; `mid` (optional): run after pass 1 (MidHook).
 static int sea_ice_fluxes(nesf_context* ctx, const nesf_interface_params* params, const nesf_ai_fields* f,
                           const nesf_solver_options* opts, nesf_stats* stats, void* stream,
-                          cudaEvent_t after_solve) {
+                          cudaEvent_t after_solve, cudaEvent_t before_pass1 = nullptr, MidHook* mid = nullptr) {
     const char* who = "nesf_compute_atmosphere_sea_ice_fluxes";
     int r = check_params(params, who);
     if (r) return r;
@@ -1032,8 +1037,9 @@ static int sea_ice_fluxes(nesf_context* ctx, const nesf_interface_params* params
     return with_stats(ctx, stats, s, [&](DevStats* ds) {
         if (f->dtype == NESF_F64)
             return launch_ai(ai_args<double>(f), P64, P32, o.precision, so, wl, rq, ws, ds, s, after_solve, &tl,
-                             &el);
-        return launch_ai(ai_args<float>(f), P64, P32, o.precision, so, wl, rq, ws, ds, s, after_solve, &tl, &el);
+                             &el, before_pass1, mid);
+        return launch_ai(ai_args<float>(f), P64, P32, o.precision, so, wl, rq, ws, ds, s, after_solve, &tl, &el,
+                         before_pass1, mid);
     });
 }
 
@@ -1536,6 +1542,7 @@ static int coupling_lane(nesf_context* ctx) {
     NESF_CUDA(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
     NESF_CUDA(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
     NESF_CUDA(cudaEventCreateWithFlags(&ctx->ev_ice, cudaEventDisableTiming));
+    NESF_CUDA(cudaEventCreateWithFlags(&ctx->ev_ocean, cudaEventDisableTiming));
     NESF_CUDA(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
     return NESF_OK;
 }
@@ -1581,6 +1588,20 @@ extern "C" int nesf_coupling_step(nesf_context* ctx, const nesf_coupling_step_ar
     if (a->interp) trace_mark(tr, "interpolate", s);
     const bool io_split = ice && a->io_params && ctx->tuning.io_overlap;
     const bool lanes = ice && ctx->tuning.two_lanes;
+    // early_ocean_classify 2: the sea-ice lane is enqueued from inside the ocean solve, once
+    // the ocean's classify pass and inference are, and its pass 1 waits for them (ev_ocean).
+    // 3: the ocean solve is enqueued from inside the sea-ice solve, after its pass 1, waits for
+    // that pass, and the sea-ice polish pass waits for the ocean's inference (ev_ocean): the
+    // ocean's classify and inference run alone after the sea-ice pass 1, the sea-ice polish
+    // beside the ocean's pass 1
+    const bool ocean_first = lanes && ctx->tuning.early_ocean_classify == 2;
+    const bool ice_polish_later = lanes && ctx->tuning.early_ocean_classify == 3;
+    struct IceLane {
+        nesf_context* ctx;
+        const nesf_coupling_step_args* a;
+        const nesf_solver_options* opts;
+    } lane{ctx, a, opts};
+    MidHook mid{nullptr, nullptr, NESF_OK, nullptr, nullptr};
     if (ice) {
         if ((r = coupling_lane(ctx))) return r;
         ctx->aux->tuning = ctx->tuning;
@@ -1589,18 +1610,63 @@ extern "C" int nesf_coupling_step(nesf_context* ctx, const nesf_coupling_step_ar
         if (lanes) {
             NESF_CUDA(cudaEventRecord(ctx->ev_fork, s));
             NESF_CUDA(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
-            if ((r = sea_ice_fluxes(ctx->aux, a->ai_params, a->ai, opts, nullptr, ctx->side, ctx->ev_ice))) return r;
-            NESF_CUDA(cudaEventRecord(ctx->ev_join, ctx->side));
+            if (!ocean_first && !ice_polish_later) {
+                if ((r = sea_ice_fluxes(ctx->aux, a->ai_params, a->ai, opts, nullptr, ctx->side, ctx->ev_ice)))
+                    return r;
+                NESF_CUDA(cudaEventRecord(ctx->ev_join, ctx->side));
+            }
         }
         if (io_split && (r = sea_ice_ocean(ctx, a->io_params, a->io, stream, 1))) return r;
         if (io_split) trace_mark(tr, "sea_ice_ocean_fluxes", s);
+        if (ice_polish_later) {
+            // the ocean solve on the main stream (after the sea-ice pass 1), enqueued from the
+            // sea-ice launch once its pass 1 is
+            struct OceanLane {
+                nesf_context* ctx;
+                const nesf_coupling_step_args* a;
+                const nesf_solver_options* opts;
+                cudaStream_t s;
+            } ol{ctx, a, opts, s};
+            MidHook om{nullptr, nullptr, NESF_OK, ctx->ev_ocean, nullptr};
+            struct Both { OceanLane* ol; MidHook* om; } both{&ol, &om};
+            MidHook im{nullptr, &both, NESF_OK, nullptr, ctx->ev_ocean};
+            im.fn = [](void* p) -> int {
+                Both* b = (Both*)p;
+                const cudaError_t e = cudaStreamWaitEvent(b->ol->s, b->ol->ctx->ev_ice, 0);
+                if (e != cudaSuccess) return cuda_fail(e, "nesf_coupling_step");
+                const int q = ocean_fluxes(b->ol->ctx, b->ol->a->ao_params, b->ol->a->ao, b->ol->opts, nullptr,
+                                           (void*)b->ol->s, nullptr, b->om);
+                return b->om->status ? b->om->status : q;
+            };
+            r = sea_ice_fluxes(ctx->aux, a->ai_params, a->ai, opts, nullptr, ctx->side, ctx->ev_ice, nullptr, &im);
+            if (im.status) return im.status;
+            if (r) return r;
+            NESF_CUDA(cudaEventRecord(ctx->ev_join, ctx->side));
+        }
         if (lanes && !ctx->tuning.early_ocean_classify) NESF_CUDA(cudaStreamWaitEvent(s, ctx->ev_ice, 0));
         else if (!lanes && (r = sea_ice_fluxes(ctx->aux, a->ai_params, a->ai, opts, nullptr, s, nullptr))) return r;
+        if (ocean_first) {
+            mid.ready = ctx->ev_ocean;
+            mid.arg = &lane;
+            mid.fn = [](void* p) -> int {
+                IceLane* l = (IceLane*)p;
+                int q = sea_ice_fluxes(l->ctx->aux, l->a->ai_params, l->a->ai, l->opts, nullptr, l->ctx->side,
+                                       l->ctx->ev_ice, l->ctx->ev_ocean);
+                if (q) return q;
+                const cudaError_t e = cudaEventRecord(l->ctx->ev_join, l->ctx->side);
+                return e == cudaSuccess ? NESF_OK : cuda_fail(e, "nesf_coupling_step");
+            };
+        }
     }
-    // with early_ocean_classify the ocean's classify pass and warm-start inference run beside the
-    // sea-ice pass 1, and its pass 1 waits for the sea-ice pass 1 instead
+    // with early_ocean_classify 1 the ocean's classify pass and warm-start inference run beside
+    // the sea-ice pass 1, with 2 before it; either way the ocean's pass 1 waits for the sea-ice
+    // pass 1
     cudaEvent_t before_pass1 = lanes && ctx->tuning.early_ocean_classify ? ctx->ev_ice : nullptr;
-    if ((r = ocean_fluxes(ctx, a->ao_params, a->ao, opts, nullptr, stream, before_pass1))) return r;
+    if (!ice_polish_later) {
+        r = ocean_fluxes(ctx, a->ao_params, a->ao, opts, nullptr, stream, before_pass1, ocean_first ? &mid : nullptr);
+        if (mid.status) return mid.status;
+        if (r) return r;
+    }
     if (lanes) {
         DeviceGuard g(ctx->device);
         NESF_CUDA(cudaStreamWaitEvent(s, ctx->ev_join, 0));
@@ -1829,8 +1895,8 @@ static int check_tuning(const nesf_tuning& t, const char* who) {
         return fail(NESF_ERR_ARG, "%s: pass1_fetch %d (1, 2, 3 or 4)", who, t.pass1_fetch);
     if (t.refill_lanes < 0 || t.refill_lanes > 32)
         return fail(NESF_ERR_ARG, "%s: refill_lanes %d (1..32)", who, t.refill_lanes);
-    if (t.early_ocean_classify < 0 || t.early_ocean_classify > 1)
-        return fail(NESF_ERR_ARG, "%s: early_ocean_classify is 0 or 1", who);
+    if (t.early_ocean_classify < 0 || t.early_ocean_classify > 3)
+        return fail(NESF_ERR_ARG, "%s: early_ocean_classify is 0, 1, 2 or 3", who);
     if (t.ice_deferred_per_sm < 0 || t.ice_deferred_per_sm > 16)
         return fail(NESF_ERR_ARG, "%s: ice_deferred_per_sm %d (0..16)", who, t.ice_deferred_per_sm);
     if (t.cells_per_thread < 0 || t.cells_per_thread > 8)
@@ -1929,7 +1995,7 @@ extern "C" int nesf_autotune(nesf_context* ctx, const nesf_coupling_step_args* a
         {&nesf_tuning::refill_lanes, {8, 4, 16}, adaptive},
         {&nesf_tuning::two_lanes, {1, 0}, ice},
         {&nesf_tuning::io_overlap, {1, 0}, ice && a->io_params != nullptr},
-        {&nesf_tuning::early_ocean_classify, {1, 0}, ice},
+        {&nesf_tuning::early_ocean_classify, {0, 3, 1, 2}, ice},
         {&nesf_tuning::ice_deferred_per_sm, {0, 1, 2}, ice && fast},
         {&nesf_tuning::cells_per_thread, {1, 2, 4}, adaptive},
     };

@@ -1152,17 +1152,33 @@ inline dim3 pass1_grid(K kernel, dim3 grid, int threads, int sms, bool fetch, in
     return grid;
 }
 
+// A host hook inside a solve's launch, for the coupling step's lanes. Atmosphere-ocean: after
+// the classify pass and the inference, `ready` (optional) is recorded on the solve's stream,
+// then fn(arg) runs. Atmosphere-sea-ice: after pass 1, fn(arg) runs, and the polish pass waits
+// for `wait` (optional). fn enqueues work of another lane; a non-zero status from it is kept
+// in `status` and ends the launch.
+struct MidHook {
+    int (*fn)(void*);
+    void* arg;
+    int status;
+    cudaEvent_t ready;
+    cudaEvent_t wait;
+};
+
 // before_pass1 (optional): an event the stream waits for after the classify pass and the
 // warm-start inference, before pass 1. tail (optional): a second lane on which pass 1's
 // replays run beside the polish pass (the queue's part 2 then holds the polish pass's).
+// mid (optional): the hook above, run before the wait for before_pass1 is enqueued.
 cudaError_t launch_ao(const AOArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream, cudaEvent_t before_pass1 = nullptr, const TailLane* tail = nullptr);
+                      cudaStream_t stream, cudaEvent_t before_pass1 = nullptr, const TailLane* tail = nullptr,
+                      MidHook* mid = nullptr);
 cudaError_t launch_ao(const AOArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32,
                       const DevIface<double>* P64s, const DevIface<float>* P32s, int members, int prec, bool skin,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
-                      cudaStream_t stream, cudaEvent_t before_pass1 = nullptr, const TailLane* tail = nullptr);
+                      cudaStream_t stream, cudaEvent_t before_pass1 = nullptr, const TailLane* tail = nullptr,
+                      MidHook* mid = nullptr);
 // Loads (under lazy module loading) every kernel that the one-member atmosphere-ocean
 // solve of storage S can launch, so that a later launch loads no module.
 cudaError_t preload_ao_kernels(const AOArgs<double>*);
@@ -1171,14 +1187,16 @@ cudaError_t preload_ao_kernels(const AOArgs<float>*);
 // tail (optional): a second stream on which pass 1's replays run beside the polish pass.
 // early (optional): a third stream on which the calm cells' replays run from the classify
 // pass on, beside pass 1 (SolveOpts::calm_wind; without it no cell is sent early).
+// before_pass1 (optional): an event the stream waits for before pass 1. mid (optional): the
+// hook above, run after pass 1.
 cudaError_t launch_ai(const AIArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
                       cudaStream_t stream, cudaEvent_t after_solve = nullptr, const TailLane* tail = nullptr,
-                      const TailLane* early = nullptr);
+                      const TailLane* early = nullptr, cudaEvent_t before_pass1 = nullptr, MidHook* mid = nullptr);
 cudaError_t launch_ai(const AIArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, const WorkList& wl, const ReplayQueue& rq, const WarmStart& ws, DevStats* stats,
                       cudaStream_t stream, cudaEvent_t after_solve = nullptr, const TailLane* tail = nullptr,
-                      const TailLane* early = nullptr);
+                      const TailLane* early = nullptr, cudaEvent_t before_pass1 = nullptr, MidHook* mid = nullptr);
 cudaError_t launch_al(const ALArgs<double>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,
                       SolveOpts so, DevStats* stats, cudaStream_t stream);
 cudaError_t launch_al(const ALArgs<float>& a, const DevIface<double>& P64, const DevIface<float>& P32, int prec,

@@ -13,7 +13,7 @@ from nesf.coupled import CoupledModel, ICE_NET, OCEAN_NET, RAD_DIAG
 pytestmark = pytest.mark.gpu
 
 DEFAULT = dict(solve_block=128, deferred_per_sm=4, infer_per_sm=4, two_lanes=1, io_overlap=1, pass1_fetch=2,
-               refill_lanes=8, early_ocean_classify=1, ice_deferred_per_sm=0, cells_per_thread=1)
+               refill_lanes=8, early_ocean_classify=0, ice_deferred_per_sm=0, cells_per_thread=1)
 
 
 @pytest.fixture(scope="module")
@@ -51,7 +51,9 @@ def test_every_tuning_gives_the_same_outputs(model, precision):
                    dict(pass1_fetch=1), dict(pass1_fetch=3), dict(pass1_fetch=3, solve_block=64),
                    dict(pass1_fetch=2, solve_block=32), dict(pass1_fetch=4), dict(pass1_fetch=4, refill_lanes=1),
                    dict(pass1_fetch=4, refill_lanes=16, solve_block=64), dict(pass1_fetch=4, refill_lanes=3),
-                   dict(early_ocean_classify=0), dict(early_ocean_classify=0, two_lanes=0),
+                   dict(early_ocean_classify=1), dict(early_ocean_classify=1, two_lanes=0),
+                   dict(early_ocean_classify=2), dict(early_ocean_classify=2, io_overlap=0),
+                   dict(early_ocean_classify=3), dict(early_ocean_classify=3, io_overlap=0),
                    dict(ice_deferred_per_sm=1), dict(ice_deferred_per_sm=2, deferred_per_sm=8),
                    dict(cells_per_thread=2), dict(cells_per_thread=4, pass1_fetch=1),
                    dict(cells_per_thread=3, pass1_fetch=3, solve_block=64),
@@ -67,7 +69,8 @@ def test_warm_start_inference_grid(model):
     try:
         ref = step(model, "f32_adaptive")
         for tuning in (dict(infer_per_sm=1), dict(infer_per_sm=2), dict(infer_per_sm=8), dict(pass1_fetch=4),
-                       dict(pass1_fetch=4, refill_lanes=5), dict(early_ocean_classify=0),
+                       dict(pass1_fetch=4, refill_lanes=5), dict(early_ocean_classify=1), dict(early_ocean_classify=2),
+                       dict(early_ocean_classify=3),
                        dict(cells_per_thread=2, pass1_fetch=3), dict(cells_per_thread=4, pass1_fetch=1)):
             got = step(model, "f32_adaptive", **tuning)
             for k in ref:
@@ -85,7 +88,7 @@ def test_autotune_sets_a_valid_tuning(model):
     assert t["step_ms"] > 0
     assert t["solve_block"] in (32, 64, 96, 128) and 1 <= t["deferred_per_sm"] <= 16
     assert t["two_lanes"] in (0, 1) and t["io_overlap"] in (0, 1) and t["pass1_fetch"] in (1, 2, 3, 4)
-    assert 1 <= t["refill_lanes"] <= 32 and t["early_ocean_classify"] in (0, 1)
+    assert 1 <= t["refill_lanes"] <= 32 and t["early_ocean_classify"] in (0, 1, 2, 3)
     assert 0 <= t["ice_deferred_per_sm"] <= 16 and 1 <= t["cells_per_thread"] <= 8
     cur = api.get_tuning()
     assert {k: cur[k] for k in DEFAULT} == {k: t[k] for k in DEFAULT}
