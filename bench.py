@@ -244,10 +244,13 @@ REPEAT_ROUNDS = 5
 # 720 x 320 coupled case): the profile summary named here holds the command and the figures.
 NCU_PIPES = {
     "source": "profiles/solve_kernels_f32adaptive_coupled_720x320.md",
-    "ao_adaptive_kernel": {"issue_active": 0.423, "fma_pipe": 0.168, "alu_pipe": 0.220, "xu_inst": 0.089,
-                           "fp64_pipe": 0.289, "warps_active": 0.256, "lanes_active_per_warp_instruction": 24.5},
-    "ai_adaptive_kernel": {"issue_active": 0.349, "fma_pipe": 0.110, "alu_pipe": 0.161, "xu_inst": 0.065,
-                           "fp64_pipe": 0.068, "warps_active": 0.152, "lanes_active_per_warp_instruction": 19.1},
+    "ao_adaptive_kernel": {"issue_active": 0.424, "fma_pipe": 0.162, "alu_pipe": 0.220, "xu_inst": 0.088,
+                           "fp64_pipe": 0.288, "warps_active": 0.257, "lanes_active_per_warp_instruction": 24.5},
+    "ai_adaptive_kernel": {"issue_active": 0.300, "fma_pipe": 0.103, "alu_pipe": 0.153, "xu_inst": 0.061,
+                           "fp64_pipe": 0.064, "warps_active": 0.136, "lanes_active_per_warp_instruction": 19.0},
+    "ai_replay_kernel_double_float": {"issue_active": 0.274, "fma_pipe": 0.192, "alu_pipe": 0.051, "xu_inst": 0.006,
+                                      "fp64_pipe": 0.0, "warps_active": 0.058,
+                                      "lanes_active_per_warp_instruction": 22.4},
 }
 
 
