@@ -81,7 +81,7 @@ __device__ __forceinline__ void io_interface(const IOArgs<S>& a, const nesf_io_p
 // state as PART 0, and PART 1 only reads the ocean state, so it may run beside
 // kernels that read it.
 template <class S, int PART>
-__global__ void __launch_bounds__(256) io_kernel(IOArgs<S> a, nesf_io_params p, IOConsts<S> C, IOConsts<double> C64) {
+__global__ void __launch_bounds__(256) io_kernel(IOArgs<S> a, nesf_io_params p, IOConsts<S> C, IOConsts<df> Cdf) {
     using R = S;
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t n = (int64_t)a.L.nx * a.L.ny;
@@ -141,12 +141,14 @@ __global__ void __launch_bounds__(256) io_kernel(IOArgs<S> a, nesf_io_params p, 
     // FP32 fields: where the ice covers part of the cell, the interface heat
     // eta (T_N - T_b) + kappa (T_i - T_b) cancels near the melting point and would
     // multiply FP32's rounding of S_b by |T_b| / |T_N - T_b|; the interface
-    // conditions are solved in FP64 there, from the FP32 inputs (exact in FP64),
-    // with a frozen top level at its melting point T_m(S_N) in FP64.
+    // conditions are solved in double-float there (48 bits, on the FP32 pipes: FP64
+    // issues one warp instruction per ~64 cycles per SM sub-partition on this GPU),
+    // from the FP32 inputs (exact in double-float), with a frozen top level at its
+    // melting point T_m(S_N) in double-float.
     if (sizeof(S) < sizeof(double) && aleph > R(0)) {
-        double SN64 = (double)SN;
-        double TN64 = top_frozen ? p.liquidus_freshwater_melting_temperature - p.liquidus_slope * SN64 : (double)TN;
-        io_interface<double>(a, p, C64, k2, TN64, SN64, Qio, Tb, Sb);
+        const df SNd((float)SN);
+        const df TNd = top_frozen ? Cdf.Tfw - Cdf.slope * SNd : df((float)TN);
+        io_interface<df>(a, p, Cdf, k2, TNd, SNd, Qio, Tb, Sb);
     } else {
         io_interface<R>(a, p, C, k2, TN, SN, Qio, Tb, Sb);
     }
@@ -536,10 +538,10 @@ template <class S>
 cudaError_t launch_io(const IOArgs<S>& a, const nesf_io_params& p, cudaStream_t s, int part) {
     int64_t n = (int64_t)a.L.nx * a.L.ny;
     const IOConsts<S> C = io_consts<S>(p);
-    const IOConsts<double> C64 = io_consts<double>(p);
-    if (part == 1) io_kernel<S, 1><<<blocks_for(n, 256), 256, 0, s>>>(a, p, C, C64);
-    else if (part == 2) io_kernel<S, 2><<<blocks_for(n, 256), 256, 0, s>>>(a, p, C, C64);
-    else io_kernel<S, 0><<<blocks_for(n, 256), 256, 0, s>>>(a, p, C, C64);
+    const IOConsts<df> Cdf = io_consts<df>(p);
+    if (part == 1) io_kernel<S, 1><<<blocks_for(n, 256), 256, 0, s>>>(a, p, C, Cdf);
+    else if (part == 2) io_kernel<S, 2><<<blocks_for(n, 256), 256, 0, s>>>(a, p, C, Cdf);
+    else io_kernel<S, 0><<<blocks_for(n, 256), 256, 0, s>>>(a, p, C, Cdf);
     return cudaGetLastError();
 }
 template cudaError_t launch_io<double>(const IOArgs<double>&, const nesf_io_params&, cudaStream_t, int);
