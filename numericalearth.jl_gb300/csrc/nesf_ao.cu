@@ -395,8 +395,11 @@ struct AOAdaptiveCell {
 
 // Pass 1 of the adaptive solver, one member, convergence stopping rule: adaptive_pass1
 // with the schedule of SolveOpts::fetch / refill.
+// Six resident blocks per SM (80 registers) with a bulk interface temperature: its sweep
+// state fits with few spills once the unused fourth state component is a constant, and the
+// extra warps measured 1.32 -> 1.23 ms on the 1/8-degree step; five with a skin temperature.
 template <class S, bool SKIN>
-__global__ void __launch_bounds__(128, NESF_ADAPTIVE_MIN_BLOCKS) ao_adaptive_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
+__global__ void __launch_bounds__(128, SKIN ? NESF_ADAPTIVE_MIN_BLOCKS : NESF_ADAPTIVE_MIN_BLOCKS + 1) ao_adaptive_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
                                                              SolveOpts so, WorkList wl, ReplayQueue rq,
                                                              const float* guess, DevStats* stats) {
     AOAdaptiveCell<S, SKIN> cell{a, P64, P32};

@@ -715,7 +715,7 @@ __device__ __forceinline__ void sweep_map(const DevIface<float>& P32, const Cell
         SurfaceConst<float> sv = s32;
         iterate_state<float, false>(P32, c32, sv, yu, yt, yq);
     }
-    y[0] = yu; y[1] = yt; y[2] = yq; y[3] = yT;
+    y[0] = yu; y[1] = yt; y[2] = yq; y[3] = SKIN ? yT : 0.0f;   // (a constant fourth component without a skin)
 }
 
 template <bool SKIN, bool ACCEPT32, bool STRICT = ACCEPT32, bool CENTRAL = !ACCEPT32>
