@@ -250,7 +250,9 @@ __global__ void __launch_bounds__(128, TRAIN ? 1 : 4) pass_kernel(Blob* __restri
     extern __shared__ __align__(1024) unsigned char sm[];
     __shared__ uint64_t bar;
     __shared__ uint32_t tslot;
-    __shared__ float sb1[kHid], sb2[kHid], sb3[kOutPad];
+    __shared__ __align__(16) float sb1[kHid];   // read as float2 pairs by the inference
+    __shared__ __align__(16) float sb2[kHid];
+    __shared__ float sb3[kOutPad];
     __shared__ float gb1[kHid], gb2[kHid], gb3[kOutPad];
     __shared__ float in_mu[8], in_sig[8], out_mu[4], out_sig[4];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, tid = threadIdx.x;
@@ -331,10 +333,16 @@ __global__ void __launch_bounds__(128, TRAIN ? 1 : 4) pass_kernel(Blob* __restri
         for (int c0 = 0; c0 < kHid; c0 += 16) {
             float v[16];
             tc::tmem_ld16(tc::tmem_at(tm + tD, warp, c0), v);
+            if constexpr (TRAIN) {
 #pragma unroll
-            for (int k = 0; k < 16; k++) {
-                Z1[c0 + k] = v[k] + sb1[c0 + k];
-                v[k] = TRAIN ? gelu(Z1[c0 + k]) : gelu_approx(Z1[c0 + k]);
+                for (int k = 0; k < 16; k++) {
+                    Z1[c0 + k] = v[k] + sb1[c0 + k];
+                    v[k] = gelu(Z1[c0 + k]);
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < 16; k += 2)
+                    gelu_bias_approx2(v[k], v[k + 1], *reinterpret_cast<const float2*>(&sb1[c0 + k]));
             }
             store_row16(sm + oH1, 128, r, c0, v);
         }
@@ -345,10 +353,16 @@ __global__ void __launch_bounds__(128, TRAIN ? 1 : 4) pass_kernel(Blob* __restri
         for (int c0 = 0; c0 < kHid; c0 += 16) {
             float v[16];
             tc::tmem_ld16(tc::tmem_at(tm + tD, warp, c0), v);
+            if constexpr (TRAIN) {
 #pragma unroll
-            for (int k = 0; k < 16; k++) {
-                Z2[c0 + k] = v[k] + sb2[c0 + k];
-                v[k] = TRAIN ? gelu(Z2[c0 + k]) : gelu_approx(Z2[c0 + k]);
+                for (int k = 0; k < 16; k++) {
+                    Z2[c0 + k] = v[k] + sb2[c0 + k];
+                    v[k] = gelu(Z2[c0 + k]);
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < 16; k += 2)
+                    gelu_bias_approx2(v[k], v[k + 1], *reinterpret_cast<const float2*>(&sb2[c0 + k]));
             }
             store_row16(sm + oH2, 128, r, c0, v);
         }
