@@ -622,7 +622,11 @@ int nesf_compute_atmosphere_ocean_fluxes_ensemble(nesf_context* ctx, const nesf_
  * GPU race on the scratch. The device must have been prepared with
  * nesf_noalloc_prepare (else NESF_ERR_ARG). No warm start (NESF_ERR_ARG if
  * requested), no statistics; the context's tuning is not used (default launch
- * shapes). */
+ * shapes). Under NESF_F32_ADAPTIVE its pass 1 forms the cancelling differences
+ * (theta_a - T_s, q_a - q_s ...) in FP64 in the kernel, where the regular entry
+ * point reads them from per-cell double-float records of its classify pass (a
+ * scratch of 64 bytes per cell): the two FP32 trajectories then differ and the
+ * results agree within the solver's tolerance, not bit for bit. */
 int nesf_compute_atmosphere_ocean_fluxes_noalloc(const nesf_interface_params* params, const nesf_ao_fields* fields,
                                                  const nesf_solver_options* opts, void* stream);
 /* Set-up of the allocation-free solve on `device`, once, at the caller's set-up:

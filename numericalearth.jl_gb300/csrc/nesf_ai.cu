@@ -85,6 +85,43 @@ __device__ __forceinline__ void ai_load_fast(const DevIface<double>& P, const De
     }
 }
 
+// The cancelling differences of ai_load_fast in double-float, as the record the classify
+// pass stores per work-list slot for the adaptive pass 1 (anchor_pack).
+template <class S, bool SKIN>
+__device__ __forceinline__ void ai_anchor_df(const DevIface<df>& P, const DevIface<float>& Pf, const AIArgs<S>& a,
+                                             int64_t k, float (&v)[kAnchorFloats]) {
+    const df Ta = ldr<df>(a.Ta, k), qa = ldr<df>(a.qa, k), lift = lift_temperature(P, qa);
+    const df tha = Ta + lift, Ts0 = ldr<df>(a.Ts, k) + P.off_ifc;
+    SurfaceConst<float> sc{};
+    SkinAnchor<float> an{};
+    if (SKIN)
+        an = skin_anchor(P, tha, ldr<df>(a.To, k) + P.off_int, ldr<df>(a.So, k), qa, ldr<df>(a.pa, k),
+                         ldzr<df>(a.sw, k), ldzr<df>(a.lw, k));
+    else
+        fast_surface(P, Pf, Ta, qa, ldr<df>(a.pa, k), lift, Ts0, sc);
+    anchor_pack<SKIN>(sc, an, 0.0f, 0.0f, tha, Ts0, v);
+}
+
+// ai_load_fast's FP32 part, after anchor_load has set the cancelling differences.
+template <class S, bool SKIN>
+__device__ __forceinline__ void ai_load_fp32(const DevIface<float>& Pf, const AIArgs<S>& a, int64_t k, Fast32& f) {
+    CellConst<float>& c = f.c;
+    c.ua = ldf(a.ua, k); c.va = ldf(a.va, k); c.Ta = ldf(a.Ta, k); c.pa = ldf(a.pa, k); c.qa = ldf(a.qa, k);
+    c.du = c.ua; c.dv = c.va;            // sea-ice velocities are not used (:97-98)
+    c.dU2 = c.du * c.du + c.dv * c.dv;
+    c.tha = (float)f.tha;
+    c.rho_a = air_density(Pf, c.Ta, c.pa, c.qa);
+    c.cp_a = cp_m(Pf, c.qa);
+    c.L_s = latent_heat_sublim(Pf, c.Ta);
+    if (SKIN) {
+        c.hi = ldf(a.hi, k);
+        c.hs = a.hs ? ldf(a.hs, k) : 0.0f;
+        c.hc = ldf(a.hc, k);
+        c.Rth = conductive_resistance(Pf, c.hs, c.hi);
+        c.kappa = -1.0f;
+    }
+}
+
 // The adaptive pass-1 epilogue (ai_store's fluxes in FP32; the interface
 // temperature in FP64).
 template <class S>
@@ -153,7 +190,7 @@ __device__ __forceinline__ void ai_store_zero(const DevIface<double>& P, const D
 template <class S>
 __global__ void __launch_bounds__(128) ai_classify_kernel(AIArgs<S> a, DevIface<double> P, DevIface<float> Pf,
                                                           WorkList wl, ReplayQueue rq, float calm2, float* feat,
-                                                          DevStats* stats) {
+                                                          DevStats* stats, DevIface<df> Pd, float* anc) {
     const int nxr = a.L.nx + 2;
     const int64_t ring = (int64_t)nxr * (a.L.ny + 2);
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -187,6 +224,12 @@ __global__ void __launch_bounds__(128) ai_classify_kernel(AIArgs<S> a, DevIface<
         float ua = ldf(a.ua, k), va = ldf(a.va, k);
         float tha = surface_atmosphere_temperature(Pf, Ta, qa);
         mlp::store_features(feat, slot, mlp::warm_features(Pf, ua * ua + va * va, tha, Ts0, qa, pa));
+    }
+    if (anc && slot >= 0) {   // the adaptive pass 1's cancelling differences
+        float v[kAnchorFloats];
+        if (P.temp_form != NESF_BULK_TEMPERATURE) ai_anchor_df<S, true>(Pd, Pf, a, k, v);
+        else ai_anchor_df<S, false>(Pd, Pf, a, k, v);
+        anchor_store(anc, slot, v);
     }
     if (skip) {
         ai_store_zero(P, Pf, a, k);
@@ -298,15 +341,21 @@ struct AIAdaptiveCell {
     const AIArgs<S>& a;
     const DevIface<double>& P64;
     const DevIface<float>& P32;
+    const float* anc;      // the classify pass's records (null: the FP64 prologue here)
     Fast32 f;
     int64_t k;
     uint32_t id;
-    __device__ __forceinline__ void load(int64_t r, float (&start)[4]) {
+    __device__ __forceinline__ void load(int64_t r, int64_t slot, float (&start)[4]) {
         const int nxr = a.L.nx + 2;
         const int i = (int)(r % nxr), j = (int)(r / nxr);
         k = a.L.at(i, j);
         id = (uint32_t)r;
-        ai_load_fast<S, SKIN>(P64, P32, a, k, f);
+        if (anc) {
+            anchor_load<SKIN>(anc, slot, f);
+            ai_load_fp32<S, SKIN>(P32, a, k, f);
+        } else {
+            ai_load_fast<S, SKIN>(P64, P32, a, k, f);
+        }
         start[0] = start[1] = start[2] = 1e-4f;   // atmosphere_sea_ice_fluxes.jl:127
         start[3] = SKIN ? (float)(f.Ts0 - f.tha) : 0.0f;
     }
@@ -320,8 +369,8 @@ struct AIAdaptiveCell {
 template <class S, bool SKIN>
 __global__ void __launch_bounds__(128, NESF_ADAPTIVE_MIN_BLOCKS) ai_adaptive_kernel(AIArgs<S> a, DevIface<double> P64, DevIface<float> P32,
                                                              SolveOpts so, WorkList wl, ReplayQueue rq,
-                                                             const float* guess, DevStats* stats) {
-    AIAdaptiveCell<S, SKIN> cell{a, P64, P32};
+                                                             const float* guess, DevStats* stats, const float* anc) {
+    AIAdaptiveCell<S, SKIN> cell{a, P64, P32, anc};
     adaptive_pass1<SKIN>(cell, P32, so, wl, rq, guess, stats, (so.fetch & NESF_FETCH_SEA_ICE) != 0);
 }
 
@@ -447,8 +496,14 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     const bool adaptive_conv = prec == NESF_F32_ADAPTIVE && so.fp32_rho > 0.0f && P64.stop_kind == NESF_STOP_CONVERGENCE;
     const bool calm = adaptive_conv && so.calm_wind > 0.0f;
     const bool early_lane = calm && early && early->stream;
+    // the adaptive pass 1 under the convergence stopping rule loads its cancelling differences
+    // from the classify pass's records (double-float) when the caller has a buffer
+    const bool anchors = prec == NESF_F32_ADAPTIVE && so.fp32_rho > 0.0f && P64.stop_kind == NESF_STOP_CONVERGENCE &&
+                         ws.anc && so.pdf;
+    float* anc = anchors ? ws.anc : nullptr;
     ai_classify_kernel<S><<<grid, block, 0, stream>>>(a, P64, P32, wl, rq, calm ? so.calm_wind * so.calm_wind : 0.0f,
-                                                      warm ? ws.feat : nullptr, stats);
+                                                      warm ? ws.feat : nullptr, stats,
+                                                      so.pdf ? *so.pdf : DevIface<df>{}, anc);
     trace_mark(so.tracer, "ai_classify", stream);
     if (early_lane) {
         if ((e = cudaEventRecord(early->fork, stream)) != cudaSuccess) return e;
@@ -479,10 +534,10 @@ static cudaError_t launch_ai_t(const AIArgs<S>& a, const DevIface<double>& P64, 
     if (prec == NESF_PLAIN_F64) NESF_AI_SKIN(NESF_PLAIN_F64, nullptr);
     else if (one && skin)
         ai_adaptive_kernel<S, true><<<pass1_grid(ai_adaptive_kernel<S, true>, grid, block, sms, fetch_ai, so.cells), block, 0,
-                                      stream>>>(a, P64, P32, so, wl, rq, guess, stats);
+                                      stream>>>(a, P64, P32, so, wl, rq, guess, stats, anc);
     else if (one)
         ai_adaptive_kernel<S, false><<<pass1_grid(ai_adaptive_kernel<S, false>, grid, block, sms, fetch_ai, so.cells), block,
-                                       0, stream>>>(a, P64, P32, so, wl, rq, guess, stats);
+                                       0, stream>>>(a, P64, P32, so, wl, rq, guess, stats, anc);
     else if (adaptive) NESF_AI_SKIN(NESF_F32_ADAPTIVE, guess);
     else NESF_AI_SKIN(NESF_F32_POLISH, guess);
 #undef NESF_AI_SKIN

@@ -183,6 +183,42 @@ __device__ __forceinline__ void ao_load_fast(const DevIface<double>& P, const De
     }
 }
 
+// The cancelling differences of ao_load_fast in double-float, as the record the classify
+// pass stores per work-list slot for the adaptive pass 1 (anchor_pack).
+template <class S, bool SKIN>
+__device__ __forceinline__ void ao_anchor_df(const DevIface<df>& P, const DevIface<float>& Pf, const AOArgs<S>& a,
+                                             int64_t k, float (&v)[kAnchorFloats]) {
+    float du = 0.0f, dv = 0.0f;
+    if (Pf.vel_form != NESF_WIND_VELOCITY) {   // u_a - u_i cancels where the air moves with the water
+        du = (float)(ldr<df>(a.ua, k) - (ldr<df>(a.uo, k) + ldr<df>(a.uo, k + 1)) / df(2));
+        dv = (float)(ldr<df>(a.va, k) - (ldr<df>(a.vo, k) + ldr<df>(a.vo, k + a.L.sj)) / df(2));
+    }
+    const df Ta = ldr<df>(a.Ta, k), qa = ldr<df>(a.qa, k), lift = lift_temperature(P, qa);
+    const df tha = Ta + lift, Ts0 = ldr<df>(a.To, k) + P.off_int;
+    SurfaceConst<float> sc{};
+    SkinAnchor<float> an{};
+    if (SKIN) an = skin_anchor(P, tha, Ts0, ldr<df>(a.So, k), qa, ldr<df>(a.pa, k), ldzr<df>(a.sw, k), ldzr<df>(a.lw, k));
+    else fast_surface(P, Pf, Ta, qa, ldr<df>(a.pa, k), lift, Ts0, sc);
+    anchor_pack<SKIN>(sc, an, du, dv, tha, Ts0, v);
+}
+
+// ao_load_fast's FP32 part, after anchor_load has set the cancelling differences.
+template <class S, bool SKIN>
+__device__ __forceinline__ void ao_load_fp32(const DevIface<float>& Pf, const AOArgs<S>& a, int64_t k, Fast32& f) {
+    CellConst<float>& c = f.c;
+    c.ua = ldf(a.ua, k); c.va = ldf(a.va, k); c.Ta = ldf(a.Ta, k); c.pa = ldf(a.pa, k); c.qa = ldf(a.qa, k);
+    if (Pf.vel_form == NESF_WIND_VELOCITY) { c.du = c.ua; c.dv = c.va; }
+    c.dU2 = c.du * c.du + c.dv * c.dv;
+    c.tha = (float)f.tha;
+    if (SKIN) {
+        c.rho_a = air_density(Pf, c.Ta, c.pa, c.qa);
+        c.cp_a = cp_m(Pf, c.qa);
+        c.L_s = latent_heat_sublim(Pf, c.Ta);
+        c.kappa = a.kappa ? ldf(a.kappa, k) : -1.0f;
+        c.hi = c.hs = c.hc = c.Rth = 0.0f;
+    }
+}
+
 // The adaptive pass-1 epilogue (ao_store's fluxes in FP32; the interface
 // temperature in FP64).
 template <class S>
@@ -226,7 +262,7 @@ template <class S, bool ENS>
 __global__ void __launch_bounds__(128) ao_classify_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
                                                           const DevIface<double>* __restrict__ P64s,
                                                           const DevIface<float>* __restrict__ P32s, WorkList wl,
-                                                          float* feat, DevStats* stats) {
+                                                          float* feat, DevStats* stats, DevIface<df> Pd, float* anc) {
     const int nxr = a.L.nx + 2;
     const int64_t ring = (int64_t)nxr * (a.L.ny + 2);
     const int m = blockIdx.y;
@@ -253,6 +289,12 @@ __global__ void __launch_bounds__(128) ao_classify_kernel(AOArgs<S> a, DevIface<
     }
     int64_t slot = worklist_push(wl, m, active, stable, (uint32_t)r);
     if (feat && slot >= 0) mlp::store_features(feat, slot, F);
+    if (!ENS && anc && slot >= 0) {   // the adaptive pass 1's cancelling differences (one member)
+        float v[kAnchorFloats];
+        if (P.temp_form != NESF_BULK_TEMPERATURE) ao_anchor_df<S, true>(Pd, Pf, a, k, v);
+        else ao_anchor_df<S, false>(Pd, Pf, a, k, v);
+        anchor_store(anc, slot, v);
+    }
     if (in && land) ao_store_land(P, Pf, a, k, needs ? 0 : P.maxiter);
     if (stats && in && land) stats_add(stats, true, false, 0, false, false, 0, false, false);
 }
@@ -376,15 +418,21 @@ struct AOAdaptiveCell {
     const AOArgs<S>& a;
     const DevIface<double>& P64;
     const DevIface<float>& P32;
+    const float* anc;      // the classify pass's records (null: the FP64 prologue here)
     Fast32 f;
     int64_t k;
     uint32_t id;
-    __device__ __forceinline__ void load(int64_t r, float (&start)[4]) {
+    __device__ __forceinline__ void load(int64_t r, int64_t slot, float (&start)[4]) {
         const int nxr = a.L.nx + 2;
         const int i = (int)(r % nxr), j = (int)(r / nxr);
         k = a.L.at(i, j);
         id = (uint32_t)r;
-        ao_load_fast<S, SKIN>(P64, P32, a, k, f);
+        if (anc) {
+            anchor_load<SKIN>(anc, slot, f);
+            ao_load_fp32<S, SKIN>(P32, a, k, f);
+        } else {
+            ao_load_fast<S, SKIN>(P64, P32, a, k, f);
+        }
         start[0] = start[1] = start[2] = 1e-4f;   // atmosphere_ocean_fluxes.jl:132
         start[3] = SKIN ? f.anc.dTi : 0.0f;
     }
@@ -401,8 +449,8 @@ struct AOAdaptiveCell {
 template <class S, bool SKIN>
 __global__ void __launch_bounds__(128, SKIN ? NESF_ADAPTIVE_MIN_BLOCKS : NESF_ADAPTIVE_MIN_BLOCKS + 1) ao_adaptive_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
                                                              SolveOpts so, WorkList wl, ReplayQueue rq,
-                                                             const float* guess, DevStats* stats) {
-    AOAdaptiveCell<S, SKIN> cell{a, P64, P32};
+                                                             const float* guess, DevStats* stats, const float* anc) {
+    AOAdaptiveCell<S, SKIN> cell{a, P64, P32, anc};
     adaptive_pass1<SKIN>(cell, P32, so, wl, rq, guess, stats, (so.fetch & NESF_FETCH_OCEAN) != 0);
 }
 
@@ -518,8 +566,17 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
     if (e == cudaSuccess && prec != NESF_PLAIN_F64)
         e = cudaMemsetAsync(rq.count, 0, kQueueCounters * sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
-    if (ens) ao_classify_kernel<S, true><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, nullptr, stats);
-    else ao_classify_kernel<S, false><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, feat, stats);
+    // the adaptive pass 1 of one member under the convergence stopping rule loads its cancelling
+    // differences from the classify pass's records (double-float) when the caller has a buffer
+    const bool anchors = prec == NESF_F32_ADAPTIVE && so.fp32_rho > 0.0f && !ens &&
+                         P64.stop_kind == NESF_STOP_CONVERGENCE && ws.anc && so.pdf;
+    float* anc = anchors ? ws.anc : nullptr;
+    if (ens)
+        ao_classify_kernel<S, true><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, nullptr, stats,
+                                                                  DevIface<df>{}, nullptr);
+    else
+        ao_classify_kernel<S, false><<<grid, threads, 0, stream>>>(a, P64, P32, P64s, P32s, wl, feat, stats,
+                                                                   so.pdf ? *so.pdf : DevIface<df>{}, anc);
     trace_mark(so.tracer, "ao_classify", stream);
     if (warm) {
         e = mlp_pass((void*)ws.mlp, ws.feat, nullptr, ws.guess, 0, wl.count, wl.per_member, so.infer_per_sm * sms,
@@ -550,10 +607,10 @@ static cudaError_t launch_ao_t(const AOArgs<S>& a, const DevIface<double>& P64, 
     if (prec == NESF_PLAIN_F64) NESF_AO_SKIN(NESF_PLAIN_F64);
     else if (one && skin)
         ao_adaptive_kernel<S, true><<<pass1_grid(ao_adaptive_kernel<S, true>, grid, threads, sms, fetch_ao, so.cells), threads,
-                                      0, stream>>>(a, P64, P32, so, wl, rq, guess, stats);
+                                      0, stream>>>(a, P64, P32, so, wl, rq, guess, stats, anc);
     else if (one)
         ao_adaptive_kernel<S, false><<<pass1_grid(ao_adaptive_kernel<S, false>, grid, threads, sms, fetch_ao, so.cells),
-                                       threads, 0, stream>>>(a, P64, P32, so, wl, rq, guess, stats);
+                                       threads, 0, stream>>>(a, P64, P32, so, wl, rq, guess, stats, anc);
     else if (adaptive) NESF_AO_SKIN(NESF_F32_ADAPTIVE);
     else NESF_AO_SKIN(NESF_F32_POLISH);
 #undef NESF_AO_SKIN

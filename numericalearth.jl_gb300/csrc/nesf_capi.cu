@@ -36,6 +36,8 @@ struct nesf_context {
     float* d_feat;              // warm start: features (8 floats) and guesses (4) per work-list slot
     float* d_guess;
     int64_t warm_capacity;
+    float* d_anchor;            // the adaptive pass 1's cancelling differences per work-list slot
+    int64_t anchor_capacity;
     // the coupling step's second lane: scratch of the sea-ice solve, its stream, fork/join events
     nesf_context* aux;
     cudaStream_t side;
@@ -393,6 +395,8 @@ int nesf_context_create(int32_t device, nesf_context** out) {
     c->d_partials = nullptr;
     c->d_feat = nullptr;
     c->d_guess = nullptr;
+    c->d_anchor = nullptr;
+    c->anchor_capacity = 0;
     c->warm_capacity = 0;
     c->aux = nullptr;
     c->side = nullptr;
@@ -435,6 +439,7 @@ int nesf_context_destroy(nesf_context* c) {
         cudaFree(c->d_partials);
         cudaFree(c->d_feat);
         cudaFree(c->d_guess);
+        cudaFree(c->d_anchor);
         if (c->side) cudaStreamDestroy(c->side);
         if (c->ev_fork) cudaEventDestroy(c->ev_fork);
         if (c->ev_ice) cudaEventDestroy(c->ev_ice);
@@ -623,7 +628,20 @@ static std::mutex g_default_lock;
 
 // The context's warm-start buffers for `cells` work-list slots (caller holds the lock).
 static int warm_buffers(nesf_context* ctx, const nesf_solver_options& o, int64_t cells, WarmStart* ws) {
-    *ws = WarmStart{nullptr, nullptr, nullptr};
+    *ws = WarmStart{nullptr, nullptr, nullptr, nullptr};
+    // the adaptive solver's per-slot records of the cancelling differences (classify -> pass 1)
+    if (o.precision == NESF_F32_ADAPTIVE) {
+        if (cells > ctx->anchor_capacity) {
+            cudaError_t e = cudaDeviceSynchronize();
+            if (e != cudaSuccess) return cuda_fail(e, "anchor buffer");
+            cudaFree(ctx->d_anchor);
+            ctx->d_anchor = nullptr;
+            ctx->anchor_capacity = 0;
+            NESF_CUDA(cudaMalloc(&ctx->d_anchor, sizeof(float) * kAnchorFloats * (size_t)cells));
+            ctx->anchor_capacity = cells;
+        }
+        ws->anc = ctx->d_anchor;
+    }
     if (!o.warm_start || o.precision == NESF_PLAIN_F64) return NESF_OK;
     if (cells > ctx->warm_capacity) {
         cudaError_t e = cudaDeviceSynchronize();
@@ -636,7 +654,9 @@ static int warm_buffers(nesf_context* ctx, const nesf_solver_options& o, int64_t
         NESF_CUDA(cudaMalloc(&ctx->d_guess, sizeof(float) * 4 * (size_t)cells));
         ctx->warm_capacity = cells;
     }
-    *ws = WarmStart{ctx->d_feat, ctx->d_guess, o.mlp};
+    ws->feat = ctx->d_feat;
+    ws->guess = ctx->d_guess;
+    ws->mlp = o.mlp;
     return NESF_OK;
 }
 

@@ -67,6 +67,8 @@ struct WarmStart {
     float* feat;           // 8 floats per slot
     float* guess;          // 4 floats per slot
     const void* mlp;       // trained network (null: cold start)
+    float* anc;            // adaptive one-member solves: the cancelling differences of each work-list
+                           // slot (kAnchorFloats), written by the classify pass (null: pass 1 computes them)
 };
 
 // Active cells of one solve, compacted and split by the sign of the surface
@@ -188,26 +190,27 @@ template <class R> struct SkinAnchor {
     R gA, gK;          // ln e_sat(T) = gA ln T - gK / T + const
 };
 
-// The anchors of a cell from theta_a and the interior temperature in FP64 (the
-// other inputs need no more than FP32's relative precision).
-__device__ __forceinline__ SkinAnchor<float> skin_anchor(const DevIface<double>& P, double tha, double Ti, double Si,
-                                                         double qa, double pa, double sw, double lw) {
+// The anchors of a cell from theta_a and the interior temperature in A, FP64 or double-float
+// (the other inputs need no more than FP32's relative precision).
+template <class A>
+__device__ __forceinline__ SkinAnchor<float> skin_anchor(const DevIface<A>& P, A tha, A Ti, A Si, A qa, A pa, A sw,
+                                                         A lw) {
     SkinAnchor<float> a;
     a.dTi = (float)(Ti - tha);
-    double Tb = P.Tfw - P.slope * Si;
+    A Tb = P.Tfw - P.slope * Si;
     Tb = Tb + P.off_ifc;
     a.dTb = (float)(Tb - tha);
     a.dTm = (float)(P.Tfw + P.off_ifc - tha);
-    double pv = P.x * esat_exp(P, tha);
-    double qsa = P.einv * pv / (pa - (1.0 - P.einv) * pv);
+    A pv = P.x * esat_exp(P, tha);
+    A qsa = P.einv * pv / (pa - (A(1.0) - P.einv) * pv);
     a.pva = (float)pv;
     a.qsa = (float)qsa;
     a.dqa = (float)(qa - qsa);
-    double sigma = P.has_rad ? P.sigma : 0.0, eps = P.has_rad ? P.emis : 0.0;
-    double alb = P.has_rad ? P.alb : 0.0, SW = P.has_rad ? sw : 0.0, LW = P.has_rad ? lw : 0.0;
-    double T2 = tha * tha;
-    double Iup = sigma * eps * (T2 * T2);
-    double Qd = -(1.0 - alb) * SW - eps * LW;
+    A sigma = P.has_rad ? P.sigma : A(0.0), eps = P.has_rad ? P.emis : A(0.0);
+    A alb = P.has_rad ? P.alb : A(0.0), SW = P.has_rad ? sw : A(0.0), LW = P.has_rad ? lw : A(0.0);
+    A T2 = tha * tha;
+    A Iup = sigma * eps * (T2 * T2);
+    A Qd = -(A(1.0) - alb) * SW - eps * LW;
     a.Iupa = (float)Iup;
     a.Qa0 = (float)(Iup + Qd);
     a.gA = (float)P.esA;
@@ -841,18 +844,21 @@ struct Fast32 {
     double Ts0;               // the interface temperature before the iteration
 };
 
-// theta_a - T_a = g h / cp_m(q_a) (surface_atmosphere_temperature), ~0.1 K. In FP64:
-// its FP32 rounding (~1e-8 K) would be a large part of a near-neutral theta_a - T_s.
-__device__ __forceinline__ double lift_temperature(const DevIface<double>& P, double qa) {
+// theta_a - T_a = g h / cp_m(q_a) (surface_atmosphere_temperature), ~0.1 K. In FP64 or
+// double-float: its FP32 rounding (~1e-8 K) would be a large part of a near-neutral
+// theta_a - T_s.
+template <class A>
+__device__ __forceinline__ A lift_temperature(const DevIface<A>& P, A qa) {
     return P.g * P.h / cp_m(P, qa);
 }
 
-// Surface constants of a bulk interface temperature Ts: q_s and the differences
-// in FP64 (from the fields' own T_a and q_a: FP64 fields are not rounded first),
-// the rest in FP32 from the rounded T_s and q_s.
-__device__ __forceinline__ void fast_surface(const DevIface<double>& P, const DevIface<float>& Pf, double Ta,
-                                             double qa, double pa, double lift, double Ts, SurfaceConst<float>& s) {
-    double qs = surface_specific_humidity<double, true>(P, pa, Ts);
+// Surface constants of a bulk interface temperature Ts: q_s and the differences in A,
+// FP64 or double-float (from the fields' own T_a and q_a: FP64 fields are not rounded
+// first), the rest in FP32 from the rounded T_s and q_s.
+template <class A>
+__device__ __forceinline__ void fast_surface(const DevIface<A>& P, const DevIface<float>& Pf, A Ta, A qa, A pa,
+                                             A lift, A Ts, SurfaceConst<float>& s) {
+    A qs = surface_specific_humidity<A, true>(P, pa, Ts);
     s.Ts = (float)Ts;
     s.qs = (float)qs;
     s.dth = (float)((Ta - Ts) + lift);
@@ -865,6 +871,55 @@ __device__ __forceinline__ void fast_surface(const DevIface<double>& P, const De
     s.nu_u = air_viscosity(Pf.rough[0], s.Ts);
     s.nu_t = air_viscosity(Pf.rough[1], s.Ts);
     s.nu_q = air_viscosity(Pf.rough[2], s.Ts);
+}
+
+// The cancelling differences of an adaptive pass-1 cell, computed once by the classify pass
+// in double-float (48 bits on the FP32 pipes: FP64 issues one warp instruction per ~64
+// cycles per SM sub-partition on this GPU) and stored per work-list slot, so that pass 1
+// loads them instead of taking FP64 steps in its prologue: 16 floats, the surface constants
+// of a bulk interface temperature (10) or the skin anchors (10), the velocity difference
+// (2), theta_a and the starting interface temperature as double-float pairs (4).
+constexpr int kAnchorFloats = 16;
+
+__device__ __forceinline__ void anchor_store(float* buf, int64_t slot, const float (&v)[kAnchorFloats]) {
+    float4* p = reinterpret_cast<float4*>(buf + slot * kAnchorFloats);
+#pragma unroll
+    for (int q = 0; q < kAnchorFloats / 4; q++) p[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+}
+
+template <bool SKIN>
+__device__ __forceinline__ void anchor_pack(const SurfaceConst<float>& s, const SkinAnchor<float>& a, float du,
+                                            float dv, df tha, df Ts0, float (&v)[kAnchorFloats]) {
+    if (SKIN) {
+        v[0] = a.dTi; v[1] = a.dTb; v[2] = a.dTm; v[3] = a.pva; v[4] = a.qsa;
+        v[5] = a.dqa; v[6] = a.Qa0; v[7] = a.Iupa; v[8] = a.gA; v[9] = a.gK;
+    } else {
+        v[0] = s.Ts; v[1] = s.qs; v[2] = s.dth; v[3] = s.dq; v[4] = s.gTv;
+        v[5] = s.A1; v[6] = s.A2; v[7] = s.nu_u; v[8] = s.nu_t; v[9] = s.nu_q;
+    }
+    v[10] = du; v[11] = dv;
+    v[12] = tha.hi; v[13] = tha.lo; v[14] = Ts0.hi; v[15] = Ts0.lo;
+}
+
+// Loads a slot's record into the pass-1 state (f.c's velocity difference, f.s or f.anc,
+// f.tha, f.Ts0).
+template <bool SKIN>
+__device__ __forceinline__ void anchor_load(const float* buf, int64_t slot, Fast32& f) {
+    const float4* p = reinterpret_cast<const float4*>(buf + slot * kAnchorFloats);
+    const float4 q0 = p[0], q1 = p[1], q2 = p[2], q3 = p[3];
+    if (SKIN) {
+        SkinAnchor<float>& a = f.anc;
+        a.dTi = q0.x; a.dTb = q0.y; a.dTm = q0.z; a.pva = q0.w; a.qsa = q1.x;
+        a.dqa = q1.y; a.Qa0 = q1.z; a.Iupa = q1.w; a.gA = q2.x; a.gK = q2.y;
+    } else {
+        SurfaceConst<float>& s = f.s;
+        s.Ts = q0.x; s.qs = q0.y; s.dth = q0.z; s.dq = q0.w; s.gTv = q1.x;
+        s.A1 = q1.y; s.A2 = q1.z; s.nu_u = q1.w; s.nu_t = q2.x; s.nu_q = q2.y;
+    }
+    f.c.du = q2.z;
+    f.c.dv = q2.w;
+    f.tha = (double)q3.x + (double)q3.y;
+    f.Ts0 = (double)q3.z + (double)q3.w;
 }
 
 // Momentum flux direction: (-u*^2 du / |dU|, -u*^2 dv / |dU|) in FP32, in FP64 where
@@ -1116,8 +1171,9 @@ __device__ __forceinline__ void adaptive_pass1(Cell& cell, const DevIface<float>
             }
             if (w >= 0) {
                 float xw[3], start[4];
-                const float* warm = mlp::guess_at(guess, worklist_slot(wl, 0, w), xw);
-                cell.load(worklist_get(wl, 0, w), start);
+                const int64_t slot = worklist_slot(wl, 0, w);
+                const float* warm = mlp::guess_at(guess, slot, xw);
+                cell.load(worklist_get(wl, 0, w), slot, start);
                 sw.begin(start, warm);
                 have = true;
             }

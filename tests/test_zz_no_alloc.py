@@ -10,7 +10,12 @@ sets up once per device. The tests:
   call's work list and replay queue in the shared scratch -- and check both calls
   against nesf_compute_atmosphere_ocean_fluxes on the same inputs, with the
   tolerance of the other GPU tests (relative error |a - b| / max(|b|, 1e-6 max|b|)
-  <= 1e-12);
+  <= 1e-12) for the FP64 and FP32 solvers; under the adaptive FP32 solver the
+  regular entry point's pass 1 reads its cancelling differences from the classify
+  pass's double-float records, a scratch this entry point does not hold (it forms
+  them in FP64 in the kernel), so the two FP32 trajectories differ and agree within
+  twice the solver's tolerance against FP64 (2e-5), while the two calls agree bit
+  for bit;
 * check that the device's free memory (cudaMemGetInfo) is the same before and
   after those calls: they allocate nothing;
 * run a grid whose halo ring is exactly the scratch capacity (2^21 cells) and
@@ -80,16 +85,20 @@ def test_noalloc_matches_regular_entry_point_twice(precision, dtype):
         assert code == A.NESF_OK, lib.nesf_last_error()
     torch.cuda.synchronize()
     assert torch.cuda.mem_get_info()[0] == free_before, "the allocation-free calls changed the free device memory"
+    tol = 2e-5 if precision == "f32_adaptive" else 1e-12
     for call in range(2):
         for k in F.AO_OUTPUTS:
             got = R(to_numpy(outs[call][k])).astype(np.float64)
             e = rel_err(got, expect[k], floor_frac=1e-6)
-            assert e.max() <= 1e-12, (precision, call, k, float(e.max()))
+            assert e.max() <= tol, (precision, call, k, float(e.max()))
+    for k in F.AO_OUTPUTS:   # (cells the solve does not write keep their NaN)
+        assert np.array_equal(to_numpy(outs[0][k]), to_numpy(outs[1][k]), equal_nan=True), (precision, k)
 
 
 def test_noalloc_at_capacity_and_beyond():
     """A grid of exactly 2^21 halo-ring cells (2046 x 1022) is solved and matches the regular
-    entry point; one row more is refused with NESF_ERR_CAPACITY before any launch."""
+    entry point (adaptive FP32 solver: within 2e-5, as above); one row more is refused with
+    NESF_ERR_CAPACITY before any launch."""
     import torch
     lib = _lib.load()
     _prepare(lib)
@@ -107,7 +116,7 @@ def test_noalloc_at_capacity_and_beyond():
     R = st.layout.ring
     for k in F.AO_OUTPUTS:
         e = rel_err(R(to_numpy(out[k])).astype(np.float64), R(to_numpy(ref[k])).astype(np.float64), floor_frac=1e-6)
-        assert e.max() <= 1e-12, (k, float(e.max()))
+        assert e.max() <= 2e-5, (k, float(e.max()))
     over = syn.Layout(nx, ny + 1, st.layout.hx, st.layout.hy)
     assert (nx + 2) * (ny + 3) > MAX_CELLS
     code = _noalloc(lib, spec, over, dev, out, "f32_adaptive")
