@@ -365,9 +365,12 @@ struct AIAdaptiveCell {
 };
 
 // Pass 1 of the adaptive solver under the convergence stopping rule: adaptive_pass1 with the
-// schedule of SolveOpts::fetch / refill.
+// schedule of SolveOpts::fetch / refill. The skin-temperature instantiation (four real
+// state components) runs 4 blocks per SM at up to 128 registers, without spills: with its
+// cancelling differences loaded from the classify pass's records it measured faster so
+// than at 5 blocks (96 registers, 190 bytes of spill stores) or 6 (80, 374 bytes).
 template <class S, bool SKIN>
-__global__ void __launch_bounds__(128, NESF_ADAPTIVE_MIN_BLOCKS) ai_adaptive_kernel(AIArgs<S> a, DevIface<double> P64, DevIface<float> P32,
+__global__ void __launch_bounds__(128, SKIN ? NESF_ADAPTIVE_MIN_BLOCKS - 1 : NESF_ADAPTIVE_MIN_BLOCKS) ai_adaptive_kernel(AIArgs<S> a, DevIface<double> P64, DevIface<float> P32,
                                                              SolveOpts so, WorkList wl, ReplayQueue rq,
                                                              const float* guess, DevStats* stats, const float* anc) {
     AIAdaptiveCell<S, SKIN> cell{a, P64, P32, anc};

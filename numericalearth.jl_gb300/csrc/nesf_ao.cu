@@ -443,11 +443,14 @@ struct AOAdaptiveCell {
 
 // Pass 1 of the adaptive solver, one member, convergence stopping rule: adaptive_pass1
 // with the schedule of SolveOpts::fetch / refill.
-// Six resident blocks per SM (80 registers) with a bulk interface temperature: its sweep
-// state fits with few spills once the unused fourth state component is a constant, and the
-// extra warps measured 1.32 -> 1.23 ms on the 1/8-degree step; five with a skin temperature.
+// Seven resident blocks per SM (72 registers) with a bulk interface temperature: its sweep
+// state fits with few spills once the unused fourth state component is a constant and the
+// cancelling differences come from the classify pass's records, and the extra warps hide
+// more of its dependent latency (1/8-degree step: 1.32 ms at 5 blocks, 1.23 at 6 with the
+// FP64 prologue; with the records 1.08 at 5, 1.03 at 6, 0.99 at 7); five with a skin
+// temperature.
 template <class S, bool SKIN>
-__global__ void __launch_bounds__(128, SKIN ? NESF_ADAPTIVE_MIN_BLOCKS : NESF_ADAPTIVE_MIN_BLOCKS + 1) ao_adaptive_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
+__global__ void __launch_bounds__(128, SKIN ? NESF_ADAPTIVE_MIN_BLOCKS : NESF_ADAPTIVE_MIN_BLOCKS + 2) ao_adaptive_kernel(AOArgs<S> a, DevIface<double> P64, DevIface<float> P32,
                                                              SolveOpts so, WorkList wl, ReplayQueue rq,
                                                              const float* guess, DevStats* stats, const float* anc) {
     AOAdaptiveCell<S, SKIN> cell{a, P64, P32, anc};
