@@ -1190,14 +1190,7 @@ static AsmArgs<S> asm_args(const nesf_assembly_fields* f, int with_rad) {
     return a;
 }
 
-static int run_assembly(const nesf_assembly_params* p, const nesf_assembly_fields* f, int which, void* stream,
-                        const char* who) {
-    if (!p || !f) return fail(NESF_ERR_ARG, "%s: null argument", who);
-    int r = check_grid(f->grid, 1, who);
-    if (r) return r;
-    if (f->dtype != NESF_F64 && f->dtype != NESF_F32) return fail(NESF_ERR_ARG, "%s: dtype %d", who, f->dtype);
-    if (!(p->ocean_reference_density > 0) || !(p->ocean_heat_capacity > 0))
-        return fail(NESF_ERR_ARG, "%s: density and heat capacity must be positive", who);
+static int check_assembly(const nesf_assembly_fields* f, int which, const char* who) {
     switch (which) {
     case 0:
         if (!f->ocean_surface_temperature || !f->ao_sensible || !f->ao_latent || !f->ao_water_vapor ||
@@ -1216,9 +1209,27 @@ static int run_assembly(const nesf_assembly_params* p, const nesf_assembly_field
         if (!f->ai_interface_temperature || !f->sw_down || !f->lw_down || !f->ice_top_heat || !f->ice_concentration)
             return fail(NESF_ERR_ARG, "%s: T_s, radiation, concentration and top heat are required", who);
     }
+    return NESF_OK;
+}
+
+// which: 0 ocean assembly, 1 sea-ice assembly, 2 / 3 their radiative add-ons. With
+// `with_radiation` (which 0 or 1, the coupling step) the assembly kernel applies the
+// add-on too, with the same operations in the same order as the separate pass (the
+// assembled J_T / top heat flux rounded to the field's type, then the radiative part
+// added), so the results are bit for bit those of the two calls.
+static int run_assembly(const nesf_assembly_params* p, const nesf_assembly_fields* f, int which, void* stream,
+                        const char* who, int with_radiation = 0) {
+    if (!p || !f) return fail(NESF_ERR_ARG, "%s: null argument", who);
+    int r = check_grid(f->grid, 1, who);
+    if (r) return r;
+    if (f->dtype != NESF_F64 && f->dtype != NESF_F32) return fail(NESF_ERR_ARG, "%s: dtype %d", who, f->dtype);
+    if (!(p->ocean_reference_density > 0) || !(p->ocean_heat_capacity > 0))
+        return fail(NESF_ERR_ARG, "%s: density and heat capacity must be positive", who);
+    if ((r = check_assembly(f, which, who))) return r;
+    if (with_radiation && (r = check_assembly(f, which + 2, who))) return r;
     cudaStream_t s = (cudaStream_t)stream;
-    cudaError_t e = f->dtype == NESF_F64 ? launch_assemble(asm_args<double>(f, 0), *p, which, s)
-                                         : launch_assemble(asm_args<float>(f, 0), *p, which, s);
+    cudaError_t e = f->dtype == NESF_F64 ? launch_assemble(asm_args<double>(f, with_radiation), *p, which, s)
+                                         : launch_assemble(asm_args<float>(f, with_radiation), *p, which, s);
     if (e != cudaSuccess) return cuda_fail(e, who);
     return NESF_OK;
 }
@@ -1694,13 +1705,13 @@ extern "C" int nesf_coupling_step(nesf_context* ctx, const nesf_coupling_step_ar
     if (a->io_params && (r = sea_ice_ocean(ctx, a->io_params, a->io, stream, io_split ? 2 : 0))) return r;
     if (a->io_params) trace_mark(tr, io_split ? "frazil_adjustment" : "sea_ice_ocean_fluxes", s);
     if (a->assembly_params) {
-        if ((r = nesf_assemble_net_ocean_fluxes(a->assembly_params, a->assembly, stream))) return r;
-        if (ice && (r = nesf_assemble_net_sea_ice_fluxes(a->assembly_params, a->assembly, stream))) return r;
-        if (a->radiation) {
-            if ((r = nesf_apply_air_sea_radiative_fluxes(a->assembly_params, a->assembly, stream))) return r;
-            if (ice && (r = nesf_apply_air_sea_ice_radiative_fluxes(a->assembly_params, a->assembly, stream)))
-                return r;
-        }
+        // the radiative add-ons inside the assembly kernels (bit for bit the separate passes)
+        const int rad = a->radiation ? 1 : 0;
+        if ((r = run_assembly(a->assembly_params, a->assembly, 0, stream, "nesf_coupling_step (ocean assembly)", rad)))
+            return r;
+        if (ice && (r = run_assembly(a->assembly_params, a->assembly, 1, stream,
+                                     "nesf_coupling_step (sea-ice assembly)", rad)))
+            return r;
         trace_mark(tr, "assembly", s);
     }
     return NESF_OK;

@@ -143,12 +143,17 @@ class CoupledModel:
 
     def kernels_per_step(self, precision, native=False):
         """Kernels one step launches: interpolation; per solve classify + solve (+ the packed
-        polish pass of the adaptive mode, + the replay pass of the FP32 modes); sea-ice-ocean
-        (in the native step its fluxes and its frazil adjustment apart); ocean and sea-ice
-        assembly and their radiative add-ons."""
+        polish pass of the adaptive mode, + the replay passes of the FP32 modes: the adaptive
+        mode replays pass 1's cells beside the polish pass and the polish pass's after it);
+        the ocean's warm-start inference; sea-ice-ocean (in the native step its fluxes and its
+        frazil adjustment apart); ocean and sea-ice assembly with their radiative add-ons (in
+        the native step inside the assembly kernels)."""
         fast = precision != "f64" and precision != "plain"
-        per_solve = 2 + (precision == "f32_adaptive") + fast + (fast and self.mlp is not None)
-        return (1 if self.atmos is not None else 0) + 2 * per_solve + (2 if native else 1) + 4
+        adaptive = precision == "f32_adaptive"
+        per_solve = 2 + adaptive + (2 if adaptive else 1) * fast
+        warm = 1 if fast and self.mlp is not None else 0
+        return ((1 if self.atmos is not None else 0) + 2 * per_solve + warm + (2 if native else 1) +
+                (2 if native else 4))
 
     # ------------------------------------------------- native step and graph
     def step_args(self):
