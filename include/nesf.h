@@ -777,7 +777,9 @@ typedef struct {
     const nesf_interp_fields* interp;               /* NULL: exchange-grid state given   */
     const nesf_assembly_params* assembly_params;    /* NULL: no net-flux assembly        */
     const nesf_assembly_fields* assembly;
-    int32_t radiation;                              /* 1: radiative add-ons after assembly */
+    int32_t radiation;                              /* 1: radiative add-ons after assembly
+                                                       (inside the assembly kernels: bit for
+                                                       bit the separate apply_* calls)     */
     int32_t pad_;
 } nesf_coupling_step_args;
 
