@@ -570,8 +570,8 @@ typedef struct {
 /* Library-owned scratch per device, grown on demand to the largest grid solved: per
    halo-ring cell the work list and replay queue (uint32 each), under NESF_F32_ADAPTIVE a
    64-byte record of pass 1's cancelling differences, with the warm start 48 bytes of
-   features and guesses (the 1/8-degree coupled step: ~0.3 GB on the caller's context and
-   as much on the sea-ice lane's). */
+   features and guesses (the 1/8-degree coupled step, 3.7 M ring cells: about 0.5 GB on
+   the caller's context and up to as much on the sea-ice lane's). */
 typedef struct nesf_context nesf_context;
 
 int32_t     nesf_abi_version(void);
